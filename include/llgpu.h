@@ -1,0 +1,201 @@
+/*
+ * llgpu.h -- C ABI of the GB300 state-vector engine (libllgpu.so).
+ *
+ * This is the drop-in boundary under the Python `quantum_sim_v3.StateVector` / `quantum_sim_v2`
+ * modules and the C++ `ll::GpuBackend` (include/ll_gpu_backend.h).  Plain pointers and sizes
+ * only.  Each entry point names the reference interface it replaces (paths inside the reference
+ * project Athleity/lightning-lite-quantum-simulator).
+ *
+ * Conventions (src/Backend.h:3-8): qubit q is bit q of the basis-state index; RX/RY/RZ(t) =
+ * exp(-i t P/2); mcz negates every amplitude whose bits are all 1 on the listed qubits.
+ * Amplitudes cross the boundary as complex128: 2 doubles (re, im) per basis state, 16 bytes,
+ * the std::complex<double> / numpy complex128 layout.
+ *
+ * Errors: every call returns an llg status.  LLG_EINVAL is the reference's
+ * std::invalid_argument (Python ValueError), LLG_ERUNTIME its std::runtime_error (Python
+ * RuntimeError).  llg_last_error() gives the message of the calling thread's last failure.
+ * Arguments are validated on the host before anything is enqueued; a rejected call leaves the
+ * state untouched.
+ *
+ * Execution: each state owns one CUDA stream.  Gate calls are validated and appended to the
+ * state's pending-gate queue; the queue is flushed (planned into fused passes and launched
+ * asynchronously) when a readout needs the amplitudes, on llg_sync/llg_flush, or when it grows
+ * past an internal limit.  A state object is not thread-safe (the reference's are not either).
+ */
+#ifndef LLGPU_H
+#define LLGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define LLG_OK 0
+#define LLG_EINVAL 1   /* invalid argument (reference: std::invalid_argument) */
+#define LLG_ERUNTIME 2 /* runtime failure (reference: std::runtime_error) */
+#define LLG_ENOMEM 3   /* device or pinned-host allocation failed */
+#define LLG_ECUDA 4    /* a CUDA call failed; the message names it */
+#define LLG_ETIMEOUT 5 /* a bounded device-side wait gave up; the kernel returned early */
+
+/* ---- amplitude precisions (how the state is held in HBM) ---- */
+#define LLG_F64 0  /* complex128 as IEEE double pairs, FP64 arithmetic (plain path) */
+#define LLG_DF64 1 /* complex128 class: each real part as an fp32 (hi, lo) pair, 16 B/amplitude,
+                      FP32-pipe error-free arithmetic, ~48-bit significand */
+#define LLG_F32 2  /* complex64: fp32 pairs, FP32 arithmetic */
+
+/* ---- fusion modes for the pending-gate queue ---- */
+#define LLG_FUSE_NONE 0 /* one streaming kernel per gate: the reference's own algorithm */
+#define LLG_FUSE_TILE 1 /* shared-memory tile passes over chosen qubit sets (cache blocking) */
+
+/* ---- gate record (96 bytes).  Kinds 0..6 are the Op kinds of the reference's random-circuit
+ * test, tests/test_backends.cpp:78-83 (h, x, rx, ry, rz, cnot, mcz). ---- */
+#define LLG_OP_H 0
+#define LLG_OP_X 1
+#define LLG_OP_RX 2
+#define LLG_OP_RY 3
+#define LLG_OP_RZ 4
+#define LLG_OP_CNOT 5 /* q0 = control, q1 = target */
+#define LLG_OP_MCZ 6  /* mask = OR of 1 << q over the listed qubits */
+#define LLG_OP_CZ 7   /* mcz({q0, q1}) */
+#define LLG_OP_U2 8   /* generic 2x2 on q0, m = {g00, g01, g10, g11} interleaved re/im */
+
+typedef struct llg_op {
+    int32_t kind;
+    int32_t q0;
+    int32_t q1;
+    int32_t param; /* index into a parameter vector (rotations), -1 if fixed */
+    uint64_t mask;
+    double theta;
+    double m[8];
+} llg_op;
+
+typedef struct llg_state llg_state;
+
+/* ---- library ---- */
+const char* llg_last_error(void);
+const char* llg_version(void);
+/* Number of CUDA devices visible; 0 when none (every compute call then fails with LLG_ECUDA). */
+int llg_device_count(void);
+
+/* ---- state lifetime ---- */
+
+/* New n-qubit state |0...0>.  Replaces StateVectorOptimized(int) (src/StateVectorOptimized.cpp:17-24)
+ * and Backend::reset (src/Backend.h:30, src/StateVectorBackend.h:49-57).  n in [1, 34]. */
+int llg_create(int n_qubits, int precision, llg_state** out);
+
+/* New state holding a copy of `len` complex128 amplitudes (2*len doubles).  Replaces the
+ * ndarray constructor (src/StateVectorOptimized.cpp:26-47): len must be a power of two
+ * (else LLG_ERUNTIME "Array size must be power of 2"); the data is copied to HBM, not aliased. */
+int llg_create_from_host(const double* amps, size_t len, int precision, llg_state** out);
+
+int llg_destroy(llg_state* st);
+
+/* Back to |0...0> on n qubits (src/Backend.h:30).  n outside [1, 34] is LLG_EINVAL. */
+int llg_reset(llg_state* st, int n_qubits);
+
+/* src/StateVectorOptimized.cpp:108-109 get_num_qubits / get_size. */
+int llg_num_qubits(const llg_state* st, int* out);
+int llg_size(const llg_state* st, uint64_t* out);
+int llg_get_precision(const llg_state* st, int* out);
+
+/* Fusion mode for this state's queue (LLG_FUSE_*) and tile width in qubits (0 = autotuned). */
+int llg_set_fusion(llg_state* st, int mode, int tile_qubits);
+
+/* ---- gates (validated now, executed at the next flush) ---- */
+
+/* quantum_sim_v3 apply_gate_cache_optimized / apply_gate_standard and quantum_sim_v2 apply_gate
+ * (src/StateVectorOptimized.cpp:56-97, src/bindings_v2.cpp:56-72): generic 2x2 `g` = 8 doubles,
+ * row-major {g00, g01, g10, g11} as (re, im).  As in the reference a target >= n is a no-op;
+ * a negative target is LLG_EINVAL. */
+int llg_apply_gate(llg_state* st, int target, const double* g);
+
+/* ll::StateVectorBackend gate set (src/StateVectorBackend.h:61-151, interface src/Backend.h:33-39):
+ * a qubit outside [0, n), a non-finite angle, cnot(q, q), an empty or repeated mcz list are
+ * LLG_EINVAL. */
+int llg_h(llg_state* st, int q);
+int llg_x(llg_state* st, int q);
+int llg_rx(llg_state* st, int q, double theta);
+int llg_ry(llg_state* st, int q, double theta);
+int llg_rz(llg_state* st, int q, double theta);
+int llg_cnot(llg_state* st, int control, int target);
+int llg_cz(llg_state* st, int a, int b);
+int llg_mcz(llg_state* st, const int* qubits, int nq);
+
+/* A list of gate records appended in order (the op-list form of the calls above; U2 records
+ * follow llg_apply_gate and are LLG_EINVAL for a target outside [0, n)). */
+int llg_apply_ops(llg_state* st, const llg_op* ops, int nops);
+
+/* Dense k-qubit block (the fused form of python/gate_fusion.py:7-37 widened to k qubits):
+ * `m` is 2^k x 2^k complex, row-major, interleaved; qubits[0] is the least-significant bit of
+ * the block's local index.  k in [1, 5], distinct qubits in [0, n). */
+int llg_apply_matrix(llg_state* st, int k, const int* qubits, const double* m);
+
+/* ---- execution and readout ---- */
+
+/* Plan and launch the pending queue without waiting. */
+int llg_flush(llg_state* st);
+/* Flush and wait for the state's stream. */
+int llg_sync(llg_state* st);
+
+/* Amplitudes to host memory (2*2^n doubles) after a flush; replaces get_numpy_view
+ * (src/StateVectorOptimized.cpp:99-106) and Backend::state (src/Backend.h:44) as an explicit
+ * device-to-host copy. */
+int llg_copy_to_host(llg_state* st, double* out);
+/* Overwrite the amplitudes from host memory (2*2^n doubles). */
+int llg_copy_from_host(llg_state* st, const double* amps);
+
+/* |a_i|^2 for every basis state into host memory (2^n doubles); replaces
+ * StateVectorBackend::probabilities (src/StateVectorBackend.h:153-161). */
+int llg_probabilities(llg_state* st, double* out);
+
+/* sum_i |a_i|^2 (FP64 result). */
+int llg_norm2(llg_state* st, double* out);
+
+/* sum_k coeff_k <Z_{a_k} Z_{b_k}>; b_k < 0 selects the single-qubit term <Z_{a_k}>.  The
+ * diagonal of python/algorithms.py:141-153 (ising_diagonal) evaluated on the fly. */
+int llg_expect_zz(llg_state* st, int nterms, const int* a, const int* b, const double* coeff, double* out);
+
+/* Scale the state to unit norm (the periodic renormalisation of the complex64 path). */
+int llg_renormalize(llg_state* st);
+
+/* Pinned host memory for fast transfers (cudaHostAlloc); NULL on failure. */
+void* llg_host_alloc(size_t bytes);
+void llg_host_free(void* p);
+
+/* ---- planner introspection (host only; no GPU needed) ----
+ * Plans `ops` on n qubits into shared-memory tile passes of `tile_qubits` qubits exactly as a
+ * flush does, and exports the passes and the executor ops they run (coefficients as doubles).
+ * Used by the CPU tests to execute a plan in numpy against the oracle.  Writes at most
+ * max_passes / max_xops records and the true counts to *npasses / *nxops. */
+typedef struct llg_pass_info {
+    uint64_t local_mask; /* qubits held in the tile */
+    int32_t t;           /* tile width in qubits */
+    int32_t low;         /* the low `low` qubits are always local (coalesced runs) */
+    int32_t op_begin;    /* first executor op of the pass */
+    int32_t nops;        /* number of executor ops */
+} llg_pass_info;
+
+/* Executor op: kind 0 U2, 1 RX, 2 RY, 3 H, 4 X, 5 DIAG, 6 CNOT, 7 MCZ.  Qubit fields are tile-local
+ * indices unless flags bit 0 marks q0 as a global qubit outside the tile; nl_mask holds global
+ * qubits that must all be 1 in the tile for the op to act. */
+typedef struct llg_exec_op {
+    int32_t kind;
+    int32_t q0;
+    int32_t q1;
+    int32_t flags;
+    uint64_t mask;
+    uint64_t nl_mask;
+    double c[8];
+} llg_exec_op;
+
+int llg_plan_export(int n, const llg_op* ops, int nops, int tile_qubits, llg_pass_info* passes, int max_passes,
+                    int* npasses, llg_exec_op* xops, int max_xops, int* nxops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LLGPU_H */

@@ -1,0 +1,649 @@
+// llg_engine.cu -- the C ABI of libllgpu.so (include/llgpu.h): state objects resident in HBM,
+// argument validation with the reference's error contract, the pending-gate queue and its
+// flush into fused tile passes or per-gate streaming kernels, and chunked host transfers.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/llgpu.h"
+#include "llg_internal.h"
+#include "llg_launch.h"
+
+using namespace llg;
+
+namespace llg {
+
+thread_local std::string g_last_error;
+
+int set_error(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return set_error(LLG_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+}  // namespace llg
+
+#define LLG_CUDA(call, what)                            \
+    do {                                                \
+        cudaError_t e_ = (call);                        \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+static constexpr int kMaxQubits = 34;
+static constexpr size_t kQueueFlushAt = 1 << 16;
+static constexpr uint64_t kStageAmps = 1ULL << 24;  // 256 MiB of complex128 per transfer chunk
+
+struct llg_state {
+    int n = 0;
+    int P = LLG_DF64;
+    uint64_t size = 1;
+    void* d_psi = nullptr;
+    cudaStream_t stream = nullptr;
+    int fuse_mode = LLG_FUSE_TILE;
+    int tile_qubits = 0;  // 0 = default
+    std::vector<llg_op> queue;
+    // op upload
+    ExecOp* d_ops = nullptr;
+    size_t d_ops_cap = 0;
+    ExecOp* h_ops = nullptr;
+    size_t h_ops_cap = 0;
+    cudaEvent_t ops_done = nullptr;
+    // reductions
+    double* d_partials = nullptr;
+    double* d_red = nullptr;
+    // transfer staging (two chunks of complex128 = double2)
+    double* d_stage[2] = {nullptr, nullptr};
+    cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+};
+
+namespace {
+
+bool finite(double x) { return std::isfinite(x); }
+
+int check_qubit(const llg_state* st, int q, const char* who) {
+    if (q < 0 || q >= st->n)
+        return set_error(LLG_EINVAL, std::string(who) + ": qubit " + std::to_string(q) + " outside [0, " +
+                                         std::to_string(st->n) + ")");
+    return LLG_OK;
+}
+
+int check_angle(double t, const char* who) {
+    if (!finite(t)) return set_error(LLG_EINVAL, std::string(who) + ": non-finite angle");
+    return LLG_OK;
+}
+
+int default_tile(int P) { return P == LLG_F32 ? 13 : 12; }
+
+int ensure_device_buffers(llg_state* st) {
+    if (!st->stream) LLG_CUDA(cudaStreamCreateWithFlags(&st->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!st->ops_done) LLG_CUDA(cudaEventCreateWithFlags(&st->ops_done, cudaEventDisableTiming), "cudaEventCreate");
+    if (!st->d_partials) {
+        LLG_CUDA(cudaMalloc(&st->d_partials, sizeof(double) * kRedBlocks * kRedSlots), "cudaMalloc(partials)");
+        LLG_CUDA(cudaMalloc(&st->d_red, sizeof(double) * kRedSlots), "cudaMalloc(red)");
+    }
+    return LLG_OK;
+}
+
+int alloc_state(llg_state* st, int n) {
+    const uint64_t size = 1ULL << n;
+    const size_t bytes = size * elem_bytes(st->P);
+    if (st->d_psi && st->n == n) return LLG_OK;
+    if (st->d_psi) {
+        cudaStreamSynchronize(st->stream);
+        cudaFree(st->d_psi);
+        st->d_psi = nullptr;
+    }
+    cudaError_t e = cudaMalloc(&st->d_psi, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        st->d_psi = nullptr;
+        return set_error(LLG_ENOMEM, "cannot allocate " + std::to_string(bytes) + " bytes of HBM for " +
+                                         std::to_string(n) + " qubits: " + cudaGetErrorString(e));
+    }
+    st->n = n;
+    st->size = size;
+    return LLG_OK;
+}
+
+int stage_buffers(llg_state* st) {
+    for (int i = 0; i < 2; ++i) {
+        if (!st->d_stage[i]) LLG_CUDA(cudaMalloc(&st->d_stage[i], kStageAmps * 2 * sizeof(double)), "cudaMalloc(stage)");
+        if (!st->stage_ev[i]) LLG_CUDA(cudaEventCreateWithFlags(&st->stage_ev[i], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    return LLG_OK;
+}
+
+int run_streaming(llg_state* st, const std::vector<llg_op>& q) {
+    std::vector<ExecOp> lowered;
+    std::string err;
+    for (const llg_op& op : q) {
+        lowered.clear();
+        if (!lower_op(st->n, op, st->P, lowered, err)) return set_error(LLG_EINVAL, err);
+        for (const ExecOp& e : lowered) LLG_CUDA(launch_exec_op(st->P, st->d_psi, st->n, e, st->stream), "gate kernel");
+    }
+    return LLG_OK;
+}
+
+int upload_ops(llg_state* st, const std::vector<ExecOp>& ops) {
+    const size_t count = std::max<size_t>(ops.size(), 1);
+    if (count > st->d_ops_cap) {
+        if (st->d_ops) {
+            cudaStreamSynchronize(st->stream);
+            cudaFree(st->d_ops);
+        }
+        const size_t cap = std::max<size_t>(count, 1024);
+        LLG_CUDA(cudaMalloc(&st->d_ops, cap * sizeof(ExecOp)), "cudaMalloc(ops)");
+        st->d_ops_cap = cap;
+    }
+    // the pinned staging buffer may still feed an earlier copy
+    LLG_CUDA(cudaEventSynchronize(st->ops_done), "cudaEventSynchronize");
+    if (count > st->h_ops_cap) {
+        if (st->h_ops) cudaFreeHost(st->h_ops);
+        const size_t cap = std::max<size_t>(count, 1024);
+        LLG_CUDA(cudaHostAlloc((void**)&st->h_ops, cap * sizeof(ExecOp), cudaHostAllocDefault), "cudaHostAlloc(ops)");
+        st->h_ops_cap = cap;
+    }
+    if (!ops.empty()) {
+        std::memcpy(st->h_ops, ops.data(), ops.size() * sizeof(ExecOp));
+        LLG_CUDA(cudaMemcpyAsync(st->d_ops, st->h_ops, ops.size() * sizeof(ExecOp), cudaMemcpyHostToDevice, st->stream),
+                 "cudaMemcpyAsync(ops)");
+    }
+    LLG_CUDA(cudaEventRecord(st->ops_done, st->stream), "cudaEventRecord");
+    return LLG_OK;
+}
+
+int run_tiles(llg_state* st, const std::vector<llg_op>& q) {
+    Plan plan;
+    std::string err;
+    const int t = st->tile_qubits > 0 ? st->tile_qubits : default_tile(st->P);
+    if (!plan_tiles(st->n, q.data(), (int)q.size(), std::min(t, tile_max_qubits(st->P)), st->P, plan, err))
+        return set_error(LLG_EINVAL, err);
+    int rc = upload_ops(st, plan.ops);
+    if (rc) return rc;
+    for (const PassDesc& pd : plan.passes)
+        if (pd.nops > 0) LLG_CUDA(launch_tile_pass(st->P, st->d_psi, st->n, pd, st->d_ops, st->stream), "tile kernel");
+    return LLG_OK;
+}
+
+int enqueue(llg_state* st, const llg_op& op) {
+    st->queue.push_back(op);
+    if (st->queue.size() >= kQueueFlushAt) return llg_flush(st);
+    return LLG_OK;
+}
+
+llg_op make_op(int kind, int q0, int q1 = 0, double theta = 0.0, uint64_t mask = 0) {
+    llg_op op;
+    std::memset(&op, 0, sizeof(op));
+    op.kind = kind;
+    op.q0 = q0;
+    op.q1 = q1;
+    op.param = -1;
+    op.theta = theta;
+    op.mask = mask;
+    return op;
+}
+
+// Validate one record against the state (host side, before anything is enqueued).
+int validate_op(const llg_state* st, const llg_op& op, const char* who) {
+    int rc;
+    switch (op.kind) {
+        case LLG_OP_H:
+        case LLG_OP_X:
+            return check_qubit(st, op.q0, who);
+        case LLG_OP_RX:
+        case LLG_OP_RY:
+        case LLG_OP_RZ:
+            if ((rc = check_qubit(st, op.q0, who))) return rc;
+            return check_angle(op.theta, who);
+        case LLG_OP_U2:
+            if ((rc = check_qubit(st, op.q0, who))) return rc;
+            for (int k = 0; k < 8; ++k)
+                if (!finite(op.m[k])) return set_error(LLG_EINVAL, std::string(who) + ": non-finite gate entry");
+            return LLG_OK;
+        case LLG_OP_CNOT:
+            if ((rc = check_qubit(st, op.q0, who)) || (rc = check_qubit(st, op.q1, who))) return rc;
+            if (op.q0 == op.q1) return set_error(LLG_EINVAL, std::string(who) + ": control == target");
+            return LLG_OK;
+        case LLG_OP_CZ:
+            if ((rc = check_qubit(st, op.q0, who)) || (rc = check_qubit(st, op.q1, who))) return rc;
+            if (op.q0 == op.q1) return set_error(LLG_EINVAL, std::string(who) + ": duplicate qubit");
+            return LLG_OK;
+        case LLG_OP_MCZ:
+            if (op.mask == 0) return set_error(LLG_EINVAL, std::string(who) + ": empty qubit list");
+            if (st->n < 64 && (op.mask >> st->n) != 0) return set_error(LLG_EINVAL, std::string(who) + ": qubit outside [0, n)");
+            return LLG_OK;
+        default:
+            return set_error(LLG_EINVAL, std::string(who) + ": unknown op kind " + std::to_string(op.kind));
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+// C ABI
+// ------------------------------------------------------------------------------------------
+extern "C" {
+
+const char* llg_last_error(void) { return g_last_error.c_str(); }
+
+const char* llg_version(void) { return "llgpu 0.1 (sm_103a)"; }
+
+int llg_device_count(void) {
+    int c = 0;
+    if (cudaGetDeviceCount(&c) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return c;
+}
+
+int llg_create(int n_qubits, int precision, llg_state** out) {
+    if (!out) return set_error(LLG_EINVAL, "llg_create: out is NULL");
+    *out = nullptr;
+    if (n_qubits < 1 || n_qubits > kMaxQubits)
+        return set_error(LLG_EINVAL, "llg_create: n_qubits must be in [1, " + std::to_string(kMaxQubits) + "]");
+    if (precision != LLG_F64 && precision != LLG_DF64 && precision != LLG_F32)
+        return set_error(LLG_EINVAL, "llg_create: unknown precision");
+    llg_state* st = new llg_state();
+    st->P = precision;
+    int rc = ensure_device_buffers(st);
+    if (!rc) rc = alloc_state(st, n_qubits);
+    if (!rc) {
+        cudaError_t e = launch_init_basis(st->P, st->d_psi, st->size, 0, st->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "init");
+    }
+    if (rc) {
+        llg_destroy(st);
+        return rc;
+    }
+    *out = st;
+    return LLG_OK;
+}
+
+int llg_create_from_host(const double* amps, size_t len, int precision, llg_state** out) {
+    if (!out) return set_error(LLG_EINVAL, "llg_create_from_host: out is NULL");
+    *out = nullptr;
+    int n = 0;
+    while ((len >> n) > 1) ++n;
+    if (len == 0 || (1ULL << n) != len) return set_error(LLG_ERUNTIME, "Array size must be power of 2");
+    if (n > kMaxQubits) return set_error(LLG_EINVAL, "llg_create_from_host: too many amplitudes");
+    if (precision != LLG_F64 && precision != LLG_DF64 && precision != LLG_F32)
+        return set_error(LLG_EINVAL, "llg_create_from_host: unknown precision");
+    if (!amps) return set_error(LLG_EINVAL, "llg_create_from_host: amps is NULL");
+    llg_state* st = new llg_state();
+    st->P = precision;
+    int rc = ensure_device_buffers(st);
+    if (!rc) {
+        // n == 0 is a one-amplitude state: kept (the reference accepts it), every gate is a no-op
+        const uint64_t size = 1ULL << n;
+        cudaError_t e = cudaMalloc(&st->d_psi, size * elem_bytes(precision));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            rc = set_error(LLG_ENOMEM, std::string("cannot allocate HBM: ") + cudaGetErrorString(e));
+        } else {
+            st->n = n;
+            st->size = size;
+            rc = llg_copy_from_host(st, amps);
+        }
+    }
+    if (rc) {
+        llg_destroy(st);
+        return rc;
+    }
+    *out = st;
+    return LLG_OK;
+}
+
+int llg_destroy(llg_state* st) {
+    if (!st) return LLG_OK;
+    if (st->stream) cudaStreamSynchronize(st->stream);
+    if (st->d_psi) cudaFree(st->d_psi);
+    if (st->d_ops) cudaFree(st->d_ops);
+    if (st->h_ops) cudaFreeHost(st->h_ops);
+    if (st->d_partials) cudaFree(st->d_partials);
+    if (st->d_red) cudaFree(st->d_red);
+    for (int i = 0; i < 2; ++i) {
+        if (st->d_stage[i]) cudaFree(st->d_stage[i]);
+        if (st->stage_ev[i]) cudaEventDestroy(st->stage_ev[i]);
+    }
+    if (st->ops_done) cudaEventDestroy(st->ops_done);
+    if (st->stream) cudaStreamDestroy(st->stream);
+    delete st;
+    return LLG_OK;
+}
+
+int llg_reset(llg_state* st, int n_qubits) {
+    if (!st) return set_error(LLG_EINVAL, "llg_reset: NULL state");
+    if (n_qubits < 1 || n_qubits > kMaxQubits)
+        return set_error(LLG_EINVAL, "llg_reset: n_qubits must be in [1, " + std::to_string(kMaxQubits) + "]");
+    st->queue.clear();
+    int rc = alloc_state(st, n_qubits);
+    if (rc) return rc;
+    LLG_CUDA(launch_init_basis(st->P, st->d_psi, st->size, 0, st->stream), "init");
+    return LLG_OK;
+}
+
+int llg_num_qubits(const llg_state* st, int* out) {
+    if (!st || !out) return set_error(LLG_EINVAL, "llg_num_qubits: NULL argument");
+    *out = st->n;
+    return LLG_OK;
+}
+
+int llg_size(const llg_state* st, uint64_t* out) {
+    if (!st || !out) return set_error(LLG_EINVAL, "llg_size: NULL argument");
+    *out = st->size;
+    return LLG_OK;
+}
+
+int llg_get_precision(const llg_state* st, int* out) {
+    if (!st || !out) return set_error(LLG_EINVAL, "llg_get_precision: NULL argument");
+    *out = st->P;
+    return LLG_OK;
+}
+
+int llg_set_fusion(llg_state* st, int mode, int tile_qubits) {
+    if (!st) return set_error(LLG_EINVAL, "llg_set_fusion: NULL state");
+    if (mode != LLG_FUSE_NONE && mode != LLG_FUSE_TILE) return set_error(LLG_EINVAL, "llg_set_fusion: unknown mode");
+    if (tile_qubits < 0 || tile_qubits > tile_max_qubits(st->P) || (tile_qubits > 0 && tile_qubits < 5))
+        return set_error(LLG_EINVAL, "llg_set_fusion: tile_qubits must be 0 or in [5, " +
+                                         std::to_string(tile_max_qubits(st->P)) + "]");
+    int rc = llg_flush(st);
+    if (rc) return rc;
+    st->fuse_mode = mode;
+    st->tile_qubits = tile_qubits;
+    return LLG_OK;
+}
+
+int llg_apply_gate(llg_state* st, int target, const double* g) {
+    if (!st || !g) return set_error(LLG_EINVAL, "apply_gate: NULL argument");
+    if (target < 0) return set_error(LLG_EINVAL, "apply_gate: negative target " + std::to_string(target));
+    if (target >= st->n) return LLG_OK;  // reference: num_blocks = size >> (k+1) = 0, a no-op
+    llg_op op = make_op(LLG_OP_U2, target);
+    std::memcpy(op.m, g, 8 * sizeof(double));
+    return enqueue(st, op);
+}
+
+#define LLG_GATE1(name, KIND, who)                                    \
+    int name(llg_state* st, int q) {                                  \
+        if (!st) return set_error(LLG_EINVAL, who ": NULL state");    \
+        llg_op op = make_op(KIND, q);                                 \
+        int rc = validate_op(st, op, who);                            \
+        return rc ? rc : enqueue(st, op);                             \
+    }
+LLG_GATE1(llg_h, LLG_OP_H, "h")
+LLG_GATE1(llg_x, LLG_OP_X, "x")
+
+#define LLG_ROT(name, KIND, who)                                      \
+    int name(llg_state* st, int q, double theta) {                    \
+        if (!st) return set_error(LLG_EINVAL, who ": NULL state");    \
+        llg_op op = make_op(KIND, q, 0, theta);                       \
+        int rc = validate_op(st, op, who);                            \
+        return rc ? rc : enqueue(st, op);                             \
+    }
+LLG_ROT(llg_rx, LLG_OP_RX, "rx")
+LLG_ROT(llg_ry, LLG_OP_RY, "ry")
+LLG_ROT(llg_rz, LLG_OP_RZ, "rz")
+
+int llg_cnot(llg_state* st, int control, int target) {
+    if (!st) return set_error(LLG_EINVAL, "cnot: NULL state");
+    llg_op op = make_op(LLG_OP_CNOT, control, target);
+    int rc = validate_op(st, op, "cnot");
+    return rc ? rc : enqueue(st, op);
+}
+
+int llg_cz(llg_state* st, int a, int b) {
+    if (!st) return set_error(LLG_EINVAL, "cz: NULL state");
+    llg_op op = make_op(LLG_OP_CZ, a, b);
+    int rc = validate_op(st, op, "cz");
+    return rc ? rc : enqueue(st, op);
+}
+
+int llg_mcz(llg_state* st, const int* qubits, int nq) {
+    if (!st) return set_error(LLG_EINVAL, "mcz: NULL state");
+    if (nq <= 0 || !qubits) return set_error(LLG_EINVAL, "mcz: empty qubit list");
+    uint64_t mask = 0;
+    for (int i = 0; i < nq; ++i) {
+        int rc = check_qubit(st, qubits[i], "mcz");
+        if (rc) return rc;
+        const uint64_t b = 1ULL << qubits[i];
+        if (mask & b) return set_error(LLG_EINVAL, "mcz: duplicate qubit");
+        mask |= b;
+    }
+    return enqueue(st, make_op(LLG_OP_MCZ, qubits[0], 0, 0.0, mask));
+}
+
+int llg_apply_ops(llg_state* st, const llg_op* ops, int nops) {
+    if (!st || (nops > 0 && !ops)) return set_error(LLG_EINVAL, "apply_ops: NULL argument");
+    if (nops < 0) return set_error(LLG_EINVAL, "apply_ops: negative count");
+    for (int i = 0; i < nops; ++i) {
+        int rc = validate_op(st, ops[i], "apply_ops");
+        if (rc) return set_error(rc, g_last_error + " (op " + std::to_string(i) + ")");
+    }
+    for (int i = 0; i < nops; ++i) {
+        int rc = enqueue(st, ops[i]);
+        if (rc) return rc;
+    }
+    return LLG_OK;
+}
+
+int llg_apply_matrix(llg_state* st, int k, const int* qubits, const double* m) {
+    (void)st;
+    (void)k;
+    (void)qubits;
+    (void)m;
+    return set_error(LLG_EINVAL, "apply_matrix: not available in this build");
+}
+
+int llg_flush(llg_state* st) {
+    if (!st) return set_error(LLG_EINVAL, "flush: NULL state");
+    if (st->queue.empty()) return LLG_OK;
+    std::vector<llg_op> q;
+    q.swap(st->queue);
+    if (st->n == 0) return LLG_OK;
+    return st->fuse_mode == LLG_FUSE_TILE ? run_tiles(st, q) : run_streaming(st, q);
+}
+
+int llg_sync(llg_state* st) {
+    int rc = llg_flush(st);
+    if (rc) return rc;
+    LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+    return LLG_OK;
+}
+
+int llg_copy_to_host(llg_state* st, double* out) {
+    if (!st || !out) return set_error(LLG_EINVAL, "copy_to_host: NULL argument");
+    int rc = llg_flush(st);
+    if (rc) return rc;
+    if (st->P == LLG_F64) {
+        LLG_CUDA(cudaMemcpyAsync(out, st->d_psi, st->size * 16, cudaMemcpyDeviceToHost, st->stream), "cudaMemcpyAsync(D2H)");
+        LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+        return LLG_OK;
+    }
+    if ((rc = stage_buffers(st))) return rc;
+    const size_t eb = elem_bytes(st->P);
+    int which = 0;
+    for (uint64_t off = 0; off < st->size; off += kStageAmps, which ^= 1) {
+        const uint64_t cnt = std::min<uint64_t>(kStageAmps, st->size - off);
+        LLG_CUDA(cudaEventSynchronize(st->stage_ev[which]), "cudaEventSynchronize");
+        LLG_CUDA(launch_to_f64(st->P, (const char*)st->d_psi + off * eb, st->d_stage[which], cnt, st->stream), "to_f64");
+        LLG_CUDA(cudaMemcpyAsync(out + 2 * off, st->d_stage[which], cnt * 16, cudaMemcpyDeviceToHost, st->stream),
+                 "cudaMemcpyAsync(D2H)");
+        LLG_CUDA(cudaEventRecord(st->stage_ev[which], st->stream), "cudaEventRecord");
+    }
+    LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+    return LLG_OK;
+}
+
+int llg_copy_from_host(llg_state* st, const double* amps) {
+    if (!st || !amps) return set_error(LLG_EINVAL, "copy_from_host: NULL argument");
+    st->queue.clear();  // overwritten anyway
+    if (st->P == LLG_F64) {
+        LLG_CUDA(cudaMemcpyAsync(st->d_psi, amps, st->size * 16, cudaMemcpyHostToDevice, st->stream), "cudaMemcpyAsync(H2D)");
+        LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+        return LLG_OK;
+    }
+    int rc = stage_buffers(st);
+    if (rc) return rc;
+    const size_t eb = elem_bytes(st->P);
+    int which = 0;
+    for (uint64_t off = 0; off < st->size; off += kStageAmps, which ^= 1) {
+        const uint64_t cnt = std::min<uint64_t>(kStageAmps, st->size - off);
+        LLG_CUDA(cudaEventSynchronize(st->stage_ev[which]), "cudaEventSynchronize");
+        LLG_CUDA(cudaMemcpyAsync(st->d_stage[which], amps + 2 * off, cnt * 16, cudaMemcpyHostToDevice, st->stream),
+                 "cudaMemcpyAsync(H2D)");
+        LLG_CUDA(launch_from_f64(st->P, st->d_stage[which], (char*)st->d_psi + off * eb, cnt, st->stream), "from_f64");
+        LLG_CUDA(cudaEventRecord(st->stage_ev[which], st->stream), "cudaEventRecord");
+    }
+    LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+    return LLG_OK;
+}
+
+int llg_probabilities(llg_state* st, double* out) {
+    if (!st || !out) return set_error(LLG_EINVAL, "probabilities: NULL argument");
+    int rc = llg_flush(st);
+    if (rc) return rc;
+    if ((rc = stage_buffers(st))) return rc;
+    const size_t eb = elem_bytes(st->P);
+    const uint64_t chunk = kStageAmps * 2;  // doubles per staging buffer
+    int which = 0;
+    for (uint64_t off = 0; off < st->size; off += chunk, which ^= 1) {
+        const uint64_t cnt = std::min<uint64_t>(chunk, st->size - off);
+        LLG_CUDA(cudaEventSynchronize(st->stage_ev[which]), "cudaEventSynchronize");
+        LLG_CUDA(launch_probabilities(st->P, (const char*)st->d_psi + off * eb, st->d_stage[which], cnt, st->stream),
+                 "probabilities");
+        LLG_CUDA(cudaMemcpyAsync(out + off, st->d_stage[which], cnt * 8, cudaMemcpyDeviceToHost, st->stream),
+                 "cudaMemcpyAsync(D2H)");
+        LLG_CUDA(cudaEventRecord(st->stage_ev[which], st->stream), "cudaEventRecord");
+    }
+    LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+    return LLG_OK;
+}
+
+static int build_zterms(int nterms, const int* a, const int* b, const double* coeff, int n, ZTerms& z) {
+    if (nterms < 0 || nterms > kMaxZTerms)
+        return set_error(LLG_EINVAL, "expect_zz: at most " + std::to_string(kMaxZTerms) + " terms");
+    std::memset(&z, 0, sizeof(z));
+    z.nterms = nterms;
+    for (int k = 0; k < nterms; ++k) {
+        if (a[k] < 0 || a[k] >= n || b[k] >= n || b[k] == a[k])
+            return set_error(LLG_EINVAL, "expect_zz: term " + std::to_string(k) + " has a bad qubit");
+        if (!std::isfinite(coeff[k])) return set_error(LLG_EINVAL, "expect_zz: non-finite coefficient");
+        int c = -1;
+        for (int j = 0; j < z.nclass; ++j)
+            if (z.coef[j] == coeff[k]) c = j;
+        if (c < 0) {
+            if (z.nclass == kMaxZClasses)
+                return set_error(LLG_EINVAL, "expect_zz: at most " + std::to_string(kMaxZClasses) + " distinct coefficients");
+            c = z.nclass++;
+            z.coef[c] = coeff[k];
+        }
+        z.a[k] = a[k];
+        z.b[k] = b[k] < 0 ? -1 : b[k];
+        z.cls[k] = c;
+    }
+    return LLG_OK;
+}
+
+static int reduce(llg_state* st, const ZTerms& z, double* slots) {
+    int rc = llg_flush(st);
+    if (rc) return rc;
+    LLG_CUDA(launch_reduce_z(st->P, st->d_psi, st->n, z, st->d_partials, st->d_red, st->stream), "reduce");
+    LLG_CUDA(cudaMemcpyAsync(slots, st->d_red, sizeof(double) * kRedSlots, cudaMemcpyDeviceToHost, st->stream),
+             "cudaMemcpyAsync(D2H)");
+    LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+    return LLG_OK;
+}
+
+int llg_norm2(llg_state* st, double* out) {
+    if (!st || !out) return set_error(LLG_EINVAL, "norm2: NULL argument");
+    ZTerms z;
+    std::memset(&z, 0, sizeof(z));
+    double slots[kRedSlots];
+    int rc = reduce(st, z, slots);
+    if (rc) return rc;
+    *out = slots[0];
+    return LLG_OK;
+}
+
+int llg_expect_zz(llg_state* st, int nterms, const int* a, const int* b, const double* coeff, double* out) {
+    if (!st || !out || (nterms > 0 && (!a || !b || !coeff))) return set_error(LLG_EINVAL, "expect_zz: NULL argument");
+    ZTerms z;
+    int rc = build_zterms(nterms, a, b, coeff, st->n, z);
+    if (rc) return rc;
+    double slots[kRedSlots];
+    if ((rc = reduce(st, z, slots))) return rc;
+    // sum_k c_k <Z..> = sum_c c_c * (count_c * N - 2 W_c)
+    double e = 0.0;
+    for (int c = 0; c < z.nclass; ++c) {
+        int cnt = 0;
+        for (int k = 0; k < nterms; ++k) cnt += z.cls[k] == c;
+        e += z.coef[c] * (cnt * slots[0] - 2.0 * slots[1 + c]);
+    }
+    *out = e;
+    return LLG_OK;
+}
+
+int llg_renormalize(llg_state* st) {
+    double nrm = 0.0;
+    int rc = llg_norm2(st, &nrm);
+    if (rc) return rc;
+    if (!(nrm > 0.0) || !std::isfinite(nrm)) return set_error(LLG_ERUNTIME, "renormalize: state norm vanished");
+    LLG_CUDA(launch_scale(st->P, st->d_psi, st->size, 1.0 / std::sqrt(nrm), st->stream), "scale");
+    return LLG_OK;
+}
+
+void* llg_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void llg_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+int llg_plan_export(int n, const llg_op* ops, int nops, int tile_qubits, llg_pass_info* passes, int max_passes,
+                    int* npasses, llg_exec_op* xops, int max_xops, int* nxops) {
+    if (n < 1 || n > kMaxQubits || nops < 0 || (nops > 0 && !ops) || !npasses || !nxops)
+        return set_error(LLG_EINVAL, "plan_export: bad argument");
+    if (tile_qubits < 1 || tile_qubits > 14) return set_error(LLG_EINVAL, "plan_export: tile_qubits out of range");
+    llg_state tmp;
+    tmp.n = n;
+    for (int i = 0; i < nops; ++i) {
+        int rc = validate_op(&tmp, ops[i], "plan_export");
+        if (rc) return rc;
+    }
+    Plan plan;
+    std::string err;
+    if (!plan_tiles(n, ops, nops, tile_qubits, LLG_F64, plan, err)) return set_error(LLG_EINVAL, err);
+    *npasses = (int)plan.passes.size();
+    *nxops = (int)plan.ops.size();
+    if (passes)
+        for (int p = 0; p < (int)plan.passes.size() && p < max_passes; ++p) {
+            const PassDesc& d = plan.passes[p];
+            passes[p].local_mask = d.local_mask;
+            passes[p].t = d.t;
+            passes[p].low = d.low;
+            passes[p].op_begin = d.op_begin;
+            passes[p].nops = d.nops;
+        }
+    if (xops)
+        for (int i = 0; i < (int)plan.ops.size() && i < max_xops; ++i) {
+            static_assert(sizeof(llg_exec_op) == sizeof(ExecOp), "llg_exec_op mirrors ExecOp");
+            std::memcpy(&xops[i], &plan.ops[i], sizeof(ExecOp));
+        }
+    return LLG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,76 @@
+// llg_internal.h -- records shared by the host engine, the fusion planner and the kernels.
+// Plain C++ (no CUDA types), so the planner compiles and is tested without a GPU.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/llgpu.h"
+
+namespace llg {
+
+// Executor op kinds (what a kernel actually runs; the planner lowers llg_op records to these).
+enum ExecKind : int32_t {
+    EX_U2 = 0,    // generic 2x2 on q0; c[0..7] = g00, g01, g10, g11 (re, im)
+    EX_RX = 1,    // c[0] = cos(t/2), c[1] = sin(t/2)
+    EX_RY = 2,    // same coefficients
+    EX_H = 3,     // c[0] = 1/sqrt(2)
+    EX_X = 4,     // swap
+    EX_DIAG = 5,  // diag(d0, d1) on q0; c[0..3] = d0 (re, im), d1 (re, im); RZ(t) = diag(e^-it/2, e^it/2)
+    EX_CNOT = 6,  // control q0, target q1
+    EX_MCZ = 7,   // negate amplitudes with all `mask` bits set
+};
+
+// Flags of a tile op.
+enum : int32_t {
+    OPF_NONLOCAL_Q0 = 1,  // q0 is a global qubit outside the tile (diagonal / control use only)
+};
+
+// One executor op.  In a tile pass q0/q1/mask are LOCAL (tile) indices unless flagged; `nl_mask`
+// holds the global bits that must all be set in the tile's base index for the op to act.
+// Coefficients are 64-bit slots packed for the state's precision (see pack_coef).
+struct ExecOp {
+    int32_t kind;
+    int32_t q0;
+    int32_t q1;
+    int32_t flags;
+    uint64_t mask;
+    uint64_t nl_mask;
+    uint64_t c[8];
+};
+static_assert(sizeof(ExecOp) == 96, "ExecOp layout");
+
+constexpr int kMaxTileQubits = 13;
+constexpr int kMaxHiPos = 16;
+
+// One fused pass: a tile of 2^t amplitudes whose index bits vary over `local` (the low `low`
+// bits 0..low-1 plus hi_pos[0..t-low-1]), ops [op_begin, op_begin + nops).
+struct PassDesc {
+    uint64_t local_mask;
+    int32_t t;
+    int32_t low;
+    int32_t op_begin;
+    int32_t nops;
+    int32_t hi_pos[kMaxHiPos];
+};
+
+struct Plan {
+    std::vector<PassDesc> passes;
+    std::vector<ExecOp> ops;
+    std::vector<int> source_index;  // for each ExecOp, index of the llg_op it came from (-1: fused)
+};
+
+// Lower and plan a gate list into tile passes (llg_plan.cpp).  Returns false with `err` set on
+// invalid input.
+bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int precision, Plan& out, std::string& err);
+
+// Lower one gate record to executor ops with GLOBAL qubit indices (streaming path).
+bool lower_op(int n, const llg_op& op, int precision, std::vector<ExecOp>& out, std::string& err);
+
+// 2x2 matrix (row-major, interleaved) of a single-qubit gate record.
+void op_matrix(const llg_op& op, double m[8]);
+
+bool is_single_qubit(int kind);
+
+}  // namespace llg

@@ -1,0 +1,507 @@
+// llg_kernels.cu -- state-vector kernels for sm_103a (GB300).
+//
+//  * streaming passes (one kernel per gate, the reference's own per-gate algorithm,
+//    src/StateVectorBackend.h:109-218 and src/StateVectorOptimized.cpp:56-78): every thread
+//    owns amplitude pairs p -> (i0 = insert0(p, q), i0 | 2^q); consecutive threads take
+//    consecutive p, so both halves of a pair stream coalesced for every q (for q = 0 one thread
+//    reads the 32 contiguous bytes of its pair).  CNOT walks the N/4 quads with control = 1 and
+//    swaps target halves; MCZ touches only the 2^(n-m) amplitudes with every mask bit set.
+//  * tile passes (llg_plan.cpp): one CTA loads 2^t amplitudes spread over a chosen qubit set into
+//    shared memory in 2^low-amplitude contiguous runs, applies a list of ops there, writes back.
+//  * conversions to/from complex128, |a|^2, scaling, and deterministic two-stage reductions
+//    (fixed grid, per-block partials, one FP64 pass over the partials).
+#include <cstdio>
+
+#include "llg_common.cuh"
+#include "llg_launch.h"
+
+namespace llg {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+int g_sms = 0;
+int sm_count() {
+    if (g_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms <= 0) g_sms = 1;
+    }
+    return g_sms;
+}
+
+unsigned grid_for(uint64_t items, int per_thread) {
+    const uint64_t want = (items + (uint64_t)kThreads * per_thread - 1) / ((uint64_t)kThreads * per_thread);
+    const uint64_t cap = (uint64_t)sm_count() * 16;
+    return (unsigned)(want < 1 ? 1 : (want > cap ? cap : want));
+}
+
+// ------------------------------------------------------------------------------------------
+// the per-pair / per-amplitude math, shared by streaming and tile kernels
+// ------------------------------------------------------------------------------------------
+template <class P, int KIND>
+struct PairMath {
+    using K = typename P::K;
+    using C = typename P::C;
+    K k[8];
+    __device__ explicit PairMath(const ExecOp& o) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) k[i] = P::k_from_bits(o.c[i]);
+        if (KIND == EX_U2) {
+            // pre-negate the imaginary parts used with a minus sign
+            k[1] = P::kneg(k[1]);  // -g00i  (re rows use -gi)
+            k[3] = P::kneg(k[3]);
+            k[5] = P::kneg(k[5]);
+            k[7] = P::kneg(k[7]);
+        }
+    }
+    __device__ __forceinline__ void apply(C& a0, C& a1) const {
+        const auto x0 = a0.re, y0 = a0.im, x1 = a1.re, y1 = a1.im;
+        if (KIND == EX_U2) {
+            // k[0] = g00r, k[1] = -g00i, k[2] = g01r, k[3] = -g01i, ...
+            a0.re = P::lin4(k[0], x0, k[1], y0, k[2], x1, k[3], y1);
+            a0.im = P::lin4(k[0], y0, P::kneg(k[1]), x0, k[2], y1, P::kneg(k[3]), x1);
+            a1.re = P::lin4(k[4], x0, k[5], y0, k[6], x1, k[7], y1);
+            a1.im = P::lin4(k[4], y0, P::kneg(k[5]), x0, k[6], y1, P::kneg(k[7]), x1);
+        } else if (KIND == EX_RX) {  // [c, -is; -is, c]
+            const auto c = k[0], s = k[1], ms = P::kneg(k[1]);
+            a0.re = P::lin2(c, x0, s, y1);
+            a0.im = P::lin2(c, y0, ms, x1);
+            a1.re = P::lin2(s, y0, c, x1);
+            a1.im = P::lin2(ms, x0, c, y1);
+        } else if (KIND == EX_RY) {  // [c, -s; s, c]
+            const auto c = k[0], s = k[1], ms = P::kneg(k[1]);
+            a0.re = P::lin2(c, x0, ms, x1);
+            a0.im = P::lin2(c, y0, ms, y1);
+            a1.re = P::lin2(s, x0, c, x1);
+            a1.im = P::lin2(s, y0, c, y1);
+        } else if (KIND == EX_H) {  // r [1, 1; 1, -1]
+            const auto r = k[0], mr = P::kneg(k[0]);
+            a0.re = P::lin2(r, x0, r, x1);
+            a0.im = P::lin2(r, y0, r, y1);
+            a1.re = P::lin2(r, x0, mr, x1);
+            a1.im = P::lin2(r, y0, mr, y1);
+        } else {  // EX_X
+            const C t = a0;
+            a0 = a1;
+            a1 = t;
+        }
+    }
+};
+
+// a <- d * a for a complex constant d = (dr, di)
+template <class P>
+__device__ __forceinline__ void cmul_const(typename P::C& a, typename P::K dr, typename P::K di, typename P::K mdi) {
+    const auto x = a.re, y = a.im;
+    a.re = P::lin2(dr, x, mdi, y);
+    a.im = P::lin2(dr, y, di, x);
+}
+
+// ------------------------------------------------------------------------------------------
+// streaming kernels (global qubit indices)
+// ------------------------------------------------------------------------------------------
+template <class P, int KIND>
+__global__ void __launch_bounds__(kThreads) k_pairs(typename P::S* __restrict__ psi, uint64_t npairs, int q, ExecOp op) {
+    using S = typename P::S;
+    using C = typename P::C;
+    const PairMath<P, KIND> m(op);
+    const uint64_t bit = 1ULL << q;
+    const uint64_t step = (uint64_t)gridDim.x * kThreads * 2;
+    for (uint64_t base = (uint64_t)blockIdx.x * kThreads * 2 + threadIdx.x; base < npairs; base += step) {
+        const uint64_t pA = base, pB = base + kThreads;
+        const bool hasB = pB < npairs;
+        const uint64_t iA = insert0(pA, q), iB = insert0(hasB ? pB : pA, q);
+        S sA0 = psi[iA], sA1 = psi[iA | bit];
+        S sB0, sB1;
+        if (hasB) {
+            sB0 = psi[iB];
+            sB1 = psi[iB | bit];
+        }
+        C a0 = P::load(sA0), a1 = P::load(sA1);
+        m.apply(a0, a1);
+        psi[iA] = P::store(a0);
+        psi[iA | bit] = P::store(a1);
+        if (hasB) {
+            C b0 = P::load(sB0), b1 = P::load(sB1);
+            m.apply(b0, b1);
+            psi[iB] = P::store(b0);
+            psi[iB | bit] = P::store(b1);
+        }
+    }
+}
+
+// diag(d0, d1) on qubit q
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_diag(typename P::S* __restrict__ psi, uint64_t size, int q, ExecOp op) {
+    using K = typename P::K;
+    const K d0r = P::k_from_bits(op.c[0]), d0i = P::k_from_bits(op.c[1]);
+    const K d1r = P::k_from_bits(op.c[2]), d1i = P::k_from_bits(op.c[3]);
+    const K md0i = P::kneg(d0i), md1i = P::kneg(d1i);
+    const uint64_t step = (uint64_t)gridDim.x * kThreads;
+    for (uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x; i < size; i += step) {
+        auto a = P::load(psi[i]);
+        if ((i >> q) & 1) cmul_const<P>(a, d1r, d1i, md1i);
+        else cmul_const<P>(a, d0r, d0i, md0i);
+        psi[i] = P::store(a);
+    }
+}
+
+// CNOT: swap (c=1, t=0) <-> (c=1, t=1) over the N/4 quads (src/StateVectorBackend.h:109-135)
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_cnot(typename P::S* __restrict__ psi, uint64_t nquads, int c, int t) {
+    const int lo = c < t ? c : t, hi = c < t ? t : c;
+    const uint64_t cbit = 1ULL << c, tbit = 1ULL << t;
+    const uint64_t step = (uint64_t)gridDim.x * kThreads;
+    for (uint64_t r = (uint64_t)blockIdx.x * kThreads + threadIdx.x; r < nquads; r += step) {
+        const uint64_t i = insert0(insert0(r, lo), hi) | cbit;
+        const auto x = psi[i];
+        psi[i] = psi[i | tbit];
+        psi[i | tbit] = x;
+    }
+}
+
+// MCZ: negate the amplitudes with every mask bit set (src/StateVectorBackend.h:137-151)
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_mcz(typename P::S* __restrict__ psi, uint64_t count, uint64_t mask) {
+    const uint64_t step = (uint64_t)gridDim.x * kThreads;
+    for (uint64_t r = (uint64_t)blockIdx.x * kThreads + threadIdx.x; r < count; r += step) {
+        const uint64_t i = insert0_mask(r, mask) | mask;
+        auto a = P::load(psi[i]);
+        a.re = P::neg(a.re);
+        a.im = P::neg(a.im);
+        psi[i] = P::store(a);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// tile pass
+// ------------------------------------------------------------------------------------------
+template <class P, int KIND>
+__device__ __forceinline__ void tile_pairs(typename P::S* tile, uint32_t npairs, int q, const ExecOp& o) {
+    const PairMath<P, KIND> m(o);
+    const uint32_t bit = 1u << q;
+    for (uint32_t p = threadIdx.x; p < npairs; p += blockDim.x) {
+        const uint32_t j0 = (uint32_t)insert0(p, q), j1 = j0 | bit;
+        auto a0 = P::load(tile[j0]);
+        auto a1 = P::load(tile[j1]);
+        m.apply(a0, a1);
+        tile[j0] = P::store(a0);
+        tile[j1] = P::store(a1);
+    }
+}
+
+template <class P>
+__global__ void __launch_bounds__(512) k_tile(typename P::S* __restrict__ psi, PassDesc pd, const ExecOp* __restrict__ ops) {
+    using S = typename P::S;
+    using K = typename P::K;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int t = pd.t, low = pd.low;
+    const uint32_t tsize = 1u << t;
+    const uint32_t nhi = 1u << (t - low);
+    S* tile = reinterpret_cast<S*>(smem_raw);
+    uint64_t* hi_off = reinterpret_cast<uint64_t*>(smem_raw + (size_t)tsize * sizeof(S));
+
+    const uint64_t base = insert0_mask((uint64_t)blockIdx.x, pd.local_mask);
+    for (uint32_t h = threadIdx.x; h < nhi; h += blockDim.x) {
+        uint64_t off = 0;
+        for (int j = 0; j < t - low; ++j)
+            if ((h >> j) & 1) off |= 1ULL << pd.hi_pos[j];
+        hi_off[h] = off;
+    }
+    __syncthreads();
+    const uint32_t lowmask = (1u << low) - 1;
+    for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x)
+        tile[l] = psi[base | hi_off[l >> low] | (l & lowmask)];
+    __syncthreads();
+
+    for (int k = 0; k < pd.nops; ++k) {
+        const ExecOp& o = ops[pd.op_begin + k];
+        const int kind = o.kind;
+        switch (kind) {
+            case EX_U2: tile_pairs<P, EX_U2>(tile, tsize >> 1, o.q0, o); break;
+            case EX_RX: tile_pairs<P, EX_RX>(tile, tsize >> 1, o.q0, o); break;
+            case EX_RY: tile_pairs<P, EX_RY>(tile, tsize >> 1, o.q0, o); break;
+            case EX_H: tile_pairs<P, EX_H>(tile, tsize >> 1, o.q0, o); break;
+            case EX_X: tile_pairs<P, EX_X>(tile, tsize >> 1, o.q0, o); break;
+            case EX_DIAG: {
+                const K d0r = P::k_from_bits(o.c[0]), d0i = P::k_from_bits(o.c[1]);
+                const K d1r = P::k_from_bits(o.c[2]), d1i = P::k_from_bits(o.c[3]);
+                if (o.flags & OPF_NONLOCAL_Q0) {
+                    const bool one = (base >> o.q0) & 1;
+                    const K dr = one ? d1r : d0r, di = one ? d1i : d0i;
+                    const K mdi = P::kneg(di);
+                    for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
+                        auto a = P::load(tile[l]);
+                        cmul_const<P>(a, dr, di, mdi);
+                        tile[l] = P::store(a);
+                    }
+                } else {
+                    const K md0i = P::kneg(d0i), md1i = P::kneg(d1i);
+                    const int q = o.q0;
+                    for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
+                        auto a = P::load(tile[l]);
+                        if ((l >> q) & 1) cmul_const<P>(a, d1r, d1i, md1i);
+                        else cmul_const<P>(a, d0r, d0i, md0i);
+                        tile[l] = P::store(a);
+                    }
+                }
+                break;
+            }
+            case EX_CNOT: {
+                const int tq = o.q1;
+                if (o.flags & OPF_NONLOCAL_Q0) {
+                    if ((base >> o.q0) & 1) tile_pairs<P, EX_X>(tile, tsize >> 1, tq, o);
+                } else {
+                    const int c = o.q0;
+                    const int lo = c < tq ? c : tq, hi = c < tq ? tq : c;
+                    const uint32_t cbit = 1u << c, tbit = 1u << tq;
+                    for (uint32_t r = threadIdx.x; r < (tsize >> 2); r += blockDim.x) {
+                        const uint32_t j = (uint32_t)insert0(insert0(r, lo), hi) | cbit;
+                        const S x = tile[j];
+                        tile[j] = tile[j | tbit];
+                        tile[j | tbit] = x;
+                    }
+                }
+                break;
+            }
+            case EX_MCZ: {
+                if ((base & o.nl_mask) == o.nl_mask) {
+                    const uint32_t lm = (uint32_t)o.mask;
+                    const uint32_t cnt = tsize >> __popc(lm);
+                    for (uint32_t r = threadIdx.x; r < cnt; r += blockDim.x) {
+                        const uint32_t j = (uint32_t)insert0_mask(r, lm) | lm;
+                        auto a = P::load(tile[j]);
+                        a.re = P::neg(a.re);
+                        a.im = P::neg(a.im);
+                        tile[j] = P::store(a);
+                    }
+                }
+                break;
+            }
+            default: break;
+        }
+        __syncthreads();
+    }
+
+    for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) psi[base | hi_off[l >> low] | (l & lowmask)] = tile[l];
+}
+
+// ------------------------------------------------------------------------------------------
+// conversions, probabilities, scaling
+// ------------------------------------------------------------------------------------------
+template <class P>
+__global__ void k_from_f64(const double2* __restrict__ src, typename P::S* __restrict__ dst, uint64_t count) {
+    const uint64_t step = (uint64_t)gridDim.x * kThreads;
+    for (uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x; i < count; i += step) dst[i] = P::store(P::from_f64(src[i]));
+}
+
+template <class P>
+__global__ void k_to_f64(const typename P::S* __restrict__ src, double2* __restrict__ dst, uint64_t count) {
+    const uint64_t step = (uint64_t)gridDim.x * kThreads;
+    for (uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x; i < count; i += step) dst[i] = P::to_f64(P::load(src[i]));
+}
+
+template <class P>
+__global__ void k_probs(const typename P::S* __restrict__ src, double* __restrict__ out, uint64_t count) {
+    const uint64_t step = (uint64_t)gridDim.x * kThreads;
+    for (uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x; i < count; i += step)
+        out[i] = P::acc_to_double(P::acc_norm(P::acc_zero(), P::load(src[i])));
+}
+
+template <class P>
+__global__ void k_scale(typename P::S* __restrict__ psi, uint64_t count, uint64_t fbits) {
+    const typename P::K f = P::k_from_bits(fbits);
+    const uint64_t step = (uint64_t)gridDim.x * kThreads;
+    for (uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x; i < count; i += step) {
+        auto a = P::load(psi[i]);
+        a.re = P::mulk(f, a.re);
+        a.im = P::mulk(f, a.im);
+        psi[i] = P::store(a);
+    }
+}
+
+template <class S>
+__global__ void k_set_one(S* psi, uint64_t index, S one) { psi[index] = one; }
+
+// ------------------------------------------------------------------------------------------
+// reductions: slot 0 = sum |a|^2, slot 1+c = sum |a_i|^2 * (#odd-parity terms of class c in i)
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += sh[w];
+    return r;
+}
+
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_reduce_z(const typename P::S* __restrict__ psi, uint64_t size, ZTerms z,
+                                                      double* __restrict__ partials) {
+    __shared__ double sh[kThreads / 32];
+    typename P::Acc acc[kRedSlots];
+#pragma unroll
+    for (int s = 0; s < kRedSlots; ++s) acc[s] = P::acc_zero();
+    const uint64_t step = (uint64_t)gridDim.x * kThreads;
+    for (uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x; i < size; i += step) {
+        const auto a = P::load(psi[i]);
+        acc[0] = P::acc_norm(acc[0], a);
+        if (z.nterms > 0) {
+            int cnt[kMaxZClasses] = {0, 0, 0, 0};
+            for (int k = 0; k < z.nterms; ++k) {
+                int par = (int)((i >> z.a[k]) & 1);
+                if (z.b[k] >= 0) par ^= (int)((i >> z.b[k]) & 1);
+                cnt[z.cls[k]] += par;
+            }
+#pragma unroll
+            for (int c = 0; c < kMaxZClasses; ++c)
+                if (c < z.nclass && cnt[c]) acc[1 + c] = P::acc_norm_w(acc[1 + c], a, (float)cnt[c]);
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < kRedSlots; ++s) {
+        const double v = block_sum(P::acc_to_double(acc[s]), sh);
+        if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kRedSlots + s] = v;
+    }
+}
+
+__global__ void k_finish(const double* __restrict__ partials, int nblocks, double* __restrict__ out) {
+    // one thread per slot, fixed order: deterministic
+    const int s = threadIdx.x;
+    if (s >= kRedSlots) return;
+    double r = 0.0;
+    for (int b = 0; b < nblocks; ++b) r += partials[(size_t)b * kRedSlots + s];
+    out[s] = r;
+}
+
+template <class P>
+cudaError_t exec_op_t(void* vpsi, int n, const ExecOp& op, cudaStream_t s) {
+    using S = typename P::S;
+    S* psi = static_cast<S*>(vpsi);
+    const uint64_t size = 1ULL << n;
+    switch (op.kind) {
+        case EX_U2: k_pairs<P, EX_U2><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
+        case EX_RX: k_pairs<P, EX_RX><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
+        case EX_RY: k_pairs<P, EX_RY><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
+        case EX_H: k_pairs<P, EX_H><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
+        case EX_X: k_pairs<P, EX_X><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
+        case EX_DIAG: k_diag<P><<<grid_for(size, 1), kThreads, 0, s>>>(psi, size, op.q0, op); break;
+        case EX_CNOT: k_cnot<P><<<grid_for(size / 4, 1), kThreads, 0, s>>>(psi, size / 4, op.q0, op.q1); break;
+        case EX_MCZ: {
+            const uint64_t cnt = size >> __builtin_popcountll(op.mask);
+            k_mcz<P><<<grid_for(cnt, 1), kThreads, 0, s>>>(psi, cnt, op.mask);
+            break;
+        }
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+template <class P>
+size_t tile_smem_bytes(int t, int low) {
+    return ((size_t)1 << t) * sizeof(typename P::S) + ((size_t)1 << (t - low)) * sizeof(uint64_t);
+}
+
+template <class P>
+cudaError_t tile_pass_t(void* vpsi, int n, const PassDesc& pd, const ExecOp* d_ops, cudaStream_t s) {
+    static bool attr_set = false;
+    const size_t smem = tile_smem_bytes<P>(pd.t, pd.low);
+    if (!attr_set) {
+        const size_t maxs = tile_smem_bytes<P>(tile_max_qubits(P::kPrecision), 4);
+        cudaError_t e = cudaFuncSetAttribute(k_tile<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxs);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    const uint64_t ntiles = 1ULL << (n - pd.t);
+    const int threads = pd.t >= 10 ? 512 : (pd.t >= 6 ? (1 << (pd.t - 1)) : 32);
+    k_tile<P><<<(unsigned)ntiles, threads, smem, s>>>(static_cast<typename P::S*>(vpsi), pd, d_ops);
+    return cudaGetLastError();
+}
+
+template <class P>
+cudaError_t init_basis_t(void* vpsi, uint64_t size, uint64_t index, cudaStream_t s) {
+    using S = typename P::S;
+    cudaError_t e = cudaMemsetAsync(vpsi, 0, size * sizeof(S), s);
+    if (e != cudaSuccess) return e;
+    S one;
+    if (sizeof(S) == 16 && P::kPrecision == 0) {
+        double2 d = make_double2(1.0, 0.0);
+        memcpy(&one, &d, sizeof(S));
+    } else if (P::kPrecision == 1) {
+        float4 f = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+        memcpy(&one, &f, sizeof(S));
+    } else {
+        float2 f = make_float2(1.0f, 0.0f);
+        memcpy(&one, &f, sizeof(S));
+    }
+    k_set_one<S><<<1, 1, 0, s>>>(static_cast<S*>(vpsi), index, one);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t elem_bytes(int P) { return P == LLG_F32 ? 8 : 16; }
+
+int tile_max_qubits(int P) { return P == LLG_F32 ? 14 : 13; }
+
+#define LLG_DISPATCH(P, ...)                                 \
+    switch (P) {                                             \
+        case LLG_F64: { using Pol = PolF64; __VA_ARGS__; }   \
+        case LLG_DF64: { using Pol = PolDF64; __VA_ARGS__; } \
+        case LLG_F32: { using Pol = PolF32; __VA_ARGS__; }   \
+        default: return cudaErrorInvalidValue;               \
+    }
+
+cudaError_t launch_init_basis(int P, void* psi, uint64_t size, uint64_t index, cudaStream_t s) {
+    LLG_DISPATCH(P, return init_basis_t<Pol>(psi, size, index, s));
+}
+
+cudaError_t launch_exec_op(int P, void* psi, int n, const ExecOp& op, cudaStream_t s) {
+    LLG_DISPATCH(P, return exec_op_t<Pol>(psi, n, op, s));
+}
+
+cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, cudaStream_t s) {
+    LLG_DISPATCH(P, return tile_pass_t<Pol>(psi, n, pd, d_ops, s));
+}
+
+cudaError_t launch_from_f64(int P, const double* src, void* dst, uint64_t count, cudaStream_t s) {
+    LLG_DISPATCH(P, k_from_f64<Pol><<<grid_for(count, 1), kThreads, 0, s>>>(reinterpret_cast<const double2*>(src),
+                                                                            static_cast<typename Pol::S*>(dst), count);
+                 return cudaGetLastError());
+}
+
+cudaError_t launch_to_f64(int P, const void* src, double* dst, uint64_t count, cudaStream_t s) {
+    LLG_DISPATCH(P, k_to_f64<Pol><<<grid_for(count, 1), kThreads, 0, s>>>(static_cast<const typename Pol::S*>(src),
+                                                                          reinterpret_cast<double2*>(dst), count);
+                 return cudaGetLastError());
+}
+
+cudaError_t launch_probabilities(int P, const void* psi, double* out, uint64_t count, cudaStream_t s) {
+    LLG_DISPATCH(P, k_probs<Pol><<<grid_for(count, 1), kThreads, 0, s>>>(static_cast<const typename Pol::S*>(psi), out,
+                                                                         count);
+                 return cudaGetLastError());
+}
+
+cudaError_t launch_scale(int P, void* psi, uint64_t count, double factor, cudaStream_t s) {
+    const uint64_t bits = pack_coef(P, factor);
+    LLG_DISPATCH(P, k_scale<Pol><<<grid_for(count, 1), kThreads, 0, s>>>(static_cast<typename Pol::S*>(psi), count, bits);
+                 return cudaGetLastError());
+}
+
+cudaError_t launch_reduce_z(int P, const void* psi, int n, const ZTerms& terms, double* d_partials, double* d_out,
+                            cudaStream_t s) {
+    const uint64_t size = 1ULL << n;
+    unsigned g = grid_for(size, 4);
+    if (g > (unsigned)kRedBlocks) g = kRedBlocks;
+    LLG_DISPATCH(P, k_reduce_z<Pol><<<g, kThreads, 0, s>>>(static_cast<const typename Pol::S*>(psi), size, terms, d_partials);
+                 cudaError_t e = cudaGetLastError(); if (e != cudaSuccess) return e;
+                 k_finish<<<1, 32, 0, s>>>(d_partials, (int)g, d_out); return cudaGetLastError());
+}
+
+}  // namespace llg

@@ -1,0 +1,44 @@
+// llg_launch.h -- host-side launchers of the state-vector kernels (llg_kernels.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "llg_internal.h"
+
+namespace llg {
+
+// Observable sum_k coef[cls[k]] * Z_{a[k]} (Z_{b[k]} if b[k] >= 0), terms grouped into at most
+// kMaxZClasses coefficient classes so the kernels count parities per class in integers.
+constexpr int kMaxZTerms = 64;
+constexpr int kMaxZClasses = 4;
+struct ZTerms {
+    int32_t nterms;
+    int32_t nclass;
+    int32_t a[kMaxZTerms];
+    int32_t b[kMaxZTerms];
+    int32_t cls[kMaxZTerms];
+    double coef[kMaxZClasses];
+};
+
+// Per-block partial results of a reduction: up to kRedSlots doubles per block.
+constexpr int kRedSlots = 1 + kMaxZClasses;
+constexpr int kRedBlocks = 1024;
+
+size_t elem_bytes(int precision);
+
+cudaError_t launch_init_basis(int P, void* psi, uint64_t size, uint64_t index, cudaStream_t s);
+cudaError_t launch_exec_op(int P, void* psi, int n, const ExecOp& op, cudaStream_t s);
+cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, cudaStream_t s);
+cudaError_t launch_from_f64(int P, const double* src, void* dst, uint64_t count, cudaStream_t s);
+cudaError_t launch_to_f64(int P, const void* src, double* dst, uint64_t count, cudaStream_t s);
+cudaError_t launch_probabilities(int P, const void* psi, double* out, uint64_t count, cudaStream_t s);
+cudaError_t launch_scale(int P, void* psi, uint64_t count, double factor, cudaStream_t s);
+// Writes [norm2, W_0 .. W_{nclass-1}] (W_c = sum_i |a_i|^2 * #odd-parity terms of class c in i)
+// to d_out (device, kRedSlots doubles), via d_partials (device, kRedBlocks * kRedSlots doubles).
+cudaError_t launch_reduce_z(int P, const void* psi, int n, const ZTerms& terms, double* d_partials, double* d_out,
+                            cudaStream_t s);
+
+int tile_max_qubits(int P);
+
+}  // namespace llg

@@ -1,0 +1,359 @@
+// llg_plan.cpp -- lowers gate records to executor ops and plans them into shared-memory tile
+// passes (the GPU form of the reference's cache blocking, src/StateVectorOptimized.cpp:55-78,
+// and of its gate fuser, python/gate_fusion.py:15-37).
+//
+// A tile pass loads 2^t amplitudes whose index bits vary over a qubit set S -- always the `low`
+// least-significant qubits, so every tile is made of contiguous 2^low-amplitude runs that load
+// coalesced, plus up to t - low qubits anywhere in the register -- applies every op it owns in
+// shared memory, and writes the tile back: one HBM read and write of the state per pass, however
+// many gates the pass applies.  Choosing S per pass replaces an explicit qubit-remap sweep.
+//
+// Greedy plan: scan the remaining ops in order with the local set S starting as the low qubits.
+// An op joins the pass if none of its qubits is blocked and the qubits it needs local (the target
+// of a non-diagonal 1-qubit gate or of a CNOT; none for RZ/CZ/MCZ, which are diagonal and act
+// tile-uniformly on non-local bits) fit in S (S grows up to t qubits).  Otherwise it is deferred
+// and its qubits are blocked, so no later op on those qubits overtakes it.  The first remaining
+// op always fits, so every pass makes progress.  Inside a pass, runs of 1-qubit gates on the same
+// qubit with nothing else on that qubit between them are multiplied into one 2x2 (g2 @ g1, the
+// fuser's rule) before lowering.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "llg_common_host.h"
+#include "llg_internal.h"
+
+namespace llg {
+
+bool is_single_qubit(int kind) {
+    return kind == LLG_OP_H || kind == LLG_OP_X || kind == LLG_OP_RX || kind == LLG_OP_RY || kind == LLG_OP_RZ ||
+           kind == LLG_OP_U2;
+}
+
+void op_matrix(const llg_op& op, double m[8]) {
+    std::memset(m, 0, 8 * sizeof(double));
+    const double c = std::cos(0.5 * op.theta), s = std::sin(0.5 * op.theta);
+    const double r = 1.0 / std::sqrt(2.0);
+    switch (op.kind) {
+        case LLG_OP_H: m[0] = r; m[2] = r; m[4] = r; m[6] = -r; break;
+        case LLG_OP_X: m[2] = 1.0; m[4] = 1.0; break;
+        case LLG_OP_RX: m[0] = c; m[3] = -s; m[5] = -s; m[6] = c; break;
+        case LLG_OP_RY: m[0] = c; m[2] = -s; m[4] = s; m[6] = c; break;
+        case LLG_OP_RZ: m[0] = c; m[1] = -s; m[6] = c; m[7] = s; break;
+        default: std::memcpy(m, op.m, 8 * sizeof(double)); break;
+    }
+}
+
+// (a @ b) for row-major interleaved 2x2 complex matrices.
+static void matmul2(const double* a, const double* b, double* out) {
+    double t[8];
+    for (int r = 0; r < 2; ++r)
+        for (int c = 0; c < 2; ++c) {
+            double re = 0.0, im = 0.0;
+            for (int k = 0; k < 2; ++k) {
+                const double ar = a[2 * (2 * r + k)], ai = a[2 * (2 * r + k) + 1];
+                const double br = b[2 * (2 * k + c)], bi = b[2 * (2 * k + c) + 1];
+                re += ar * br - ai * bi;
+                im += ar * bi + ai * br;
+            }
+            t[2 * (2 * r + c)] = re;
+            t[2 * (2 * r + c) + 1] = im;
+        }
+    std::memcpy(out, t, sizeof(t));
+}
+
+static ExecOp blank(int kind) {
+    ExecOp e;
+    std::memset(&e, 0, sizeof(e));
+    e.kind = kind;
+    return e;
+}
+
+// Lower one record with GLOBAL indices.  Validation of qubits/angles is done by the caller.
+bool lower_op(int n, const llg_op& op, int P, std::vector<ExecOp>& out, std::string& err) {
+    (void)n;
+    const double c = std::cos(0.5 * op.theta), s = std::sin(0.5 * op.theta);
+    switch (op.kind) {
+        case LLG_OP_H: {
+            ExecOp e = blank(EX_H);
+            e.q0 = op.q0;
+            e.c[0] = pack_coef(P, 1.0 / std::sqrt(2.0));
+            out.push_back(e);
+            return true;
+        }
+        case LLG_OP_X: {
+            ExecOp e = blank(EX_X);
+            e.q0 = op.q0;
+            out.push_back(e);
+            return true;
+        }
+        case LLG_OP_RX:
+        case LLG_OP_RY: {
+            ExecOp e = blank(op.kind == LLG_OP_RX ? EX_RX : EX_RY);
+            e.q0 = op.q0;
+            e.c[0] = pack_coef(P, c);
+            e.c[1] = pack_coef(P, s);
+            out.push_back(e);
+            return true;
+        }
+        case LLG_OP_RZ: {
+            ExecOp e = blank(EX_DIAG);
+            e.q0 = op.q0;
+            e.c[0] = pack_coef(P, c);
+            e.c[1] = pack_coef(P, -s);
+            e.c[2] = pack_coef(P, c);
+            e.c[3] = pack_coef(P, s);
+            out.push_back(e);
+            return true;
+        }
+        case LLG_OP_U2: {
+            ExecOp e = blank(EX_U2);
+            e.q0 = op.q0;
+            for (int k = 0; k < 8; ++k) e.c[k] = pack_coef(P, op.m[k]);
+            out.push_back(e);
+            return true;
+        }
+        case LLG_OP_CNOT: {
+            ExecOp e = blank(EX_CNOT);
+            e.q0 = op.q0;
+            e.q1 = op.q1;
+            out.push_back(e);
+            return true;
+        }
+        case LLG_OP_CZ: {
+            ExecOp e = blank(EX_MCZ);
+            e.mask = (1ULL << op.q0) | (1ULL << op.q1);
+            out.push_back(e);
+            return true;
+        }
+        case LLG_OP_MCZ: {
+            ExecOp e = blank(EX_MCZ);
+            e.mask = op.mask;
+            out.push_back(e);
+            return true;
+        }
+        default:
+            err = "unknown op kind " + std::to_string(op.kind);
+            return false;
+    }
+}
+
+namespace {
+
+// qubits an op touches, and those it needs inside the tile
+void op_qubits(const llg_op& op, std::vector<int>& touched, std::vector<int>& need) {
+    touched.clear();
+    need.clear();
+    switch (op.kind) {
+        case LLG_OP_RZ: touched.push_back(op.q0); break;
+        case LLG_OP_CNOT:
+            touched.push_back(op.q0);
+            touched.push_back(op.q1);
+            need.push_back(op.q1);
+            break;
+        case LLG_OP_CZ:
+            touched.push_back(op.q0);
+            touched.push_back(op.q1);
+            break;
+        case LLG_OP_MCZ:
+            for (int q = 0; q < 64; ++q)
+                if (op.mask >> q & 1) touched.push_back(q);
+            break;
+        default:
+            touched.push_back(op.q0);
+            need.push_back(op.q0);
+            break;
+    }
+}
+
+struct Pending {
+    bool active = false;
+    bool diag = true;
+    int count = 0;
+    int first = -1;
+    double m[8];
+};
+
+}  // namespace
+
+bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan& out, std::string& err) {
+    out.passes.clear();
+    out.ops.clear();
+    out.source_index.clear();
+    const int t = std::min(n, tile_qubits);
+    // the low qubits are always local; when the register is wider than the tile at least one slot
+    // stays free, so the first remaining op (which needs at most one qubit local) always fits
+    const int low = n > t ? std::min(4, t - 1) : std::min(4, t);
+    if (t < 1 || t > kMaxTileQubits + 1) {
+        err = "tile width out of range";
+        return false;
+    }
+    const uint64_t low_mask = (low >= 64) ? ~0ULL : ((1ULL << low) - 1);
+
+    std::vector<int> remaining(nops);
+    for (int i = 0; i < nops; ++i) remaining[i] = i;
+    std::vector<int> touched, need, deferred, included;
+    std::vector<char> blocked(64, 0);
+
+    while (!remaining.empty()) {
+        uint64_t local = low_mask;
+        int local_count = low;
+        std::fill(blocked.begin(), blocked.end(), 0);
+        deferred.clear();
+        included.clear();
+        for (int idx : remaining) {
+            const llg_op& op = ops[idx];
+            op_qubits(op, touched, need);
+            bool is_blocked = false;
+            for (int q : touched) is_blocked |= blocked[q] != 0;
+            if (!is_blocked) {
+                uint64_t add = 0;
+                for (int q : need)
+                    if (!(local >> q & 1)) add |= 1ULL << q;
+                const int extra = __builtin_popcountll(add);
+                if (local_count + extra <= t) {
+                    local |= add;
+                    local_count += extra;
+                    included.push_back(idx);
+                    continue;
+                }
+            }
+            deferred.push_back(idx);
+            for (int q : touched) blocked[q] = 1;
+        }
+
+        // Fill the local set up to t qubits with the lowest unused positions so every pass has
+        // the same tile width (and therefore the same grid).
+        for (int q = 0; q < n && local_count < t; ++q)
+            if (!(local >> q & 1)) {
+                local |= 1ULL << q;
+                ++local_count;
+            }
+
+        PassDesc pd;
+        std::memset(&pd, 0, sizeof(pd));
+        pd.local_mask = local;
+        pd.t = t;
+        pd.low = low;
+        pd.op_begin = (int)out.ops.size();
+        int to_local[64];
+        for (int q = 0; q < 64; ++q) to_local[q] = -1;
+        {
+            int j = 0, h = 0;
+            for (int q = 0; q < n; ++q)
+                if (local >> q & 1) {
+                    to_local[q] = j++;
+                    if (q >= low) pd.hi_pos[h++] = q;
+                }
+        }
+
+        // Peephole fusion of same-qubit 1-qubit runs, then lowering to local indices.
+        std::vector<Pending> pend(n);
+        auto emit_lowered = [&](const llg_op& gop, int src) -> bool {
+            std::vector<ExecOp> tmp;
+            if (!lower_op(n, gop, P, tmp, err)) return false;
+            for (ExecOp& e : tmp) {
+                switch (e.kind) {
+                    case EX_U2:
+                    case EX_RX:
+                    case EX_RY:
+                    case EX_H:
+                    case EX_X: e.q0 = to_local[e.q0]; break;
+                    case EX_DIAG:
+                        if (to_local[e.q0] >= 0) e.q0 = to_local[e.q0];
+                        else e.flags |= OPF_NONLOCAL_Q0;
+                        break;
+                    case EX_CNOT:
+                        e.q1 = to_local[e.q1];
+                        if (to_local[e.q0] >= 0) e.q0 = to_local[e.q0];
+                        else e.flags |= OPF_NONLOCAL_Q0;
+                        break;
+                    case EX_MCZ: {
+                        uint64_t lm = 0, nl = 0;
+                        for (int q = 0; q < 64; ++q)
+                            if (e.mask >> q & 1) {
+                                if (to_local[q] >= 0) lm |= 1ULL << to_local[q];
+                                else nl |= 1ULL << q;
+                            }
+                        e.mask = lm;
+                        e.nl_mask = nl;
+                        break;
+                    }
+                    default: break;
+                }
+                out.ops.push_back(e);
+                out.source_index.push_back(src);
+            }
+            return true;
+        };
+        auto flush_pending = [&](int q) -> bool {
+            Pending& p = pend[q];
+            if (!p.active) return true;
+            p.active = false;
+            if (p.count == 1) return emit_lowered(ops[p.first], p.first);
+            llg_op u;
+            std::memset(&u, 0, sizeof(u));
+            u.kind = LLG_OP_U2;
+            u.q0 = q;
+            u.param = -1;
+            std::memcpy(u.m, p.m, sizeof(p.m));
+            if (p.diag) {
+                // product of diagonal gates stays diagonal: emit it as a diagonal op so it may act on
+                // a non-local qubit
+                std::vector<ExecOp> tmp;
+                ExecOp e = blank(EX_DIAG);
+                e.q0 = q;
+                e.c[0] = pack_coef(P, p.m[0]);
+                e.c[1] = pack_coef(P, p.m[1]);
+                e.c[2] = pack_coef(P, p.m[6]);
+                e.c[3] = pack_coef(P, p.m[7]);
+                if (to_local[q] >= 0) e.q0 = to_local[q];
+                else e.flags |= OPF_NONLOCAL_Q0;
+                out.ops.push_back(e);
+                out.source_index.push_back(-1);
+                return true;
+            }
+            return emit_lowered(u, -1);
+        };
+
+        for (int idx : included) {
+            const llg_op& op = ops[idx];
+            if (is_single_qubit(op.kind)) {
+                Pending& p = pend[op.q0];
+                double m[8];
+                op_matrix(op, m);
+                if (!p.active) {
+                    p.active = true;
+                    p.diag = op.kind == LLG_OP_RZ;
+                    p.count = 1;
+                    p.first = idx;
+                    std::memcpy(p.m, m, sizeof(m));
+                } else {
+                    matmul2(m, p.m, p.m);  // later gate on the left: g2 @ g1
+                    p.diag = p.diag && op.kind == LLG_OP_RZ;
+                    ++p.count;
+                }
+                continue;
+            }
+            op_qubits(op, touched, need);
+            for (int q : touched)
+                if (!flush_pending(q)) return false;
+            if (!emit_lowered(op, idx)) return false;
+        }
+        for (int q = 0; q < n; ++q)
+            if (!flush_pending(q)) return false;
+
+        pd.nops = (int)out.ops.size() - pd.op_begin;
+        if (included.empty()) {
+            err = "planner made no progress";
+            return false;
+        }
+        out.passes.push_back(pd);
+        remaining.swap(deferred);
+    }
+    return true;
+}
+
+}  // namespace llg

@@ -1,0 +1,271 @@
+"""ctypes binding of libllgpu.so's C ABI (include/llgpu.h).
+
+This is the plain-C view of the engine: the same entry points a cgo/JNI/ctypes caller of the C
+ABI binds.  The pybind11 modules ``quantum_sim_v3`` / ``quantum_sim_v2`` are the reference-
+compatible Python API; this module exists for callers (and tests) that want the C ABI itself,
+and for the batched forms (adjoint gradients, trajectories, mixed-size batches).
+
+Loading fails loudly if the shared library is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Iterable, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libllgpu.so")
+
+# status codes / enums (include/llgpu.h)
+LLG_OK, LLG_EINVAL, LLG_ERUNTIME, LLG_ENOMEM, LLG_ECUDA, LLG_ETIMEOUT = range(6)
+LLG_F64, LLG_DF64, LLG_F32 = 0, 1, 2
+LLG_FUSE_NONE, LLG_FUSE_TILE = 0, 1
+OP_H, OP_X, OP_RX, OP_RY, OP_RZ, OP_CNOT, OP_MCZ, OP_CZ, OP_U2 = range(9)
+
+PRECISIONS = {"fp64": LLG_F64, "complex128": LLG_DF64, "df64": LLG_DF64, "complex64": LLG_F32}
+
+# numpy view of llg_op (96 bytes)
+OP_DTYPE = np.dtype([
+    ("kind", np.int32), ("q0", np.int32), ("q1", np.int32), ("param", np.int32),
+    ("mask", np.uint64), ("theta", np.float64), ("m", np.float64, (8,)),
+])
+assert OP_DTYPE.itemsize == 96
+
+PASS_DTYPE = np.dtype([("local_mask", np.uint64), ("t", np.int32), ("low", np.int32),
+                       ("op_begin", np.int32), ("nops", np.int32)])
+XOP_DTYPE = np.dtype([("kind", np.int32), ("q0", np.int32), ("q1", np.int32), ("flags", np.int32),
+                      ("mask", np.uint64), ("nl_mask", np.uint64), ("c", np.float64, (8,))])
+
+
+class LLGError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is not built; run build_ext.py (there is no CPU fallback)")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i, d, u64, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_uint64, ctypes.c_size_t
+        P = ctypes.POINTER
+        sigs = {
+            "llg_last_error": (ctypes.c_char_p, []),
+            "llg_version": (ctypes.c_char_p, []),
+            "llg_device_count": (i, []),
+            "llg_create": (i, [i, i, P(vp)]),
+            "llg_create_from_host": (i, [vp, sz, i, P(vp)]),
+            "llg_destroy": (i, [vp]),
+            "llg_reset": (i, [vp, i]),
+            "llg_num_qubits": (i, [vp, P(i)]),
+            "llg_size": (i, [vp, P(u64)]),
+            "llg_get_precision": (i, [vp, P(i)]),
+            "llg_set_fusion": (i, [vp, i, i]),
+            "llg_apply_gate": (i, [vp, i, vp]),
+            "llg_h": (i, [vp, i]),
+            "llg_x": (i, [vp, i]),
+            "llg_rx": (i, [vp, i, d]),
+            "llg_ry": (i, [vp, i, d]),
+            "llg_rz": (i, [vp, i, d]),
+            "llg_cnot": (i, [vp, i, i]),
+            "llg_cz": (i, [vp, i, i]),
+            "llg_mcz": (i, [vp, vp, i]),
+            "llg_apply_ops": (i, [vp, vp, i]),
+            "llg_apply_matrix": (i, [vp, i, vp, vp]),
+            "llg_flush": (i, [vp]),
+            "llg_sync": (i, [vp]),
+            "llg_copy_to_host": (i, [vp, vp]),
+            "llg_copy_from_host": (i, [vp, vp]),
+            "llg_probabilities": (i, [vp, vp]),
+            "llg_norm2": (i, [vp, P(d)]),
+            "llg_expect_zz": (i, [vp, i, vp, vp, vp, P(d)]),
+            "llg_renormalize": (i, [vp]),
+            "llg_host_alloc": (vp, [sz]),
+            "llg_host_free": (None, [vp]),
+            "llg_plan_export": (i, [i, vp, i, i, vp, i, P(i), vp, i, P(i)]),
+        }
+        for name, (res, args) in sigs.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    return lib().llg_last_error().decode()
+
+
+def check(rc: int) -> None:
+    if rc == LLG_OK:
+        return
+    msg = last_error()
+    if rc == LLG_EINVAL:
+        raise ValueError(msg)
+    if rc == LLG_ENOMEM:
+        raise MemoryError(msg)
+    raise LLGError(f"[{rc}] {msg}")
+
+
+def device_count() -> int:
+    return lib().llg_device_count()
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+# ---------------------------------------------------------------------------------------------
+# gate records
+# ---------------------------------------------------------------------------------------------
+def make_ops(records: Iterable[tuple]) -> np.ndarray:
+    """Build an llg_op array from tuples (kind, q0, q1, theta[, mask[, m[, param]]])."""
+    recs = list(records)
+    ops = np.zeros(len(recs), dtype=OP_DTYPE)
+    ops["param"] = -1
+    for i, r in enumerate(recs):
+        ops[i]["kind"] = r[0]
+        ops[i]["q0"] = r[1]
+        ops[i]["q1"] = r[2] if len(r) > 2 else 0
+        ops[i]["theta"] = r[3] if len(r) > 3 else 0.0
+        if len(r) > 4 and r[4] is not None:
+            ops[i]["mask"] = r[4]
+        if len(r) > 5 and r[5] is not None:
+            g = np.asarray(r[5], dtype=np.complex128).reshape(4)
+            ops[i]["m"] = np.stack([g.real, g.imag], axis=1).reshape(8)
+        if len(r) > 6 and r[6] is not None:
+            ops[i]["param"] = r[6]
+    return ops
+
+
+def ops_from_fused(fused: Sequence[tuple]) -> np.ndarray:
+    """GateFuser output [(target, [g00, g01, g10, g11]), ...] -> U2 records."""
+    return make_ops([(OP_U2, int(t), 0, 0.0, None, g) for t, g in fused])
+
+
+# ---------------------------------------------------------------------------------------------
+# State: thin object over llg_state*
+# ---------------------------------------------------------------------------------------------
+class State:
+    def __init__(self, n: int | None = None, precision: str = "complex128", amps: np.ndarray | None = None):
+        L = lib()
+        self._h = ctypes.c_void_p()
+        p = PRECISIONS[precision]
+        if amps is not None:
+            a = np.ascontiguousarray(amps, dtype=np.complex128)
+            check(L.llg_create_from_host(_ptr(a), a.size, p, ctypes.byref(self._h)))
+        else:
+            check(L.llg_create(int(n), p, ctypes.byref(self._h)))
+
+    def close(self) -> None:
+        if self._h:
+            lib().llg_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    @property
+    def n(self) -> int:
+        v = ctypes.c_int()
+        check(lib().llg_num_qubits(self._h, ctypes.byref(v)))
+        return v.value
+
+    @property
+    def size(self) -> int:
+        v = ctypes.c_uint64()
+        check(lib().llg_size(self._h, ctypes.byref(v)))
+        return v.value
+
+    def set_fusion(self, mode: str = "tile", tile_qubits: int = 0) -> None:
+        check(lib().llg_set_fusion(self._h, LLG_FUSE_TILE if mode == "tile" else LLG_FUSE_NONE, tile_qubits))
+
+    def apply_gate(self, target: int, gate) -> None:
+        g = np.asarray(gate, dtype=np.complex128).reshape(4)
+        buf = np.ascontiguousarray(np.stack([g.real, g.imag], axis=1).reshape(8))
+        check(lib().llg_apply_gate(self._h, target, _ptr(buf)))
+
+    def h(self, q): check(lib().llg_h(self._h, q))
+    def x(self, q): check(lib().llg_x(self._h, q))
+    def rx(self, q, t): check(lib().llg_rx(self._h, q, t))
+    def ry(self, q, t): check(lib().llg_ry(self._h, q, t))
+    def rz(self, q, t): check(lib().llg_rz(self._h, q, t))
+    def cnot(self, c, t): check(lib().llg_cnot(self._h, c, t))
+    def cz(self, a, b): check(lib().llg_cz(self._h, a, b))
+
+    def mcz(self, qubits: Sequence[int]) -> None:
+        q = np.ascontiguousarray(qubits, dtype=np.int32)
+        check(lib().llg_mcz(self._h, _ptr(q) if q.size else None, q.size))
+
+    def apply_ops(self, ops: np.ndarray) -> None:
+        ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
+        check(lib().llg_apply_ops(self._h, _ptr(ops) if ops.size else None, ops.size))
+
+    def flush(self): check(lib().llg_flush(self._h))
+    def sync(self): check(lib().llg_sync(self._h))
+
+    def state(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.size, dtype=np.complex128)
+        check(lib().llg_copy_to_host(self._h, _ptr(out)))
+        return out
+
+    def load(self, amps: np.ndarray) -> None:
+        a = np.ascontiguousarray(amps, dtype=np.complex128)
+        check(lib().llg_copy_from_host(self._h, _ptr(a)))
+
+    def probabilities(self) -> np.ndarray:
+        out = np.empty(self.size, dtype=np.float64)
+        check(lib().llg_probabilities(self._h, _ptr(out)))
+        return out
+
+    def norm2(self) -> float:
+        v = ctypes.c_double()
+        check(lib().llg_norm2(self._h, ctypes.byref(v)))
+        return v.value
+
+    def expect_zz(self, a: Sequence[int], b: Sequence[int], coeff: Sequence[float]) -> float:
+        aa = np.ascontiguousarray(a, dtype=np.int32)
+        bb = np.ascontiguousarray(b, dtype=np.int32)
+        cc = np.ascontiguousarray(coeff, dtype=np.float64)
+        v = ctypes.c_double()
+        check(lib().llg_expect_zz(self._h, aa.size, _ptr(aa), _ptr(bb), _ptr(cc), ctypes.byref(v)))
+        return v.value
+
+    def renormalize(self) -> None:
+        check(lib().llg_renormalize(self._h))
+
+
+# ---------------------------------------------------------------------------------------------
+# planner introspection (host only)
+# ---------------------------------------------------------------------------------------------
+def plan_export(n: int, ops: np.ndarray, tile_qubits: int):
+    ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
+    npasses, nx = ctypes.c_int(), ctypes.c_int()
+    check(lib().llg_plan_export(n, _ptr(ops) if ops.size else None, ops.size, tile_qubits, None, 0,
+                                ctypes.byref(npasses), None, 0, ctypes.byref(nx)))
+    passes = np.zeros(npasses.value, dtype=PASS_DTYPE)
+    xops = np.zeros(max(nx.value, 1), dtype=XOP_DTYPE)
+    check(lib().llg_plan_export(n, _ptr(ops) if ops.size else None, ops.size, tile_qubits, _ptr(passes),
+                                passes.size, ctypes.byref(npasses), _ptr(xops), xops.size, ctypes.byref(nx)))
+    return passes, xops[: nx.value]
+
+
+def ring_zz_terms(n: int):
+    """Observable sum_i Z_i Z_{i+1 mod n} as (a, b, coeff) lists."""
+    a = list(range(n))
+    b = [(i + 1) % n for i in range(n)]
+    return a, b, [1.0] * n
+

@@ -1,0 +1,168 @@
+"""ctypes loader for the ORACLE (oracle/_build/liboracle.so) -- test infrastructure only.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference legs may import
+this module; it is the checker, never the thing shipped or measured as the GPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:
+    sys.path.insert(0, HERE)
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        import build_oracle  # noqa: E402  (same directory)
+
+        path = build_oracle.build_oracle()
+        L = ctypes.CDLL(path)
+        vp, i, d, u64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_uint64
+        P = ctypes.POINTER
+        sigs = {
+            "orc_set_threads": (None, [i]),
+            "orc_max_threads": (i, []),
+            "orc_init_zero": (None, [vp, i]),
+            "orc_apply_gate_v3": (None, [vp, i, i, vp]),
+            "orc_apply_gate_standard": (None, [vp, i, i, vp]),
+            "orc_run_ops": (i, [vp, i, vp, i]),
+            "orc_apply_op": (i, [vp, i, vp]),
+            "orc_probabilities": (None, [vp, i, vp]),
+            "orc_apply_matrix": (i, [vp, i, i, vp, vp]),
+            "orc_expect_zz": (d, [vp, i, i, vp, vp, vp]),
+            "orc_norm2": (d, [vp, i]),
+            "orc_philox4x32_10": (None, [vp, vp, vp]),
+            "orc_uniform_pair": (None, [u64, u64, u64, P(d), P(d)]),
+            "orc_traj_run": (i, [i, vp, i, d, d, u64, u64, u64, vp, vp, vp, ctypes.c_int64, P(d)]),
+            "orc_density_z0": (i, [i, vp, i, d, d, P(d)]),
+            "orc_param_shift": (i, [i, vp, i, vp, i, i, vp, vp, vp, P(d), vp]),
+        }
+        for name, (res, args) in sigs.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+def set_threads(t: int) -> None:
+    lib().orc_set_threads(int(t))
+
+
+def max_threads() -> int:
+    return lib().orc_max_threads()
+
+
+def zero_state(n: int) -> np.ndarray:
+    s = np.zeros(1 << n, dtype=np.complex128)
+    s[0] = 1.0
+    return s
+
+
+def run_ops(n: int, ops: np.ndarray, state: np.ndarray | None = None) -> np.ndarray:
+    psi = zero_state(n) if state is None else np.array(state, dtype=np.complex128, copy=True)
+    ops = np.ascontiguousarray(ops)
+    rc = lib().orc_run_ops(_p(psi), n, _p(ops) if ops.size else None, ops.size)
+    if rc:
+        raise ValueError(f"oracle rejected the op list (rc={rc})")
+    return psi
+
+
+def apply_gate_v3(psi: np.ndarray, n: int, target: int, gate) -> None:
+    g = np.asarray(gate, dtype=np.complex128).reshape(4)
+    buf = np.ascontiguousarray(np.stack([g.real, g.imag], axis=1).reshape(8))
+    lib().orc_apply_gate_v3(_p(psi), n, target, _p(buf))
+
+
+def apply_gate_standard(psi: np.ndarray, n: int, target: int, gate) -> None:
+    g = np.asarray(gate, dtype=np.complex128).reshape(4)
+    buf = np.ascontiguousarray(np.stack([g.real, g.imag], axis=1).reshape(8))
+    lib().orc_apply_gate_standard(_p(psi), n, target, _p(buf))
+
+
+def probabilities(psi: np.ndarray, n: int) -> np.ndarray:
+    out = np.empty(1 << n, dtype=np.float64)
+    lib().orc_probabilities(_p(psi), n, _p(out))
+    return out
+
+
+def apply_matrix(psi: np.ndarray, n: int, qubits, m: np.ndarray) -> None:
+    qs = np.ascontiguousarray(qubits, dtype=np.int32)
+    mm = np.ascontiguousarray(np.asarray(m, dtype=np.complex128))
+    rc = lib().orc_apply_matrix(_p(psi), n, qs.size, _p(qs), _p(mm))
+    if rc:
+        raise ValueError("oracle apply_matrix rejected its arguments")
+
+
+def expect_zz(psi: np.ndarray, n: int, a, b, coeff) -> float:
+    aa = np.ascontiguousarray(a, dtype=np.int32)
+    bb = np.ascontiguousarray(b, dtype=np.int32)
+    cc = np.ascontiguousarray(coeff, dtype=np.float64)
+    return lib().orc_expect_zz(_p(psi), n, aa.size, _p(aa), _p(bb), _p(cc))
+
+
+def philox(ctr, key) -> np.ndarray:
+    c = np.ascontiguousarray(ctr, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    out = np.zeros(4, dtype=np.uint32)
+    lib().orc_philox4x32_10(_p(c), _p(k), _p(out))
+    return out
+
+
+def uniform_pair(seed: int, traj: int, site: int) -> tuple[float, float]:
+    u1, u2 = ctypes.c_double(), ctypes.c_double()
+    lib().orc_uniform_pair(seed, traj, site, ctypes.byref(u1), ctypes.byref(u2))
+    return u1.value, u2.value
+
+
+def traj_run(n: int, ops: np.ndarray, gamma: float, lam: float, seed: int, begin: int, end: int,
+             log_sites: int = 0):
+    """Returns (z0[end-begin], jumps[end-begin], log or None, min margin)."""
+    cnt = end - begin
+    z0 = np.zeros(cnt, dtype=np.float64)
+    jumps = np.zeros(cnt, dtype=np.uint32)
+    log = np.zeros((cnt, log_sites), dtype=np.uint8) if log_sites else None
+    margin = ctypes.c_double()
+    ops = np.ascontiguousarray(ops)
+    rc = lib().orc_traj_run(n, _p(ops), ops.size, gamma, lam, seed, begin, end, _p(z0), _p(jumps),
+                            _p(log) if log is not None else None, log_sites, ctypes.byref(margin))
+    if rc:
+        raise ValueError(f"oracle trajectory run failed (rc={rc})")
+    return z0, jumps, log, margin.value
+
+
+def density_z0(n: int, ops: np.ndarray, gamma: float, lam: float) -> float:
+    out = ctypes.c_double()
+    ops = np.ascontiguousarray(ops)
+    rc = lib().orc_density_z0(n, _p(ops), ops.size, gamma, lam, ctypes.byref(out))
+    if rc:
+        raise ValueError("oracle density evolution failed")
+    return out.value
+
+
+def param_shift(n: int, ops: np.ndarray, params: np.ndarray, a, b, coeff):
+    """(energy, gradient) by the parameter-shift rule on the oracle state vector."""
+    ops = np.ascontiguousarray(ops)
+    pr = np.ascontiguousarray(params, dtype=np.float64)
+    aa = np.ascontiguousarray(a, dtype=np.int32)
+    bb = np.ascontiguousarray(b, dtype=np.int32)
+    cc = np.ascontiguousarray(coeff, dtype=np.float64)
+    e = ctypes.c_double()
+    g = np.zeros(pr.size, dtype=np.float64)
+    rc = lib().orc_param_shift(n, _p(ops), ops.size, _p(pr), pr.size, aa.size, _p(aa), _p(bb), _p(cc),
+                               ctypes.byref(e), _p(g))
+    if rc:
+        raise ValueError(f"oracle parameter shift failed (rc={rc})")
+    return e.value, g

@@ -1,0 +1,169 @@
+// ref_capi.cpp -- C entry points over the REFERENCE's own header-only C++ backends, used only to
+// pin the oracle and to write golden fixtures (test infrastructure; never part of the product).
+//
+// Built by oracle/build_oracle.py with -I<reference>/src into oracle/_ref/libref.so, directly
+// from the reference's headers where they lie: src/Backend.h (ReferenceBackend),
+// src/StateVectorBackend.h (StateVectorBackend) and src/Algorithms.h (Grover, VQE::prepare).
+// Nothing from the reference is copied here; this file only drives its classes.
+
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <random>
+#include <stdexcept>
+#include <vector>
+
+#include "Algorithms.h"
+#include "Backend.h"
+#include "StateVectorBackend.h"
+
+#include "sv_oracle.h"
+
+namespace {
+
+int run_on(ll::Backend& be, int n, const orc_op* ops, int nops) {
+    be.reset(n);
+    for (int i = 0; i < nops; ++i) {
+        const orc_op& op = ops[i];
+        switch (op.kind) {
+            case ORC_OP_H: be.h(op.q0); break;
+            case ORC_OP_X: be.x(op.q0); break;
+            case ORC_OP_RX: be.rx(op.q0, op.theta); break;
+            case ORC_OP_RY: be.ry(op.q0, op.theta); break;
+            case ORC_OP_RZ: be.rz(op.q0, op.theta); break;
+            case ORC_OP_CNOT: be.cnot(op.q0, op.q1); break;
+            case ORC_OP_CZ: be.mcz({op.q0, op.q1}); break;
+            case ORC_OP_MCZ: {
+                std::vector<int> qs;
+                for (int q = 0; q < 64; ++q)
+                    if (op.mask >> q & 1) qs.push_back(q);
+                be.mcz(qs);
+                break;
+            }
+            default: throw std::invalid_argument("ref_capi: op kind has no ll::Backend call");
+        }
+    }
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// backend: 0 = ll::ReferenceBackend, 1 = ll::StateVectorBackend.  out: 2*2^n doubles.
+// Returns 0, 1 for std::invalid_argument, 2 for any other exception.
+int ref_run_ops(int backend, int n, const orc_op* ops, int nops, double* out) {
+    try {
+        std::vector<std::complex<double>> s;
+        if (backend == 0) {
+            ll::ReferenceBackend be(1);
+            run_on(be, n, ops, nops);
+            s = be.state();
+        } else {
+            ll::StateVectorBackend be(1);
+            run_on(be, n, ops, nops);
+            s = be.state();
+        }
+        std::memcpy(out, s.data(), s.size() * sizeof(std::complex<double>));
+        return 0;
+    } catch (const std::invalid_argument&) {
+        return 1;
+    } catch (...) {
+        return 2;
+    }
+}
+
+// Probabilities through the backend's own probabilities() (StateVectorBackend.h:153-161).
+int ref_probabilities(int backend, int n, const orc_op* ops, int nops, double* out) {
+    try {
+        std::vector<double> p;
+        if (backend == 0) {
+            ll::ReferenceBackend be(1);
+            run_on(be, n, ops, nops);
+            p = be.probabilities();
+        } else {
+            ll::StateVectorBackend be(1);
+            run_on(be, n, ops, nops);
+            p = be.probabilities();
+        }
+        std::memcpy(out, p.data(), p.size() * sizeof(double));
+        return 0;
+    } catch (const std::invalid_argument&) {
+        return 1;
+    } catch (...) {
+        return 2;
+    }
+}
+
+// The reference's random-circuit recipe (tests/test_backends.cpp:85-103) driven from one
+// mt19937_64 stream: draws happen in the order kind, qubit a, angle, then b (cnot) or the coin
+// flips (mcz).  Writes up to cap ops; returns the count.  rng_state carries the engine across
+// calls so successive circuits continue the same stream, as the reference's test loop does.
+struct RefRng {
+    std::mt19937_64 rng;
+};
+
+void* ref_rng_new(uint64_t seed) { return new RefRng{std::mt19937_64(seed)}; }
+void ref_rng_free(void* r) { delete static_cast<RefRng*>(r); }
+
+int ref_random_circuit(void* r, int n, int depth, orc_op* out) {
+    std::mt19937_64& rng = static_cast<RefRng*>(r)->rng;
+    std::uniform_int_distribution<int> qd(0, n - 1);
+    std::uniform_int_distribution<int> kd(0, n >= 2 ? 6 : 4);
+    std::uniform_real_distribution<double> ang(-3.2, 3.2);
+    std::bernoulli_distribution coin(0.5);
+    for (int d = 0; d < depth; ++d) {
+        orc_op op;
+        std::memset(&op, 0, sizeof(op));
+        op.param = -1;
+        op.kind = kd(rng);
+        op.q0 = qd(rng);
+        op.theta = ang(rng);
+        if (op.kind == 5) {
+            do op.q1 = qd(rng);
+            while (op.q1 == op.q0);
+        } else if (op.kind == 6) {
+            for (int q = 0; q < n; ++q)
+                if (coin(rng)) op.mask |= 1ULL << q;
+            if (op.mask == 0) op.mask = 1ULL << op.q0;
+        }
+        out[d] = op;
+    }
+    return depth;
+}
+
+// ll::Grover::run on StateVectorBackend (Algorithms.h:62-101).
+int ref_grover(int n, const int* marked, int nmarked, int iterations, double* probs, int* marked_index, int* iters) {
+    try {
+        ll::StateVectorBackend be(1);
+        std::vector<int> m(marked, marked + nmarked);
+        ll::GroverResult res = ll::Grover::run(be, n, m, iterations);
+        std::memcpy(probs, res.probabilities.data(), res.probabilities.size() * sizeof(double));
+        *marked_index = res.marked_index;
+        *iters = res.iterations;
+        return 0;
+    } catch (const std::invalid_argument&) {
+        return 1;
+    } catch (...) {
+        return 2;
+    }
+}
+
+// ll::VQE::prepare (Algorithms.h:240-252) on StateVectorBackend: RY layer + CNOT ring per layer.
+int ref_vqe_prepare(int n, int layers, const double* params, double* out_state) {
+    try {
+        ll::VQE vqe(n, layers);
+        ll::StateVectorBackend be(1);
+        std::vector<double> p(params, params + vqe.n_params());
+        vqe.prepare(be, p);
+        const auto s = be.state();
+        std::memcpy(out_state, s.data(), s.size() * sizeof(std::complex<double>));
+        return 0;
+    } catch (const std::invalid_argument&) {
+        return 1;
+    } catch (...) {
+        return 2;
+    }
+}
+
+}  // extern "C"

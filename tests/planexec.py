@@ -1,0 +1,81 @@
+"""numpy executor for exported tile plans (llg_plan_export): runs each pass over all tiles at
+once, so the CPU tests can check the planner's output against the oracle without a GPU."""
+from __future__ import annotations
+
+import numpy as np
+
+
+def _matrix(x) -> np.ndarray:
+    k, c = int(x["kind"]), x["c"]
+    if k == 0:
+        return np.array([[c[0] + 1j * c[1], c[2] + 1j * c[3]], [c[4] + 1j * c[5], c[6] + 1j * c[7]]])
+    if k == 1:
+        return np.array([[c[0], -1j * c[1]], [-1j * c[1], c[0]]])
+    if k == 2:
+        return np.array([[c[0], -c[1]], [c[1], c[0]]], dtype=complex)
+    if k == 3:
+        return np.array([[c[0], c[0]], [c[0], -c[0]]], dtype=complex)
+    return np.array([[0, 1], [1, 0]], dtype=complex)
+
+
+def _pair(tile: np.ndarray, q: int, m: np.ndarray) -> None:
+    nt, size = tile.shape
+    v = tile.reshape(nt, size >> (q + 1), 2, 1 << q)
+    a0, a1 = v[:, :, 0, :].copy(), v[:, :, 1, :].copy()
+    v[:, :, 0, :] = m[0, 0] * a0 + m[0, 1] * a1
+    v[:, :, 1, :] = m[1, 0] * a0 + m[1, 1] * a1
+
+
+def execute(psi: np.ndarray, n: int, passes: np.ndarray, xops: np.ndarray) -> np.ndarray:
+    psi = psi.copy()
+    for p in passes:
+        lm = int(p["local_mask"])
+        t = int(p["t"])
+        local = [q for q in range(n) if lm >> q & 1]
+        assert len(local) == t
+        nonlocal_q = [q for q in range(n) if not lm >> q & 1]
+        bases = np.zeros(1 << (n - t), dtype=np.int64)
+        for j, q in enumerate(nonlocal_q):
+            bases |= ((np.arange(1 << (n - t)) >> j) & 1) << q
+        offs = np.zeros(1 << t, dtype=np.int64)
+        for j, q in enumerate(local):
+            offs |= ((np.arange(1 << t) >> j) & 1) << q
+        idx = bases[:, None] | offs[None, :]
+        tile = psi[idx]
+        lidx = np.arange(1 << t)
+        for x in xops[p["op_begin"]:p["op_begin"] + p["nops"]]:
+            k, q0, q1, fl = int(x["kind"]), int(x["q0"]), int(x["q1"]), int(x["flags"])
+            if k <= 4:
+                _pair(tile, q0, _matrix(x))
+            elif k == 5:
+                c = x["c"]
+                d0, d1 = c[0] + 1j * c[1], c[2] + 1j * c[3]
+                if fl & 1:
+                    sel = ((bases >> q0) & 1).astype(bool)
+                    tile[sel] *= d1
+                    tile[~sel] *= d0
+                else:
+                    bit = ((lidx >> q0) & 1).astype(bool)
+                    tile[:, bit] *= d1
+                    tile[:, ~bit] *= d0
+            elif k == 6:
+                if fl & 1:
+                    sel = ((bases >> q0) & 1).astype(bool)
+                    sub = tile[sel]
+                    _pair(sub, q1, _matrix({"kind": 4, "c": x["c"]}))
+                    tile[sel] = sub
+                else:
+                    src = lidx[(((lidx >> q0) & 1) == 1) & (((lidx >> q1) & 1) == 0)]
+                    dst = src | (1 << q1)
+                    tmp = tile[:, src].copy()
+                    tile[:, src] = tile[:, dst]
+                    tile[:, dst] = tmp
+            elif k == 7:
+                nl, lmk = int(x["nl_mask"]), int(x["mask"])
+                rows = (bases & nl) == nl
+                cols = (lidx & lmk) == lmk
+                tile[np.ix_(rows, cols)] *= -1
+            else:
+                raise AssertionError(f"unknown executor op {k}")
+        psi[idx] = tile
+    return psi

@@ -1,0 +1,120 @@
+"""The C ABI boundary without a GPU: the library loads, exports every symbol include/*.h
+declares, fails loudly (no CPU fallback) when no device exists, validates arguments with the
+reference's error contract, and its fusion planner computes the same state as the oracle."""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import llgpu
+import oracle
+import workloads
+from conftest import REPO, split
+from llgpu import OP_CNOT, OP_CZ, OP_DTYPE, OP_H, OP_MCZ, OP_RX, OP_RY, OP_RZ, OP_U2, OP_X, make_ops
+from planexec import execute
+
+
+def header_symbols():
+    names = set()
+    inc = os.path.join(REPO, "include")
+    for f in os.listdir(inc):
+        if f.endswith(".h"):
+            src = open(os.path.join(inc, f)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"^\s*(?:const\s+)?[\w\*]+[\s\*]+(llg_\w+)\s*\(", src, flags=re.M))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol(built):
+    L = ctypes.CDLL(llgpu.LIB_PATH)
+    names = header_symbols()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_no_gpu_means_loud_failure(built):
+    if llgpu.device_count() > 0:
+        pytest.skip("a GPU is present")
+    with pytest.raises(llgpu.LLGError, match="cuda|CUDA|driver"):
+        llgpu.State(4)
+    import quantum_sim_v3
+
+    with pytest.raises(RuntimeError):
+        quantum_sim_v3.StateVector(4)
+
+
+def test_plan_export_validates_like_the_reference(built):
+    bad = [(OP_H, -1), (OP_X, 3), (OP_RX, 0, 0, float("nan")), (OP_RY, 0, 0, float("inf")), (OP_RZ, 5, 0, 0.1),
+           (OP_CNOT, 1, 1), (OP_CNOT, 0, 3), (OP_MCZ, 0, 0, 0.0, 0), (OP_MCZ, 0, 0, 0.0, 0b10001), (OP_CZ, 2, 2)]
+    for rec in bad:
+        with pytest.raises(ValueError):
+            llgpu.plan_export(3, make_ops([rec]), 3)
+
+
+def random_ops(n, depth, rng):
+    recs = []
+    for _ in range(depth):
+        k = rng.integers(10)
+        q = int(rng.integers(n))
+        if k == 0:
+            recs.append((OP_H, q))
+        elif k == 1:
+            recs.append((OP_X, q))
+        elif k in (2, 3, 4):
+            recs.append(((OP_RX, OP_RY, OP_RZ)[k - 2], q, 0, float(rng.uniform(-3.2, 3.2))))
+        elif k in (5, 6):
+            a, b = rng.choice(n, 2, replace=False)
+            recs.append(((OP_CNOT, OP_CZ)[k - 5], int(a), int(b)))
+        elif k == 7:
+            mask = int(rng.integers(1, 1 << n))
+            recs.append((OP_MCZ, 0, 0, 0.0, mask))
+        else:
+            u, _ = np.linalg.qr(rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2)))
+            recs.append((OP_U2, q, 0, 0.0, None, u.reshape(4)))
+    return make_ops(recs)
+
+
+@pytest.mark.parametrize("n,tile", [(6, 5), (8, 5), (9, 6), (10, 7), (11, 5)])
+def test_planned_passes_reproduce_the_oracle(built, n, tile):
+    rng = np.random.default_rng(100 + n)
+    ops = random_ops(n, 300, rng)
+    passes, xops = llgpu.plan_export(n, ops, tile)
+    if n > tile:
+        assert len(passes) > 1
+    got = execute(oracle.zero_state(n), n, passes, xops)
+    want = oracle.run_ops(n, ops)
+    assert np.max(np.abs(got - want)) < 1e-12
+
+
+def test_plan_of_layered_circuit(built, golden):
+    g = golden("config2_layered")
+    for n, ops in zip(g["n"], split(g["ops"], g["offsets"])):
+        n = int(n)
+        passes, xops = llgpu.plan_export(n, ops, 5)
+        got = execute(oracle.zero_state(n), n, passes, xops)
+        assert np.max(np.abs(got - oracle.run_ops(n, ops))) < 1e-12
+        # fewer passes than gates: runs of rotations share a pass
+        assert len(passes) < len(ops) / 4
+
+
+def test_plan_of_random_2024_circuits(built, golden):
+    g = golden("random_2024")
+    for n, ops in zip(g["n"], split(g["ops"], g["offsets"])):
+        n = int(n)
+        passes, xops = llgpu.plan_export(n, ops, 3)
+        got = execute(oracle.zero_state(n), n, passes, xops)
+        assert np.max(np.abs(got - oracle.run_ops(n, ops))) < 1e-12
+
+
+def test_thirty_qubit_plan_is_compact(built):
+    ops = workloads.layered_rotations(30, layers=20)
+    passes, xops = llgpu.plan_export(30, ops, 12)
+    # every pass holds the 4 low qubits plus at most 8 more
+    assert all(bin(int(p["local_mask"])).count("1") == 12 for p in passes)
+    assert all(int(p["local_mask"]) & 0xF == 0xF for p in passes)
+    assert len(passes) < 60

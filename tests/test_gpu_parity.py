@@ -1,0 +1,222 @@
+"""GPU parity: the CUDA engine against the oracle and the reference's own outputs (golden
+fixtures), through the C ABI (llgpu) and the drop-in pybind11 modules.
+
+Tolerances: complex128 (double-float) and fp64 states <= 1e-12 max |amplitude difference|, the
+spec bar; complex64 states <= 5e-5 (fp32 rounding over a few hundred gates)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import llgpu
+import oracle
+import workloads
+from conftest import split, split_states
+from llgpu import OP_CNOT, OP_CZ, OP_H, OP_MCZ, OP_RX, OP_RY, OP_RZ, OP_U2, OP_X, make_ops
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"complex128": 1e-12, "fp64": 1e-12, "complex64": 5e-5}
+PRECISIONS = ["complex128", "fp64", "complex64"]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built(built):
+    assert llgpu.device_count() > 0, "no CUDA device visible"
+
+
+def run_gpu(n, ops, precision="complex128", fusion="tile", tile=0, init=None):
+    st = llgpu.State(n, precision) if init is None else llgpu.State(precision=precision, amps=init)
+    st.set_fusion(fusion, tile)
+    st.apply_ops(ops)
+    out = st.state()
+    st.close()
+    return out
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("fusion", ["tile", "none"])
+def test_random_2024_circuits(golden, precision, fusion):
+    g = golden("random_2024")
+    worst = 0.0
+    for n, ops, ref in zip(g["n"], split(g["ops"], g["offsets"]), split_states(g["ref_states"], g["state_offsets"])):
+        got = run_gpu(int(n), ops, precision, fusion)
+        worst = max(worst, float(np.max(np.abs(got - ref))))
+    assert worst <= TOL[precision], worst
+
+
+@pytest.mark.parametrize("tile", [5, 8, 12])
+def test_config2_layered_fixture(golden, tile):
+    g = golden("config2_layered")
+    for n, ops, ref in zip(g["n"], split(g["ops"], g["offsets"]), split_states(g["states"], g["state_offsets"])):
+        got = run_gpu(int(n), ops, "complex128", "tile", tile)
+        assert np.max(np.abs(got - ref)) <= 1e-12
+
+
+def test_config1_through_drop_in(golden):
+    import quantum_sim_v3
+
+    g = golden("config1_h_cnot")
+    for n, ops, ref in zip(g["n"], split(g["ops"], g["offsets"]), split_states(g["states"], g["state_offsets"])):
+        sv = quantum_sim_v3.StateVector(int(n))
+        for op in ops:
+            if op["kind"] == OP_H:
+                sv.h(int(op["q0"]))
+            else:
+                sv.cnot(int(op["q0"]), int(op["q1"]))
+        got = np.array(sv.get_numpy_view(), copy=True)
+        assert np.max(np.abs(got - ref)) <= 1e-12
+
+
+def test_v3_and_v2_gate_semantics(golden):
+    import quantum_sim_v2
+    import quantum_sim_v3
+
+    g = golden("v3_gates")
+    n = int(g["n"])
+    for label, mod, meth in (("v3_cache", quantum_sim_v3, "apply_gate_cache_optimized"),
+                             ("v3_standard", quantum_sim_v3, "apply_gate_standard"),
+                             ("v2", quantum_sim_v2, "apply_gate")):
+        buf = g["init"].copy()
+        sv = mod.StateVector(buf)
+        for t, gate in zip(g["targets"], g["gates"]):
+            if t >= n and label != "v3_cache":
+                continue  # the reference's mask-scan variants corrupt memory there
+            getattr(sv, meth)(int(t), [complex(x) for x in gate])  # list of 4, as the reference takes
+        view = sv.get_numpy_view()
+        assert view.base is sv
+        assert np.max(np.abs(view - g[label])) <= 1e-12
+        assert np.max(np.abs(buf - g[label])) <= 1e-12  # caller's array updated at the sync point
+    # |0..0> constructor
+    sv = quantum_sim_v3.StateVector(5)
+    h = 1 / np.sqrt(2)
+    sv.apply_gate_cache_optimized(0, [h, h, h, -h])
+    sv.apply_gate_cache_optimized(4, np.array([0, 1, 1, 0], dtype=complex))  # numpy gates accepted too
+    assert np.max(np.abs(sv.get_numpy_view() - g["ctor5_view"])) <= 1e-15
+    assert sv.get_num_qubits() == 5 and sv.get_size() == 32
+
+
+def test_drop_in_error_contract():
+    import quantum_sim_v3
+
+    sv = quantum_sim_v3.StateVector(3)
+    for call in (lambda: sv.h(-1), lambda: sv.x(3), lambda: sv.rx(0, float("nan")), lambda: sv.ry(0, float("inf")),
+                 lambda: sv.rz(5, 0.1), lambda: sv.cnot(1, 1), lambda: sv.cnot(0, 3), lambda: sv.mcz([]),
+                 lambda: sv.mcz([0, 0]), lambda: sv.mcz([0, 4]), lambda: sv.cz(1, 1),
+                 lambda: sv.apply_gate_cache_optimized(-1, [1, 0, 0, 1])):
+        with pytest.raises(ValueError):
+            call()
+    assert sv.get_num_qubits() == 3
+    sv.apply_gate_cache_optimized(7, [0, 1, 1, 0])  # target >= n: a no-op, as in the reference
+    v = sv.get_numpy_view()
+    assert v[0] == 1 and np.all(v[1:] == 0)
+    with pytest.raises(RuntimeError, match="power of 2"):
+        quantum_sim_v3.StateVector(np.zeros(6, dtype=np.complex128))
+    with pytest.raises(TypeError):
+        quantum_sim_v3.StateVector(np.zeros(8, dtype=np.float64))
+
+
+def test_closed_forms_on_gpu():
+    import quantum_sim_v3 as q
+
+    r = 1 / np.sqrt(2)
+    for precision in PRECISIONS:
+        tol = 1e-14 if precision != "complex64" else 1e-6
+        sv = q.StateVector(4, precision)
+        sv.x(2)
+        assert sv.probabilities()[4] > 1 - tol
+        sv = q.StateVector(2, precision)
+        sv.h(0)
+        sv.cnot(0, 1)
+        p = sv.probabilities()
+        assert abs(p[0] - 0.5) < tol and abs(p[3] - 0.5) < tol
+        sv = q.StateVector(3, precision)
+        sv.x(2)
+        sv.cnot(2, 0)
+        assert sv.probabilities()[5] > 1 - tol
+        sv = q.StateVector(1, precision)
+        sv.rx(0, np.pi)
+        assert abs(sv.get_numpy_view()[1] - (-1j)) < tol
+        sv = q.StateVector(1, precision)
+        sv.h(0)
+        sv.rz(0, 0.7)
+        s = sv.get_numpy_view()
+        assert abs(s[0] - r * np.exp(-0.35j)) < tol and abs(s[1] - r * np.exp(0.35j)) < tol
+        sv = q.StateVector(3, precision)
+        for k in range(3):
+            sv.h(k)
+        sv.mcz([0, 1, 2])
+        m = sv.get_numpy_view()
+        assert abs(m[7] + r ** 3) < tol and np.all(np.abs(m[:7] - r ** 3) < tol)
+
+
+def test_grover_on_gpu(golden):
+    import quantum_sim_v3
+
+    from test_oracle_golden import grover_ops
+
+    g = golden("grover")
+    for key, n in (("n8_m85", 8), ("n10_i10", 10), ("n12_i10", 12)):
+        sv = quantum_sim_v3.StateVector(n)
+        sv.apply_ops(grover_ops(n, g[key + "_marked"].tolist(), int(g[key + "_iterations"])))
+        assert np.max(np.abs(sv.probabilities() - g[key + "_probs"])) <= 1e-12
+    assert abs(quantum_sim_v3.StateVector(8).probabilities()[0] - 1.0) == 0.0
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_readouts_match_oracle(precision):
+    rng = np.random.default_rng(3)
+    for n in (7, 12, 16):
+        psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+        psi /= np.linalg.norm(psi)
+        st = llgpu.State(precision=precision, amps=psi)
+        tol = 1e-12 if precision != "complex64" else 1e-6
+        assert np.max(np.abs(st.probabilities() - oracle.probabilities(psi, n))) <= tol
+        assert abs(st.norm2() - 1.0) <= tol
+        a, b, c = llgpu.ring_zz_terms(n)
+        a = a + [0, 3]
+        b = b + [-1, -1]
+        c = c + [0.5, -0.25]
+        assert abs(st.expect_zz(a, b, c) - oracle.expect_zz(psi, n, a, b, c)) <= 20 * tol
+        st.close()
+
+
+@pytest.mark.parametrize("precision", ["complex128", "fp64"])
+def test_every_gate_kind_both_paths(precision):
+    rng = np.random.default_rng(8)
+    n = 13
+    recs = []
+    for _ in range(400):
+        k = rng.integers(9)
+        q = int(rng.integers(n))
+        if k == 0:
+            recs.append((OP_H, q))
+        elif k == 1:
+            recs.append((OP_X, q))
+        elif k < 5:
+            recs.append(((OP_RX, OP_RY, OP_RZ)[k - 2], q, 0, float(rng.uniform(0, 2 * np.pi))))
+        elif k < 7:
+            a, b = rng.choice(n, 2, replace=False)
+            recs.append(((OP_CNOT, OP_CZ)[k - 5], int(a), int(b)))
+        elif k == 7:
+            recs.append((OP_MCZ, 0, 0, 0.0, int(rng.integers(1, 1 << n))))
+        else:
+            u, _ = np.linalg.qr(rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2)))
+            recs.append((OP_U2, q, 0, 0.0, None, u.reshape(4)))
+    ops = make_ops(recs)
+    want = oracle.run_ops(n, ops)
+    for fusion, tile in (("none", 0), ("tile", 5), ("tile", 9), ("tile", 12)):
+        got = run_gpu(n, ops, precision, fusion, tile)
+        assert np.max(np.abs(got - want)) <= 1e-12, (fusion, tile)
+
+
+def test_twenty_qubit_layered_vs_oracle():
+    n = 20
+    ops = workloads.layered_rotations(n, layers=4, seed=12)
+    want = oracle.run_ops(n, ops)
+    for fusion in ("tile", "none"):
+        got = run_gpu(n, ops, "complex128", fusion)
+        assert np.max(np.abs(got - want)) <= 1e-12
+    got = run_gpu(n, ops, "complex64", "tile")
+    fid = abs(np.vdot(want, got)) ** 2
+    assert 1 - fid < 1e-9
