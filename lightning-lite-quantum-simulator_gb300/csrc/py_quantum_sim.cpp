@@ -92,6 +92,7 @@ public:
             throw py::type_error("StateVector(ndarray) needs a 1-D C-contiguous complex128 array");
         if (arr.ndim() != 1) throw std::runtime_error("NumPy array must be 1-dimensional");
         user_ = arr;
+        has_user_ = true;
         const size_t len = (size_t)arr.shape(0);
         const double* data = static_cast<const double*>(arr.data());
         int rc;
@@ -103,7 +104,7 @@ public:
     }
 
     ~StateVector() {
-        if (st_ && user_) {
+        if (st_ && has_user_) {
             try {
                 writeback();
             } catch (...) {
@@ -192,7 +193,7 @@ public:
             rc = llg_sync(st_);
         }
         check(rc);
-        if (user_) writeback();
+        if (has_user_) writeback();
         else if (mirror_) {
             py::gil_scoped_release nogil;
             rc = llg_copy_to_host(st_, mirror_);
@@ -202,7 +203,7 @@ public:
 
     // Upload the host buffer (the caller's array, or the get_numpy_view mirror) to the GPU.
     void push() {
-        const double* src = user_ ? static_cast<const double*>(user_.data()) : mirror_;
+        const double* src = has_user_ ? static_cast<const double*>(user_.data()) : mirror_;
         if (!src) throw std::runtime_error("push: no host buffer (call get_numpy_view first)");
         int rc;
         {
@@ -265,7 +266,7 @@ public:
 
 private:
     double* host_buffer() {
-        if (user_) return static_cast<double*>(user_.mutable_data());
+        if (has_user_) return static_cast<double*>(user_.mutable_data());
         const size_t bytes = (size_t)size() * 16;
         if (!mirror_) {
             mirror_ = static_cast<double*>(llg_host_alloc(bytes));
@@ -285,7 +286,10 @@ private:
     }
 
     llg_state* st_ = nullptr;
+    // The caller's array for the ndarray constructor.  A default py::array is an empty array, not a
+    // null handle, so `has_user_` (not the handle) says whether there is one.
     py::array user_;
+    bool has_user_ = false;
     double* mirror_ = nullptr;
 };
 
