@@ -1,0 +1,343 @@
+#!/usr/bin/env python
+"""Benchmark: 30-qubit complex128 layered circuit on one GB300 (the headline workload).
+
+Workload (seeded, synthetic): a 30-qubit state from |0..0> (16 GiB of complex128), 20 layers of
+RX, RY, RZ on every qubit (angles U[0, 2pi)) plus a CNOT brickwork on (i, i+1) with alternating
+offsets -- 1800 rotations + 290 CNOTs = 2090 gates.  One step = reset the state and run the whole
+circuit through the engine (fused shared-memory tile passes, complex128 as double-float).
+
+Printed as one JSON line:
+  value        gates/s over the whole job (logical, pre-fusion gates), device-timed with CUDA
+               events on the engine's stream, inputs resident in HBM;
+  e2e          the same metric through the drop-in API (quantum_sim_v3.StateVector) with the
+               final amplitudes read back to host memory (get_numpy_view) every step;
+  roofline     the dominant kernel (the tile pass): algorithmic bytes per launch (32 B x 2^30
+               amplitudes: one read and one write of the state) / its mean launch time, measured
+               with CUDA events around every launch inside the timed region;
+  cpu_baseline the reference's per-gate algorithm (the oracle's restatement of
+               ll::StateVectorBackend, OpenMP on every host core) on the first gates of the same
+               30-qubit circuit.
+`--impl reference` times that CPU implementation alone as the reference arm.
+
+Multi-GPU: the path does not shard (one state per GPU); with torchrun each rank runs an
+independent replica and `value` sums them ("replicas only", weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "lightning-lite-quantum-simulator_gb300")
+ORACLE = os.path.join(REPO, "oracle")
+for _p in (PKG, ORACLE):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "30q gates/s"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--qubits", type=int, default=30)
+    ap.add_argument("--layers", type=int, default=20)
+    ap.add_argument("--precision", default="complex128")
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--cpu-gates", type=int, default=12, help="gates in each CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# --------------------------------------------------------------------------------------------
+# CPU side: the reference's per-gate algorithm (oracle restatement), bounded sample
+# --------------------------------------------------------------------------------------------
+def cpu_sample(n: int, ops: np.ndarray, gates: int, reps: int, warm: int):
+    """Times `gates` gates of the circuit on an n-qubit state with every host core; returns
+    (gates/s best-of, threads, seconds per sample)."""
+    import oracle
+
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    psi = oracle.zero_state(n)
+    sample = np.ascontiguousarray(ops[:gates])
+    times = []
+    for k in range(warm + reps):
+        t0 = time.perf_counter()
+        rc = oracle.lib().orc_run_ops(psi.ctypes.data, n, sample.ctypes.data, sample.size)
+        t1 = time.perf_counter()
+        if rc:
+            raise RuntimeError("oracle rejected the sample")
+        if k >= warm:
+            times.append(t1 - t0)
+    best = min(times)
+    return gates / best, threads, best, times
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import workloads
+
+    ops = workloads.layered_rotations(args.qubits, args.layers)
+    warm = max(1, min(args.warmup, 1))
+    rate, threads, best, times = cpu_sample(args.qubits, ops, args.cpu_gates, args.steps, warm)
+    sample = (f"first {args.cpu_gates} gates of the {args.qubits}-qubit layered circuit per step, "
+              f"{args.steps} steps after {warm} warm-up; per-gate OpenMP passes of the reference algorithm")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "gates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": warm, "ms_per_step": 1e3 * statistics.mean(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.qubits}-qubit complex128 layered circuit ({args.layers} layers), "
+                               f"per-gate CPU sample", "qubits": args.qubits, "layers": args.layers},
+        "cpu_baseline": {"value": rate, "unit": "gates/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": "gates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------------------------
+# GPU side
+# --------------------------------------------------------------------------------------------
+def run_ours(args, rank, world, local):
+    import __graft_entry__
+
+    __graft_entry__.build()
+    import llgpu
+    import workloads
+
+    torch = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        import torch
+
+    n = args.qubits
+    ops = workloads.layered_rotations(n, args.layers)
+    ngates = len(ops)
+    st = llgpu.State(n, args.precision)
+    st.set_fusion("tile", args.tile)
+    tile_q = args.tile or (13 if args.precision == "complex64" else 12)
+    passes, xops = llgpu.plan_export(n, ops, tile_q)
+    elem = 8 if args.precision == "complex64" else 16
+    state_bytes = elem * (1 << n)
+
+    stream = torch.cuda.ExternalStream(st.stream)
+    # warm-up
+    for _ in range(args.warmup):
+        st.reset(n)
+        st.apply_ops(ops)
+        st.flush()
+    st.sync()
+    st.profile(True)
+    st.profile_read(reset=True)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    launches0 = llgpu.kernel_launches()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        st.sync()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            st.reset(n)
+            st.apply_ops(ops)
+            st.flush()
+        ev1.record(stream)
+        st.sync()
+        torch.cuda.synchronize()
+        barrier()
+    launches = llgpu.kernel_launches() - launches0
+    elapsed_ms = ev0.elapsed_time(ev1)
+    prof = st.profile_read(reset=True)
+    st.profile(False)
+    if world > 1:
+        t = torch.tensor([elapsed_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    ms_step = elapsed_ms / args.steps
+    value = ngates * args.steps * world / (elapsed_ms / 1e3)
+
+    tile_ms, tile_n = prof["tile"]
+    peak, peak_kind = peaks()
+    per_launch_s = (tile_ms / tile_n) / 1e3 if tile_n else float("nan")
+    achieved = state_bytes * 2 / per_launch_s / 1e9 if tile_n else None
+    traffic = profile_traffic()
+    st.close()
+
+    # end to end through the drop-in module: op records in, final amplitudes out, every step
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, ops, xops, n, elem, world, torch)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rate, threads, best, _ = cpu_sample(n, ops, args.cpu_gates, 1, 1)
+        cpu = {"value": rate, "unit": "gates/s", "cores": threads, "kind": "port",
+               "sample": f"first {args.cpu_gates} gates of the same {n}-qubit circuit, best of 1 after 1 warm-up, "
+                         f"{best:.1f} s per sample; oracle restatement of ll::StateVectorBackend (OpenMP)"}
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "gates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "df64" if args.precision == "complex128" else args.precision,
+        "data": "synthetic (seeded layered circuit)",
+        "config": {"workload": f"{n}-qubit complex128 layered circuit: {args.layers} layers of RX/RY/RZ on every "
+                               f"qubit + CNOT brickwork, {ngates} gates, fused into {len(passes)} shared-memory tile "
+                               f"passes of {tile_q} qubits", "qubits": n, "layers": args.layers, "gates": ngates,
+                   "tile_passes": int(len(passes)), "tile_qubits": tile_q, "precision": args.precision,
+                   "l2": "inputs larger than L2 (16 GiB state), no flush needed"},
+        "sweeps_per_s": len(passes) * args.steps * world / (elapsed_ms / 1e3),
+        "hbm_gbs_algorithmic": len(passes) * 2 * state_bytes * args.steps * world / (elapsed_ms / 1e3) / 1e9,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "kernel": "k_tile<PolDF64> (tile pass)", "launches": tile_n,
+                     "mean_launch_ms": tile_ms / tile_n if tile_n else None,
+                     "peak_source": f"{peak_kind} hbm_gbs"},
+        "kernel_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def profile_traffic():
+    """DRAM bytes per tile-pass launch from the committed ncu summary, if present."""
+    path = os.path.join(REPO, "profiles", "k_tile_df64_30q.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            if line.startswith("traffic_bytes_per_launch:"):
+                try:
+                    return float(line.split(":", 1)[1].strip())
+                except ValueError:
+                    return None
+    return None
+
+
+def run_e2e(args, ops, xops, n, elem, world, torch):
+    import quantum_sim_v3
+
+    sv = quantum_sim_v3.StateVector(n, args.precision)
+    sv.apply_ops(ops)
+    sv.get_numpy_view()  # allocates the pinned host mirror once
+    steps = max(1, args.steps)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sv.reset(n)
+        sv.apply_ops(ops)
+        view = sv.get_numpy_view()
+    _ = float(view[0].real)
+    t1 = time.perf_counter()
+    del sv, view
+    return {"value": len(ops) * steps * world / (t1 - t0), "unit": "gates/s",
+            "h2d_bytes_per_step": int(ops.nbytes + xops.nbytes), "d2h_bytes_per_step": int((1 << n) * 16),
+            "api": "quantum_sim_v3.StateVector: reset, apply_ops, get_numpy_view (host copy of all amplitudes)"}
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

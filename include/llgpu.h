@@ -161,6 +161,23 @@ int llg_expect_zz(llg_state* st, int nterms, const int* a, const int* b, const d
 /* Scale the state to unit norm (the periodic renormalisation of the complex64 path). */
 int llg_renormalize(llg_state* st);
 
+/* ---- tracing ----
+ * Per-state kernel timing with CUDA events recorded on the state's own stream around every
+ * engine launch, summed per kernel class.  Off by default (a few microseconds per launch). */
+#define LLG_PROF_TILE 0    /* fused shared-memory tile passes */
+#define LLG_PROF_GATE 1    /* per-gate streaming kernels */
+#define LLG_PROF_INIT 2    /* state initialisation */
+#define LLG_PROF_READOUT 3 /* conversions, |a|^2, reductions, scaling */
+#define LLG_PROF_CLASSES 4
+int llg_profile(llg_state* st, int on);
+/* Waits for the stream, then writes the summed milliseconds and launch counts per class
+ * (arrays of LLG_PROF_CLASSES); reset != 0 clears the sums. */
+int llg_profile_read(llg_state* st, double* ms, int64_t* launches, int reset);
+/* Process-wide number of kernels the engine has launched (all states). */
+int64_t llg_kernel_launches(void);
+/* The state's CUDA stream (a cudaStream_t), for callers that order their own work after it. */
+int llg_get_stream(const llg_state* st, void** out);
+
 /* Pinned host memory for fast transfers (cudaHostAlloc); NULL on failure. */
 void* llg_host_alloc(size_t bytes);
 void llg_host_free(void* p);

@@ -2,6 +2,7 @@
 // argument validation with the reference's error contract, the pending-gate queue and its
 // flush into fused tile passes or per-gate streaming kernels, and chunked host transfers.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -62,11 +63,56 @@ struct llg_state {
     // transfer staging (two chunks of complex128 = double2)
     double* d_stage[2] = {nullptr, nullptr};
     cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+    // tracing
+    bool prof_on = false;
+    struct ProfRec {
+        int cls;
+        cudaEvent_t a, b;
+    };
+    std::vector<ProfRec> prof_recs;
+    std::vector<cudaEvent_t> ev_pool;
+    double prof_ms[LLG_PROF_CLASSES] = {0, 0, 0, 0};
+    int64_t prof_n[LLG_PROF_CLASSES] = {0, 0, 0, 0};
 };
+
+static std::atomic<int64_t> g_launches{0};
 
 namespace {
 
 bool finite(double x) { return std::isfinite(x); }
+
+cudaEvent_t pool_event(llg_state* st) {
+    if (!st->ev_pool.empty()) {
+        cudaEvent_t e = st->ev_pool.back();
+        st->ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return e;
+}
+
+// Launch through `f` (returns cudaError_t), count `nk` kernels, and time it when tracing is on.
+template <class F>
+int traced(llg_state* st, int cls, int nk, const char* what, F&& f) {
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (st->prof_on) {
+        a = pool_event(st);
+        b = pool_event(st);
+        if (a) cudaEventRecord(a, st->stream);
+    }
+    const cudaError_t e = f();
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    g_launches += nk;
+    if (st->prof_on && a && b) {
+        cudaEventRecord(b, st->stream);
+        st->prof_recs.push_back({cls, a, b});
+    }
+    return LLG_OK;
+}
 
 int check_qubit(const llg_state* st, int q, const char* who) {
     if (q < 0 || q >= st->n)
@@ -127,7 +173,11 @@ int run_streaming(llg_state* st, const std::vector<llg_op>& q) {
     for (const llg_op& op : q) {
         lowered.clear();
         if (!lower_op(st->n, op, st->P, lowered, err)) return set_error(LLG_EINVAL, err);
-        for (const ExecOp& e : lowered) LLG_CUDA(launch_exec_op(st->P, st->d_psi, st->n, e, st->stream), "gate kernel");
+        for (const ExecOp& e : lowered) {
+            int rc = traced(st, LLG_PROF_GATE, 1, "gate kernel",
+                            [&] { return launch_exec_op(st->P, st->d_psi, st->n, e, st->stream); });
+            if (rc) return rc;
+        }
     }
     return LLG_OK;
 }
@@ -168,8 +218,12 @@ int run_tiles(llg_state* st, const std::vector<llg_op>& q) {
         return set_error(LLG_EINVAL, err);
     int rc = upload_ops(st, plan.ops);
     if (rc) return rc;
-    for (const PassDesc& pd : plan.passes)
-        if (pd.nops > 0) LLG_CUDA(launch_tile_pass(st->P, st->d_psi, st->n, pd, st->d_ops, st->stream), "tile kernel");
+    for (const PassDesc& pd : plan.passes) {
+        if (pd.nops <= 0) continue;
+        rc = traced(st, LLG_PROF_TILE, 1, "tile kernel",
+                    [&] { return launch_tile_pass(st->P, st->d_psi, st->n, pd, st->d_ops, st->stream); });
+        if (rc) return rc;
+    }
     return LLG_OK;
 }
 
@@ -256,10 +310,8 @@ int llg_create(int n_qubits, int precision, llg_state** out) {
     st->P = precision;
     int rc = ensure_device_buffers(st);
     if (!rc) rc = alloc_state(st, n_qubits);
-    if (!rc) {
-        cudaError_t e = launch_init_basis(st->P, st->d_psi, st->size, 0, st->stream);
-        if (e != cudaSuccess) rc = cuda_fail(e, "init");
-    }
+    if (!rc)
+        rc = traced(st, LLG_PROF_INIT, 1, "init", [&] { return launch_init_basis(st->P, st->d_psi, st->size, 0, st->stream); });
     if (rc) {
         llg_destroy(st);
         return rc;
@@ -315,6 +367,11 @@ int llg_destroy(llg_state* st) {
         if (st->stage_ev[i]) cudaEventDestroy(st->stage_ev[i]);
     }
     if (st->ops_done) cudaEventDestroy(st->ops_done);
+    for (auto& r : st->prof_recs) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    for (cudaEvent_t e : st->ev_pool) cudaEventDestroy(e);
     if (st->stream) cudaStreamDestroy(st->stream);
     delete st;
     return LLG_OK;
@@ -327,8 +384,7 @@ int llg_reset(llg_state* st, int n_qubits) {
     st->queue.clear();
     int rc = alloc_state(st, n_qubits);
     if (rc) return rc;
-    LLG_CUDA(launch_init_basis(st->P, st->d_psi, st->size, 0, st->stream), "init");
-    return LLG_OK;
+    return traced(st, LLG_PROF_INIT, 1, "init", [&] { return launch_init_basis(st->P, st->d_psi, st->size, 0, st->stream); });
 }
 
 int llg_num_qubits(const llg_state* st, int* out) {
@@ -473,7 +529,10 @@ int llg_copy_to_host(llg_state* st, double* out) {
     for (uint64_t off = 0; off < st->size; off += kStageAmps, which ^= 1) {
         const uint64_t cnt = std::min<uint64_t>(kStageAmps, st->size - off);
         LLG_CUDA(cudaEventSynchronize(st->stage_ev[which]), "cudaEventSynchronize");
-        LLG_CUDA(launch_to_f64(st->P, (const char*)st->d_psi + off * eb, st->d_stage[which], cnt, st->stream), "to_f64");
+        rc = traced(st, LLG_PROF_READOUT, 1, "to_f64", [&] {
+            return launch_to_f64(st->P, (const char*)st->d_psi + off * eb, st->d_stage[which], cnt, st->stream);
+        });
+        if (rc) return rc;
         LLG_CUDA(cudaMemcpyAsync(out + 2 * off, st->d_stage[which], cnt * 16, cudaMemcpyDeviceToHost, st->stream),
                  "cudaMemcpyAsync(D2H)");
         LLG_CUDA(cudaEventRecord(st->stage_ev[which], st->stream), "cudaEventRecord");
@@ -499,7 +558,10 @@ int llg_copy_from_host(llg_state* st, const double* amps) {
         LLG_CUDA(cudaEventSynchronize(st->stage_ev[which]), "cudaEventSynchronize");
         LLG_CUDA(cudaMemcpyAsync(st->d_stage[which], amps + 2 * off, cnt * 16, cudaMemcpyHostToDevice, st->stream),
                  "cudaMemcpyAsync(H2D)");
-        LLG_CUDA(launch_from_f64(st->P, st->d_stage[which], (char*)st->d_psi + off * eb, cnt, st->stream), "from_f64");
+        rc = traced(st, LLG_PROF_READOUT, 1, "from_f64", [&] {
+            return launch_from_f64(st->P, st->d_stage[which], (char*)st->d_psi + off * eb, cnt, st->stream);
+        });
+        if (rc) return rc;
         LLG_CUDA(cudaEventRecord(st->stage_ev[which], st->stream), "cudaEventRecord");
     }
     LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
@@ -517,8 +579,10 @@ int llg_probabilities(llg_state* st, double* out) {
     for (uint64_t off = 0; off < st->size; off += chunk, which ^= 1) {
         const uint64_t cnt = std::min<uint64_t>(chunk, st->size - off);
         LLG_CUDA(cudaEventSynchronize(st->stage_ev[which]), "cudaEventSynchronize");
-        LLG_CUDA(launch_probabilities(st->P, (const char*)st->d_psi + off * eb, st->d_stage[which], cnt, st->stream),
-                 "probabilities");
+        rc = traced(st, LLG_PROF_READOUT, 1, "probabilities", [&] {
+            return launch_probabilities(st->P, (const char*)st->d_psi + off * eb, st->d_stage[which], cnt, st->stream);
+        });
+        if (rc) return rc;
         LLG_CUDA(cudaMemcpyAsync(out + off, st->d_stage[which], cnt * 8, cudaMemcpyDeviceToHost, st->stream),
                  "cudaMemcpyAsync(D2H)");
         LLG_CUDA(cudaEventRecord(st->stage_ev[which], st->stream), "cudaEventRecord");
@@ -555,7 +619,9 @@ static int build_zterms(int nterms, const int* a, const int* b, const double* co
 static int reduce(llg_state* st, const ZTerms& z, double* slots) {
     int rc = llg_flush(st);
     if (rc) return rc;
-    LLG_CUDA(launch_reduce_z(st->P, st->d_psi, st->n, z, st->d_partials, st->d_red, st->stream), "reduce");
+    rc = traced(st, LLG_PROF_READOUT, 2, "reduce",
+                [&] { return launch_reduce_z(st->P, st->d_psi, st->n, z, st->d_partials, st->d_red, st->stream); });
+    if (rc) return rc;
     LLG_CUDA(cudaMemcpyAsync(slots, st->d_red, sizeof(double) * kRedSlots, cudaMemcpyDeviceToHost, st->stream),
              "cudaMemcpyAsync(D2H)");
     LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
@@ -596,8 +662,8 @@ int llg_renormalize(llg_state* st) {
     int rc = llg_norm2(st, &nrm);
     if (rc) return rc;
     if (!(nrm > 0.0) || !std::isfinite(nrm)) return set_error(LLG_ERUNTIME, "renormalize: state norm vanished");
-    LLG_CUDA(launch_scale(st->P, st->d_psi, st->size, 1.0 / std::sqrt(nrm), st->stream), "scale");
-    return LLG_OK;
+    return traced(st, LLG_PROF_READOUT, 1, "scale",
+                  [&] { return launch_scale(st->P, st->d_psi, st->size, 1.0 / std::sqrt(nrm), st->stream); });
 }
 
 void* llg_host_alloc(size_t bytes) {
@@ -611,6 +677,43 @@ void* llg_host_alloc(size_t bytes) {
 
 void llg_host_free(void* p) {
     if (p) cudaFreeHost(p);
+}
+
+int llg_profile(llg_state* st, int on) {
+    if (!st) return set_error(LLG_EINVAL, "profile: NULL state");
+    st->prof_on = on != 0;
+    return LLG_OK;
+}
+
+int llg_profile_read(llg_state* st, double* ms, int64_t* launches, int reset) {
+    if (!st) return set_error(LLG_EINVAL, "profile_read: NULL state");
+    LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+    for (auto& r : st->prof_recs) {
+        float t = 0.0f;
+        if (cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) st->prof_ms[r.cls] += t;
+        else cudaGetLastError();
+        st->prof_n[r.cls] += 1;
+        st->ev_pool.push_back(r.a);
+        st->ev_pool.push_back(r.b);
+    }
+    st->prof_recs.clear();
+    for (int c = 0; c < LLG_PROF_CLASSES; ++c) {
+        if (ms) ms[c] = st->prof_ms[c];
+        if (launches) launches[c] = st->prof_n[c];
+        if (reset) {
+            st->prof_ms[c] = 0.0;
+            st->prof_n[c] = 0;
+        }
+    }
+    return LLG_OK;
+}
+
+int64_t llg_kernel_launches(void) { return g_launches.load(); }
+
+int llg_get_stream(const llg_state* st, void** out) {
+    if (!st || !out) return set_error(LLG_EINVAL, "get_stream: NULL argument");
+    *out = (void*)st->stream;
+    return LLG_OK;
 }
 
 int llg_plan_export(int n, const llg_op* ops, int nops, int tile_qubits, llg_pass_info* passes, int max_passes,

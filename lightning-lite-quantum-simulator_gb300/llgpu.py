@@ -24,6 +24,9 @@ LLG_F64, LLG_DF64, LLG_F32 = 0, 1, 2
 LLG_FUSE_NONE, LLG_FUSE_TILE = 0, 1
 OP_H, OP_X, OP_RX, OP_RY, OP_RZ, OP_CNOT, OP_MCZ, OP_CZ, OP_U2 = range(9)
 
+PROF_CLASSES = 4
+PROF_NAMES = ("tile", "gate", "init", "readout")
+
 PRECISIONS = {"fp64": LLG_F64, "complex128": LLG_DF64, "df64": LLG_DF64, "complex64": LLG_F32}
 
 # numpy view of llg_op (96 bytes)
@@ -88,6 +91,10 @@ def lib() -> ctypes.CDLL:
             "llg_host_alloc": (vp, [sz]),
             "llg_host_free": (None, [vp]),
             "llg_plan_export": (i, [i, vp, i, i, vp, i, P(i), vp, i, P(i)]),
+            "llg_profile": (i, [vp, i]),
+            "llg_profile_read": (i, [vp, vp, vp, i]),
+            "llg_kernel_launches": (ctypes.c_int64, []),
+            "llg_get_stream": (i, [vp, P(vp)]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
@@ -114,6 +121,10 @@ def check(rc: int) -> None:
 
 def device_count() -> int:
     return lib().llg_device_count()
+
+
+def kernel_launches() -> int:
+    return int(lib().llg_kernel_launches())
 
 
 def _ptr(a: np.ndarray) -> int:
@@ -246,6 +257,25 @@ class State:
 
     def renormalize(self) -> None:
         check(lib().llg_renormalize(self._h))
+
+    def reset(self, n: int) -> None:
+        check(lib().llg_reset(self._h, n))
+
+    def profile(self, on: bool = True) -> None:
+        check(lib().llg_profile(self._h, 1 if on else 0))
+
+    def profile_read(self, reset: bool = True):
+        """{class: (milliseconds, launches)} for tile / gate / init / readout kernels."""
+        ms = np.zeros(PROF_CLASSES, dtype=np.float64)
+        n = np.zeros(PROF_CLASSES, dtype=np.int64)
+        check(lib().llg_profile_read(self._h, _ptr(ms), _ptr(n), 1 if reset else 0))
+        return {name: (float(ms[k]), int(n[k])) for k, name in enumerate(PROF_NAMES)}
+
+    @property
+    def stream(self) -> int:
+        v = ctypes.c_void_p()
+        check(lib().llg_get_stream(self._h, ctypes.byref(v)))
+        return v.value or 0
 
 
 # ---------------------------------------------------------------------------------------------
