@@ -158,6 +158,21 @@ int llg_norm2(llg_state* st, double* out);
  * diagonal of python/algorithms.py:141-153 (ising_diagonal) evaluated on the fly. */
 int llg_expect_zz(llg_state* st, int nterms, const int* a, const int* b, const double* coeff, double* out);
 
+/* No counterpart in the reference.  llg_expect_zz for callers that cannot allocate GPU memory:
+ * callers whose device memory belongs to another allocator (a framework that reserves most of
+ * the GPU up front) and callers in latency-critical loops where cudaMalloc/cudaFree would
+ * synchronise the device.  The caller passes the amplitudes (d_amps: 2^n elements in the
+ * `precision` layout, device or managed memory it owns) and d_out (2 device doubles, receiving
+ * [sum_k coeff_k <Z..>, sum |a|^2]); kernels are enqueued on `stream` (a cudaStream_t, NULL for
+ * the default stream) and the call returns without waiting.  Nothing is allocated: the partial
+ * sums go to a fixed 40 KiB device array inside the library (1024 blocks x 5 doubles), held by
+ * every GPU that loads it until exit.  The first call on a device resolves that array's address
+ * and should come before any stream capture on that device.  All calls share the array; each
+ * call writes every partial it reads, but calls that overlap on the GPU race.  Limits:
+ * n_qubits in [1, 34], at most 64 terms with at most 4 distinct coefficients. */
+int llg_expect_zz_noalloc(const void* d_amps, int n_qubits, int precision, int nterms, const int* a, const int* b,
+                          const double* coeff, double* d_out, void* stream);
+
 /* Scale the state to unit norm (the periodic renormalisation of the complex64 path). */
 int llg_renormalize(llg_state* st);
 

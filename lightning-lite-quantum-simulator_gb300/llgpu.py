@@ -95,6 +95,7 @@ def lib() -> ctypes.CDLL:
             "llg_profile_read": (i, [vp, vp, vp, i]),
             "llg_kernel_launches": (ctypes.c_int64, []),
             "llg_get_stream": (i, [vp, P(vp)]),
+            "llg_expect_zz_noalloc": (i, [vp, i, i, i, vp, vp, vp, vp, vp]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
