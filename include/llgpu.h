@@ -176,6 +176,35 @@ int llg_expect_zz_noalloc(const void* d_amps, int n_qubits, int precision, int n
 /* Scale the state to unit norm (the periodic renormalisation of the complex64 path). */
 int llg_renormalize(llg_state* st);
 
+/* ---- batched parametrised circuits: adjoint gradients and parameter shift ----
+ * A circuit whose RX/RY/RZ records carry param >= 0 takes theta = params[set][param] for each
+ * parameter set of a batch; the states of a batch live side by side in HBM ([batch][2^n]).
+ * The observable is O = sum_k coeff_k Z_{za[k]} Z_{zb[k]} (zb[k] < 0: single Z), as in
+ * python/algorithms.py:141-153; E = <psi|O|psi>.  Parameters, energies and gradients may be host
+ * or device pointers.  Calls block until their results are written. */
+typedef struct llg_adjoint llg_adjoint;
+
+/* Plans the circuit once for up to max_batch parameter sets.  n in [1, 30]. */
+int llg_adjoint_create(int n, const llg_op* ops, int nops, int nparams, int max_batch, int precision, int nterms,
+                       const int* za, const int* zb, const double* zcoeff, llg_adjoint** out);
+int llg_adjoint_destroy(llg_adjoint* h);
+int llg_adjoint_info(const llg_adjoint* h, int* fwd_passes, int* bwd_passes, int* n_param_ops);
+
+/* E(theta) for `batch` parameter sets (params [batch][nparams]) and, if grads != NULL, every
+ * dE/dtheta by the adjoint method: one forward sweep, one reverse sweep of psi and lambda = O psi
+ * with one inner-product reduction per parametrised gate.  The reference's gradient is the
+ * parameter-shift rule (src/Algorithms.h:277-292).  checkpoint_every = C > 0 stores the forward
+ * state every C tile passes and restarts the reverse sweep from those states. */
+int llg_adjoint_run(llg_adjoint* h, const double* params, int batch, double* energies, double* grads, int checkpoint_every);
+
+/* The same gradients by the reference's parameter-shift rule (src/Algorithms.h:210-212, :277-292),
+ * each shifted circuit evaluated as one member of a batched forward sweep: 1 + 2 * (number of
+ * parametrised gates) evaluations per parameter set. */
+int llg_param_shift_run(llg_adjoint* h, const double* params, int sets, double* energies, double* grads);
+
+/* The handle's CUDA stream (cudaStream_t). */
+int llg_adjoint_stream(const llg_adjoint* h, void** out);
+
 /* ---- tracing ----
  * Per-state kernel timing with CUDA events recorded on the state's own stream around every
  * engine launch, summed per kernel class.  Off by default (a few microseconds per launch). */

@@ -1,0 +1,882 @@
+// llg_adjoint.cu -- batched circuits with parameters: forward passes, adjoint-method gradients
+// and the parameter-shift comparison (include/llgpu.h, "adjoint" section).
+//
+// The reference differentiates with the parameter-shift rule, 2 circuit evaluations per
+// parameter (src/Algorithms.h:277-292).  Here one forward sweep and one reverse sweep give every
+// gradient (adjoint method; Jones & Gacon, arXiv:2009.02823):
+//   forward   psi = U_N .. U_1 |0>, then lambda = O psi and E = <psi|lambda> in one pass
+//             (O = sum_k c_k Z_a Z_b is diagonal);
+//   backward  for g = N .. 1: if U_g = exp(-i theta P / 2), dE/dtheta += Im <lambda|P|psi>;
+//             then psi <- U_g^+ psi, lambda <- U_g^+ lambda.
+// Both sweeps run as shared-memory tile passes (the forward plan's passes mirrored for the
+// backward), over a batch of parameter sets laid out [batch][2^n]; a tile's batch index picks its
+// row of the (cos, sin) coefficient table.  Inner products are reduced per tile into a partial
+// array and summed in a fixed order, so gradients are deterministic.  Forward states can be
+// checkpointed every C passes; the backward sweep then restarts psi from each checkpoint instead
+// of relying on uncomputation alone (deep circuits).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/llgpu.h"
+#include "llg_common.cuh"
+#include "llg_internal.h"
+#include "llg_launch.h"
+#include "llg_tile.cuh"
+
+namespace llg {
+int set_error(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+}  // namespace llg
+
+using namespace llg;
+
+#define ADJ_CUDA(call, what)                               \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+namespace {
+
+constexpr int kAdjTile = 11;  // two 2^11 tiles (psi, lambda) per CTA in the backward pass
+constexpr int kThreads = 256;
+constexpr int kEBlocksPerState = 64;
+
+// ------------------------------------------------------------------------------------------
+// coefficient table: table[row][j] = (cos(theta/2), sin(theta/2)) packed for the precision
+// ------------------------------------------------------------------------------------------
+template <class P>
+__device__ uint64_t pack_dev(double x) {
+    if (P::kPrecision == 0) return (uint64_t)__double_as_longlong(x);
+    if (P::kPrecision == 2) return (uint64_t)__float_as_uint(__double2float_rn(x));
+    const df d = double_to_df(x);
+    return (uint64_t)__float_as_uint(d.hi) | ((uint64_t)__float_as_uint(d.lo) << 32);
+}
+
+template <class P>
+__global__ void k_coef_table(const double* __restrict__ params, int nparams, const int* __restrict__ occ_param, int nocc,
+                             int rows, const int* __restrict__ row_set, const int* __restrict__ shift_occ,
+                             const double* __restrict__ shift_val, uint64_t* __restrict__ table) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= rows * nocc) return;
+    const int r = idx / nocc, j = idx % nocc;
+    const int set = row_set ? row_set[r] : r;
+    double theta = params[(size_t)set * nparams + occ_param[j]];
+    if (shift_occ && shift_occ[r] == j) theta += shift_val[r];
+    double s, c;
+    sincos(0.5 * theta, &s, &c);
+    table[2 * (size_t)idx] = pack_dev<P>(c);
+    table[2 * (size_t)idx + 1] = pack_dev<P>(s);
+}
+
+// ------------------------------------------------------------------------------------------
+// one op on a shared-memory tile (all kinds, parametrised ones read their table row)
+// ------------------------------------------------------------------------------------------
+template <class P>
+__device__ void tile_apply(typename P::S* tile, uint32_t tsize, uint64_t base, const ExecOp& o,
+                           const uint64_t* __restrict__ trow) {
+    using K = typename P::K;
+    using S = typename P::S;
+    switch (o.kind) {
+        case EX_U2: tile_pairs<P, EX_U2>(tile, tsize >> 1, o.q0, o); break;
+        case EX_RX: tile_pairs<P, EX_RX>(tile, tsize >> 1, o.q0, o); break;
+        case EX_RY: tile_pairs<P, EX_RY>(tile, tsize >> 1, o.q0, o); break;
+        case EX_H: tile_pairs<P, EX_H>(tile, tsize >> 1, o.q0, o); break;
+        case EX_X: tile_pairs<P, EX_X>(tile, tsize >> 1, o.q0, o); break;
+        case EX_RX_P:
+        case EX_RY_P: {
+            ExecOp r = o;
+            r.c[0] = trow[2 * o.q1];
+            const K s = P::k_from_bits(trow[2 * o.q1 + 1]);
+            K sv = (o.flags & OPF_ADJOINT) ? P::kneg(s) : s;
+            // re-pack the (possibly negated) sine through a local copy of the op
+            if (o.kind == EX_RX_P) {
+                PairMath<P, EX_RX> m(r);
+                m.k[1] = sv;
+                const uint32_t bit = 1u << o.q0;
+                for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += blockDim.x) {
+                    const uint32_t j0 = (uint32_t)insert0(p, o.q0), j1 = j0 | bit;
+                    auto a0 = P::load(tile[j0]);
+                    auto a1 = P::load(tile[j1]);
+                    m.apply(a0, a1);
+                    tile[j0] = P::store(a0);
+                    tile[j1] = P::store(a1);
+                }
+            } else {
+                PairMath<P, EX_RY> m(r);
+                m.k[1] = sv;
+                const uint32_t bit = 1u << o.q0;
+                for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += blockDim.x) {
+                    const uint32_t j0 = (uint32_t)insert0(p, o.q0), j1 = j0 | bit;
+                    auto a0 = P::load(tile[j0]);
+                    auto a1 = P::load(tile[j1]);
+                    m.apply(a0, a1);
+                    tile[j0] = P::store(a0);
+                    tile[j1] = P::store(a1);
+                }
+            }
+            break;
+        }
+        case EX_DIAG:
+        case EX_RZ_P: {
+            K d0r, d0i, d1r, d1i;
+            if (o.kind == EX_DIAG) {
+                d0r = P::k_from_bits(o.c[0]);
+                d0i = P::k_from_bits(o.c[1]);
+                d1r = P::k_from_bits(o.c[2]);
+                d1i = P::k_from_bits(o.c[3]);
+            } else {  // RZ(t) = diag(c - i s, c + i s); its inverse swaps the signs
+                const K c = P::k_from_bits(trow[2 * o.q1]);
+                K s = P::k_from_bits(trow[2 * o.q1 + 1]);
+                if (o.flags & OPF_ADJOINT) s = P::kneg(s);
+                d0r = c;
+                d0i = P::kneg(s);
+                d1r = c;
+                d1i = s;
+            }
+            if (o.flags & OPF_NONLOCAL_Q0) {
+                const bool one = (base >> o.q0) & 1;
+                const K dr = one ? d1r : d0r, di = one ? d1i : d0i;
+                const K mdi = P::kneg(di);
+                for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
+                    auto a = P::load(tile[l]);
+                    cmul_const<P>(a, dr, di, mdi);
+                    tile[l] = P::store(a);
+                }
+            } else {
+                const K md0i = P::kneg(d0i), md1i = P::kneg(d1i);
+                for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
+                    auto a = P::load(tile[l]);
+                    if ((l >> o.q0) & 1) cmul_const<P>(a, d1r, d1i, md1i);
+                    else cmul_const<P>(a, d0r, d0i, md0i);
+                    tile[l] = P::store(a);
+                }
+            }
+            break;
+        }
+        case EX_CNOT: {
+            const int tq = o.q1;
+            if (o.flags & OPF_NONLOCAL_Q0) {
+                if ((base >> o.q0) & 1) tile_pairs<P, EX_X>(tile, tsize >> 1, tq, o);
+            } else {
+                const int c = o.q0;
+                const int lo = c < tq ? c : tq, hi = c < tq ? tq : c;
+                const uint32_t cbit = 1u << c, tbit = 1u << tq;
+                for (uint32_t r = threadIdx.x; r < (tsize >> 2); r += blockDim.x) {
+                    const uint32_t j = (uint32_t)insert0(insert0(r, lo), hi) | cbit;
+                    const S x = tile[j];
+                    tile[j] = tile[j | tbit];
+                    tile[j | tbit] = x;
+                }
+            }
+            break;
+        }
+        case EX_MCZ: {
+            if ((base & o.nl_mask) == o.nl_mask) {
+                const uint32_t lm = (uint32_t)o.mask;
+                const uint32_t cnt = tsize >> __popc(lm);
+                for (uint32_t r = threadIdx.x; r < cnt; r += blockDim.x) {
+                    const uint32_t j = (uint32_t)insert0_mask(r, lm) | lm;
+                    auto a = P::load(tile[j]);
+                    a.re = P::neg(a.re);
+                    a.im = P::neg(a.im);
+                    tile[j] = P::store(a);
+                }
+            }
+            break;
+        }
+        default: break;
+    }
+}
+
+__device__ __forceinline__ double block_sum_d(double v, double* sh) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += sh[w];
+    return r;
+}
+
+// Im <lambda | P | psi> over the tile for the generator P of a parametrised op.
+template <class P>
+__device__ double tile_generator_inner(const typename P::S* psi, const typename P::S* lam, uint32_t tsize, uint64_t base,
+                                       const ExecOp& o) {
+    typename P::Acc pos = P::acc_zero(), neg = P::acc_zero();
+    if (o.kind == EX_RZ_P) {
+        if (o.flags & OPF_NONLOCAL_Q0) {
+            for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x)
+                pos = P::acc_dot_im(pos, P::load(lam[l]), P::load(psi[l]));
+            const double v = P::acc_to_double(pos);
+            return ((base >> o.q0) & 1) ? -v : v;
+        }
+        for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
+            if ((l >> o.q0) & 1) neg = P::acc_dot_im(neg, P::load(lam[l]), P::load(psi[l]));
+            else pos = P::acc_dot_im(pos, P::load(lam[l]), P::load(psi[l]));
+        }
+        return P::acc_to_double(pos) - P::acc_to_double(neg);
+    }
+    const uint32_t bit = 1u << o.q0;
+    for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += blockDim.x) {
+        const uint32_t j0 = (uint32_t)insert0(p, o.q0), j1 = j0 | bit;
+        const auto p0 = P::load(psi[j0]), p1 = P::load(psi[j1]);
+        const auto l0 = P::load(lam[j0]), l1 = P::load(lam[j1]);
+        if (o.kind == EX_RY_P) {  // Y: Re(conj(l1) p0) - Re(conj(l0) p1)
+            pos = P::acc_dot_re(pos, l1, p0);
+            neg = P::acc_dot_re(neg, l0, p1);
+        } else {  // X: Im(conj(l0) p1) + Im(conj(l1) p0)
+            pos = P::acc_dot_im(pos, l0, p1);
+            pos = P::acc_dot_im(pos, l1, p0);
+        }
+    }
+    return P::acc_to_double(pos) - P::acc_to_double(neg);
+}
+
+// ------------------------------------------------------------------------------------------
+// batched forward tile pass: grid (tiles per state, batch)
+// ------------------------------------------------------------------------------------------
+template <class P>
+__global__ void __launch_bounds__(512) k_tile_fwd(typename P::S* __restrict__ psi_all, int n, PassDesc pd,
+                                                  const ExecOp* __restrict__ ops, const uint64_t* __restrict__ table,
+                                                  int nocc) {
+    using S = typename P::S;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int t = pd.t, low = pd.low;
+    const uint32_t tsize = 1u << t, nhi = 1u << (t - low);
+    S* tile = reinterpret_cast<S*>(smem_raw);
+    uint64_t* hi_off = reinterpret_cast<uint64_t*>(smem_raw + (size_t)tsize * sizeof(S));
+    const uint64_t b = blockIdx.y;
+    S* psi = psi_all + (b << n);
+    const uint64_t* trow = table + b * (uint64_t)nocc * 2;
+    const uint64_t base = insert0_mask((uint64_t)blockIdx.x, pd.local_mask);
+    for (uint32_t h = threadIdx.x; h < nhi; h += blockDim.x) {
+        uint64_t off = 0;
+        for (int j = 0; j < t - low; ++j)
+            if ((h >> j) & 1) off |= 1ULL << pd.hi_pos[j];
+        hi_off[h] = off;
+    }
+    __syncthreads();
+    const uint32_t lowmask = (1u << low) - 1;
+    for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) tile[l] = psi[base | hi_off[l >> low] | (l & lowmask)];
+    __syncthreads();
+    for (int k = 0; k < pd.nops; ++k) {
+        tile_apply<P>(tile, tsize, base, ops[pd.op_begin + k], trow);
+        __syncthreads();
+    }
+    for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) psi[base | hi_off[l >> low] | (l & lowmask)] = tile[l];
+}
+
+// batched backward tile pass over psi and lambda; gpart[b][occ][tile]
+template <class P>
+__global__ void __launch_bounds__(512) k_tile_bwd(typename P::S* __restrict__ psi_all, typename P::S* __restrict__ lam_all,
+                                                  int n, PassDesc pd, const ExecOp* __restrict__ ops,
+                                                  const uint64_t* __restrict__ table, int nocc, double* __restrict__ gpart,
+                                                  int tiles) {
+    using S = typename P::S;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double red[16];
+    const int t = pd.t, low = pd.low;
+    const uint32_t tsize = 1u << t, nhi = 1u << (t - low);
+    S* tp = reinterpret_cast<S*>(smem_raw);
+    S* tl = tp + tsize;
+    uint64_t* hi_off = reinterpret_cast<uint64_t*>(smem_raw + 2 * (size_t)tsize * sizeof(S));
+    const uint64_t b = blockIdx.y;
+    S* psi = psi_all + (b << n);
+    S* lam = lam_all + (b << n);
+    const uint64_t* trow = table + b * (uint64_t)nocc * 2;
+    const uint64_t base = insert0_mask((uint64_t)blockIdx.x, pd.local_mask);
+    for (uint32_t h = threadIdx.x; h < nhi; h += blockDim.x) {
+        uint64_t off = 0;
+        for (int j = 0; j < t - low; ++j)
+            if ((h >> j) & 1) off |= 1ULL << pd.hi_pos[j];
+        hi_off[h] = off;
+    }
+    __syncthreads();
+    const uint32_t lowmask = (1u << low) - 1;
+    for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
+        const uint64_t g = base | hi_off[l >> low] | (l & lowmask);
+        tp[l] = psi[g];
+        tl[l] = lam[g];
+    }
+    __syncthreads();
+    for (int k = 0; k < pd.nops; ++k) {
+        const ExecOp& o = ops[pd.op_begin + k];
+        if (o.flags & OPF_GRAD) {
+            const double v = block_sum_d(tile_generator_inner<P>(tp, tl, tsize, base, o), red);
+            if (threadIdx.x == 0) gpart[((size_t)b * nocc + o.q1) * tiles + blockIdx.x] = v;
+            __syncthreads();
+        }
+        tile_apply<P>(tp, tsize, base, o, trow);
+        tile_apply<P>(tl, tsize, base, o, trow);
+        __syncthreads();
+    }
+    for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
+        const uint64_t g = base | hi_off[l >> low] | (l & lowmask);
+        psi[g] = tp[l];
+        lam[g] = tl[l];
+    }
+}
+
+// lambda = O psi (if lam != nullptr) and per-block energy partials, grid (kEBlocksPerState, batch)
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_energy_lambda(const typename P::S* __restrict__ psi_all,
+                                                            typename P::S* __restrict__ lam_all, int n, ZTerms z,
+                                                            double* __restrict__ epart) {
+    using K = typename P::K;
+    __shared__ double sh[kThreads / 32];
+    const uint64_t b = blockIdx.y;
+    const uint64_t size = 1ULL << n;
+    const typename P::S* psi = psi_all + b * size;
+    typename P::S* lam = lam_all ? lam_all + b * size : nullptr;
+    int tot[kMaxZClasses] = {0, 0, 0, 0};
+    for (int k = 0; k < z.nterms; ++k) tot[z.cls[k]] += 1;
+    K cf[kMaxZClasses];
+#pragma unroll
+    for (int c = 0; c < kMaxZClasses; ++c) cf[c] = P::k_from_bits(0);
+    for (int c = 0; c < z.nclass; ++c) {
+        const double v = z.coef[c];
+        if (P::kPrecision == 0) cf[c] = P::k_from_bits((uint64_t)__double_as_longlong(v));
+        else if (P::kPrecision == 2) cf[c] = P::k_from_bits((uint64_t)__float_as_uint(__double2float_rn(v)));
+        else {
+            const df d = double_to_df(v);
+            cf[c] = P::k_from_bits((uint64_t)__float_as_uint(d.hi) | ((uint64_t)__float_as_uint(d.lo) << 32));
+        }
+    }
+    typename P::Acc acc[kMaxZClasses];
+#pragma unroll
+    for (int c = 0; c < kMaxZClasses; ++c) acc[c] = P::acc_zero();
+    const uint64_t step = (uint64_t)gridDim.x * kThreads;
+    for (uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x; i < size; i += step) {
+        const auto a = P::load(psi[i]);
+        int odd[kMaxZClasses] = {0, 0, 0, 0};
+        for (int k = 0; k < z.nterms; ++k) {
+            int par = (int)((i >> z.a[k]) & 1);
+            if (z.b[k] >= 0) par ^= (int)((i >> z.b[k]) & 1);
+            odd[z.cls[k]] += par;
+        }
+        typename P::R dre = P::zero(), dim_unused = P::zero();
+        (void)dim_unused;
+#pragma unroll
+        for (int c = 0; c < kMaxZClasses; ++c) {
+            if (c >= z.nclass) break;
+            const float m = (float)(tot[c] - 2 * odd[c]);  // sum over the class of the +-1 eigenvalues
+            acc[c] = P::acc_norm_w(acc[c], a, m);
+            if (lam) dre = P::add(dre, P::mulk(cf[c], P::r_from_float(m)));
+        }
+        if (lam) {
+            typename P::C out;
+            out.re = P::mulk(dre, a.re);
+            out.im = P::mulk(dre, a.im);
+            lam[i] = P::store(out);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < kMaxZClasses; ++c) {
+        const double v = block_sum_d(P::acc_to_double(acc[c]), sh);
+        if (threadIdx.x == 0) epart[((size_t)b * gridDim.x + blockIdx.x) * kMaxZClasses + c] = v;
+    }
+}
+
+__global__ void k_energy_finish(const double* __restrict__ epart, int blocks, int batch, ZTerms z, double* __restrict__ energies) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= batch) return;
+    double e = 0.0;
+    for (int c = 0; c < z.nclass; ++c) {
+        double w = 0.0;
+        for (int k = 0; k < blocks; ++k) w += epart[((size_t)b * blocks + k) * kMaxZClasses + c];
+        e += z.coef[c] * w;
+    }
+    energies[b] = e;
+}
+
+// grads[b][k] = sum over the occurrences of parameter k (CSR list) and tiles, fixed order
+__global__ void k_grad_finish(const double* __restrict__ gpart, int batch, int nocc, int tiles, int nparams,
+                              const int* __restrict__ csr_ptr, const int* __restrict__ csr_occ, double* __restrict__ grads) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= batch * nparams) return;
+    const int b = idx / nparams, k = idx % nparams;
+    double g = 0.0;
+    for (int e = csr_ptr[k]; e < csr_ptr[k + 1]; ++e) {
+        const double* row = gpart + ((size_t)b * nocc + csr_occ[e]) * tiles;
+        for (int t = 0; t < tiles; ++t) g += row[t];
+    }
+    grads[idx] = g;
+}
+
+template <class P>
+size_t fwd_smem(int t, int low) {
+    return ((size_t)1 << t) * sizeof(typename P::S) + ((size_t)1 << (t - low)) * sizeof(uint64_t);
+}
+template <class P>
+size_t bwd_smem(int t, int low) {
+    return 2 * ((size_t)1 << t) * sizeof(typename P::S) + ((size_t)1 << (t - low)) * sizeof(uint64_t);
+}
+
+template <class P>
+cudaError_t set_smem_attrs() {
+    static bool done = false;
+    if (done) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(k_tile_fwd<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem<P>(kAdjTile, 4));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_tile_bwd<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bwd_smem<P>(kAdjTile, 4));
+    if (e == cudaSuccess) done = true;
+    return e;
+}
+
+// |0..0> in every batch element: element 0 of each row is 1 (the rows were zeroed)
+template <class P>
+__global__ void k_set_rows(typename P::S* psi, int n, int batch) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= batch) return;
+    typename P::C one;
+    one.re = P::r_from_float(1.0f);
+    one.im = P::zero();
+    psi[(uint64_t)b << n] = P::store(one);
+}
+
+int threads_for(int t) { return t >= 10 ? 512 : (t >= 6 ? (1 << (t - 1)) : 32); }
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+// host object
+// ------------------------------------------------------------------------------------------
+struct llg_adjoint {
+    int n = 0, P = LLG_DF64, nparams = 0, max_batch = 0, nocc = 0, tiles = 1;
+    ZTerms z;
+    Plan fwd;
+    std::vector<PassDesc> bwd_passes;
+    std::vector<ExecOp> bwd_ops;
+    std::vector<int> occ_param;
+    cudaStream_t stream = nullptr;
+    void* d_psi = nullptr;
+    void* d_lam = nullptr;
+    ExecOp* d_fwd_ops = nullptr;
+    ExecOp* d_bwd_ops = nullptr;
+    uint64_t* d_table = nullptr;
+    int* d_occ_param = nullptr;
+    int* d_csr_ptr = nullptr;
+    int* d_csr_occ = nullptr;
+    double* d_params = nullptr;
+    double* d_gpart = nullptr;
+    double* d_epart = nullptr;
+    double* d_energy = nullptr;
+    double* d_grad = nullptr;
+    int* d_row_set = nullptr;
+    int* d_shift_occ = nullptr;
+    double* d_shift_val = nullptr;
+    std::vector<void*> ckpt;
+    size_t state_bytes = 0;  // one batch element
+};
+
+namespace {
+
+template <class T>
+int dmalloc(T** p, size_t count, const char* what) {
+    cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return set_error(LLG_ENOMEM, std::string("adjoint: cannot allocate ") + what + ": " + cudaGetErrorString(e));
+    }
+    return LLG_OK;
+}
+
+bool is_device_ptr(const void* p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// conjugate-transpose an executor op in place (packed coefficients: negation flips sign bits)
+uint64_t neg_packed(int P, uint64_t v) {
+    if (P == LLG_F64) return v ^ 0x8000000000000000ULL;
+    if (P == LLG_F32) return v ^ 0x80000000ULL;
+    return v ^ 0x8000000080000000ULL;
+}
+
+ExecOp adjoint_of(int P, const ExecOp& e) {
+    ExecOp a = e;
+    switch (e.kind) {
+        case EX_U2:  // (g^+)_{rc} = conj(g_{cr})
+            a.c[0] = e.c[0];
+            a.c[1] = neg_packed(P, e.c[1]);
+            a.c[2] = e.c[4];
+            a.c[3] = neg_packed(P, e.c[5]);
+            a.c[4] = e.c[2];
+            a.c[5] = neg_packed(P, e.c[3]);
+            a.c[6] = e.c[6];
+            a.c[7] = neg_packed(P, e.c[7]);
+            break;
+        case EX_RX:
+        case EX_RY: a.c[1] = neg_packed(P, e.c[1]); break;
+        case EX_DIAG:
+            a.c[1] = neg_packed(P, e.c[1]);
+            a.c[3] = neg_packed(P, e.c[3]);
+            break;
+        case EX_RX_P:
+        case EX_RY_P:
+        case EX_RZ_P: a.flags |= OPF_ADJOINT | OPF_GRAD; break;
+        default: break;  // H, X, CNOT, MCZ are their own inverses
+    }
+    return a;
+}
+
+template <class P>
+int run_forward(llg_adjoint* h, int batch, bool make_lambda, const int* ckpt_every) {
+    const uint64_t size = 1ULL << h->n;
+    cudaStream_t s = h->stream;
+    ADJ_CUDA(cudaMemsetAsync(h->d_psi, 0, (size_t)batch * h->state_bytes, s), "memset psi");
+    k_set_rows<P><<<(batch + 255) / 256, 256, 0, s>>>(static_cast<typename P::S*>(h->d_psi), h->n, batch);
+    ADJ_CUDA(cudaGetLastError(), "init rows");
+    ADJ_CUDA(set_smem_attrs<P>(), "smem attribute");
+    const int C = ckpt_every ? *ckpt_every : 0;
+    for (size_t j = 0; j < h->fwd.passes.size(); ++j) {
+        const PassDesc& pd = h->fwd.passes[j];
+        const dim3 grid((unsigned)(1ULL << (h->n - pd.t)), (unsigned)batch);
+        k_tile_fwd<P><<<grid, threads_for(pd.t), fwd_smem<P>(pd.t, pd.low), s>>>(
+            static_cast<typename P::S*>(h->d_psi), h->n, pd, h->d_fwd_ops, h->d_table, h->nocc);
+        ADJ_CUDA(cudaGetLastError(), "forward tile pass");
+        if (C > 0 && (j + 1) % C == 0 && j + 1 < h->fwd.passes.size()) {
+            const size_t m = (j + 1) / C - 1;
+            ADJ_CUDA(cudaMemcpyAsync(h->ckpt[m], h->d_psi, (size_t)batch * h->state_bytes, cudaMemcpyDeviceToDevice, s),
+                     "checkpoint");
+        }
+    }
+    const dim3 eg(kEBlocksPerState, (unsigned)batch);
+    k_energy_lambda<P><<<eg, kThreads, 0, s>>>(static_cast<const typename P::S*>(h->d_psi),
+                                               make_lambda ? static_cast<typename P::S*>(h->d_lam) : nullptr, h->n, h->z,
+                                               h->d_epart);
+    ADJ_CUDA(cudaGetLastError(), "energy");
+    k_energy_finish<<<(batch + 127) / 128, 128, 0, s>>>(h->d_epart, kEBlocksPerState, batch, h->z, h->d_energy);
+    ADJ_CUDA(cudaGetLastError(), "energy finish");
+    (void)size;
+    return LLG_OK;
+}
+
+template <class P>
+int run_backward(llg_adjoint* h, int batch, int C) {
+    cudaStream_t s = h->stream;
+    const int np = (int)h->bwd_passes.size();
+    for (int j = 0; j < np; ++j) {
+        const PassDesc& pd = h->bwd_passes[j];
+        const dim3 grid((unsigned)(1ULL << (h->n - pd.t)), (unsigned)batch);
+        k_tile_bwd<P><<<grid, threads_for(pd.t), bwd_smem<P>(pd.t, pd.low), s>>>(
+            static_cast<typename P::S*>(h->d_psi), static_cast<typename P::S*>(h->d_lam), h->n, pd, h->d_bwd_ops,
+            h->d_table, h->nocc, h->d_gpart, h->tiles);
+        ADJ_CUDA(cudaGetLastError(), "backward tile pass");
+        // backward pass j undoes forward pass fj = np - 1 - j; psi is now the state after fj forward
+        // passes; restart it from the checkpoint taken there, if any
+        const int fj = np - 1 - j;
+        if (C > 0 && fj > 0 && fj % C == 0) {
+            const size_t m = fj / C - 1;
+            ADJ_CUDA(cudaMemcpyAsync(h->d_psi, h->ckpt[m], (size_t)batch * h->state_bytes, cudaMemcpyDeviceToDevice, s),
+                     "restore checkpoint");
+        }
+    }
+    const int total = batch * h->nparams;
+    k_grad_finish<<<(total + 255) / 256, 256, 0, s>>>(h->d_gpart, batch, h->nocc, h->tiles, h->nparams, h->d_csr_ptr,
+                                                      h->d_csr_occ, h->d_grad);
+    ADJ_CUDA(cudaGetLastError(), "gradient finish");
+    return LLG_OK;
+}
+
+int build_table(llg_adjoint* h, int rows, bool shifted) {
+    const int total = rows * h->nocc;
+    if (total == 0) return LLG_OK;
+    const int blocks = (total + 255) / 256;
+    switch (h->P) {
+        case LLG_F64:
+            k_coef_table<PolF64><<<blocks, 256, 0, h->stream>>>(h->d_params, h->nparams, h->d_occ_param, h->nocc, rows,
+                                                                shifted ? h->d_row_set : nullptr,
+                                                                shifted ? h->d_shift_occ : nullptr, h->d_shift_val, h->d_table);
+            break;
+        case LLG_F32:
+            k_coef_table<PolF32><<<blocks, 256, 0, h->stream>>>(h->d_params, h->nparams, h->d_occ_param, h->nocc, rows,
+                                                                shifted ? h->d_row_set : nullptr,
+                                                                shifted ? h->d_shift_occ : nullptr, h->d_shift_val, h->d_table);
+            break;
+        default:
+            k_coef_table<PolDF64><<<blocks, 256, 0, h->stream>>>(h->d_params, h->nparams, h->d_occ_param, h->nocc, rows,
+                                                                 shifted ? h->d_row_set : nullptr,
+                                                                 shifted ? h->d_shift_occ : nullptr, h->d_shift_val, h->d_table);
+    }
+    ADJ_CUDA(cudaGetLastError(), "coefficient table");
+    return LLG_OK;
+}
+
+int forward_dispatch(llg_adjoint* h, int batch, bool lam, const int* C) {
+    switch (h->P) {
+        case LLG_F64: return run_forward<PolF64>(h, batch, lam, C);
+        case LLG_F32: return run_forward<PolF32>(h, batch, lam, C);
+        default: return run_forward<PolDF64>(h, batch, lam, C);
+    }
+}
+
+int backward_dispatch(llg_adjoint* h, int batch, int C) {
+    switch (h->P) {
+        case LLG_F64: return run_backward<PolF64>(h, batch, C);
+        case LLG_F32: return run_backward<PolF32>(h, batch, C);
+        default: return run_backward<PolDF64>(h, batch, C);
+    }
+}
+
+int load_params(llg_adjoint* h, const double* params, int sets) {
+    const size_t bytes = (size_t)sets * h->nparams * sizeof(double);
+    if (bytes == 0) return LLG_OK;
+    ADJ_CUDA(cudaMemcpyAsync(h->d_params, params, bytes, is_device_ptr(params) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                             h->stream),
+             "params upload");
+    return LLG_OK;
+}
+
+int store_out(llg_adjoint* h, double* dst, const double* src, size_t count) {
+    if (!dst || count == 0) return LLG_OK;
+    ADJ_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(double), is_device_ptr(dst) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                             h->stream),
+             "result copy");
+    return LLG_OK;
+}
+
+int ensure_checkpoints(llg_adjoint* h, int C) {
+    if (C <= 0) return LLG_OK;
+    const size_t need = h->fwd.passes.size() > 1 ? (h->fwd.passes.size() - 1) / C : 0;
+    while (h->ckpt.size() < need) {
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, (size_t)h->max_batch * h->state_bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(LLG_ENOMEM, "adjoint: cannot allocate checkpoint states");
+        }
+        h->ckpt.push_back(p);
+    }
+    return LLG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int llg_adjoint_create(int n, const llg_op* ops, int nops, int nparams, int max_batch, int precision, int nterms,
+                       const int* za, const int* zb, const double* zcoeff, llg_adjoint** out) {
+    if (!out) return set_error(LLG_EINVAL, "adjoint_create: out is NULL");
+    *out = nullptr;
+    if (n < 1 || n > 30) return set_error(LLG_EINVAL, "adjoint_create: n must be in [1, 30]");
+    if (nops < 0 || (nops > 0 && !ops) || nparams < 0 || max_batch < 1 || max_batch > 65535)
+        return set_error(LLG_EINVAL, "adjoint_create: bad sizes");
+    if (precision != LLG_F64 && precision != LLG_DF64 && precision != LLG_F32)
+        return set_error(LLG_EINVAL, "adjoint_create: unknown precision");
+    if (nterms < 1 || nterms > kMaxZTerms || !za || !zb || !zcoeff)
+        return set_error(LLG_EINVAL, "adjoint_create: observable needs 1.." + std::to_string(kMaxZTerms) + " terms");
+    llg_adjoint* h = new llg_adjoint();
+    h->n = n;
+    h->P = precision;
+    h->nparams = nparams;
+    h->max_batch = max_batch;
+    // observable
+    std::memset(&h->z, 0, sizeof(h->z));
+    h->z.nterms = nterms;
+    for (int k = 0; k < nterms; ++k) {
+        if (za[k] < 0 || za[k] >= n || zb[k] >= n || zb[k] == za[k] || !std::isfinite(zcoeff[k])) {
+            delete h;
+            return set_error(LLG_EINVAL, "adjoint_create: bad observable term " + std::to_string(k));
+        }
+        int c = -1;
+        for (int j = 0; j < h->z.nclass; ++j)
+            if (h->z.coef[j] == zcoeff[k]) c = j;
+        if (c < 0) {
+            if (h->z.nclass == kMaxZClasses) {
+                delete h;
+                return set_error(LLG_EINVAL, "adjoint_create: at most 4 distinct observable coefficients");
+            }
+            c = h->z.nclass++;
+            h->z.coef[c] = zcoeff[k];
+        }
+        h->z.a[k] = za[k];
+        h->z.b[k] = zb[k] < 0 ? -1 : zb[k];
+        h->z.cls[k] = c;
+    }
+    // validate ops (bad qubits, angles; parameter indices)
+    for (int i = 0; i < nops; ++i) {
+        const llg_op& o = ops[i];
+        const bool rot = o.kind == LLG_OP_RX || o.kind == LLG_OP_RY || o.kind == LLG_OP_RZ;
+        bool ok = o.q0 >= 0 && o.q0 < n;
+        if (o.kind == LLG_OP_CNOT || o.kind == LLG_OP_CZ) ok = ok && o.q1 >= 0 && o.q1 < n && o.q1 != o.q0;
+        if (o.kind == LLG_OP_MCZ) ok = o.mask != 0 && (n >= 64 || (o.mask >> n) == 0);
+        if (o.kind < 0 || o.kind > LLG_OP_U2) ok = false;
+        if (rot && o.param < 0 && !std::isfinite(o.theta)) ok = false;
+        if (o.param >= nparams || (o.param >= 0 && !rot)) ok = false;
+        if (!ok) {
+            delete h;
+            return set_error(LLG_EINVAL, "adjoint_create: invalid op " + std::to_string(i));
+        }
+        if (o.param >= 0) h->occ_param.push_back(o.param);
+    }
+    h->nocc = (int)h->occ_param.size();
+    std::string err;
+    const int t = std::min(n, kAdjTile);
+    if (!plan_tiles(n, ops, nops, t, precision, h->fwd, err, true)) {
+        delete h;
+        return set_error(LLG_EINVAL, "adjoint_create: " + err);
+    }
+    h->tiles = 1 << (n - t);
+    // backward plan: passes reversed, ops reversed and inverted, parametrised ops flagged
+    for (int j = (int)h->fwd.passes.size() - 1; j >= 0; --j) {
+        PassDesc pd = h->fwd.passes[j];
+        const int begin = (int)h->bwd_ops.size();
+        for (int k = pd.op_begin + pd.nops - 1; k >= pd.op_begin; --k) h->bwd_ops.push_back(adjoint_of(precision, h->fwd.ops[k]));
+        pd.op_begin = begin;
+        h->bwd_passes.push_back(pd);
+    }
+    h->state_bytes = ((size_t)1 << n) * elem_bytes(precision);
+    // CSR: parameter -> occurrences
+    std::vector<int> ptr(nparams + 1, 0), occ(h->nocc);
+    for (int j = 0; j < h->nocc; ++j) ptr[h->occ_param[j] + 1]++;
+    for (int k = 0; k < nparams; ++k) ptr[k + 1] += ptr[k];
+    {
+        std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+        for (int j = 0; j < h->nocc; ++j) occ[fill[h->occ_param[j]]++] = j;
+    }
+    int rc = LLG_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaStreamCreate");
+    if (!rc) rc = dmalloc((char**)&h->d_psi, (size_t)max_batch * h->state_bytes, "psi");
+    if (!rc) rc = dmalloc((char**)&h->d_lam, (size_t)max_batch * h->state_bytes, "lambda");
+    if (!rc) rc = dmalloc(&h->d_fwd_ops, h->fwd.ops.size(), "ops");
+    if (!rc) rc = dmalloc(&h->d_bwd_ops, h->bwd_ops.size(), "ops");
+    if (!rc) rc = dmalloc(&h->d_table, (size_t)max_batch * h->nocc * 2, "coefficient table");
+    if (!rc) rc = dmalloc(&h->d_occ_param, h->nocc, "occurrence map");
+    if (!rc) rc = dmalloc(&h->d_csr_ptr, nparams + 1, "csr");
+    if (!rc) rc = dmalloc(&h->d_csr_occ, h->nocc, "csr");
+    if (!rc) rc = dmalloc(&h->d_params, (size_t)max_batch * std::max(nparams, 1), "params");
+    if (!rc) rc = dmalloc(&h->d_gpart, (size_t)max_batch * h->nocc * h->tiles, "gradient partials");
+    if (!rc) rc = dmalloc(&h->d_epart, (size_t)max_batch * kEBlocksPerState * kMaxZClasses, "energy partials");
+    if (!rc) rc = dmalloc(&h->d_energy, max_batch, "energies");
+    if (!rc) rc = dmalloc(&h->d_grad, (size_t)max_batch * std::max(nparams, 1), "gradients");
+    if (!rc) rc = dmalloc(&h->d_row_set, max_batch, "rows");
+    if (!rc) rc = dmalloc(&h->d_shift_occ, max_batch, "rows");
+    if (!rc) rc = dmalloc(&h->d_shift_val, max_batch, "rows");
+    if (!rc && !h->fwd.ops.empty())
+        rc = cudaMemcpy(h->d_fwd_ops, h->fwd.ops.data(), h->fwd.ops.size() * sizeof(ExecOp), cudaMemcpyHostToDevice)
+                 ? set_error(LLG_ECUDA, "adjoint_create: op upload") : LLG_OK;
+    if (!rc && !h->bwd_ops.empty())
+        rc = cudaMemcpy(h->d_bwd_ops, h->bwd_ops.data(), h->bwd_ops.size() * sizeof(ExecOp), cudaMemcpyHostToDevice)
+                 ? set_error(LLG_ECUDA, "adjoint_create: op upload") : LLG_OK;
+    if (!rc && h->nocc)
+        rc = cudaMemcpy(h->d_occ_param, h->occ_param.data(), h->nocc * sizeof(int), cudaMemcpyHostToDevice) ||
+                     cudaMemcpy(h->d_csr_occ, occ.data(), h->nocc * sizeof(int), cudaMemcpyHostToDevice)
+                 ? set_error(LLG_ECUDA, "adjoint_create: map upload") : LLG_OK;
+    if (!rc)
+        rc = cudaMemcpy(h->d_csr_ptr, ptr.data(), (nparams + 1) * sizeof(int), cudaMemcpyHostToDevice)
+                 ? set_error(LLG_ECUDA, "adjoint_create: map upload") : LLG_OK;
+    if (rc) {
+        llg_adjoint_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return LLG_OK;
+}
+
+int llg_adjoint_destroy(llg_adjoint* h) {
+    if (!h) return LLG_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    void* ptrs[] = {h->d_psi, h->d_lam, h->d_fwd_ops, h->d_bwd_ops, h->d_table, h->d_occ_param, h->d_csr_ptr,
+                    h->d_csr_occ, h->d_params, h->d_gpart, h->d_epart, h->d_energy, h->d_grad, h->d_row_set,
+                    h->d_shift_occ, h->d_shift_val};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    for (void* p : h->ckpt) cudaFree(p);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return LLG_OK;
+}
+
+int llg_adjoint_info(const llg_adjoint* h, int* fwd_passes, int* bwd_passes, int* n_param_ops) {
+    if (!h) return set_error(LLG_EINVAL, "adjoint_info: NULL handle");
+    if (fwd_passes) *fwd_passes = (int)h->fwd.passes.size();
+    if (bwd_passes) *bwd_passes = (int)h->bwd_passes.size();
+    if (n_param_ops) *n_param_ops = h->nocc;
+    return LLG_OK;
+}
+
+int llg_adjoint_run(llg_adjoint* h, const double* params, int batch, double* energies, double* grads, int checkpoint_every) {
+    if (!h || (!params && h->nparams > 0)) return set_error(LLG_EINVAL, "adjoint_run: NULL argument");
+    if (batch < 1 || batch > h->max_batch)
+        return set_error(LLG_EINVAL, "adjoint_run: batch must be in [1, " + std::to_string(h->max_batch) + "]");
+    if (checkpoint_every < 0) return set_error(LLG_EINVAL, "adjoint_run: checkpoint_every must be >= 0");
+    int rc = load_params(h, params, batch);
+    if (!rc) rc = build_table(h, batch, false);
+    if (!rc && grads) rc = ensure_checkpoints(h, checkpoint_every);
+    if (!rc) rc = forward_dispatch(h, batch, grads != nullptr, grads ? &checkpoint_every : nullptr);
+    if (!rc && grads) rc = backward_dispatch(h, batch, checkpoint_every);
+    if (!rc) rc = store_out(h, energies, h->d_energy, batch);
+    if (!rc && grads) rc = store_out(h, grads, h->d_grad, (size_t)batch * h->nparams);
+    if (!rc) ADJ_CUDA(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
+    return rc;
+}
+
+int llg_param_shift_run(llg_adjoint* h, const double* params, int sets, double* energies, double* grads) {
+    if (!h || (!params && h->nparams > 0) || !grads) return set_error(LLG_EINVAL, "param_shift_run: NULL argument");
+    if (sets < 1 || sets > h->max_batch)
+        return set_error(LLG_EINVAL, "param_shift_run: sets must be in [1, " + std::to_string(h->max_batch) + "]");
+    int rc = load_params(h, params, sets);
+    if (rc) return rc;
+    const double half_pi = 1.57079632679489661923;
+    const int rows_per_set = 1 + 2 * h->nocc;
+    std::vector<double> g((size_t)sets * h->nparams, 0.0), e(sets, 0.0);
+    std::vector<int> row_set(h->max_batch), shift_occ(h->max_batch);
+    std::vector<double> shift_val(h->max_batch), row_e(h->max_batch);
+    // rows enumerate (set, r): r = 0 unshifted, r = 2j+1 occurrence j shifted +pi/2, r = 2j+2 -pi/2
+    const long long total = (long long)sets * rows_per_set;
+    for (long long start = 0; start < total; start += h->max_batch) {
+        const int rows = (int)std::min<long long>(h->max_batch, total - start);
+        for (int i = 0; i < rows; ++i) {
+            const long long g_row = start + i;
+            const int set = (int)(g_row / rows_per_set), r = (int)(g_row % rows_per_set);
+            row_set[i] = set;
+            shift_occ[i] = r == 0 ? -1 : (r - 1) / 2;
+            shift_val[i] = r == 0 ? 0.0 : ((r % 2) ? half_pi : -half_pi);
+        }
+        ADJ_CUDA(cudaMemcpyAsync(h->d_row_set, row_set.data(), rows * sizeof(int), cudaMemcpyHostToDevice, h->stream), "rows");
+        ADJ_CUDA(cudaMemcpyAsync(h->d_shift_occ, shift_occ.data(), rows * sizeof(int), cudaMemcpyHostToDevice, h->stream), "rows");
+        ADJ_CUDA(cudaMemcpyAsync(h->d_shift_val, shift_val.data(), rows * sizeof(double), cudaMemcpyHostToDevice, h->stream),
+                 "rows");
+        if ((rc = build_table(h, rows, true))) return rc;
+        if ((rc = forward_dispatch(h, rows, false, nullptr))) return rc;
+        ADJ_CUDA(cudaMemcpyAsync(row_e.data(), h->d_energy, rows * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "energies");
+        ADJ_CUDA(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
+        for (int i = 0; i < rows; ++i) {
+            const int set = row_set[i], occ = shift_occ[i];
+            if (occ < 0) e[set] = row_e[i];
+            else g[(size_t)set * h->nparams + h->occ_param[occ]] += (shift_val[i] > 0 ? 0.5 : -0.5) * row_e[i];
+        }
+    }
+    const bool dev_g = is_device_ptr(grads);
+    ADJ_CUDA(cudaMemcpy(grads, g.data(), g.size() * sizeof(double), dev_g ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost),
+             "gradients");
+    if (energies)
+        ADJ_CUDA(cudaMemcpy(energies, e.data(), e.size() * sizeof(double),
+                            is_device_ptr(energies) ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost),
+                 "energies");
+    return LLG_OK;
+}
+
+int llg_adjoint_stream(const llg_adjoint* h, void** out) {
+    if (!h || !out) return set_error(LLG_EINVAL, "adjoint_stream: NULL argument");
+    *out = (void*)h->stream;
+    return LLG_OK;
+}
+
+}  // extern "C"

@@ -20,11 +20,18 @@ enum ExecKind : int32_t {
     EX_DIAG = 5,  // diag(d0, d1) on q0; c[0..3] = d0 (re, im), d1 (re, im); RZ(t) = diag(e^-it/2, e^it/2)
     EX_CNOT = 6,  // control q0, target q1
     EX_MCZ = 7,   // negate amplitudes with all `mask` bits set
+    // parametrised rotations of the batched / adjoint engine: q1 = occurrence slot, the (cos, sin)
+    // of the half angle come from a per-batch table; RZ_P is diagonal (q0 may be non-local)
+    EX_RX_P = 8,
+    EX_RY_P = 9,
+    EX_RZ_P = 10,
 };
 
 // Flags of a tile op.
 enum : int32_t {
     OPF_NONLOCAL_Q0 = 1,  // q0 is a global qubit outside the tile (diagonal / control use only)
+    OPF_ADJOINT = 2,      // parametrised op applied as its inverse (angle negated)
+    OPF_GRAD = 4,         // backward pass: accumulate Im<lambda|P|psi> before applying the op
 };
 
 // One executor op.  In a tile pass q0/q1/mask are LOCAL (tile) indices unless flagged; `nl_mask`
@@ -63,7 +70,10 @@ struct Plan {
 
 // Lower and plan a gate list into tile passes (llg_plan.cpp).  Returns false with `err` set on
 // invalid input.
-bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int precision, Plan& out, std::string& err);
+// With use_params, rotations whose `param` >= 0 are kept unfused and lowered to EX_*_P ops whose
+// q1 is the op's occurrence slot (the index of that op among all parametrised ops, in order).
+bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int precision, Plan& out, std::string& err,
+                bool use_params = false);
 
 // Lower one gate record to executor ops with GLOBAL qubit indices (streaming path).
 bool lower_op(int n, const llg_op& op, int precision, std::vector<ExecOp>& out, std::string& err);

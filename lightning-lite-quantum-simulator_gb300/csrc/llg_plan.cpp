@@ -178,7 +178,12 @@ struct Pending {
 
 }  // namespace
 
-bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan& out, std::string& err) {
+static bool is_param_op(const llg_op& op, bool use_params) {
+    return use_params && op.param >= 0 && (op.kind == LLG_OP_RX || op.kind == LLG_OP_RY || op.kind == LLG_OP_RZ);
+}
+
+bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan& out, std::string& err,
+                bool use_params) {
     out.passes.clear();
     out.ops.clear();
     out.source_index.clear();
@@ -194,6 +199,12 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
 
     std::vector<int> remaining(nops);
     for (int i = 0; i < nops; ++i) remaining[i] = i;
+    std::vector<int> occ_of(nops, -1);
+    {
+        int occ = 0;
+        for (int i = 0; i < nops; ++i)
+            if (is_param_op(ops[i], use_params)) occ_of[i] = occ++;
+    }
     std::vector<int> touched, need, deferred, included;
     std::vector<char> blocked(64, 0);
 
@@ -320,6 +331,20 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
 
         for (int idx : included) {
             const llg_op& op = ops[idx];
+            if (occ_of[idx] >= 0) {
+                // parametrised rotation: never fused, coefficients come from the batch table
+                if (!flush_pending(op.q0)) return false;
+                ExecOp e = blank(op.kind == LLG_OP_RX ? EX_RX_P : (op.kind == LLG_OP_RY ? EX_RY_P : EX_RZ_P));
+                e.q1 = occ_of[idx];
+                if (to_local[op.q0] >= 0) e.q0 = to_local[op.q0];
+                else {
+                    e.q0 = op.q0;
+                    e.flags |= OPF_NONLOCAL_Q0;
+                }
+                out.ops.push_back(e);
+                out.source_index.push_back(idx);
+                continue;
+            }
             if (is_single_qubit(op.kind)) {
                 Pending& p = pend[op.q0];
                 double m[8];

@@ -96,6 +96,12 @@ def lib() -> ctypes.CDLL:
             "llg_kernel_launches": (ctypes.c_int64, []),
             "llg_get_stream": (i, [vp, P(vp)]),
             "llg_expect_zz_noalloc": (i, [vp, i, i, i, vp, vp, vp, vp, vp]),
+            "llg_adjoint_create": (i, [i, vp, i, i, i, i, i, vp, vp, vp, P(vp)]),
+            "llg_adjoint_destroy": (i, [vp]),
+            "llg_adjoint_info": (i, [vp, P(i), P(i), P(i)]),
+            "llg_adjoint_run": (i, [vp, vp, i, vp, vp, i]),
+            "llg_param_shift_run": (i, [vp, vp, i, vp, vp]),
+            "llg_adjoint_stream": (i, [vp, P(vp)]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
@@ -300,3 +306,70 @@ def ring_zz_terms(n: int):
     b = [(i + 1) % n for i in range(n)]
     return a, b, [1.0] * n
 
+
+
+# ---------------------------------------------------------------------------------------------
+# batched parametrised circuits (adjoint gradients, parameter shift)
+# ---------------------------------------------------------------------------------------------
+class Adjoint:
+    """A planned parametrised circuit for batches of up to `max_batch` parameter sets.
+
+    `ops` is an llg_op array whose RX/RY/RZ records carry `param` >= 0 for trainable angles;
+    the observable is sum_k coeff[k] Z_a[k] Z_b[k] (b[k] < 0: single Z)."""
+
+    def __init__(self, n: int, ops: np.ndarray, nparams: int, observable, max_batch: int = 64,
+                 precision: str = "complex128"):
+        a, b, c = observable
+        aa = np.ascontiguousarray(a, dtype=np.int32)
+        bb = np.ascontiguousarray(b, dtype=np.int32)
+        cc = np.ascontiguousarray(c, dtype=np.float64)
+        self._ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
+        self.n, self.nparams, self.max_batch = n, nparams, max_batch
+        self._h = ctypes.c_void_p()
+        check(lib().llg_adjoint_create(n, _ptr(self._ops) if self._ops.size else None, self._ops.size, nparams,
+                                       max_batch, PRECISIONS[precision], aa.size, _ptr(aa), _ptr(bb), _ptr(cc),
+                                       ctypes.byref(self._h)))
+
+    def close(self) -> None:
+        if self._h:
+            lib().llg_adjoint_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> dict:
+        f, b_, n = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(lib().llg_adjoint_info(self._h, ctypes.byref(f), ctypes.byref(b_), ctypes.byref(n)))
+        return {"forward_passes": f.value, "backward_passes": b_.value, "param_ops": n.value}
+
+    @property
+    def stream(self) -> int:
+        v = ctypes.c_void_p()
+        check(lib().llg_adjoint_stream(self._h, ctypes.byref(v)))
+        return v.value or 0
+
+    def run(self, params: np.ndarray, grads: bool = True, checkpoint_every: int = 0):
+        """(energies[batch], grads[batch, nparams] or None) for host parameter sets."""
+        p = np.ascontiguousarray(np.atleast_2d(params), dtype=np.float64)
+        batch = p.shape[0]
+        e = np.zeros(batch)
+        g = np.zeros((batch, self.nparams)) if grads else None
+        check(lib().llg_adjoint_run(self._h, _ptr(p), batch, _ptr(e), _ptr(g) if grads else None, checkpoint_every))
+        return e, g
+
+    def run_device(self, params_ptr: int, batch: int, energies_ptr: int, grads_ptr: int | None,
+                   checkpoint_every: int = 0) -> None:
+        """Same, on device pointers (e.g. torch CUDA tensors' data_ptr())."""
+        check(lib().llg_adjoint_run(self._h, params_ptr, batch, energies_ptr, grads_ptr, checkpoint_every))
+
+    def param_shift(self, params: np.ndarray):
+        p = np.ascontiguousarray(np.atleast_2d(params), dtype=np.float64)
+        sets = p.shape[0]
+        e = np.zeros(sets)
+        g = np.zeros((sets, self.nparams))
+        check(lib().llg_param_shift_run(self._h, _ptr(p), sets, _ptr(e), _ptr(g)))
+        return e, g
