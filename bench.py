@@ -59,6 +59,7 @@ def parse_args():
     ap.add_argument("--cpu-gates", type=int, default=12, help="gates in each CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient measurement")
     return ap.parse_args()
 
 
@@ -258,6 +259,10 @@ def run_ours(args, rank, world, local):
     if not args.no_e2e:
         e2e = run_e2e(args, ops, xops, n, elem, world, torch)
 
+    adj = None
+    if not args.no_adjoint:
+        adj = run_adjoint_bench(args, torch)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rate, threads, best, _ = cpu_sample(n, ops, args.cpu_gates, 1, 1)
@@ -290,6 +295,7 @@ def run_ours(args, rank, world, local):
         "clocks": clk.summary(),
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "adjoint": adj,
     }
     print(json.dumps(line), flush=True)
 
@@ -307,6 +313,48 @@ def profile_traffic():
                 except ValueError:
                     return None
     return None
+
+
+def run_adjoint_bench(args, torch):
+    """Adjoint gradients of the 20-qubit, 10-layer RY/RZ + CZ-ring ansatz (400 parameters,
+    observable sum_i Z_i Z_{i+1} periodic) for a batch of 64 parameter sets, against the
+    parameter-shift rule evaluated on the same GPU (batched shifted circuits) for one set."""
+    import llgpu
+    import workloads
+
+    n, layers, batch = 20, 10, 64
+    ops = workloads.hea_ansatz(n, layers)
+    nparams = layers * 2 * n
+    params = workloads.hea_params(n, layers, batch)
+    adj = llgpu.Adjoint(n, ops, nparams, llgpu.ring_zz_terms(n), max_batch=batch, precision=args.precision)
+    stream = torch.cuda.ExternalStream(adj.stream)
+    for _ in range(2):
+        adj.run(params)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(1, args.steps)
+    ev0.record(stream)
+    for _ in range(reps):
+        e, g = adj.run(params)
+    ev1.record(stream)
+    ev1.synchronize()
+    t_adj = ev0.elapsed_time(ev1) / 1e3 / reps
+    adj.param_shift(params[:1])  # warm-up
+    ev0.record(stream)
+    e_ps, g_ps = adj.param_shift(params[:1])
+    ev1.record(stream)
+    ev1.synchronize()
+    t_ps = ev0.elapsed_time(ev1) / 1e3
+    info = adj.info()
+    adj.close()
+    grads_adj = batch * nparams / t_adj
+    grads_ps = nparams / t_ps
+    return {"workload": f"{n}-qubit hardware-efficient ansatz, {layers} layers RY/RZ + CZ ring, {nparams} "
+                        f"parameters, batch {batch}, observable sum Z_i Z_i+1",
+            "grads_per_s": grads_adj, "param_shift_grads_per_s": grads_ps, "speedup_vs_param_shift": grads_adj / grads_ps,
+            "adjoint_s_per_batch": t_adj, "param_shift_s_per_set": t_ps,
+            "max_abs_grad_diff_vs_param_shift": float(np.max(np.abs(g[0] - g_ps[0]))),
+            "forward_passes": info["forward_passes"], "backward_passes": info["backward_passes"],
+            "precision": args.precision}
 
 
 def run_e2e(args, ops, xops, n, elem, world, torch):

@@ -205,6 +205,23 @@ int llg_param_shift_run(llg_adjoint* h, const double* params, int sets, double* 
 /* The handle's CUDA stream (cudaStream_t). */
 int llg_adjoint_stream(const llg_adjoint* h, void** out);
 
+/* ---- batched noisy trajectories ----
+ * Runs trajectories [traj_begin, traj_begin + n_traj) of an n-qubit circuit (n in [1, 14]) in one
+ * persistent launch, each state resident in shared memory (a 2-CTA cluster for 14-qubit complex128
+ * states).  After every gate, for each qubit it touches (1-qubit gates: its qubit; cnot/cz:
+ * control then target; mcz: its qubits in increasing order -- the noise sites of
+ * src/Mitigation.h:146-204), amplitude damping (gamma_ad) then phase damping (lambda_pd) are
+ * unravelled with the jump rule of src/TrajectorySolver.h:421-455 using Philox4x32-10 uniforms
+ * (key = seed, counter = (site, trajectory); u = (x >> 11) * 2^-53 as src/Mitigation.h:207).
+ * Writes <Z_0> of each trajectory's final state to z0_out, and optionally the jump count per
+ * trajectory and a jump log (one byte per touched-qubit site: bit 0 amplitude-damping jump, bit 1
+ * dephasing jump; row stride log_stride >= sites).  *min_margin receives the smallest
+ * |u - survive| seen (a decision closer than rounding could go either way).  Outputs may be host
+ * or device pointers; the call blocks until they are written. */
+int llg_traj_run(int n, const llg_op* ops, int nops, double gamma_ad, double lambda_pd, uint64_t seed,
+                 uint64_t traj_begin, uint64_t n_traj, int precision, double* z0_out, uint32_t* jumps_out,
+                 uint8_t* jump_log, int64_t log_stride, double* min_margin);
+
 /* ---- tracing ----
  * Per-state kernel timing with CUDA events recorded on the state's own stream around every
  * engine launch, summed per kernel class.  Off by default (a few microseconds per launch). */

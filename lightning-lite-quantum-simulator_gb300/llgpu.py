@@ -102,6 +102,7 @@ def lib() -> ctypes.CDLL:
             "llg_adjoint_run": (i, [vp, vp, i, vp, vp, i]),
             "llg_param_shift_run": (i, [vp, vp, i, vp, vp]),
             "llg_adjoint_stream": (i, [vp, P(vp)]),
+            "llg_traj_run": (i, [i, vp, i, d, d, u64, u64, u64, i, vp, vp, vp, ctypes.c_int64, P(d)]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
@@ -373,3 +374,29 @@ class Adjoint:
         g = np.zeros((sets, self.nparams))
         check(lib().llg_param_shift_run(self._h, _ptr(p), sets, _ptr(e), _ptr(g)))
         return e, g
+
+
+# ---------------------------------------------------------------------------------------------
+# batched noisy trajectories
+# ---------------------------------------------------------------------------------------------
+def noise_sites(ops: np.ndarray) -> int:
+    """Number of touched-qubit noise sites of a circuit (each runs amplitude then phase damping)."""
+    k = np.asarray(ops["kind"])
+    two = np.isin(k, [OP_CNOT, OP_CZ]).sum()
+    mcz = sum(bin(int(m)).count("1") for m in np.asarray(ops["mask"])[k == OP_MCZ])
+    return int(len(ops) - two - (k == OP_MCZ).sum() + 2 * two + mcz)
+
+
+def traj_run(n: int, ops: np.ndarray, gamma: float, lam: float, seed: int, n_traj: int, begin: int = 0,
+             precision: str = "complex128", log: bool = False):
+    """(z0[n_traj], jumps[n_traj], jump_log[n_traj, sites] or None, min margin)."""
+    ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
+    z0 = np.zeros(n_traj)
+    jumps = np.zeros(n_traj, dtype=np.uint32)
+    sites = noise_sites(ops)
+    jl = np.zeros((n_traj, max(sites, 1)), dtype=np.uint8) if log else None
+    margin = ctypes.c_double()
+    check(lib().llg_traj_run(n, _ptr(ops) if ops.size else None, ops.size, gamma, lam, seed, begin, n_traj,
+                             PRECISIONS[precision], _ptr(z0), _ptr(jumps), _ptr(jl) if log else None,
+                             jl.shape[1] if log else 0, ctypes.byref(margin)))
+    return z0, jumps, jl, margin.value

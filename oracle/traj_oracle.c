@@ -128,11 +128,20 @@ static int kraus_site(double* psi, int n, int q, double g, int ad, double u1, do
     return 0;
 }
 
-static int touched(const orc_op* op, int qs[2]) {
+/* Touched qubits of a gate, in noise-site order: its qubit for 1-qubit gates, control then target
+ * for cnot / cz, and every listed qubit in increasing order for mcz (src/Mitigation.h:196-204
+ * puts one single-qubit site on each qubit of a gate wider than two). */
+static int touched(const orc_op* op, int qs[64]) {
     if (op->kind == ORC_OP_CNOT || op->kind == ORC_OP_CZ) {
         qs[0] = op->q0;
         qs[1] = op->q1;
         return 2;
+    }
+    if (op->kind == ORC_OP_MCZ) {
+        int k = 0;
+        for (int q = 0; q < 64; ++q)
+            if (op->mask >> q & 1) qs[k++] = q;
+        return k;
     }
     qs[0] = op->q0;
     return 1;
@@ -146,44 +155,68 @@ int orc_traj_run(int n, const orc_op* ops, int nops, double gamma_ad, double lam
                  uint8_t* jump_log, int64_t jump_log_stride, double* margin_out) {
     if (n < 1 || n > 24) return ORC_EINVAL;
     const int64_t size = 1LL << n;
-    double* psi = (double*)malloc(sizeof(double) * 2 * (size_t)size);
-    if (!psi) return ORC_ENOMEM;
-    double margin = 1.0;
-    for (uint64_t t = traj_begin; t < traj_end; ++t) {
-        orc_init_zero(psi, n);
-        uint64_t site = 0;
-        uint32_t jumps = 0;
-        for (int g = 0; g < nops; ++g) {
-            const int rc = orc_apply_op(psi, n, &ops[g]);
-            if (rc) {
-                free(psi);
-                return rc;
-            }
-            int qs[2];
-            const int nq = touched(&ops[g], qs);
-            for (int k = 0; k < nq; ++k) {
-                double p1 = p1_of(psi, n, qs[k]);
-                double u1, u2;
-                uint8_t code = 0;
-                orc_uniform_pair(seed, t, site, &u1, &u2);
-                if (kraus_site(psi, n, qs[k], gamma_ad, 1, u1, &p1, &margin)) code |= 1;
-                ++site;
-                orc_uniform_pair(seed, t, site, &u1, &u2);
-                if (kraus_site(psi, n, qs[k], lambda_pd, 0, u1, &p1, &margin)) code |= 2;
-                ++site;
-                jumps += (code & 1) + (code >> 1);
-                if (jump_log) jump_log[(int64_t)(t - traj_begin) * jump_log_stride + (int64_t)(site / 2 - 1)] = code;
-            }
-        }
-        double z = 0.0;
-        for (int64_t i = 0; i < size; ++i) {
-            const double p = psi[2 * i] * psi[2 * i] + psi[2 * i + 1] * psi[2 * i + 1];
-            z += (i & 1) ? -p : p;
-        }
-        z0_out[t - traj_begin] = z;
-        if (jump_counts) jump_counts[t - traj_begin] = jumps;
+    /* validate the circuit once, serially, on a scratch state */
+    {
+        double* scratch = (double*)malloc(sizeof(double) * 2 * (size_t)size);
+        if (!scratch) return ORC_ENOMEM;
+        orc_init_zero(scratch, n);
+        const int rc = orc_run_ops(scratch, n, ops, nops);
+        free(scratch);
+        if (rc) return rc;
     }
-    free(psi);
+    double margin = 1.0;
+    int failed = 0;
+    /* trajectories are independent: spread them over the host threads, as the reference's
+     * trajectory solver does (src/TrajectorySolver.h:211-229); each trajectory's state is small
+     * enough that its own loops run single-threaded */
+#pragma omp parallel
+    {
+        double* psi = (double*)malloc(sizeof(double) * 2 * (size_t)size);
+        double local_margin = 1.0;
+        if (!psi) {
+#pragma omp atomic write
+            failed = 1;
+        }
+#pragma omp for schedule(dynamic, 4)
+        for (int64_t tt = (int64_t)traj_begin; tt < (int64_t)traj_end; ++tt) {
+            if (!psi) continue;
+            const uint64_t t = (uint64_t)tt;
+            orc_init_zero(psi, n);
+            uint64_t site = 0;
+            uint32_t jumps = 0;
+            for (int g = 0; g < nops; ++g) {
+                orc_apply_op(psi, n, &ops[g]);
+                int qs[64];
+                const int nq = touched(&ops[g], qs);
+                for (int k = 0; k < nq; ++k) {
+                    double p1 = p1_of(psi, n, qs[k]);
+                    double u1, u2;
+                    uint8_t code = 0;
+                    orc_uniform_pair(seed, t, site, &u1, &u2);
+                    if (kraus_site(psi, n, qs[k], gamma_ad, 1, u1, &p1, &local_margin)) code |= 1;
+                    ++site;
+                    orc_uniform_pair(seed, t, site, &u1, &u2);
+                    if (kraus_site(psi, n, qs[k], lambda_pd, 0, u1, &p1, &local_margin)) code |= 2;
+                    ++site;
+                    jumps += (code & 1) + (code >> 1);
+                    if (jump_log) jump_log[(int64_t)(t - traj_begin) * jump_log_stride + (int64_t)(site / 2 - 1)] = code;
+                }
+            }
+            double z = 0.0;
+            for (int64_t i = 0; i < size; ++i) {
+                const double p = psi[2 * i] * psi[2 * i] + psi[2 * i + 1] * psi[2 * i + 1];
+                z += (i & 1) ? -p : p;
+            }
+            z0_out[t - traj_begin] = z;
+            if (jump_counts) jump_counts[t - traj_begin] = jumps;
+        }
+#pragma omp critical
+        {
+            if (local_margin < margin) margin = local_margin;
+        }
+        free(psi);
+    }
+    if (failed) return ORC_ENOMEM;
     if (margin_out) *margin_out = margin;
     return 0;
 }
@@ -270,7 +303,7 @@ int orc_density_z0(int n, const orc_op* ops, int nops, double gamma_ad, double l
             conj2(u, c);
             apply_2x2(rho, nn, n + op->q0, c);
         }
-        int qs[2];
+        int qs[64];
         const int nq = touched(op, qs);
         for (int k = 0; k < nq; ++k) {
             channel(rho, tmp, acc, n, qs[k], gamma_ad, 1);
