@@ -222,6 +222,30 @@ int llg_traj_run(int n, const llg_op* ops, int nops, double gamma_ad, double lam
                  uint64_t traj_begin, uint64_t n_traj, int precision, double* z0_out, uint32_t* jumps_out,
                  uint8_t* jump_log, int64_t log_stride, double* min_margin);
 
+/* ---- mixed-size batches ----
+ * `count` circuits (circuit c: n_qubits[c] in [1, 30], ops[op_offsets[c] .. op_offsets[c+1]))
+ * planned into shared-memory tile passes of tile_qubits qubits (0: default) and run together from
+ * |0..0> in ONE persistent launch: persistent CTAs take (circuit, pass, tile) work items from a
+ * queue; a tile waits, with a bounded poll, for the previous pass of its own circuit.  The
+ * reference runs such circuits one at a time on StateVectorBackend (src/StateVectorBackend.h). */
+typedef struct llg_batch llg_batch;
+int llg_batch_create(int count, const int* n_qubits, const llg_op* ops, const int64_t* op_offsets, int precision,
+                     int tile_qubits, llg_batch** out);
+int llg_batch_destroy(llg_batch* b);
+int llg_batch_info(const llg_batch* b, int64_t* work_items, int64_t* total_amps, int* total_passes);
+/* Reset every state to |0..0> and run all circuits; spin_limit bounds each dependency wait in
+ * polls (0: about a second).  A wait that runs out makes the call return LLG_ETIMEOUT. */
+int llg_batch_run(llg_batch* b, int64_t spin_limit);
+/* Test hook: make one work item wait for a count no tile reaches, so the next run's bounded wait
+ * runs out and reports LLG_ETIMEOUT (the kernel returns normally). */
+int llg_batch_debug_block_item(llg_batch* b, int64_t item);
+/* Amplitudes of circuit `index` as complex128 into host memory (2 * 2^n doubles). */
+int llg_batch_copy_state(llg_batch* b, int index, double* out);
+/* Per circuit: fidelity |<a|b>|^2 / (|a|^2 |b|^2) (FP64 accumulation), |a|^2, |b|^2 into
+ * out[3 * i + 0..2].  a and b hold the same circuit sizes (e.g. complex64 vs complex128 runs). */
+int llg_batch_fidelity(llg_batch* a, llg_batch* b, double* out);
+int llg_batch_stream(const llg_batch* b, void** out);
+
 /* ---- tracing ----
  * Per-state kernel timing with CUDA events recorded on the state's own stream around every
  * engine launch, summed per kernel class.  Off by default (a few microseconds per launch). */

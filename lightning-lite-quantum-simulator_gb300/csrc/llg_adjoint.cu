@@ -74,126 +74,6 @@ __global__ void k_coef_table(const double* __restrict__ params, int nparams, con
     table[2 * (size_t)idx + 1] = pack_dev<P>(s);
 }
 
-// ------------------------------------------------------------------------------------------
-// one op on a shared-memory tile (all kinds, parametrised ones read their table row)
-// ------------------------------------------------------------------------------------------
-template <class P>
-__device__ void tile_apply(typename P::S* tile, uint32_t tsize, uint64_t base, const ExecOp& o,
-                           const uint64_t* __restrict__ trow) {
-    using K = typename P::K;
-    using S = typename P::S;
-    switch (o.kind) {
-        case EX_U2: tile_pairs<P, EX_U2>(tile, tsize >> 1, o.q0, o); break;
-        case EX_RX: tile_pairs<P, EX_RX>(tile, tsize >> 1, o.q0, o); break;
-        case EX_RY: tile_pairs<P, EX_RY>(tile, tsize >> 1, o.q0, o); break;
-        case EX_H: tile_pairs<P, EX_H>(tile, tsize >> 1, o.q0, o); break;
-        case EX_X: tile_pairs<P, EX_X>(tile, tsize >> 1, o.q0, o); break;
-        case EX_RX_P:
-        case EX_RY_P: {
-            ExecOp r = o;
-            r.c[0] = trow[2 * o.q1];
-            const K s = P::k_from_bits(trow[2 * o.q1 + 1]);
-            K sv = (o.flags & OPF_ADJOINT) ? P::kneg(s) : s;
-            // re-pack the (possibly negated) sine through a local copy of the op
-            if (o.kind == EX_RX_P) {
-                PairMath<P, EX_RX> m(r);
-                m.k[1] = sv;
-                const uint32_t bit = 1u << o.q0;
-                for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += blockDim.x) {
-                    const uint32_t j0 = (uint32_t)insert0(p, o.q0), j1 = j0 | bit;
-                    auto a0 = P::load(tile[j0]);
-                    auto a1 = P::load(tile[j1]);
-                    m.apply(a0, a1);
-                    tile[j0] = P::store(a0);
-                    tile[j1] = P::store(a1);
-                }
-            } else {
-                PairMath<P, EX_RY> m(r);
-                m.k[1] = sv;
-                const uint32_t bit = 1u << o.q0;
-                for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += blockDim.x) {
-                    const uint32_t j0 = (uint32_t)insert0(p, o.q0), j1 = j0 | bit;
-                    auto a0 = P::load(tile[j0]);
-                    auto a1 = P::load(tile[j1]);
-                    m.apply(a0, a1);
-                    tile[j0] = P::store(a0);
-                    tile[j1] = P::store(a1);
-                }
-            }
-            break;
-        }
-        case EX_DIAG:
-        case EX_RZ_P: {
-            K d0r, d0i, d1r, d1i;
-            if (o.kind == EX_DIAG) {
-                d0r = P::k_from_bits(o.c[0]);
-                d0i = P::k_from_bits(o.c[1]);
-                d1r = P::k_from_bits(o.c[2]);
-                d1i = P::k_from_bits(o.c[3]);
-            } else {  // RZ(t) = diag(c - i s, c + i s); its inverse swaps the signs
-                const K c = P::k_from_bits(trow[2 * o.q1]);
-                K s = P::k_from_bits(trow[2 * o.q1 + 1]);
-                if (o.flags & OPF_ADJOINT) s = P::kneg(s);
-                d0r = c;
-                d0i = P::kneg(s);
-                d1r = c;
-                d1i = s;
-            }
-            if (o.flags & OPF_NONLOCAL_Q0) {
-                const bool one = (base >> o.q0) & 1;
-                const K dr = one ? d1r : d0r, di = one ? d1i : d0i;
-                const K mdi = P::kneg(di);
-                for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
-                    auto a = P::load(tile[l]);
-                    cmul_const<P>(a, dr, di, mdi);
-                    tile[l] = P::store(a);
-                }
-            } else {
-                const K md0i = P::kneg(d0i), md1i = P::kneg(d1i);
-                for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
-                    auto a = P::load(tile[l]);
-                    if ((l >> o.q0) & 1) cmul_const<P>(a, d1r, d1i, md1i);
-                    else cmul_const<P>(a, d0r, d0i, md0i);
-                    tile[l] = P::store(a);
-                }
-            }
-            break;
-        }
-        case EX_CNOT: {
-            const int tq = o.q1;
-            if (o.flags & OPF_NONLOCAL_Q0) {
-                if ((base >> o.q0) & 1) tile_pairs<P, EX_X>(tile, tsize >> 1, tq, o);
-            } else {
-                const int c = o.q0;
-                const int lo = c < tq ? c : tq, hi = c < tq ? tq : c;
-                const uint32_t cbit = 1u << c, tbit = 1u << tq;
-                for (uint32_t r = threadIdx.x; r < (tsize >> 2); r += blockDim.x) {
-                    const uint32_t j = (uint32_t)insert0(insert0(r, lo), hi) | cbit;
-                    const S x = tile[j];
-                    tile[j] = tile[j | tbit];
-                    tile[j | tbit] = x;
-                }
-            }
-            break;
-        }
-        case EX_MCZ: {
-            if ((base & o.nl_mask) == o.nl_mask) {
-                const uint32_t lm = (uint32_t)o.mask;
-                const uint32_t cnt = tsize >> __popc(lm);
-                for (uint32_t r = threadIdx.x; r < cnt; r += blockDim.x) {
-                    const uint32_t j = (uint32_t)insert0_mask(r, lm) | lm;
-                    auto a = P::load(tile[j]);
-                    a.re = P::neg(a.re);
-                    a.im = P::neg(a.im);
-                    tile[j] = P::store(a);
-                }
-            }
-            break;
-        }
-        default: break;
-    }
-}
-
 __device__ __forceinline__ double block_sum_d(double v, double* sh) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);

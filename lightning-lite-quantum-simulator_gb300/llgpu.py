@@ -103,6 +103,14 @@ def lib() -> ctypes.CDLL:
             "llg_param_shift_run": (i, [vp, vp, i, vp, vp]),
             "llg_adjoint_stream": (i, [vp, P(vp)]),
             "llg_traj_run": (i, [i, vp, i, d, d, u64, u64, u64, i, vp, vp, vp, ctypes.c_int64, P(d)]),
+            "llg_batch_create": (i, [i, vp, vp, vp, i, i, P(vp)]),
+            "llg_batch_destroy": (i, [vp]),
+            "llg_batch_info": (i, [vp, P(ctypes.c_int64), P(ctypes.c_int64), P(i)]),
+            "llg_batch_run": (i, [vp, ctypes.c_int64]),
+            "llg_batch_debug_block_item": (i, [vp, ctypes.c_int64]),
+            "llg_batch_copy_state": (i, [vp, i, vp]),
+            "llg_batch_fidelity": (i, [vp, vp, vp]),
+            "llg_batch_stream": (i, [vp, P(vp)]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
@@ -400,3 +408,53 @@ def traj_run(n: int, ops: np.ndarray, gamma: float, lam: float, seed: int, n_tra
                              PRECISIONS[precision], _ptr(z0), _ptr(jumps), _ptr(jl) if log else None,
                              jl.shape[1] if log else 0, ctypes.byref(margin)))
     return z0, jumps, jl, margin.value
+
+
+# ---------------------------------------------------------------------------------------------
+# mixed-size batches
+# ---------------------------------------------------------------------------------------------
+class Batch:
+    """Circuits of uneven sizes run together in one persistent launch."""
+
+    def __init__(self, n_qubits, ops: np.ndarray, offsets, precision: str = "complex128", tile_qubits: int = 0):
+        self.nq = np.ascontiguousarray(n_qubits, dtype=np.int32)
+        self._ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
+        self._off = np.ascontiguousarray(offsets, dtype=np.int64)
+        self._h = ctypes.c_void_p()
+        check(lib().llg_batch_create(self.nq.size, _ptr(self.nq), _ptr(self._ops) if self._ops.size else None,
+                                     _ptr(self._off), PRECISIONS[precision], tile_qubits, ctypes.byref(self._h)))
+
+    def close(self) -> None:
+        if self._h:
+            lib().llg_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> dict:
+        w, a, p = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int()
+        check(lib().llg_batch_info(self._h, ctypes.byref(w), ctypes.byref(a), ctypes.byref(p)))
+        return {"work_items": w.value, "total_amps": a.value, "total_passes": p.value}
+
+    def run(self, spin_limit: int = 0) -> None:
+        check(lib().llg_batch_run(self._h, spin_limit))
+
+    def state(self, index: int) -> np.ndarray:
+        out = np.empty(1 << int(self.nq[index]), dtype=np.complex128)
+        check(lib().llg_batch_copy_state(self._h, index, _ptr(out)))
+        return out
+
+    def fidelity(self, other: "Batch") -> np.ndarray:
+        out = np.zeros((self.nq.size, 3))
+        check(lib().llg_batch_fidelity(self._h, other._h, _ptr(out)))
+        return out
+
+    @property
+    def stream(self) -> int:
+        v = ctypes.c_void_p()
+        check(lib().llg_batch_stream(self._h, ctypes.byref(v)))
+        return v.value or 0
