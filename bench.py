@@ -60,6 +60,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient measurement")
+    ap.add_argument("--no-forms", action="store_true", help="skip the trajectory and mixed-batch measurements")
     return ap.parse_args()
 
 
@@ -161,7 +162,7 @@ def run_reference(args, rank, world):
     import workloads
 
     ops = workloads.layered_rotations(args.qubits, args.layers)
-    warm = max(1, min(args.warmup, 1))
+    warm = max(1, args.warmup)
     rate, threads, best, times = cpu_sample(args.qubits, ops, args.cpu_gates, args.steps, warm)
     sample = (f"first {args.cpu_gates} gates of the {args.qubits}-qubit layered circuit per step, "
               f"{args.steps} steps after {warm} warm-up; per-gate OpenMP passes of the reference algorithm")
@@ -262,6 +263,10 @@ def run_ours(args, rank, world, local):
     adj = None
     if not args.no_adjoint:
         adj = run_adjoint_bench(args, torch)
+    traj = batch = None
+    if not args.no_forms:
+        traj = run_traj_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
+        batch = run_batch_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -296,6 +301,8 @@ def run_ours(args, rank, world, local):
         "e2e": e2e,
         "cpu_baseline": cpu,
         "adjoint": adj,
+        "trajectories": traj,
+        "mixed_batch": batch,
     }
     print(json.dumps(line), flush=True)
 
@@ -355,6 +362,88 @@ def run_adjoint_bench(args, torch):
             "max_abs_grad_diff_vs_param_shift": float(np.max(np.abs(g[0] - g_ps[0]))),
             "forward_passes": info["forward_passes"], "backward_passes": info["backward_passes"],
             "precision": args.precision}
+
+
+def _timed(stream, torch, fn, reps=1):
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(reps):
+        out = fn()
+    ev1.record(stream)
+    ev1.synchronize()
+    return ev0.elapsed_time(ev1) / 1e3 / reps, out
+
+
+def run_traj_bench(args, torch, cpu: bool):
+    """4096 noisy trajectories of the 14-qubit, 8-layer RX/RY + CNOT-chain circuit with amplitude
+    damping (0.01) then dephasing (0.005) after every gate on touched qubits; complex128 and
+    complex64; the CPU figure runs the oracle's restatement of the same step on every core."""
+    import llgpu
+    import workloads
+
+    n, ntraj, gamma, lam, seed = 14, 4096, 0.01, 0.005, 2024
+    ops = workloads.noisy_layers(n, 8)
+    out = {"workload": f"{ntraj} trajectories x {n} qubits, {len(ops)} gates, {llgpu.noise_sites(ops)} noise sites "
+                       f"(amplitude damping {gamma} then dephasing {lam})"}
+    cur = torch.cuda.current_stream()
+    for prec in ("complex128", "complex64"):
+        llgpu.traj_run(n, ops, gamma, lam, seed, 256, precision=prec)
+        t0 = time.perf_counter()
+        z, j, _, _ = llgpu.traj_run(n, ops, gamma, lam, seed, ntraj, precision=prec)
+        dt = time.perf_counter() - t0
+        key = "c128" if prec == "complex128" else "c64"
+        out[key] = {"traj_per_s": ntraj / dt, "seconds": dt, "mean_z0": float(z.mean()),
+                    "std_error": float(z.std(ddof=1) / np.sqrt(ntraj)), "jumps_per_traj": float(j.mean())}
+    del cur
+    if cpu:
+        import oracle
+
+        oracle.set_threads(os.cpu_count() or 1)
+        sample = 64
+        t0 = time.perf_counter()
+        oracle.traj_run(n, ops, gamma, lam, seed, 0, sample)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": sample / dt, "unit": "traj/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"first {sample} trajectories, oracle restatement of the Kraus-jump step"}
+    return out
+
+
+def run_batch_bench(args, torch, cpu: bool):
+    """512 circuits with n uniform in 10..22 and 200 random gates each in one persistent launch;
+    complex128 and complex64 with the per-circuit fidelity of the complex64 result."""
+    import llgpu
+    import workloads
+
+    nq, ops, off = workloads.mixed_batch(512, 10, 22, 200)
+    ngates = int(off[-1])
+    res = {"workload": f"512 circuits, n in 10..22 (total {int(np.sum(2.0 ** nq))} amplitudes), 200 gates each"}
+    batches = {}
+    for prec in ("complex128", "complex64"):
+        b = llgpu.Batch(nq, ops, off, prec)
+        stream = torch.cuda.ExternalStream(b.stream)
+        b.run()
+        dt, _ = _timed(stream, torch, b.run, reps=max(1, args.steps))
+        key = "c128" if prec == "complex128" else "c64"
+        res[key] = {"circuits_per_s": 512 / dt, "gates_per_s": ngates / dt, "seconds": dt,
+                    "work_items": b.info()["work_items"]}
+        batches[key] = b
+    f = batches["c64"].fidelity(batches["c128"])
+    res["c64_fidelity_error"] = {"max": float(np.max(1 - f[:, 0])), "median": float(np.median(1 - f[:, 0]))}
+    for b in batches.values():
+        b.close()
+    if cpu:
+        import oracle
+
+        oracle.set_threads(os.cpu_count() or 1)
+        idx = list(range(0, 512, 32))  # 16 circuits spread over the batch
+        t0 = time.perf_counter()
+        for i in idx:
+            oracle.run_ops(int(nq[i]), ops[off[i]:off[i + 1]])
+        dt = time.perf_counter() - t0
+        frac = float(np.sum(2.0 ** nq[idx]) / np.sum(2.0 ** nq))  # share of the batch's work in the sample
+        res["cpu_baseline"] = {"value": 512 / (dt / frac), "unit": "circuits/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"circuits {idx[0]}..{idx[-1]} step 32, scaled to the batch by amplitude count"}
+    return res
 
 
 def run_e2e(args, ops, xops, n, elem, world, torch):
