@@ -61,6 +61,7 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient measurement")
     ap.add_argument("--no-forms", action="store_true", help="skip the trajectory and mixed-batch measurements")
+    ap.add_argument("--no-sweeps", action="store_true", help="skip the per-gate sweep roofline measurement")
     return ap.parse_args()
 
 
@@ -260,6 +261,10 @@ def run_ours(args, rank, world, local):
     if not args.no_e2e:
         e2e = run_e2e(args, ops, xops, n, elem, world, torch)
 
+    sweeps = None
+    if not args.no_sweeps:
+        sweeps = run_sweep_bench(args, torch)
+
     adj = None
     if not args.no_adjoint:
         adj = run_adjoint_bench(args, torch)
@@ -300,6 +305,7 @@ def run_ours(args, rank, world, local):
         "clocks": clk.summary(),
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "gate_sweeps": sweeps,
         "adjoint": adj,
         "trajectories": traj,
         "mixed_batch": batch,
@@ -362,6 +368,49 @@ def run_adjoint_bench(args, torch):
             "max_abs_grad_diff_vs_param_shift": float(np.max(np.abs(g[0] - g_ps[0]))),
             "forward_passes": info["forward_passes"], "backward_passes": info["backward_passes"],
             "precision": args.precision}
+
+
+def run_sweep_bench(args, torch):
+    """Per-gate streaming sweeps on the 30-qubit state (the reference's one-pass-per-gate method):
+    each gate kind on several target qubits, timed per launch with CUDA events on the engine's
+    stream.  Algorithmic bytes per sweep: 32 B x 2^n for 1-qubit gates (read + write every
+    amplitude), 16 B x 2^n for CNOT (the control = 1 half), 8 B x 2^n for CZ (one quarter)."""
+    import llgpu
+    from llgpu import OP_CNOT, OP_CZ, OP_H, OP_RX, OP_RY, OP_RZ, OP_U2, make_ops
+
+    n = args.qubits
+    peak, peak_kind = peaks()
+    u = np.array([[0.6 + 0.1j, 0.3 - 0.2j], [-0.3 - 0.2j, 0.6 - 0.1j]], dtype=complex)
+    u, _ = np.linalg.qr(u)
+    targets = [0, 5, 13, 22, n - 1]
+    kinds = {"RX": [(OP_RX, q, 0, 0.7) for q in targets], "RY": [(OP_RY, q, 0, 1.1) for q in targets],
+             "RZ": [(OP_RZ, q, 0, 0.4) for q in targets], "H": [(OP_H, q) for q in targets],
+             "U2": [(OP_U2, q, 0, 0.0, None, u.reshape(4)) for q in targets],
+             "CNOT": [(OP_CNOT, 0, n - 1), (OP_CNOT, n - 1, 0), (OP_CNOT, 12, 13), (OP_CNOT, 3, 20)],
+             "CZ": [(OP_CZ, 0, n - 1), (OP_CZ, 12, 13), (OP_CZ, 3, 20)]}
+    bytes_per = {"CNOT": 16, "CZ": 8}
+    out = {"qubits": n, "peak_gbs": peak, "peak_source": f"{peak_kind} hbm_gbs"}
+    for prec in ("complex128", "fp64"):
+        st = llgpu.State(n, prec)
+        st.set_fusion("none")
+        res = {}
+        for name, recs in kinds.items():
+            ops = make_ops(recs)
+            st.apply_ops(ops)  # warm-up
+            st.sync()
+            st.profile(True)
+            st.profile_read(reset=True)
+            for _ in range(2):
+                st.apply_ops(ops)
+            st.sync()
+            ms, cnt = st.profile_read(reset=True)["gate"]
+            st.profile(False)
+            per = ms / cnt / 1e3
+            gbs = bytes_per.get(name, 32) * (1 << n) / per / 1e9
+            res[name] = {"ms_per_sweep": per * 1e3, "gbs": gbs, "frac": gbs / peak}
+        st.close()
+        out[prec] = res
+    return out
 
 
 def _timed(stream, torch, fn, reps=1):
