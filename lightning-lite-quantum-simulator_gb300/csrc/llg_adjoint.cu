@@ -74,36 +74,23 @@ __global__ void k_coef_table(const double* __restrict__ params, int nparams, con
     table[2 * (size_t)idx + 1] = pack_dev<P>(s);
 }
 
-__device__ __forceinline__ double block_sum_d(double v, double* sh) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __syncthreads();
-    if (lane == 0) sh[warp] = v;
-    __syncthreads();
-    double r = 0.0;
-    if (threadIdx.x == 0)
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += sh[w];
-    return r;
-}
-
-// Im <lambda | P | psi> over the tile for the generator P of a parametrised op.
+// Im <lambda | P | psi> over the tile for the generator P of a parametrised op, this thread's part
+// as an accumulator (double-float for the FP32-pipe precisions; summed over the block once).
 template <class P>
-__device__ double tile_generator_inner(const typename P::S* psi, const typename P::S* lam, uint32_t tsize, uint64_t base,
-                                       const ExecOp& o) {
+__device__ typename P::Acc tile_generator_inner(const typename P::S* psi, const typename P::S* lam, uint32_t tsize,
+                                                uint64_t base, const ExecOp& o) {
     typename P::Acc pos = P::acc_zero(), neg = P::acc_zero();
     if (o.kind == EX_RZ_P) {
         if (o.flags & OPF_NONLOCAL_Q0) {
             for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x)
                 pos = P::acc_dot_im(pos, P::load(lam[l]), P::load(psi[l]));
-            const double v = P::acc_to_double(pos);
-            return ((base >> o.q0) & 1) ? -v : v;
+            return ((base >> o.q0) & 1) ? acc_minus(P::acc_zero(), pos) : pos;
         }
         for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
             if ((l >> o.q0) & 1) neg = P::acc_dot_im(neg, P::load(lam[l]), P::load(psi[l]));
             else pos = P::acc_dot_im(pos, P::load(lam[l]), P::load(psi[l]));
         }
-        return P::acc_to_double(pos) - P::acc_to_double(neg);
+        return acc_minus(pos, neg);
     }
     const uint32_t bit = 1u << o.q0;
     for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += blockDim.x) {
@@ -118,7 +105,7 @@ __device__ double tile_generator_inner(const typename P::S* psi, const typename 
             pos = P::acc_dot_im(pos, l1, p0);
         }
     }
-    return P::acc_to_double(pos) - P::acc_to_double(neg);
+    return acc_minus(pos, neg);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -157,13 +144,13 @@ __global__ void __launch_bounds__(512) k_tile_fwd(typename P::S* __restrict__ ps
 
 // batched backward tile pass over psi and lambda; gpart[b][occ][tile]
 template <class P>
-__global__ void __launch_bounds__(512) k_tile_bwd(typename P::S* __restrict__ psi_all, typename P::S* __restrict__ lam_all,
+__global__ void __launch_bounds__(512, 2) k_tile_bwd(typename P::S* __restrict__ psi_all, typename P::S* __restrict__ lam_all,
                                                   int n, PassDesc pd, const ExecOp* __restrict__ ops,
                                                   const uint64_t* __restrict__ table, int nocc, double* __restrict__ gpart,
                                                   int tiles) {
     using S = typename P::S;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ double red[16];
+    __shared__ typename P::Acc red[16];
     const int t = pd.t, low = pd.low;
     const uint32_t tsize = 1u << t, nhi = 1u << (t - low);
     S* tp = reinterpret_cast<S*>(smem_raw);
@@ -191,8 +178,8 @@ __global__ void __launch_bounds__(512) k_tile_bwd(typename P::S* __restrict__ ps
     for (int k = 0; k < pd.nops; ++k) {
         const ExecOp& o = ops[pd.op_begin + k];
         if (o.flags & OPF_GRAD) {
-            const double v = block_sum_d(tile_generator_inner<P>(tp, tl, tsize, base, o), red);
-            if (threadIdx.x == 0) gpart[((size_t)b * nocc + o.q1) * tiles + blockIdx.x] = v;
+            const auto v = block_sum_acc(tile_generator_inner<P>(tp, tl, tsize, base, o), red);
+            if (threadIdx.x == 0) gpart[((size_t)b * nocc + o.q1) * tiles + blockIdx.x] = acc_value(v);
             __syncthreads();
         }
         tile_apply<P>(tp, tsize, base, o, trow);
@@ -212,7 +199,7 @@ __global__ void __launch_bounds__(kThreads) k_energy_lambda(const typename P::S*
                                                             typename P::S* __restrict__ lam_all, int n, ZTerms z,
                                                             double* __restrict__ epart) {
     using K = typename P::K;
-    __shared__ double sh[kThreads / 32];
+    __shared__ typename P::Acc sh[kThreads / 32];
     const uint64_t b = blockIdx.y;
     const uint64_t size = 1ULL << n;
     const typename P::S* psi = psi_all + b * size;
@@ -261,8 +248,8 @@ __global__ void __launch_bounds__(kThreads) k_energy_lambda(const typename P::S*
     }
 #pragma unroll
     for (int c = 0; c < kMaxZClasses; ++c) {
-        const double v = block_sum_d(P::acc_to_double(acc[c]), sh);
-        if (threadIdx.x == 0) epart[((size_t)b * gridDim.x + blockIdx.x) * kMaxZClasses + c] = v;
+        const auto v = block_sum_acc(acc[c], sh);
+        if (threadIdx.x == 0) epart[((size_t)b * gridDim.x + blockIdx.x) * kMaxZClasses + c] = acc_value(v);
     }
 }
 

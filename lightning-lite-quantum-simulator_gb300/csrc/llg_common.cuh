@@ -248,6 +248,54 @@ struct PolDF64 {
 };
 
 // ------------------------------------------------------------------------------------------
+// reductions on the FP32 pipe: warp and block sums of double-float values.  GB300 issues FP64
+// at ~1.6 ops/clk/SM, so a warp-wide DADD holds the FP64 pipe for ~20 cycles; partial sums of
+// per-thread accumulators are therefore combined as double-float and converted once.
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ df shfl_down_df(df v, int off) {
+    return {__shfl_down_sync(0xffffffffu, v.hi, off), __shfl_down_sync(0xffffffffu, v.lo, off)};
+}
+
+__device__ __forceinline__ df warp_sum_df(df v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = df_add(v, shfl_down_df(v, off));
+    return v;
+}
+
+__device__ __forceinline__ double warp_sum_dbl(double v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    return v;
+}
+
+__device__ __forceinline__ df warp_sum_acc(df v) { return warp_sum_df(v); }
+__device__ __forceinline__ double warp_sum_acc(double v) { return warp_sum_dbl(v); }
+
+__device__ __forceinline__ df acc_plus(df a, df b) { return df_add(a, b); }
+__device__ __forceinline__ double acc_plus(double a, double b) { return a + b; }
+__device__ __forceinline__ df acc_minus(df a, df b) { return df_add(a, df_neg(b)); }
+__device__ __forceinline__ double acc_minus(double a, double b) { return a - b; }
+__device__ __forceinline__ double acc_value(df a) { return df_to_double(a); }
+__device__ __forceinline__ double acc_value(double a) { return a; }
+
+// Sum over the block of one accumulator per thread; the result is valid in thread 0.  `sh` holds
+// one entry per warp.  Starts with a barrier, so `sh` may be reused by consecutive calls.
+template <class A>
+__device__ __forceinline__ A block_sum_acc(A v, A* sh) {
+    v = warp_sum_acc(v);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    A r = v;
+    if (threadIdx.x == 0) {
+        r = sh[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = acc_plus(r, sh[w]);
+    }
+    return r;
+}
+
+// ------------------------------------------------------------------------------------------
 // index helpers
 // ------------------------------------------------------------------------------------------
 __host__ __device__ __forceinline__ uint64_t insert0(uint64_t p, int q) {

@@ -222,7 +222,7 @@ struct Traj {
 
     // sum over the group of |a|^2 for amplitudes with (global bit q) == 1 (q < 0: all), or of
     // (1 - 2 bit0)|a|^2 when z0 is set; identical in every CTA of the group
-    __device__ double reduce(int q, bool z0, double* red, double* slot) {
+    __device__ double reduce(int q, bool z0, typename P::Acc* red, typename P::Acc* slot) {
         typename P::Acc pos = P::acc_zero(), neg = P::acc_zero();
         for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x) {
             const auto a = P::load(s[l]);
@@ -234,26 +234,18 @@ struct Traj {
                 if (bit) pos = P::acc_norm(pos, a);
             }
         }
-        double v = P::acc_to_double(pos) - P::acc_to_double(neg);
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        if (lane == 0) red[warp] = v;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double t = 0.0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
-            *slot = t;
-        }
+        using A = typename P::Acc;
+        const A v = block_sum_acc(acc_minus(pos, neg), red);
+        if (threadIdx.x == 0) *slot = v;
         group_sync<CL>();
         double total;
         if (CL == 1) {
-            total = *slot;
+            total = acc_value(*slot);
         } else {
             cg::cluster_group cl = cg::this_cluster();
-            const double* s0 = cl.map_shared_rank(slot, 0);
-            const double* s1 = cl.map_shared_rank(slot, 1);
-            total = *s0 + *s1;  // the same order on both CTAs
+            const A* s0 = cl.map_shared_rank(slot, 0);
+            const A* s1 = cl.map_shared_rank(slot, 1);
+            total = acc_value(acc_plus(*s0, *s1));  // the same order on both CTAs
         }
         return total;
     }
@@ -370,8 +362,8 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
                                  uint8_t* __restrict__ jump_log, int64_t log_stride, double* __restrict__ margin_out) {
     using S = typename P::S;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ double red[32];
-    __shared__ double slot;
+    __shared__ typename P::Acc red[32];
+    __shared__ typename P::Acc slot;
     __shared__ Decision dec;
     Traj<P, CL> T;
     T.nl = (CL == 2) ? n - 1 : n;
