@@ -55,7 +55,8 @@ def parse_args():
     ap.add_argument("--qubits", type=int, default=30)
     ap.add_argument("--layers", type=int, default=20)
     ap.add_argument("--precision", default="complex128")
-    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--tile", type=int, default=-1,
+                    help="tile width in qubits; -1 (default): the autotuner picks width and CTA threads")
     ap.add_argument("--cpu-gates", type=int, default=12, help="gates in each CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -203,9 +204,17 @@ def run_ours(args, rank, world, local):
     ops = workloads.layered_rotations(n, args.layers)
     ngates = len(ops)
     st = llgpu.State(n, args.precision)
-    st.set_fusion("tile", args.tile)
-    tile_q = args.tile or (13 if args.precision == "complex64" else 12)
+    tune = None
+    if args.tile < 0:
+        # autotuner: two layers of the circuit on a scratch state, outside the timed region
+        tune = st.autotune(ops, sample_ops=2 * len(ops) // max(1, args.layers))
+    else:
+        st.set_fusion("tile", args.tile)
+    tuning = st.tuning()
+    tile_q = tuning["tile_qubits"]
     passes, xops = llgpu.plan_export(n, ops, tile_q)
+    if tuning["fuse_mode"] == "none":
+        passes = np.zeros(ngates)  # one streaming pass per gate
     elem = 8 if args.precision == "complex64" else 16
     state_bytes = elem * (1 << n)
 
@@ -249,7 +258,7 @@ def run_ours(args, rank, world, local):
     ms_step = elapsed_ms / args.steps
     value = ngates * args.steps * world / (elapsed_ms / 1e3)
 
-    tile_ms, tile_n = prof["tile"]
+    tile_ms, tile_n = prof["tile"] if prof["tile"][1] else prof["gate"]
     peak, peak_kind = peaks()
     per_launch_s = (tile_ms / tile_n) / 1e3 if tile_n else float("nan")
     achieved = state_bytes * 2 / per_launch_s / 1e9 if tile_n else None
@@ -292,6 +301,7 @@ def run_ours(args, rank, world, local):
                                f"qubit + CNOT brickwork, {ngates} gates, fused into {len(passes)} shared-memory tile "
                                f"passes of {tile_q} qubits", "qubits": n, "layers": args.layers, "gates": ngates,
                    "tile_passes": int(len(passes)), "tile_qubits": tile_q, "precision": args.precision,
+                   "fusion": tuning, "autotune": tune,
                    "l2": "inputs larger than L2 (16 GiB state), no flush needed"},
         "sweeps_per_s": len(passes) * args.steps * world / (elapsed_ms / 1e3),
         "hbm_gbs_algorithmic": len(passes) * 2 * state_bytes * args.steps * world / (elapsed_ms / 1e3) / 1e9,
@@ -434,16 +444,26 @@ def run_traj_bench(args, torch, cpu: bool):
     ops = workloads.noisy_layers(n, 8)
     out = {"workload": f"{ntraj} trajectories x {n} qubits, {len(ops)} gates, {llgpu.noise_sites(ops)} noise sites "
                        f"(amplitude damping {gamma} then dephasing {lam})"}
-    cur = torch.cuda.current_stream()
     for prec in ("complex128", "complex64"):
-        llgpu.traj_run(n, ops, gamma, lam, seed, 256, precision=prec)
+        # a handle planned once; the autotuner picks cluster split and CTA threads, and every
+        # launch replays the captured CUDA graph (outputs copied to host inside the timing)
+        h = llgpu.Traj(n, ops, gamma, lam, ntraj, prec)
+        default_cfg = h.config()
+        h.launch(seed, 256)
         t0 = time.perf_counter()
-        z, j, _, _ = llgpu.traj_run(n, ops, gamma, lam, seed, ntraj, precision=prec)
+        h.launch(seed, ntraj)
+        dt_default = time.perf_counter() - t0
+        tune = h.autotune()
+        h.launch(seed, 256)
+        t0 = time.perf_counter()
+        z, j, _ = h.launch(seed, ntraj)
         dt = time.perf_counter() - t0
         key = "c128" if prec == "complex128" else "c64"
         out[key] = {"traj_per_s": ntraj / dt, "seconds": dt, "mean_z0": float(z.mean()),
-                    "std_error": float(z.std(ddof=1) / np.sqrt(ntraj)), "jumps_per_traj": float(j.mean())}
-    del cur
+                    "std_error": float(z.std(ddof=1) / np.sqrt(ntraj)), "jumps_per_traj": float(j.mean()),
+                    "config": h.config(), "default_config": default_cfg,
+                    "default_traj_per_s": ntraj / dt_default, "autotune": tune}
+        h.close()
     if cpu:
         import oracle
 
@@ -468,13 +488,16 @@ def run_batch_bench(args, torch, cpu: bool):
     res = {"workload": f"512 circuits, n in 10..22 (total {int(np.sum(2.0 ** nq))} amplitudes), 200 gates each"}
     batches = {}
     for prec in ("complex128", "complex64"):
-        b = llgpu.Batch(nq, ops, off, prec)
+        tune = llgpu.batch_autotune(nq, ops, off, prec)  # tile width by measurement (cached)
+        b = llgpu.Batch(nq, ops, off, prec, llgpu.TUNE_AUTO)
         stream = torch.cuda.ExternalStream(b.stream)
-        b.run()
+        b.run()  # captures the CUDA graph; later runs replay it
         dt, _ = _timed(stream, torch, b.run, reps=max(1, args.steps))
         key = "c128" if prec == "complex128" else "c64"
+        info = b.info()
         res[key] = {"circuits_per_s": 512 / dt, "gates_per_s": ngates / dt, "seconds": dt,
-                    "work_items": b.info()["work_items"]}
+                    "work_items": info["work_items"], "tile_qubits": info["tile_qubits"],
+                    "autotune": tune}
         batches[key] = b
     f = batches["c64"].fidelity(batches["c128"])
     res["c64_fidelity_error"] = {"max": float(np.max(1 - f[:, 0])), "median": float(np.median(1 - f[:, 0]))}
@@ -499,6 +522,10 @@ def run_e2e(args, ops, xops, n, elem, world, torch):
     import quantum_sim_v3
 
     sv = quantum_sim_v3.StateVector(n, args.precision)
+    if args.tile < 0:
+        sv.autotune(ops, 2 * len(ops) // max(1, args.layers))  # the headline's tuning, from the cache
+    else:
+        sv.set_fusion("tile", args.tile)
     sv.apply_ops(ops)
     sv.get_numpy_view()  # allocates the pinned host mirror once
     steps = max(1, args.steps)

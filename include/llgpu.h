@@ -101,8 +101,39 @@ int llg_num_qubits(const llg_state* st, int* out);
 int llg_size(const llg_state* st, uint64_t* out);
 int llg_get_precision(const llg_state* st, int* out);
 
-/* Fusion mode for this state's queue (LLG_FUSE_*) and tile width in qubits (0 = autotuned). */
+/* Fusion mode for this state's queue (LLG_FUSE_*) and tile width in qubits (0 = the default:
+ * 12 for 16-byte amplitudes, 13 for complex64; llg_autotune picks one by measurement). */
 int llg_set_fusion(llg_state* st, int mode, int tile_qubits);
+/* Threads per CTA of the tile kernel: 0 (default: 512 for tiles of 10+ qubits, else half the
+ * tile) or a multiple of 32 in [32, 512]. */
+int llg_set_tile_threads(llg_state* st, int threads);
+/* The settings the next flush uses (tile_qubits with the default resolved). */
+int llg_get_tuning(const llg_state* st, int* fuse_mode, int* tile_qubits, int* tile_threads);
+
+/* ---- autotuning ----
+ * Fusion width and CTA shape picked by timing candidates on the device (CUDA events on the
+ * object's own stream), cached process-wide under a hash of the workload's shape (sizes, gate
+ * kinds and qubits; angles do not change the work).  No reference counterpart: the reference's
+ * cache blocking uses fixed sizes (src/StateVectorOptimized.cpp:56-78). */
+typedef struct llg_tune_result {
+    int32_t fuse_mode;   /* LLG_FUSE_NONE / LLG_FUSE_TILE (states) */
+    int32_t tile_qubits; /* fusion width: qubits per shared-memory tile */
+    int32_t cta_threads; /* threads per CTA (0: the kernel's default) */
+    int32_t cluster;     /* CTAs per trajectory (trajectories; 1 elsewhere) */
+    int32_t candidates;  /* configurations timed (0 when taken from the cache) */
+    int32_t cached;      /* 1 if the result came from the cache */
+    double best_ms;      /* the chosen configuration on the sample */
+    double default_ms;   /* the default configuration on the same sample */
+} llg_tune_result;
+#define LLG_TUNE_AUTO (-1)
+
+/* Times ops[0 .. sample_ops) (0: all) on a scratch state of st's size and precision under each
+ * candidate -- per-gate kernels; tile passes of 8..max qubits with 256 threads per CTA, and 512
+ * from 10 qubits -- and applies the fastest to st.  Needs device memory for a second state;
+ * st's amplitudes are not touched. */
+int llg_autotune(llg_state* st, const llg_op* ops, int nops, int sample_ops, llg_tune_result* out);
+/* Forget every cached tuning result. */
+void llg_tune_cache_clear(void);
 
 /* ---- gates (validated now, executed at the next flush) ---- */
 
@@ -222,16 +253,43 @@ int llg_traj_run(int n, const llg_op* ops, int nops, double gamma_ad, double lam
                  uint64_t traj_begin, uint64_t n_traj, int precision, double* z0_out, uint32_t* jumps_out,
                  uint8_t* jump_log, int64_t log_stride, double* min_margin);
 
+/* The same trajectories from a handle planned once: gates uploaded, outputs for up to max_traj
+ * trajectories, and the persistent launch captured as a CUDA graph that every llg_traj_launch
+ * replays with its own seed and trajectory range.  cluster: CTAs per trajectory (1, or 2 with the
+ * state split on its top qubit; 0: 1 when the state fits one CTA's shared memory, else 2);
+ * cta_threads: 0 for the default (half the CTA's amplitudes, at most 1024), else a multiple of 32.
+ * LLG_TUNE_AUTO in either runs llg_traj_autotune at creation. */
+typedef struct llg_traj llg_traj;
+int llg_traj_create(int n, const llg_op* ops, int nops, double gamma_ad, double lambda_pd, int precision,
+                    uint64_t max_traj, int cluster, int cta_threads, llg_traj** out);
+int llg_traj_destroy(llg_traj* h);
+/* Trajectories [traj_begin, traj_begin + n_traj), n_traj <= max_traj; outputs as llg_traj_run
+ * (no jump log); blocks until they are written. */
+int llg_traj_launch(llg_traj* h, uint64_t seed, uint64_t traj_begin, uint64_t n_traj, double* z0_out,
+                    uint32_t* jumps_out, double* min_margin);
+/* Times `sample_traj` trajectories (0: two per persistent CTA group) under each feasible
+ * (cluster, 256/512/1024 threads) and keeps the fastest (cached by the circuit's shape). */
+int llg_traj_autotune(llg_traj* h, uint64_t sample_traj, llg_tune_result* out);
+int llg_traj_config(const llg_traj* h, int* cluster, int* cta_threads, int* grid, int64_t* sites);
+int llg_traj_stream(const llg_traj* h, void** out);
+
 /* ---- mixed-size batches ----
  * `count` circuits (circuit c: n_qubits[c] in [1, 30], ops[op_offsets[c] .. op_offsets[c+1]))
- * planned into shared-memory tile passes of tile_qubits qubits (0: default) and run together from
- * |0..0> in ONE persistent launch: persistent CTAs take (circuit, pass, tile) work items from a
- * queue; a tile waits, with a bounded poll, for the previous pass of its own circuit.  The
- * reference runs such circuits one at a time on StateVectorBackend (src/StateVectorBackend.h). */
+ * planned into shared-memory tile passes of tile_qubits qubits (0: default, 12 or 13 for
+ * complex64; LLG_TUNE_AUTO: picked by llg_batch_autotune) and run together from |0..0> in ONE
+ * persistent launch: persistent CTAs take (circuit, pass, tile) work items from a queue; a tile
+ * waits, with a bounded poll, for the previous pass of its own circuit.  Each run replays a CUDA
+ * graph captured at the first run (state reset + the persistent kernel).  The reference runs such
+ * circuits one at a time on StateVectorBackend (src/StateVectorBackend.h). */
 typedef struct llg_batch llg_batch;
 int llg_batch_create(int count, const int* n_qubits, const llg_op* ops, const int64_t* op_offsets, int precision,
                      int tile_qubits, llg_batch** out);
 int llg_batch_destroy(llg_batch* b);
+/* Builds and times the batch once per tile width from 8 qubits to the maximum (one untimed run
+ * each) and returns the fastest in out->tile_qubits (cached by the batch's shape). */
+int llg_batch_autotune(int count, const int* n_qubits, const llg_op* ops, const int64_t* op_offsets, int precision,
+                       llg_tune_result* out);
+int llg_batch_config(const llg_batch* b, int* tile_qubits, int* grid, int* cta_threads);
 int llg_batch_info(const llg_batch* b, int64_t* work_items, int64_t* total_amps, int* total_passes);
 /* Reset every state to |0..0> and run all circuits; spin_limit bounds each dependency wait in
  * polls (0: about a second).  A wait that runs out makes the call return LLG_ETIMEOUT. */

@@ -198,36 +198,77 @@ struct llg_batch {
     int* d_err = nullptr;
     int grid = 0;
     size_t smem = 0;
+    // the run captured as a CUDA graph (state reset + persistent kernel), re-captured when the
+    // spin limit changes
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long graph_spin = -1;
 };
 
 namespace {
 
+// Grid and shared memory of the persistent kernel (once per batch, outside any capture).
 template <class P>
-int launch_batch(llg_batch* b, long long spin_limit) {
+int setup_batch(llg_batch* b) {
+    if (b->grid) return LLG_OK;
+    b->smem = batch_smem<P>(b->tile);
+    cudaError_t e = cudaFuncSetAttribute(k_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
+    if (e != cudaSuccess) return cuda_fail(e, "batch attributes");
+    int per_sm = 1, dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<P>, kBatchThreads, b->smem)))
+        return cuda_fail(e, "batch occupancy");
+    b->grid = std::max(1, sms * std::max(per_sm, 1));
+    return LLG_OK;
+}
+
+// Stream work of one run: every state to |0..0>, queue and counters reset, the persistent kernel.
+template <class P>
+cudaError_t enqueue_batch(llg_batch* b, long long spin_limit) {
     cudaStream_t s = b->stream;
     cudaError_t e;
-    if ((e = cudaMemsetAsync(b->d_arena, 0, b->total_amps * sizeof(typename P::S), s))) return cuda_fail(e, "batch init");
+    if ((e = cudaMemsetAsync(b->d_arena, 0, b->total_amps * sizeof(typename P::S), s))) return e;
     k_batch_init<P><<<(b->count + 255) / 256, 256, 0, s>>>(static_cast<typename P::S*>(b->d_arena), b->d_circs, b->count);
-    if ((e = cudaGetLastError())) return cuda_fail(e, "batch init");
-    if ((e = cudaMemsetAsync(b->d_next, 0, sizeof(unsigned long long), s))) return cuda_fail(e, "batch reset");
-    if ((e = cudaMemsetAsync(b->d_completed, 0, b->count * sizeof(unsigned), s))) return cuda_fail(e, "batch reset");
-    if ((e = cudaMemsetAsync(b->d_err, 0, sizeof(int), s))) return cuda_fail(e, "batch reset");
-    if (b->grid == 0) {
-        const int t = b->tile;
-        b->smem = batch_smem<P>(t);
-        if ((e = cudaFuncSetAttribute(k_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem)))
-            return cuda_fail(e, "batch attributes");
-        int per_sm = 1, dev = 0, sms = 1;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<P>, kBatchThreads, b->smem)))
-            return cuda_fail(e, "batch occupancy");
-        b->grid = std::max(1, sms * std::max(per_sm, 1));
-    }
+    if ((e = cudaGetLastError())) return e;
+    if ((e = cudaMemsetAsync(b->d_next, 0, sizeof(unsigned long long), s))) return e;
+    if ((e = cudaMemsetAsync(b->d_completed, 0, b->count * sizeof(unsigned), s))) return e;
+    if ((e = cudaMemsetAsync(b->d_err, 0, sizeof(int), s))) return e;
     k_batch<P><<<b->grid, kBatchThreads, b->smem, s>>>(static_cast<typename P::S*>(b->d_arena), b->d_circs, b->d_passes,
                                                        b->d_ops, b->d_items, (long long)b->items.size(), b->d_next,
                                                        b->d_completed, b->d_err, spin_limit);
-    if ((e = cudaGetLastError())) return cuda_fail(e, "batch kernel");
+    return cudaGetLastError();
+}
+
+void drop_graph(llg_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->graph_spin = -1;
+}
+
+template <class P>
+int launch_batch(llg_batch* b, long long spin_limit) {
+    int rc = setup_batch<P>(b);
+    if (rc) return rc;
+    cudaError_t e = cudaSuccess;
+    if (!b->exec || b->graph_spin != spin_limit) {
+        drop_graph(b);
+        e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            const cudaError_t le = enqueue_batch<P>(b, spin_limit);
+            e = cudaStreamEndCapture(b->stream, &b->graph);
+            if (le != cudaSuccess) e = le;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+        if (e != cudaSuccess) {
+            drop_graph(b);
+            return cuda_fail(e, "batch graph capture");
+        }
+        b->graph_spin = spin_limit;
+    }
+    if ((e = cudaGraphLaunch(b->exec, b->stream))) return cuda_fail(e, "batch launch");
     return LLG_OK;
 }
 
@@ -235,17 +276,8 @@ int launch_batch(llg_batch* b, long long spin_limit) {
 
 extern "C" {
 
-int llg_batch_create(int count, const int* n_qubits, const llg_op* ops, const int64_t* op_offsets, int precision,
-                     int tile_qubits, llg_batch** out) {
-    if (!out) return set_error(LLG_EINVAL, "batch_create: out is NULL");
-    *out = nullptr;
-    if (count < 1 || !n_qubits || !op_offsets || (op_offsets[count] > 0 && !ops))
-        return set_error(LLG_EINVAL, "batch_create: bad arguments");
-    if (precision != LLG_F64 && precision != LLG_DF64 && precision != LLG_F32)
-        return set_error(LLG_EINVAL, "batch_create: unknown precision");
-    const int tmax = tile_max_qubits(precision);
-    const int tile = tile_qubits > 0 ? std::min(tile_qubits, tmax) : (precision == LLG_F32 ? 13 : 12);
-    if (tile < 2) return set_error(LLG_EINVAL, "batch_create: tile_qubits too small");
+static int batch_build(int count, const int* n_qubits, const llg_op* ops, const int64_t* op_offsets, int precision,
+                       int tile, llg_batch** out) {
     llg_batch* b = new llg_batch();
     b->P = precision;
     b->count = count;
@@ -331,9 +363,104 @@ int llg_batch_create(int count, const int* n_qubits, const llg_op* ops, const in
     return LLG_OK;
 }
 
+int llg_batch_create(int count, const int* n_qubits, const llg_op* ops, const int64_t* op_offsets, int precision,
+                     int tile_qubits, llg_batch** out) {
+    if (!out) return set_error(LLG_EINVAL, "batch_create: out is NULL");
+    *out = nullptr;
+    if (count < 1 || !n_qubits || !op_offsets || (op_offsets[count] > 0 && !ops))
+        return set_error(LLG_EINVAL, "batch_create: bad arguments");
+    if (precision != LLG_F64 && precision != LLG_DF64 && precision != LLG_F32)
+        return set_error(LLG_EINVAL, "batch_create: unknown precision");
+    if (tile_qubits < LLG_TUNE_AUTO) return set_error(LLG_EINVAL, "batch_create: tile_qubits must be -1, 0 or positive");
+    const int tmax = tile_max_qubits(precision);
+    if (tile_qubits != LLG_TUNE_AUTO) {
+        const int tile = tile_qubits > 0 ? std::min(tile_qubits, tmax) : (precision == LLG_F32 ? 13 : 12);
+        if (tile < 2) return set_error(LLG_EINVAL, "batch_create: tile_qubits too small");
+        return batch_build(count, n_qubits, ops, op_offsets, precision, tile, out);
+    }
+    llg_tune_result res;
+    int rc = llg_batch_autotune(count, n_qubits, ops, op_offsets, precision, &res);
+    if (rc) return rc;
+    return batch_build(count, n_qubits, ops, op_offsets, precision, res.tile_qubits, out);
+}
+
+int llg_batch_autotune(int count, const int* n_qubits, const llg_op* ops, const int64_t* op_offsets, int precision,
+                       llg_tune_result* out) {
+    if (count < 1 || !n_qubits || !op_offsets || (op_offsets[count] > 0 && !ops) || !out)
+        return set_error(LLG_EINVAL, "batch_autotune: bad arguments");
+    if (precision != LLG_F64 && precision != LLG_DF64 && precision != LLG_F32)
+        return set_error(LLG_EINVAL, "batch_autotune: unknown precision");
+    uint64_t key = tune_hash(tune_hash(1469598103934665603ULL, 0x424154), (uint64_t)precision);
+    int nmax = 1;
+    for (int c = 0; c < count; ++c) {
+        key = tune_hash(key, (uint64_t)n_qubits[c]);
+        nmax = std::max(nmax, n_qubits[c]);
+    }
+    key = tune_hash_ops(key, ops, (int)op_offsets[count]);
+    llg_tune_result res;
+    std::memset(&res, 0, sizeof(res));
+    if (tune_cache_get(key, &res)) {
+        *out = res;
+        return LLG_OK;
+    }
+    res.fuse_mode = LLG_FUSE_TILE;
+    res.cluster = 1;
+    res.cta_threads = kBatchThreads;
+    const int tdef = precision == LLG_F32 ? 13 : 12;
+    const int tmax = std::min(tile_max_qubits(precision), std::max(nmax, 8));
+    double best = 1e300;
+    cudaEvent_t ea = nullptr, eb = nullptr;
+    cudaError_t e = cudaEventCreate(&ea);
+    if (e == cudaSuccess) e = cudaEventCreate(&eb);
+    if (e != cudaSuccess) return cuda_fail(e, "batch autotune events");
+    int rc = LLG_OK;
+    for (int t = std::min(8, tmax); t <= tmax && !rc; ++t) {
+        llg_batch* b = nullptr;
+        rc = batch_build(count, n_qubits, ops, op_offsets, precision, t, &b);
+        if (rc) break;
+        rc = llg_batch_run(b, 0);  // untimed (captures the graph)
+        if (!rc) {
+            e = cudaEventRecord(ea, b->stream);
+            if (e == cudaSuccess) {
+                rc = llg_batch_run(b, 0);
+                if (!rc) e = cudaEventRecord(eb, b->stream);
+            }
+            if (!rc && e == cudaSuccess) e = cudaEventSynchronize(eb);
+            float ms = 0.f;
+            if (!rc && e == cudaSuccess) e = cudaEventElapsedTime(&ms, ea, eb);
+            if (!rc && e != cudaSuccess) rc = cuda_fail(e, "batch autotune timing");
+            if (!rc) {
+                ++res.candidates;
+                if (t == tdef) res.default_ms = ms;
+                if (ms < best) {
+                    best = ms;
+                    res.best_ms = ms;
+                    res.tile_qubits = t;
+                }
+            }
+        }
+        llg_batch_destroy(b);
+    }
+    cudaEventDestroy(ea);
+    cudaEventDestroy(eb);
+    if (rc) return rc;
+    tune_cache_put(key, res);
+    *out = res;
+    return LLG_OK;
+}
+
+int llg_batch_config(const llg_batch* b, int* tile_qubits, int* grid, int* cta_threads) {
+    if (!b) return set_error(LLG_EINVAL, "batch_config: NULL handle");
+    if (tile_qubits) *tile_qubits = b->tile;
+    if (grid) *grid = b->grid;
+    if (cta_threads) *cta_threads = kBatchThreads;
+    return LLG_OK;
+}
+
 int llg_batch_destroy(llg_batch* b) {
     if (!b) return LLG_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
+    drop_graph(b);
     void* ptrs[] = {b->d_arena, b->d_circs, b->d_passes, b->d_ops, b->d_items, b->d_next, b->d_completed, b->d_err};
     for (void* p : ptrs)
         if (p) cudaFree(p);

@@ -49,7 +49,8 @@ struct llg_state {
     void* d_psi = nullptr;
     cudaStream_t stream = nullptr;
     int fuse_mode = LLG_FUSE_TILE;
-    int tile_qubits = 0;  // 0 = default
+    int tile_qubits = 0;   // 0 = default
+    int tile_threads = 0;  // CTA size of the tile kernel, 0 = default
     std::vector<llg_op> queue;
     // op upload
     ExecOp* d_ops = nullptr;
@@ -221,7 +222,7 @@ int run_tiles(llg_state* st, const std::vector<llg_op>& q) {
     for (const PassDesc& pd : plan.passes) {
         if (pd.nops <= 0) continue;
         rc = traced(st, LLG_PROF_TILE, 1, "tile kernel",
-                    [&] { return launch_tile_pass(st->P, st->d_psi, st->n, pd, st->d_ops, st->stream); });
+                    [&] { return launch_tile_pass(st->P, st->d_psi, st->n, pd, st->d_ops, st->tile_threads, st->stream); });
         if (rc) return rc;
     }
     return LLG_OK;
@@ -415,6 +416,24 @@ int llg_set_fusion(llg_state* st, int mode, int tile_qubits) {
     if (rc) return rc;
     st->fuse_mode = mode;
     st->tile_qubits = tile_qubits;
+    return LLG_OK;
+}
+
+int llg_set_tile_threads(llg_state* st, int threads) {
+    if (!st) return set_error(LLG_EINVAL, "llg_set_tile_threads: NULL state");
+    if (threads != 0 && (threads < 32 || threads > 512 || (threads & 31)))
+        return set_error(LLG_EINVAL, "llg_set_tile_threads: threads must be 0 or a multiple of 32 in [32, 512]");
+    int rc = llg_flush(st);
+    if (rc) return rc;
+    st->tile_threads = threads;
+    return LLG_OK;
+}
+
+int llg_get_tuning(const llg_state* st, int* fuse_mode, int* tile_qubits, int* tile_threads) {
+    if (!st) return set_error(LLG_EINVAL, "llg_get_tuning: NULL state");
+    if (fuse_mode) *fuse_mode = st->fuse_mode;
+    if (tile_qubits) *tile_qubits = st->tile_qubits > 0 ? st->tile_qubits : default_tile(st->P);
+    if (tile_threads) *tile_threads = st->tile_threads;
     return LLG_OK;
 }
 

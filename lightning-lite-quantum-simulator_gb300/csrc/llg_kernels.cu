@@ -335,7 +335,7 @@ size_t tile_smem_bytes(int t, int low) {
 }
 
 template <class P>
-cudaError_t tile_pass_t(void* vpsi, int n, const PassDesc& pd, const ExecOp* d_ops, cudaStream_t s) {
+cudaError_t tile_pass_t(void* vpsi, int n, const PassDesc& pd, const ExecOp* d_ops, int threads, cudaStream_t s) {
     static bool attr_set = false;
     const size_t smem = tile_smem_bytes<P>(pd.t, pd.low);
     if (!attr_set) {
@@ -345,7 +345,7 @@ cudaError_t tile_pass_t(void* vpsi, int n, const PassDesc& pd, const ExecOp* d_o
         attr_set = true;
     }
     const uint64_t ntiles = 1ULL << (n - pd.t);
-    const int threads = pd.t >= 10 ? 512 : (pd.t >= 6 ? (1 << (pd.t - 1)) : 32);
+    if (threads <= 0) threads = pd.t >= 10 ? 512 : (pd.t >= 6 ? (1 << (pd.t - 1)) : 32);
     k_tile<P><<<(unsigned)ntiles, threads, smem, s>>>(static_cast<typename P::S*>(vpsi), pd, d_ops);
     return cudaGetLastError();
 }
@@ -392,8 +392,8 @@ cudaError_t launch_exec_op(int P, void* psi, int n, const ExecOp& op, cudaStream
     LLG_DISPATCH(P, return exec_op_t<Pol>(psi, n, op, s));
 }
 
-cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, cudaStream_t s) {
-    LLG_DISPATCH(P, return tile_pass_t<Pol>(psi, n, pd, d_ops, s));
+cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, int threads, cudaStream_t s) {
+    LLG_DISPATCH(P, return tile_pass_t<Pol>(psi, n, pd, d_ops, threads, s));
 }
 
 cudaError_t launch_from_f64(int P, const double* src, void* dst, uint64_t count, cudaStream_t s) {

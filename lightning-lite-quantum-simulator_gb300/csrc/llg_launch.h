@@ -4,6 +4,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "../../include/llgpu.h"
 #include "llg_internal.h"
 
 namespace llg {
@@ -29,7 +30,8 @@ size_t elem_bytes(int precision);
 
 cudaError_t launch_init_basis(int P, void* psi, uint64_t size, uint64_t index, cudaStream_t s);
 cudaError_t launch_exec_op(int P, void* psi, int n, const ExecOp& op, cudaStream_t s);
-cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, cudaStream_t s);
+// threads: CTA size of the tile kernel (0: 512 for tiles of 10+ qubits, else half the tile)
+cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, int threads, cudaStream_t s);
 cudaError_t launch_from_f64(int P, const double* src, void* dst, uint64_t count, cudaStream_t s);
 cudaError_t launch_to_f64(int P, const void* src, double* dst, uint64_t count, cudaStream_t s);
 cudaError_t launch_probabilities(int P, const void* psi, double* out, uint64_t count, cudaStream_t s);
@@ -40,5 +42,11 @@ cudaError_t launch_reduce_z(int P, const void* psi, int n, const ZTerms& terms, 
                             cudaStream_t s);
 
 int tile_max_qubits(int P);
+
+// process-wide tuning cache (llg_tune.cu), keyed by an FNV-1a hash of the workload's shape
+uint64_t tune_hash(uint64_t h, uint64_t v);
+uint64_t tune_hash_ops(uint64_t h, const llg_op* ops, int nops);
+bool tune_cache_get(uint64_t key, llg_tune_result* out);
+void tune_cache_put(uint64_t key, const llg_tune_result& r);
 
 }  // namespace llg

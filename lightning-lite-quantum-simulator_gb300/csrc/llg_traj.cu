@@ -432,64 +432,188 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTrajThreads)
 }
 
 template <class P>
-int launch_traj(int n, int cl, const TrajGate* d_gates, int ngates, const KrausParams& kp, uint64_t traj_begin,
-                uint64_t n_traj, double* d_z0, uint32_t* d_jumps, uint8_t* d_log, int64_t log_stride, double* d_margin,
-                int* grid_out, cudaStream_t s) {
-    using S = typename P::S;
-    const int nl = cl == 2 ? n - 1 : n;
-    const size_t smem = ((size_t)1 << nl) * sizeof(S);
-    const int threads = std::min(kTrajThreads, std::max(32, 1 << std::max(0, nl - 1)));
-    int dev = 0, sms = 1;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaError_t e;
-    int per_sm = 1;
-    if (cl == 1) {
-        e = cudaFuncSetAttribute(k_traj1<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_traj1<P>, threads, smem);
-    } else {
-        e = cudaFuncSetAttribute(k_traj2<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_traj2<P>, threads, smem);
-    }
-    if (e != cudaSuccess) return cuda_fail(e, "trajectory kernel attributes");
-    per_sm = std::max(per_sm, 1);
-    uint64_t groups = (uint64_t)sms * per_sm / cl;
-    groups = std::max<uint64_t>(1, std::min<uint64_t>(groups, n_traj));
-    groups = std::min<uint64_t>(groups, (uint64_t)(kMaxGrid / cl));  // margin buffer holds kMaxGrid CTAs
-    const unsigned grid = (unsigned)(groups * cl);
-    *grid_out = (int)grid;
-    if (cl == 1)
-        k_traj1<P><<<grid, threads, smem, s>>>(n, d_gates, ngates, kp, traj_begin, n_traj, d_z0, d_jumps, d_log, log_stride,
-                                               d_margin);
-    else
-        k_traj2<P><<<grid, threads, smem, s>>>(n, d_gates, ngates, kp, traj_begin, n_traj, d_z0, d_jumps, d_log, log_stride,
-                                               d_margin);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "trajectory kernel");
-    return LLG_OK;
+const void* traj_kernel(int cl) {
+    return cl == 2 ? reinterpret_cast<const void*>(&k_traj2<P>) : reinterpret_cast<const void*>(&k_traj1<P>);
 }
 
-bool is_dev(const void* p) {
-    cudaPointerAttributes at;
-    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-        cudaGetLastError();
-        return false;
+template <class P>
+size_t traj_elem() {
+    return sizeof(typename P::S);
+}
+
+const void* kernel_for(int P, int cl) {
+    switch (P) {
+        case LLG_F64: return traj_kernel<PolF64>(cl);
+        case LLG_F32: return traj_kernel<PolF32>(cl);
+        default: return traj_kernel<PolDF64>(cl);
     }
-    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
 }
 
 }  // namespace
 
-extern "C" int llg_traj_run(int n, const llg_op* ops, int nops, double gamma_ad, double lambda_pd, uint64_t seed,
-                            uint64_t traj_begin, uint64_t n_traj, int precision, double* z0_out, uint32_t* jumps_out,
-                            uint8_t* jump_log, int64_t log_stride, double* min_margin) {
+// A trajectory circuit planned once: gates on the device, output buffers for up to max_traj
+// trajectories, and the persistent launch captured as a CUDA graph whose kernel-node arguments
+// (seed, first trajectory, count, log) are updated before each replay.
+struct llg_traj {
+    int n = 0, P = LLG_DF64;
+    int cl = 1, threads = 0, grid = 0;
+    size_t smem = 0;
+    int ngates = 0;
+    int64_t sites = 0;
+    KrausParams kp{};
+    uint64_t max_traj = 0;
+    uint64_t shape_key = 0;
+    TrajGate* d_gates = nullptr;
+    double* d_z0 = nullptr;
+    uint32_t* d_jumps = nullptr;
+    double* d_margin = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t node = nullptr;
+};
+
+namespace {
+
+void drop_graph(llg_traj* h) {
+    if (h->exec) cudaGraphExecDestroy(h->exec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    h->exec = nullptr;
+    h->graph = nullptr;
+    h->node = nullptr;
+}
+
+// The CTA threads a (cluster, threads) request resolves to, or 0 if it cannot run: the state
+// slice must fit shared memory, and a cross-CTA step holds at most kMaxPerThread amplitudes per
+// thread in registers.
+int resolve_threads(int n, int P, int cl, int threads, size_t* smem_out) {
+    if (cl != 1 && cl != 2) return 0;
+    if (cl == 2 && n < 2) return 0;
+    const int nl = cl == 2 ? n - 1 : n;
+    const size_t smem = ((size_t)1 << nl) * elem_bytes(P);
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (smem > (size_t)optin) return 0;
+    if (threads <= 0) threads = std::min(kTrajThreads, std::max(32, 1 << std::max(0, nl - 1)));
+    if (threads < 32 || threads > kTrajThreads || (threads & 31)) return 0;
+    if (cl == 2 && (((1u << nl) + threads - 1) / threads) > (unsigned)kMaxPerThread) return 0;
+    *smem_out = smem;
+    return threads;
+}
+
+// Sets (cluster, threads), sizes the persistent grid from the occupancy and captures the graph.
+int configure(llg_traj* h, int cl, int threads) {
+    size_t smem = 0;
+    const int th = resolve_threads(h->n, h->P, cl, threads, &smem);
+    if (!th) return set_error(LLG_EINVAL, "traj: cluster " + std::to_string(cl) + " with " + std::to_string(threads) +
+                                              " threads cannot hold a " + std::to_string(h->n) + "-qubit state");
+    const void* fn = kernel_for(h->P, cl);
+    int dev = 0, sms = 1, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, th, smem);
+    if (e != cudaSuccess) return cuda_fail(e, "trajectory kernel attributes");
+    if (per_sm < 1) return set_error(LLG_EINVAL, "traj: configuration does not fit an SM");
+    uint64_t groups = (uint64_t)sms * per_sm / cl;
+    groups = std::max<uint64_t>(1, std::min<uint64_t>(groups, h->max_traj));
+    groups = std::min<uint64_t>(groups, (uint64_t)(kMaxGrid / cl));  // margin buffer holds kMaxGrid CTAs
+    drop_graph(h);
+    h->cl = cl;
+    h->threads = th;
+    h->smem = smem;
+    h->grid = (int)(groups * cl);
+    // capture one launch; its arguments are replaced before every replay
+    int n = h->n, ngates = h->ngates;
+    uint64_t b0 = 0, c0 = 0;
+    uint8_t* lg = nullptr;
+    int64_t ls = 0;
+    void* args[] = {&n, &h->d_gates, &ngates, &h->kp, &b0, &c0, &h->d_z0, &h->d_jumps, &lg, &ls, &h->d_margin};
+    e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t le = cudaLaunchKernel(fn, dim3(h->grid), dim3(th), args, smem, h->stream);
+        e = cudaStreamEndCapture(h->stream, &h->graph);
+        if (le != cudaSuccess) e = le;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&h->exec, h->graph, 0);
+    size_t count = 1;
+    if (e == cudaSuccess) e = cudaGraphGetNodes(h->graph, &h->node, &count);
+    if (e == cudaSuccess && count != 1) return set_error(LLG_ECUDA, "traj: captured graph has an unexpected shape");
+    if (e != cudaSuccess) {
+        drop_graph(h);
+        return cuda_fail(e, "trajectory graph capture");
+    }
+    return LLG_OK;
+}
+
+// Replays the graph for trajectories [begin, begin + count) (outputs stay on the device).
+int replay(llg_traj* h, uint64_t seed, uint64_t begin, uint64_t count, uint8_t* d_log, int64_t log_stride) {
+    int n = h->n, ngates = h->ngates;
+    KrausParams kp = h->kp;
+    kp.seed = seed;
+    void* args[] = {&n, &h->d_gates, &ngates, &kp, &begin, &count, &h->d_z0, &h->d_jumps, &d_log, &log_stride, &h->d_margin};
+    cudaKernelNodeParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.func = const_cast<void*>(kernel_for(h->P, h->cl));
+    p.gridDim = dim3(h->grid);
+    p.blockDim = dim3(h->threads);
+    p.sharedMemBytes = (unsigned)h->smem;
+    p.kernelParams = args;
+    cudaError_t e = cudaGraphExecKernelNodeSetParams(h->exec, h->node, &p);
+    if (e == cudaSuccess) e = cudaGraphLaunch(h->exec, h->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "trajectory launch");
+    return LLG_OK;
+}
+
+int collect(llg_traj* h, uint64_t count, double* z0_out, uint32_t* jumps_out, double* min_margin) {
+    cudaError_t e = cudaSuccess;
+    if (z0_out) e = cudaMemcpyAsync(z0_out, h->d_z0, count * sizeof(double), cudaMemcpyDefault, h->stream);
+    if (e == cudaSuccess && jumps_out)
+        e = cudaMemcpyAsync(jumps_out, h->d_jumps, count * sizeof(uint32_t), cudaMemcpyDefault, h->stream);
+    std::vector<double> margins(min_margin ? h->grid : 0);
+    if (e == cudaSuccess && min_margin)
+        e = cudaMemcpyAsync(margins.data(), h->d_margin, h->grid * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "trajectory kernel");
+    if (min_margin) {
+        double m = 1.0;
+        for (double v : margins) m = std::min(m, v);
+        *min_margin = m;
+    }
+    return LLG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int llg_traj_destroy(llg_traj* h) {
+    if (!h) return LLG_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    drop_graph(h);
+    cudaFree(h->d_gates);
+    cudaFree(h->d_z0);
+    cudaFree(h->d_jumps);
+    cudaFree(h->d_margin);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return LLG_OK;
+}
+
+int llg_traj_create(int n, const llg_op* ops, int nops, double gamma_ad, double lambda_pd, int precision,
+                    uint64_t max_traj, int cluster, int cta_threads, llg_traj** out) {
+    if (!out) return set_error(LLG_EINVAL, "traj_create: out is NULL");
+    *out = nullptr;
     if (n < 1 || n > 14) return set_error(LLG_EINVAL, "traj_run: n must be in [1, 14]");
     if (precision != LLG_F64 && precision != LLG_DF64 && precision != LLG_F32)
         return set_error(LLG_EINVAL, "traj_run: unknown precision");
-    if (nops < 0 || (nops > 0 && !ops) || !z0_out) return set_error(LLG_EINVAL, "traj_run: NULL argument");
+    if (nops < 0 || (nops > 0 && !ops)) return set_error(LLG_EINVAL, "traj_run: NULL argument");
     if (!(gamma_ad >= 0.0 && gamma_ad <= 1.0) || !(lambda_pd >= 0.0 && lambda_pd <= 1.0))
         return set_error(LLG_EINVAL, "traj_run: gamma and lambda must be in [0, 1]");
-    if (n_traj == 0) return LLG_OK;
+    if (max_traj == 0) return set_error(LLG_EINVAL, "traj_create: max_traj must be positive");
+    if (cluster < LLG_TUNE_AUTO || cluster > 2 || cta_threads < LLG_TUNE_AUTO)
+        return set_error(LLG_EINVAL, "traj_create: cluster must be -1, 0, 1 or 2 and cta_threads >= -1");
     // lower the gates with global qubits and record the touched qubits of each
     std::vector<TrajGate> gates;
     gates.reserve(nops);
@@ -513,9 +637,9 @@ extern "C" int llg_traj_run(int n, const llg_op* ops, int nops, double gamma_ad,
             g.q[0] = o.q0;
             g.q[1] = o.q1;
         } else if (o.kind == LLG_OP_MCZ) {
+            if (__builtin_popcountll(o.mask) > 6) return set_error(LLG_EINVAL, "traj_run: mcz on more than 6 qubits");
             for (int q = 0; q < n && g.nt < 6; ++q)
                 if ((o.mask >> q) & 1) g.q[g.nt++] = q;
-            if (__builtin_popcountll(o.mask) > 6) return set_error(LLG_EINVAL, "traj_run: mcz on more than 6 qubits");
         } else {
             g.nt = 1;
             g.q[0] = o.q0;
@@ -523,79 +647,171 @@ extern "C" int llg_traj_run(int n, const llg_op* ops, int nops, double gamma_ad,
         sites += g.nt;
         gates.push_back(g);
     }
-    if (jump_log && log_stride < sites) return set_error(LLG_EINVAL, "traj_run: log_stride smaller than the site count");
-    const int cl = (precision != LLG_F32 && n == 14) ? 2 : 1;
-    KrausParams kp;
-    kp.gamma = gamma_ad;
-    kp.lambda = lambda_pd;
-    kp.sq1mg = std::sqrt(1.0 - gamma_ad);
-    kp.sq1ml = std::sqrt(1.0 - lambda_pd);
-    kp.seed = seed;
-
-    TrajGate* d_gates = nullptr;
-    double *d_z0 = nullptr, *d_margin = nullptr;
-    uint32_t* d_jumps = nullptr;
-    uint8_t* d_log = nullptr;
-    cudaStream_t s = nullptr;
+    llg_traj* h = new llg_traj();
+    h->n = n;
+    h->P = precision;
+    h->ngates = (int)gates.size();
+    h->sites = sites;
+    h->max_traj = max_traj;
+    h->kp.gamma = gamma_ad;
+    h->kp.lambda = lambda_pd;
+    h->kp.sq1mg = std::sqrt(1.0 - gamma_ad);
+    h->kp.sq1ml = std::sqrt(1.0 - lambda_pd);
+    h->kp.seed = 0;
+    h->shape_key = tune_hash_ops(tune_hash(tune_hash(1469598103934665603ULL, 0x54524a), (uint64_t)n << 8 | (uint64_t)precision),
+                                 ops, nops);
     int rc = LLG_OK;
-    auto fail = [&](cudaError_t e, const char* what) {
-        rc = cuda_fail(e, what);
-    };
-    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-    if (e) fail(e, "cudaStreamCreate");
-    const bool z_dev = is_dev(z0_out);
-    if (!rc && (e = cudaMalloc(&d_gates, std::max<size_t>(gates.size(), 1) * sizeof(TrajGate)))) fail(e, "cudaMalloc");
-    if (!rc && !z_dev && (e = cudaMalloc(&d_z0, n_traj * sizeof(double)))) fail(e, "cudaMalloc");
-    if (!rc && jumps_out && (e = cudaMalloc(&d_jumps, n_traj * sizeof(uint32_t)))) fail(e, "cudaMalloc");
-    if (!rc && jump_log && (e = cudaMalloc(&d_log, n_traj * (size_t)log_stride))) fail(e, "cudaMalloc");
-    if (!rc && (e = cudaMalloc(&d_margin, kMaxGrid * sizeof(double)))) fail(e, "cudaMalloc");
-    if (!rc && !gates.empty() &&
-        (e = cudaMemcpyAsync(d_gates, gates.data(), gates.size() * sizeof(TrajGate), cudaMemcpyHostToDevice, s)))
-        fail(e, "gate upload");
-    int grid = 0;
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_gates, std::max<size_t>(gates.size(), 1) * sizeof(TrajGate));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_z0, max_traj * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_jumps, max_traj * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_margin, kMaxGrid * sizeof(double));
+    if (e == cudaSuccess && !gates.empty())
+        e = cudaMemcpy(h->d_gates, gates.data(), gates.size() * sizeof(TrajGate), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        rc = set_error(LLG_ENOMEM, std::string("traj_create: ") + cudaGetErrorString(e));
+    }
     if (!rc) {
-        double* zt = z_dev ? z0_out : d_z0;
-        switch (precision) {
-            case LLG_F64:
-                rc = launch_traj<PolF64>(n, cl, d_gates, (int)gates.size(), kp, traj_begin, n_traj, zt, d_jumps, d_log,
-                                         log_stride, d_margin, &grid, s);
-                break;
-            case LLG_F32:
-                rc = launch_traj<PolF32>(n, cl, d_gates, (int)gates.size(), kp, traj_begin, n_traj, zt, d_jumps, d_log,
-                                         log_stride, d_margin, &grid, s);
-                break;
-            default:
-                rc = launch_traj<PolDF64>(n, cl, d_gates, (int)gates.size(), kp, traj_begin, n_traj, zt, d_jumps, d_log,
-                                          log_stride, d_margin, &grid, s);
+        // default: one CTA per trajectory, a 2-CTA cluster when the state does not fit one CTA
+        size_t smem = 0;
+        const int cl_default = resolve_threads(n, precision, 1, 0, &smem) ? 1 : 2;
+        const int cl = cluster > 0 ? cluster : cl_default;
+        rc = configure(h, cl, cta_threads > 0 ? cta_threads : 0);
+        if (!rc && (cluster == LLG_TUNE_AUTO || cta_threads == LLG_TUNE_AUTO)) rc = llg_traj_autotune(h, 0, nullptr);
+    }
+    if (rc) {
+        llg_traj_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return LLG_OK;
+}
+
+int llg_traj_launch(llg_traj* h, uint64_t seed, uint64_t traj_begin, uint64_t n_traj, double* z0_out, uint32_t* jumps_out,
+                    double* min_margin) {
+    if (!h) return set_error(LLG_EINVAL, "traj_launch: NULL handle");
+    if (n_traj > h->max_traj) return set_error(LLG_EINVAL, "traj_launch: n_traj exceeds the handle's max_traj");
+    if (n_traj == 0) return LLG_OK;
+    int rc = replay(h, seed, traj_begin, n_traj, nullptr, 0);
+    if (rc) return rc;
+    return collect(h, n_traj, z0_out, jumps_out, min_margin);
+}
+
+int llg_traj_config(const llg_traj* h, int* cluster, int* cta_threads, int* grid, int64_t* sites) {
+    if (!h) return set_error(LLG_EINVAL, "traj_config: NULL handle");
+    if (cluster) *cluster = h->cl;
+    if (cta_threads) *cta_threads = h->threads;
+    if (grid) *grid = h->grid;
+    if (sites) *sites = h->sites;
+    return LLG_OK;
+}
+
+int llg_traj_stream(const llg_traj* h, void** out) {
+    if (!h || !out) return set_error(LLG_EINVAL, "traj_stream: NULL argument");
+    *out = h->stream;
+    return LLG_OK;
+}
+
+int llg_traj_autotune(llg_traj* h, uint64_t sample_traj, llg_tune_result* out) {
+    if (!h) return set_error(LLG_EINVAL, "traj_autotune: NULL handle");
+    llg_tune_result res;
+    std::memset(&res, 0, sizeof(res));
+    const int cl0 = h->cl, th0 = h->threads;
+    if (!tune_cache_get(h->shape_key, &res)) {
+        const uint64_t sample = std::min<uint64_t>(h->max_traj, sample_traj > 0 ? sample_traj : 2ULL * (h->grid / h->cl));
+        cudaEvent_t a = nullptr, b = nullptr;
+        cudaError_t e = cudaEventCreate(&a);
+        if (e == cudaSuccess) e = cudaEventCreate(&b);
+        if (e != cudaSuccess) return cuda_fail(e, "traj autotune events");
+        auto time_it = [&](double* ms) -> int {
+            int rc = replay(h, 0, 0, sample, nullptr, 0);  // untimed
+            if (rc) return rc;
+            cudaError_t ee = cudaEventRecord(a, h->stream);
+            if (ee == cudaSuccess) {
+                rc = replay(h, 0, 0, sample, nullptr, 0);
+                if (rc) return rc;
+                ee = cudaEventRecord(b, h->stream);
+            }
+            if (ee == cudaSuccess) ee = cudaEventSynchronize(b);
+            float t = 0.f;
+            if (ee == cudaSuccess) ee = cudaEventElapsedTime(&t, a, b);
+            if (ee != cudaSuccess) return cuda_fail(ee, "traj autotune timing");
+            *ms = t;
+            return LLG_OK;
+        };
+        int rc = time_it(&res.default_ms);
+        double best = 1e300;
+        int best_cl = cl0, best_th = th0;
+        for (int cl = 1; cl <= 2 && !rc; ++cl) {
+            for (int th : {256, 512, 1024}) {
+                size_t smem = 0;
+                if (resolve_threads(h->n, h->P, cl, th, &smem) != th) continue;
+                if (th > std::max(32, 1 << std::max(0, (cl == 2 ? h->n - 1 : h->n) - 1))) continue;
+                rc = configure(h, cl, th);
+                double ms = 0.0;
+                if (!rc) rc = time_it(&ms);
+                if (rc) break;
+                ++res.candidates;
+                if (ms < best) {
+                    best = ms;
+                    best_cl = cl;
+                    best_th = th;
+                    res.best_ms = ms;
+                }
+            }
         }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        if (rc) {
+            configure(h, cl0, th0);
+            return rc;
+        }
+        res.cluster = best_cl;
+        res.cta_threads = best_th;
+        res.tile_qubits = h->cl == 2 ? h->n - 1 : h->n;
+        res.fuse_mode = LLG_FUSE_TILE;
+        tune_cache_put(h->shape_key, res);
     }
-    std::vector<double> margins;
-    if (!rc && !z_dev && (e = cudaMemcpyAsync(z0_out, d_z0, n_traj * sizeof(double), cudaMemcpyDeviceToHost, s)))
-        fail(e, "z0 copy");
-    if (!rc && jumps_out &&
-        (e = cudaMemcpyAsync(jumps_out, d_jumps, n_traj * sizeof(uint32_t),
-                             is_dev(jumps_out) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s)))
-        fail(e, "jumps copy");
-    if (!rc && jump_log &&
-        (e = cudaMemcpyAsync(jump_log, d_log, n_traj * (size_t)log_stride,
-                             is_dev(jump_log) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s)))
-        fail(e, "log copy");
-    if (!rc && min_margin) {
-        margins.resize(grid);
-        if ((e = cudaMemcpyAsync(margins.data(), d_margin, grid * sizeof(double), cudaMemcpyDeviceToHost, s)))
-            fail(e, "margin copy");
+    int rc = configure(h, res.cluster, res.cta_threads);
+    if (rc) return rc;
+    res.tile_qubits = h->cl == 2 ? h->n - 1 : h->n;
+    if (out) *out = res;
+    return LLG_OK;
+}
+
+int llg_traj_run(int n, const llg_op* ops, int nops, double gamma_ad, double lambda_pd, uint64_t seed, uint64_t traj_begin,
+                 uint64_t n_traj, int precision, double* z0_out, uint32_t* jumps_out, uint8_t* jump_log, int64_t log_stride,
+                 double* min_margin) {
+    if (!z0_out) return set_error(LLG_EINVAL, "traj_run: NULL argument");
+    if (n_traj == 0) {
+        // validate the arguments all the same
+        llg_traj* h = nullptr;
+        int rc = llg_traj_create(n, ops, nops, gamma_ad, lambda_pd, precision, 1, 0, 0, &h);
+        llg_traj_destroy(h);
+        return rc;
     }
-    if (!rc && (e = cudaStreamSynchronize(s))) fail(e, "trajectory kernel");
-    if (!rc && min_margin) {
-        double m = 1.0;
-        for (double v : margins) m = std::min(m, v);
-        *min_margin = m;
+    llg_traj* h = nullptr;
+    int rc = llg_traj_create(n, ops, nops, gamma_ad, lambda_pd, precision, n_traj, 0, 0, &h);
+    if (rc) return rc;
+    uint8_t* d_log = nullptr;
+    if (jump_log && log_stride < h->sites) rc = set_error(LLG_EINVAL, "traj_run: log_stride smaller than the site count");
+    if (!rc && jump_log) {
+        cudaError_t e = cudaMalloc(&d_log, n_traj * (size_t)log_stride);
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaMalloc(jump log)");
     }
-    cudaFree(d_gates);
-    cudaFree(d_z0);
-    cudaFree(d_jumps);
-    cudaFree(d_log);
-    cudaFree(d_margin);
-    if (s) cudaStreamDestroy(s);
+    if (!rc) rc = replay(h, seed, traj_begin, n_traj, d_log, jump_log ? log_stride : 0);
+    if (!rc && jump_log) {
+        cudaError_t e = cudaMemcpyAsync(jump_log, d_log, n_traj * (size_t)log_stride, cudaMemcpyDefault, h->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "jump log copy");
+    }
+    if (!rc) rc = collect(h, n_traj, z0_out, jumps_out, min_margin);
+    if (d_log) {
+        cudaStreamSynchronize(h->stream);
+        cudaFree(d_log);
+    }
+    llg_traj_destroy(h);
     return rc;
 }
+
+}  // extern "C"

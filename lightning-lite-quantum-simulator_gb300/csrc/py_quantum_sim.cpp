@@ -171,6 +171,24 @@ public:
         check(llg_set_fusion(st_, m, tile_qubits));
     }
 
+    // picks fusion mode, tile width and CTA threads by timing ops[:sample_ops] on a scratch state
+    py::dict autotune(py::array ops, int sample_ops) {
+        if (ops.itemsize() * ops.size() % (py::ssize_t)sizeof(llg_op) != 0 || !(ops.flags() & py::array::c_style))
+            throw py::type_error("autotune needs a C-contiguous array of llg_op records");
+        const int n = (int)(ops.itemsize() * ops.size() / (py::ssize_t)sizeof(llg_op));
+        llg_tune_result r;
+        check(llg_autotune(st_, static_cast<const llg_op*>(ops.data()), n, sample_ops, &r));
+        py::dict d;
+        d["fuse_mode"] = r.fuse_mode == LLG_FUSE_TILE ? "tile" : "none";
+        d["tile_qubits"] = r.tile_qubits;
+        d["cta_threads"] = r.cta_threads;
+        d["candidates"] = r.candidates;
+        d["cached"] = r.cached;
+        d["best_ms"] = r.best_ms;
+        d["default_ms"] = r.default_ms;
+        return d;
+    }
+
     void flush() { check(llg_flush(st_)); }
 
     // Copy amplitudes into the host mirror (or the caller's array) and return a view of it.
@@ -325,6 +343,7 @@ PYBIND11_MODULE(quantum_sim_v3, m) {
         .def("apply_fused", &StateVector::apply_fused)
         .def("apply_ops", &StateVector::apply_ops)
         .def("set_fusion", &StateVector::set_fusion, py::arg("mode"), py::arg("tile_qubits") = 0)
+        .def("autotune", &StateVector::autotune, py::arg("ops"), py::arg("sample_ops") = 0)
         .def("flush", &StateVector::flush)
         .def("sync", &StateVector::sync)
         .def("push", &StateVector::push)

@@ -46,6 +46,20 @@ class LLGError(RuntimeError):
     pass
 
 
+TUNE_AUTO = -1
+TUNE_DTYPE = np.dtype([("fuse_mode", np.int32), ("tile_qubits", np.int32), ("cta_threads", np.int32),
+                       ("cluster", np.int32), ("candidates", np.int32), ("cached", np.int32),
+                       ("best_ms", np.float64), ("default_ms", np.float64)])
+
+
+def _tune_dict(r: np.ndarray) -> dict:
+    return {k: (float(r[k][0]) if r.dtype[k].kind == "f" else int(r[k][0])) for k in r.dtype.names}
+
+
+def tune_cache_clear() -> None:
+    lib().llg_tune_cache_clear()
+
+
 _lib = None
 
 
@@ -111,6 +125,18 @@ def lib() -> ctypes.CDLL:
             "llg_batch_copy_state": (i, [vp, i, vp]),
             "llg_batch_fidelity": (i, [vp, vp, vp]),
             "llg_batch_stream": (i, [vp, P(vp)]),
+            "llg_batch_autotune": (i, [i, vp, vp, vp, i, vp]),
+            "llg_batch_config": (i, [vp, P(i), P(i), P(i)]),
+            "llg_set_tile_threads": (i, [vp, i]),
+            "llg_get_tuning": (i, [vp, P(i), P(i), P(i)]),
+            "llg_autotune": (i, [vp, vp, i, i, vp]),
+            "llg_tune_cache_clear": (None, []),
+            "llg_traj_create": (i, [i, vp, i, d, d, i, u64, i, i, P(vp)]),
+            "llg_traj_destroy": (i, [vp]),
+            "llg_traj_launch": (i, [vp, u64, u64, u64, vp, vp, P(d)]),
+            "llg_traj_autotune": (i, [vp, u64, vp]),
+            "llg_traj_config": (i, [vp, P(i), P(i), P(i), P(ctypes.c_int64)]),
+            "llg_traj_stream": (i, [vp, P(vp)]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
@@ -218,6 +244,23 @@ class State:
 
     def set_fusion(self, mode: str = "tile", tile_qubits: int = 0) -> None:
         check(lib().llg_set_fusion(self._h, LLG_FUSE_TILE if mode == "tile" else LLG_FUSE_NONE, tile_qubits))
+
+    def set_tile_threads(self, threads: int) -> None:
+        check(lib().llg_set_tile_threads(self._h, threads))
+
+    def tuning(self) -> dict:
+        m, t, th = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(lib().llg_get_tuning(self._h, ctypes.byref(m), ctypes.byref(t), ctypes.byref(th)))
+        return {"fuse_mode": "tile" if m.value == LLG_FUSE_TILE else "none", "tile_qubits": t.value,
+                "cta_threads": th.value}
+
+    def autotune(self, ops: np.ndarray, sample_ops: int = 0) -> dict:
+        """Time candidate (fusion mode, tile width, CTA threads) settings on a scratch state with
+        ops[:sample_ops] and keep the fastest for this state."""
+        ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
+        r = np.zeros(1, dtype=TUNE_DTYPE)
+        check(lib().llg_autotune(self._h, _ptr(ops) if ops.size else None, ops.size, sample_ops, _ptr(r)))
+        return _tune_dict(r)
 
     def apply_gate(self, target: int, gate) -> None:
         g = np.asarray(gate, dtype=np.complex128).reshape(4)
@@ -410,9 +453,66 @@ def traj_run(n: int, ops: np.ndarray, gamma: float, lam: float, seed: int, n_tra
     return z0, jumps, jl, margin.value
 
 
+class Traj:
+    """A trajectory circuit planned once; every launch replays its captured CUDA graph."""
+
+    def __init__(self, n: int, ops: np.ndarray, gamma: float, lam: float, max_traj: int,
+                 precision: str = "complex128", cluster: int = 0, cta_threads: int = 0):
+        self._ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
+        self._h = ctypes.c_void_p()
+        self.max_traj = int(max_traj)
+        check(lib().llg_traj_create(n, _ptr(self._ops) if self._ops.size else None, self._ops.size, gamma, lam,
+                                    PRECISIONS[precision], self.max_traj, cluster, cta_threads, ctypes.byref(self._h)))
+
+    def launch(self, seed: int, n_traj: int, begin: int = 0):
+        """(z0[n_traj], jumps[n_traj], min margin)."""
+        z0 = np.zeros(n_traj)
+        jumps = np.zeros(n_traj, dtype=np.uint32)
+        margin = ctypes.c_double()
+        check(lib().llg_traj_launch(self._h, seed, begin, n_traj, _ptr(z0), _ptr(jumps), ctypes.byref(margin)))
+        return z0, jumps, margin.value
+
+    def autotune(self, sample_traj: int = 0) -> dict:
+        r = np.zeros(1, dtype=TUNE_DTYPE)
+        check(lib().llg_traj_autotune(self._h, sample_traj, _ptr(r)))
+        return _tune_dict(r)
+
+    def config(self) -> dict:
+        c, t, g, s = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int64()
+        check(lib().llg_traj_config(self._h, ctypes.byref(c), ctypes.byref(t), ctypes.byref(g), ctypes.byref(s)))
+        return {"cluster": c.value, "cta_threads": t.value, "grid": g.value, "sites": s.value}
+
+    @property
+    def stream(self) -> int:
+        v = ctypes.c_void_p()
+        check(lib().llg_traj_stream(self._h, ctypes.byref(v)))
+        return v.value or 0
+
+    def close(self) -> None:
+        if self._h:
+            lib().llg_traj_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # ---------------------------------------------------------------------------------------------
 # mixed-size batches
 # ---------------------------------------------------------------------------------------------
+def batch_autotune(n_qubits, ops: np.ndarray, offsets, precision: str = "complex128") -> dict:
+    nq = np.ascontiguousarray(n_qubits, dtype=np.int32)
+    ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
+    off = np.ascontiguousarray(offsets, dtype=np.int64)
+    r = np.zeros(1, dtype=TUNE_DTYPE)
+    check(lib().llg_batch_autotune(nq.size, _ptr(nq), _ptr(ops) if ops.size else None, _ptr(off),
+                                   PRECISIONS[precision], _ptr(r)))
+    return _tune_dict(r)
+
+
 class Batch:
     """Circuits of uneven sizes run together in one persistent launch."""
 
@@ -438,7 +538,10 @@ class Batch:
     def info(self) -> dict:
         w, a, p = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int()
         check(lib().llg_batch_info(self._h, ctypes.byref(w), ctypes.byref(a), ctypes.byref(p)))
-        return {"work_items": w.value, "total_amps": a.value, "total_passes": p.value}
+        t, g, th = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(lib().llg_batch_config(self._h, ctypes.byref(t), ctypes.byref(g), ctypes.byref(th)))
+        return {"work_items": w.value, "total_amps": a.value, "total_passes": p.value, "tile_qubits": t.value,
+                "grid": g.value, "cta_threads": th.value}
 
     def run(self, spin_limit: int = 0) -> None:
         check(lib().llg_batch_run(self._h, spin_limit))
