@@ -57,6 +57,7 @@ def parse_args():
     ap.add_argument("--precision", default="complex128")
     ap.add_argument("--tile", type=int, default=-1,
                     help="tile width in qubits; -1 (default): the autotuner picks width and CTA threads")
+    ap.add_argument("--cta-threads", type=int, default=0, help="tile-kernel CTA threads with an explicit --tile")
     ap.add_argument("--cpu-gates", type=int, default=12, help="gates in each CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -210,6 +211,7 @@ def run_ours(args, rank, world, local):
         tune = st.autotune(ops, sample_ops=2 * len(ops) // max(1, args.layers))
     else:
         st.set_fusion("tile", args.tile)
+        st.set_tile_threads(args.cta_threads)
     tuning = st.tuning()
     tile_q = tuning["tile_qubits"]
     passes, xops = llgpu.plan_export(n, ops, tile_q)
@@ -291,6 +293,7 @@ def run_ours(args, rank, world, local):
 
     if rank != 0:
         return
+    clocks = clk.summary()
     line = {
         "metric": METRIC, "value": value, "unit": "gates/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -310,9 +313,11 @@ def run_ours(args, rank, world, local):
                      "kernel": "k_tile<PolDF64> (tile pass)", "launches": tile_n,
                      "mean_launch_ms": tile_ms / tile_n if tile_n else None,
                      "peak_source": f"{peak_kind} hbm_gbs"},
+        "compute_roofline": compute_roofline(args.precision, n, xops if tuning["fuse_mode"] == "tile" else [],
+                                             prof["tile"][0] / args.steps, (clocks or {}).get("sm_mhz")),
         "kernel_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()},
         "gpu_launches": launches,
-        "clocks": clk.summary(),
+        "clocks": clocks,
         "e2e": e2e,
         "cpu_baseline": cpu,
         "gate_sweeps": sweeps,
@@ -321,6 +326,32 @@ def run_ours(args, rank, world, local):
         "mixed_batch": batch,
     }
     print(json.dumps(line), flush=True)
+
+
+# FP32 lane instructions per amplitude pair of each executor op kind (0 U2, 1 RX, 2 RY, 3 H, 4 X,
+# 5 DIAG, 6 CNOT, 7 MCZ), counted from the double-float routines of the kernels: a 4-term
+# double-float dot product (df_lin4) is 43 instructions (4 FMUL + 4 FFMA product errors, 3 TwoSum
+# of 6, 8 FFMA cross terms, 6 FADD, Fast2Sum of 3), a 2-term one (df_lin2) 19; a U2 pair needs four
+# 4-term products, RX/RY/H four 2-term ones, a diagonal two 2-term ones per amplitude.  CNOT, MCZ
+# and X move or negate data without arithmetic.
+FP32_INST_PER_PAIR = {"complex128": {0: 172, 1: 76, 2: 76, 3: 76, 4: 0, 5: 76, 6: 0, 7: 0},
+                      "complex64": {0: 16, 1: 8, 2: 8, 3: 8, 4: 0, 5: 8, 6: 0, 7: 0}}
+SMS, FP32_LANES_PER_SM = 152, 128
+
+
+def compute_roofline(precision, n, xops, tile_ms_step, sm_mhz):
+    """FP32-issue roofline of the tile passes: algorithmic FP32 lane instructions per step over
+    the measured tile-pass time, against 152 SMs x 128 lanes x the sampled SM clock."""
+    table = FP32_INST_PER_PAIR.get(precision)
+    if table is None or not tile_ms_step or not len(xops):
+        return None
+    per_pair = sum(table.get(int(k), 0) for k in xops["kind"])
+    inst = per_pair * float(1 << (n - 1))
+    achieved = inst / (tile_ms_step / 1e3) / 1e12
+    mhz = sm_mhz or 2070.0
+    peak = SMS * FP32_LANES_PER_SM * mhz * 1e6 / 1e12
+    return {"bound": "fp32_issue", "achieved": achieved, "peak": peak, "unit": "Tinst/s", "frac": achieved / peak,
+            "fp32_inst_per_step": inst, "peak_basis": f"{SMS} SMs x {FP32_LANES_PER_SM} FP32 lanes x {mhz:.0f} MHz"}
 
 
 def profile_traffic():
