@@ -214,7 +214,7 @@ def run_ours(args, rank, world, local):
         st.set_tile_threads(args.cta_threads)
     tuning = st.tuning()
     tile_q = tuning["tile_qubits"]
-    passes, xops = llgpu.plan_export(n, ops, tile_q)
+    passes, xops = llgpu.plan_export(n, ops, tile_q, zyz=args.precision == "complex128")
     if tuning["fuse_mode"] == "none":
         passes = np.zeros(ngates)  # one streaming pass per gate
     elem = 8 if args.precision == "complex64" else 16
@@ -332,10 +332,10 @@ def run_ours(args, rank, world, local):
 # 5 DIAG, 6 CNOT, 7 MCZ), counted from the double-float routines of the kernels: a 4-term
 # double-float dot product (df_lin4) is 43 instructions (4 FMUL + 4 FFMA product errors, 3 TwoSum
 # of 6, 8 FFMA cross terms, 6 FADD, Fast2Sum of 3), a 2-term one (df_lin2) 19; a U2 pair needs four
-# 4-term products, RX/RY/H four 2-term ones, a diagonal two 2-term ones per amplitude.  CNOT, MCZ
-# and X move or negate data without arithmetic.
-FP32_INST_PER_PAIR = {"complex128": {0: 172, 1: 76, 2: 76, 3: 76, 4: 0, 5: 76, 6: 0, 7: 0},
-                      "complex64": {0: 16, 1: 8, 2: 8, 3: 8, 4: 0, 5: 8, 6: 0, 7: 0}}
+# 4-term products, RX/RY/H four 2-term ones, a diagonal two 2-term ones per amplitude, a ZYZ
+# (phase-free unitary) eight 2-term ones.  CNOT, MCZ and X move or negate data without arithmetic.
+FP32_INST_PER_PAIR = {"complex128": {0: 172, 1: 76, 2: 76, 3: 76, 4: 0, 5: 76, 6: 0, 7: 0, 11: 152},
+                      "complex64": {0: 16, 1: 8, 2: 8, 3: 8, 4: 0, 5: 8, 6: 0, 7: 0, 11: 16}}
 SMS, FP32_LANES_PER_SM = 152, 128
 
 

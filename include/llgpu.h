@@ -338,9 +338,11 @@ typedef struct llg_pass_info {
     int32_t nops;        /* number of executor ops */
 } llg_pass_info;
 
-/* Executor op: kind 0 U2, 1 RX, 2 RY, 3 H, 4 X, 5 DIAG, 6 CNOT, 7 MCZ.  Qubit fields are tile-local
- * indices unless flags bit 0 marks q0 as a global qubit outside the tile; nl_mask holds global
- * qubits that must all be 1 in the tile for the op to act. */
+/* Executor op: kind 0 U2, 1 RX, 2 RY, 3 H, 4 X, 5 DIAG, 6 CNOT, 7 MCZ, 11 ZYZ (a unitary 2x2
+ * without its global phase: diag(1, c4 + i c5) [c2, -c3; c3, c2] diag(1, c0 + i c1); the dropped
+ * phases are multiplied into the plan's first U2).  Qubit fields are tile-local indices unless
+ * flags bit 0 marks q0 as a global qubit outside the tile; nl_mask holds global qubits that must
+ * all be 1 in the tile for the op to act. */
 typedef struct llg_exec_op {
     int32_t kind;
     int32_t q0;
@@ -353,6 +355,11 @@ typedef struct llg_exec_op {
 
 int llg_plan_export(int n, const llg_op* ops, int nops, int tile_qubits, llg_pass_info* passes, int max_passes,
                     int* npasses, llg_exec_op* xops, int max_xops, int* nxops);
+/* The same with planner options: LLG_PLAN_ZYZ lowers fused unitary 2x2s to ZYZ ops as the
+ * engine does for complex128 (double-float) states; llg_plan_export plans without it. */
+#define LLG_PLAN_ZYZ 1
+int llg_plan_export_ex(int n, const llg_op* ops, int nops, int tile_qubits, int flags, llg_pass_info* passes,
+                       int max_passes, int* npasses, llg_exec_op* xops, int max_xops, int* nxops);
 
 #ifdef __cplusplus
 }

@@ -737,6 +737,11 @@ int llg_get_stream(const llg_state* st, void** out) {
 
 int llg_plan_export(int n, const llg_op* ops, int nops, int tile_qubits, llg_pass_info* passes, int max_passes,
                     int* npasses, llg_exec_op* xops, int max_xops, int* nxops) {
+    return llg_plan_export_ex(n, ops, nops, tile_qubits, 0, passes, max_passes, npasses, xops, max_xops, nxops);
+}
+
+int llg_plan_export_ex(int n, const llg_op* ops, int nops, int tile_qubits, int flags, llg_pass_info* passes,
+                       int max_passes, int* npasses, llg_exec_op* xops, int max_xops, int* nxops) {
     if (n < 1 || n > kMaxQubits || nops < 0 || (nops > 0 && !ops) || !npasses || !nxops)
         return set_error(LLG_EINVAL, "plan_export: bad argument");
     if (tile_qubits < 1 || tile_qubits > 14) return set_error(LLG_EINVAL, "plan_export: tile_qubits out of range");
@@ -748,7 +753,8 @@ int llg_plan_export(int n, const llg_op* ops, int nops, int tile_qubits, llg_pas
     }
     Plan plan;
     std::string err;
-    if (!plan_tiles(n, ops, nops, tile_qubits, LLG_F64, plan, err)) return set_error(LLG_EINVAL, err);
+    if (!plan_tiles(n, ops, nops, tile_qubits, LLG_F64, plan, err, false, (flags & LLG_PLAN_ZYZ) ? ZYZ_ON : ZYZ_OFF))
+        return set_error(LLG_EINVAL, err);
     *npasses = (int)plan.passes.size();
     *nxops = (int)plan.ops.size();
     if (passes)

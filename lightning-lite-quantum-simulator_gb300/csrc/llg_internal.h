@@ -25,6 +25,11 @@ enum ExecKind : int32_t {
     EX_RX_P = 8,
     EX_RY_P = 9,
     EX_RZ_P = 10,
+    // unitary 2x2 without its global phase, as diag(1, e^{ia}) RY(b) diag(1, e^{ig}) on q0:
+    // c[0..1] = cos g, sin g; c[2..3] = cos b/2, sin b/2; c[4..5] = cos a, sin a.  152 FP32
+    // instructions per double-float pair against 172 for EX_U2; the plan carries the dropped
+    // phases in one EX_U2 of the same flush.
+    EX_ZYZ = 11,
 };
 
 // Flags of a tile op.
@@ -72,8 +77,11 @@ struct Plan {
 // invalid input.
 // With use_params, rotations whose `param` >= 0 are kept unfused and lowered to EX_*_P ops whose
 // q1 is the op's occurrence slot (the index of that op among all parametrised ops, in order).
+// With zyz, fused unitary 2x2s are lowered to EX_ZYZ and their global phases folded into the
+// first EX_U2 of the plan (default: on for double-float states without parametrised ops).
+enum PlanZyz : int { ZYZ_DEFAULT = -1, ZYZ_OFF = 0, ZYZ_ON = 1 };
 bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int precision, Plan& out, std::string& err,
-                bool use_params = false);
+                bool use_params = false, int zyz = ZYZ_DEFAULT);
 
 // Lower one gate record to executor ops with GLOBAL qubit indices (streaming path).
 bool lower_op(int n, const llg_op& op, int precision, std::vector<ExecOp>& out, std::string& err);

@@ -147,6 +147,7 @@ __global__ void __launch_bounds__(512) k_tile(typename P::S* __restrict__ psi, P
         const int kind = o.kind;
         switch (kind) {
             case EX_U2: tile_pairs<P, EX_U2>(tile, tsize >> 1, o.q0, o); break;
+            case EX_ZYZ: tile_pairs<P, EX_ZYZ>(tile, tsize >> 1, o.q0, o); break;
             case EX_RX: tile_pairs<P, EX_RX>(tile, tsize >> 1, o.q0, o); break;
             case EX_RY: tile_pairs<P, EX_RY>(tile, tsize >> 1, o.q0, o); break;
             case EX_H: tile_pairs<P, EX_H>(tile, tsize >> 1, o.q0, o); break;

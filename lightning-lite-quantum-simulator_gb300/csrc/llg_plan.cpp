@@ -18,6 +18,7 @@
 // fuser's rule) before lowering.
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -182,11 +183,48 @@ static bool is_param_op(const llg_op& op, bool use_params) {
     return use_params && op.param >= 0 && (op.kind == LLG_OP_RX || op.kind == LLG_OP_RY || op.kind == LLG_OP_RZ);
 }
 
+// Splits a unitary 2x2 m (row-major (re, im) pairs) as z * diag(1, ea) * [[c, -s], [s, c]] *
+// diag(1, eg) with |z| = |ea| = |eg| = 1, c = |m00|, s = |m10|.  Returns false when m is not
+// unitary to within 2e-15 (then the op stays a generic EX_U2).
+static bool split_zyz(const double* m, std::complex<double>& z, double& c, double& s, std::complex<double>& ea,
+                      std::complex<double>& eg) {
+    using cd = std::complex<double>;
+    const cd u00(m[0], m[1]), u01(m[2], m[3]), u10(m[4], m[5]), u11(m[6], m[7]);
+    const double n0 = std::norm(u00) + std::norm(u10), n1 = std::norm(u01) + std::norm(u11);
+    const cd cross = std::conj(u00) * u01 + std::conj(u10) * u11;
+    const double tol = 2e-15;
+    if (!(std::fabs(n0 - 1.0) <= tol && std::fabs(n1 - 1.0) <= tol && std::abs(cross) <= tol)) return false;
+    c = std::abs(u00);
+    s = std::abs(u10);
+    if (c > 0.0 && s > 0.0) {
+        z = u00 / c;
+        ea = u10 * std::conj(z) / s;
+        eg = -u01 * std::conj(z) / s;
+    } else if (s > 0.0) {  // anti-diagonal: take a = 0
+        z = u10 / s;
+        ea = 1.0;
+        eg = -u01 * std::conj(z) / s;
+    } else if (c > 0.0) {  // diagonal: take g = 0
+        z = u00 / c;
+        ea = u11 * std::conj(z) / c;
+        eg = 1.0;
+    } else {
+        return false;
+    }
+    return true;
+}
+
 bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan& out, std::string& err,
-                bool use_params) {
+                bool use_params, int zyz) {
     out.passes.clear();
     out.ops.clear();
     out.source_index.clear();
+    const bool use_zyz = zyz == ZYZ_DEFAULT ? (P == LLG_DF64 && !use_params) : zyz == ZYZ_ON;
+    // the phase carrier: the plan's first EX_U2, which also applies the global phases dropped by
+    // every EX_ZYZ (a scalar factor commutes with every op, so any op of the flush may carry it)
+    int carrier = -1;
+    double carrier_m[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    std::complex<double> phase(1.0, 0.0);
     const int t = std::min(n, tile_qubits);
     // the low qubits are always local; when the register is wider than the tile at least one slot
     // stays free, so the first remaining op (which needs at most one qubit local) always fits
@@ -265,9 +303,25 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
         auto emit_lowered = [&](const llg_op& gop, int src) -> bool {
             std::vector<ExecOp> tmp;
             if (!lower_op(n, gop, P, tmp, err)) return false;
+            if (use_zyz && gop.kind == LLG_OP_U2 && tmp.size() == 1) {
+                std::complex<double> z, ea, eg;
+                double c = 0.0, s = 0.0;
+                if (carrier < 0) {
+                    carrier = (int)out.ops.size();
+                    std::memcpy(carrier_m, gop.m, sizeof(carrier_m));
+                } else if (split_zyz(gop.m, z, c, s, ea, eg)) {
+                    ExecOp e = blank(EX_ZYZ);
+                    e.q0 = gop.q0;
+                    const double v[6] = {eg.real(), eg.imag(), c, s, ea.real(), ea.imag()};
+                    for (int k = 0; k < 6; ++k) e.c[k] = pack_coef(P, v[k]);
+                    tmp[0] = e;
+                    phase *= z;
+                }
+            }
             for (ExecOp& e : tmp) {
                 switch (e.kind) {
                     case EX_U2:
+                    case EX_ZYZ:
                     case EX_RX:
                     case EX_RY:
                     case EX_H:
@@ -377,6 +431,13 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
         }
         out.passes.push_back(pd);
         remaining.swap(deferred);
+    }
+    if (carrier >= 0 && (phase.real() != 1.0 || phase.imag() != 0.0)) {
+        for (int r = 0; r < 4; ++r) {
+            const std::complex<double> v = phase * std::complex<double>(carrier_m[2 * r], carrier_m[2 * r + 1]);
+            out.ops[carrier].c[2 * r] = pack_coef(P, v.real());
+            out.ops[carrier].c[2 * r + 1] = pack_coef(P, v.imag());
+        }
     }
     return true;
 }

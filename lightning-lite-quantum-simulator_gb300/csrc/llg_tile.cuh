@@ -46,6 +46,16 @@ struct PairMath {
             a0.im = P::lin2(c, y0, ms, y1);
             a1.re = P::lin2(s, x0, c, x1);
             a1.im = P::lin2(s, y0, c, y1);
+        } else if (KIND == EX_ZYZ) {  // diag(1, ea) [c, -s; s, c] diag(1, eg)
+            const auto gr = k[0], gi = k[1], c = k[2], s = k[3], ar = k[4], ai = k[5];
+            const auto tr = P::lin2(gr, x1, P::kneg(gi), y1);  // eg * a1
+            const auto ti = P::lin2(gr, y1, gi, x1);
+            a0.re = P::lin2(c, x0, P::kneg(s), tr);
+            a0.im = P::lin2(c, y0, P::kneg(s), ti);
+            const auto ur = P::lin2(s, x0, c, tr);
+            const auto ui = P::lin2(s, y0, c, ti);
+            a1.re = P::lin2(ar, ur, P::kneg(ai), ui);  // ea * u
+            a1.im = P::lin2(ar, ui, ai, ur);
         } else if (KIND == EX_H) {  // r [1, 1; 1, -1]
             const auto r = k[0], mr = P::kneg(k[0]);
             a0.re = P::lin2(r, x0, r, x1);
@@ -94,6 +104,7 @@ __device__ void tile_apply(typename P::S* tile, uint32_t tsize, uint64_t base, c
     using S = typename P::S;
     switch (o.kind) {
         case EX_U2: tile_pairs<P, EX_U2>(tile, tsize >> 1, o.q0, o); break;
+        case EX_ZYZ: tile_pairs<P, EX_ZYZ>(tile, tsize >> 1, o.q0, o); break;
         case EX_RX: tile_pairs<P, EX_RX>(tile, tsize >> 1, o.q0, o); break;
         case EX_RY: tile_pairs<P, EX_RY>(tile, tsize >> 1, o.q0, o); break;
         case EX_H: tile_pairs<P, EX_H>(tile, tsize >> 1, o.q0, o); break;

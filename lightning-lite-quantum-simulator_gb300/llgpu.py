@@ -105,6 +105,7 @@ def lib() -> ctypes.CDLL:
             "llg_host_alloc": (vp, [sz]),
             "llg_host_free": (None, [vp]),
             "llg_plan_export": (i, [i, vp, i, i, vp, i, P(i), vp, i, P(i)]),
+            "llg_plan_export_ex": (i, [i, vp, i, i, i, vp, i, P(i), vp, i, P(i)]),
             "llg_profile": (i, [vp, i]),
             "llg_profile_read": (i, [vp, vp, vp, i]),
             "llg_kernel_launches": (ctypes.c_int64, []),
@@ -340,15 +341,21 @@ class State:
 # ---------------------------------------------------------------------------------------------
 # planner introspection (host only)
 # ---------------------------------------------------------------------------------------------
-def plan_export(n: int, ops: np.ndarray, tile_qubits: int):
+PLAN_ZYZ = 1
+
+
+def plan_export(n: int, ops: np.ndarray, tile_qubits: int, zyz: bool = False):
+    """Host-side plan of `ops` (passes, executor ops; coefficients as doubles).  zyz=True plans
+    as the engine does for complex128 states (fused unitary 2x2s as ZYZ ops)."""
     ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
+    flags = PLAN_ZYZ if zyz else 0
     npasses, nx = ctypes.c_int(), ctypes.c_int()
-    check(lib().llg_plan_export(n, _ptr(ops) if ops.size else None, ops.size, tile_qubits, None, 0,
-                                ctypes.byref(npasses), None, 0, ctypes.byref(nx)))
+    check(lib().llg_plan_export_ex(n, _ptr(ops) if ops.size else None, ops.size, tile_qubits, flags, None, 0,
+                                   ctypes.byref(npasses), None, 0, ctypes.byref(nx)))
     passes = np.zeros(npasses.value, dtype=PASS_DTYPE)
     xops = np.zeros(max(nx.value, 1), dtype=XOP_DTYPE)
-    check(lib().llg_plan_export(n, _ptr(ops) if ops.size else None, ops.size, tile_qubits, _ptr(passes),
-                                passes.size, ctypes.byref(npasses), _ptr(xops), xops.size, ctypes.byref(nx)))
+    check(lib().llg_plan_export_ex(n, _ptr(ops) if ops.size else None, ops.size, tile_qubits, flags, _ptr(passes),
+                                   passes.size, ctypes.byref(npasses), _ptr(xops), xops.size, ctypes.byref(nx)))
     return passes, xops[: nx.value]
 
 

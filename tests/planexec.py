@@ -15,6 +15,10 @@ def _matrix(x) -> np.ndarray:
         return np.array([[c[0], -c[1]], [c[1], c[0]]], dtype=complex)
     if k == 3:
         return np.array([[c[0], c[0]], [c[0], -c[0]]], dtype=complex)
+    if k == 11:  # diag(1, ea) [c, -s; s, c] diag(1, eg)
+        eg, ea = c[0] + 1j * c[1], c[4] + 1j * c[5]
+        ry = np.array([[c[2], -c[3]], [c[3], c[2]]], dtype=complex)
+        return np.diag([1, ea]) @ ry @ np.diag([1, eg])
     return np.array([[0, 1], [1, 0]], dtype=complex)
 
 
@@ -45,7 +49,7 @@ def execute(psi: np.ndarray, n: int, passes: np.ndarray, xops: np.ndarray) -> np
         lidx = np.arange(1 << t)
         for x in xops[p["op_begin"]:p["op_begin"] + p["nops"]]:
             k, q0, q1, fl = int(x["kind"]), int(x["q0"]), int(x["q1"]), int(x["flags"])
-            if k <= 4:
+            if k <= 4 or k == 11:
                 _pair(tile, q0, _matrix(x))
             elif k == 5:
                 c = x["c"]

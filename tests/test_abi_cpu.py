@@ -79,11 +79,12 @@ def random_ops(n, depth, rng):
     return make_ops(recs)
 
 
+@pytest.mark.parametrize("zyz", [False, True])
 @pytest.mark.parametrize("n,tile", [(6, 5), (8, 5), (9, 6), (10, 7), (11, 5)])
-def test_planned_passes_reproduce_the_oracle(built, n, tile):
+def test_planned_passes_reproduce_the_oracle(built, n, tile, zyz):
     rng = np.random.default_rng(100 + n)
     ops = random_ops(n, 300, rng)
-    passes, xops = llgpu.plan_export(n, ops, tile)
+    passes, xops = llgpu.plan_export(n, ops, tile, zyz=zyz)
     if n > tile:
         assert len(passes) > 1
     got = execute(oracle.zero_state(n), n, passes, xops)
@@ -91,11 +92,12 @@ def test_planned_passes_reproduce_the_oracle(built, n, tile):
     assert np.max(np.abs(got - want)) < 1e-12
 
 
-def test_plan_of_layered_circuit(built, golden):
+@pytest.mark.parametrize("zyz", [False, True])
+def test_plan_of_layered_circuit(built, golden, zyz):
     g = golden("config2_layered")
     for n, ops in zip(g["n"], split(g["ops"], g["offsets"])):
         n = int(n)
-        passes, xops = llgpu.plan_export(n, ops, 5)
+        passes, xops = llgpu.plan_export(n, ops, 5, zyz=zyz)
         got = execute(oracle.zero_state(n), n, passes, xops)
         assert np.max(np.abs(got - oracle.run_ops(n, ops))) < 1e-12
         # fewer passes than gates: runs of rotations share a pass
@@ -109,6 +111,35 @@ def test_plan_of_random_2024_circuits(built, golden):
         passes, xops = llgpu.plan_export(n, ops, 3)
         got = execute(oracle.zero_state(n), n, passes, xops)
         assert np.max(np.abs(got - oracle.run_ops(n, ops))) < 1e-12
+
+
+def test_zyz_plan_carries_the_global_phase_in_one_u2(built):
+    # fused rotations become ZYZ ops; exactly one generic 2x2 remains and carries the phases
+    n = 12
+    ops = workloads.layered_rotations(n, layers=6)
+    passes, xops = llgpu.plan_export(n, ops, 8, zyz=True)
+    kinds = np.bincount(xops["kind"], minlength=12)
+    assert kinds[0] == 1 and kinds[11] > 50
+    got = execute(oracle.zero_state(n), n, passes, xops)
+    assert np.max(np.abs(got - oracle.run_ops(n, ops))) < 1e-12
+
+
+def test_zyz_keeps_non_unitary_gates_generic(built):
+    rng = np.random.default_rng(7)
+    recs = []
+    for k in range(40):
+        g = rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2))
+        if k % 2:
+            g, _ = np.linalg.qr(g)  # unitary
+        recs.append((OP_U2, int(rng.integers(6)), 0, 0.0, None, g.reshape(4)))
+        recs.append((OP_CNOT, k % 6, (k + 1) % 6, 0.0))
+    ops = make_ops(recs)
+    passes, xops = llgpu.plan_export(6, ops, 5, zyz=True)
+    kinds = np.bincount(xops["kind"], minlength=12)
+    assert kinds[0] >= 10 and kinds[11] >= 5  # non-unitary products stay generic
+    got = execute(oracle.zero_state(6), 6, passes, xops)
+    want = oracle.run_ops(6, ops)
+    assert np.max(np.abs(got - want)) <= 1e-12 * max(1.0, np.max(np.abs(want)))
 
 
 def test_thirty_qubit_plan_is_compact(built):
