@@ -273,6 +273,46 @@ int llg_traj_autotune(llg_traj* h, uint64_t sample_traj, llg_tune_result* out);
 int llg_traj_config(const llg_traj* h, int* cluster, int* cta_threads, int* grid, int64_t* sites);
 int llg_traj_stream(const llg_traj* h, void** out);
 
+/* ---- depolarizing noise with gate folding, and zero-noise extrapolation ----
+ * Batched form of ll::NoisyBackend (src/Mitigation.h:110-240): every gate U of `ops` runs as
+ * U (U^+ U)^k for scale = 2k + 1 (odd, 1..99), each application followed by its noise site(s):
+ * one 2-qubit depolarizing site over (q0, q1) for cnot, cz and 2-qubit mcz, else a 1-qubit site
+ * per touched qubit.  A site draws u; u < p applies a non-identity Pauli chosen by a second
+ * uniform u2: 1 + floor(3 u2) in {X, Y, Z}, or 1 + floor(15 u2) with the low two bits on the
+ * first qubit and the high two on the second; Y = Z then X.  u and u2 come from one
+ * Philox4x32-10 call (key = seed, counter = (site, trajectory)) instead of the reference's
+ * sequential mt19937_64 stream.  The handle is an llg_traj: llg_traj_launch writes, per
+ * trajectory, the observable sum_k zcoeff[k] Z_za[k] Z_zb[k] (zb[k] < 0: Z_za[k] alone; at most
+ * 16 terms with at most 3 distinct coefficients; nterms = 0: <Z_0>) of the final state, and the
+ * number of non-identity Paulis applied. */
+int llg_noisy_create(int n, const llg_op* ops, int nops, double p, int scale, int precision, uint64_t max_traj,
+                     int nterms, const int* za, const int* zb, const double* zcoeff, int cluster, int cta_threads,
+                     llg_traj** out);
+
+/* ll::ZNE (src/Mitigation.h:243-377). */
+#define LLG_ZNE_MAX_SCALES 8
+typedef struct llg_zne_result {
+    double value;                           /* E(0) = sum_k weights[k] values[k] */
+    double std_error;                       /* sqrt(sum_k weights[k]^2 std_errors[k]^2); NaN if not estimable */
+    int32_t nscales;
+    int32_t pad;
+    int64_t trajectories;                   /* run per scale (1 when p == 0) */
+    double scales[LLG_ZNE_MAX_SCALES];
+    double values[LLG_ZNE_MAX_SCALES];      /* trajectory mean at each scale */
+    double std_errors[LLG_ZNE_MAX_SCALES];  /* sample std / sqrt(N) (Welford) */
+    double weights[LLG_ZNE_MAX_SCALES];     /* Richardson weights */
+} llg_zne_result;
+/* c_k = prod_{j != k} s_j / (s_j - s_k) (ZNE::richardson_weights, src/Mitigation.h:287-301). */
+int llg_richardson_weights(const double* scales, int nscales, double* weights);
+/* ZNE::extrapolate (src/Mitigation.h:313-377) over the circuit: `trajectories` runs per scale
+ * (scales: 2..8 distinct odd integers in [1, 99]) in one persistent launch each, trajectory
+ * indices [k N, (k + 1) N) for scale k; Richardson extrapolation to zero noise.  Errors as the
+ * reference: bad scales, p, trajectories or observable are LLG_EINVAL; an empty circuit is
+ * LLG_ERUNTIME ("applied no gates"). */
+int llg_zne_run(int n, const llg_op* ops, int nops, double p, int precision, const double* scales, int nscales,
+                int64_t trajectories, uint64_t seed, int nterms, const int* za, const int* zb, const double* zcoeff,
+                llg_zne_result* out);
+
 /* ---- mixed-size batches ----
  * `count` circuits (circuit c: n_qubits[c] in [1, 30], ops[op_offsets[c] .. op_offsets[c+1]))
  * planned into shared-memory tile passes of tile_qubits qubits (0: default, 12 or 13 for

@@ -54,15 +54,31 @@ constexpr int kMaxGrid = 4096;     // persistent CTAs at most (per-CTA margin sl
 // one gate of a trajectory circuit: the executor op (global qubits) and the touched qubits
 struct TrajGate {
     ExecOp op;
-    int32_t nt;
+    int32_t nt;     // touched qubits, in noise-site order
     int32_t q[6];
-    int32_t pad;
+    int32_t pair;   // depolarizing mode: 1 = one 2-qubit site over (q[0], q[1]), 0 = a 1-qubit site per qubit
 };
 
+constexpr int kObsTerms = 16;
+constexpr int kObsClasses = 3;
+
+// Observable sum_k coef[cls[k]] Z_a[k] Z_b[k] (b < 0: Z_a alone) read at the end of every
+// trajectory; nterms = 0 reads <Z_0>.  Terms are grouped into coefficient classes so the kernel
+// counts parities in integers and weights |a|^2 once per class.
+struct ObsTerms {
+    int32_t nterms, nclass;
+    int32_t a[kObsTerms], b[kObsTerms], cls[kObsTerms];
+    double coef[kObsClasses];
+};
+
+enum : int32_t { NOISE_KRAUS = 0, NOISE_DEPOL = 1 };
+
 struct KrausParams {
-    double gamma, lambda;
-    double sq1mg, sq1ml;  // sqrt(1 - gamma), sqrt(1 - lambda)
+    double gamma, lambda;  // NOISE_DEPOL: gamma = p, the non-identity Pauli probability per site
+    double sq1mg, sq1ml;   // sqrt(1 - gamma), sqrt(1 - lambda)
     uint64_t seed;
+    int32_t mode;          // NOISE_KRAUS / NOISE_DEPOL
+    int32_t pad;
 };
 
 // ------------------------------------------------------------------------------------------
@@ -87,6 +103,29 @@ __device__ __forceinline__ double philox_u1(uint64_t seed, uint64_t traj, uint64
     }
     const uint64_t a = ((uint64_t)c1 << 32) | c0;
     return (double)(a >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// both uniforms of one Philox call: u1 from the low 64 bits, u2 from the high 64 bits
+__device__ __forceinline__ void philox_u12(uint64_t seed, uint64_t traj, uint64_t site, double* u1, double* u2) {
+    uint32_t c0 = (uint32_t)site, c1 = (uint32_t)(site >> 32), c2 = (uint32_t)traj, c3 = (uint32_t)(traj >> 32);
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+    }
+    const uint64_t a = ((uint64_t)c1 << 32) | c0, b = ((uint64_t)c3 << 32) | c2;
+    *u1 = (double)(a >> 11) * (1.0 / 9007199254740992.0);
+    *u2 = (double)(b >> 11) * (1.0 / 9007199254740992.0);
 }
 
 template <class P>
@@ -234,9 +273,15 @@ struct Traj {
                 if (bit) pos = P::acc_norm(pos, a);
             }
         }
+        return group_total(acc_minus(pos, neg), red, slot);
+    }
+
+    // group-wide sum of one accumulator per thread, identical in every CTA of the group.  The
+    // caller separates two calls by a group barrier (the partner may still read `slot`).
+    __device__ double group_total(typename P::Acc v, typename P::Acc* red, typename P::Acc* slot) {
         using A = typename P::Acc;
-        const A v = block_sum_acc(acc_minus(pos, neg), red);
-        if (threadIdx.x == 0) *slot = v;
+        const A t = block_sum_acc(v, red);
+        if (threadIdx.x == 0) *slot = t;
         group_sync<CL>();
         double total;
         if (CL == 1) {
@@ -248,6 +293,85 @@ struct Traj {
             total = acc_value(acc_plus(*s0, *s1));  // the same order on both CTAs
         }
         return total;
+    }
+
+    // the observable sum_c coef_c * sum_i |a_i|^2 (tot_c - 2 odd_c(i)) over the group's state
+    __device__ double observable(const ObsTerms& ob, typename P::Acc* red, typename P::Acc* slot) {
+        typename P::Acc acc[kObsClasses];
+        int tot[kObsClasses] = {0, 0, 0};
+#pragma unroll
+        for (int c = 0; c < kObsClasses; ++c) acc[c] = P::acc_zero();
+        for (int k = 0; k < ob.nterms; ++k) tot[ob.cls[k]] += 1;
+        for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x) {
+            const uint32_t gi = l | ((uint32_t)rank << nl);
+            int odd[kObsClasses] = {0, 0, 0};
+            for (int k = 0; k < ob.nterms; ++k) {
+                int par = (int)((gi >> ob.a[k]) & 1);
+                if (ob.b[k] >= 0) par ^= (int)((gi >> ob.b[k]) & 1);
+                odd[ob.cls[k]] += par;
+            }
+            const auto a = P::load(s[l]);
+#pragma unroll
+            for (int c = 0; c < kObsClasses; ++c)
+                if (c < ob.nclass) acc[c] = P::acc_norm_w(acc[c], a, (float)(tot[c] - 2 * odd[c]));
+        }
+        double e = 0.0;
+        for (int c = 0; c < ob.nclass; ++c) {
+            e += ob.coef[c] * group_total(acc[c], red, slot);
+            group_sync<CL>();  // both CTAs have read the slots before the next class reuses them
+        }
+        return e;
+    }
+
+    // Pauli Z on global qubit q: negate the amplitudes whose bit q is 1
+    __device__ void pauli_z(int q) {
+        if (cross(q)) {
+            if (rank == 1)
+                for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x) {
+                    auto a = P::load(s[l]);
+                    a.re = P::neg(a.re);
+                    a.im = P::neg(a.im);
+                    s[l] = P::store(a);
+                }
+        } else {
+            const uint32_t bit = 1u << q;
+            for (uint32_t p = threadIdx.x; p < (NL >> 1); p += blockDim.x) {
+                const uint32_t j = (uint32_t)insert0(p, q) | bit;
+                auto a = P::load(s[j]);
+                a.re = P::neg(a.re);
+                a.im = P::neg(a.im);
+                s[j] = P::store(a);
+            }
+        }
+        group_sync<CL>();
+    }
+
+    // Pauli X on global qubit q: swap the amplitude pairs along q (across the two CTAs for the
+    // top qubit of a cluster: each CTA takes the partner's half)
+    __device__ void pauli_x(int q) {
+        if (cross(q)) {
+            S out[kMaxPerThread];
+            int cnt = 0;
+            for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x, ++cnt) out[cnt] = remote[l];
+            group_sync<CL>();  // both CTAs hold the partner's half
+            cnt = 0;
+            for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x, ++cnt) s[l] = out[cnt];
+        } else {
+            const uint32_t bit = 1u << q;
+            for (uint32_t p = threadIdx.x; p < (NL >> 1); p += blockDim.x) {
+                const uint32_t j0 = (uint32_t)insert0(p, q), j1 = j0 | bit;
+                const S t = s[j0];
+                s[j0] = s[j1];
+                s[j1] = t;
+            }
+        }
+        group_sync<CL>();
+    }
+
+    // Pauli 1 = X, 2 = Y (Z then X, up to a global phase), 3 = Z
+    __device__ void pauli(int q, int which) {
+        if (which == 2 || which == 3) pauli_z(q);
+        if (which == 1 || which == 2) pauli_x(q);
     }
 
     // amplitude damping then phase damping on qubit q, decisions in *d (already filled)
@@ -357,7 +481,8 @@ __device__ void decide(double P1, const KrausParams& kp, uint64_t traj, uint64_t
 }
 
 template <class P, int CL>
-__device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int ngates, KrausParams kp, uint64_t traj_begin,
+__device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int ngates, KrausParams kp,
+                                 const ObsTerms* __restrict__ obs, uint64_t traj_begin,
                                  uint64_t n_traj, double* __restrict__ z0_out, uint32_t* __restrict__ jumps_out,
                                  uint8_t* __restrict__ jump_log, int64_t log_stride, double* __restrict__ margin_out) {
     using S = typename P::S;
@@ -365,6 +490,11 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
     __shared__ typename P::Acc red[32];
     __shared__ typename P::Acc slot;
     __shared__ Decision dec;
+    __shared__ ObsTerms ob;  // the observable, copied once from global memory
+    static_assert(sizeof(ObsTerms) % 4 == 0, "ObsTerms copies as 32-bit words");
+    for (uint32_t w = threadIdx.x; w < sizeof(ObsTerms) / 4; w += blockDim.x)
+        reinterpret_cast<int32_t*>(&ob)[w] = reinterpret_cast<const int32_t*>(obs)[w];
+    __syncthreads();
     Traj<P, CL> T;
     T.nl = (CL == 2) ? n - 1 : n;
     T.NL = 1u << T.nl;
@@ -394,6 +524,27 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
         for (int g = 0; g < ngates; ++g) {
             const TrajGate& G = gates[g];
             T.gate(G.op);
+            if (kp.mode == NOISE_DEPOL) {
+                // decisions do not depend on the state: every thread draws the same uniforms, so
+                // the branch is uniform and needs no broadcast
+                if (!(kp.gamma > 0.0)) continue;
+                const int nsites = G.pair ? 1 : G.nt;
+                for (int k = 0; k < nsites; ++k) {
+                    double u, u2;
+                    philox_u12(kp.seed, traj, site, &u, &u2);
+                    ++site;
+                    if (u >= kp.gamma) continue;
+                    ++jumps;
+                    if (G.pair) {
+                        const int idx = 1 + (int)(u2 * 15.0);
+                        T.pauli(G.q[0], idx & 3);
+                        T.pauli(G.q[1], idx >> 2);
+                    } else {
+                        T.pauli(G.q[k], 1 + (int)(u2 * 3.0));
+                    }
+                }
+                continue;
+            }
             for (int k = 0; k < G.nt; ++k) {
                 const int q = G.q[k];
                 const double P1 = T.reduce(q, false, red, &slot);
@@ -407,7 +558,7 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
                 site += 2;
             }
         }
-        const double z = T.reduce(0, true, red, &slot);
+        const double z = ob.nterms > 0 ? T.observable(ob, red, &slot) : T.reduce(0, true, red, &slot);
         if (threadIdx.x == 0 && T.rank == 0) {
             z0_out[tt] = z;
             if (jumps_out) jumps_out[tt] = jumps;
@@ -419,16 +570,18 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
 
 template <class P>
 __global__ void __launch_bounds__(kTrajThreads) k_traj1(int n, const TrajGate* gates, int ngates, KrausParams kp,
+                                                        const ObsTerms* ob,
                                                         uint64_t traj_begin, uint64_t n_traj, double* z0, uint32_t* jumps,
                                                         uint8_t* log, int64_t log_stride, double* margins) {
-    traj_kernel_body<P, 1>(n, gates, ngates, kp, traj_begin, n_traj, z0, jumps, log, log_stride, margins);
+    traj_kernel_body<P, 1>(n, gates, ngates, kp, ob, traj_begin, n_traj, z0, jumps, log, log_stride, margins);
 }
 
 template <class P>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTrajThreads)
-    k_traj2(int n, const TrajGate* gates, int ngates, KrausParams kp, uint64_t traj_begin, uint64_t n_traj, double* z0,
+    k_traj2(int n, const TrajGate* gates, int ngates, KrausParams kp, const ObsTerms* ob, uint64_t traj_begin, uint64_t n_traj,
+            double* z0,
             uint32_t* jumps, uint8_t* log, int64_t log_stride, double* margins) {
-    traj_kernel_body<P, 2>(n, gates, ngates, kp, traj_begin, n_traj, z0, jumps, log, log_stride, margins);
+    traj_kernel_body<P, 2>(n, gates, ngates, kp, ob, traj_begin, n_traj, z0, jumps, log, log_stride, margins);
 }
 
 template <class P>
@@ -461,6 +614,8 @@ struct llg_traj {
     int ngates = 0;
     int64_t sites = 0;
     KrausParams kp{};
+    ObsTerms obs{};
+    ObsTerms* d_obs = nullptr;  // device copy of obs, read by the kernel
     uint64_t max_traj = 0;
     uint64_t shape_key = 0;
     TrajGate* d_gates = nullptr;
@@ -529,7 +684,7 @@ int configure(llg_traj* h, int cl, int threads) {
     uint64_t b0 = 0, c0 = 0;
     uint8_t* lg = nullptr;
     int64_t ls = 0;
-    void* args[] = {&n, &h->d_gates, &ngates, &h->kp, &b0, &c0, &h->d_z0, &h->d_jumps, &lg, &ls, &h->d_margin};
+    void* args[] = {&n, &h->d_gates, &ngates, &h->kp, &h->d_obs, &b0, &c0, &h->d_z0, &h->d_jumps, &lg, &ls, &h->d_margin};
     e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         cudaError_t le = cudaLaunchKernel(fn, dim3(h->grid), dim3(th), args, smem, h->stream);
@@ -552,7 +707,8 @@ int replay(llg_traj* h, uint64_t seed, uint64_t begin, uint64_t count, uint8_t* 
     int n = h->n, ngates = h->ngates;
     KrausParams kp = h->kp;
     kp.seed = seed;
-    void* args[] = {&n, &h->d_gates, &ngates, &kp, &begin, &count, &h->d_z0, &h->d_jumps, &d_log, &log_stride, &h->d_margin};
+    void* args[] = {&n,     &h->d_gates, &ngates,     &kp,        &h->d_obs,    &begin,
+                    &count, &h->d_z0,    &h->d_jumps, &d_log,     &log_stride, &h->d_margin};
     cudaKernelNodeParams p;
     std::memset(&p, 0, sizeof(p));
     p.func = const_cast<void*>(kernel_for(h->P, h->cl));
@@ -584,40 +740,14 @@ int collect(llg_traj* h, uint64_t count, double* z0_out, uint32_t* jumps_out, do
     return LLG_OK;
 }
 
-}  // namespace
-
-extern "C" {
-
-int llg_traj_destroy(llg_traj* h) {
-    if (!h) return LLG_OK;
-    if (h->stream) cudaStreamSynchronize(h->stream);
-    drop_graph(h);
-    cudaFree(h->d_gates);
-    cudaFree(h->d_z0);
-    cudaFree(h->d_jumps);
-    cudaFree(h->d_margin);
-    if (h->stream) cudaStreamDestroy(h->stream);
-    delete h;
-    return LLG_OK;
-}
-
-int llg_traj_create(int n, const llg_op* ops, int nops, double gamma_ad, double lambda_pd, int precision,
-                    uint64_t max_traj, int cluster, int cta_threads, llg_traj** out) {
-    if (!out) return set_error(LLG_EINVAL, "traj_create: out is NULL");
-    *out = nullptr;
-    if (n < 1 || n > 14) return set_error(LLG_EINVAL, "traj_run: n must be in [1, 14]");
-    if (precision != LLG_F64 && precision != LLG_DF64 && precision != LLG_F32)
-        return set_error(LLG_EINVAL, "traj_run: unknown precision");
-    if (nops < 0 || (nops > 0 && !ops)) return set_error(LLG_EINVAL, "traj_run: NULL argument");
-    if (!(gamma_ad >= 0.0 && gamma_ad <= 1.0) || !(lambda_pd >= 0.0 && lambda_pd <= 1.0))
-        return set_error(LLG_EINVAL, "traj_run: gamma and lambda must be in [0, 1]");
-    if (max_traj == 0) return set_error(LLG_EINVAL, "traj_create: max_traj must be positive");
-    if (cluster < LLG_TUNE_AUTO || cluster > 2 || cta_threads < LLG_TUNE_AUTO)
-        return set_error(LLG_EINVAL, "traj_create: cluster must be -1, 0, 1 or 2 and cta_threads >= -1");
-    // lower the gates with global qubits and record the touched qubits of each
-    std::vector<TrajGate> gates;
-    gates.reserve(nops);
-    int64_t sites = 0;
+// Lowers the circuit to trajectory gates with global qubits.  NOISE_KRAUS: one site per touched
+// qubit (control then target; mcz qubits in increasing order).  NOISE_DEPOL: the gate list folded
+// as U (U^+ U)^folds per gate, each application followed by its noise site(s): a 2-qubit site
+// for cnot, cz and 2-qubit mcz, else a 1-qubit site per touched qubit (src/Mitigation.h:184-205).
+bool build_gates(int n, const llg_op* ops, int nops, int precision, int mode, int folds, std::vector<TrajGate>& gates,
+                 int64_t& sites, std::string& err) {
+    gates.clear();
+    sites = 0;
     for (int i = 0; i < nops; ++i) {
         const llg_op& o = ops[i];
         bool ok = o.q0 >= 0 && o.q0 < n;
@@ -625,47 +755,105 @@ int llg_traj_create(int n, const llg_op* ops, int nops, double gamma_ad, double 
         if (o.kind == LLG_OP_MCZ) ok = o.mask != 0 && (o.mask >> n) == 0;
         if ((o.kind == LLG_OP_RX || o.kind == LLG_OP_RY || o.kind == LLG_OP_RZ) && !std::isfinite(o.theta)) ok = false;
         if (o.kind < 0 || o.kind > LLG_OP_U2) ok = false;
-        if (!ok) return set_error(LLG_EINVAL, "traj_run: invalid op " + std::to_string(i));
-        std::vector<ExecOp> lowered;
-        std::string err;
-        if (!lower_op(n, o, precision, lowered, err) || lowered.size() != 1) return set_error(LLG_EINVAL, "traj_run: " + err);
-        TrajGate g;
-        std::memset(&g, 0, sizeof(g));
-        g.op = lowered[0];
-        if (o.kind == LLG_OP_CNOT || o.kind == LLG_OP_CZ) {
-            g.nt = 2;
-            g.q[0] = o.q0;
-            g.q[1] = o.q1;
-        } else if (o.kind == LLG_OP_MCZ) {
-            if (__builtin_popcountll(o.mask) > 6) return set_error(LLG_EINVAL, "traj_run: mcz on more than 6 qubits");
-            for (int q = 0; q < n && g.nt < 6; ++q)
-                if ((o.mask >> q) & 1) g.q[g.nt++] = q;
-        } else {
-            g.nt = 1;
-            g.q[0] = o.q0;
+        if (!ok) {
+            err = "traj_run: invalid op " + std::to_string(i);
+            return false;
         }
-        sites += g.nt;
-        gates.push_back(g);
+        if (o.kind == LLG_OP_MCZ && __builtin_popcountll(o.mask) > 6) {
+            err = "traj_run: mcz on more than 6 qubits";
+            return false;
+        }
+        // the op and (for folding) its inverse: R(-t) for rotations, the adjoint for a 2x2
+        llg_op inv = o;
+        if (o.kind == LLG_OP_RX || o.kind == LLG_OP_RY || o.kind == LLG_OP_RZ) inv.theta = -o.theta;
+        if (o.kind == LLG_OP_U2)
+            for (int r = 0; r < 2; ++r)
+                for (int c = 0; c < 2; ++c) {
+                    inv.m[2 * (2 * r + c)] = o.m[2 * (2 * c + r)];
+                    inv.m[2 * (2 * r + c) + 1] = -o.m[2 * (2 * c + r) + 1];
+                }
+        TrajGate g[2];
+        for (int v = 0; v < 2; ++v) {
+            std::vector<ExecOp> lowered;
+            if (!lower_op(n, v ? inv : o, precision, lowered, err) || lowered.size() != 1) {
+                err = "traj_run: " + err;
+                return false;
+            }
+            std::memset(&g[v], 0, sizeof(TrajGate));
+            g[v].op = lowered[0];
+            if (o.kind == LLG_OP_CNOT || o.kind == LLG_OP_CZ) {
+                g[v].nt = 2;
+                g[v].q[0] = o.q0;
+                g[v].q[1] = o.q1;
+            } else if (o.kind == LLG_OP_MCZ) {
+                for (int q = 0; q < n && g[v].nt < 6; ++q)
+                    if ((o.mask >> q) & 1) g[v].q[g[v].nt++] = q;
+            } else {
+                g[v].nt = 1;
+                g[v].q[0] = o.q0;
+            }
+            g[v].pair = (mode == NOISE_DEPOL && g[v].nt == 2) ? 1 : 0;
+        }
+        const int64_t per_app = mode == NOISE_DEPOL ? (g[0].pair ? 1 : g[0].nt) : g[0].nt;
+        gates.push_back(g[0]);
+        for (int f = 0; f < folds; ++f) {
+            gates.push_back(g[1]);
+            gates.push_back(g[0]);
+        }
+        sites += per_app * (1 + 2 * (int64_t)folds);
     }
+    return true;
+}
+
+// Groups observable terms into at most kObsClasses coefficient classes.
+bool build_obs(int n, int nterms, const int* za, const int* zb, const double* zc, ObsTerms& ob, std::string& err) {
+    std::memset(&ob, 0, sizeof(ob));
+    if (nterms < 0 || nterms > kObsTerms || (nterms > 0 && (!za || !zb || !zc))) {
+        err = "observable: at most 16 terms";
+        return false;
+    }
+    for (int k = 0; k < nterms; ++k) {
+        if (za[k] < 0 || za[k] >= n || zb[k] >= n || zb[k] == za[k] || !std::isfinite(zc[k])) {
+            err = "observable: bad term " + std::to_string(k);
+            return false;
+        }
+        int c = 0;
+        while (c < ob.nclass && ob.coef[c] != zc[k]) ++c;
+        if (c == ob.nclass) {
+            if (ob.nclass == kObsClasses) {
+                err = "observable: at most 3 distinct coefficients";
+                return false;
+            }
+            ob.coef[ob.nclass++] = zc[k];
+        }
+        ob.a[k] = za[k];
+        ob.b[k] = zb[k] < 0 ? -1 : zb[k];
+        ob.cls[k] = c;
+    }
+    ob.nterms = nterms;
+    return true;
+}
+
+// Allocates and configures a handle for already-lowered gates.
+int create_handle(int n, int precision, const std::vector<TrajGate>& gates, int64_t sites, const KrausParams& kp,
+                  const ObsTerms& ob, uint64_t shape_key, uint64_t max_traj, int cluster, int cta_threads, llg_traj** out) {
     llg_traj* h = new llg_traj();
     h->n = n;
     h->P = precision;
     h->ngates = (int)gates.size();
     h->sites = sites;
     h->max_traj = max_traj;
-    h->kp.gamma = gamma_ad;
-    h->kp.lambda = lambda_pd;
-    h->kp.sq1mg = std::sqrt(1.0 - gamma_ad);
-    h->kp.sq1ml = std::sqrt(1.0 - lambda_pd);
-    h->kp.seed = 0;
-    h->shape_key = tune_hash_ops(tune_hash(tune_hash(1469598103934665603ULL, 0x54524a), (uint64_t)n << 8 | (uint64_t)precision),
-                                 ops, nops);
+    h->kp = kp;
+    h->obs = ob;
+    h->shape_key = shape_key;
     int rc = LLG_OK;
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&h->d_gates, std::max<size_t>(gates.size(), 1) * sizeof(TrajGate));
     if (e == cudaSuccess) e = cudaMalloc(&h->d_z0, max_traj * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&h->d_jumps, max_traj * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc(&h->d_margin, kMaxGrid * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_obs, sizeof(ObsTerms));
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_obs, &h->obs, sizeof(ObsTerms), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !gates.empty())
         e = cudaMemcpy(h->d_gates, gates.data(), gates.size() * sizeof(TrajGate), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
@@ -685,6 +873,160 @@ int llg_traj_create(int n, const llg_op* ops, int nops, double gamma_ad, double 
         return rc;
     }
     *out = h;
+    return LLG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int llg_traj_destroy(llg_traj* h) {
+    if (!h) return LLG_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    drop_graph(h);
+    cudaFree(h->d_gates);
+    cudaFree(h->d_z0);
+    cudaFree(h->d_jumps);
+    cudaFree(h->d_margin);
+    cudaFree(h->d_obs);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return LLG_OK;
+}
+
+int llg_traj_create(int n, const llg_op* ops, int nops, double gamma_ad, double lambda_pd, int precision,
+                    uint64_t max_traj, int cluster, int cta_threads, llg_traj** out) {
+    if (!out) return set_error(LLG_EINVAL, "traj_create: out is NULL");
+    *out = nullptr;
+    if (n < 1 || n > 14) return set_error(LLG_EINVAL, "traj_run: n must be in [1, 14]");
+    if (precision != LLG_F64 && precision != LLG_DF64 && precision != LLG_F32)
+        return set_error(LLG_EINVAL, "traj_run: unknown precision");
+    if (nops < 0 || (nops > 0 && !ops)) return set_error(LLG_EINVAL, "traj_run: NULL argument");
+    if (!(gamma_ad >= 0.0 && gamma_ad <= 1.0) || !(lambda_pd >= 0.0 && lambda_pd <= 1.0))
+        return set_error(LLG_EINVAL, "traj_run: gamma and lambda must be in [0, 1]");
+    if (max_traj == 0) return set_error(LLG_EINVAL, "traj_create: max_traj must be positive");
+    if (cluster < LLG_TUNE_AUTO || cluster > 2 || cta_threads < LLG_TUNE_AUTO)
+        return set_error(LLG_EINVAL, "traj_create: cluster must be -1, 0, 1 or 2 and cta_threads >= -1");
+    std::vector<TrajGate> gates;
+    int64_t sites = 0;
+    std::string err;
+    if (!build_gates(n, ops, nops, precision, NOISE_KRAUS, 0, gates, sites, err)) return set_error(LLG_EINVAL, err);
+    KrausParams kp;
+    std::memset(&kp, 0, sizeof(kp));
+    kp.gamma = gamma_ad;
+    kp.lambda = lambda_pd;
+    kp.sq1mg = std::sqrt(1.0 - gamma_ad);
+    kp.sq1ml = std::sqrt(1.0 - lambda_pd);
+    kp.mode = NOISE_KRAUS;
+    ObsTerms ob;
+    std::memset(&ob, 0, sizeof(ob));
+    const uint64_t key =
+        tune_hash_ops(tune_hash(tune_hash(1469598103934665603ULL, 0x54524a), (uint64_t)n << 8 | (uint64_t)precision), ops, nops);
+    return create_handle(n, precision, gates, sites, kp, ob, key, max_traj, cluster, cta_threads, out);
+}
+
+int llg_noisy_create(int n, const llg_op* ops, int nops, double p, int scale, int precision, uint64_t max_traj,
+                     int nterms, const int* za, const int* zb, const double* zcoeff, int cluster, int cta_threads,
+                     llg_traj** out) {
+    if (!out) return set_error(LLG_EINVAL, "noisy_create: out is NULL");
+    *out = nullptr;
+    if (n < 1 || n > 14) return set_error(LLG_EINVAL, "noisy_create: n must be in [1, 14]");
+    if (precision != LLG_F64 && precision != LLG_DF64 && precision != LLG_F32)
+        return set_error(LLG_EINVAL, "noisy_create: unknown precision");
+    if (nops < 0 || (nops > 0 && !ops)) return set_error(LLG_EINVAL, "noisy_create: NULL argument");
+    if (!(p >= 0.0 && p <= 1.0)) return set_error(LLG_EINVAL, "NoisyBackend: p must be in [0, 1]");
+    if (scale < 1 || scale > 99 || scale % 2 == 0)
+        return set_error(LLG_EINVAL, "NoisyBackend::set_scale: scale must be an odd integer in [1, 99]");
+    if (max_traj == 0) return set_error(LLG_EINVAL, "noisy_create: max_traj must be positive");
+    if (cluster < LLG_TUNE_AUTO || cluster > 2 || cta_threads < LLG_TUNE_AUTO)
+        return set_error(LLG_EINVAL, "noisy_create: cluster must be -1, 0, 1 or 2 and cta_threads >= -1");
+    std::vector<TrajGate> gates;
+    int64_t sites = 0;
+    std::string err;
+    if (!build_gates(n, ops, nops, precision, NOISE_DEPOL, (scale - 1) / 2, gates, sites, err))
+        return set_error(LLG_EINVAL, err);
+    ObsTerms ob;
+    if (!build_obs(n, nterms, za, zb, zcoeff, ob, err)) return set_error(LLG_EINVAL, "noisy_create: " + err);
+    KrausParams kp;
+    std::memset(&kp, 0, sizeof(kp));
+    kp.gamma = p;
+    kp.mode = NOISE_DEPOL;
+    uint64_t key = tune_hash(tune_hash(tune_hash(1469598103934665603ULL, 0x44504c), (uint64_t)n << 8 | (uint64_t)precision),
+                             (uint64_t)scale);
+    key = tune_hash_ops(key, ops, nops);
+    return create_handle(n, precision, gates, sites, kp, ob, key, max_traj, cluster, cta_threads, out);
+}
+
+int llg_richardson_weights(const double* scales, int nscales, double* weights) {
+    if (!scales || !weights || nscales < 2) return set_error(LLG_EINVAL, "ZNE::richardson_weights: need at least 2 scales");
+    for (int k = 0; k < nscales; ++k)
+        if (!std::isfinite(scales[k]) || scales[k] == 0.0)
+            return set_error(LLG_EINVAL, "ZNE::richardson_weights: scales must be finite and nonzero");
+    for (int k = 0; k < nscales; ++k) {
+        double c = 1.0;
+        for (int j = 0; j < nscales; ++j) {
+            if (j == k) continue;
+            if (scales[j] == scales[k]) return set_error(LLG_EINVAL, "ZNE::richardson_weights: scales must be distinct");
+            c *= scales[j] / (scales[j] - scales[k]);
+        }
+        weights[k] = c;
+    }
+    return LLG_OK;
+}
+
+int llg_zne_run(int n, const llg_op* ops, int nops, double p, int precision, const double* scales, int nscales,
+                int64_t trajectories, uint64_t seed, int nterms, const int* za, const int* zb, const double* zcoeff,
+                llg_zne_result* out) {
+    if (!out || !scales) return set_error(LLG_EINVAL, "ZNE::extrapolate: NULL argument");
+    if (trajectories < 1) return set_error(LLG_EINVAL, "ZNE: trajectories must be >= 1");
+    if (nscales < 2 || nscales > LLG_ZNE_MAX_SCALES)
+        return set_error(LLG_EINVAL, "ZNE::validate_scales: need between 2 and 8 noise scales");
+    for (int k = 0; k < nscales; ++k) {
+        const double v = scales[k];
+        if (!std::isfinite(v) || v < 1.0 || v > 99.0 || v != std::floor(v) || std::fmod(v, 2.0) != 1.0)
+            return set_error(LLG_EINVAL, "ZNE::validate_scales: each scale must be an odd integer in [1, 99]");
+        for (int j = 0; j < k; ++j)
+            if (scales[j] == v) return set_error(LLG_EINVAL, "ZNE::validate_scales: scales must be distinct");
+    }
+    if (!(p >= 0.0 && p <= 1.0)) return set_error(LLG_EINVAL, "NoisyBackend: p must be in [0, 1]");
+    llg_zne_result r;
+    std::memset(&r, 0, sizeof(r));
+    int rc = llg_richardson_weights(scales, nscales, r.weights);
+    if (rc) return rc;
+    if (nops < 1) return set_error(LLG_ERUNTIME, "ZNE::extrapolate: circuit_fn applied no gates to the backend");
+    const bool noisy = p > 0.0;
+    const int64_t nt = noisy ? trajectories : 1;
+    r.nscales = nscales;
+    r.trajectories = nt;
+    std::vector<double> vals((size_t)nt);
+    for (int k = 0; k < nscales && !rc; ++k) {
+        llg_traj* h = nullptr;
+        rc = llg_noisy_create(n, ops, nops, p, (int)scales[k], precision, (uint64_t)nt, nterms, za, zb, zcoeff, 0, 0, &h);
+        if (!rc) rc = llg_traj_launch(h, seed, (uint64_t)k * (uint64_t)nt, (uint64_t)nt, vals.data(), nullptr, nullptr);
+        llg_traj_destroy(h);
+        if (rc) break;
+        double mean = 0.0, m2 = 0.0;  // Welford, as the reference (src/Mitigation.h:350-353)
+        for (int64_t t = 0; t < nt; ++t) {
+            if (!std::isfinite(vals[t])) return set_error(LLG_EINVAL, "ZNE::extrapolate: observable returned a non-finite value");
+            const double d = vals[t] - mean;
+            mean += d / (double)(t + 1);
+            m2 += d * (vals[t] - mean);
+        }
+        double se = 0.0;
+        if (nt > 1) se = std::sqrt(std::max(0.0, m2 / (double)(nt - 1)) / (double)nt);
+        else if (noisy) se = std::nan("");
+        r.scales[k] = scales[k];
+        r.values[k] = mean;
+        r.std_errors[k] = se;
+    }
+    if (rc) return rc;
+    double var = 0.0;
+    for (int k = 0; k < nscales; ++k) {
+        r.value += r.weights[k] * r.values[k];
+        var += r.weights[k] * r.weights[k] * r.std_errors[k] * r.std_errors[k];
+    }
+    r.std_error = std::sqrt(var);
+    *out = r;
     return LLG_OK;
 }
 

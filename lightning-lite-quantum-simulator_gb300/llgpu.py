@@ -138,6 +138,9 @@ def lib() -> ctypes.CDLL:
             "llg_traj_autotune": (i, [vp, u64, vp]),
             "llg_traj_config": (i, [vp, P(i), P(i), P(i), P(ctypes.c_int64)]),
             "llg_traj_stream": (i, [vp, P(vp)]),
+            "llg_noisy_create": (i, [i, vp, i, d, i, i, u64, i, vp, vp, vp, i, i, P(vp)]),
+            "llg_richardson_weights": (i, [vp, i, vp]),
+            "llg_zne_run": (i, [i, vp, i, d, i, vp, i, ctypes.c_int64, u64, i, vp, vp, vp, vp]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
@@ -505,6 +508,59 @@ class Traj:
             self.close()
         except Exception:
             pass
+
+
+class NoisyTraj(Traj):
+    """Depolarizing-noise trajectories of a folded circuit (batched ll::NoisyBackend); launch()
+    returns (observable[n_traj], non-identity Paulis[n_traj], margin)."""
+
+    def __init__(self, n: int, ops: np.ndarray, p: float, scale: int, max_traj: int, terms=(),
+                 precision: str = "complex128", cluster: int = 0, cta_threads: int = 0):
+        self._ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
+        self._h = ctypes.c_void_p()
+        self.max_traj = int(max_traj)
+        a, b, c = _obs_terms(terms)
+        check(lib().llg_noisy_create(n, _ptr(self._ops) if self._ops.size else None, self._ops.size, p, scale,
+                                     PRECISIONS[precision], self.max_traj, a.size, _ptr(a), _ptr(b), _ptr(c),
+                                     cluster, cta_threads, ctypes.byref(self._h)))
+
+
+def _obs_terms(terms):
+    """[(a, b, coeff), ...] with b = -1 for a single Z -> three contiguous arrays."""
+    terms = list(terms)
+    a = np.ascontiguousarray([t[0] for t in terms], dtype=np.int32)
+    b = np.ascontiguousarray([t[1] for t in terms], dtype=np.int32)
+    c = np.ascontiguousarray([t[2] for t in terms], dtype=np.float64)
+    return a, b, c
+
+
+ZNE_DTYPE = np.dtype([("value", np.float64), ("std_error", np.float64), ("nscales", np.int32), ("pad", np.int32),
+                      ("trajectories", np.int64), ("scales", np.float64, (8,)), ("values", np.float64, (8,)),
+                      ("std_errors", np.float64, (8,)), ("weights", np.float64, (8,))])
+
+
+def richardson_weights(scales) -> np.ndarray:
+    s = np.ascontiguousarray(scales, dtype=np.float64)
+    w = np.zeros(s.size)
+    check(lib().llg_richardson_weights(_ptr(s), s.size, _ptr(w)))
+    return w
+
+
+def zne(n: int, ops: np.ndarray, p: float, scales=(1, 3, 5), trajectories: int = 1000, seed: int = 1, terms=(),
+        precision: str = "complex128") -> dict:
+    """ll::ZNE::extrapolate over the GPU noisy trajectories: value, std_error, per-scale values,
+    standard errors and Richardson weights."""
+    ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
+    s = np.ascontiguousarray(scales, dtype=np.float64)
+    a, b, c = _obs_terms(terms)
+    r = np.zeros(1, dtype=ZNE_DTYPE)
+    check(lib().llg_zne_run(n, _ptr(ops) if ops.size else None, ops.size, p, PRECISIONS[precision], _ptr(s), s.size,
+                            trajectories, seed, a.size, _ptr(a), _ptr(b), _ptr(c), _ptr(r)))
+    k = int(r["nscales"][0])
+    return {"value": float(r["value"][0]), "std_error": float(r["std_error"][0]),
+            "trajectories": int(r["trajectories"][0]), "scales": r["scales"][0][:k].copy(),
+            "values": r["values"][0][:k].copy(), "std_errors": r["std_errors"][0][:k].copy(),
+            "weights": r["weights"][0][:k].copy()}
 
 
 # ---------------------------------------------------------------------------------------------

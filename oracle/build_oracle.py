@@ -6,7 +6,8 @@
   ``oracle/_ref/``: the pybind11 modules ``quantum_sim_v3`` (src/StateVectorOptimized.cpp) and
   ``quantum_sim_v2`` (src/bindings_v2.cpp) with the reference's own build flags
   (README.md:124-133: ``-O3 -Wall -shared -std=c++17 -fopenmp -fPIC``), and ``libref.so`` from
-  ref_capi.cpp over the header-only src/Backend.h, src/StateVectorBackend.h, src/Algorithms.h.
+  ref_capi.cpp over the header-only src/Backend.h, src/StateVectorBackend.h, src/Algorithms.h and
+  src/Mitigation.h.
   It needs the reference tree and pybind11 headers, so it only runs where both exist.
 
 Run ``python oracle/build_oracle.py [--ref]``.
@@ -44,7 +45,7 @@ def oracle_lib_path() -> str:
 
 def build_oracle(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    srcs = [os.path.join(HERE, f) for f in ("sv_oracle.c", "traj_oracle.c", "adjoint_oracle.c")]
+    srcs = [os.path.join(HERE, f) for f in ("sv_oracle.c", "traj_oracle.c", "adjoint_oracle.c", "noise_oracle.c")]
     out = oracle_lib_path()
     if force or _stale(out, srcs + [os.path.join(HERE, "sv_oracle.h")]):
         tmp = out + ".tmp"
@@ -80,7 +81,7 @@ def build_ref(ref: str = DEFAULT_REF, force: bool = False) -> dict[str, str]:
              os.path.join(src, "bindings_v2.cpp"), "-I" + py_inc, "-I" + pb_inc]),
         os.path.join(REF_OUT, "libref.so"): (
             [os.path.join(HERE, "ref_capi.cpp"), os.path.join(src, "StateVectorBackend.h"),
-             os.path.join(src, "Algorithms.h"), os.path.join(src, "Backend.h")],
+             os.path.join(src, "Algorithms.h"), os.path.join(src, "Backend.h"), os.path.join(src, "Mitigation.h")],
             ["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-I" + src, "-I" + HERE,
              os.path.join(HERE, "ref_capi.cpp")]),
     }

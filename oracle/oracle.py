@@ -44,6 +44,10 @@ def lib() -> ctypes.CDLL:
             "orc_traj_run": (i, [i, vp, i, d, d, u64, u64, u64, vp, vp, vp, ctypes.c_int64, P(d)]),
             "orc_density_z0": (i, [i, vp, i, d, d, P(d)]),
             "orc_param_shift": (i, [i, vp, i, vp, i, i, vp, vp, vp, P(d), vp]),
+            "orc_mt64_first": (u64, [u64, i]),
+            "orc_noisy_run": (i, [i, vp, i, d, i, i, u64, u64, u64, i, vp, vp, vp, vp, vp]),
+            "orc_richardson_weights": (i, [vp, i, vp]),
+            "orc_zne": (i, [i, vp, i, d, vp, i, i, i, u64, i, vp, vp, vp, vp]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
@@ -166,3 +170,56 @@ def param_shift(n: int, ops: np.ndarray, params: np.ndarray, a, b, coeff):
     if rc:
         raise ValueError(f"oracle parameter shift failed (rc={rc})")
     return e.value, g
+
+
+RNG_PHILOX, RNG_MT = 0, 1
+
+
+def _terms(terms):
+    """[(a, b, coeff), ...] (b = -1: Z_a alone) -> int32 / int32 / float64 arrays."""
+    terms = list(terms) or [(0, -1, 1.0)]
+    a = np.ascontiguousarray([t[0] for t in terms], dtype=np.int32)
+    b = np.ascontiguousarray([t[1] for t in terms], dtype=np.int32)
+    c = np.ascontiguousarray([t[2] for t in terms], dtype=np.float64)
+    return a, b, c
+
+
+def noisy_run(n: int, ops: np.ndarray, p: float, scale: int, seed: int, begin: int, end: int, terms=(),
+              rng: int = RNG_PHILOX):
+    """Observable per trajectory and non-identity Pauli count per trajectory of the folded
+    depolarizing-noise circuit (NoisyBackend restatement)."""
+    ops = np.ascontiguousarray(ops)
+    a, b, c = _terms(terms)
+    obs = np.zeros(end - begin)
+    paulis = np.zeros(end - begin, dtype=np.uint32)
+    rc = lib().orc_noisy_run(n, _p(ops), ops.size, p, scale, rng, seed, begin, end, a.size, _p(a), _p(b), _p(c),
+                             _p(obs), _p(paulis))
+    if rc:
+        raise ValueError(f"oracle noisy run failed (rc={rc})")
+    return obs, paulis
+
+
+def richardson_weights(scales) -> np.ndarray:
+    s = np.ascontiguousarray(scales, dtype=np.float64)
+    w = np.zeros(s.size)
+    if lib().orc_richardson_weights(_p(s), s.size, _p(w)):
+        raise ValueError("bad scales")
+    return w
+
+
+def zne(n: int, ops: np.ndarray, p: float, scales, trajectories: int, seed: int, terms=(), rng: int = RNG_PHILOX):
+    """ZNE::extrapolate restatement: dict(value, std_error, trajectories, values, std_errors,
+    weights).  Raises ValueError (bad arguments) or RuntimeError (no gates)."""
+    ops = np.ascontiguousarray(ops)
+    s = np.ascontiguousarray(scales, dtype=np.float64)
+    a, b, c = _terms(terms)
+    ns = s.size
+    out = np.zeros(4 * ns + 3)
+    rc = lib().orc_zne(n, _p(ops) if ops.size else None, ops.size, p, _p(s), ns, trajectories, rng, seed, a.size,
+                       _p(a), _p(b), _p(c), _p(out))
+    if rc == 3:
+        raise RuntimeError("circuit applied no gates")
+    if rc:
+        raise ValueError(f"oracle zne failed (rc={rc})")
+    return {"value": out[0], "std_error": out[1], "trajectories": int(out[2]), "values": out[3:3 + ns],
+            "std_errors": out[3 + ns:3 + 2 * ns], "weights": out[3 + 2 * ns:3 + 3 * ns]}

@@ -3,7 +3,8 @@
 //
 // Built by oracle/build_oracle.py with -I<reference>/src into oracle/_ref/libref.so, directly
 // from the reference's headers where they lie: src/Backend.h (ReferenceBackend),
-// src/StateVectorBackend.h (StateVectorBackend) and src/Algorithms.h (Grover, VQE::prepare).
+// src/StateVectorBackend.h (StateVectorBackend), src/Algorithms.h (Grover, VQE::prepare) and
+// src/Mitigation.h (NoisyBackend, ZNE).
 // Nothing from the reference is copied here; this file only drives its classes.
 
 #include <complex>
@@ -15,6 +16,7 @@
 
 #include "Algorithms.h"
 #include "Backend.h"
+#include "Mitigation.h"
 #include "StateVectorBackend.h"
 
 #include "sv_oracle.h"
@@ -161,6 +163,74 @@ int ref_vqe_prepare(int n, int layers, const double* params, double* out_state) 
         return 0;
     } catch (const std::invalid_argument&) {
         return 1;
+    } catch (...) {
+        return 2;
+    }
+}
+
+// Diagonal observable sum_k c[k] Z_a[k] Z_b[k] (b < 0: Z_a) from the backend's probabilities().
+static double zz_observable(const ll::Backend& b, int nterms, const int* za, const int* zb, const double* zc) {
+    const std::vector<double> p = b.probabilities();
+    double e = 0.0;
+    for (std::size_t i = 0; i < p.size(); ++i) {
+        double d = 0.0;
+        for (int k = 0; k < nterms; ++k) {
+            int par = (int)((i >> za[k]) & 1);
+            if (zb[k] >= 0) par ^= (int)((i >> zb[k]) & 1);
+            d += par ? -zc[k] : zc[k];
+        }
+        e += p[i] * d;
+    }
+    return e;
+}
+
+// ll::NoisyBackend over ll::ReferenceBackend (Mitigation.h:110-240): `ntraj` trajectories in order
+// on one noisy backend (one mt19937_64 stream), the observable of each.
+int ref_noisy_obs(int n, const orc_op* ops, int nops, double p, int scale, uint64_t seed, int ntraj, int nterms,
+                  const int* za, const int* zb, const double* zc, double* out) {
+    try {
+        ll::ReferenceBackend inner(n);
+        ll::NoisyBackend nb(inner, p, seed);
+        nb.set_scale(scale);
+        for (int t = 0; t < ntraj; ++t) {
+            run_on(nb, n, ops, nops);
+            out[t] = zz_observable(nb, nterms, za, zb, zc);
+        }
+        return 0;
+    } catch (const std::invalid_argument&) {
+        return 1;
+    } catch (...) {
+        return 2;
+    }
+}
+
+// ll::ZNE::extrapolate (Mitigation.h:313-377).  out: value, std_error, trajectories, then
+// values[ns], std_errors[ns], weights[ns].  Returns 1 for std::invalid_argument, 3 for
+// std::runtime_error, 2 otherwise.
+int ref_zne(int n, const orc_op* ops, int nops, double p, uint64_t seed, const double* scales, int ns, int trajectories,
+            int nterms, const int* za, const int* zb, const double* zc, double* out) {
+    try {
+        ll::ReferenceBackend inner(n);
+        ll::NoisyBackend nb(inner, p, seed);
+        nb.reset(n);
+        const ll::ZNE zne(trajectories);
+        const ll::ZNEResult r = zne.extrapolate(
+            nb, [&](ll::Backend& b) { run_on(b, n, ops, nops); },
+            [&](const ll::Backend& b) { return zz_observable(b, nterms, za, zb, zc); },
+            std::vector<double>(scales, scales + ns));
+        out[0] = r.value;
+        out[1] = r.std_error;
+        out[2] = r.trajectories;
+        for (int k = 0; k < ns; ++k) {
+            out[3 + k] = r.values[k];
+            out[3 + ns + k] = r.std_errors[k];
+            out[3 + 2 * ns + k] = r.weights[k];
+        }
+        return 0;
+    } catch (const std::invalid_argument&) {
+        return 1;
+    } catch (const std::runtime_error&) {
+        return 3;
     } catch (...) {
         return 2;
     }

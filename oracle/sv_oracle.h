@@ -13,6 +13,7 @@ extern "C" {
 
 #define ORC_EINVAL 1
 #define ORC_ENOMEM 2
+#define ORC_ERUNTIME 3
 
 /* Op record.  Kinds 0..6 are the Op kinds of tests/test_backends.cpp:78-83 in the reference
  * (h, x, rx, ry, rz, cnot, mcz); 7 = cz, 8 = generic 2x2 (quantum_sim_v3 gate list). */
@@ -67,6 +68,17 @@ int orc_traj_run(int n, const orc_op* ops, int nops, double gamma_ad, double lam
                  uint64_t traj_begin, uint64_t traj_end, double* z0_out, uint32_t* jump_counts,
                  uint8_t* jump_log, int64_t jump_log_stride, double* margin_out);
 int orc_density_z0(int n, const orc_op* ops, int nops, double gamma_ad, double lambda_pd, double* z0_out);
+
+/* noise_oracle.c: NoisyBackend + ZNE restatement */
+#define ORC_RNG_PHILOX 0
+#define ORC_RNG_MT 1
+uint64_t orc_mt64_first(uint64_t seed, int k);
+int orc_noisy_run(int n, const orc_op* ops, int nops, double p, int scale, int rng, uint64_t seed, uint64_t traj_begin,
+                  uint64_t traj_end, int nterms, const int* za, const int* zb, const double* zc, double* obs_out,
+                  uint32_t* paulis_out);
+int orc_richardson_weights(const double* scales, int ns, double* w);
+int orc_zne(int n, const orc_op* ops, int nops, double p, const double* scales, int ns, int trajectories, int rng,
+            uint64_t seed, int nterms, const int* za, const int* zb, const double* zc, double* out);
 
 /* adjoint_oracle.c */
 int orc_param_shift(int n, const orc_op* ops, int nops, const double* params, int nparams, int nterms,

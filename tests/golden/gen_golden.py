@@ -1,8 +1,9 @@
 """Writes the golden fixtures in this directory by running the REFERENCE's own code.
 
 Runs only where the reference tree is present (it is read at /root/reference, never copied):
-  * oracle/_ref/libref.so -- ll::ReferenceBackend, ll::StateVectorBackend, ll::Grover and
-    ll::VQE::prepare compiled from the reference headers (oracle/build_oracle.py --ref);
+  * oracle/_ref/libref.so -- ll::ReferenceBackend, ll::StateVectorBackend, ll::Grover,
+    ll::VQE::prepare, ll::NoisyBackend and ll::ZNE compiled from the reference headers
+    (oracle/build_oracle.py --ref);
   * oracle/_ref/quantum_sim_v3 / quantum_sim_v2 -- the reference pybind11 modules built from
     src/StateVectorOptimized.cpp and src/bindings_v2.cpp;
   * python/gate_fusion.py imported from the reference tree.
@@ -44,6 +45,8 @@ def load_ref():
     L.ref_random_circuit.argtypes = [vp, i, i, vp]
     L.ref_grover.argtypes = [i, vp, i, i, vp, ctypes.POINTER(i), ctypes.POINTER(i)]
     L.ref_vqe_prepare.argtypes = [i, i, vp, vp]
+    L.ref_noisy_obs.argtypes = [i, vp, i, d, i, u64, i, i, vp, vp, vp, vp]
+    L.ref_zne.argtypes = [i, vp, i, d, u64, vp, i, i, i, vp, vp, vp, vp]
     mods = {}
     for name in ("quantum_sim_v3", "quantum_sim_v2"):
         path = [p for k, p in paths.items() if k.startswith(name)][0]
@@ -264,6 +267,65 @@ def gen_hea(L):
     np.savez_compressed(os.path.join(HERE, "hea_param_shift.npz"), **out)
 
 
+def noise_circuits():
+    """Our own seeded circuits for the NoisyBackend / ZNE fixtures: every gate kind the noise
+    sites distinguish (1-qubit gates, cnot, 2-qubit cz, 1- and 3-qubit mcz)."""
+    from llgpu import OP_CNOT, OP_CZ, OP_H, OP_MCZ, OP_RX, OP_RY, OP_RZ, OP_X, make_ops
+
+    rng = np.random.default_rng(6060)
+    recs = []
+    for _ in range(5):
+        recs += [(OP_H, int(rng.integers(3))), (OP_RY, int(rng.integers(3)), 0, float(rng.uniform(-3, 3))),
+                 (OP_CNOT, 0, 2), (OP_RZ, 2, 0, float(rng.uniform(-3, 3))), (OP_CZ, 1, 2),
+                 (OP_MCZ, 0, 0, 0.0, 0b111), (OP_X, 1), (OP_RX, 0, 0, float(rng.uniform(-3, 3))),
+                 (OP_CNOT, 1, 0), (OP_MCZ, 0, 0, 0.0, 0b100)]
+    three = make_ops(recs)
+    one = make_ops([(OP_RY, 0, 0, 0.9), (OP_RZ, 0, 0, -0.6), (OP_RX, 0, 0, 0.35)])
+    bell = make_ops([(OP_H, 0), (OP_CNOT, 0, 1)])
+    return three, one, bell
+
+
+def gen_noise(L):
+    three, one, bell = noise_circuits()
+    terms3 = (np.array([0, 2], dtype=np.int32), np.array([1, -1], dtype=np.int32), np.array([1.0, 0.5]))
+    z0 = (np.array([0], dtype=np.int32), np.array([-1], dtype=np.int32), np.array([1.0]))
+    zz = (np.array([0], dtype=np.int32), np.array([1], dtype=np.int32), np.array([1.0]))
+    out = {"three_ops": three, "one_ops": one, "bell_ops": bell}
+
+    def obs(ops, n, p, scale, seed, ntraj, terms):
+        a, b, c = terms
+        v = np.zeros(ntraj)
+        rc = L.ref_noisy_obs(n, ops.ctypes.data, ops.size, p, scale, seed, ntraj, a.size, a.ctypes.data,
+                             b.ctypes.data, c.ctypes.data, v.ctypes.data)
+        assert rc == 0, rc
+        return v
+
+    def zne(ops, n, p, seed, scales, ntraj, terms):
+        a, b, c = terms
+        s = np.array(scales, dtype=np.float64)
+        o = np.zeros(3 + 3 * s.size)
+        rc = L.ref_zne(n, ops.ctypes.data if ops.size else None, ops.size, p, seed, s.ctypes.data, s.size, ntraj,
+                       a.size, a.ctypes.data, b.ctypes.data, c.ctypes.data, o.ctypes.data)
+        return rc, o
+
+    # per-trajectory observables on one NoisyBackend (one mt19937_64 stream)
+    out["obs3_p05_s1"] = obs(three, 3, 0.05, 1, 2024, 200, terms3)
+    out["obs3_p05_s3"] = obs(three, 3, 0.05, 3, 2024, 200, terms3)
+    out["obs3_p0_s5"] = obs(three, 3, 0.0, 5, 1, 3, terms3)
+    # ZNE::extrapolate
+    cases = {"zne3": (three, 3, 0.03, 77, [1, 3, 5], 300, terms3), "zne1": (one, 1, 0.02, 2024, [1, 3], 2000, z0),
+             "zne_bell": (bell, 2, 0.03, 99, [1, 3], 1000, zz), "zne_p0": (three, 3, 0.0, 5, [1, 3, 5], 7, terms3),
+             "zne_single": (one, 1, 0.02, 3, [1, 3], 1, z0)}
+    for name, (ops, n, p, seed, scales, ntraj, terms) in cases.items():
+        rc, o = zne(ops, n, p, seed, scales, ntraj, terms)
+        assert rc == 0, (name, rc)
+        out[name] = o
+    # the contract: bad scales are invalid_argument (1); a circuit without gates is runtime_error (3)
+    out["zne_rc_bad_scale"] = np.array(zne(one, 1, 0.02, 1, [1, 4], 10, z0)[0])
+    out["zne_rc_no_gates"] = np.array(zne(one[:0], 1, 0.02, 1, [1, 3], 10, z0)[0])
+    np.savez_compressed(os.path.join(HERE, "noisy_zne.npz"), **out)
+
+
 def main():
     L, mods = load_ref()
     gen_random_2024(L)
@@ -274,6 +336,7 @@ def main():
     gen_grover(L)
     gen_vqe(L)
     gen_hea(L)
+    gen_noise(L)
     print("fixtures written to", HERE)
 
 
