@@ -279,10 +279,11 @@ def run_ours(args, rank, world, local):
     adj = None
     if not args.no_adjoint:
         adj = run_adjoint_bench(args, torch)
-    traj = batch = None
+    traj = batch = zne = None
     if not args.no_forms:
         traj = run_traj_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
         batch = run_batch_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
+        zne = run_zne_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -324,6 +325,7 @@ def run_ours(args, rank, world, local):
         "adjoint": adj,
         "trajectories": traj,
         "mixed_batch": batch,
+        "zne": zne,
     }
     print(json.dumps(line), flush=True)
 
@@ -506,6 +508,45 @@ def run_traj_bench(args, torch, cpu: bool):
         out["cpu_baseline"] = {"value": sample / dt, "unit": "traj/s", "cores": os.cpu_count(), "kind": "port",
                                "sample": f"first {sample} trajectories, oracle restatement of the Kraus-jump step"}
     return out
+
+
+def run_zne_bench(args, torch, cpu: bool):
+    """Zero-noise extrapolation with the reference NoisyBackend's depolarizing model: a 12-qubit,
+    4-layer RX/RY + CNOT-chain circuit (100 gates), p = 0.005 per site, fold scales {1, 3, 5},
+    4096 trajectories per scale, observable sum_i Z_i Z_i+1 (ring); complex128."""
+    import llgpu
+    import workloads
+
+    n, p, scales, ntraj, seed = 12, 0.005, [1, 3, 5], 4096, 909
+    ops = workloads.noisy_layers(n, 4)
+    terms = [(q, (q + 1) % n, 1.0) for q in range(n)]
+    llgpu.zne(n, ops, p, scales, 256, seed, terms)  # warm-up (module load, first launches)
+    t0 = time.perf_counter()
+    r = llgpu.zne(n, ops, p, scales, ntraj, seed, terms)
+    dt = time.perf_counter() - t0
+    st = llgpu.State(n)
+    st.apply_ops(ops)
+    ideal = st.expect_zz([t[0] for t in terms], [t[1] for t in terms], [t[2] for t in terms])
+    st.close()
+    total = ntraj * len(scales)
+    res = {"workload": f"ZNE: {n} qubits, {len(ops)} gates, p = {p}, scales {scales}, {ntraj} trajectories per "
+                       f"scale, observable ring ZZ", "traj_per_s": total / dt, "seconds": dt,
+           "value": r["value"], "std_error": r["std_error"], "values": [float(v) for v in r["values"]],
+           "ideal": ideal, "unmitigated_error": abs(float(r["values"][0]) - ideal),
+           "mitigated_error": abs(r["value"] - ideal)}
+    if cpu:
+        import oracle
+
+        oracle.set_threads(os.cpu_count() or 1)
+        sample = 64
+        t0 = time.perf_counter()
+        for s in scales:
+            oracle.noisy_run(n, ops, p, s, seed, 0, sample, terms)
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": sample * len(scales) / dt, "unit": "traj/s", "cores": os.cpu_count(),
+                               "kind": "port", "sample": f"{sample} trajectories per scale, oracle restatement of "
+                                                         "NoisyBackend with folding"}
+    return res
 
 
 def run_batch_bench(args, torch, cpu: bool):

@@ -63,3 +63,25 @@ def test_grover_through_gpu_backend(built, golden):
         assert r.returncode == 0, r.stderr
         p = np.array([float(x) for x in r.stdout.split()])
         assert np.max(np.abs(p - g[key + "_probs"])) <= 1e-12
+
+
+def test_gpu_zne_header_compiles_and_validates(built):
+    # CPU side: the driver builds against the restated interface; bad arguments are rejected on
+    # the host before any GPU work (p out of range -> invalid_argument)
+    exe = compile_driver("zne_on_gpu.cpp", "zne_gpu", os.path.join(CPP, "iface"))
+    r = subprocess.run([exe, "1.5", "10"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 3 and "p must be in [0, 1]" in r.stderr
+
+
+@pytest.mark.gpu
+def test_gpu_zne_through_the_cpp_interface(built):
+    exe = compile_driver("zne_on_gpu.cpp", "zne_gpu", os.path.join(CPP, "iface"))
+    r = subprocess.run([exe, "0.03", "40000"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.split("\n")
+    value, se = (float(x) for x in lines[0].split())
+    r2 = 1 - 16 * 0.03 / 15
+    for line in lines[1:3]:
+        s, v, e = (float(x) for x in line.split())
+        assert abs(v - r2 ** s) < 5 * e
+    assert abs(value - 1.0) < abs(float(lines[1].split()[1]) - 1.0)  # mitigated closer to the ideal 1
