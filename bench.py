@@ -451,6 +451,24 @@ def run_sweep_bench(args, torch):
             per = ms / cnt / 1e3
             gbs = bytes_per.get(name, 32) * (1 << n) / per / 1e9
             res[name] = {"ms_per_sweep": per * 1e3, "gbs": gbs, "frac": gbs / peak}
+        # dense k-qubit blocks (llg_apply_matrix): 32 B x 2^n per application and 8 x 4^k x 2^(n-k)
+        # real FLOP of complex multiply-adds
+        rng = np.random.default_rng(17)
+        for k, qs in ((2, [0, n - 1]), (5, [0, 7, 13, 22, n - 1])):
+            m, _ = np.linalg.qr(rng.normal(size=(1 << k, 1 << k)) + 1j * rng.normal(size=(1 << k, 1 << k)))
+            st.apply_matrix(qs, m)  # warm-up
+            st.sync()
+            st.profile(True)
+            st.profile_read(reset=True)
+            for _ in range(2):
+                st.apply_matrix(qs, m)
+            st.sync()
+            ms, cnt = st.profile_read(reset=True)["gate"]
+            st.profile(False)
+            per = ms / cnt / 1e3
+            gbs = 32 * (1 << n) / per / 1e9
+            res[f"block{k}"] = {"ms_per_sweep": per * 1e3, "gbs": gbs, "frac": gbs / peak,
+                                "tflops": 8 * (4 ** k) * (1 << (n - k)) / per / 1e12, "qubits": qs}
         st.close()
         out[prec] = res
     return out

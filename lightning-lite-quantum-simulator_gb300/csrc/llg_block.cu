@@ -1,0 +1,127 @@
+// llg_block.cu -- dense k-qubit blocks (llg_apply_matrix, include/llgpu.h): a 2^k x 2^k complex
+// matrix applied to every group of 2^k amplitudes that differ only in the k target qubits, the
+// fused form of python/gate_fusion.py:7-37 widened to k qubits (k <= 5).
+//
+// One warp holds 32 >> k groups, one lane per row: lane r of a group loads amplitude r (the
+// group's base index with the bits of r deposited at the target positions, bit j -> qubits[j]),
+// then forms row r of M a with the group's amplitudes broadcast by warp shuffles.  The matrix sits
+// in shared memory.  complex128 (double-float) rows are accumulated as exact products summed with
+// TwoSum (the Dot2 scheme of Ogita, Rump and Oishi, SIAM J. Sci. Comput. 2005) and rounded once to
+// double-float; FP64 and complex64 rows use fused multiply-adds.
+#include <cuda_runtime.h>
+
+#include "llg_common.cuh"
+#include "llg_internal.h"
+#include "llg_launch.h"
+
+namespace llg {
+
+namespace {
+
+constexpr int kBlockThreads = 256;
+
+__device__ __forceinline__ float shfl(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ double shfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ df shfl(df v, int src) { return {shfl(v.hi, src), shfl(v.lo, src)}; }
+
+// Row accumulators: sum of products a * b.
+struct DotDF {  // Dot2: s + e carries the sum; products split exactly by FMA
+    float s = 0.0f, e = 0.0f;
+    __device__ __forceinline__ void add(df a, df b) {
+        const float p = __fmul_rn(a.hi, b.hi);
+        const float pe = fmaf(a.hi, b.hi, -p);
+        const df t = two_sum(s, p);
+        s = t.hi;
+        float c = fmaf(a.hi, b.lo, pe);
+        c = fmaf(a.lo, b.hi, c);
+        e = __fadd_rn(e, __fadd_rn(c, t.lo));
+    }
+    __device__ __forceinline__ df value() const { return fast_two_sum(s, e); }
+};
+struct DotD {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
+    __device__ __forceinline__ double value() const { return s; }
+};
+struct DotF {
+    float s = 0.0f;
+    __device__ __forceinline__ void add(float a, float b) { s = fmaf(a, b, s); }
+    __device__ __forceinline__ float value() const { return s; }
+};
+template <class P> struct DotOf;
+template <> struct DotOf<PolDF64> { using T = DotDF; };
+template <> struct DotOf<PolF64> { using T = DotD; };
+template <> struct DotOf<PolF32> { using T = DotF; };
+
+template <class P>
+__global__ void __launch_bounds__(kBlockThreads) k_block(typename P::S* __restrict__ psi, int n, BlockDesc bd,
+                                                         const uint64_t* __restrict__ mat) {
+    using K = typename P::K;
+    using C = typename P::C;
+    using D = typename DotOf<P>::T;
+    // (re, im) per entry, stored transposed (column-major): at step j the lanes of a group read
+    // M[r][j] for consecutive r, so a warp's reads are contiguous instead of one bank apart
+    __shared__ K sm[2 * kMaxBlockDim * kMaxBlockDim];
+    const int k = bd.k, dk = 1 << k;
+    for (int i = threadIdx.x; i < dk * dk; i += blockDim.x) {
+        const int row = i / dk, col = i % dk;
+        sm[2 * (col * dk + row)] = P::k_from_bits(mat[2 * i]);
+        sm[2 * (col * dk + row) + 1] = P::k_from_bits(mat[2 * i + 1]);
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int r = lane & (dk - 1);
+    const int gsub = lane >> k;
+    const int gpw = 32 >> k;
+    uint64_t toff = 0;
+    for (int j = 0; j < k; ++j)
+        if ((r >> j) & 1) toff |= 1ULL << bd.q[j];
+    const uint64_t ngroups = 1ULL << (n - k);
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    // g0 is the same on every lane of the warp, so every shuffle below has all 32 lanes
+    for (uint64_t g0 = warp * gpw; g0 < ngroups; g0 += nwarps * gpw) {
+        const uint64_t g = g0 + (uint64_t)gsub;
+        const bool valid = g < ngroups;
+        const uint64_t idx = insert0_mask(valid ? g : 0, bd.tmask) | toff;
+        C a;
+        if (valid) a = P::load(psi[idx]);
+        else a.re = a.im = P::zero();
+        D re, im;
+        const int src0 = gsub << k;
+        for (int j = 0; j < dk; ++j) {
+            const auto xr = shfl(a.re, src0 | j), xi = shfl(a.im, src0 | j);
+            const K mr = sm[2 * (j * dk + r)], mi = sm[2 * (j * dk + r) + 1];
+            re.add(mr, xr);
+            re.add(P::kneg(mi), xi);
+            im.add(mr, xi);
+            im.add(mi, xr);
+        }
+        C out;
+        out.re = re.value();
+        out.im = im.value();
+        if (valid) psi[idx] = P::store(out);
+    }
+}
+
+template <class P>
+cudaError_t block_t(void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat, cudaStream_t s) {
+    const uint64_t ngroups = 1ULL << (n - bd.k);
+    const uint64_t warps = (ngroups + (uint64_t)(32 >> bd.k) - 1) / (uint64_t)(32 >> bd.k);
+    const uint64_t blocks = (warps + kBlockThreads / 32 - 1) / (kBlockThreads / 32);
+    const unsigned grid = (unsigned)(blocks < 152ULL * 8 ? blocks : 152ULL * 8);
+    k_block<P><<<grid, kBlockThreads, 0, s>>>(static_cast<typename P::S*>(psi), n, bd, d_mat);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_block(int P, void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat, cudaStream_t s) {
+    switch (P) {
+        case LLG_F64: return block_t<PolF64>(psi, n, bd, d_mat, s);
+        case LLG_F32: return block_t<PolF32>(psi, n, bd, d_mat, s);
+        default: return block_t<PolDF64>(psi, n, bd, d_mat, s);
+    }
+}
+
+}  // namespace llg

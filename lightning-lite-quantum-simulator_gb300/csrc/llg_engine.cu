@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/llgpu.h"
+#include "llg_common_host.h"
 #include "llg_internal.h"
 #include "llg_launch.h"
 
@@ -58,6 +59,11 @@ struct llg_state {
     ExecOp* h_ops = nullptr;
     size_t h_ops_cap = 0;
     cudaEvent_t ops_done = nullptr;
+    // dense-block matrix upload (pinned staging, reused once the previous copy has finished)
+    uint64_t* d_block = nullptr;
+    uint64_t* h_block = nullptr;
+    cudaEvent_t block_done = nullptr;
+    bool block_pending = false;
     // reductions
     double* d_partials = nullptr;
     double* d_red = nullptr;
@@ -368,6 +374,9 @@ int llg_destroy(llg_state* st) {
         if (st->stage_ev[i]) cudaEventDestroy(st->stage_ev[i]);
     }
     if (st->ops_done) cudaEventDestroy(st->ops_done);
+    if (st->d_block) cudaFree(st->d_block);
+    if (st->h_block) cudaFreeHost(st->h_block);
+    if (st->block_done) cudaEventDestroy(st->block_done);
     for (auto& r : st->prof_recs) {
         cudaEventDestroy(r.a);
         cudaEventDestroy(r.b);
@@ -510,11 +519,38 @@ int llg_apply_ops(llg_state* st, const llg_op* ops, int nops) {
 }
 
 int llg_apply_matrix(llg_state* st, int k, const int* qubits, const double* m) {
-    (void)st;
-    (void)k;
-    (void)qubits;
-    (void)m;
-    return set_error(LLG_EINVAL, "apply_matrix: not available in this build");
+    if (!st || !qubits || !m) return set_error(LLG_EINVAL, "apply_matrix: NULL argument");
+    if (k < 1 || k > kMaxBlockQubits || k > st->n)
+        return set_error(LLG_EINVAL, "apply_matrix: k must be in [1, 5] and at most the register size");
+    BlockDesc bd;
+    std::memset(&bd, 0, sizeof(bd));
+    bd.k = k;
+    for (int j = 0; j < k; ++j) {
+        int rc = check_qubit(st, qubits[j], "apply_matrix");
+        if (rc) return rc;
+        if ((bd.tmask >> qubits[j]) & 1) return set_error(LLG_EINVAL, "apply_matrix: repeated qubit");
+        bd.tmask |= 1ULL << qubits[j];
+        bd.q[j] = qubits[j];
+    }
+    const int slots = 2 << (2 * k);  // 2 * 4^k
+    for (int i = 0; i < slots; ++i)
+        if (!std::isfinite(m[i])) return set_error(LLG_EINVAL, "apply_matrix: non-finite matrix entry");
+    int rc = llg_flush(st);  // earlier gates first
+    if (rc) return rc;
+    const size_t cap = (size_t)2 * kMaxBlockDim * kMaxBlockDim;
+    if (!st->d_block) {
+        LLG_CUDA(cudaMalloc(&st->d_block, cap * sizeof(uint64_t)), "cudaMalloc(block)");
+        LLG_CUDA(cudaHostAlloc((void**)&st->h_block, cap * sizeof(uint64_t), cudaHostAllocDefault), "cudaHostAlloc(block)");
+        LLG_CUDA(cudaEventCreateWithFlags(&st->block_done, cudaEventDisableTiming), "cudaEventCreate");
+    }
+    if (st->block_pending) LLG_CUDA(cudaEventSynchronize(st->block_done), "block staging");
+    for (int i = 0; i < slots; ++i) st->h_block[i] = pack_coef(st->P, m[i]);
+    LLG_CUDA(cudaMemcpyAsync(st->d_block, st->h_block, slots * sizeof(uint64_t), cudaMemcpyHostToDevice, st->stream),
+             "cudaMemcpyAsync(block)");
+    LLG_CUDA(cudaEventRecord(st->block_done, st->stream), "cudaEventRecord");
+    st->block_pending = true;
+    return traced(st, LLG_PROF_GATE, 1, "block kernel",
+                  [&] { return launch_block(st->P, st->d_psi, st->n, bd, st->d_block, st->stream); });
 }
 
 int llg_flush(llg_state* st) {

@@ -43,6 +43,17 @@ cudaError_t launch_reduce_z(int P, const void* psi, int n, const ZTerms& terms, 
 
 int tile_max_qubits(int P);
 
+// dense k-qubit block (llg_block.cu): bit j of a row/column index is qubit q[j]; the matrix is
+// 2 * 4^k coefficient slots, row-major (re, im), packed for the state's precision
+constexpr int kMaxBlockQubits = 5;
+constexpr int kMaxBlockDim = 1 << kMaxBlockQubits;
+struct BlockDesc {
+    int32_t k;
+    int32_t q[kMaxBlockQubits];
+    uint64_t tmask;
+};
+cudaError_t launch_block(int P, void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat, cudaStream_t s);
+
 // process-wide tuning cache (llg_tune.cu), keyed by an FNV-1a hash of the workload's shape
 uint64_t tune_hash(uint64_t h, uint64_t v);
 uint64_t tune_hash_ops(uint64_t h, const llg_op* ops, int nops);

@@ -156,6 +156,16 @@ public:
         }
     }
 
+    // dense k-qubit block (k <= 5): `m` is a 2^k x 2^k complex128 array (or nested lists);
+    // bit j of its row / column index is qubits[j]
+    void apply_matrix(const std::vector<int>& qubits, py::object m) {
+        py::array_t<std::complex<double>, py::array::c_style | py::array::forcecast> a(m);
+        const size_t dim = (size_t)1 << qubits.size();
+        if (qubits.empty() || qubits.size() > 5 || (size_t)a.size() != dim * dim)
+            throw py::value_error("apply_matrix: need 1..5 qubits and a 2^k x 2^k matrix");
+        check(llg_apply_matrix(st_, (int)qubits.size(), qubits.data(), reinterpret_cast<const double*>(a.data())));
+    }
+
     void apply_ops(py::array ops) {
         if (ops.itemsize() * ops.size() % (py::ssize_t)sizeof(llg_op) != 0 || !(ops.flags() & py::array::c_style))
             throw py::type_error("apply_ops needs a C-contiguous array of llg_op records");
@@ -342,6 +352,7 @@ PYBIND11_MODULE(quantum_sim_v3, m) {
         .def("mcz", &StateVector::mcz)
         .def("apply_fused", &StateVector::apply_fused)
         .def("apply_ops", &StateVector::apply_ops)
+        .def("apply_matrix", &StateVector::apply_matrix, py::arg("qubits"), py::arg("matrix"))
         .def("set_fusion", &StateVector::set_fusion, py::arg("mode"), py::arg("tile_qubits") = 0)
         .def("autotune", &StateVector::autotune, py::arg("ops"), py::arg("sample_ops") = 0)
         .def("flush", &StateVector::flush)

@@ -287,6 +287,15 @@ class State:
         ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
         check(lib().llg_apply_ops(self._h, _ptr(ops) if ops.size else None, ops.size))
 
+    def apply_matrix(self, qubits: Sequence[int], m) -> None:
+        """Dense 2^k x 2^k complex block on `qubits` (k <= 5); bit j of the block's row / column
+        index is qubits[j]."""
+        qs = np.ascontiguousarray(qubits, dtype=np.int32)
+        mm = np.ascontiguousarray(np.asarray(m, dtype=np.complex128).reshape(-1))
+        if mm.size != (1 << (2 * qs.size)):
+            raise ValueError("apply_matrix: matrix must be 2^k x 2^k for k qubits")
+        check(lib().llg_apply_matrix(self._h, qs.size, _ptr(qs), _ptr(mm)))
+
     def flush(self): check(lib().llg_flush(self._h))
     def sync(self): check(lib().llg_sync(self._h))
 

@@ -1,0 +1,87 @@
+"""Dense k-qubit blocks (llg_apply_matrix, k <= 5) against the oracle's restatement
+(orc_apply_matrix), interleaved with queued gates, through the C ABI and the drop-in module."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import llgpu
+import oracle
+import workloads
+
+pytestmark = pytest.mark.gpu
+TOL = {"complex128": 1e-12, "fp64": 1e-12, "complex64": 5e-5}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built(built):
+    assert llgpu.device_count() > 0
+
+
+def rand_unitary(d, rng):
+    q, r = np.linalg.qr(rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d)))
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+@pytest.mark.parametrize("precision", ["complex128", "fp64", "complex64"])
+@pytest.mark.parametrize("n,k", [(4, 1), (6, 2), (8, 3), (11, 4), (13, 5), (5, 5), (3, 2), (16, 5)])
+def test_block_matches_oracle(precision, n, k):
+    ops = workloads.layered_rotations(n, 2, seed=n)
+    st2 = llgpu.State(n, precision)
+    st2.apply_ops(ops)
+    want = oracle.run_ops(n, ops)
+    rng = np.random.default_rng(1000 * n + k)
+    for rep in range(3):
+        qs = [int(x) for x in rng.choice(n, size=k, replace=False)]
+        m = rand_unitary(1 << k, rng)
+        q = int(rng.integers(n))
+        st2.apply_matrix(qs, m)
+        st2.rx(q, 0.3)
+        oracle.apply_matrix(want, n, qs, m)
+        want = oracle.run_ops(n, llgpu.make_ops([(llgpu.OP_RX, q, 0, 0.3)]), want)
+    assert np.max(np.abs(st2.state() - want)) <= TOL[precision]
+    st2.close()
+
+
+def test_non_unitary_block_and_high_qubits():
+    rng = np.random.default_rng(3)
+    n = 20
+    st = llgpu.State(n)
+    psi = (rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)) / 1000.0
+    st.load(psi)
+    want = psi.copy()
+    for qs in ([19, 18, 17], [0, 19], [5, 1, 12, 19, 0]):
+        m = rng.normal(size=(1 << len(qs),) * 2) + 1j * rng.normal(size=(1 << len(qs),) * 2)
+        st.apply_matrix(qs, m)
+        oracle.apply_matrix(want, n, qs, m)
+    got = st.state()
+    assert np.max(np.abs(got - want)) <= 1e-12 * max(1.0, np.max(np.abs(want)))
+    st.close()
+
+
+def test_block_contract():
+    st = llgpu.State(4)
+    eye = np.eye(4)
+    with pytest.raises(ValueError):
+        st.apply_matrix([0, 0], eye)  # repeated qubit
+    with pytest.raises(ValueError):
+        st.apply_matrix([0, 4], eye)  # outside the register
+    with pytest.raises(ValueError):
+        st.apply_matrix([0, 1], np.full((4, 4), np.nan))
+    with pytest.raises(ValueError):
+        st.apply_matrix([0, 1, 2, 3, 0, 1], np.eye(64))  # k > 5
+    st.close()
+
+
+def test_drop_in_module_apply_matrix():
+    import quantum_sim_v3
+
+    rng = np.random.default_rng(8)
+    sv = quantum_sim_v3.StateVector(7)
+    m = rand_unitary(8, rng)
+    sv.h(0)
+    sv.apply_matrix([2, 0, 5], m)
+    want = oracle.zero_state(7)
+    want = oracle.run_ops(7, llgpu.make_ops([(llgpu.OP_H, 0)]), want)
+    oracle.apply_matrix(want, 7, [2, 0, 5], m)
+    assert np.max(np.abs(sv.get_numpy_view() - want)) <= 1e-12
