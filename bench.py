@@ -279,11 +279,12 @@ def run_ours(args, rank, world, local):
     adj = None
     if not args.no_adjoint:
         adj = run_adjoint_bench(args, torch)
-    traj = batch = zne = None
+    traj = batch = zne = config1 = None
     if not args.no_forms:
         traj = run_traj_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
         batch = run_batch_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
         zne = run_zne_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
+        config1 = run_config1_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -326,6 +327,7 @@ def run_ours(args, rank, world, local):
         "trajectories": traj,
         "mixed_batch": batch,
         "zne": zne,
+        "config1_12q": config1,
     }
     print(json.dumps(line), flush=True)
 
@@ -526,6 +528,73 @@ def run_traj_bench(args, torch, cpu: bool):
         out["cpu_baseline"] = {"value": sample / dt, "unit": "traj/s", "cores": os.cpu_count(), "kind": "port",
                                "sample": f"first {sample} trajectories, oracle restatement of the Kraus-jump step"}
     return out
+
+
+def run_config1_bench(args, torch, cpu: bool):
+    """The published 12-qubit workload: 1000 ops, H (p = 0.5) on a uniform qubit else CNOT on a
+    uniform distinct pair, from |0..0>, amplitudes read back.  The 64 KiB state is one shared-
+    memory tile, so the whole circuit is one launch.  Reported: device time per circuit (CUDA
+    events), end to end through quantum_sim_v3 with the op list in one call and with one Python
+    call per gate (each with the full host readback), and the published reference time."""
+    import llgpu
+    import quantum_sim_v3
+    import workloads
+    from llgpu import OP_CNOT, OP_H
+
+    n, reps = 12, 50
+    ops = workloads.mixed_h_cnot(n, 1000, seed=1234)
+    st = llgpu.State(n)
+    stream = torch.cuda.ExternalStream(st.stream)
+
+    def one():
+        st.reset(n)
+        st.apply_ops(ops)
+        st.flush()
+
+    one()
+    st.sync()
+    launches0 = llgpu.kernel_launches()
+    dt, _ = _timed(stream, torch, one, reps=reps)
+    launches = (llgpu.kernel_launches() - launches0) / reps
+    got = st.state()
+    st.close()
+    sv = quantum_sim_v3.StateVector(n)
+    sv.get_numpy_view()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        sv.reset(n)
+        sv.apply_ops(ops)
+        view = sv.get_numpy_view()
+    e2e_batch = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        sv.reset(n)
+        for o in ops:
+            if o["kind"] == OP_H:
+                sv.h(int(o["q0"]))
+            else:
+                sv.cnot(int(o["q0"]), int(o["q1"]))
+        view = sv.get_numpy_view()
+    e2e_calls = (time.perf_counter() - t0) / reps
+    res = {"workload": "12 qubits, 1000 ops (H p=0.5 else CNOT), seed 1234, from |0..0>", "device_ms": dt * 1e3,
+           "launches_per_circuit": launches, "e2e_ms_op_list": e2e_batch * 1e3, "e2e_ms_per_gate_calls": e2e_calls * 1e3,
+           "ops_per_s_device": 1000 / dt, "published_reference_ms": 25.91,
+           "published_reference_note": "8 cores, README.md:17-27 / docs/RESULTS.md:19-25"}
+    del view
+    if cpu:
+        import oracle
+
+        want = oracle.run_ops(n, ops)
+        res["max_abs_diff_vs_oracle"] = float(np.max(np.abs(got - want)))
+        for threads in (1, os.cpu_count() or 1):
+            oracle.set_threads(threads)
+            best = 1e9
+            for _ in range(5):
+                t0 = time.perf_counter()
+                oracle.run_ops(n, ops)
+                best = min(best, time.perf_counter() - t0)
+            res[f"cpu_ms_{threads}t"] = best * 1e3
+    return res
 
 
 def run_zne_bench(args, torch, cpu: bool):
