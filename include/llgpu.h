@@ -164,6 +164,19 @@ int llg_apply_ops(llg_state* st, const llg_op* ops, int nops);
  * the block's local index.  k in [1, 5], distinct qubits in [0, n). */
 int llg_apply_matrix(llg_state* st, int k, const int* qubits, const double* m);
 
+/* ---- density matrices (the reference's KrausChannel, src/Noise.h:85-147) ----
+ * rho on n qubits lives in a state of 2n qubits: element (row, col) is amplitude
+ * row + col * 2^n, so qubit q is bit q of the row and qubit n + q bit q of the column.  Create it
+ * with llg_create(2n, ...) (|0..0> of 2n qubits is |0..0><0..0|) or llg_create_from_host. */
+/* U rho U^+ for one gate record on qubits [0, n): U on the row qubits, conj(U) on the column
+ * qubits. */
+int llg_dm_apply_op(llg_state* st, int n, const llg_op* op);
+/* KrausChannel::apply (src/Noise.cpp:174-258): rho <- sum_k K_k rho K_k^+ for nkraus operators
+ * of 2^m x 2^m (m = 1 or 2; row-major, interleaved; bit j of an operator's index is
+ * targets[j]), applied as one dense block sum_k K_k (x) conj(K_k) on the 2m row and column
+ * qubits.  Operators must be trace preserving to 1e-10 (src/Noise.cpp:166-172). */
+int llg_dm_apply_kraus(llg_state* st, int n, int nkraus, const double* kraus, int m, const int* targets);
+
 /* ---- execution and readout ---- */
 
 /* Plan and launch the pending queue without waiting. */

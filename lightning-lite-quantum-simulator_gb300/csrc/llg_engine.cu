@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -551,6 +552,73 @@ int llg_apply_matrix(llg_state* st, int k, const int* qubits, const double* m) {
     st->block_pending = true;
     return traced(st, LLG_PROF_GATE, 1, "block kernel",
                   [&] { return launch_block(st->P, st->d_psi, st->n, bd, st->d_block, st->stream); });
+}
+
+int llg_dm_apply_op(llg_state* st, int n, const llg_op* op) {
+    if (!st || !op) return set_error(LLG_EINVAL, "dm_apply_op: NULL argument");
+    if (n < 1 || n > 17 || st->n != 2 * n) return set_error(LLG_EINVAL, "dm_apply_op: the state must hold 2n qubits");
+    const bool two = op->kind == LLG_OP_CNOT || op->kind == LLG_OP_CZ;
+    if (op->kind == LLG_OP_MCZ) {
+        if (op->mask == 0 || (op->mask >> n) != 0) return set_error(LLG_EINVAL, "dm_apply_op: mcz mask outside the register");
+    } else if (op->q0 < 0 || op->q0 >= n || (two && (op->q1 < 0 || op->q1 >= n))) {
+        return set_error(LLG_EINVAL, "dm_apply_op: qubit outside the register");
+    }
+    // U rho U^+: U on the row qubits [0, n), conj(U) on the column qubits [n, 2n)
+    llg_op col = *op;
+    col.q0 = op->q0 + n;
+    col.q1 = op->q1 + n;
+    col.mask = op->mask << n;
+    if (op->kind == LLG_OP_RX || op->kind == LLG_OP_RZ) col.theta = -op->theta;
+    if (op->kind == LLG_OP_U2)
+        for (int i = 0; i < 4; ++i) col.m[2 * i + 1] = -op->m[2 * i + 1];
+    const llg_op pair[2] = {*op, col};
+    return llg_apply_ops(st, pair, 2);
+}
+
+int llg_dm_apply_kraus(llg_state* st, int n, int nkraus, const double* kraus, int m, const int* targets) {
+    if (!st || !kraus || !targets) return set_error(LLG_EINVAL, "KrausChannel::apply: NULL argument");
+    if (n < 1 || n > 17 || st->n != 2 * n) return set_error(LLG_EINVAL, "KrausChannel::apply: the state must hold 2n qubits");
+    if (m < 1 || m > 2 || nkraus < 1) return set_error(LLG_EINVAL, "KrausChannel::apply: 1 or 2 targets and at least one operator");
+    for (int j = 0; j < m; ++j) {
+        if (targets[j] < 0 || targets[j] >= n) return set_error(LLG_EINVAL, "KrausChannel::apply: target qubit outside the register");
+        for (int i = 0; i < j; ++i)
+            if (targets[i] == targets[j]) return set_error(LLG_EINVAL, "KrausChannel: repeated target qubit");
+    }
+    const int d = 1 << m;
+    typedef std::complex<double> cd;
+    auto K = [&](int k, int r, int c) { return cd(kraus[2 * ((size_t)k * d * d + r * d + c)], kraus[2 * ((size_t)k * d * d + r * d + c) + 1]); };
+    // trace preservation to 1e-10 (src/Noise.cpp:166-172, DEFAULT_TOL)
+    double worst = 0.0;
+    for (int i = 0; i < d; ++i)
+        for (int j = 0; j < d; ++j) {
+            cd sum = 0.0;
+            for (int k = 0; k < nkraus; ++k)
+                for (int r = 0; r < d; ++r) sum += std::conj(K(k, r, i)) * K(k, r, j);
+            if (i == j) sum -= 1.0;
+            if (!std::isfinite(sum.real()) || !std::isfinite(sum.imag())) return set_error(LLG_EINVAL, "KrausChannel: non-finite operator entry");
+            worst = std::max(worst, std::abs(sum));
+        }
+    if (!(worst <= 1e-10)) return set_error(LLG_EINVAL, "KrausChannel: operators are not trace preserving");
+    // superoperator S = sum_k K (x) conj(K) on qubits [targets..., n + targets...]: block index
+    // bits 0..m-1 are the row targets, bits m..2m-1 the column targets
+    const int D = d * d;
+    std::vector<double> S((size_t)2 * D * D, 0.0);
+    for (int k = 0; k < nkraus; ++k)
+        for (int r = 0; r < d; ++r)
+            for (int c = 0; c < d; ++c)
+                for (int r2 = 0; r2 < d; ++r2)
+                    for (int c2 = 0; c2 < d; ++c2) {
+                        const cd v = K(k, r, r2) * std::conj(K(k, c, c2));
+                        const size_t e = (size_t)(r | (c << m)) * D + (size_t)(r2 | (c2 << m));
+                        S[2 * e] += v.real();
+                        S[2 * e + 1] += v.imag();
+                    }
+    int qs[4];
+    for (int j = 0; j < m; ++j) {
+        qs[j] = targets[j];
+        qs[m + j] = targets[j] + n;
+    }
+    return llg_apply_matrix(st, 2 * m, qs, S.data());
 }
 
 int llg_flush(llg_state* st) {

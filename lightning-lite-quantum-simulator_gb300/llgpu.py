@@ -139,6 +139,8 @@ def lib() -> ctypes.CDLL:
             "llg_traj_config": (i, [vp, P(i), P(i), P(i), P(ctypes.c_int64)]),
             "llg_traj_stream": (i, [vp, P(vp)]),
             "llg_noisy_create": (i, [i, vp, i, d, i, i, u64, i, vp, vp, vp, i, i, P(vp)]),
+            "llg_dm_apply_op": (i, [vp, i, vp]),
+            "llg_dm_apply_kraus": (i, [vp, i, i, vp, i, vp]),
             "llg_richardson_weights": (i, [vp, i, vp]),
             "llg_zne_run": (i, [i, vp, i, d, i, vp, i, ctypes.c_int64, u64, i, vp, vp, vp, vp]),
         }
@@ -570,6 +572,86 @@ def zne(n: int, ops: np.ndarray, p: float, scales=(1, 3, 5), trajectories: int =
             "trajectories": int(r["trajectories"][0]), "scales": r["scales"][0][:k].copy(),
             "values": r["values"][0][:k].copy(), "std_errors": r["std_errors"][0][:k].copy(),
             "weights": r["weights"][0][:k].copy()}
+
+
+# ---------------------------------------------------------------------------------------------
+# density matrices (the reference's KrausChannel on a GPU-resident rho)
+# ---------------------------------------------------------------------------------------------
+_PAULI = [np.eye(2), np.array([[0, 1], [1, 0]]), np.array([[0, -1j], [1j, 0]]), np.diag([1.0, -1.0])]
+
+
+def amplitude_damping(gamma: float):
+    """Kraus operators of src/Noise.cpp:274-285."""
+    if not 0.0 <= gamma <= 1.0:
+        raise ValueError("KrausChannel::amplitude_damping: gamma must be in [0, 1]")
+    return [np.array([[1, 0], [0, np.sqrt(max(0.0, 1 - gamma))]], dtype=complex),
+            np.array([[0, np.sqrt(gamma)], [0, 0]], dtype=complex)]
+
+
+def phase_damping(lam: float):
+    """Kraus operators of src/Noise.cpp:287-298."""
+    if not 0.0 <= lam <= 1.0:
+        raise ValueError("KrausChannel::phase_damping: lambda must be in [0, 1]")
+    return [np.array([[1, 0], [0, np.sqrt(max(0.0, 1 - lam))]], dtype=complex),
+            np.array([[0, 0], [0, np.sqrt(lam)]], dtype=complex)]
+
+
+def depolarizing(p: float, m: int = 1):
+    """DepolarizingChannel(p, m).to_kraus (src/Noise.cpp:309-333): sqrt(1-p) I and
+    sqrt(p / (4^m - 1)) P for each non-identity Pauli string; digit j of the string code (base 4)
+    acts on target j, the most significant target first in the Kronecker product."""
+    if not 0.0 <= p <= 1.0 or m not in (1, 2):
+        raise ValueError("DepolarizingChannel: p in [0, 1] and 1 or 2 qubits")
+    ops = []
+    for code in range(4 ** m):
+        w = np.sqrt(1 - p) if code == 0 else np.sqrt(p / (4 ** m - 1))
+        if w > 0:
+            mat = np.eye(1)
+            for j in range(m - 1, -1, -1):
+                mat = np.kron(mat, _PAULI[(code >> (2 * j)) & 3])
+            ops.append(w * mat)
+    return ops
+
+
+class DensityMatrix:
+    """rho on n qubits held on the GPU as a 2n-qubit state (element (row, col) at amplitude
+    row + col * 2^n).  Gates act as U rho U^+; kraus() applies the reference's
+    KrausChannel::apply."""
+
+    def __init__(self, n: int, precision: str = "complex128", rho: np.ndarray | None = None):
+        self.n = int(n)
+        if rho is None:
+            self._st = State(2 * self.n, precision)
+        else:
+            rho = np.asarray(rho, dtype=np.complex128)
+            if rho.shape != (1 << self.n, 1 << self.n):
+                raise ValueError("rho must be 2^n x 2^n")
+            self._st = State(precision=precision, amps=np.ascontiguousarray(rho.T).reshape(-1))
+
+    def apply_ops(self, ops: np.ndarray) -> None:
+        for op in np.ascontiguousarray(ops, dtype=OP_DTYPE):
+            one = np.ascontiguousarray(np.array([op], dtype=OP_DTYPE))
+            check(lib().llg_dm_apply_op(self._st.handle, self.n, _ptr(one)))
+
+    def kraus(self, ops, targets: Sequence[int]) -> None:
+        kk = np.ascontiguousarray(np.asarray(ops, dtype=np.complex128))
+        tg = np.ascontiguousarray(targets, dtype=np.int32)
+        if kk.ndim != 3 or kk.shape[1] != kk.shape[2] or kk.shape[1] != (1 << tg.size):
+            raise ValueError("KrausChannel: operators must be 2^m x 2^m for m targets")
+        check(lib().llg_dm_apply_kraus(self._st.handle, self.n, kk.shape[0], _ptr(kk), tg.size, _ptr(tg)))
+
+    def rho(self) -> np.ndarray:
+        dim = 1 << self.n
+        return np.ascontiguousarray(self._st.state().reshape(dim, dim).T)
+
+    def probabilities(self) -> np.ndarray:
+        return np.real(np.diag(self.rho())).copy()
+
+    def trace(self) -> complex:
+        return complex(np.trace(self.rho()))
+
+    def close(self) -> None:
+        self._st.close()
 
 
 # ---------------------------------------------------------------------------------------------

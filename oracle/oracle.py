@@ -48,6 +48,9 @@ def lib() -> ctypes.CDLL:
             "orc_noisy_run": (i, [i, vp, i, d, i, i, u64, u64, u64, i, vp, vp, vp, vp, vp]),
             "orc_richardson_weights": (i, [vp, i, vp]),
             "orc_zne": (i, [i, vp, i, d, vp, i, i, i, u64, i, vp, vp, vp, vp]),
+            "orc_kraus_trace_preserving": (i, [i, vp, i, d]),
+            "orc_kraus_apply": (i, [vp, i, i, vp, i, vp]),
+            "orc_dm_apply_op": (i, [vp, i, vp]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
@@ -223,3 +226,42 @@ def zne(n: int, ops: np.ndarray, p: float, scales, trajectories: int, seed: int,
         raise ValueError(f"oracle zne failed (rc={rc})")
     return {"value": out[0], "std_error": out[1], "trajectories": int(out[2]), "values": out[3:3 + ns],
             "std_errors": out[3 + ns:3 + 2 * ns], "weights": out[3 + 2 * ns:3 + 3 * ns]}
+
+
+def dm_zero(n: int) -> np.ndarray:
+    """|0..0><0..0| as a dim x dim complex matrix (row, col)."""
+    rho = np.zeros((1 << n, 1 << n), dtype=np.complex128)
+    rho[0, 0] = 1.0
+    return rho
+
+
+def _dm_buf(rho: np.ndarray) -> np.ndarray:
+    # element (row, col) at row + col * dim: the column-major order of the matrix
+    return np.ascontiguousarray(rho.T)
+
+
+def kraus_apply(rho: np.ndarray, n: int, ops, targets) -> np.ndarray:
+    """KrausChannel::apply restatement: sum_k K rho K^+ on `targets` (bit j of K's index is
+    targets[j])."""
+    buf = _dm_buf(rho)
+    kk = np.ascontiguousarray(np.asarray(ops, dtype=np.complex128))
+    tg = np.ascontiguousarray(targets, dtype=np.int32)
+    rc = lib().orc_kraus_apply(_p(buf), n, kk.shape[0], _p(kk), tg.size, _p(tg))
+    if rc:
+        raise ValueError("oracle kraus_apply rejected its arguments")
+    return np.ascontiguousarray(buf.T)
+
+
+def kraus_trace_preserving(ops, tol: float = 1e-10) -> bool:
+    kk = np.ascontiguousarray(np.asarray(ops, dtype=np.complex128))
+    m = int(np.log2(kk.shape[1]))
+    return bool(lib().orc_kraus_trace_preserving(kk.shape[0], _p(kk), m, tol))
+
+
+def dm_apply_ops(rho: np.ndarray, n: int, ops: np.ndarray) -> np.ndarray:
+    buf = _dm_buf(rho)
+    for op in np.ascontiguousarray(ops):
+        one = np.ascontiguousarray(np.array([op]))
+        if lib().orc_dm_apply_op(_p(buf), n, _p(one)):
+            raise ValueError("oracle dm_apply_op rejected an op")
+    return np.ascontiguousarray(buf.T)

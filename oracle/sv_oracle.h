@@ -69,6 +69,11 @@ int orc_traj_run(int n, const orc_op* ops, int nops, double gamma_ad, double lam
                  uint8_t* jump_log, int64_t jump_log_stride, double* margin_out);
 int orc_density_z0(int n, const orc_op* ops, int nops, double gamma_ad, double lambda_pd, double* z0_out);
 
+/* dm_oracle.c: KrausChannel::apply restatement; rho(row, col) at row + col * 2^n */
+int orc_kraus_trace_preserving(int nk, const double* ops, int m, double tol);
+int orc_kraus_apply(double* rho, int n, int nk, const double* ops, int m, const int* targets);
+int orc_dm_apply_op(double* rho, int n, const orc_op* op);
+
 /* noise_oracle.c: NoisyBackend + ZNE restatement */
 #define ORC_RNG_PHILOX 0
 #define ORC_RNG_MT 1
