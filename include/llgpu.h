@@ -326,6 +326,41 @@ int llg_zne_run(int n, const llg_op* ops, int nops, double p, int precision, con
                 int64_t trajectories, uint64_t seed, int nterms, const int* za, const int* zb, const double* zcoeff,
                 llg_zne_result* out);
 
+/* ---- dense trajectory solver (the reference's TrajectorySolver, src/TrajectorySolver.h) ----
+ * Lindblad equation d rho/dt = -i [H(t), rho] + sum_k gamma_k (L rho L^+ - {L^+L, rho}/2) on
+ * n <= 10 qubits with dense dim x dim operators (row-major, interleaved), unravelled into
+ * trajectories that run together in one persistent launch: STANDARD (norm-loss quantum jumps),
+ * PROJECTOR (Pauli-like channels as sqrt(g)(1 - P)) and ANALOG (homodyne diffusion).  Plans,
+ * step sizes, the jump selection and the error contract follow src/TrajectorySolver.h:124-514.
+ * Uniforms come from Philox4x32-10 (key = seed, counter = (draw, trajectory)), not the
+ * reference's per-trajectory mt19937_64 streams. */
+#define LLG_UNRAVEL_STANDARD 0
+#define LLG_UNRAVEL_PROJECTOR 1
+#define LLG_UNRAVEL_ANALOG 2
+typedef struct llg_tsolver llg_tsolver;
+/* H(t) callback: writes the dim x dim Hermitian matrix (row-major, interleaved) at time t. */
+typedef void (*llg_hamiltonian_fn)(double t, double* h_out, void* user);
+int llg_tsolver_create(int n_qubits, llg_tsolver** out);
+int llg_tsolver_destroy(llg_tsolver* s);
+int llg_tsolver_set_hamiltonian(llg_tsolver* s, const double* h);
+int llg_tsolver_set_hamiltonian_fn(llg_tsolver* s, llg_hamiltonian_fn fn, void* user);
+/* Adds gamma (L rho L^+ - 1/2 {L^+L, rho}); gamma = 0 adds nothing; at most 64 channels. */
+int llg_tsolver_add_lindblad(llg_tsolver* s, const double* l, double gamma);
+int llg_tsolver_clear_lindblad(llg_tsolver* s);
+int llg_tsolver_info(const llg_tsolver* s, int* n_channels, int* dim);
+int llg_tsolver_projector_applies(const llg_tsolver* s, int channel, int* out);
+/* n_traj trajectories from psi0 (normalised here) over `duration` with step ~dt.  Optional
+ * outputs: states_out (n_traj x dim complex), rho_out = (1/N) sum |psi><psi| (dim x dim, in
+ * trajectory order), obs_out[t] = <psi_t| obs |psi_t> for a Hermitian obs.  run_one is
+ * n_traj = 1. */
+int llg_tsolver_run(llg_tsolver* s, const double* psi0, double duration, double dt, int64_t n_traj, int kind,
+                    uint64_t seed, double* states_out, double* rho_out, const double* obs, double* obs_out);
+/* The last run's plan (row-major, interleaved): steps, h, constant H or not, the unraveling,
+ * the propagator, the RK4 / diffusion nodes (written when n_nodes <= max_nodes), the jump
+ * operators and their J^+ J. */
+int llg_tsolver_plan_export(const llg_tsolver* s, long long* steps, double* h, int* constant, int* kind, double* prop,
+                            double* nodes, int64_t max_nodes, double* ops, double* ops_dop, int* n_ops, int64_t* n_nodes);
+
 /* ---- mixed-size batches ----
  * `count` circuits (circuit c: n_qubits[c] in [1, 30], ops[op_offsets[c] .. op_offsets[c+1]))
  * planned into shared-memory tile passes of tile_qubits qubits (0: default, 12 or 13 for

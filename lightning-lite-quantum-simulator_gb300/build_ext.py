@@ -27,7 +27,8 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", *ARCH, "-
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-I" + INCLUDE, "-I" + CSRC]
 
 CU_SOURCES = ["llg_kernels.cu", "llg_engine.cu", "llg_noalloc.cu", "llg_adjoint.cu", "llg_traj.cu", "llg_batch.cu",
-              "llg_tune.cu", "llg_block.cu"]
+              "llg_tune.cu", "llg_block.cu",
+              "llg_tsolver.cu"]
 CXX_SOURCES = ["llg_plan.cpp"]
 
 LIB = os.path.join(HERE, "libllgpu.so")

@@ -140,6 +140,17 @@ def lib() -> ctypes.CDLL:
             "llg_traj_stream": (i, [vp, P(vp)]),
             "llg_noisy_create": (i, [i, vp, i, d, i, i, u64, i, vp, vp, vp, i, i, P(vp)]),
             "llg_dm_apply_op": (i, [vp, i, vp]),
+            "llg_tsolver_create": (i, [i, P(vp)]),
+            "llg_tsolver_destroy": (i, [vp]),
+            "llg_tsolver_set_hamiltonian": (i, [vp, vp]),
+            "llg_tsolver_set_hamiltonian_fn": (i, [vp, vp, vp]),
+            "llg_tsolver_add_lindblad": (i, [vp, vp, d]),
+            "llg_tsolver_clear_lindblad": (i, [vp]),
+            "llg_tsolver_info": (i, [vp, P(i), P(i)]),
+            "llg_tsolver_projector_applies": (i, [vp, i, P(i)]),
+            "llg_tsolver_run": (i, [vp, vp, d, d, ctypes.c_int64, i, u64, vp, vp, vp, vp]),
+            "llg_tsolver_plan_export": (i, [vp, P(ctypes.c_longlong), P(d), P(i), P(i), vp, vp, ctypes.c_int64, vp,
+                                            vp, P(i), P(ctypes.c_int64)]),
             "llg_dm_apply_kraus": (i, [vp, i, i, vp, i, vp]),
             "llg_richardson_weights": (i, [vp, i, vp]),
             "llg_zne_run": (i, [i, vp, i, d, i, vp, i, ctypes.c_int64, u64, i, vp, vp, vp, vp]),
@@ -652,6 +663,136 @@ class DensityMatrix:
 
     def close(self) -> None:
         self._st.close()
+
+
+# ---------------------------------------------------------------------------------------------
+# dense trajectory solver (the reference's TrajectorySolver)
+# ---------------------------------------------------------------------------------------------
+UNRAVEL = {"STANDARD": 0, "PROJECTOR": 1, "ANALOG": 2}
+_HFN = ctypes.CFUNCTYPE(None, ctypes.c_double, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p)
+
+
+def _cmat(m, dim: int) -> np.ndarray:
+    a = np.ascontiguousarray(np.asarray(m, dtype=np.complex128))
+    if a.shape != (dim, dim):
+        raise ValueError(f"operator must be {dim} x {dim}")
+    return a
+
+
+class TrajectorySolver:
+    """Lindblad trajectories with dense operators on n <= 10 qubits (src/TrajectorySolver.h),
+    every call one persistent GPU launch over all trajectories."""
+
+    def __init__(self, n_qubits: int):
+        self._h = ctypes.c_void_p()
+        check(lib().llg_tsolver_create(n_qubits, ctypes.byref(self._h)))
+        self.n_qubits = int(n_qubits)
+        self.dim = 1 << self.n_qubits
+        self._fn = None
+
+    def set_hamiltonian(self, h) -> None:
+        """A dim x dim Hermitian matrix, or a function t -> matrix (sampled at the plan's nodes)."""
+        if callable(h):
+            dim = self.dim
+
+            def cb(t, out, user):
+                m = np.ascontiguousarray(np.asarray(h(t), dtype=np.complex128))
+                if m.shape != (dim, dim):
+                    m = np.full((dim, dim), np.nan, dtype=np.complex128)
+                ctypes.memmove(out, m.ctypes.data, m.nbytes)
+
+            fn = _HFN(cb)
+            check(lib().llg_tsolver_set_hamiltonian_fn(self._h, ctypes.cast(fn, ctypes.c_void_p), None))
+            self._fn = fn  # the callback lives as long as the solver uses it
+        else:
+            m = _cmat(h, self.dim)
+            check(lib().llg_tsolver_set_hamiltonian(self._h, _ptr(m)))
+            self._fn = None
+
+    def add_lindblad(self, l, gamma: float) -> None:
+        m = _cmat(l, self.dim)
+        check(lib().llg_tsolver_add_lindblad(self._h, _ptr(m), float(gamma)))
+
+    def clear_lindblad(self) -> None:
+        check(lib().llg_tsolver_clear_lindblad(self._h))
+
+    def n_channels(self) -> int:
+        v = ctypes.c_int()
+        check(lib().llg_tsolver_info(self._h, ctypes.byref(v), None))
+        return v.value
+
+    def projector_applies(self, i: int) -> bool:
+        v = ctypes.c_int()
+        check(lib().llg_tsolver_projector_applies(self._h, i, ctypes.byref(v)))
+        return bool(v.value)
+
+    def _run(self, psi0, duration, dt, n, kind, seed, states=False, rho=False, obs=None):
+        p0 = np.ascontiguousarray(np.asarray(psi0, dtype=np.complex128).reshape(-1))
+        if p0.size != self.dim:
+            raise ValueError("psi0 must have length 2^n_qubits")
+        st = np.zeros((n, self.dim), dtype=np.complex128) if states else None
+        r = np.zeros((self.dim, self.dim), dtype=np.complex128) if rho else None
+        o = _cmat(obs, self.dim) if obs is not None else None
+        ov = np.zeros(n) if obs is not None else None
+        check(lib().llg_tsolver_run(self._h, _ptr(p0), float(duration), float(dt), int(n), UNRAVEL[kind], int(seed),
+                                    _ptr(st) if states else None, _ptr(r) if rho else None,
+                                    _ptr(o) if o is not None else None, _ptr(ov) if ov is not None else None))
+        return st, r, ov
+
+    def run_one(self, psi0, duration: float, dt: float, seed: int, kind: str = "STANDARD") -> np.ndarray:
+        st, _, _ = self._run(psi0, duration, dt, 1, kind, seed, states=True)
+        return st[0]
+
+    def evolve_ensemble(self, psi0, duration: float, dt: float, n_trajectories: int, kind: str = "STANDARD",
+                        seed: int = 0) -> np.ndarray:
+        _, r, _ = self._run(psi0, duration, dt, n_trajectories, kind, seed, rho=True)
+        return r
+
+    def states(self, psi0, duration: float, dt: float, n_trajectories: int, kind: str = "STANDARD",
+               seed: int = 0) -> np.ndarray:
+        st, _, _ = self._run(psi0, duration, dt, n_trajectories, kind, seed, states=True)
+        return st
+
+    def estimate_observable(self, psi0, duration: float, dt: float, n_trajectories: int, kind: str, obs,
+                            seed: int = 0) -> dict:
+        """Mean and standard error of obs(psi_T); obs is a Hermitian matrix (evaluated on the GPU)
+        or a function of the state vector (evaluated on the host over the returned states)."""
+        if callable(obs):
+            st, _, _ = self._run(psi0, duration, dt, n_trajectories, kind, seed, states=True)
+            v = np.array([float(obs(x)) for x in st])
+        else:
+            _, _, v = self._run(psi0, duration, dt, n_trajectories, kind, seed, obs=obs)
+        n = v.size
+        mean = float(v.sum() / n)
+        se = float(np.sqrt(np.sum((v - mean) ** 2) / (n - 1) / n)) if n > 1 else 0.0
+        return {"mean": mean, "std_error": se, "n": n}
+
+    def plan(self) -> dict:
+        steps, h, const, kind = ctypes.c_longlong(), ctypes.c_double(), ctypes.c_int(), ctypes.c_int()
+        nops, nnodes = ctypes.c_int(), ctypes.c_int64()
+        check(lib().llg_tsolver_plan_export(self._h, ctypes.byref(steps), ctypes.byref(h), ctypes.byref(const),
+                                            ctypes.byref(kind), None, None, 0, None, None, ctypes.byref(nops),
+                                            ctypes.byref(nnodes)))
+        d = self.dim
+        prop = np.zeros((d, d), dtype=np.complex128)
+        nodes = np.zeros((max(nnodes.value, 1), d, d), dtype=np.complex128)
+        ops = np.zeros((max(nops.value, 1), d, d), dtype=np.complex128)
+        dop = np.zeros_like(ops)
+        check(lib().llg_tsolver_plan_export(self._h, None, None, None, None, _ptr(prop), _ptr(nodes), nodes.shape[0],
+                                            _ptr(ops), _ptr(dop), ctypes.byref(nops), ctypes.byref(nnodes)))
+        return {"steps": steps.value, "h": h.value, "constant": bool(const.value), "kind": kind.value, "prop": prop,
+                "nodes": nodes[:nnodes.value], "ops": ops[:nops.value], "ops_dop": dop[:nops.value]}
+
+    def close(self) -> None:
+        if self._h:
+            lib().llg_tsolver_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------------------------------------

@@ -45,7 +45,7 @@ def oracle_lib_path() -> str:
 
 def build_oracle(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    srcs = [os.path.join(HERE, f) for f in ("sv_oracle.c", "traj_oracle.c", "adjoint_oracle.c", "noise_oracle.c", "dm_oracle.c")]
+    srcs = [os.path.join(HERE, f) for f in ("sv_oracle.c", "traj_oracle.c", "adjoint_oracle.c", "noise_oracle.c", "dm_oracle.c", "tsolver_oracle.c")]
     out = oracle_lib_path()
     if force or _stale(out, srcs + [os.path.join(HERE, "sv_oracle.h")]):
         tmp = out + ".tmp"

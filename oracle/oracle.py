@@ -51,6 +51,9 @@ def lib() -> ctypes.CDLL:
             "orc_kraus_trace_preserving": (i, [i, vp, i, d]),
             "orc_kraus_apply": (i, [vp, i, i, vp, i, vp]),
             "orc_dm_apply_op": (i, [vp, i, vp]),
+            "orc_expm": (i, [vp, i, vp]),
+            "orc_tsolver_run": (i, [i, i, ctypes.c_longlong, d, i, vp, vp, i, vp, vp, vp, u64, u64, u64, vp]),
+            "orc_lindblad_exact": (i, [i, vp, i, vp, vp, vp, d, i, vp]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
@@ -265,3 +268,84 @@ def dm_apply_ops(rho: np.ndarray, n: int, ops: np.ndarray) -> np.ndarray:
         if lib().orc_dm_apply_op(_p(buf), n, _p(one)):
             raise ValueError("oracle dm_apply_op rejected an op")
     return np.ascontiguousarray(buf.T)
+
+
+def expm(a: np.ndarray) -> np.ndarray:
+    """exp(A): the reference's scaling and squaring with an 18-term Taylor series."""
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.complex128))
+    out = np.zeros_like(a)
+    if lib().orc_expm(_p(a), a.shape[0], _p(out)):
+        raise MemoryError("oracle expm")
+    return out
+
+
+def pauli_like(l: np.ndarray):
+    """(True, P, c) when L is Hermitian with L^2 = c 1, c > 1e-12 (src/TrajectorySolver.h:363-373)."""
+    if np.linalg.norm(l - l.conj().T) > 1e-9 * max(1.0, np.linalg.norm(l)):
+        return False, None, 0.0
+    l2 = l @ l
+    c = l2[0, 0].real
+    if not c > 1e-12 or np.linalg.norm(l2 - c * np.eye(l.shape[0])) > 1e-9 * max(1.0, np.linalg.norm(l2)):
+        return False, None, 0.0
+    return True, l / np.sqrt(c), c
+
+
+def tsolver_plan(h, channels, kind: int, duration: float, dt: float, h_fn=None) -> dict:
+    """The reference's make_plan (src/TrajectorySolver.h:400-441): channels [(L, gamma), ...],
+    kind 0 STANDARD, 1 PROJECTOR, 2 ANALOG."""
+    d = (h_fn(0.0) if h_fn is not None else h).shape[0]
+    if not channels:
+        kind = 0
+    steps = max(1, int(np.ceil(duration / dt - 1e-9)))
+    hh = duration / steps
+    ops = []
+    for l, gamma in channels:
+        pl, pm, c = pauli_like(np.asarray(l, dtype=complex))
+        if kind == 1 and pl:
+            ops.append(np.sqrt(gamma * c) * (np.eye(d) - pm))
+        else:
+            ops.append(np.sqrt(gamma) * np.asarray(l, dtype=complex))
+    dop = [j.conj().T @ j for j in ops]
+    hnh = np.zeros((d, d), dtype=complex)
+    if kind != 2:
+        for m in dop:
+            hnh -= 0.5j * m
+    plan = {"steps": steps, "h": hh, "kind": kind, "ops": ops, "ops_dop": dop, "constant": h_fn is None}
+    if h_fn is None:
+        plan["prop"] = expm(-1j * (h + hnh) * hh)
+        plan["nodes"] = []
+    else:
+        n_nodes = 2 * steps + 1 if kind != 2 else steps
+        plan["prop"] = None
+        plan["nodes"] = [-1j * (h_fn(0.5 * hh * j if kind != 2 else hh * j) + hnh) for j in range(n_nodes)]
+    return plan
+
+
+def tsolver_run(plan: dict, psi0, seed: int, begin: int, end: int) -> np.ndarray:
+    """Trajectory states [end - begin, dim] for a plan (tsolver_plan's or the engine's export)."""
+    d = np.asarray(psi0).size
+    p0 = np.ascontiguousarray(np.asarray(psi0, dtype=np.complex128) / np.linalg.norm(psi0))
+    ops = np.ascontiguousarray(np.array(plan["ops"], dtype=np.complex128).reshape(-1, d, d)) if len(plan["ops"]) else \
+        np.zeros((1, d, d), dtype=np.complex128)
+    dop = np.ascontiguousarray(np.array(plan["ops_dop"], dtype=np.complex128).reshape(-1, d, d)) if len(plan["ops"]) else ops
+    prop = np.ascontiguousarray(plan["prop"] if plan["prop"] is not None else np.eye(d), dtype=np.complex128)
+    nodes = np.ascontiguousarray(np.array(plan["nodes"], dtype=np.complex128)) if len(plan["nodes"]) else prop
+    out = np.zeros((end - begin, d), dtype=np.complex128)
+    rc = lib().orc_tsolver_run(d, int(plan["kind"]), int(plan["steps"]), float(plan["h"]), int(bool(plan["constant"])),
+                               _p(prop), _p(nodes), len(plan["ops"]), _p(ops), _p(dop), _p(p0), seed, begin, end,
+                               _p(out))
+    if rc:
+        raise RuntimeError(f"oracle trajectory solver failed (rc={rc})")
+    return out
+
+
+def lindblad_exact(h, channels, rho0, duration: float, steps: int) -> np.ndarray:
+    """RK4 on the Lindblad equation for constant H (the reference's own check)."""
+    d = h.shape[0]
+    hh = np.ascontiguousarray(h, dtype=np.complex128)
+    ls = np.ascontiguousarray(np.array([c[0] for c in channels], dtype=np.complex128).reshape(-1, d, d))
+    gs = np.ascontiguousarray([c[1] for c in channels], dtype=np.float64)
+    r0 = np.ascontiguousarray(rho0, dtype=np.complex128)
+    out = np.zeros_like(r0)
+    lib().orc_lindblad_exact(d, _p(hh), len(channels), _p(ls), _p(gs), _p(r0), duration, steps, _p(out))
+    return out

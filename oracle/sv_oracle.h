@@ -74,6 +74,14 @@ int orc_kraus_trace_preserving(int nk, const double* ops, int m, double tol);
 int orc_kraus_apply(double* rho, int n, int nk, const double* ops, int m, const int* targets);
 int orc_dm_apply_op(double* rho, int n, const orc_op* op);
 
+/* tsolver_oracle.c: TrajectorySolver restatement */
+int orc_expm(const double* a, int d, double* out);
+int orc_tsolver_run(int d, int kind, long long steps, double h, int constant, const double* prop, const double* nodes,
+                    int nch, const double* ops, const double* ops_dop, const double* psi0, uint64_t seed,
+                    uint64_t traj_begin, uint64_t traj_end, double* states_out);
+int orc_lindblad_exact(int d, const double* h, int nch, const double* ls, const double* gs, const double* rho0,
+                       double duration, int steps, double* rho_out);
+
 /* noise_oracle.c: NoisyBackend + ZNE restatement */
 #define ORC_RNG_PHILOX 0
 #define ORC_RNG_MT 1
