@@ -279,12 +279,13 @@ def run_ours(args, rank, world, local):
     adj = None
     if not args.no_adjoint:
         adj = run_adjoint_bench(args, torch)
-    traj = batch = zne = config1 = None
+    traj = batch = zne = config1 = tsolver = None
     if not args.no_forms:
         traj = run_traj_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
         batch = run_batch_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
         zne = run_zne_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
         config1 = run_config1_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
+        tsolver = run_tsolver_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -328,6 +329,7 @@ def run_ours(args, rank, world, local):
         "mixed_batch": batch,
         "zne": zne,
         "config1_12q": config1,
+        "trajectory_solver": tsolver,
     }
     print(json.dumps(line), flush=True)
 
@@ -594,6 +596,63 @@ def run_config1_bench(args, torch, cpu: bool):
                 oracle.run_ops(n, ops)
                 best = min(best, time.perf_counter() - t0)
             res[f"cpu_ms_{threads}t"] = best * 1e3
+    return res
+
+
+def run_tsolver_bench(args, torch, cpu: bool):
+    """The dense trajectory solver: (a) the reference's published case, 1 qubit, T1 = 2 amplitude
+    damping from |1>, STANDARD, duration 2, dt 0.02, 20000 trajectories (published: 0.00635 ms per
+    trajectory on 2 cores); (b) 10 qubits (dim 1024), random Hermitian H, sigma_- on qubit 0 and Z
+    on qubit 1, PROJECTOR, 20 steps, 1024 trajectories: one dense complex matrix-vector product per
+    step and trajectory, 8 dim^2 real FLOP, FP64."""
+    import llgpu
+
+    sm = np.array([[0, 1], [0, 0]], dtype=complex)
+    res = {}
+    s = llgpu.TrajectorySolver(1)
+    s.add_lindblad(sm, 0.5)
+    p1 = np.diag([0.0, 1.0])
+    s.estimate_observable([0, 1], 2.0, 0.02, 2000, "STANDARD", p1, seed=1)  # warm-up
+    t0 = time.perf_counter()
+    e = s.estimate_observable([0, 1], 2.0, 0.02, 20000, "STANDARD", p1, seed=101)
+    dt1 = time.perf_counter() - t0
+    s.close()
+    res["one_qubit_t1"] = {"ms_per_trajectory": dt1 / 20000 * 1e3, "trajectories_per_s": 20000 / dt1,
+                           "mean_p1": e["mean"], "exact": float(np.exp(-1.0)), "std_error": e["std_error"],
+                           "published_reference_ms_per_trajectory": 0.00635,
+                           "published_note": "2 cores, docs/trajectory_benchmark.json:221"}
+    rng = np.random.default_rng(11)
+    d, steps, ntraj = 1024, 20, 1024
+    a = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    h = (a + a.conj().T) / (4 * np.sqrt(d))
+    s = llgpu.TrajectorySolver(10)
+    s.set_hamiltonian(h)
+    s.add_lindblad(np.kron(np.eye(d // 2), sm), 0.4)
+    s.add_lindblad(np.diag(np.where(np.arange(d) & 2, -1.0, 1.0)).astype(complex), 0.3)
+    psi0 = rng.normal(size=d) + 1j * rng.normal(size=d)
+    s.states(psi0, 0.02 * steps, 0.02, 64, "PROJECTOR", seed=4)  # warm-up (plan + kernel)
+    t0 = time.perf_counter()
+    st = s.states(psi0, 0.02 * steps, 0.02, ntraj, "PROJECTOR", seed=5)
+    dt10 = time.perf_counter() - t0
+    plan = s.plan()
+    flop = 8.0 * d * d * steps * ntraj
+    res["ten_qubit_dense"] = {"trajectories_per_s": ntraj / dt10, "seconds": dt10, "steps": steps,
+                              "tflops_fp64_incl_plan": flop / dt10 / 1e12,
+                              "note": "seconds include the plan (expm of the 1024 x 1024 H_eff on the GPU) "
+                                      "and the host copy of all final states"}
+    if cpu:
+        import oracle
+
+        oracle.set_threads(os.cpu_count() or 1)
+        sample = 32
+        t0 = time.perf_counter()
+        oracle.tsolver_run(plan, psi0, 5, 0, sample)
+        dtc = time.perf_counter() - t0
+        res["ten_qubit_dense"]["cpu_baseline"] = {"value": sample / dtc, "unit": "traj/s", "cores": os.cpu_count(),
+                                                  "kind": "port", "sample": f"{sample} trajectories, oracle "
+                                                  "restatement of the solver's jump step with the GPU's plan"}
+    del st
+    s.close()
     return res
 
 
