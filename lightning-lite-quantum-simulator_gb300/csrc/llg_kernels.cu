@@ -118,6 +118,8 @@ __global__ void __launch_bounds__(kThreads) k_mcz(typename P::S* __restrict__ ps
 // ------------------------------------------------------------------------------------------
 // tile pass
 // ------------------------------------------------------------------------------------------
+constexpr int kOpChunk = 32;  // op records staged per shared-memory chunk in k_tile
+
 template <class P>
 __global__ void __launch_bounds__(512) k_tile(typename P::S* __restrict__ psi, PassDesc pd, const ExecOp* __restrict__ ops) {
     using S = typename P::S;
@@ -142,8 +144,19 @@ __global__ void __launch_bounds__(512) k_tile(typename P::S* __restrict__ psi, P
         tile[l] = psi[base | hi_off[l >> low] | (l & lowmask)];
     __syncthreads();
 
+    // op records are staged through shared memory in chunks (one coalesced copy per chunk
+    // instead of a dependent global load before every op's barrier)
+    __shared__ __align__(16) ExecOp sops[kOpChunk];
+    static_assert(sizeof(ExecOp) % 16 == 0, "ExecOp copies as 16-byte words");
+    constexpr int kWords = (int)(sizeof(ExecOp) / 16);
     for (int k = 0; k < pd.nops; ++k) {
-        const ExecOp& o = ops[pd.op_begin + k];
+        if (k % kOpChunk == 0) {
+            const int cnt = min(kOpChunk, pd.nops - k);
+            const uint4* src = reinterpret_cast<const uint4*>(ops + pd.op_begin + k);
+            for (int w = threadIdx.x; w < cnt * kWords; w += blockDim.x) reinterpret_cast<uint4*>(sops)[w] = src[w];
+            __syncthreads();
+        }
+        const ExecOp& o = sops[k % kOpChunk];
         const int kind = o.kind;
         switch (kind) {
             case EX_U2: tile_pairs<P, EX_U2>(tile, tsize >> 1, o.q0, o); break;
