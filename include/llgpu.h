@@ -373,8 +373,10 @@ typedef struct llg_batch llg_batch;
 int llg_batch_create(int count, const int* n_qubits, const llg_op* ops, const int64_t* op_offsets, int precision,
                      int tile_qubits, llg_batch** out);
 int llg_batch_destroy(llg_batch* b);
-/* Builds and times the batch once per tile width from 8 qubits to the maximum (one untimed run
- * each) and returns the fastest in out->tile_qubits (cached by the batch's shape). */
+/* Builds and times the batch once per (tile width from 8 qubits to the maximum) x (256 or 512
+ * threads per CTA), one untimed run each, and returns the fastest in out->tile_qubits and
+ * out->cta_threads (cached by the batch's shape).  Batches created with an explicit tile width
+ * use 256 threads. */
 int llg_batch_autotune(int count, const int* n_qubits, const llg_op* ops, const int64_t* op_offsets, int precision,
                        llg_tune_result* out);
 int llg_batch_config(const llg_batch* b, int* tile_qubits, int* grid, int* cta_threads);

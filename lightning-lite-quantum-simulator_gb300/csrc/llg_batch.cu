@@ -33,7 +33,8 @@ using namespace llg;
 
 namespace {
 
-constexpr int kBatchThreads = 512;
+constexpr int kBatchThreads = 512;  // largest CTA; the default and the tuner's other choice is 256
+constexpr int kBatchOpChunk = 32;   // op records staged per shared-memory chunk
 constexpr long long kDefaultSpinLimit = 1LL << 24;  // ~1 s of 64 ns polls
 
 struct CircDesc {
@@ -99,8 +100,17 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(typename P::S* __restri
             const uint32_t lowmask = (1u << low) - 1;
             for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) tile[l] = __ldcg(&psi[base | hi_off[l >> low] | (l & lowmask)]);
             __syncthreads();
+            // op records staged through shared memory in chunks (as in the single-state tile pass)
+            __shared__ __align__(16) ExecOp sops[kBatchOpChunk];
+            constexpr int kWords = (int)(sizeof(ExecOp) / 16);
             for (int k = 0; k < pd.nops; ++k) {
-                tile_apply<P>(tile, tsize, base, ops[pd.op_begin + k], nullptr);
+                if (k % kBatchOpChunk == 0) {
+                    const int cnt = min(kBatchOpChunk, pd.nops - k);
+                    const uint4* src = reinterpret_cast<const uint4*>(ops + pd.op_begin + k);
+                    for (int q = threadIdx.x; q < cnt * kWords; q += blockDim.x) reinterpret_cast<uint4*>(sops)[q] = src[q];
+                    __syncthreads();
+                }
+                tile_apply<P>(tile, tsize, base, sops[k % kBatchOpChunk], nullptr);
                 __syncthreads();
             }
             for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) psi[base | hi_off[l >> low] | (l & lowmask)] = tile[l];
@@ -197,6 +207,7 @@ struct llg_batch {
     unsigned* d_completed = nullptr;
     int* d_err = nullptr;
     int grid = 0;
+    int threads = 256;
     size_t smem = 0;
     // the run captured as a CUDA graph (state reset + persistent kernel), re-captured when the
     // spin limit changes
@@ -217,7 +228,7 @@ int setup_batch(llg_batch* b) {
     int per_sm = 1, dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<P>, kBatchThreads, b->smem)))
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<P>, b->threads, b->smem)))
         return cuda_fail(e, "batch occupancy");
     b->grid = std::max(1, sms * std::max(per_sm, 1));
     return LLG_OK;
@@ -234,7 +245,7 @@ cudaError_t enqueue_batch(llg_batch* b, long long spin_limit) {
     if ((e = cudaMemsetAsync(b->d_next, 0, sizeof(unsigned long long), s))) return e;
     if ((e = cudaMemsetAsync(b->d_completed, 0, b->count * sizeof(unsigned), s))) return e;
     if ((e = cudaMemsetAsync(b->d_err, 0, sizeof(int), s))) return e;
-    k_batch<P><<<b->grid, kBatchThreads, b->smem, s>>>(static_cast<typename P::S*>(b->d_arena), b->d_circs, b->d_passes,
+    k_batch<P><<<b->grid, b->threads, b->smem, s>>>(static_cast<typename P::S*>(b->d_arena), b->d_circs, b->d_passes,
                                                        b->d_ops, b->d_items, (long long)b->items.size(), b->d_next,
                                                        b->d_completed, b->d_err, spin_limit);
     return cudaGetLastError();
@@ -277,8 +288,9 @@ int launch_batch(llg_batch* b, long long spin_limit) {
 extern "C" {
 
 static int batch_build(int count, const int* n_qubits, const llg_op* ops, const int64_t* op_offsets, int precision,
-                       int tile, llg_batch** out) {
+                       int tile, int threads, llg_batch** out) {
     llg_batch* b = new llg_batch();
+    b->threads = threads;
     b->P = precision;
     b->count = count;
     b->tile = tile;
@@ -376,12 +388,12 @@ int llg_batch_create(int count, const int* n_qubits, const llg_op* ops, const in
     if (tile_qubits != LLG_TUNE_AUTO) {
         const int tile = tile_qubits > 0 ? std::min(tile_qubits, tmax) : (precision == LLG_F32 ? 13 : 12);
         if (tile < 2) return set_error(LLG_EINVAL, "batch_create: tile_qubits too small");
-        return batch_build(count, n_qubits, ops, op_offsets, precision, tile, out);
+        return batch_build(count, n_qubits, ops, op_offsets, precision, tile, 256, out);
     }
     llg_tune_result res;
     int rc = llg_batch_autotune(count, n_qubits, ops, op_offsets, precision, &res);
     if (rc) return rc;
-    return batch_build(count, n_qubits, ops, op_offsets, precision, res.tile_qubits, out);
+    return batch_build(count, n_qubits, ops, op_offsets, precision, res.tile_qubits, res.cta_threads, out);
 }
 
 int llg_batch_autotune(int count, const int* n_qubits, const llg_op* ops, const int64_t* op_offsets, int precision,
@@ -405,7 +417,7 @@ int llg_batch_autotune(int count, const int* n_qubits, const llg_op* ops, const 
     }
     res.fuse_mode = LLG_FUSE_TILE;
     res.cluster = 1;
-    res.cta_threads = kBatchThreads;
+    res.cta_threads = 256;
     const int tdef = precision == LLG_F32 ? 13 : 12;
     const int tmax = std::min(tile_max_qubits(precision), std::max(nmax, 8));
     double best = 1e300;
@@ -414,33 +426,36 @@ int llg_batch_autotune(int count, const int* n_qubits, const llg_op* ops, const 
     if (e == cudaSuccess) e = cudaEventCreate(&eb);
     if (e != cudaSuccess) return cuda_fail(e, "batch autotune events");
     int rc = LLG_OK;
-    for (int t = std::min(8, tmax); t <= tmax && !rc; ++t) {
-        llg_batch* b = nullptr;
-        rc = batch_build(count, n_qubits, ops, op_offsets, precision, t, &b);
-        if (rc) break;
-        rc = llg_batch_run(b, 0);  // untimed (captures the graph)
-        if (!rc) {
-            e = cudaEventRecord(ea, b->stream);
-            if (e == cudaSuccess) {
-                rc = llg_batch_run(b, 0);
-                if (!rc) e = cudaEventRecord(eb, b->stream);
-            }
-            if (!rc && e == cudaSuccess) e = cudaEventSynchronize(eb);
-            float ms = 0.f;
-            if (!rc && e == cudaSuccess) e = cudaEventElapsedTime(&ms, ea, eb);
-            if (!rc && e != cudaSuccess) rc = cuda_fail(e, "batch autotune timing");
+    for (int t = std::min(8, tmax); t <= tmax && !rc; ++t)
+        for (int th : {256, 512}) {
+            if (rc) break;
+            llg_batch* b = nullptr;
+            rc = batch_build(count, n_qubits, ops, op_offsets, precision, t, th, &b);
+            if (rc) break;
+            rc = llg_batch_run(b, 0);  // untimed (captures the graph)
             if (!rc) {
-                ++res.candidates;
-                if (t == tdef) res.default_ms = ms;
-                if (ms < best) {
-                    best = ms;
-                    res.best_ms = ms;
-                    res.tile_qubits = t;
+                e = cudaEventRecord(ea, b->stream);
+                if (e == cudaSuccess) {
+                    rc = llg_batch_run(b, 0);
+                    if (!rc) e = cudaEventRecord(eb, b->stream);
+                }
+                if (!rc && e == cudaSuccess) e = cudaEventSynchronize(eb);
+                float ms = 0.f;
+                if (!rc && e == cudaSuccess) e = cudaEventElapsedTime(&ms, ea, eb);
+                if (!rc && e != cudaSuccess) rc = cuda_fail(e, "batch autotune timing");
+                if (!rc) {
+                    ++res.candidates;
+                    if (t == tdef && th == 256) res.default_ms = ms;
+                    if (ms < best) {
+                        best = ms;
+                        res.best_ms = ms;
+                        res.tile_qubits = t;
+                        res.cta_threads = th;
+                    }
                 }
             }
+            llg_batch_destroy(b);
         }
-        llg_batch_destroy(b);
-    }
     cudaEventDestroy(ea);
     cudaEventDestroy(eb);
     if (rc) return rc;
@@ -453,7 +468,7 @@ int llg_batch_config(const llg_batch* b, int* tile_qubits, int* grid, int* cta_t
     if (!b) return set_error(LLG_EINVAL, "batch_config: NULL handle");
     if (tile_qubits) *tile_qubits = b->tile;
     if (grid) *grid = b->grid;
-    if (cta_threads) *cta_threads = kBatchThreads;
+    if (cta_threads) *cta_threads = b->threads;
     return LLG_OK;
 }
 
