@@ -339,9 +339,12 @@ def run_ours(args, rank, world, local):
 # double-float dot product (df_lin4) is 43 instructions (4 FMUL + 4 FFMA product errors, 3 TwoSum
 # of 6, 8 FFMA cross terms, 6 FADD, Fast2Sum of 3), a 2-term one (df_lin2) 19; a U2 pair needs four
 # 4-term products, RX/RY/H four 2-term ones, a diagonal two 2-term ones per amplitude, a ZYZ
-# (phase-free unitary) eight 2-term ones.  CNOT, MCZ and X move or negate data without arithmetic.
-FP32_INST_PER_PAIR = {"complex128": {0: 172, 1: 76, 2: 76, 3: 76, 4: 0, 5: 76, 6: 0, 7: 0, 11: 152},
-                      "complex64": {0: 16, 1: 8, 2: 8, 3: 8, 4: 0, 5: 8, 6: 0, 7: 0, 11: 16}}
+# (phase-free unitary) eight 2-term ones, a ZY (RY after an input phase) six, a carried-phase flush
+# (13) two per amplitude pair; a CNOT carrying a pushed phase multiplies a quarter of the amplitudes.
+# CNOT, MCZ and X otherwise move or negate data without arithmetic.
+FP32_INST_PER_PAIR = {"complex128": {0: 172, 1: 76, 2: 76, 3: 76, 4: 0, 5: 76, 6: 0, 7: 0, 11: 152, 12: 114, 13: 38},
+                      "complex64": {0: 16, 1: 8, 2: 8, 3: 8, 4: 0, 5: 8, 6: 0, 7: 0, 11: 16, 12: 12, 13: 4}}
+PHASED_CNOT_PER_PAIR = {"complex128": 19, "complex64": 2}  # a complex multiply on a quarter of the amplitudes
 SMS, FP32_LANES_PER_SM = 152, 128
 
 
@@ -352,6 +355,7 @@ def compute_roofline(precision, n, xops, tile_ms_step, sm_mhz):
     if table is None or not tile_ms_step or not len(xops):
         return None
     per_pair = sum(table.get(int(k), 0) for k in xops["kind"])
+    per_pair += PHASED_CNOT_PER_PAIR.get(precision, 0) * int(np.sum((xops["kind"] == 6) & ((xops["flags"] & 8) != 0)))
     inst = per_pair * float(1 << (n - 1))
     achieved = inst / (tile_ms_step / 1e3) / 1e12
     mhz = sm_mhz or 2070.0

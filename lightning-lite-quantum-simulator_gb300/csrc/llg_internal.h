@@ -30,6 +30,12 @@ enum ExecKind : int32_t {
     // instructions per double-float pair against 172 for EX_U2; the plan carries the dropped
     // phases in one EX_U2 of the same flush.
     EX_ZYZ = 11,
+    // EX_ZYZ without its output phase: RY(b) diag(1, e^{ig}) on q0, c[0..1] = cos g, sin g,
+    // c[2..3] = cos b/2, sin b/2 (114 FP32 instructions per double-float pair); the planner carries
+    // the dropped output phase forward to the next op on the qubit
+    EX_ZY = 12,
+    // diag(1, c[0] + i c[1]) on q0 (q0 may be non-local): the planner's flush of a carried phase
+    EX_PHASE1 = 13,
 };
 
 // Flags of a tile op.
@@ -37,6 +43,8 @@ enum : int32_t {
     OPF_NONLOCAL_Q0 = 1,  // q0 is a global qubit outside the tile (diagonal / control use only)
     OPF_ADJOINT = 2,      // parametrised op applied as its inverse (angle negated)
     OPF_GRAD = 4,         // backward pass: accumulate Im<lambda|P|psi> before applying the op
+    OPF_PHASE = 8,        // EX_CNOT: multiply the amplitudes with control = target = 1 after the swap
+                          // by c[0] + i c[1] (a carried target phase pushed through the CNOT)
 };
 
 // One executor op.  In a tile pass q0/q1/mask are LOCAL (tile) indices unless flagged; `nl_mask`

@@ -161,6 +161,8 @@ __global__ void __launch_bounds__(512) k_tile(typename P::S* __restrict__ psi, P
         switch (kind) {
             case EX_U2: tile_pairs<P, EX_U2>(tile, tsize >> 1, o.q0, o); break;
             case EX_ZYZ: tile_pairs<P, EX_ZYZ>(tile, tsize >> 1, o.q0, o); break;
+            case EX_ZY: tile_pairs<P, EX_ZY>(tile, tsize >> 1, o.q0, o); break;
+            case EX_PHASE1: tile_phase1<P>(tile, tsize, base, o); break;
             case EX_RX: tile_pairs<P, EX_RX>(tile, tsize >> 1, o.q0, o); break;
             case EX_RY: tile_pairs<P, EX_RY>(tile, tsize >> 1, o.q0, o); break;
             case EX_H: tile_pairs<P, EX_H>(tile, tsize >> 1, o.q0, o); break;
@@ -189,23 +191,7 @@ __global__ void __launch_bounds__(512) k_tile(typename P::S* __restrict__ psi, P
                 }
                 break;
             }
-            case EX_CNOT: {
-                const int tq = o.q1;
-                if (o.flags & OPF_NONLOCAL_Q0) {
-                    if ((base >> o.q0) & 1) tile_pairs<P, EX_X>(tile, tsize >> 1, tq, o);
-                } else {
-                    const int c = o.q0;
-                    const int lo = c < tq ? c : tq, hi = c < tq ? tq : c;
-                    const uint32_t cbit = 1u << c, tbit = 1u << tq;
-                    for (uint32_t r = threadIdx.x; r < (tsize >> 2); r += blockDim.x) {
-                        const uint32_t j = (uint32_t)insert0(insert0(r, lo), hi) | cbit;
-                        const S x = tile[j];
-                        tile[j] = tile[j | tbit];
-                        tile[j | tbit] = x;
-                    }
-                }
-                break;
-            }
+            case EX_CNOT: tile_cnot<P>(tile, tsize, base, o); break;
             case EX_MCZ: {
                 if ((base & o.nl_mask) == o.nl_mask) {
                     const uint32_t lm = (uint32_t)o.mask;

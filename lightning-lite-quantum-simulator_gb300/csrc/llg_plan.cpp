@@ -225,6 +225,14 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
     int carrier = -1;
     double carrier_m[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     std::complex<double> phase(1.0, 0.0);
+    // carried phases: ph[q] is a pending diag(1, ph[q]) on global qubit q that has not been applied
+    // yet.  A rotation's output phase is carried instead of applied; it commutes with diagonal
+    // gates and CNOT controls, merges into the next rotation on the qubit, and is pushed through a
+    // CNOT target as phases on both qubits plus a controlled phase folded into the CNOT:
+    //   CNOT diag_t(1, p) = diag_t(1, p) diag_c(1, p) CP(c, t; p^-2) CNOT.
+    using cd = std::complex<double>;
+    std::vector<cd> ph(n, cd(1.0, 0.0));
+    auto is_one = [](const cd& v) { return v.real() == 1.0 && v.imag() == 0.0; };
     const int t = std::min(n, tile_qubits);
     // the low qubits are always local; when the register is wider than the tile at least one slot
     // stays free, so the first remaining op (which needs at most one qubit local) always fits
@@ -300,57 +308,130 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
 
         // Peephole fusion of same-qubit 1-qubit runs, then lowering to local indices.
         std::vector<Pending> pend(n);
+        // local indices for one executor op (global qubits in), then append it
+        auto emit_raw = [&](ExecOp e, int src) {
+            switch (e.kind) {
+                case EX_U2:
+                case EX_ZYZ:
+                case EX_ZY:
+                case EX_RX:
+                case EX_RY:
+                case EX_H:
+                case EX_X: e.q0 = to_local[e.q0]; break;
+                case EX_DIAG:
+                case EX_PHASE1:
+                    if (to_local[e.q0] >= 0) e.q0 = to_local[e.q0];
+                    else e.flags |= OPF_NONLOCAL_Q0;
+                    break;
+                case EX_CNOT:
+                    e.q1 = to_local[e.q1];
+                    if (to_local[e.q0] >= 0) e.q0 = to_local[e.q0];
+                    else e.flags |= OPF_NONLOCAL_Q0;
+                    break;
+                case EX_MCZ: {
+                    uint64_t lm = 0, nl = 0;
+                    for (int q = 0; q < 64; ++q)
+                        if (e.mask >> q & 1) {
+                            if (to_local[q] >= 0) lm |= 1ULL << to_local[q];
+                            else nl |= 1ULL << q;
+                        }
+                    e.mask = lm;
+                    e.nl_mask = nl;
+                    break;
+                }
+                default: break;
+            }
+            out.ops.push_back(e);
+            out.source_index.push_back(src);
+        };
+        // a generic 2x2 on q after folding in the carried phase: the phase carrier (first one),
+        // else RY diag(1, g) with the output phase carried, else (not unitary) a generic 2x2
+        auto emit_u2 = [&](const double* m_in, int q, int src) {
+            double m[8];
+            std::memcpy(m, m_in, sizeof(m));
+            const cd p = ph[q];
+            if (!is_one(p)) {  // U diag(1, p): column 1 times p
+                const cd m01 = cd(m[2], m[3]) * p, m11 = cd(m[6], m[7]) * p;
+                m[2] = m01.real();
+                m[3] = m01.imag();
+                m[6] = m11.real();
+                m[7] = m11.imag();
+                ph[q] = 1.0;
+            }
+            ExecOp e = blank(EX_U2);
+            e.q0 = q;
+            cd z, ea, eg;
+            double c = 0.0, sn = 0.0;
+            if (carrier < 0) {
+                carrier = (int)out.ops.size();
+                std::memcpy(carrier_m, m, sizeof(carrier_m));
+            } else if (split_zyz(m, z, c, sn, ea, eg)) {
+                e = blank(EX_ZY);
+                e.q0 = q;
+                const double v[4] = {eg.real(), eg.imag(), c, sn};
+                for (int k = 0; k < 4; ++k) e.c[k] = pack_coef(P, v[k]);
+                ph[q] = ea;
+                phase *= z;
+                emit_raw(e, src);
+                return;
+            }
+            for (int k = 0; k < 8; ++k) e.c[k] = pack_coef(P, m[k]);
+            emit_raw(e, src);
+        };
         auto emit_lowered = [&](const llg_op& gop, int src) -> bool {
+            if (!use_zyz) {
+                std::vector<ExecOp> tmp;
+                if (!lower_op(n, gop, P, tmp, err)) return false;
+                for (ExecOp& e : tmp) emit_raw(e, src);
+                return true;
+            }
+            const int q = gop.q0;
+            switch (gop.kind) {
+                case LLG_OP_RZ: {  // diag(e^-it/2, e^it/2) = e^-it/2 diag(1, e^it): global phase + carried phase
+                    const cd d0(std::cos(0.5 * gop.theta), -std::sin(0.5 * gop.theta));
+                    const cd d1(std::cos(0.5 * gop.theta), std::sin(0.5 * gop.theta));
+                    phase *= d0;
+                    ph[q] *= d1 / d0;
+                    return true;
+                }
+                case LLG_OP_X: {  // X diag(1, p) = p diag(1, 1/p) X
+                    const cd p = ph[q];
+                    if (!is_one(p)) {
+                        phase *= p;
+                        ph[q] = 1.0 / p;
+                    }
+                    break;  // the swap itself below
+                }
+                case LLG_OP_H:
+                case LLG_OP_RX:
+                case LLG_OP_RY:
+                    if (is_one(ph[q])) break;  // nothing carried: the cheaper specialised form
+                    {
+                        double m[8];
+                        op_matrix(gop, m);
+                        emit_u2(m, q, src);
+                    }
+                    return true;
+                case LLG_OP_U2: emit_u2(gop.m, q, src); return true;
+                case LLG_OP_CNOT: {
+                    std::vector<ExecOp> tmp;
+                    if (!lower_op(n, gop, P, tmp, err)) return false;
+                    const cd p = ph[gop.q1];
+                    if (!is_one(p)) {
+                        ph[gop.q0] *= p;
+                        const cd cp = 1.0 / (p * p);
+                        tmp[0].flags |= OPF_PHASE;
+                        tmp[0].c[0] = pack_coef(P, cp.real());
+                        tmp[0].c[1] = pack_coef(P, cp.imag());
+                    }
+                    emit_raw(tmp[0], src);
+                    return true;
+                }
+                default: break;  // cz, mcz: diagonal, they commute with the carried phases
+            }
             std::vector<ExecOp> tmp;
             if (!lower_op(n, gop, P, tmp, err)) return false;
-            if (use_zyz && gop.kind == LLG_OP_U2 && tmp.size() == 1) {
-                std::complex<double> z, ea, eg;
-                double c = 0.0, s = 0.0;
-                if (carrier < 0) {
-                    carrier = (int)out.ops.size();
-                    std::memcpy(carrier_m, gop.m, sizeof(carrier_m));
-                } else if (split_zyz(gop.m, z, c, s, ea, eg)) {
-                    ExecOp e = blank(EX_ZYZ);
-                    e.q0 = gop.q0;
-                    const double v[6] = {eg.real(), eg.imag(), c, s, ea.real(), ea.imag()};
-                    for (int k = 0; k < 6; ++k) e.c[k] = pack_coef(P, v[k]);
-                    tmp[0] = e;
-                    phase *= z;
-                }
-            }
-            for (ExecOp& e : tmp) {
-                switch (e.kind) {
-                    case EX_U2:
-                    case EX_ZYZ:
-                    case EX_RX:
-                    case EX_RY:
-                    case EX_H:
-                    case EX_X: e.q0 = to_local[e.q0]; break;
-                    case EX_DIAG:
-                        if (to_local[e.q0] >= 0) e.q0 = to_local[e.q0];
-                        else e.flags |= OPF_NONLOCAL_Q0;
-                        break;
-                    case EX_CNOT:
-                        e.q1 = to_local[e.q1];
-                        if (to_local[e.q0] >= 0) e.q0 = to_local[e.q0];
-                        else e.flags |= OPF_NONLOCAL_Q0;
-                        break;
-                    case EX_MCZ: {
-                        uint64_t lm = 0, nl = 0;
-                        for (int q = 0; q < 64; ++q)
-                            if (e.mask >> q & 1) {
-                                if (to_local[q] >= 0) lm |= 1ULL << to_local[q];
-                                else nl |= 1ULL << q;
-                            }
-                        e.mask = lm;
-                        e.nl_mask = nl;
-                        break;
-                    }
-                    default: break;
-                }
-                out.ops.push_back(e);
-                out.source_index.push_back(src);
-            }
+            for (ExecOp& e : tmp) emit_raw(e, src);
             return true;
         };
         auto flush_pending = [&](int q) -> bool {
@@ -364,6 +445,12 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
             u.q0 = q;
             u.param = -1;
             std::memcpy(u.m, p.m, sizeof(p.m));
+            if (p.diag && use_zyz) {  // diag(d0, d1) = d0 diag(1, d1 / d0): nothing to emit
+                const cd d0(p.m[0], p.m[1]), d1(p.m[6], p.m[7]);
+                phase *= d0;
+                ph[q] *= d1 / d0;
+                return true;
+            }
             if (p.diag) {
                 // product of diagonal gates stays diagonal: emit it as a diagonal op so it may act on
                 // a non-local qubit
@@ -431,6 +518,41 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
         }
         out.passes.push_back(pd);
         remaining.swap(deferred);
+    }
+    if (use_zyz && !out.passes.empty()) {
+        // the carried phases that reached the end, as diag(1, p) ops in the last pass; the global
+        // phase goes there too when no generic 2x2 can carry it
+        PassDesc& last = out.passes.back();
+        int to_local[64];
+        for (int q = 0; q < 64; ++q) to_local[q] = -1;
+        for (int q = 0, j = 0; q < n; ++q)
+            if (last.local_mask >> q & 1) to_local[q] = j++;
+        auto append = [&](ExecOp e) {
+            out.ops.push_back(e);
+            out.source_index.push_back(-1);
+            ++last.nops;
+        };
+        for (int q = 0; q < n; ++q) {
+            if (is_one(ph[q])) continue;
+            ExecOp e = blank(EX_PHASE1);
+            e.c[0] = pack_coef(P, ph[q].real());
+            e.c[1] = pack_coef(P, ph[q].imag());
+            if (to_local[q] >= 0) e.q0 = to_local[q];
+            else {
+                e.q0 = q;
+                e.flags |= OPF_NONLOCAL_Q0;
+            }
+            append(e);
+            ph[q] = 1.0;
+        }
+        if (carrier < 0 && !is_one(phase)) {
+            ExecOp e = blank(EX_DIAG);  // local qubit 0 of the tile, both entries the phase
+            e.q0 = 0;
+            e.c[0] = e.c[2] = pack_coef(P, phase.real());
+            e.c[1] = e.c[3] = pack_coef(P, phase.imag());
+            append(e);
+            phase = 1.0;
+        }
     }
     if (carrier >= 0 && (phase.real() != 1.0 || phase.imag() != 0.0)) {
         for (int r = 0; r < 4; ++r) {

@@ -56,6 +56,14 @@ struct PairMath {
             const auto ui = P::lin2(s, y0, c, ti);
             a1.re = P::lin2(ar, ur, P::kneg(ai), ui);  // ea * u
             a1.im = P::lin2(ar, ui, ai, ur);
+        } else if (KIND == EX_ZY) {  // [c, -s; s, c] diag(1, eg)
+            const auto gr = k[0], gi = k[1], c = k[2], s = k[3];
+            const auto tr = P::lin2(gr, x1, P::kneg(gi), y1);  // eg * a1
+            const auto ti = P::lin2(gr, y1, gi, x1);
+            a0.re = P::lin2(c, x0, P::kneg(s), tr);
+            a0.im = P::lin2(c, y0, P::kneg(s), ti);
+            a1.re = P::lin2(s, x0, c, tr);
+            a1.im = P::lin2(s, y0, c, ti);
         } else if (KIND == EX_H) {  // r [1, 1; 1, -1]
             const auto r = k[0], mr = P::kneg(k[0]);
             a0.re = P::lin2(r, x0, r, x1);
@@ -94,6 +102,72 @@ __device__ __forceinline__ void tile_pairs(typename P::S* tile, uint32_t npairs,
 }
 
 
+// diag(1, ph) on tile qubit q (or on the tile-uniform global qubit q when it is not local)
+template <class P>
+__device__ __forceinline__ void tile_phase1(typename P::S* tile, uint32_t tsize, uint64_t base, const ExecOp& o) {
+    using K = typename P::K;
+    const K pr = P::k_from_bits(o.c[0]), pi = P::k_from_bits(o.c[1]), mpi = P::kneg(pi);
+    if (o.flags & OPF_NONLOCAL_Q0) {
+        if ((base >> o.q0) & 1)
+            for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
+                auto a = P::load(tile[l]);
+                cmul_const<P>(a, pr, pi, mpi);
+                tile[l] = P::store(a);
+            }
+        return;
+    }
+    const uint32_t bit = 1u << o.q0;
+    for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += blockDim.x) {
+        const uint32_t j = (uint32_t)insert0(p, o.q0) | bit;
+        auto a = P::load(tile[j]);
+        cmul_const<P>(a, pr, pi, mpi);
+        tile[j] = P::store(a);
+    }
+}
+
+// CNOT (control q0, possibly a tile-uniform global qubit; target q1 local); with OPF_PHASE the
+// amplitudes that end with control = target = 1 are then multiplied by c[0] + i c[1]
+template <class P>
+__device__ __forceinline__ void tile_cnot(typename P::S* tile, uint32_t tsize, uint64_t base, const ExecOp& o) {
+    using K = typename P::K;
+    using S = typename P::S;
+    const int tq = o.q1;
+    const bool phased = (o.flags & OPF_PHASE) != 0;
+    const K pr = P::k_from_bits(o.c[0]), pi = P::k_from_bits(o.c[1]), mpi = P::kneg(pi);
+    if (o.flags & OPF_NONLOCAL_Q0) {
+        if (!((base >> o.q0) & 1)) return;
+        const uint32_t tbit = 1u << tq;
+        for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += blockDim.x) {
+            const uint32_t j0 = (uint32_t)insert0(p, tq), j1 = j0 | tbit;
+            const S x = tile[j0];
+            tile[j0] = tile[j1];
+            if (phased) {
+                auto a = P::load(x);
+                cmul_const<P>(a, pr, pi, mpi);
+                tile[j1] = P::store(a);
+            } else {
+                tile[j1] = x;
+            }
+        }
+        return;
+    }
+    const int c = o.q0;
+    const int lo = c < tq ? c : tq, hi = c < tq ? tq : c;
+    const uint32_t cbit = 1u << c, tbit = 1u << tq;
+    for (uint32_t r = threadIdx.x; r < (tsize >> 2); r += blockDim.x) {
+        const uint32_t j = (uint32_t)insert0(insert0(r, lo), hi) | cbit;
+        const S x = tile[j];
+        tile[j] = tile[j | tbit];
+        if (phased) {
+            auto a = P::load(x);
+            cmul_const<P>(a, pr, pi, mpi);
+            tile[j | tbit] = P::store(a);
+        } else {
+            tile[j | tbit] = x;
+        }
+    }
+}
+
 // ------------------------------------------------------------------------------------------
 // one op on a shared-memory tile (all kinds, parametrised ones read their table row)
 // ------------------------------------------------------------------------------------------
@@ -105,6 +179,8 @@ __device__ void tile_apply(typename P::S* tile, uint32_t tsize, uint64_t base, c
     switch (o.kind) {
         case EX_U2: tile_pairs<P, EX_U2>(tile, tsize >> 1, o.q0, o); break;
         case EX_ZYZ: tile_pairs<P, EX_ZYZ>(tile, tsize >> 1, o.q0, o); break;
+        case EX_ZY: tile_pairs<P, EX_ZY>(tile, tsize >> 1, o.q0, o); break;
+        case EX_PHASE1: tile_phase1<P>(tile, tsize, base, o); break;
         case EX_RX: tile_pairs<P, EX_RX>(tile, tsize >> 1, o.q0, o); break;
         case EX_RY: tile_pairs<P, EX_RY>(tile, tsize >> 1, o.q0, o); break;
         case EX_H: tile_pairs<P, EX_H>(tile, tsize >> 1, o.q0, o); break;
@@ -180,23 +256,7 @@ __device__ void tile_apply(typename P::S* tile, uint32_t tsize, uint64_t base, c
             }
             break;
         }
-        case EX_CNOT: {
-            const int tq = o.q1;
-            if (o.flags & OPF_NONLOCAL_Q0) {
-                if ((base >> o.q0) & 1) tile_pairs<P, EX_X>(tile, tsize >> 1, tq, o);
-            } else {
-                const int c = o.q0;
-                const int lo = c < tq ? c : tq, hi = c < tq ? tq : c;
-                const uint32_t cbit = 1u << c, tbit = 1u << tq;
-                for (uint32_t r = threadIdx.x; r < (tsize >> 2); r += blockDim.x) {
-                    const uint32_t j = (uint32_t)insert0(insert0(r, lo), hi) | cbit;
-                    const S x = tile[j];
-                    tile[j] = tile[j | tbit];
-                    tile[j | tbit] = x;
-                }
-            }
-            break;
-        }
+        case EX_CNOT: tile_cnot<P>(tile, tsize, base, o); break;
         case EX_MCZ: {
             if ((base & o.nl_mask) == o.nl_mask) {
                 const uint32_t lm = (uint32_t)o.mask;

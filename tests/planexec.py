@@ -15,6 +15,9 @@ def _matrix(x) -> np.ndarray:
         return np.array([[c[0], -c[1]], [c[1], c[0]]], dtype=complex)
     if k == 3:
         return np.array([[c[0], c[0]], [c[0], -c[0]]], dtype=complex)
+    if k == 12:  # [c, -s; s, c] diag(1, eg)
+        eg = c[0] + 1j * c[1]
+        return np.array([[c[2], -c[3]], [c[3], c[2]]], dtype=complex) @ np.diag([1, eg])
     if k == 11:  # diag(1, ea) [c, -s; s, c] diag(1, eg)
         eg, ea = c[0] + 1j * c[1], c[4] + 1j * c[5]
         ry = np.array([[c[2], -c[3]], [c[3], c[2]]], dtype=complex)
@@ -49,8 +52,16 @@ def execute(psi: np.ndarray, n: int, passes: np.ndarray, xops: np.ndarray) -> np
         lidx = np.arange(1 << t)
         for x in xops[p["op_begin"]:p["op_begin"] + p["nops"]]:
             k, q0, q1, fl = int(x["kind"]), int(x["q0"]), int(x["q1"]), int(x["flags"])
-            if k <= 4 or k == 11:
+            if k <= 4 or k in (11, 12):
                 _pair(tile, q0, _matrix(x))
+            elif k == 13:  # diag(1, ph) on q0 (tile-uniform when q0 is not local)
+                ph = x["c"][0] + 1j * x["c"][1]
+                if fl & 1:
+                    sel = ((bases >> q0) & 1).astype(bool)
+                    tile[sel] *= ph
+                else:
+                    bit = ((lidx >> q0) & 1).astype(bool)
+                    tile[:, bit] *= ph
             elif k == 5:
                 c = x["c"]
                 d0, d1 = c[0] + 1j * c[1], c[2] + 1j * c[3]
@@ -63,17 +74,20 @@ def execute(psi: np.ndarray, n: int, passes: np.ndarray, xops: np.ndarray) -> np
                     tile[:, bit] *= d1
                     tile[:, ~bit] *= d0
             elif k == 6:
+                ph = x["c"][0] + 1j * x["c"][1] if fl & 8 else 1.0  # phased: control = target = 1 after
                 if fl & 1:
                     sel = ((bases >> q0) & 1).astype(bool)
                     sub = tile[sel]
                     _pair(sub, q1, _matrix({"kind": 4, "c": x["c"]}))
+                    if fl & 8:
+                        sub[:, ((lidx >> q1) & 1).astype(bool)] *= ph
                     tile[sel] = sub
                 else:
                     src = lidx[(((lidx >> q0) & 1) == 1) & (((lidx >> q1) & 1) == 0)]
                     dst = src | (1 << q1)
                     tmp = tile[:, src].copy()
                     tile[:, src] = tile[:, dst]
-                    tile[:, dst] = tmp
+                    tile[:, dst] = tmp * ph
             elif k == 7:
                 nl, lmk = int(x["nl_mask"]), int(x["mask"])
                 rows = (bases & nl) == nl

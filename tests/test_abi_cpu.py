@@ -118,8 +118,12 @@ def test_zyz_plan_carries_the_global_phase_in_one_u2(built):
     n = 12
     ops = workloads.layered_rotations(n, layers=6)
     passes, xops = llgpu.plan_export(n, ops, 8, zyz=True)
-    kinds = np.bincount(xops["kind"], minlength=12)
-    assert kinds[0] == 1 and kinds[11] > 50
+    kinds = np.bincount(xops["kind"], minlength=14)
+    assert kinds[0] == 1 and kinds[12] > 50  # rotations as RY diag(1, g), output phases carried
+    assert kinds[5] == 0  # every RZ folded into carried phases
+    phased = (xops["kind"] == 6) & ((xops["flags"] & 8) != 0)
+    assert phased.sum() > 10  # carried target phases pushed through CNOTs
+    assert 0 < kinds[13] <= n  # the phases still carried at the end, one op per qubit at most
     got = execute(oracle.zero_state(n), n, passes, xops)
     assert np.max(np.abs(got - oracle.run_ops(n, ops))) < 1e-12
 
@@ -135,11 +139,33 @@ def test_zyz_keeps_non_unitary_gates_generic(built):
         recs.append((OP_CNOT, k % 6, (k + 1) % 6, 0.0))
     ops = make_ops(recs)
     passes, xops = llgpu.plan_export(6, ops, 5, zyz=True)
-    kinds = np.bincount(xops["kind"], minlength=12)
-    assert kinds[0] >= 10 and kinds[11] >= 5  # non-unitary products stay generic
+    kinds = np.bincount(xops["kind"], minlength=14)
+    assert kinds[0] >= 10 and kinds[12] >= 5  # non-unitary products stay generic
     got = execute(oracle.zero_state(6), 6, passes, xops)
     want = oracle.run_ops(6, ops)
     assert np.max(np.abs(got - want)) <= 1e-12 * max(1.0, np.max(np.abs(want)))
+
+
+def test_carried_phases_through_every_gate_kind(built):
+    # RZ and X on qubits carrying phases, CNOTs with carried phases on control and target,
+    # H / RX / RY after a carried phase, CZ / MCZ in between, non-local qubits: the plan with
+    # carried phases reproduces the oracle
+    rng = np.random.default_rng(23)
+    n = 9
+    recs = []
+    for _ in range(300):
+        k = rng.integers(9)
+        q = int(rng.integers(n))
+        a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+        ang = float(rng.uniform(-3, 3))
+        recs.append([(OP_RZ, q, 0, ang), (OP_X, q), (OP_H, q), (OP_RX, q, 0, ang), (OP_RY, q, 0, ang),
+                     (OP_CNOT, a, b), (OP_CZ, a, b), (OP_MCZ, 0, 0, 0.0, int(rng.integers(1, 1 << n))),
+                     (OP_U2, q, 0, 0.0, None, np.linalg.qr(rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2)))[0].reshape(4))][k])
+    ops = make_ops(recs)
+    for tile in (4, 6, 9):
+        passes, xops = llgpu.plan_export(n, ops, tile, zyz=True)
+        got = execute(oracle.zero_state(n), n, passes, xops)
+        assert np.max(np.abs(got - oracle.run_ops(n, ops))) < 1e-12, tile
 
 
 def test_thirty_qubit_plan_is_compact(built):
