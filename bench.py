@@ -550,6 +550,7 @@ def run_config1_bench(args, torch, cpu: bool):
     n, reps = 12, 50
     ops = workloads.mixed_h_cnot(n, 1000, seed=1234)
     st = llgpu.State(n)
+    tune = st.autotune(ops)  # tile width and CTA threads for this small register
     stream = torch.cuda.ExternalStream(st.stream)
 
     def one():
@@ -565,6 +566,7 @@ def run_config1_bench(args, torch, cpu: bool):
     got = st.state()
     st.close()
     sv = quantum_sim_v3.StateVector(n)
+    sv.autotune(ops)  # the cached result
     sv.get_numpy_view()
     t0 = time.perf_counter()
     for _ in range(reps):
@@ -584,6 +586,7 @@ def run_config1_bench(args, torch, cpu: bool):
     e2e_calls = (time.perf_counter() - t0) / reps
     res = {"workload": "12 qubits, 1000 ops (H p=0.5 else CNOT), seed 1234, from |0..0>", "device_ms": dt * 1e3,
            "launches_per_circuit": launches, "e2e_ms_op_list": e2e_batch * 1e3, "e2e_ms_per_gate_calls": e2e_calls * 1e3,
+           "autotune": tune,
            "ops_per_s_device": 1000 / dt, "published_reference_ms": 25.91,
            "published_reference_note": "8 cores, README.md:17-27 / docs/RESULTS.md:19-25"}
     del view

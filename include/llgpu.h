@@ -105,7 +105,7 @@ int llg_get_precision(const llg_state* st, int* out);
  * 12 for 16-byte amplitudes, 13 for complex64; llg_autotune picks one by measurement). */
 int llg_set_fusion(llg_state* st, int mode, int tile_qubits);
 /* Threads per CTA of the tile kernel: 0 (default: 512 for tiles of 10+ qubits, else half the
- * tile) or a multiple of 32 in [32, 512]. */
+ * tile) or a multiple of 32 in [32, 1024]. */
 int llg_set_tile_threads(llg_state* st, int threads);
 /* The settings the next flush uses (tile_qubits with the default resolved). */
 int llg_get_tuning(const llg_state* st, int* fuse_mode, int* tile_qubits, int* tile_threads);
@@ -128,8 +128,9 @@ typedef struct llg_tune_result {
 #define LLG_TUNE_AUTO (-1)
 
 /* Times ops[0 .. sample_ops) (0: all) on a scratch state of st's size and precision under each
- * candidate -- per-gate kernels; tile passes of 8..max qubits with 256 threads per CTA, and 512
- * from 10 qubits -- and applies the fastest to st.  Needs device memory for a second state;
+ * candidate -- per-gate kernels; tile passes of 8..max qubits with 256 threads per CTA, 512 from
+ * 10 qubits, and 1024 from 11 qubits on registers of at most 16 qubits -- and applies the fastest
+ * to st.  Needs device memory for a second state;
  * st's amplitudes are not touched. */
 int llg_autotune(llg_state* st, const llg_op* ops, int nops, int sample_ops, llg_tune_result* out);
 /* Forget every cached tuning result. */

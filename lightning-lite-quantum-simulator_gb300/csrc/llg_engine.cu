@@ -431,8 +431,8 @@ int llg_set_fusion(llg_state* st, int mode, int tile_qubits) {
 
 int llg_set_tile_threads(llg_state* st, int threads) {
     if (!st) return set_error(LLG_EINVAL, "llg_set_tile_threads: NULL state");
-    if (threads != 0 && (threads < 32 || threads > 512 || (threads & 31)))
-        return set_error(LLG_EINVAL, "llg_set_tile_threads: threads must be 0 or a multiple of 32 in [32, 512]");
+    if (threads != 0 && (threads < 32 || threads > 1024 || (threads & 31)))
+        return set_error(LLG_EINVAL, "llg_set_tile_threads: threads must be 0 or a multiple of 32 in [32, 1024]");
     int rc = llg_flush(st);
     if (rc) return rc;
     st->tile_threads = threads;

@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(kThreads) k_mcz(typename P::S* __restrict__ ps
 constexpr int kOpChunk = 32;  // op records staged per shared-memory chunk in k_tile
 
 template <class P>
-__global__ void __launch_bounds__(512) k_tile(typename P::S* __restrict__ psi, PassDesc pd, const ExecOp* __restrict__ ops) {
+__global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, PassDesc pd, const ExecOp* __restrict__ ops) {
     using S = typename P::S;
     using K = typename P::K;
     extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -124,9 +124,11 @@ int llg_autotune(llg_state* st, const llg_op* ops, int nops, int sample_ops, llg
         std::vector<Candidate> cands;
         cands.push_back({LLG_FUSE_NONE, 0, 0});
         const int tmax = std::min(n, tile_max_qubits(P));
+        // 1024 threads only pays where few tiles leave SMs idle (small registers)
+        const bool small = n <= 16;
         for (int t = std::max(5, std::min(8, tmax)); t <= tmax; ++t)
-            for (int th : {256, 512})
-                if (th == 256 || t >= 10) cands.push_back({LLG_FUSE_TILE, t, th});
+            for (int th : {256, 512, 1024})
+                if (th == 256 || (th == 512 && t >= 10) || (th == 1024 && small && t >= 11)) cands.push_back({LLG_FUSE_TILE, t, th});
         llg_state* tmp = nullptr;
         int rc = llg_create(n, P, &tmp);
         if (rc) return set_error(rc, "autotune: cannot create the scratch state (a second state of the same size)");

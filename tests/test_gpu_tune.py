@@ -47,7 +47,7 @@ def test_state_autotune_then_parity(precision):
     st2.close()
 
 
-@pytest.mark.parametrize("tile,threads", [(8, 128), (10, 256), (12, 512), (12, 64)])
+@pytest.mark.parametrize("tile,threads", [(8, 128), (10, 256), (12, 512), (12, 64), (12, 1024), (11, 1024)])
 def test_tile_threads_parity(tile, threads):
     n = 14
     ops = workloads.layered_rotations(n, 3)
@@ -57,7 +57,7 @@ def test_tile_threads_parity(tile, threads):
     st.apply_ops(ops)
     assert np.max(np.abs(st.state() - oracle.run_ops(n, ops))) <= 1e-12
     with pytest.raises(ValueError):
-        st.set_tile_threads(1024)
+        st.set_tile_threads(2048)
     with pytest.raises(ValueError):
         st.set_tile_threads(100)
     st.close()
