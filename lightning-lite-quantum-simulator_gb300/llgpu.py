@@ -117,6 +117,7 @@ def lib() -> ctypes.CDLL:
             "llg_adjoint_run": (i, [vp, vp, i, vp, vp, i]),
             "llg_param_shift_run": (i, [vp, vp, i, vp, vp]),
             "llg_adjoint_stream": (i, [vp, P(vp)]),
+            "llg_adjoint_set_threads": (i, [vp, i]),
             "llg_traj_run": (i, [i, vp, i, d, d, u64, u64, u64, i, vp, vp, vp, ctypes.c_int64, P(d)]),
             "llg_batch_create": (i, [i, vp, vp, vp, i, i, P(vp)]),
             "llg_batch_destroy": (i, [vp]),
@@ -424,6 +425,9 @@ class Adjoint:
             self.close()
         except Exception:
             pass
+
+    def set_threads(self, threads: int) -> None:
+        check(lib().llg_adjoint_set_threads(self._h, threads))
 
     def info(self) -> dict:
         f, b_, n = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
