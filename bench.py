@@ -342,8 +342,9 @@ def run_ours(args, rank, world, local):
 # (phase-free unitary) eight 2-term ones, a ZY (RY after an input phase) six, a carried-phase flush
 # (13) two per amplitude pair; a CNOT carrying a pushed phase multiplies a quarter of the amplitudes.
 # CNOT, MCZ and X otherwise move or negate data without arithmetic.
-FP32_INST_PER_PAIR = {"complex128": {0: 172, 1: 76, 2: 76, 3: 76, 4: 0, 5: 76, 6: 0, 7: 0, 11: 152, 12: 114, 13: 38},
-                      "complex64": {0: 16, 1: 8, 2: 8, 3: 8, 4: 0, 5: 8, 6: 0, 7: 0, 11: 16, 12: 12, 13: 4}}
+FP32_INST_PER_PAIR = {"complex128": {0: 172, 1: 76, 2: 76, 3: 76, 4: 0, 5: 76, 6: 0, 7: 0, 11: 152, 12: 114, 13: 38, 14: 92,
+                                     15: 92},
+                      "complex64": {0: 16, 1: 8, 2: 8, 3: 8, 4: 0, 5: 8, 6: 0, 7: 0, 11: 16, 12: 12, 13: 4, 14: 8, 15: 8}}
 PHASED_CNOT_PER_PAIR = {"complex128": 19, "complex64": 2}  # a complex multiply on a quarter of the amplitudes
 SMS, FP32_LANES_PER_SM = 152, 128
 

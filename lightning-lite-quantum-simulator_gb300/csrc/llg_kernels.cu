@@ -162,6 +162,8 @@ __global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, 
             case EX_U2: tile_pairs<P, EX_U2>(tile, tsize >> 1, o.q0, o); break;
             case EX_ZYZ: tile_pairs<P, EX_ZYZ>(tile, tsize >> 1, o.q0, o); break;
             case EX_ZY: tile_pairs<P, EX_ZY>(tile, tsize >> 1, o.q0, o); break;
+            case EX_ZT: tile_pairs<P, EX_ZT>(tile, tsize >> 1, o.q0, o); break;
+            case EX_ZC: tile_pairs<P, EX_ZC>(tile, tsize >> 1, o.q0, o); break;
             case EX_PHASE1: tile_phase1<P>(tile, tsize, base, o); break;
             case EX_RX: tile_pairs<P, EX_RX>(tile, tsize >> 1, o.q0, o); break;
             case EX_RY: tile_pairs<P, EX_RY>(tile, tsize >> 1, o.q0, o); break;

@@ -28,6 +28,9 @@
 
 namespace llg {
 
+// Smallest |product of dropped rotation factors| a pass may carry before a full EX_ZY absorbs it.
+constexpr double kMinPassScale = 0x1p-40;
+
 bool is_single_qubit(int kind) {
     return kind == LLG_OP_H || kind == LLG_OP_X || kind == LLG_OP_RX || kind == LLG_OP_RY || kind == LLG_OP_RZ ||
            kind == LLG_OP_U2;
@@ -308,12 +311,23 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
 
         // Peephole fusion of same-qubit 1-qubit runs, then lowering to local indices.
         std::vector<Pending> pend(n);
+        // Rotations as EX_ZT / EX_ZC leave the pass's amplitudes divided by sigma, the product of
+        // their dropped factors f (|f| >= 1/sqrt 2 each).  One full EX_ZY absorbs sigma: mid-pass
+        // when |sigma| would fall below 2^-40 (amplitudes stay below 2^40 of their true scale), and
+        // at the end of the pass the last EX_ZT / EX_ZC is rewritten as that EX_ZY, so every pass
+        // stores true amplitudes.
+        double sigma = 1.0;
+        int last_t = -1;             // index in out.ops of the last EX_ZT / EX_ZC since sigma was 1
+        double last_f = 1.0, last_c = 1.0, last_s = 0.0;
+        std::complex<double> last_g(1.0, 0.0);
         // local indices for one executor op (global qubits in), then append it
         auto emit_raw = [&](ExecOp e, int src) {
             switch (e.kind) {
                 case EX_U2:
                 case EX_ZYZ:
                 case EX_ZY:
+                case EX_ZT:
+                case EX_ZC:
                 case EX_RX:
                 case EX_RY:
                 case EX_H:
@@ -366,12 +380,29 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
                 carrier = (int)out.ops.size();
                 std::memcpy(carrier_m, m, sizeof(carrier_m));
             } else if (split_zyz(m, z, c, sn, ea, eg)) {
-                e = blank(EX_ZY);
-                e.q0 = q;
-                const double v[4] = {eg.real(), eg.imag(), c, sn};
-                for (int k = 0; k < 4; ++k) e.c[k] = pack_coef(P, v[k]);
                 ph[q] = ea;
                 phase *= z;
+                const bool tan_form = std::fabs(c) >= std::fabs(sn);
+                const double f = tan_form ? c : sn;
+                if (std::fabs(sigma * f) < kMinPassScale) {  // absorb sigma here: a full EX_ZY
+                    e = blank(EX_ZY);
+                    e.q0 = q;
+                    const double v[4] = {eg.real(), eg.imag(), sigma * c, sigma * sn};
+                    for (int k = 0; k < 4; ++k) e.c[k] = pack_coef(P, v[k]);
+                    sigma = 1.0;
+                    last_t = -1;
+                } else {
+                    e = blank(tan_form ? EX_ZT : EX_ZC);
+                    e.q0 = q;
+                    const double v[3] = {eg.real(), eg.imag(), tan_form ? sn / c : c / sn};
+                    for (int k = 0; k < 3; ++k) e.c[k] = pack_coef(P, v[k]);
+                    sigma *= f;
+                    last_t = (int)out.ops.size();
+                    last_f = f;
+                    last_c = c;
+                    last_s = sn;
+                    last_g = eg;
+                }
                 emit_raw(e, src);
                 return;
             }
@@ -511,6 +542,15 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
         for (int q = 0; q < n; ++q)
             if (!flush_pending(q)) return false;
 
+        if (last_t >= 0 && sigma != 1.0) {
+            // the pass's last EX_ZT / EX_ZC becomes the EX_ZY that absorbs sigma: before it the
+            // amplitudes carry 1 / (sigma / last_f), so its rotation is scaled by sigma / last_f
+            ExecOp& e = out.ops[last_t];
+            const double g = sigma / last_f;
+            e.kind = EX_ZY;
+            const double v[4] = {last_g.real(), last_g.imag(), g * last_c, g * last_s};
+            for (int k = 0; k < 4; ++k) e.c[k] = pack_coef(P, v[k]);
+        }
         pd.nops = (int)out.ops.size() - pd.op_begin;
         if (included.empty()) {
             err = "planner made no progress";

@@ -64,6 +64,22 @@ struct PairMath {
             a0.im = P::lin2(c, y0, P::kneg(s), ti);
             a1.re = P::lin2(s, x0, c, tr);
             a1.im = P::lin2(s, y0, c, ti);
+        } else if (KIND == EX_ZT) {  // [1, -t; t, 1] diag(1, eg)
+            const auto gr = k[0], gi = k[1], t = k[2];
+            const auto zr = P::lin2_raw(gr, x1, P::kneg(gi), y1);  // z = eg * a1
+            const auto zi = P::lin2_raw(gr, y1, gi, x1);
+            a0.re = P::fma1(P::kneg(t), zr, x0);
+            a0.im = P::fma1(P::kneg(t), zi, y0);
+            a1.re = P::fma1(t, x0, zr);
+            a1.im = P::fma1(t, y0, zi);
+        } else if (KIND == EX_ZC) {  // [u, -1; 1, u] diag(1, eg)
+            const auto gr = k[0], gi = k[1], u = k[2];
+            const auto zr = P::lin2_raw(gr, x1, P::kneg(gi), y1);
+            const auto zi = P::lin2_raw(gr, y1, gi, x1);
+            a0.re = P::fma1(u, x0, P::neg(zr));
+            a0.im = P::fma1(u, y0, P::neg(zi));
+            a1.re = P::fma1(u, zr, x0);
+            a1.im = P::fma1(u, zi, y0);
         } else if (KIND == EX_H) {  // r [1, 1; 1, -1]
             const auto r = k[0], mr = P::kneg(k[0]);
             a0.re = P::lin2(r, x0, r, x1);
@@ -180,6 +196,8 @@ __device__ void tile_apply(typename P::S* tile, uint32_t tsize, uint64_t base, c
         case EX_U2: tile_pairs<P, EX_U2>(tile, tsize >> 1, o.q0, o); break;
         case EX_ZYZ: tile_pairs<P, EX_ZYZ>(tile, tsize >> 1, o.q0, o); break;
         case EX_ZY: tile_pairs<P, EX_ZY>(tile, tsize >> 1, o.q0, o); break;
+        case EX_ZT: tile_pairs<P, EX_ZT>(tile, tsize >> 1, o.q0, o); break;
+        case EX_ZC: tile_pairs<P, EX_ZC>(tile, tsize >> 1, o.q0, o); break;
         case EX_PHASE1: tile_phase1<P>(tile, tsize, base, o); break;
         case EX_RX: tile_pairs<P, EX_RX>(tile, tsize >> 1, o.q0, o); break;
         case EX_RY: tile_pairs<P, EX_RY>(tile, tsize >> 1, o.q0, o); break;

@@ -18,6 +18,12 @@ def _matrix(x) -> np.ndarray:
     if k == 12:  # [c, -s; s, c] diag(1, eg)
         eg = c[0] + 1j * c[1]
         return np.array([[c[2], -c[3]], [c[3], c[2]]], dtype=complex) @ np.diag([1, eg])
+    if k == 14:  # [1, -t; t, 1] diag(1, eg)
+        eg, t = c[0] + 1j * c[1], c[2]
+        return np.array([[1, -t], [t, 1]], dtype=complex) @ np.diag([1, eg])
+    if k == 15:  # [u, -1; 1, u] diag(1, eg)
+        eg, u = c[0] + 1j * c[1], c[2]
+        return np.array([[u, -1], [1, u]], dtype=complex) @ np.diag([1, eg])
     if k == 11:  # diag(1, ea) [c, -s; s, c] diag(1, eg)
         eg, ea = c[0] + 1j * c[1], c[4] + 1j * c[5]
         ry = np.array([[c[2], -c[3]], [c[3], c[2]]], dtype=complex)
@@ -52,7 +58,7 @@ def execute(psi: np.ndarray, n: int, passes: np.ndarray, xops: np.ndarray) -> np
         lidx = np.arange(1 << t)
         for x in xops[p["op_begin"]:p["op_begin"] + p["nops"]]:
             k, q0, q1, fl = int(x["kind"]), int(x["q0"]), int(x["q1"]), int(x["flags"])
-            if k <= 4 or k in (11, 12):
+            if k <= 4 or k in (11, 12, 14, 15):
                 _pair(tile, q0, _matrix(x))
             elif k == 13:  # diag(1, ph) on q0 (tile-uniform when q0 is not local)
                 ph = x["c"][0] + 1j * x["c"][1]

@@ -118,8 +118,10 @@ def test_zyz_plan_carries_the_global_phase_in_one_u2(built):
     n = 12
     ops = workloads.layered_rotations(n, layers=6)
     passes, xops = llgpu.plan_export(n, ops, 8, zyz=True)
-    kinds = np.bincount(xops["kind"], minlength=14)
-    assert kinds[0] == 1 and kinds[12] > 50  # rotations as RY diag(1, g), output phases carried
+    kinds = np.bincount(xops["kind"], minlength=16)
+    # rotations as RY diag(1, g) over their dropped cos / sin factor (kinds 14, 15), output phases
+    # carried; one full RY per pass (kind 12) absorbs the pass's factors
+    assert kinds[0] == 1 and kinds[14] + kinds[15] > 50 and kinds[12] <= len(passes)
     assert kinds[5] == 0  # every RZ folded into carried phases
     phased = (xops["kind"] == 6) & ((xops["flags"] & 8) != 0)
     assert phased.sum() > 10  # carried target phases pushed through CNOTs
@@ -139,11 +141,59 @@ def test_zyz_keeps_non_unitary_gates_generic(built):
         recs.append((OP_CNOT, k % 6, (k + 1) % 6, 0.0))
     ops = make_ops(recs)
     passes, xops = llgpu.plan_export(6, ops, 5, zyz=True)
-    kinds = np.bincount(xops["kind"], minlength=14)
-    assert kinds[0] >= 10 and kinds[12] >= 5  # non-unitary products stay generic
+    kinds = np.bincount(xops["kind"], minlength=16)
+    assert kinds[0] >= 10 and kinds[12] + kinds[14] + kinds[15] >= 5  # non-unitary products stay generic
     got = execute(oracle.zero_state(6), 6, passes, xops)
     want = oracle.run_ops(6, ops)
     assert np.max(np.abs(got - want)) <= 1e-12 * max(1.0, np.max(np.abs(want)))
+
+
+def _pass_scales(passes, xops):
+    """Per pass: the smallest running product of the factors dropped by kind 14/15 ops since the
+    last full rotation (kind 12), and the product left at the end of the pass."""
+    out = []
+    for p in passes:
+        sig, low = 1.0, 1.0
+        for x in xops[p["op_begin"]:p["op_begin"] + p["nops"]]:
+            k = int(x["kind"])
+            if k in (14, 15):
+                sig /= np.sqrt(1.0 + x["c"][2] ** 2)
+                low = min(low, sig)
+            elif k == 12:
+                sig = 1.0
+        out.append((low, sig))
+    return out
+
+
+def test_tangent_rotations_renormalise_each_pass(built):
+    # one 8-qubit pass of 600 rotations: the dropped factors (|f| >= 1/sqrt 2 each) would shrink
+    # to ~2^-300; full rotations absorb them before 2^-40 and at the end of every pass
+    n = 8
+    ops = workloads.layered_rotations(n, layers=75)
+    for tile in (8, 5):
+        passes, xops = llgpu.plan_export(n, ops, tile, zyz=True)
+        if tile == 8:
+            assert len(passes) == 1
+        kinds = np.bincount(xops["kind"], minlength=16)
+        # one full rotation per pass, plus one per ~60 or more rotations inside a long pass
+        assert 0 < kinds[12] <= len(passes) + (kinds[14] + kinds[15]) // 60
+        for low, end in _pass_scales(passes, xops):
+            assert low >= 2.0 ** -40.5 and end == 1.0
+        got = execute(oracle.zero_state(n), n, passes, xops)
+        assert np.max(np.abs(got - oracle.run_ops(n, ops))) < 1e-12
+    # angles near 0 and pi/2 (tangent and cotangent forms, |coefficient| <= 1), and exactly pi
+    rng = np.random.default_rng(5)
+    recs = []
+    for k in range(200):
+        q = int(rng.integers(4))
+        ang = [0.0, np.pi, -np.pi, np.pi / 2, 1e-9, np.pi - 1e-9, float(rng.uniform(-7, 7))][k % 7]
+        recs += [(OP_RY, q, 0, ang), (OP_RZ, q, 0, float(rng.uniform(-3, 3))), (OP_CNOT, q, (q + 1) % 4)]
+    ops = make_ops(recs)
+    passes, xops = llgpu.plan_export(4, ops, 4, zyz=True)
+    t = xops["c"][:, 2][np.isin(xops["kind"], (14, 15))]
+    assert t.size and np.all(np.abs(t) <= 1.0)
+    got = execute(oracle.zero_state(4), 4, passes, xops)
+    assert np.max(np.abs(got - oracle.run_ops(4, ops))) < 1e-12
 
 
 def test_carried_phases_through_every_gate_kind(built):
