@@ -103,7 +103,7 @@ __device__ typename P::Acc tile_generator_inner(const typename P::S* psi, const 
     }
     const uint32_t bit = 1u << o.q0;
     for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += blockDim.x) {
-        const uint32_t j0 = (uint32_t)insert0(p, o.q0), j1 = j0 | bit;
+        const uint32_t j0 = ins0(p, bit), j1 = j0 | bit;
         const auto p0 = P::load(psi[j0]), p1 = P::load(psi[j1]);
         const auto l0 = P::load(lam[j0]), l1 = P::load(lam[j1]);
         if (o.kind == EX_RY_P) {  // Y: Re(conj(l1) p0) - Re(conj(l0) p1)

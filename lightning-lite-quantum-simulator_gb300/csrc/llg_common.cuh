@@ -333,6 +333,10 @@ __device__ __forceinline__ A block_sum_acc(A v, A* sh) {
 // ------------------------------------------------------------------------------------------
 // index helpers
 // ------------------------------------------------------------------------------------------
+// Insert a 0 at bit `bit` (a power of two) of a 32-bit tile-local index: p + (p & ~(bit - 1))
+// doubles the part above the bit and keeps the part below (two integer instructions).
+__device__ __forceinline__ uint32_t ins0(uint32_t p, uint32_t bit) { return p + (p & (0u - bit)); }
+
 __host__ __device__ __forceinline__ uint64_t insert0(uint64_t p, int q) {
     const uint64_t low = p & ((1ULL << q) - 1);
     return ((p >> q) << (q + 1)) | low;

@@ -108,7 +108,7 @@ __device__ __forceinline__ void tile_pairs(typename P::S* tile, uint32_t npairs,
     const PairMath<P, KIND> m(o);
     const uint32_t bit = 1u << q;
     for (uint32_t p = threadIdx.x; p < npairs; p += blockDim.x) {
-        const uint32_t j0 = (uint32_t)insert0(p, q), j1 = j0 | bit;
+        const uint32_t j0 = ins0(p, bit), j1 = j0 | bit;
         auto a0 = P::load(tile[j0]);
         auto a1 = P::load(tile[j1]);
         m.apply(a0, a1);
@@ -134,7 +134,7 @@ __device__ __forceinline__ void tile_phase1(typename P::S* tile, uint32_t tsize,
     }
     const uint32_t bit = 1u << o.q0;
     for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += blockDim.x) {
-        const uint32_t j = (uint32_t)insert0(p, o.q0) | bit;
+        const uint32_t j = ins0(p, bit) | bit;
         auto a = P::load(tile[j]);
         cmul_const<P>(a, pr, pi, mpi);
         tile[j] = P::store(a);
@@ -154,7 +154,7 @@ __device__ __forceinline__ void tile_cnot(typename P::S* tile, uint32_t tsize, u
         if (!((base >> o.q0) & 1)) return;
         const uint32_t tbit = 1u << tq;
         for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += blockDim.x) {
-            const uint32_t j0 = (uint32_t)insert0(p, tq), j1 = j0 | tbit;
+            const uint32_t j0 = ins0(p, tbit), j1 = j0 | tbit;
             const S x = tile[j0];
             tile[j0] = tile[j1];
             if (phased) {
@@ -171,7 +171,7 @@ __device__ __forceinline__ void tile_cnot(typename P::S* tile, uint32_t tsize, u
     const int lo = c < tq ? c : tq, hi = c < tq ? tq : c;
     const uint32_t cbit = 1u << c, tbit = 1u << tq;
     for (uint32_t r = threadIdx.x; r < (tsize >> 2); r += blockDim.x) {
-        const uint32_t j = (uint32_t)insert0(insert0(r, lo), hi) | cbit;
+        const uint32_t j = ins0(ins0(r, 1u << lo), 1u << hi) | cbit;
         const S x = tile[j];
         tile[j] = tile[j | tbit];
         if (phased) {
@@ -215,7 +215,7 @@ __device__ void tile_apply(typename P::S* tile, uint32_t tsize, uint64_t base, c
                 m.k[1] = sv;
                 const uint32_t bit = 1u << o.q0;
                 for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += blockDim.x) {
-                    const uint32_t j0 = (uint32_t)insert0(p, o.q0), j1 = j0 | bit;
+                    const uint32_t j0 = ins0(p, bit), j1 = j0 | bit;
                     auto a0 = P::load(tile[j0]);
                     auto a1 = P::load(tile[j1]);
                     m.apply(a0, a1);
@@ -227,7 +227,7 @@ __device__ void tile_apply(typename P::S* tile, uint32_t tsize, uint64_t base, c
                 m.k[1] = sv;
                 const uint32_t bit = 1u << o.q0;
                 for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += blockDim.x) {
-                    const uint32_t j0 = (uint32_t)insert0(p, o.q0), j1 = j0 | bit;
+                    const uint32_t j0 = ins0(p, bit), j1 = j0 | bit;
                     auto a0 = P::load(tile[j0]);
                     auto a1 = P::load(tile[j1]);
                     m.apply(a0, a1);

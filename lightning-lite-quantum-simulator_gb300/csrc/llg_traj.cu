@@ -216,7 +216,7 @@ struct Traj {
                         const int lo = c < t ? c : t, hi = c < t ? t : c;
                         const uint32_t cbit = 1u << c, tbit = 1u << t;
                         for (uint32_t r = threadIdx.x; r < (NL >> 2); r += blockDim.x) {
-                            const uint32_t j = (uint32_t)insert0(insert0(r, lo), hi) | cbit;
+                            const uint32_t j = ins0(ins0(r, 1u << lo), 1u << hi) | cbit;
                             const S x = s[j];
                             s[j] = s[j | tbit];
                             s[j | tbit] = x;
@@ -336,7 +336,7 @@ struct Traj {
         } else {
             const uint32_t bit = 1u << q;
             for (uint32_t p = threadIdx.x; p < (NL >> 1); p += blockDim.x) {
-                const uint32_t j = (uint32_t)insert0(p, q) | bit;
+                const uint32_t j = ins0(p, bit) | bit;
                 auto a = P::load(s[j]);
                 a.re = P::neg(a.re);
                 a.im = P::neg(a.im);
@@ -359,7 +359,7 @@ struct Traj {
         } else {
             const uint32_t bit = 1u << q;
             for (uint32_t p = threadIdx.x; p < (NL >> 1); p += blockDim.x) {
-                const uint32_t j0 = (uint32_t)insert0(p, q), j1 = j0 | bit;
+                const uint32_t j0 = ins0(p, bit), j1 = j0 | bit;
                 const S t = s[j0];
                 s[j0] = s[j1];
                 s[j1] = t;
@@ -394,7 +394,7 @@ struct Traj {
         if (!cross(q)) {
             const uint32_t bit = 1u << q;
             for (uint32_t p = threadIdx.x; p < (NL >> 1); p += blockDim.x) {
-                const uint32_t j0 = (uint32_t)insert0(p, q), j1 = j0 | bit;
+                const uint32_t j0 = ins0(p, bit), j1 = j0 | bit;
                 C a0 = P::load(s[j0]), a1 = P::load(s[j1]);
                 C t0, t1;
                 if (adj) {
