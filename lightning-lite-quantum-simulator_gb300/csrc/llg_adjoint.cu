@@ -57,7 +57,11 @@ constexpr int kThreads = 256;
 constexpr int kEBlocksPerState = 64;
 
 // ------------------------------------------------------------------------------------------
-// coefficient table: table[row][j] = (cos(theta/2), sin(theta/2)) packed for the precision
+// coefficient table: table[row][j] = (cos(theta/2), sin(theta/2)) packed for the precision; for an
+// RZ occurrence (cos theta, sin theta): RZ runs as diag(1, e^{i theta}) without its global phase
+// e^{-i theta/2}.  psi and lambda pick up the same phases through both sweeps, so energies
+// <psi|O|psi> and gradients Im <lambda|P|psi> are unchanged, and RZ costs one complex product on
+// half of the amplitudes instead of one on every amplitude.
 // ------------------------------------------------------------------------------------------
 template <class P>
 __device__ uint64_t pack_dev(double x) {
@@ -75,10 +79,11 @@ __global__ void k_coef_table(const double* __restrict__ params, int nparams, con
     if (idx >= rows * nocc) return;
     const int r = idx / nocc, j = idx % nocc;
     const int set = row_set ? row_set[r] : r;
-    double theta = params[(size_t)set * nparams + occ_param[j]];
+    const int code = occ_param[j];  // 2 * parameter + (1 for an RZ occurrence)
+    double theta = params[(size_t)set * nparams + (code >> 1)];
     if (shift_occ && shift_occ[r] == j) theta += shift_val[r];
     double s, c;
-    sincos(0.5 * theta, &s, &c);
+    sincos((code & 1) ? theta : 0.5 * theta, &s, &c);
     table[2 * (size_t)idx] = pack_dev<P>(c);
     table[2 * (size_t)idx + 1] = pack_dev<P>(s);
 }
@@ -617,6 +622,9 @@ int llg_adjoint_create(int n, const llg_op* ops, int nops, int nparams, int max_
         if (o.param >= 0) h->occ_param.push_back(o.param);
     }
     h->nocc = (int)h->occ_param.size();
+    std::vector<int> occ_code;  // the device copy: 2 * parameter + (1 for RZ, whose table entry is the full angle)
+    for (int i = 0; i < nops; ++i)
+        if (ops[i].param >= 0) occ_code.push_back(2 * ops[i].param + (ops[i].kind == LLG_OP_RZ ? 1 : 0));
     std::string err;
     const int t = std::min(n, kAdjTile);
     if (!plan_tiles(n, ops, nops, t, precision, h->fwd, err, true)) {
@@ -667,7 +675,7 @@ int llg_adjoint_create(int n, const llg_op* ops, int nops, int nparams, int max_
         rc = cudaMemcpy(h->d_bwd_ops, h->bwd_ops.data(), h->bwd_ops.size() * sizeof(ExecOp), cudaMemcpyHostToDevice)
                  ? set_error(LLG_ECUDA, "adjoint_create: op upload") : LLG_OK;
     if (!rc && h->nocc)
-        rc = cudaMemcpy(h->d_occ_param, h->occ_param.data(), h->nocc * sizeof(int), cudaMemcpyHostToDevice) ||
+        rc = cudaMemcpy(h->d_occ_param, occ_code.data(), h->nocc * sizeof(int), cudaMemcpyHostToDevice) ||
                      cudaMemcpy(h->d_csr_occ, occ.data(), h->nocc * sizeof(int), cudaMemcpyHostToDevice)
                  ? set_error(LLG_ECUDA, "adjoint_create: map upload") : LLG_OK;
     if (!rc)

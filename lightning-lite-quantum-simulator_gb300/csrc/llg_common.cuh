@@ -323,9 +323,9 @@ __device__ __forceinline__ A block_sum_acc(A v, A* sh) {
     if (lane == 0) sh[warp] = v;
     __syncthreads();
     A r = v;
-    if (threadIdx.x == 0) {
-        r = sh[0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = acc_plus(r, sh[w]);
+    if (warp == 0) {  // the warp sums in a second shuffle tree (no serial loop in one thread)
+        r = lane < (int)(blockDim.x >> 5) ? sh[lane] : A{};
+        r = warp_sum_acc(r);
     }
     return r;
 }

@@ -237,23 +237,34 @@ __device__ void tile_apply(typename P::S* tile, uint32_t tsize, uint64_t base, c
             }
             break;
         }
-        case EX_DIAG:
         case EX_RZ_P: {
-            K d0r, d0i, d1r, d1i;
-            if (o.kind == EX_DIAG) {
-                d0r = P::k_from_bits(o.c[0]);
-                d0i = P::k_from_bits(o.c[1]);
-                d1r = P::k_from_bits(o.c[2]);
-                d1i = P::k_from_bits(o.c[3]);
-            } else {  // RZ(t) = diag(c - i s, c + i s); its inverse swaps the signs
-                const K c = P::k_from_bits(trow[2 * o.q1]);
-                K s = P::k_from_bits(trow[2 * o.q1 + 1]);
-                if (o.flags & OPF_ADJOINT) s = P::kneg(s);
-                d0r = c;
-                d0i = P::kneg(s);
-                d1r = c;
-                d1i = s;
+            // RZ(t) up to its global phase e^{-it/2}: diag(1, e^{it}), the table row holding
+            // (cos t, sin t); the inverse conjugates
+            const K pr = P::k_from_bits(trow[2 * o.q1]);
+            K pi = P::k_from_bits(trow[2 * o.q1 + 1]);
+            if (o.flags & OPF_ADJOINT) pi = P::kneg(pi);
+            const K mpi = P::kneg(pi);
+            if (o.flags & OPF_NONLOCAL_Q0) {
+                if ((base >> o.q0) & 1)
+                    for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
+                        auto a = P::load(tile[l]);
+                        cmul_const<P>(a, pr, pi, mpi);
+                        tile[l] = P::store(a);
+                    }
+            } else {
+                const uint32_t bit = 1u << o.q0;
+                for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += blockDim.x) {
+                    const uint32_t j = ins0(p, bit) | bit;
+                    auto a = P::load(tile[j]);
+                    cmul_const<P>(a, pr, pi, mpi);
+                    tile[j] = P::store(a);
+                }
             }
+            break;
+        }
+        case EX_DIAG: {
+            const K d0r = P::k_from_bits(o.c[0]), d0i = P::k_from_bits(o.c[1]);
+            const K d1r = P::k_from_bits(o.c[2]), d1i = P::k_from_bits(o.c[3]);
             if (o.flags & OPF_NONLOCAL_Q0) {
                 const bool one = (base >> o.q0) & 1;
                 const K dr = one ? d1r : d0r, di = one ? d1i : d0i;
