@@ -50,6 +50,7 @@ namespace {
 constexpr int kTrajThreads = 1024;
 constexpr int kMaxPerThread = 16;  // amplitudes per thread in a cross-CTA step (2^14 / 1024)
 constexpr int kMaxGrid = 4096;     // persistent CTAs at most (per-CTA margin slots)
+constexpr int kUChunk = 512;       // noise sites whose uniforms are drawn together (one Philox call per thread)
 
 // one gate of a trajectory circuit: the executor op (global qubits) and the touched qubits
 struct TrajGate {
@@ -263,15 +264,18 @@ struct Traj {
     // (1 - 2 bit0)|a|^2 when z0 is set; identical in every CTA of the group
     __device__ double reduce(int q, bool z0, typename P::Acc* red, typename P::Acc* slot) {
         typename P::Acc pos = P::acc_zero(), neg = P::acc_zero();
-        for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x) {
-            const auto a = P::load(s[l]);
-            if (z0) {
+        if (z0) {
+            for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x) {
+                const auto a = P::load(s[l]);
                 if (l & 1) neg = P::acc_norm(neg, a);
                 else pos = P::acc_norm(pos, a);
-            } else {
-                const int bit = cross(q) ? rank : (int)((l >> q) & 1);
-                if (bit) pos = P::acc_norm(pos, a);
             }
+        } else if (cross(q)) {  // the partner with the top qubit set holds the whole bit-1 half
+            if (rank)
+                for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x) pos = P::acc_norm(pos, P::load(s[l]));
+        } else {  // only the amplitudes with bit q set are read
+            const uint32_t bit = 1u << q;
+            for (uint32_t p = threadIdx.x; p < (NL >> 1); p += blockDim.x) pos = P::acc_norm(pos, P::load(s[ins0(p, bit) | bit]));
         }
         return group_total(acc_minus(pos, neg), red, slot);
     }
@@ -439,11 +443,11 @@ struct Traj {
     }
 };
 
-// thread 0: draw and decide one site pair (AD at `site`, PD at site + 1), as the oracle does
+// thread 0: decide one site pair (AD at a site, PD at the next) from its two uniforms, as the
+// oracle does
 template <class P>
-__device__ void decide(double P1, const KrausParams& kp, uint64_t traj, uint64_t site, Decision* d, double* min_margin) {
+__device__ void decide(double P1, const KrausParams& kp, double u1, double u2, Decision* d, double* min_margin) {
     // amplitude damping
-    const double u1 = philox_u1(kp.seed, traj, site);
     double s_ad = 1.0 - kp.gamma * P1;
     const double tot_ad = kp.gamma * P1;
     double m = fabs(u1 - s_ad);
@@ -462,7 +466,6 @@ __device__ void decide(double P1, const KrausParams& kp, uint64_t traj, uint64_t
         p1 = (1.0 - kp.gamma) * P1 / s_ad;
     }
     // phase damping
-    const double u2 = philox_u1(kp.seed, traj, site + 1);
     const double s_pd = 1.0 - kp.lambda * p1;
     const double tot_pd = kp.lambda * p1;
     m = fabs(u2 - s_pd);
@@ -491,6 +494,11 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
     __shared__ typename P::Acc slot;
     __shared__ Decision dec;
     __shared__ ObsTerms ob;  // the observable, copied once from global memory
+    // uniforms of sites [u_begin, u_end): Kraus mode uni[site - u_begin] = philox_u1(site); depolarizing
+    // mode (uni[2 i], uni[2 i + 1]) = philox_u12(u_begin + i).  Drawn together, one Philox call per
+    // thread, instead of serially by the deciding thread.
+    __shared__ double uni[2 * kUChunk];
+    uint64_t u_begin = 0, u_end = 0;
     static_assert(sizeof(ObsTerms) % 4 == 0, "ObsTerms copies as 32-bit words");
     for (uint32_t w = threadIdx.x; w < sizeof(ObsTerms) / 4; w += blockDim.x)
         reinterpret_cast<int32_t*>(&ob)[w] = reinterpret_cast<const int32_t*>(obs)[w];
@@ -521,6 +529,17 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
         group_sync<CL>();
         uint64_t site = 0;
         uint32_t jumps = 0;
+        u_begin = u_end = 0;
+        auto draw = [&](uint64_t first) {  // every thread, at the same site
+            __syncthreads();
+            for (int i = threadIdx.x; i < kUChunk; i += blockDim.x) {
+                if (kp.mode == NOISE_DEPOL) philox_u12(kp.seed, traj, first + i, &uni[2 * i], &uni[2 * i + 1]);
+                else uni[i] = philox_u1(kp.seed, traj, first + i);
+            }
+            u_begin = first;
+            u_end = first + kUChunk;
+            __syncthreads();
+        };
         for (int g = 0; g < ngates; ++g) {
             const TrajGate& G = gates[g];
             T.gate(G.op);
@@ -530,8 +549,8 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
                 if (!(kp.gamma > 0.0)) continue;
                 const int nsites = G.pair ? 1 : G.nt;
                 for (int k = 0; k < nsites; ++k) {
-                    double u, u2;
-                    philox_u12(kp.seed, traj, site, &u, &u2);
+                    if (site >= u_end) draw(site);
+                    const double u = uni[2 * (site - u_begin)], u2 = uni[2 * (site - u_begin) + 1];
                     ++site;
                     if (u >= kp.gamma) continue;
                     ++jumps;
@@ -547,8 +566,10 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
             }
             for (int k = 0; k < G.nt; ++k) {
                 const int q = G.q[k];
+                if (site + 1 >= u_end) draw(site);  // AD and PD uniforms of this pair in one chunk
                 const double P1 = T.reduce(q, false, red, &slot);
-                if (threadIdx.x == 0) decide<P>(P1, kp, traj, site, &dec, &min_margin);
+                if (threadIdx.x == 0)
+                    decide<P>(P1, kp, uni[site - u_begin], uni[site + 1 - u_begin], &dec, &min_margin);
                 __syncthreads();
                 const int code = dec.ad_jump | (dec.pd_jump << 1);
                 T.kraus_apply(q, &dec);
