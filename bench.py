@@ -460,6 +460,22 @@ def run_sweep_bench(args, torch):
             per = ms / cnt / 1e3
             gbs = bytes_per.get(name, 32) * (1 << n) / per / 1e9
             res[name] = {"ms_per_sweep": per * 1e3, "gbs": gbs, "frac": gbs / peak}
+            if name in bytes_per:
+                # per (control, target): with qubit 0 among the touched bits, touched and untouched
+                # amplitudes share every 32-byte sector, so DRAM moves twice the algorithmic bytes
+                cases = []
+                for rec in recs:
+                    one = make_ops([rec])
+                    st.profile(True)
+                    st.profile_read(reset=True)
+                    for _ in range(2):
+                        st.apply_ops(one)
+                    st.sync()
+                    ms1, cnt1 = st.profile_read(reset=True)["gate"]
+                    st.profile(False)
+                    g1 = bytes_per[name] * (1 << n) / (ms1 / cnt1 / 1e3) / 1e9
+                    cases.append({"qubits": [rec[1], rec[2]], "gbs": g1, "frac": g1 / peak})
+                res[name]["cases"] = cases
         # dense k-qubit blocks (llg_apply_matrix): 32 B x 2^n per application and 8 x 4^k x 2^(n-k)
         # real FLOP of complex multiply-adds
         rng = np.random.default_rng(17)

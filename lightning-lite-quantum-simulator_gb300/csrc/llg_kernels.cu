@@ -88,30 +88,60 @@ __global__ void __launch_bounds__(kThreads) k_diag(typename P::S* __restrict__ p
     }
 }
 
-// CNOT: swap (c=1, t=0) <-> (c=1, t=1) over the N/4 quads (src/StateVectorBackend.h:109-135)
+// CNOT: swap (c=1, t=0) <-> (c=1, t=1) over the N/4 quads (src/StateVectorBackend.h:109-135).
+// kStreamItems quads per thread per step, all loads issued before the stores (memory-level
+// parallelism for a kernel that does no arithmetic).
+constexpr int kStreamItems = 4;
+
 template <class P>
 __global__ void __launch_bounds__(kThreads) k_cnot(typename P::S* __restrict__ psi, uint64_t nquads, int c, int t) {
+    using S = typename P::S;
     const int lo = c < t ? c : t, hi = c < t ? t : c;
     const uint64_t cbit = 1ULL << c, tbit = 1ULL << t;
-    const uint64_t step = (uint64_t)gridDim.x * kThreads;
-    for (uint64_t r = (uint64_t)blockIdx.x * kThreads + threadIdx.x; r < nquads; r += step) {
-        const uint64_t i = insert0(insert0(r, lo), hi) | cbit;
-        const auto x = psi[i];
-        psi[i] = psi[i | tbit];
-        psi[i | tbit] = x;
+    const uint64_t step = (uint64_t)gridDim.x * kThreads * kStreamItems;
+    for (uint64_t base = (uint64_t)blockIdx.x * kThreads * kStreamItems + threadIdx.x; base < nquads; base += step) {
+        uint64_t idx[kStreamItems];
+        S x[kStreamItems], y[kStreamItems];
+#pragma unroll
+        for (int u = 0; u < kStreamItems; ++u) {
+            const uint64_t r = base + (uint64_t)u * kThreads;
+            idx[u] = r < nquads ? (insert0(insert0(r, lo), hi) | cbit) : ~0ULL;
+            if (idx[u] != ~0ULL) {
+                x[u] = psi[idx[u]];
+                y[u] = psi[idx[u] | tbit];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kStreamItems; ++u)
+            if (idx[u] != ~0ULL) {
+                psi[idx[u]] = y[u];
+                psi[idx[u] | tbit] = x[u];
+            }
     }
 }
 
 // MCZ: negate the amplitudes with every mask bit set (src/StateVectorBackend.h:137-151)
 template <class P>
 __global__ void __launch_bounds__(kThreads) k_mcz(typename P::S* __restrict__ psi, uint64_t count, uint64_t mask) {
-    const uint64_t step = (uint64_t)gridDim.x * kThreads;
-    for (uint64_t r = (uint64_t)blockIdx.x * kThreads + threadIdx.x; r < count; r += step) {
-        const uint64_t i = insert0_mask(r, mask) | mask;
-        auto a = P::load(psi[i]);
-        a.re = P::neg(a.re);
-        a.im = P::neg(a.im);
-        psi[i] = P::store(a);
+    using S = typename P::S;
+    const uint64_t step = (uint64_t)gridDim.x * kThreads * kStreamItems;
+    for (uint64_t base = (uint64_t)blockIdx.x * kThreads * kStreamItems + threadIdx.x; base < count; base += step) {
+        uint64_t idx[kStreamItems];
+        S v[kStreamItems];
+#pragma unroll
+        for (int u = 0; u < kStreamItems; ++u) {
+            const uint64_t r = base + (uint64_t)u * kThreads;
+            idx[u] = r < count ? (insert0_mask(r, mask) | mask) : ~0ULL;
+            if (idx[u] != ~0ULL) v[u] = psi[idx[u]];
+        }
+#pragma unroll
+        for (int u = 0; u < kStreamItems; ++u)
+            if (idx[u] != ~0ULL) {
+                auto a = P::load(v[u]);
+                a.re = P::neg(a.re);
+                a.im = P::neg(a.im);
+                psi[idx[u]] = P::store(a);
+            }
     }
 }
 
@@ -320,10 +350,10 @@ cudaError_t exec_op_t(void* vpsi, int n, const ExecOp& op, cudaStream_t s) {
         case EX_H: k_pairs<P, EX_H><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
         case EX_X: k_pairs<P, EX_X><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
         case EX_DIAG: k_diag<P><<<grid_for(size, 1), kThreads, 0, s>>>(psi, size, op.q0, op); break;
-        case EX_CNOT: k_cnot<P><<<grid_for(size / 4, 1), kThreads, 0, s>>>(psi, size / 4, op.q0, op.q1); break;
+        case EX_CNOT: k_cnot<P><<<grid_for(size / 4, kStreamItems), kThreads, 0, s>>>(psi, size / 4, op.q0, op.q1); break;
         case EX_MCZ: {
             const uint64_t cnt = size >> __builtin_popcountll(op.mask);
-            k_mcz<P><<<grid_for(cnt, 1), kThreads, 0, s>>>(psi, cnt, op.mask);
+            k_mcz<P><<<grid_for(cnt, kStreamItems), kThreads, 0, s>>>(psi, cnt, op.mask);
             break;
         }
         default: return cudaErrorInvalidValue;
