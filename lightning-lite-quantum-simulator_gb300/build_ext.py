@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", *ARCH, "-
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-I" + INCLUDE, "-I" + CSRC]
 
 CU_SOURCES = ["llg_kernels.cu", "llg_engine.cu", "llg_noalloc.cu", "llg_adjoint.cu", "llg_traj.cu", "llg_batch.cu",
-              "llg_tune.cu", "llg_block.cu",
+              "llg_tune.cu", "llg_block.cu", "llg_block_tc.cu",
               "llg_tsolver.cu"]
 CXX_SOURCES = ["llg_plan.cpp"]
 

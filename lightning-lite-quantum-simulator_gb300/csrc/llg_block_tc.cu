@@ -1,0 +1,392 @@
+// llg_block_tc.cu -- dense 5-qubit blocks on complex128 (double-float) states with the fifth-
+// generation tensor cores (tcgen05.mma, accumulators in tensor memory).
+//
+// A 5-qubit block maps every group of 32 amplitudes that differ only in the target qubits through
+// a 32x32 complex matrix.  Written over reals it is one product per tile of 128 groups:
+//     D[g][r] = sum_k X[g][k] W[r][k],   X[g] = (re a_0 .. re a_31, im a_0 .. im a_31),
+// with W the 64x64 real form of the matrix.  Double-float operands (~48-bit significands) are
+// split exactly into six signed 8-bit slices against a power-of-two scale per row (the Ozaki
+// scheme: Ozaki, Ogita, Oishi and Rump, Numer. Algorithms 2012):
+//     X[g][k] = 2^(e_g - 8) sum_i x_i[g][k] 2^(-8 i),   W[r][k] = 2^(e_r - 8) sum_j w_j[r][k] 2^(-8 j),
+// where every slice is an integer of magnitude <= 256, exact in bf16.  The 21 slice products
+// with i + j <= 5 are accumulated by diagonal d = i + j into six fp32 accumulators in tensor
+// memory.  A product of two slices is below 2^16 and 64 of them below 2^22, so each diagonal sum
+// is an integer below 2^24 and the fp32 accumulation is exact.  The epilogue recombines
+//     D = 2^(e_g + e_r - 16) sum_d 2^(-8 d) D_d
+// into double-float.  Dropped terms (i + j >= 6) and the final rounding stay near 2^-46 of each
+// group's largest amplitude.
+//
+// One persistent CTA of 512 threads per SM.  Per tile: every thread takes its 8 amplitudes from
+// shared memory (copied asynchronously while the previous tile was in the tensor cores), the
+// group scales come from the largest high part, slices go to shared memory in the no-swizzle
+// K-major core-matrix layout, one thread issues the 84 MMAs (M = 128 groups, N = 64, K = 16 per
+// instruction) and commits them to an mbarrier, all threads wait (bounded), read the
+// accumulators with tcgen05.ld, recombine and stage the amplitudes in shared memory, and store
+// them.  The gate's slices are prepared on the host in double (exact) and copied to shared
+// memory once per CTA.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#include <cuda_runtime.h>
+
+#include "llg_common.cuh"
+#include "llg_internal.h"
+#include "llg_launch.h"
+
+namespace llg {
+
+namespace {
+
+constexpr int kTcThreads = 512;
+constexpr int kTcGroups = 128;            // groups per tile (the MMA's M)
+constexpr int kTcPer = kTcGroups * 32 / kTcThreads;  // amplitudes per thread (8)
+constexpr int kTcReals = 64;              // reals per group (the MMA's K and N)
+constexpr int kTcSlices = 6;              // 8-bit slices per operand
+constexpr int kTcSliceBytes = kTcGroups * kTcReals * 2;   // one state slice, bf16
+constexpr int kTcWSliceBytes = kTcReals * kTcReals * 2;   // one gate slice, bf16
+constexpr int kTcTmemCols = 512;          // six 64-column accumulators, rounded to a power of two
+constexpr long kTcWaitLimit = 1L << 26;   // mbarrier polls before the kernel reports a timeout
+
+__device__ int g_block_tc_error = 0;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// tcgen05 shared-memory descriptor, no swizzle: start, leading (K-direction core) byte offset,
+// stride (8-row group) byte offset, descriptor version 1
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// byte offset of element (row, k) of a rows x kTcReals bf16 operand in the core-matrix layout:
+// 8x8 cores of 128 bytes, K-direction cores adjacent, 8-row groups kTcReals / 8 cores apart
+__host__ __device__ __forceinline__ uint32_t core_off(int row, int k) {
+    return (uint32_t)((row >> 3) * (kTcReals / 8) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// 2^e as a float for e in [-126, 127]
+__device__ __forceinline__ float pow2f(int e) { return __uint_as_float((uint32_t)(e + 127) << 23); }
+
+// double-float plus float (error-free up to the final renormalisation)
+__device__ __forceinline__ df df_add_f(df a, float b) {
+    const df s = two_sum(a.hi, b);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_block_tc(float4* __restrict__ psi, int n, BlockDesc bd, const uint16_t* __restrict__ wslices,
+               const int32_t* __restrict__ wexp) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* sA = smem;                                   // kTcSlices state slices (also the output stage)
+    unsigned char* sW = smem + kTcSlices * kTcSliceBytes;       // kTcSlices gate slices
+    // the next tile's amplitudes, [amplitude][group] so that a warp's 32 groups are 32 consecutive
+    // float4s (a [group][amplitude] layout puts them 512 bytes apart: one bank, 32-way conflicts)
+    float4* sIn = reinterpret_cast<float4*>(sW + kTcSlices * kTcWSliceBytes);
+    __shared__ uint64_t toff[32];
+    __shared__ int32_t eg_s[kTcGroups];
+    __shared__ int32_t er_s[kTcReals];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_s;
+    __shared__ int abort_s;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    for (int j = tid; j < 32; j += blockDim.x) {
+        uint64_t o = 0;
+        for (int b = 0; b < 5; ++b)
+            if ((j >> b) & 1) o |= 1ULL << bd.q[b];
+        toff[j] = o;
+    }
+    for (int r = tid; r < kTcReals; r += blockDim.x) er_s[r] = wexp[r];
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(wslices);
+        uint4* dst = reinterpret_cast<uint4*>(sW);
+        for (int i = tid; i < kTcSlices * kTcWSliceBytes / 16; i += blockDim.x) dst[i] = src[i];
+    }
+    if (tid == 0) {
+        abort_s = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_s)),
+                     "r"(kTcTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_s;
+
+    const uint64_t ngroups = 1ULL << (n - 5);
+    const uint64_t ntiles = ngroups / kTcGroups;
+    // instruction descriptor: fp32 accumulate, bf16 A and B, both K-major, N = 64, M = 128
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcReals >> 3) << 17) |
+                           ((uint32_t)(kTcGroups >> 4) << 24);
+    const uint32_t lbo = 128, sbo = (kTcReals / 8) * 128;
+    const int gl = tid & (kTcGroups - 1);  // the group this thread loads, slices and stores
+    const int h = tid >> 7;                // which kTcPer of its 32 amplitudes
+    uint32_t phase = 0;
+    // a thread's amplitudes of a tile go to sIn[(kTcPer h + i) * 128 + gl] by asynchronous copies,
+    // issued one tile ahead so that their latency hides behind the products and the epilogue
+    auto prefetch = [&](uint64_t tile) {
+        const uint64_t b = insert0_mask(tile * kTcGroups + (uint64_t)gl, bd.tmask);
+#pragma unroll
+        for (int i = 0; i < kTcPer; ++i)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(&sIn[(kTcPer * h + i) * kTcGroups + gl])),
+                         "l"(psi + (b | toff[kTcPer * h + i]))
+                         : "memory");
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    __syncthreads();  // toff
+    if ((uint64_t)blockIdx.x < ntiles) prefetch(blockIdx.x);
+
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        // ---- this thread's amplitudes of group gl (its own copies), the group's scale ----
+        const uint64_t g = tile * kTcGroups + (uint64_t)gl;
+        const uint64_t base = insert0_mask(g, bd.tmask);
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        float4 a[kTcPer];
+        float mx = 0.0f;
+#pragma unroll
+        for (int i = 0; i < kTcPer; ++i) {
+            a[i] = sIn[(kTcPer * h + i) * kTcGroups + gl];
+            mx = fmaxf(mx, fmaxf(fabsf(a[i].x), fabsf(a[i].y)));
+        }
+        if (h == 0) eg_s[gl] = 0;
+        __syncthreads();
+        // all |x| < 2^e with e from the high parts' largest exponent; clamped so that the scale
+        // factors 2^(8 - e) and 2^(32 - e) below stay normal floats (groups under 2^-94 keep their
+        // absolute error below 2^-134 instead of a relative one)
+        int e = (int)((__float_as_uint(mx) >> 23) & 0xFF) - 126;
+        e = max(e, -94);
+        atomicMax(&eg_s[gl], e + 1000);  // the group's threads agree on the largest exponent
+        __syncthreads();
+        e = eg_s[gl] - 1000;
+        // ---- six 8-bit slices per real, into the core-matrix layout ----
+        {
+            const float sc = pow2f(8 - e), sclo = pow2f(32 - e);
+#pragma unroll
+            for (int part = 0; part < 2; ++part) {  // 0: real parts (k = j), 1: imaginary (k = 32 + j)
+#pragma unroll
+                for (int c8 = 0; c8 < kTcPer / 8; ++c8) {  // cores of 8 consecutive k
+                    uint32_t packed[kTcSlices][4];
+#pragma unroll
+                    for (int i2 = 0; i2 < 4; ++i2) {
+                        float sl[2][kTcSlices];
+#pragma unroll
+                        for (int w = 0; w < 2; ++w) {
+                            const float4 v = a[8 * c8 + 2 * i2 + w];
+                            const float hi = part ? v.y : v.x, lo = part ? v.w : v.z;
+                            float r = hi * sc;
+#pragma unroll
+                            for (int s = 0; s < 3; ++s) {
+                                sl[w][s] = rintf(r);
+                                r = (r - sl[w][s]) * 256.0f;
+                            }
+                            r = fmaf(lo, sclo, r);
+#pragma unroll
+                            for (int s = 3; s < kTcSlices; ++s) {
+                                sl[w][s] = rintf(r);
+                                r = (r - sl[w][s]) * 256.0f;
+                            }
+                        }
+                        // integers of magnitude <= 256: the bf16 value is the float's high half
+#pragma unroll
+                        for (int s = 0; s < kTcSlices; ++s)
+                            packed[s][i2] = (__float_as_uint(sl[0][s]) >> 16) | (__float_as_uint(sl[1][s]) & 0xFFFF0000u);
+                    }
+                    const int k0 = 32 * part + kTcPer * h + 8 * c8;
+#pragma unroll
+                    for (int s = 0; s < kTcSlices; ++s)
+                        *reinterpret_cast<uint4*>(sA + s * kTcSliceBytes + core_off(gl, k0)) =
+                            make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
+                }
+            }
+        }
+        // every thread has read its amplitudes out of sIn: start the next tile's copies
+        if (tile + gridDim.x < ntiles) prefetch(tile + gridDim.x);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // ---- 21 slice products (i + j <= 5) into six accumulators, 4 K-steps each ----
+        if (tid == 0) {
+            for (int d = 0; d < kTcSlices; ++d) {
+                uint32_t acc = 0;
+                for (int i = 0; i <= d; ++i) {
+                    const int j = d - i;
+                    for (int ks = 0; ks < kTcReals / 16; ++ks) {
+                        const uint64_t da = tc_desc(smem_u32(sA + i * kTcSliceBytes) + ks * 256, lbo, sbo);
+                        const uint64_t dw = tc_desc(smem_u32(sW + j * kTcWSliceBytes) + ks * 256, lbo, sbo);
+                        asm volatile(
+                            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
+                                tmem + (uint32_t)(d * kTcReals)),
+                            "l"(da), "l"(dw), "r"(idesc), "r"(acc));
+                        acc = 1;
+                    }
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(&mbar)));
+        }
+        // ---- bounded wait for the products ----
+        uint32_t done = 0;
+        for (long it = 0; it < kTcWaitLimit && !done; ++it)
+            asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                         : "=r"(done)
+                         : "r"(smem_u32(&mbar)), "r"(phase));
+        if (!done) abort_s = 1;
+        __syncthreads();
+        if (abort_s) {
+            // report, then give the products in flight a second bounded wait before the
+            // accumulators are freed
+            if (tid == 0) atomicExch(&g_block_tc_error, 1);
+            done = 0;
+            for (long it = 0; it < kTcWaitLimit && !done; ++it)
+                asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                             : "=r"(done)
+                             : "r"(smem_u32(&mbar)), "r"(phase));
+            break;
+        }
+        phase ^= 1;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // ---- epilogue: warp w reads lanes 32 (w & 3) .. +31 (its groups) and the real and imaginary
+        // columns of amplitudes 8 (w >> 2) .. +7, so that each thread writes whole amplitudes ----
+        {
+            const int row = 32 * (warp & 3) + lane;
+            const int a0 = 8 * (warp >> 2);
+            const int eg = eg_s[row] - 1000;  // stored with the atomicMax offset
+            float4* stage = reinterpret_cast<float4*>(sA);  // [amplitude][group]; the MMAs are done
+            df out[2][8];
+#pragma unroll
+            for (int part = 0; part < 2; ++part) {
+                uint32_t v[kTcSlices][8];
+#pragma unroll
+                for (int d = 0; d < kTcSlices; ++d) {
+                    const uint32_t taddr =
+                        tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(d * kTcReals + 32 * part + a0);
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                                 : "=r"(v[d][0]), "=r"(v[d][1]), "=r"(v[d][2]), "=r"(v[d][3]), "=r"(v[d][4]), "=r"(v[d][5]),
+                                   "=r"(v[d][6]), "=r"(v[d][7])
+                                 : "r"(taddr));
+                }
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    // D_0 + 2^-8 D_1 + 2^-16 D_2 exactly, the rest rounded once (below 2^-46)
+                    const float d0 = __uint_as_float(v[0][c]), d1 = __uint_as_float(v[1][c]) * 0x1p-8f;
+                    const float d2 = __uint_as_float(v[2][c]) * 0x1p-16f;
+                    float t = fmaf(__uint_as_float(v[5][c]), 0x1p-40f, __uint_as_float(v[4][c]) * 0x1p-32f);
+                    t = fmaf(__uint_as_float(v[3][c]), 0x1p-24f, t);
+                    df acc = two_sum(d0, d1);
+                    acc = df_add_f(acc, d2);
+                    acc = fast_two_sum(acc.hi, __fadd_rn(acc.lo, t));
+                    // 2^(e_g + e_r - 16), split in two factors so that each stays a normal float
+                    const int et = eg + er_s[32 * part + a0 + c] - 16;
+                    const int e1 = max(min(et, 100), -100), e2 = max(min(et - e1, 100), -126);
+                    const float f1 = pow2f(e1), f2 = pow2f(e2);
+                    out[part][c] = {acc.hi * f1 * f2, acc.lo * f1 * f2};
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+                stage[(a0 + c) * kTcGroups + row] = make_float4(out[0][c].hi, out[1][c].hi, out[0][c].lo, out[1][c].lo);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        // ---- store ----
+        {
+            const float4* stage = reinterpret_cast<const float4*>(sA);
+#pragma unroll
+            for (int i = 0; i < kTcPer; ++i) psi[base | toff[kTcPer * h + i]] = stage[(kTcPer * h + i) * kTcGroups + gl];
+        }
+        __syncthreads();  // the stage is the next tile's slice area
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");  // no copy left in flight on any exit
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols));
+}
+
+constexpr size_t kTcSmem = (size_t)kTcSlices * (kTcSliceBytes + kTcWSliceBytes) + (size_t)kTcGroups * 32 * sizeof(float4);
+
+}  // namespace
+
+// Host side: the gate's real form in slices (exact in double), in the kernel's layout.
+void block_tc_prepare(const double* m, uint16_t* wslices, int32_t* wexp) {
+    std::memset(wslices, 0, (size_t)kTcSlices * kTcWSliceBytes);
+    for (int r = 0; r < kTcReals; ++r) {
+        double w[kTcReals];
+        const int orow = r & 31, oim = r >> 5;
+        for (int k = 0; k < kTcReals; ++k) {
+            const int col = k & 31, iim = k >> 5;
+            const double re = m[2 * (orow * 32 + col)], im = m[2 * (orow * 32 + col) + 1];
+            // re out: Re M x_re - Im M x_im; im out: Im M x_re + Re M x_im
+            w[k] = oim == 0 ? (iim == 0 ? re : -im) : (iim == 0 ? im : re);
+        }
+        int e = -1000;
+        for (int k = 0; k < kTcReals; ++k)
+            if (w[k] != 0.0) {
+                int ex;
+                std::frexp(w[k], &ex);  // |w| < 2^ex
+                e = std::max(e, ex);
+            }
+        if (e == -1000) e = 0;
+        wexp[r] = e;
+        for (int k = 0; k < kTcReals; ++k) {
+            double v = std::ldexp(w[k], 8 - e);
+            for (int s = 0; s < kTcSlices; ++s) {
+                const double q = std::nearbyint(v);
+                v = (v - q) * 256.0;
+                const float f = (float)q;  // an integer of magnitude <= 256: exact in bf16
+                uint32_t bits;
+                std::memcpy(&bits, &f, 4);
+                const uint32_t off = core_off(r, k);
+                std::memcpy(reinterpret_cast<unsigned char*>(wslices) + (size_t)s * kTcWSliceBytes + off,
+                            reinterpret_cast<const unsigned char*>(&bits) + 2, 2);
+            }
+        }
+    }
+}
+
+size_t block_tc_weight_bytes() { return (size_t)kTcSlices * kTcWSliceBytes + kTcReals * sizeof(int32_t); }
+
+bool block_tc_eligible(int P, int n, int k) { return P == LLG_DF64 && k == 5 && n >= 12; }
+
+cudaError_t launch_block_tc(void* psi, int n, const BlockDesc& bd, const void* d_weights, cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_block_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const uint64_t ntiles = (1ULL << (n - 5)) / kTcGroups;
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned grid = (unsigned)(ntiles < (uint64_t)sms ? ntiles : (uint64_t)sms);
+    const uint16_t* w = static_cast<const uint16_t*>(d_weights);
+    const int32_t* ex = reinterpret_cast<const int32_t*>(static_cast<const unsigned char*>(d_weights) +
+                                                          (size_t)kTcSlices * kTcWSliceBytes);
+    k_block_tc<<<grid, kTcThreads, kTcSmem, s>>>(static_cast<float4*>(psi), n, bd, w, ex);
+    return cudaGetLastError();
+}
+
+// 1 if a tensor-core block kernel timed out waiting for its products since the last call
+int block_tc_take_error() {
+    int h = 0;
+    cudaMemcpyFromSymbol(&h, g_block_tc_error, sizeof(int));
+    if (h) {
+        const int zero = 0;
+        cudaMemcpyToSymbol(g_block_tc_error, &zero, sizeof(int));
+    }
+    return h;
+}
+
+}  // namespace llg

@@ -65,6 +65,10 @@ struct llg_state {
     uint64_t* h_block = nullptr;
     cudaEvent_t block_done = nullptr;
     bool block_pending = false;
+    // tensor-core 5-qubit blocks: sliced matrix (device, pinned staging) and a launch to check
+    void* d_block_tc = nullptr;
+    unsigned char* h_block_tc = nullptr;
+    bool block_tc_launched = false;
     // reductions
     double* d_partials = nullptr;
     double* d_red = nullptr;
@@ -377,6 +381,8 @@ int llg_destroy(llg_state* st) {
     if (st->ops_done) cudaEventDestroy(st->ops_done);
     if (st->d_block) cudaFree(st->d_block);
     if (st->h_block) cudaFreeHost(st->h_block);
+    if (st->d_block_tc) cudaFree(st->d_block_tc);
+    if (st->h_block_tc) cudaFreeHost(st->h_block_tc);
     if (st->block_done) cudaEventDestroy(st->block_done);
     for (auto& r : st->prof_recs) {
         cudaEventDestroy(r.a);
@@ -545,6 +551,22 @@ int llg_apply_matrix(llg_state* st, int k, const int* qubits, const double* m) {
         LLG_CUDA(cudaEventCreateWithFlags(&st->block_done, cudaEventDisableTiming), "cudaEventCreate");
     }
     if (st->block_pending) LLG_CUDA(cudaEventSynchronize(st->block_done), "block staging");
+    if (block_tc_eligible(st->P, st->n, k)) {
+        const size_t wb = block_tc_weight_bytes();
+        if (!st->d_block_tc) {
+            LLG_CUDA(cudaMalloc(&st->d_block_tc, wb), "cudaMalloc(block weights)");
+            LLG_CUDA(cudaHostAlloc((void**)&st->h_block_tc, wb, cudaHostAllocDefault), "cudaHostAlloc(block weights)");
+        }
+        block_tc_prepare(m, reinterpret_cast<uint16_t*>(st->h_block_tc),
+                         reinterpret_cast<int32_t*>(st->h_block_tc + wb - 32 * 2 * sizeof(int32_t)));
+        LLG_CUDA(cudaMemcpyAsync(st->d_block_tc, st->h_block_tc, wb, cudaMemcpyHostToDevice, st->stream),
+                 "cudaMemcpyAsync(block weights)");
+        LLG_CUDA(cudaEventRecord(st->block_done, st->stream), "cudaEventRecord");
+        st->block_pending = true;
+        st->block_tc_launched = true;
+        return traced(st, LLG_PROF_GATE, 1, "block kernel (tensor cores)",
+                      [&] { return launch_block_tc(st->d_psi, st->n, bd, st->d_block_tc, st->stream); });
+    }
     for (int i = 0; i < slots; ++i) st->h_block[i] = pack_coef(st->P, m[i]);
     LLG_CUDA(cudaMemcpyAsync(st->d_block, st->h_block, slots * sizeof(uint64_t), cudaMemcpyHostToDevice, st->stream),
              "cudaMemcpyAsync(block)");
@@ -634,6 +656,11 @@ int llg_sync(llg_state* st) {
     int rc = llg_flush(st);
     if (rc) return rc;
     LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+    if (st->block_tc_launched) {
+        st->block_tc_launched = false;
+        if (block_tc_take_error())
+            return set_error(LLG_ECUDA, "apply_matrix: a tensor-core block kernel timed out waiting for its products");
+    }
     return LLG_OK;
 }
 

@@ -54,6 +54,16 @@ struct BlockDesc {
 };
 cudaError_t launch_block(int P, void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat, cudaStream_t s);
 
+// 5-qubit blocks on double-float states of at least 12 qubits on the tensor cores
+// (llg_block_tc.cu): the host slices the matrix (2 * 32 * 32 doubles, row-major re/im) into
+// block_tc_weight_bytes() of device input; a kernel whose products do not arrive within its
+// wait limit sets a flag that block_tc_take_error() returns (and clears)
+bool block_tc_eligible(int P, int n, int k);
+size_t block_tc_weight_bytes();
+void block_tc_prepare(const double* m, uint16_t* wslices, int32_t* wexp);
+cudaError_t launch_block_tc(void* psi, int n, const BlockDesc& bd, const void* d_weights, cudaStream_t s);
+int block_tc_take_error();
+
 // process-wide tuning cache (llg_tune.cu), keyed by an FNV-1a hash of the workload's shape
 uint64_t tune_hash(uint64_t h, uint64_t v);
 uint64_t tune_hash_ops(uint64_t h, const llg_op* ops, int nops);

@@ -59,6 +59,42 @@ def test_non_unitary_block_and_high_qubits():
     st.close()
 
 
+@pytest.mark.parametrize("n", [12, 14])
+def test_tensor_core_block_edge_values(n):
+    # 5-qubit blocks on double-float states of 12+ qubits run on the tensor cores (exact 8-bit
+    # slices against a scale per group of 32 amplitudes): zero groups, tiny groups, 20 orders of
+    # magnitude inside one group, a non-unitary matrix with large entries and a zero row
+    rng = np.random.default_rng(40 + n)
+    psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    qs = [0, 3, n - 5, n - 2, n - 1]
+    tmask = sum(1 << q for q in qs)
+    free = [i for i in range(1 << n) if i & tmask == 0]
+    offs = [sum(((j >> b) & 1) << q for b, q in enumerate(qs)) for j in range(32)]
+    psi[[free[0] | o for o in offs]] = 0.0                       # an all-zero group
+    psi[[free[1] | o for o in offs]] *= 1e-25                    # a tiny group
+    psi[[free[2] | o for o in offs[1:]]] *= 1e-20                # one large amplitude, the rest tiny
+    psi[free[3] | offs[5]] = 3.0 - 4.0j
+    st = llgpu.State(n)
+    st.load(psi)
+    want = psi.copy()
+    m = (rng.normal(size=(32, 32)) + 1j * rng.normal(size=(32, 32))) * 4.0
+    m[7, :] = 0.0
+    m[:, 9] *= 1e-12
+    st.apply_matrix(qs, m)
+    oracle.apply_matrix(want, n, qs, m)
+    u = rand_unitary(32, rng)
+    st.apply_matrix(qs[::-1], u)
+    oracle.apply_matrix(want, n, qs[::-1], u)
+    got = st.state()
+    # error bound per group: ~2^-46 of the group's largest amplitude times the matrix norm
+    scale = np.max(np.abs(want))
+    assert np.max(np.abs(got - want)) <= 1e-12 * scale
+    assert np.all(got[[free[0] | o for o in offs]] == 0)
+    tiny = np.array([free[1] | o for o in offs])
+    assert np.max(np.abs(got[tiny] - want[tiny])) <= 1e-12 * np.max(np.abs(want[tiny]))
+    st.close()
+
+
 def test_block_contract():
     st = llgpu.State(4)
     eye = np.eye(4)
