@@ -479,7 +479,7 @@ def run_sweep_bench(args, torch):
         # dense k-qubit blocks (llg_apply_matrix): 32 B x 2^n per application and 8 x 4^k x 2^(n-k)
         # real FLOP of complex multiply-adds
         rng = np.random.default_rng(17)
-        for k, qs in ((2, [0, n - 1]), (5, [0, 7, 13, 22, n - 1])):
+        for k, qs in ((2, [0, n - 1]), (4, [0, 11, 20, n - 1]), (5, [0, 7, 13, 22, n - 1])):
             m, _ = np.linalg.qr(rng.normal(size=(1 << k, 1 << k)) + 1j * rng.normal(size=(1 << k, 1 << k)))
             st.apply_matrix(qs, m)  # warm-up
             st.sync()
@@ -779,8 +779,15 @@ def run_e2e(args, ops, xops, n, elem, world, torch):
         view = sv.get_numpy_view()
     _ = float(view[0].real)
     t1 = time.perf_counter()
+    # the host readback alone (nothing pending), to split the step: device passes + readback
+    rb = []
+    for _ in range(2):
+        r0 = time.perf_counter()
+        view = sv.get_numpy_view()
+        rb.append(time.perf_counter() - r0)
     del sv, view
     return {"value": len(ops) * steps * world / (t1 - t0), "unit": "gates/s",
+            "readback_ms": 1e3 * min(rb), "ms_per_step": 1e3 * (t1 - t0) / steps,
             "h2d_bytes_per_step": int(ops.nbytes + xops.nbytes), "d2h_bytes_per_step": int((1 << n) * 16),
             "api": "quantum_sim_v3.StateVector: reset, apply_ops, get_numpy_view (host copy of all amplitudes)"}
 

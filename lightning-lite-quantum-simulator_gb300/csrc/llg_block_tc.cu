@@ -1,26 +1,27 @@
-// llg_block_tc.cu -- dense 5-qubit blocks on complex128 (double-float) states with the fifth-
-// generation tensor cores (tcgen05.mma, accumulators in tensor memory).
+// llg_block_tc.cu -- dense 4- and 5-qubit blocks on complex128 (double-float) states with the
+// fifth-generation tensor cores (tcgen05.mma, accumulators in tensor memory).
 //
-// A 5-qubit block maps every group of 32 amplitudes that differ only in the target qubits through
-// a 32x32 complex matrix.  Written over reals it is one product per tile of 128 groups:
-//     D[g][r] = sum_k X[g][k] W[r][k],   X[g] = (re a_0 .. re a_31, im a_0 .. im a_31),
-// with W the 64x64 real form of the matrix.  Double-float operands (~48-bit significands) are
+// A k-qubit block maps every group of A = 2^k amplitudes that differ only in the target qubits
+// through an A x A complex matrix.  Written over reals it is one product per tile of 128 groups:
+//     D[g][r] = sum_c X[g][c] W[r][c],   X[g] = (re a_0 .. re a_(A-1), im a_0 .. im a_(A-1)),
+// with W the 2A x 2A real form of the matrix (K = N = 64 for k = 5, 32 for k = 4).  Double-float operands (~48-bit significands) are
 // split exactly into six signed 8-bit slices against a power-of-two scale per row (the Ozaki
 // scheme: Ozaki, Ogita, Oishi and Rump, Numer. Algorithms 2012):
 //     X[g][k] = 2^(e_g - 8) sum_i x_i[g][k] 2^(-8 i),   W[r][k] = 2^(e_r - 8) sum_j w_j[r][k] 2^(-8 j),
 // where every slice is an integer of magnitude <= 256, exact in bf16.  The 21 slice products
 // with i + j <= 5 are accumulated by diagonal d = i + j into six fp32 accumulators in tensor
 // memory.  A product of two slices is below 2^16 and 64 of them below 2^22, so each diagonal sum
-// is an integer below 2^24 and the fp32 accumulation is exact.  The epilogue recombines
+// is an integer below 2^24 and the fp32 accumulation is exact (K = 32 leaves a factor 2 spare).  The epilogue recombines
 //     D = 2^(e_g + e_r - 16) sum_d 2^(-8 d) D_d
 // into double-float.  Dropped terms (i + j >= 6) and the final rounding stay near 2^-46 of each
 // group's largest amplitude.
 //
-// One persistent CTA of 512 threads per SM.  Per tile: every thread takes its 8 amplitudes from
+// Persistent CTAs (k = 5: one of 512 threads per SM; k = 4: two of 256).  Per tile: every thread
+// takes its 8 amplitudes from
 // shared memory (copied asynchronously while the previous tile was in the tensor cores), the
 // group scales come from the largest high part, slices go to shared memory in the no-swizzle
-// K-major core-matrix layout, one thread issues the 84 MMAs (M = 128 groups, N = 64, K = 16 per
-// instruction) and commits them to an mbarrier, all threads wait (bounded), read the
+// K-major core-matrix layout, one thread issues the 21 x K/16 MMAs (M = 128 groups, N = 2A, K = 16
+// per instruction) and commits them to an mbarrier, all threads wait (bounded), read the
 // accumulators with tcgen05.ld, recombine and stage the amplitudes in shared memory, and store
 // them.  The gate's slices are prepared on the host in double (exact) and copied to shared
 // memory once per CTA.
@@ -28,6 +29,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -39,15 +41,26 @@ namespace llg {
 
 namespace {
 
-constexpr int kTcThreads = 512;
 constexpr int kTcGroups = 128;            // groups per tile (the MMA's M)
-constexpr int kTcPer = kTcGroups * 32 / kTcThreads;  // amplitudes per thread (8)
-constexpr int kTcReals = 64;              // reals per group (the MMA's K and N)
 constexpr int kTcSlices = 6;              // 8-bit slices per operand
-constexpr int kTcSliceBytes = kTcGroups * kTcReals * 2;   // one state slice, bf16
-constexpr int kTcWSliceBytes = kTcReals * kTcReals * 2;   // one gate slice, bf16
-constexpr int kTcTmemCols = 512;          // six 64-column accumulators, rounded to a power of two
 constexpr long kTcWaitLimit = 1L << 26;   // mbarrier polls before the kernel reports a timeout
+
+// shapes of the k = 4 and k = 5 kernels
+template <int KQ>
+struct TcShape {
+    static constexpr int kAmps = 1 << KQ;                          // amplitudes per group
+    static constexpr int kReals = 2 * kAmps;                       // the MMA's K and N
+    static constexpr int kThreads = KQ == 5 ? 512 : 256;
+    static constexpr int kMinBlocks = KQ == 5 ? 1 : 2;             // CTAs per SM
+    static constexpr int kPer = kTcGroups * kAmps / kThreads;      // amplitudes per thread (8)
+    static constexpr int kSliceBytes = kTcGroups * kReals * 2;     // one state slice, bf16
+    static constexpr int kWSliceBytes = kReals * kReals * 2;       // one gate slice, bf16
+    static constexpr int kTmemCols = KQ == 5 ? 512 : 256;          // six accumulators, power of two
+    static constexpr size_t kSmem =
+        (size_t)kTcSlices * (kSliceBytes + kWSliceBytes) + (size_t)kTcGroups * kAmps * sizeof(float4);
+    static_assert(kPer == 8, "one 8-wide core of real and one of imaginary parts per thread");
+    static_assert(6 * kReals <= kTmemCols, "accumulators fit the allocation");
+};
 
 __device__ int g_block_tc_error = 0;
 
@@ -64,10 +77,10 @@ __device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_
     return d;
 }
 
-// byte offset of element (row, k) of a rows x kTcReals bf16 operand in the core-matrix layout:
-// 8x8 cores of 128 bytes, K-direction cores adjacent, 8-row groups kTcReals / 8 cores apart
-__host__ __device__ __forceinline__ uint32_t core_off(int row, int k) {
-    return (uint32_t)((row >> 3) * (kTcReals / 8) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+// byte offset of element (row, c) of a rows x kreals bf16 operand in the core-matrix layout:
+// 8x8 cores of 128 bytes, K-direction cores adjacent, 8-row groups kreals / 8 cores apart
+__host__ __device__ __forceinline__ uint32_t core_off(int row, int c, int kreals) {
+    return (uint32_t)((row >> 3) * (kreals / 8) * 128 + (c >> 3) * 128 + (row & 7) * 16 + (c & 7) * 2);
 }
 
 // 2^e as a float for e in [-126, 127]
@@ -79,34 +92,37 @@ __device__ __forceinline__ df df_add_f(df a, float b) {
     return fast_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1)
+template <int KQ>
+__global__ void __launch_bounds__(TcShape<KQ>::kThreads, TcShape<KQ>::kMinBlocks)
     k_block_tc(float4* __restrict__ psi, int n, BlockDesc bd, const uint16_t* __restrict__ wslices,
                const int32_t* __restrict__ wexp) {
+    using T = TcShape<KQ>;
+    constexpr int kAmps = T::kAmps, kReals = T::kReals, kPer = T::kPer;
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* sA = smem;                                   // kTcSlices state slices (also the output stage)
-    unsigned char* sW = smem + kTcSlices * kTcSliceBytes;       // kTcSlices gate slices
+    unsigned char* sA = smem;                                  // kTcSlices state slices (also the output stage)
+    unsigned char* sW = smem + kTcSlices * T::kSliceBytes;     // kTcSlices gate slices
     // the next tile's amplitudes, [amplitude][group] so that a warp's 32 groups are 32 consecutive
-    // float4s (a [group][amplitude] layout puts them 512 bytes apart: one bank, 32-way conflicts)
-    float4* sIn = reinterpret_cast<float4*>(sW + kTcSlices * kTcWSliceBytes);
-    __shared__ uint64_t toff[32];
+    // float4s (a [group][amplitude] layout puts them kAmps * 16 bytes apart: 32-way bank conflicts)
+    float4* sIn = reinterpret_cast<float4*>(sW + kTcSlices * T::kWSliceBytes);
+    __shared__ uint64_t toff[kAmps];
     __shared__ int32_t eg_s[kTcGroups];
-    __shared__ int32_t er_s[kTcReals];
+    __shared__ int32_t er_s[kReals];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_s;
     __shared__ int abort_s;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    for (int j = tid; j < 32; j += blockDim.x) {
+    for (int j = tid; j < kAmps; j += blockDim.x) {
         uint64_t o = 0;
-        for (int b = 0; b < 5; ++b)
+        for (int b = 0; b < KQ; ++b)
             if ((j >> b) & 1) o |= 1ULL << bd.q[b];
         toff[j] = o;
     }
-    for (int r = tid; r < kTcReals; r += blockDim.x) er_s[r] = wexp[r];
+    for (int r = tid; r < kReals; r += blockDim.x) er_s[r] = wexp[r];
     {
         const uint4* src = reinterpret_cast<const uint4*>(wslices);
         uint4* dst = reinterpret_cast<uint4*>(sW);
-        for (int i = tid; i < kTcSlices * kTcWSliceBytes / 16; i += blockDim.x) dst[i] = src[i];
+        for (int i = tid; i < kTcSlices * T::kWSliceBytes / 16; i += blockDim.x) dst[i] = src[i];
     }
     if (tid == 0) {
         abort_s = 0;
@@ -115,7 +131,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_s)),
-                     "r"(kTcTmemCols));
+                     "r"(T::kTmemCols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -123,23 +139,23 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_s;
 
-    const uint64_t ngroups = 1ULL << (n - 5);
+    const uint64_t ngroups = 1ULL << (n - KQ);
     const uint64_t ntiles = ngroups / kTcGroups;
-    // instruction descriptor: fp32 accumulate, bf16 A and B, both K-major, N = 64, M = 128
-    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcReals >> 3) << 17) |
+    // instruction descriptor: fp32 accumulate, bf16 A and B, both K-major, N = kReals, M = 128
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kReals >> 3) << 17) |
                            ((uint32_t)(kTcGroups >> 4) << 24);
-    const uint32_t lbo = 128, sbo = (kTcReals / 8) * 128;
+    const uint32_t lbo = 128, sbo = (kReals / 8) * 128;
     const int gl = tid & (kTcGroups - 1);  // the group this thread loads, slices and stores
-    const int h = tid >> 7;                // which kTcPer of its 32 amplitudes
+    const int h = tid >> 7;                // which kPer of its kAmps amplitudes
     uint32_t phase = 0;
-    // a thread's amplitudes of a tile go to sIn[(kTcPer h + i) * 128 + gl] by asynchronous copies,
+    // a thread's amplitudes of a tile go to sIn[(kPer h + i) * 128 + gl] by asynchronous copies,
     // issued one tile ahead so that their latency hides behind the products and the epilogue
     auto prefetch = [&](uint64_t tile) {
         const uint64_t b = insert0_mask(tile * kTcGroups + (uint64_t)gl, bd.tmask);
 #pragma unroll
-        for (int i = 0; i < kTcPer; ++i)
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(&sIn[(kTcPer * h + i) * kTcGroups + gl])),
-                         "l"(psi + (b | toff[kTcPer * h + i]))
+        for (int i = 0; i < kPer; ++i)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(&sIn[(kPer * h + i) * kTcGroups + gl])),
+                         "l"(psi + (b | toff[kPer * h + i]))
                          : "memory");
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
@@ -151,11 +167,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const uint64_t g = tile * kTcGroups + (uint64_t)gl;
         const uint64_t base = insert0_mask(g, bd.tmask);
         asm volatile("cp.async.wait_group 0;" ::: "memory");
-        float4 a[kTcPer];
+        float4 a[kPer];
         float mx = 0.0f;
 #pragma unroll
-        for (int i = 0; i < kTcPer; ++i) {
-            a[i] = sIn[(kTcPer * h + i) * kTcGroups + gl];
+        for (int i = 0; i < kPer; ++i) {
+            a[i] = sIn[(kPer * h + i) * kTcGroups + gl];
             mx = fmaxf(mx, fmaxf(fabsf(a[i].x), fabsf(a[i].y)));
         }
         if (h == 0) eg_s[gl] = 0;
@@ -172,41 +188,38 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         {
             const float sc = pow2f(8 - e), sclo = pow2f(32 - e);
 #pragma unroll
-            for (int part = 0; part < 2; ++part) {  // 0: real parts (k = j), 1: imaginary (k = 32 + j)
+            for (int part = 0; part < 2; ++part) {  // 0: real parts (c = j), 1: imaginary (c = kAmps + j)
+                uint32_t packed[kTcSlices][4];
 #pragma unroll
-                for (int c8 = 0; c8 < kTcPer / 8; ++c8) {  // cores of 8 consecutive k
-                    uint32_t packed[kTcSlices][4];
+                for (int i2 = 0; i2 < 4; ++i2) {
+                    float sl[2][kTcSlices];
 #pragma unroll
-                    for (int i2 = 0; i2 < 4; ++i2) {
-                        float sl[2][kTcSlices];
+                    for (int w = 0; w < 2; ++w) {
+                        const float4 v = a[2 * i2 + w];
+                        const float hi = part ? v.y : v.x, lo = part ? v.w : v.z;
+                        float r = hi * sc;
 #pragma unroll
-                        for (int w = 0; w < 2; ++w) {
-                            const float4 v = a[8 * c8 + 2 * i2 + w];
-                            const float hi = part ? v.y : v.x, lo = part ? v.w : v.z;
-                            float r = hi * sc;
-#pragma unroll
-                            for (int s = 0; s < 3; ++s) {
-                                sl[w][s] = rintf(r);
-                                r = (r - sl[w][s]) * 256.0f;
-                            }
-                            r = fmaf(lo, sclo, r);
-#pragma unroll
-                            for (int s = 3; s < kTcSlices; ++s) {
-                                sl[w][s] = rintf(r);
-                                r = (r - sl[w][s]) * 256.0f;
-                            }
+                        for (int s = 0; s < 3; ++s) {
+                            sl[w][s] = rintf(r);
+                            r = (r - sl[w][s]) * 256.0f;
                         }
-                        // integers of magnitude <= 256: the bf16 value is the float's high half
+                        r = fmaf(lo, sclo, r);
 #pragma unroll
-                        for (int s = 0; s < kTcSlices; ++s)
-                            packed[s][i2] = (__float_as_uint(sl[0][s]) >> 16) | (__float_as_uint(sl[1][s]) & 0xFFFF0000u);
+                        for (int s = 3; s < kTcSlices; ++s) {
+                            sl[w][s] = rintf(r);
+                            r = (r - sl[w][s]) * 256.0f;
+                        }
                     }
-                    const int k0 = 32 * part + kTcPer * h + 8 * c8;
+                    // integers of magnitude <= 256: the bf16 value is the float's high half
 #pragma unroll
                     for (int s = 0; s < kTcSlices; ++s)
-                        *reinterpret_cast<uint4*>(sA + s * kTcSliceBytes + core_off(gl, k0)) =
-                            make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
+                        packed[s][i2] = (__float_as_uint(sl[0][s]) >> 16) | (__float_as_uint(sl[1][s]) & 0xFFFF0000u);
                 }
+                const int c0 = kAmps * part + kPer * h;
+#pragma unroll
+                for (int s = 0; s < kTcSlices; ++s)
+                    *reinterpret_cast<uint4*>(sA + s * T::kSliceBytes + core_off(gl, c0, kReals)) =
+                        make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
             }
         }
         // every thread has read its amplitudes out of sIn: start the next tile's copies
@@ -215,18 +228,18 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // ---- 21 slice products (i + j <= 5) into six accumulators, 4 K-steps each ----
+        // ---- 21 slice products (i + j <= 5) into six accumulators, K / 16 steps each ----
         if (tid == 0) {
             for (int d = 0; d < kTcSlices; ++d) {
                 uint32_t acc = 0;
                 for (int i = 0; i <= d; ++i) {
                     const int j = d - i;
-                    for (int ks = 0; ks < kTcReals / 16; ++ks) {
-                        const uint64_t da = tc_desc(smem_u32(sA + i * kTcSliceBytes) + ks * 256, lbo, sbo);
-                        const uint64_t dw = tc_desc(smem_u32(sW + j * kTcWSliceBytes) + ks * 256, lbo, sbo);
+                    for (int ks = 0; ks < kReals / 16; ++ks) {
+                        const uint64_t da = tc_desc(smem_u32(sA + i * T::kSliceBytes) + ks * 256, lbo, sbo);
+                        const uint64_t dw = tc_desc(smem_u32(sW + j * T::kWSliceBytes) + ks * 256, lbo, sbo);
                         asm volatile(
                             "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
-                                tmem + (uint32_t)(d * kTcReals)),
+                                tmem + (uint32_t)(d * kReals)),
                             "l"(da), "l"(dw), "r"(idesc), "r"(acc));
                         acc = 1;
                     }
@@ -269,7 +282,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
                 for (int d = 0; d < kTcSlices; ++d) {
                     const uint32_t taddr =
-                        tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(d * kTcReals + 32 * part + a0);
+                        tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(d * kReals + kAmps * part + a0);
                     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                                  : "=r"(v[d][0]), "=r"(v[d][1]), "=r"(v[d][2]), "=r"(v[d][3]), "=r"(v[d][4]), "=r"(v[d][5]),
                                    "=r"(v[d][6]), "=r"(v[d][7])
@@ -287,7 +300,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     acc = df_add_f(acc, d2);
                     acc = fast_two_sum(acc.hi, __fadd_rn(acc.lo, t));
                     // 2^(e_g + e_r - 16), split in two factors so that each stays a normal float
-                    const int et = eg + er_s[32 * part + a0 + c] - 16;
+                    const int et = eg + er_s[kAmps * part + a0 + c] - 16;
                     const int e1 = max(min(et, 100), -100), e2 = max(min(et - e1, 100), -126);
                     const float f1 = pow2f(e1), f2 = pow2f(e2);
                     out[part][c] = {acc.hi * f1 * f2, acc.lo * f1 * f2};
@@ -303,7 +316,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         {
             const float4* stage = reinterpret_cast<const float4*>(sA);
 #pragma unroll
-            for (int i = 0; i < kTcPer; ++i) psi[base | toff[kTcPer * h + i]] = stage[(kTcPer * h + i) * kTcGroups + gl];
+            for (int i = 0; i < kPer; ++i) psi[base | toff[kPer * h + i]] = stage[(kPer * h + i) * kTcGroups + gl];
         }
         __syncthreads();  // the stage is the next tile's slice area
     }
@@ -311,71 +324,82 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols));
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(T::kTmemCols));
 }
 
-constexpr size_t kTcSmem = (size_t)kTcSlices * (kTcSliceBytes + kTcWSliceBytes) + (size_t)kTcGroups * 32 * sizeof(float4);
+template <int KQ>
+cudaError_t launch_tc(void* psi, int n, const BlockDesc& bd, const void* d_weights, cudaStream_t s) {
+    using T = TcShape<KQ>;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_block_tc<KQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::kSmem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const uint64_t ntiles = (1ULL << (n - KQ)) / kTcGroups;
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint64_t cap = (uint64_t)sms * T::kMinBlocks;
+    const unsigned grid = (unsigned)(ntiles < cap ? ntiles : cap);
+    const uint16_t* w = static_cast<const uint16_t*>(d_weights);
+    const int32_t* ex = reinterpret_cast<const int32_t*>(static_cast<const unsigned char*>(d_weights) +
+                                                          (size_t)kTcSlices * T::kWSliceBytes);
+    k_block_tc<KQ><<<grid, T::kThreads, T::kSmem, s>>>(static_cast<float4*>(psi), n, bd, w, ex);
+    return cudaGetLastError();
+}
 
 }  // namespace
 
-// Host side: the gate's real form in slices (exact in double), in the kernel's layout.
-void block_tc_prepare(const double* m, uint16_t* wslices, int32_t* wexp) {
-    std::memset(wslices, 0, (size_t)kTcSlices * kTcWSliceBytes);
-    for (int r = 0; r < kTcReals; ++r) {
-        double w[kTcReals];
-        const int orow = r & 31, oim = r >> 5;
-        for (int k = 0; k < kTcReals; ++k) {
-            const int col = k & 31, iim = k >> 5;
-            const double re = m[2 * (orow * 32 + col)], im = m[2 * (orow * 32 + col) + 1];
+// Host side: the gate's real form in slices (exact in double), in the kernel's layout:
+// kTcSlices slices of 2A x 2A bf16, then 2A row exponents.
+void block_tc_prepare(int k, const double* m, void* weights) {
+    const int amps = 1 << k, reals = 2 * amps;
+    const size_t wslice = (size_t)reals * reals * 2;
+    unsigned char* out = static_cast<unsigned char*>(weights);
+    int32_t* wexp = reinterpret_cast<int32_t*>(out + kTcSlices * wslice);
+    std::memset(out, 0, kTcSlices * wslice);
+    std::vector<double> w(reals);
+    for (int r = 0; r < reals; ++r) {
+        const int orow = r & (amps - 1), oim = r >> k;
+        for (int c = 0; c < reals; ++c) {
+            const int col = c & (amps - 1), iim = c >> k;
+            const double re = m[2 * (orow * amps + col)], im = m[2 * (orow * amps + col) + 1];
             // re out: Re M x_re - Im M x_im; im out: Im M x_re + Re M x_im
-            w[k] = oim == 0 ? (iim == 0 ? re : -im) : (iim == 0 ? im : re);
+            w[c] = oim == 0 ? (iim == 0 ? re : -im) : (iim == 0 ? im : re);
         }
         int e = -1000;
-        for (int k = 0; k < kTcReals; ++k)
-            if (w[k] != 0.0) {
+        for (int c = 0; c < reals; ++c)
+            if (w[c] != 0.0) {
                 int ex;
-                std::frexp(w[k], &ex);  // |w| < 2^ex
+                std::frexp(w[c], &ex);  // |w| < 2^ex
                 e = std::max(e, ex);
             }
         if (e == -1000) e = 0;
         wexp[r] = e;
-        for (int k = 0; k < kTcReals; ++k) {
-            double v = std::ldexp(w[k], 8 - e);
+        for (int c = 0; c < reals; ++c) {
+            double v = std::ldexp(w[c], 8 - e);
             for (int s = 0; s < kTcSlices; ++s) {
                 const double q = std::nearbyint(v);
                 v = (v - q) * 256.0;
                 const float f = (float)q;  // an integer of magnitude <= 256: exact in bf16
                 uint32_t bits;
                 std::memcpy(&bits, &f, 4);
-                const uint32_t off = core_off(r, k);
-                std::memcpy(reinterpret_cast<unsigned char*>(wslices) + (size_t)s * kTcWSliceBytes + off,
-                            reinterpret_cast<const unsigned char*>(&bits) + 2, 2);
+                std::memcpy(out + s * wslice + core_off(r, c, reals), reinterpret_cast<const unsigned char*>(&bits) + 2, 2);
             }
         }
     }
 }
 
-size_t block_tc_weight_bytes() { return (size_t)kTcSlices * kTcWSliceBytes + kTcReals * sizeof(int32_t); }
+size_t block_tc_weight_bytes(int k) {
+    const size_t reals = (size_t)2 << k;
+    return kTcSlices * reals * reals * 2 + reals * sizeof(int32_t);
+}
 
-bool block_tc_eligible(int P, int n, int k) { return P == LLG_DF64 && k == 5 && n >= 12; }
+bool block_tc_eligible(int P, int n, int k) { return P == LLG_DF64 && (k == 4 || k == 5) && n >= k + 7; }
 
 cudaError_t launch_block_tc(void* psi, int n, const BlockDesc& bd, const void* d_weights, cudaStream_t s) {
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_block_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
-    const uint64_t ntiles = (1ULL << (n - 5)) / kTcGroups;
-    int sms = 0, dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const unsigned grid = (unsigned)(ntiles < (uint64_t)sms ? ntiles : (uint64_t)sms);
-    const uint16_t* w = static_cast<const uint16_t*>(d_weights);
-    const int32_t* ex = reinterpret_cast<const int32_t*>(static_cast<const unsigned char*>(d_weights) +
-                                                          (size_t)kTcSlices * kTcWSliceBytes);
-    k_block_tc<<<grid, kTcThreads, kTcSmem, s>>>(static_cast<float4*>(psi), n, bd, w, ex);
-    return cudaGetLastError();
+    return bd.k == 5 ? launch_tc<5>(psi, n, bd, d_weights, s) : launch_tc<4>(psi, n, bd, d_weights, s);
 }
 
 // 1 if a tensor-core block kernel timed out waiting for its products since the last call

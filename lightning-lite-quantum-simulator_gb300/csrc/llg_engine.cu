@@ -552,13 +552,13 @@ int llg_apply_matrix(llg_state* st, int k, const int* qubits, const double* m) {
     }
     if (st->block_pending) LLG_CUDA(cudaEventSynchronize(st->block_done), "block staging");
     if (block_tc_eligible(st->P, st->n, k)) {
-        const size_t wb = block_tc_weight_bytes();
+        const size_t wb = block_tc_weight_bytes(k);
         if (!st->d_block_tc) {
-            LLG_CUDA(cudaMalloc(&st->d_block_tc, wb), "cudaMalloc(block weights)");
-            LLG_CUDA(cudaHostAlloc((void**)&st->h_block_tc, wb, cudaHostAllocDefault), "cudaHostAlloc(block weights)");
+            const size_t cap = block_tc_weight_bytes(kMaxBlockQubits);
+            LLG_CUDA(cudaMalloc(&st->d_block_tc, cap), "cudaMalloc(block weights)");
+            LLG_CUDA(cudaHostAlloc((void**)&st->h_block_tc, cap, cudaHostAllocDefault), "cudaHostAlloc(block weights)");
         }
-        block_tc_prepare(m, reinterpret_cast<uint16_t*>(st->h_block_tc),
-                         reinterpret_cast<int32_t*>(st->h_block_tc + wb - 32 * 2 * sizeof(int32_t)));
+        block_tc_prepare(k, m, st->h_block_tc);
         LLG_CUDA(cudaMemcpyAsync(st->d_block_tc, st->h_block_tc, wb, cudaMemcpyHostToDevice, st->stream),
                  "cudaMemcpyAsync(block weights)");
         LLG_CUDA(cudaEventRecord(st->block_done, st->stream), "cudaEventRecord");

@@ -54,13 +54,13 @@ struct BlockDesc {
 };
 cudaError_t launch_block(int P, void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat, cudaStream_t s);
 
-// 5-qubit blocks on double-float states of at least 12 qubits on the tensor cores
-// (llg_block_tc.cu): the host slices the matrix (2 * 32 * 32 doubles, row-major re/im) into
-// block_tc_weight_bytes() of device input; a kernel whose products do not arrive within its
+// 4- and 5-qubit blocks on double-float states of at least k + 7 qubits on the tensor cores
+// (llg_block_tc.cu): the host slices the matrix (2 * 4^k doubles, row-major re/im) into
+// block_tc_weight_bytes(k) of device input; a kernel whose products do not arrive within its
 // wait limit sets a flag that block_tc_take_error() returns (and clears)
 bool block_tc_eligible(int P, int n, int k);
-size_t block_tc_weight_bytes();
-void block_tc_prepare(const double* m, uint16_t* wslices, int32_t* wexp);
+size_t block_tc_weight_bytes(int k);
+void block_tc_prepare(int k, const double* m, void* weights);
 cudaError_t launch_block_tc(void* psi, int n, const BlockDesc& bd, const void* d_weights, cudaStream_t s);
 int block_tc_take_error();
 

@@ -59,17 +59,18 @@ def test_non_unitary_block_and_high_qubits():
     st.close()
 
 
-@pytest.mark.parametrize("n", [12, 14])
-def test_tensor_core_block_edge_values(n):
-    # 5-qubit blocks on double-float states of 12+ qubits run on the tensor cores (exact 8-bit
-    # slices against a scale per group of 32 amplitudes): zero groups, tiny groups, 20 orders of
-    # magnitude inside one group, a non-unitary matrix with large entries and a zero row
-    rng = np.random.default_rng(40 + n)
+@pytest.mark.parametrize("n,k", [(12, 5), (14, 5), (11, 4), (13, 4)])
+def test_tensor_core_block_edge_values(n, k):
+    # 4- and 5-qubit blocks on double-float states of k + 7 or more qubits run on the tensor cores
+    # (exact 8-bit slices against a scale per group of 2^k amplitudes): zero groups, tiny groups,
+    # 20 orders of magnitude inside one group, a non-unitary matrix with large entries and a zero row
+    rng = np.random.default_rng(40 + n + k)
     psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
-    qs = [0, 3, n - 5, n - 2, n - 1]
+    qs = [0, 3, n - 5, n - 2, n - 1][5 - k:]
+    d = 1 << k
     tmask = sum(1 << q for q in qs)
     free = [i for i in range(1 << n) if i & tmask == 0]
-    offs = [sum(((j >> b) & 1) << q for b, q in enumerate(qs)) for j in range(32)]
+    offs = [sum(((j >> b) & 1) << q for b, q in enumerate(qs)) for j in range(d)]
     psi[[free[0] | o for o in offs]] = 0.0                       # an all-zero group
     psi[[free[1] | o for o in offs]] *= 1e-25                    # a tiny group
     psi[[free[2] | o for o in offs[1:]]] *= 1e-20                # one large amplitude, the rest tiny
@@ -77,12 +78,12 @@ def test_tensor_core_block_edge_values(n):
     st = llgpu.State(n)
     st.load(psi)
     want = psi.copy()
-    m = (rng.normal(size=(32, 32)) + 1j * rng.normal(size=(32, 32))) * 4.0
+    m = (rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))) * 4.0
     m[7, :] = 0.0
     m[:, 9] *= 1e-12
     st.apply_matrix(qs, m)
     oracle.apply_matrix(want, n, qs, m)
-    u = rand_unitary(32, rng)
+    u = rand_unitary(d, rng)
     st.apply_matrix(qs[::-1], u)
     oracle.apply_matrix(want, n, qs[::-1], u)
     got = st.state()
