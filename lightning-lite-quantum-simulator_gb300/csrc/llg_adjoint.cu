@@ -88,35 +88,81 @@ __global__ void k_coef_table(const double* __restrict__ params, int nparams, con
     table[2 * (size_t)idx + 1] = pack_dev<P>(s);
 }
 
-// Im <lambda | P | psi> over the tile for the generator P of a parametrised op, this thread's part
-// as an accumulator (double-float for the FP32-pipe precisions; summed over the block once).
+// One gradient op fused: this thread's part of Im <lambda | P | psi> from the amplitudes before the
+// op, and the op's inverse applied to both tiles in the same loop (each pair or amplitude belongs
+// to one thread, so it reads its values before it overwrites them).  The caller's block sum
+// provides the barrier before the next op.
 template <class P>
-__device__ typename P::Acc tile_generator_inner(const typename P::S* psi, const typename P::S* lam, uint32_t tsize,
-                                                uint64_t base, const ExecOp& o) {
+__device__ typename P::Acc tile_grad_apply(typename P::S* psi, typename P::S* lam, uint32_t tsize, uint64_t base,
+                                           const ExecOp& o, const uint64_t* __restrict__ trow) {
+    using K = typename P::K;
+    using C = typename P::C;
     typename P::Acc pos = P::acc_zero(), neg = P::acc_zero();
-    if (o.kind == EX_RZ_P) {
+    const K c0 = P::k_from_bits(trow[2 * o.q1]);
+    K s0 = P::k_from_bits(trow[2 * o.q1 + 1]);
+    if (o.flags & OPF_ADJOINT) s0 = P::kneg(s0);
+    if (o.kind == EX_RZ_P) {  // generator Z; the op is diag(1, e^{i t}) (table row cos t, sin t)
+        const K ms0 = P::kneg(s0);
         if (o.flags & OPF_NONLOCAL_Q0) {
-            for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x)
-                pos = P::acc_dot_im(pos, P::load(lam[l]), P::load(psi[l]));
-            return ((base >> o.q0) & 1) ? acc_minus(P::acc_zero(), pos) : pos;
+            const bool one = (base >> o.q0) & 1;
+            for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
+                C p = P::load(psi[l]), q = P::load(lam[l]);
+                pos = P::acc_dot_im(pos, q, p);
+                if (one) {
+                    cmul_const<P>(p, c0, s0, ms0);
+                    cmul_const<P>(q, c0, s0, ms0);
+                    psi[l] = P::store(p);
+                    lam[l] = P::store(q);
+                }
+            }
+            return one ? acc_minus(P::acc_zero(), pos) : pos;
         }
-        for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
-            if ((l >> o.q0) & 1) neg = P::acc_dot_im(neg, P::load(lam[l]), P::load(psi[l]));
-            else pos = P::acc_dot_im(pos, P::load(lam[l]), P::load(psi[l]));
+        const uint32_t bit = 1u << o.q0;
+        for (uint32_t pp = threadIdx.x; pp < (tsize >> 1); pp += blockDim.x) {
+            const uint32_t j0 = ins0(pp, bit), j1 = j0 | bit;
+            const C p0 = P::load(psi[j0]), q0 = P::load(lam[j0]);
+            C p1 = P::load(psi[j1]), q1 = P::load(lam[j1]);
+            pos = P::acc_dot_im(pos, q0, p0);
+            neg = P::acc_dot_im(neg, q1, p1);
+            cmul_const<P>(p1, c0, s0, ms0);
+            cmul_const<P>(q1, c0, s0, ms0);
+            psi[j1] = P::store(p1);
+            lam[j1] = P::store(q1);
         }
         return acc_minus(pos, neg);
     }
+    ExecOp r = o;  // RX / RY with the (possibly negated) sine of the table row
+    r.c[0] = trow[2 * o.q1];
     const uint32_t bit = 1u << o.q0;
-    for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += blockDim.x) {
-        const uint32_t j0 = ins0(p, bit), j1 = j0 | bit;
-        const auto p0 = P::load(psi[j0]), p1 = P::load(psi[j1]);
-        const auto l0 = P::load(lam[j0]), l1 = P::load(lam[j1]);
-        if (o.kind == EX_RY_P) {  // Y: Re(conj(l1) p0) - Re(conj(l0) p1)
-            pos = P::acc_dot_re(pos, l1, p0);
-            neg = P::acc_dot_re(neg, l0, p1);
-        } else {  // X: Im(conj(l0) p1) + Im(conj(l1) p0)
-            pos = P::acc_dot_im(pos, l0, p1);
-            pos = P::acc_dot_im(pos, l1, p0);
+    if (o.kind == EX_RY_P) {
+        PairMath<P, EX_RY> m(r);
+        m.k[1] = s0;
+        for (uint32_t pp = threadIdx.x; pp < (tsize >> 1); pp += blockDim.x) {
+            const uint32_t j0 = ins0(pp, bit), j1 = j0 | bit;
+            C p0 = P::load(psi[j0]), p1 = P::load(psi[j1]), q0 = P::load(lam[j0]), q1 = P::load(lam[j1]);
+            pos = P::acc_dot_re(pos, q1, p0);  // Y: Re(conj(l1) p0) - Re(conj(l0) p1)
+            neg = P::acc_dot_re(neg, q0, p1);
+            m.apply(p0, p1);
+            m.apply(q0, q1);
+            psi[j0] = P::store(p0);
+            psi[j1] = P::store(p1);
+            lam[j0] = P::store(q0);
+            lam[j1] = P::store(q1);
+        }
+    } else {
+        PairMath<P, EX_RX> m(r);
+        m.k[1] = s0;
+        for (uint32_t pp = threadIdx.x; pp < (tsize >> 1); pp += blockDim.x) {
+            const uint32_t j0 = ins0(pp, bit), j1 = j0 | bit;
+            C p0 = P::load(psi[j0]), p1 = P::load(psi[j1]), q0 = P::load(lam[j0]), q1 = P::load(lam[j1]);
+            pos = P::acc_dot_im(pos, q0, p1);  // X: Im(conj(l0) p1) + Im(conj(l1) p0)
+            pos = P::acc_dot_im(pos, q1, p0);
+            m.apply(p0, p1);
+            m.apply(q0, q1);
+            psi[j0] = P::store(p0);
+            psi[j1] = P::store(p1);
+            lam[j0] = P::store(q0);
+            lam[j1] = P::store(q1);
         }
     }
     return acc_minus(pos, neg);
@@ -202,9 +248,13 @@ __global__ void __launch_bounds__(512, 2) k_tile_bwd(typename P::S* __restrict__
         }
         const ExecOp& o = sops[k % kAdjOpChunk];
         if (o.flags & OPF_GRAD) {
-            const auto v = block_sum_acc(tile_generator_inner<P>(tp, tl, tsize, base, o), red);
-            if (threadIdx.x == 0) gpart[((size_t)b * nocc + o.q1) * tiles + blockIdx.x] = acc_value(v);
-            __syncthreads();
+            // inner product and un-application in one loop; the block sum's barriers order the
+            // tile writes before the next op.  The slot is read before them: once they are passed,
+            // the next chunk may be staged over this op's record.
+            const int slot = o.q1;
+            const auto v = block_sum_acc(tile_grad_apply<P>(tp, tl, tsize, base, o, trow), red);
+            if (threadIdx.x == 0) gpart[((size_t)b * nocc + slot) * tiles + blockIdx.x] = acc_value(v);
+            continue;
         }
         tile_apply<P>(tp, tsize, base, o, trow);
         tile_apply<P>(tl, tsize, base, o, trow);
