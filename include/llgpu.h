@@ -198,6 +198,11 @@ int llg_probabilities(llg_state* st, double* out);
 
 /* sum_i |a_i|^2 (FP64 result). */
 int llg_norm2(llg_state* st, double* out);
+/* Two states of the same qubit count, any precisions, compared on the device in double:
+ * fidelity |<a|b>|^2 / (<a|a><b|b>) and max over i of |Re(a_i - b_i)|, |Im(a_i - b_i)| (either
+ * output may be NULL).  No reference counterpart: a check for parity tests at sizes whose host
+ * copies would be too large. */
+int llg_compare(llg_state* a, llg_state* b, double* fidelity, double* max_abs_diff);
 
 /* sum_k coeff_k <Z_{a_k} Z_{b_k}>; b_k < 0 selects the single-qubit term <Z_{a_k}>.  The
  * diagonal of python/algorithms.py:141-153 (ising_diagonal) evaluated on the fly. */

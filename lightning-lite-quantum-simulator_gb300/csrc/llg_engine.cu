@@ -778,6 +778,33 @@ static int reduce(llg_state* st, const ZTerms& z, double* slots) {
     return LLG_OK;
 }
 
+int llg_compare(llg_state* a, llg_state* b, double* fidelity, double* max_abs_diff) {
+    if (!a || !b) return set_error(LLG_EINVAL, "compare: NULL state");
+    if (a->n != b->n) return set_error(LLG_EINVAL, "compare: the states have different qubit counts");
+    int rc = llg_flush(a);
+    if (!rc) rc = llg_flush(b);
+    if (rc) return rc;
+    if ((rc = ensure_device_buffers(a))) return rc;  // the partial-sum buffer
+    LLG_CUDA(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+    int nblocks = 0;
+    LLG_CUDA(launch_compare(a->P, a->d_psi, b->P, b->d_psi, a->size, a->d_partials, &nblocks, a->stream), "compare kernel");
+    std::vector<double> part((size_t)nblocks * kRedSlots);
+    LLG_CUDA(cudaMemcpyAsync(part.data(), a->d_partials, part.size() * sizeof(double), cudaMemcpyDeviceToHost, a->stream),
+             "cudaMemcpyAsync(D2H)");
+    LLG_CUDA(cudaStreamSynchronize(a->stream), "cudaStreamSynchronize");
+    double re = 0.0, im = 0.0, na = 0.0, nb = 0.0, mx = 0.0;
+    for (int k = 0; k < nblocks; ++k) {  // fixed order
+        re += part[(size_t)k * kRedSlots];
+        im += part[(size_t)k * kRedSlots + 1];
+        na += part[(size_t)k * kRedSlots + 2];
+        nb += part[(size_t)k * kRedSlots + 3];
+        mx = std::max(mx, part[(size_t)k * kRedSlots + 4]);
+    }
+    if (fidelity) *fidelity = (na > 0.0 && nb > 0.0) ? (re * re + im * im) / (na * nb) : 0.0;
+    if (max_abs_diff) *max_abs_diff = mx;
+    return LLG_OK;
+}
+
 int llg_norm2(llg_state* st, double* out) {
     if (!st || !out) return set_error(LLG_EINVAL, "norm2: NULL argument");
     ZTerms z;

@@ -329,6 +329,44 @@ __global__ void __launch_bounds__(kThreads) k_reduce_z(const typename P::S* __re
     }
 }
 
+__device__ __forceinline__ double block_max(double v, double* sh) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, off));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, sh[w]);
+    return r;
+}
+
+// Two states of any precisions, in double: per block [Re <a|b>, Im <a|b>, <a|a>, <b|b>, max |a_i - b_i|]
+template <class PA, class PB>
+__global__ void __launch_bounds__(kThreads) k_compare(const typename PA::S* __restrict__ a, const typename PB::S* __restrict__ b,
+                                                      uint64_t size, double* __restrict__ partials) {
+    __shared__ double sh[kThreads / 32];
+    double re = 0.0, im = 0.0, na = 0.0, nb = 0.0, mx = 0.0;
+    const uint64_t step = (uint64_t)gridDim.x * kThreads;
+    for (uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x; i < size; i += step) {
+        const double2 x = PA::to_f64(PA::load(a[i])), y = PB::to_f64(PB::load(b[i]));
+        re = fma(x.x, y.x, fma(x.y, y.y, re));
+        im = fma(x.x, y.y, fma(-x.y, y.x, im));
+        na = fma(x.x, x.x, fma(x.y, x.y, na));
+        nb = fma(y.x, y.x, fma(y.y, y.y, nb));
+        mx = fmax(mx, fmax(fabs(x.x - y.x), fabs(x.y - y.y)));
+    }
+    const double v[4] = {re, im, na, nb};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const double t = block_sum(v[k], sh);
+        if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kRedSlots + k] = t;
+    }
+    const double m = block_max(mx, sh);
+    if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kRedSlots + 4] = m;
+}
+
 __global__ void k_finish(const double* __restrict__ partials, int nblocks, double* __restrict__ out) {
     // one thread per slot, fixed order: deterministic
     const int s = threadIdx.x;
@@ -426,6 +464,20 @@ cudaError_t launch_exec_op(int P, void* psi, int n, const ExecOp& op, cudaStream
 
 cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, int threads, cudaStream_t s) {
     LLG_DISPATCH(P, return tile_pass_t<Pol>(psi, n, pd, d_ops, threads, s));
+}
+
+template <class PA>
+cudaError_t compare_a(int PB, const void* a, const void* b, uint64_t size, double* partials, cudaStream_t s) {
+    const unsigned grid = (unsigned)std::min<uint64_t>(kRedBlocks, (size + kThreads - 1) / kThreads);
+    LLG_DISPATCH(PB, k_compare<PA, Pol><<<grid, kThreads, 0, s>>>(static_cast<const typename PA::S*>(a),
+                                                                    static_cast<const typename Pol::S*>(b), size, partials);
+                 return cudaGetLastError());
+}
+
+cudaError_t launch_compare(int PA, const void* a, int PB, const void* b, uint64_t size, double* partials, int* nblocks,
+                           cudaStream_t s) {
+    *nblocks = (int)std::min<uint64_t>(kRedBlocks, (size + kThreads - 1) / kThreads);
+    LLG_DISPATCH(PA, return compare_a<Pol>(PB, a, b, size, partials, s));
 }
 
 cudaError_t launch_from_f64(int P, const double* src, void* dst, uint64_t count, cudaStream_t s) {

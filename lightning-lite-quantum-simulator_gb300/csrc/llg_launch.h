@@ -41,6 +41,11 @@ cudaError_t launch_scale(int P, void* psi, uint64_t count, double factor, cudaSt
 cudaError_t launch_reduce_z(int P, const void* psi, int n, const ZTerms& terms, double* d_partials, double* d_out,
                             cudaStream_t s);
 
+// Two states of equal size, any precisions: per block (kRedSlots doubles each) Re <a|b>, Im <a|b>,
+// <a|a>, <b|b> and max |a_i - b_i| (re and im parts); *nblocks = blocks written
+cudaError_t launch_compare(int PA, const void* a, int PB, const void* b, uint64_t size, double* partials, int* nblocks,
+                           cudaStream_t s);
+
 int tile_max_qubits(int P);
 
 // dense k-qubit block (llg_block.cu): bit j of a row/column index is qubit q[j]; the matrix is

@@ -130,6 +130,7 @@ def lib() -> ctypes.CDLL:
             "llg_batch_autotune": (i, [i, vp, vp, vp, i, vp]),
             "llg_batch_config": (i, [vp, P(i), P(i), P(i)]),
             "llg_set_tile_threads": (i, [vp, i]),
+            "llg_compare": (i, [vp, vp, P(d), P(d)]),
             "llg_get_tuning": (i, [vp, P(i), P(i), P(i)]),
             "llg_autotune": (i, [vp, vp, i, i, vp]),
             "llg_tune_cache_clear": (None, []),
@@ -332,6 +333,13 @@ class State:
         v = ctypes.c_double()
         check(lib().llg_norm2(self._h, ctypes.byref(v)))
         return v.value
+
+    def compare(self, other: "State") -> tuple[float, float]:
+        """(fidelity, max |amplitude difference|) against another state of the same size, on the
+        device in double."""
+        f, d = ctypes.c_double(), ctypes.c_double()
+        check(lib().llg_compare(self._h, other._h, ctypes.byref(f), ctypes.byref(d)))
+        return f.value, d.value
 
     def expect_zz(self, a: Sequence[int], b: Sequence[int], coeff: Sequence[float]) -> float:
         aa = np.ascontiguousarray(a, dtype=np.int32)

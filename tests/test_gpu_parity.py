@@ -213,6 +213,45 @@ def test_every_gate_kind_both_paths(precision):
         assert np.max(np.abs(got - want)) <= 1e-12, (fusion, tile)
 
 
+def test_config2_recipe_at_24_qubits_vs_oracle():
+    # the headline circuit's recipe (20 layers of RX/RY/RZ + CNOT brickwork) at 24 qubits against
+    # the CPU restatement, gate by gate, through the fused double-float plan
+    n = 24
+    ops = workloads.layered_rotations(n, layers=20)
+    want = oracle.run_ops(n, ops)
+    st = llgpu.State(n, "complex128")
+    st.apply_ops(ops)
+    assert np.max(np.abs(st.state() - want)) <= 1e-12
+    st.close()
+
+
+def test_config2_at_30_qubits_fused_vs_unfused_fp64():
+    # the 30-qubit headline circuit: fused double-float tile passes against one IEEE FP64 sweep per
+    # gate, compared on the device (16 GiB each)
+    n = 30
+    ops = workloads.layered_rotations(n, layers=20)
+    a = llgpu.State(n, "complex128")
+    a.apply_ops(ops)
+    b = llgpu.State(n, "fp64")
+    b.set_fusion("none")
+    b.apply_ops(ops)
+    fid, dmax = a.compare(b)
+    assert dmax <= 1e-12 and abs(1.0 - fid) <= 1e-12
+    a.close()
+    b.close()
+
+
+def test_compare_contract():
+    a, b, c = llgpu.State(4), llgpu.State(4, "complex64"), llgpu.State(5)
+    a.h(0)
+    fid, d = a.compare(b)
+    assert abs(fid - 0.5) < 1e-12 and abs(d - 2 ** -0.5) < 1e-7
+    with pytest.raises(ValueError):
+        a.compare(c)
+    for s in (a, b, c):
+        s.close()
+
+
 def test_twenty_qubit_layered_vs_oracle():
     n = 20
     ops = workloads.layered_rotations(n, layers=4, seed=12)
