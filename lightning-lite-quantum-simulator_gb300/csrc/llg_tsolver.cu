@@ -95,6 +95,12 @@ struct Gemm {
         if (e == cudaSuccess) e = cudaMalloc(&c, bytes);
         return e;
     }
+    // out = op(x) y on device buffers of d x d row-major complex (out may not alias x or y)
+    cudaError_t mul_dev(const double2* x, const double2* y, double2* out, bool adj_x) {
+        const dim3 grid((d + kTile - 1) / kTile, (d + kTile - 1) / kTile), block(kTile, kTile);
+        k_zgemm<<<grid, block, 0, s>>>(x, y, out, d, adj_x ? 1 : 0);
+        return cudaGetLastError();
+    }
     // out = op(x) y
     cudaError_t mul(const std::vector<cd>& x, const std::vector<cd>& y, std::vector<cd>& out, bool adj_x) {
         const size_t bytes = (size_t)d * d * sizeof(double2);
@@ -124,7 +130,21 @@ std::vector<cd> adjoint(const std::vector<cd>& m, int d) {
     return r;
 }
 
-// exp(A), the reference's scaling and squaring with an 18-term Taylor series.
+// term <- tmp / k, out <- out + term: the Taylor update of expm, on the device (the same IEEE
+// double division and addition as a host loop, so the plan is bit-identical to one)
+__global__ void k_taylor_step(const double2* __restrict__ tmp, double2* __restrict__ term, double2* __restrict__ out,
+                              size_t count, double k) {
+    const size_t step = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += step) {
+        const double2 t = make_double2(tmp[i].x / k, tmp[i].y / k);
+        term[i] = t;
+        out[i] = make_double2(out[i].x + t.x, out[i].y + t.y);
+    }
+}
+
+// exp(A), the reference's scaling and squaring with an 18-term Taylor series
+// (src/TrajectorySolver.h:95-110).  The series stays on the device: one product and one
+// elementwise update per term, one copy in and one out.
 cudaError_t expm(Gemm& g, const std::vector<cd>& a, std::vector<cd>& out) {
     const int d = g.d;
     double nrm = 0.0;
@@ -136,22 +156,33 @@ cudaError_t expm(Gemm& g, const std::vector<cd>& a, std::vector<cd>& out) {
     int s = 0;
     if (nrm > 0.5) s = std::max(0, (int)std::ceil(std::log2(nrm / 0.5)));
     const double scale = std::pow(2.0, s);
-    std::vector<cd> b(a.size()), term((size_t)d * d, 0.0), tmp;
+    const size_t count = (size_t)d * d, bytes = count * sizeof(double2);
+    std::vector<cd> b(a.size()), eye(count, 0.0);
     for (size_t i = 0; i < a.size(); ++i) b[i] = a[i] / scale;
-    for (int i = 0; i < d; ++i) term[(size_t)i * d + i] = 1.0;
-    out = term;
-    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < d; ++i) eye[(size_t)i * d + i] = 1.0;
+    double2 *term = nullptr, *acc = nullptr;
+    cudaError_t e = cudaMalloc(&term, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&acc, bytes);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(g.b, b.data(), bytes, cudaMemcpyHostToDevice, g.s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(term, eye.data(), bytes, cudaMemcpyHostToDevice, g.s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(acc, eye.data(), bytes, cudaMemcpyHostToDevice, g.s);
+    const unsigned blocks = (unsigned)std::min<size_t>((count + 255) / 256, 4096);
     for (int k = 1; k <= 18 && e == cudaSuccess; ++k) {
-        e = g.mul(term, b, tmp, false);
-        for (size_t i = 0; i < tmp.size(); ++i) {
-            term[i] = tmp[i] / (double)k;
-            out[i] += term[i];
+        e = g.mul_dev(term, g.b, g.c, false);
+        if (e == cudaSuccess) {
+            k_taylor_step<<<blocks, 256, 0, g.s>>>(g.c, term, acc, count, (double)k);
+            e = cudaGetLastError();
         }
     }
     for (int i = 0; i < s && e == cudaSuccess; ++i) {
-        e = g.mul(out, out, tmp, false);
-        out.swap(tmp);
+        e = g.mul_dev(acc, acc, g.c, false);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(acc, g.c, bytes, cudaMemcpyDeviceToDevice, g.s);
     }
+    out.resize(count);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out.data(), acc, bytes, cudaMemcpyDeviceToHost, g.s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g.s);
+    cudaFree(term);
+    cudaFree(acc);
     return e;
 }
 
