@@ -24,20 +24,7 @@ __device__ __forceinline__ float shfl(float v, int src) { return __shfl_sync(0xf
 __device__ __forceinline__ double shfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 __device__ __forceinline__ df shfl(df v, int src) { return {shfl(v.hi, src), shfl(v.lo, src)}; }
 
-// Row accumulators: sum of products a * b.
-struct DotDF {  // Dot2: s + e carries the sum; products split exactly by FMA
-    float s = 0.0f, e = 0.0f;
-    __device__ __forceinline__ void add(df a, df b) {
-        const float p = __fmul_rn(a.hi, b.hi);
-        const float pe = fmaf(a.hi, b.hi, -p);
-        const df t = two_sum(s, p);
-        s = t.hi;
-        float c = fmaf(a.hi, b.lo, pe);
-        c = fmaf(a.lo, b.hi, c);
-        e = __fadd_rn(e, __fadd_rn(c, t.lo));
-    }
-    __device__ __forceinline__ df value() const { return fast_two_sum(s, e); }
-};
+// Row accumulators: sum of products a * b (DotDF, the double-float Dot2, is in llg_common.cuh).
 struct DotD {
     double s = 0.0;
     __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }

@@ -133,6 +133,22 @@ __device__ __forceinline__ df df_lin4(df a, df x, df b, df y, df c, df z, df d, 
     return fast_two_sum(s.hi, t);
 }
 
+// Dot2 accumulator (Ogita, Rump and Oishi, SIAM J. Sci. Comput. 2005): s + e carries a sum of
+// double-float products, each high product split exactly by FMA and added by TwoSum
+struct DotDF {
+    float s = 0.0f, e = 0.0f;
+    __device__ __forceinline__ void add(df a, df b) {
+        const float p = __fmul_rn(a.hi, b.hi);
+        const float pe = fmaf(a.hi, b.hi, -p);
+        const df t = two_sum(s, p);
+        s = t.hi;
+        float c = fmaf(a.hi, b.lo, pe);
+        c = fmaf(a.lo, b.hi, c);
+        e = __fadd_rn(e, __fadd_rn(c, t.lo));
+    }
+    __device__ __forceinline__ df value() const { return fast_two_sum(s, e); }
+};
+
 // x*x + y*y (for |a|^2 accumulation)
 __device__ __forceinline__ df df_sqsum(df x, df y) { return df_lin2(x, x, y, y); }
 

@@ -6,14 +6,17 @@
 // Plan (host, once per run, src/TrajectorySolver.h:400-441): steps and h; jump operators
 // J_k = sqrt(gamma) L, or sqrt(g) (1 - P) for Pauli-like channels under PROJECTOR; H_eff =
 // H - i/2 sum J^+ J for the jump unravelings; a constant H gives one propagator exp(-i H_eff h)
-// by scaling and squaring with an 18-term Taylor series (:95-110), a time-dependent H the RK4
-// nodes -i (H(t_j) + hnh).  The matrix products of the plan (powers, J^+ J, L^2) run on a tiled
+// by scaling and squaring with an 18-term Taylor series (:95-110, evaluated by Paterson-Stockmeyer),
+// a time-dependent H the RK4 nodes -i (H(t_j) + hnh).  The matrix products of the plan (powers, J^+ J, L^2) run on a tiled
 // FP64 GEMM kernel.
 //
 // Trajectories (k_tsolve): one CTA per trajectory at a time (persistent over the trajectory
 // range), the state and its work vectors in shared memory.  A matrix-vector product is one thread
 // per row streaming the matrix column-major (coalesced, L2-resident across CTAs) against the
-// vector broadcast from shared memory.  Norm reductions are FP64 block sums.  Uniforms come from
+// vector broadcast from shared memory.  The matrices are stored and multiplied in double-float
+// (rows accumulated with the Dot2 scheme on the FP32 pipe, ~2^-46 relative), states stay FP64:
+// this GPU issues ~1.6 FP64 operations per clock per SM against ~115 FP32, and the FP64 product
+// was FP64-bound.  Norm reductions are FP64 block sums.  Uniforms come from
 // Philox4x32-10 (key = seed, counter = (draw, trajectory)): a jump step s uses draw s (u1, and
 // u2 for the channel pick), a diffusive step channel k draw s * nch + k (Box-Muller).
 #include <algorithm>
@@ -26,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/llgpu.h"
+#include "llg_common.cuh"
 
 namespace llg {
 int set_error(int code, const std::string& msg);
@@ -130,21 +134,31 @@ std::vector<cd> adjoint(const std::vector<cd>& m, int d) {
     return r;
 }
 
-// term <- tmp / k, out <- out + term: the Taylor update of expm, on the device (the same IEEE
-// double division and addition as a host loop, so the plan is bit-identical to one)
-__global__ void k_taylor_step(const double2* __restrict__ tmp, double2* __restrict__ term, double2* __restrict__ out,
-                              size_t count, double k) {
-    const size_t step = (size_t)gridDim.x * blockDim.x;
+// acc[i] = (tmp ? tmp[i] : 0) + c0 [row == col] + c1 p1[i] + c2 p2[i] + c3 p3[i] over a d x d
+// row-major matrix: one Paterson-Stockmeyer step of expm (FP64)
+__global__ void k_ps_step(const double2* __restrict__ tmp, const double2* __restrict__ p1, const double2* __restrict__ p2,
+                          const double2* __restrict__ p3, double2* __restrict__ acc, int d, double c0, double c1, double c2,
+                          double c3) {
+    const size_t count = (size_t)d * d, step = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += step) {
-        const double2 t = make_double2(tmp[i].x / k, tmp[i].y / k);
-        term[i] = t;
-        out[i] = make_double2(out[i].x + t.x, out[i].y + t.y);
+        double re = tmp ? tmp[i].x : 0.0, im = tmp ? tmp[i].y : 0.0;
+        if (i / d == i % d) re += c0;
+        re = fma(c1, p1[i].x, re);
+        im = fma(c1, p1[i].y, im);
+        re = fma(c2, p2[i].x, re);
+        im = fma(c2, p2[i].y, im);
+        re = fma(c3, p3[i].x, re);
+        im = fma(c3, p3[i].y, im);
+        acc[i] = make_double2(re, im);
     }
 }
 
-// exp(A), the reference's scaling and squaring with an 18-term Taylor series
-// (src/TrajectorySolver.h:95-110).  The series stays on the device: one product and one
-// elementwise update per term, one copy in and one out.
+// exp(A) by the reference's scaling and squaring with an 18-term Taylor series
+// (src/TrajectorySolver.h:95-110).  The degree-18 polynomial of B = A / 2^s is evaluated on the
+// device by Paterson-Stockmeyer with blocks of four: B^2, B^3, B^4, then
+//     p(B) = (((C_4 B^4 + C_3) B^4 + C_2) B^4 + C_1) B^4 + C_0,  C_j = sum_i B^i / (4j + i)!,
+// 7 products instead of 18 (FP64 throughout; only the rounding order differs from term-by-term
+// summation), then s squarings.  One copy in, one out.
 cudaError_t expm(Gemm& g, const std::vector<cd>& a, std::vector<cd>& out) {
     const int d = g.d;
     double nrm = 0.0;
@@ -157,31 +171,42 @@ cudaError_t expm(Gemm& g, const std::vector<cd>& a, std::vector<cd>& out) {
     if (nrm > 0.5) s = std::max(0, (int)std::ceil(std::log2(nrm / 0.5)));
     const double scale = std::pow(2.0, s);
     const size_t count = (size_t)d * d, bytes = count * sizeof(double2);
-    std::vector<cd> b(a.size()), eye(count, 0.0);
+    std::vector<cd> b(a.size());
     for (size_t i = 0; i < a.size(); ++i) b[i] = a[i] / scale;
-    for (int i = 0; i < d; ++i) eye[(size_t)i * d + i] = 1.0;
-    double2 *term = nullptr, *acc = nullptr;
-    cudaError_t e = cudaMalloc(&term, bytes);
+    double coef[19];  // 1 / k!
+    coef[0] = 1.0;
+    for (int k = 1; k <= 18; ++k) coef[k] = coef[k - 1] / (double)k;
+    double2 *p2 = nullptr, *p3 = nullptr, *p4 = nullptr, *acc = nullptr;
+    cudaError_t e = cudaMalloc(&p2, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&p3, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&p4, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&acc, bytes);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(g.b, b.data(), bytes, cudaMemcpyHostToDevice, g.s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(term, eye.data(), bytes, cudaMemcpyHostToDevice, g.s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(acc, eye.data(), bytes, cudaMemcpyHostToDevice, g.s);
+    double2* p1 = g.b;
+    double2* tmp = g.c;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p1, b.data(), bytes, cudaMemcpyHostToDevice, g.s);
+    if (e == cudaSuccess) e = g.mul_dev(p1, p1, p2, false);
+    if (e == cudaSuccess) e = g.mul_dev(p2, p1, p3, false);
+    if (e == cudaSuccess) e = g.mul_dev(p2, p2, p4, false);
     const unsigned blocks = (unsigned)std::min<size_t>((count + 255) / 256, 4096);
-    for (int k = 1; k <= 18 && e == cudaSuccess; ++k) {
-        e = g.mul_dev(term, g.b, g.c, false);
+    auto c = [&](int k) { return k <= 18 ? coef[k] : 0.0; };
+    for (int j = 4; j >= 0 && e == cudaSuccess; --j) {
+        if (j < 4) e = g.mul_dev(acc, p4, tmp, false);  // acc B^4
         if (e == cudaSuccess) {
-            k_taylor_step<<<blocks, 256, 0, g.s>>>(g.c, term, acc, count, (double)k);
+            k_ps_step<<<blocks, 256, 0, g.s>>>(j < 4 ? tmp : nullptr, p1, p2, p3, acc, d, c(4 * j), c(4 * j + 1),
+                                                c(4 * j + 2), c(4 * j + 3));
             e = cudaGetLastError();
         }
     }
     for (int i = 0; i < s && e == cudaSuccess; ++i) {
-        e = g.mul_dev(acc, acc, g.c, false);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(acc, g.c, bytes, cudaMemcpyDeviceToDevice, g.s);
+        e = g.mul_dev(acc, acc, tmp, false);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(acc, tmp, bytes, cudaMemcpyDeviceToDevice, g.s);
     }
     out.resize(count);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out.data(), acc, bytes, cudaMemcpyDeviceToHost, g.s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g.s);
-    cudaFree(term);
+    cudaFree(p2);
+    cudaFree(p3);
+    cudaFree(p4);
     cudaFree(acc);
     return e;
 }
@@ -200,12 +225,13 @@ struct TsParams {
     int32_t dim, nch, kind, constant;
     long long steps;
     double h;
-    const double2* prop;     // dim x dim, column-major
-    const double2* nodes;    // n_nodes x dim x dim, column-major
-    const double2* ops;      // nch x dim x dim, column-major
-    const double2* ops_dop;  // nch x dim x dim, column-major (ANALOG)
+    // matrices column-major, each entry double-float {re.hi, im.hi, re.lo, im.lo}
+    const float4* prop;      // dim x dim
+    const float4* nodes;     // n_nodes x dim x dim
+    const float4* ops;       // nch x dim x dim
+    const float4* ops_dop;   // nch x dim x dim (ANALOG)
     const double2* psi0;     // dim, normalised
-    const double2* obs;      // dim x dim, column-major, or null
+    const float4* obs;       // dim x dim, or null
     uint64_t seed;
     uint64_t traj_begin, n_traj;
     double2* states;         // n_traj x dim, or null
@@ -235,16 +261,26 @@ __device__ __forceinline__ void philox_pair(uint64_t seed, uint64_t traj, uint64
     *u2 = (double)(b >> 11) * (1.0 / 9007199254740992.0);
 }
 
-// y = A x, A column-major dim x dim; one thread per row
-__device__ __forceinline__ void matvec(const double2* __restrict__ a, const double2* x, double2* y, int d) {
+// y = A x, A column-major dim x dim in double-float; one thread per row.  x is converted to
+// double-float into xs (shared memory, dim entries) first; each row's real and imaginary parts
+// are Dot2 sums, converted to double once.
+__device__ __forceinline__ void matvec(const float4* __restrict__ a, const double2* x, double2* y, int d, float4* xs) {
+    for (int c = threadIdx.x; c < d; c += blockDim.x) {
+        const df xr = double_to_df(x[c].x), xi = double_to_df(x[c].y);
+        xs[c] = make_float4(xr.hi, xi.hi, xr.lo, xi.lo);
+    }
+    __syncthreads();
     for (int r = threadIdx.x; r < d; r += blockDim.x) {
-        double sr = 0.0, si = 0.0;
+        DotDF re, im;
         for (int c = 0; c < d; ++c) {
-            const double2 m = a[(size_t)c * d + r], v = x[c];
-            sr = fma(m.x, v.x, fma(-m.y, v.y, sr));
-            si = fma(m.x, v.y, fma(m.y, v.x, si));
+            const float4 m = a[(size_t)c * d + r], v = xs[c];
+            const df mr{m.x, m.z}, mi{m.y, m.w}, vr{v.x, v.z}, vi{v.y, v.w};
+            re.add(mr, vr);
+            re.add(df_neg(mi), vi);
+            im.add(mr, vi);
+            im.add(mi, vr);
         }
-        y[r] = make_double2(sr, si);
+        y[r] = make_double2(df_to_double(re.value()), df_to_double(im.value()));
     }
     __syncthreads();
 }
@@ -283,6 +319,7 @@ __global__ void __launch_bounds__(kTsThreads) k_tsolve(TsParams p) {
     double2* w = tmp + d;
     double2* k = w + d;
     double2* acc = k + d;
+    float4* xs = reinterpret_cast<float4*>(acc + d);  // matvec scratch
     const size_t dd = (size_t)d * d;
     for (uint64_t tt = blockIdx.x; tt < p.n_traj; tt += gridDim.x) {
         const uint64_t traj = p.traj_begin + tt;
@@ -292,19 +329,19 @@ __global__ void __launch_bounds__(kTsThreads) k_tsolve(TsParams p) {
         for (long long s = 0; s < p.steps && !failed; ++s) {
             if (p.kind == 2) {  // diffusive
                 if (p.constant) {
-                    matvec(p.prop, psi, tmp, d);
+                    matvec(p.prop, psi, tmp, d, xs);
                     for (int r = threadIdx.x; r < d; r += blockDim.x) {
                         psi[r] = tmp[r];
                         acc[r] = make_double2(0.0, 0.0);  // drift
                     }
                 } else {
-                    matvec(p.nodes + (size_t)s * dd, psi, acc, d);
+                    matvec(p.nodes + (size_t)s * dd, psi, acc, d, xs);
                 }
                 for (int r = threadIdx.x; r < d; r += blockDim.x) tmp[r] = make_double2(0.0, 0.0);  // noise
                 __syncthreads();
                 for (int c = 0; c < p.nch; ++c) {
-                    matvec(p.ops + (size_t)c * dd, psi, w, d);      // cp
-                    matvec(p.ops_dop + (size_t)c * dd, psi, k, d);  // t2
+                    matvec(p.ops + (size_t)c * dd, psi, w, d, xs);      // cp
+                    matvec(p.ops_dop + (size_t)c * dd, psi, k, d, xs);  // t2
                     double part = 0.0;
                     for (int r = threadIdx.x; r < d; r += blockDim.x) part = fma(psi[r].x, w[r].x, fma(psi[r].y, w[r].y, part));
                     const double x = 2.0 * block_sum(part, red);
@@ -338,33 +375,33 @@ __global__ void __launch_bounds__(kTsThreads) k_tsolve(TsParams p) {
             }
             // jump unravelings: tmp = psi~
             if (p.constant) {
-                matvec(p.prop, psi, tmp, d);
+                matvec(p.prop, psi, tmp, d, xs);
             } else {
-                const double2* a0 = p.nodes + (size_t)(2 * s) * dd;
-                const double2* a1 = a0 + dd;
-                const double2* a2 = a1 + dd;
+                const float4* a0 = p.nodes + (size_t)(2 * s) * dd;
+                const float4* a1 = a0 + dd;
+                const float4* a2 = a1 + dd;
                 const double h = p.h;
-                matvec(a0, psi, k, d);  // k1
+                matvec(a0, psi, k, d, xs);  // k1
                 for (int r = threadIdx.x; r < d; r += blockDim.x) {
                     acc[r] = make_double2(k[r].x, k[r].y);  // k1 + 2 k2 + 2 k3 + k4, accumulated
                     w[r] = make_double2(psi[r].x + 0.5 * h * k[r].x, psi[r].y + 0.5 * h * k[r].y);
                 }
                 __syncthreads();
-                matvec(a1, w, k, d);  // k2
+                matvec(a1, w, k, d, xs);  // k2
                 for (int r = threadIdx.x; r < d; r += blockDim.x) {
                     acc[r].x += 2.0 * k[r].x;
                     acc[r].y += 2.0 * k[r].y;
                     w[r] = make_double2(psi[r].x + 0.5 * h * k[r].x, psi[r].y + 0.5 * h * k[r].y);
                 }
                 __syncthreads();
-                matvec(a1, w, k, d);  // k3
+                matvec(a1, w, k, d, xs);  // k3
                 for (int r = threadIdx.x; r < d; r += blockDim.x) {
                     acc[r].x += 2.0 * k[r].x;
                     acc[r].y += 2.0 * k[r].y;
                     w[r] = make_double2(psi[r].x + h * k[r].x, psi[r].y + h * k[r].y);
                 }
                 __syncthreads();
-                matvec(a2, w, k, d);  // k4
+                matvec(a2, w, k, d, xs);  // k4
                 for (int r = threadIdx.x; r < d; r += blockDim.x) {
                     tmp[r].x = psi[r].x + (h / 6.0) * (acc[r].x + k[r].x);
                     tmp[r].y = psi[r].y + (h / 6.0) * (acc[r].y + k[r].y);
@@ -382,7 +419,7 @@ __global__ void __launch_bounds__(kTsThreads) k_tsolve(TsParams p) {
             if (p.nch > 0 && u1 >= survive) {  // uniform across the block
                 double total = 0.0;
                 for (int c = 0; c < p.nch; ++c) {
-                    matvec(p.ops + (size_t)c * dd, tmp, w, d);
+                    matvec(p.ops + (size_t)c * dd, tmp, w, d, xs);
                     const double wc = norm2(w, d, red);
                     if (threadIdx.x == 0) weight[c] = wc;
                     total += wc;
@@ -405,7 +442,7 @@ __global__ void __launch_bounds__(kTsThreads) k_tsolve(TsParams p) {
                                 pick = c;
                                 break;
                             }
-                    matvec(p.ops + (size_t)pick * dd, tmp, psi, d);
+                    matvec(p.ops + (size_t)pick * dd, tmp, psi, d, xs);
                     const double inv = 1.0 / sqrt(weight[pick]);
                     for (int r = threadIdx.x; r < d; r += blockDim.x) {
                         psi[r].x *= inv;
@@ -429,7 +466,7 @@ __global__ void __launch_bounds__(kTsThreads) k_tsolve(TsParams p) {
         if (p.states)
             for (int r = threadIdx.x; r < d; r += blockDim.x) p.states[tt * (uint64_t)d + r] = psi[r];
         if (p.obs) {
-            matvec(p.obs, psi, w, d);
+            matvec(p.obs, psi, w, d, xs);
             double part = 0.0;
             for (int r = threadIdx.x; r < d; r += blockDim.x) part = fma(psi[r].x, w[r].x, fma(psi[r].y, w[r].y, part));
             const double v = block_sum(part, red);
@@ -700,14 +737,28 @@ int llg_tsolver_run(llg_tsolver* s, const double* psi0, double duration, double 
 
     // device buffers
     const size_t dd = (size_t)d * d;
-    double2 *d_prop = nullptr, *d_nodes = nullptr, *d_ops = nullptr, *d_dop = nullptr, *d_psi0 = nullptr, *d_obs = nullptr,
-            *d_states = nullptr, *d_rho = nullptr;
+    float4 *d_prop = nullptr, *d_nodes = nullptr, *d_ops = nullptr, *d_dop = nullptr, *d_obs = nullptr;
+    double2 *d_psi0 = nullptr, *d_states = nullptr, *d_rho = nullptr;
     double* d_obs_out = nullptr;
     int* d_err = nullptr;
     auto up = [&](double2** dst, const std::vector<cd>& src) {
         if (e != cudaSuccess || src.empty()) return;
         e = cudaMalloc(dst, src.size() * sizeof(double2));
         if (e == cudaSuccess) e = cudaMemcpyAsync(*dst, src.data(), src.size() * sizeof(double2), cudaMemcpyHostToDevice, s->stream);
+    };
+    std::vector<std::vector<float4>> staged;  // host copies alive until the stream synchronises
+    auto up_df = [&](float4** dst, const std::vector<cd>& src) {  // matrices: double-float entries
+        if (e != cudaSuccess || src.empty()) return;
+        staged.emplace_back(src.size());
+        std::vector<float4>& h = staged.back();
+        for (size_t i = 0; i < src.size(); ++i) {
+            float rh, rl, ih, il;
+            split_double(src[i].real(), &rh, &rl);
+            split_double(src[i].imag(), &ih, &il);
+            h[i] = make_float4(rh, ih, rl, il);
+        }
+        e = cudaMalloc(dst, h.size() * sizeof(float4));
+        if (e == cudaSuccess) e = cudaMemcpyAsync(*dst, h.data(), h.size() * sizeof(float4), cudaMemcpyHostToDevice, s->stream);
     };
     auto colmajor_list = [&](const std::vector<cd>& list) {
         std::vector<cd> r(list.size());
@@ -726,12 +777,12 @@ int llg_tsolver_run(llg_tsolver* s, const double* psi0, double duration, double 
         dop_cm = colmajor_list(s->ops_dop);
     }
     if (obs) obs_cm = col_major(obs_m, d);
-    up(&d_prop, prop_cm);
-    up(&d_nodes, nodes_cm);
-    up(&d_ops, ops_cm);
-    up(&d_dop, dop_cm);
+    up_df(&d_prop, prop_cm);
+    up_df(&d_nodes, nodes_cm);
+    up_df(&d_ops, ops_cm);
+    up_df(&d_dop, dop_cm);
     up(&d_psi0, start);
-    up(&d_obs, obs_cm);
+    up_df(&d_obs, obs_cm);
     const bool need_states = states_out || rho_out;
     if (e == cudaSuccess && need_states) e = cudaMalloc(&d_states, (size_t)n_traj * d * sizeof(double2));
     if (e == cudaSuccess && obs) e = cudaMalloc(&d_obs_out, (size_t)n_traj * sizeof(double));
@@ -759,7 +810,7 @@ int llg_tsolver_run(llg_tsolver* s, const double* psi0, double duration, double 
         p.obs_out = d_obs_out;
         p.err = d_err;
         const int threads = std::min(kTsThreads, std::max(32, ((d + 31) / 32) * 32));
-        const size_t smem = 5 * (size_t)d * sizeof(double2);
+        const size_t smem = 5 * (size_t)d * sizeof(double2) + (size_t)d * sizeof(float4);
         int dev = 0, sms = 1, per_sm = 1;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
