@@ -7,8 +7,8 @@
 // J_k = sqrt(gamma) L, or sqrt(g) (1 - P) for Pauli-like channels under PROJECTOR; H_eff =
 // H - i/2 sum J^+ J for the jump unravelings; a constant H gives one propagator exp(-i H_eff h)
 // by scaling and squaring with an 18-term Taylor series (:95-110, evaluated by Paterson-Stockmeyer),
-// a time-dependent H the RK4 nodes -i (H(t_j) + hnh).  The matrix products of the plan (powers, J^+ J, L^2) run on a tiled
-// FP64 GEMM kernel.
+// a time-dependent H the RK4 nodes -i (H(t_j) + hnh).  The matrix products of the plan (powers,
+// J^+ J, L^2) run on a tiled FP64 GEMM kernel.
 //
 // Trajectories (k_tsolve): one CTA per trajectory at a time (persistent over the trajectory
 // range), the state and its work vectors in shared memory.  A matrix-vector product is one thread
