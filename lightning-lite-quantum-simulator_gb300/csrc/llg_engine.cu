@@ -69,6 +69,7 @@ struct llg_state {
     void* d_block_tc = nullptr;
     unsigned char* h_block_tc = nullptr;
     bool block_tc_launched = false;
+    bool tiles_launched = false;  // a tile pass ran since the last sync (its load-timeout flag to check)
     // reductions
     double* d_partials = nullptr;
     double* d_red = nullptr;
@@ -230,6 +231,7 @@ int run_tiles(llg_state* st, const std::vector<llg_op>& q) {
         return set_error(LLG_EINVAL, err);
     int rc = upload_ops(st, plan.ops);
     if (rc) return rc;
+    st->tiles_launched = true;
     for (const PassDesc& pd : plan.passes) {
         if (pd.nops <= 0) continue;
         rc = traced(st, LLG_PROF_TILE, 1, "tile kernel",
@@ -660,6 +662,10 @@ int llg_sync(llg_state* st) {
         st->block_tc_launched = false;
         if (block_tc_take_error())
             return set_error(LLG_ECUDA, "apply_matrix: a tensor-core block kernel timed out waiting for its products");
+    }
+    if (st->tiles_launched) {
+        st->tiles_launched = false;
+        if (tile_copy_take_error()) return set_error(LLG_ECUDA, "tile pass: a bulk tile load timed out");
     }
     return LLG_OK;
 }

@@ -149,6 +149,21 @@ __global__ void __launch_bounds__(kThreads) k_mcz(typename P::S* __restrict__ ps
 // tile pass
 // ------------------------------------------------------------------------------------------
 constexpr int kOpChunk = 32;  // op records staged per shared-memory chunk in k_tile
+constexpr long kTileCopyWaitLimit = 1L << 24;  // mbarrier polls before a tile load is reported as timed out
+
+__device__ int g_tile_copy_error = 0;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// bounded wait for phase `parity` of an mbarrier; false if it did not complete
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t done = 0;
+    for (long it = 0; it < kTileCopyWaitLimit && !done; ++it)
+        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(done)
+                     : "r"(smem_addr(bar)), "r"(parity));
+    return done != 0;
+}
 
 template <class P>
 __global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, PassDesc pd, const ExecOp* __restrict__ ops) {
@@ -168,11 +183,40 @@ __global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, 
             if ((h >> j) & 1) off |= 1ULL << pd.hi_pos[j];
         hi_off[h] = off;
     }
+    // The tile is nhi contiguous runs of 2^low amplitudes, each starting at a multiple of its own
+    // size (base and hi_off are zero in the low bits).  Runs of 128 bytes or more move with the
+    // bulk-copy engine (cp.async.bulk into shared memory, completing on an mbarrier that expects
+    // the tile's bytes; stores back the same way); shorter ones with plain loads and stores.
+    __shared__ __align__(8) uint64_t tile_bar;
+    const uint32_t run_bytes = (uint32_t)sizeof(S) << low;
+    const bool bulk = run_bytes >= 128;
+    if (bulk && threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&tile_bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&tile_bar)),
+                     "r"((uint32_t)(tsize * sizeof(S)))
+                     : "memory");
+    }
     __syncthreads();
     const uint32_t lowmask = (1u << low) - 1;
-    for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x)
-        tile[l] = psi[base | hi_off[l >> low] | (l & lowmask)];
+    bool loaded = true;
+    if (bulk) {
+        for (uint32_t h = threadIdx.x; h < nhi; h += blockDim.x)
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    smem_addr(tile + ((size_t)h << low))),
+                "l"(psi + (base | hi_off[h])), "r"(run_bytes), "r"(smem_addr(&tile_bar))
+                : "memory");
+        loaded = mbar_wait(&tile_bar, 0);
+        if (!loaded && threadIdx.x == 0) atomicExch(&g_tile_copy_error, 1);
+    } else {
+        for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) tile[l] = psi[base | hi_off[l >> low] | (l & lowmask)];
+    }
     __syncthreads();
+    if (!__syncthreads_and(loaded)) {
+        (void)mbar_wait(&tile_bar, 0);  // give copies still in flight a second bounded wait, store nothing
+        return;
+    }
 
     // op records are staged through shared memory in chunks (one coalesced copy per chunk
     // instead of a dependent global load before every op's barrier)
@@ -243,7 +287,18 @@ __global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, 
         __syncthreads();
     }
 
-    for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) psi[base | hi_off[l >> low] | (l & lowmask)] = tile[l];
+    if (bulk) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // this thread's tile writes, to the copy engine
+        __syncthreads();
+        for (uint32_t h = threadIdx.x; h < nhi; h += blockDim.x)
+            asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(psi + (base | hi_off[h])),
+                         "r"(smem_addr(tile + ((size_t)h << low))), "r"(run_bytes)
+                         : "memory");
+        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // the tile is read before the CTA exits
+    } else {
+        for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) psi[base | hi_off[l >> low] | (l & lowmask)] = tile[l];
+    }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -460,6 +515,16 @@ cudaError_t launch_init_basis(int P, void* psi, uint64_t size, uint64_t index, c
 
 cudaError_t launch_exec_op(int P, void* psi, int n, const ExecOp& op, cudaStream_t s) {
     LLG_DISPATCH(P, return exec_op_t<Pol>(psi, n, op, s));
+}
+
+int tile_copy_take_error() {
+    int h = 0;
+    cudaMemcpyFromSymbol(&h, g_tile_copy_error, sizeof(int));
+    if (h) {
+        const int zero = 0;
+        cudaMemcpyToSymbol(g_tile_copy_error, &zero, sizeof(int));
+    }
+    return h;
 }
 
 cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, int threads, cudaStream_t s) {

@@ -32,6 +32,8 @@ cudaError_t launch_init_basis(int P, void* psi, uint64_t size, uint64_t index, c
 cudaError_t launch_exec_op(int P, void* psi, int n, const ExecOp& op, cudaStream_t s);
 // threads: CTA size of the tile kernel (0: 512 for tiles of 10+ qubits, else half the tile)
 cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, int threads, cudaStream_t s);
+// 1 if a tile pass's bulk load timed out since the last call (the flag is cleared)
+int tile_copy_take_error();
 cudaError_t launch_from_f64(int P, const double* src, void* dst, uint64_t count, cudaStream_t s);
 cudaError_t launch_to_f64(int P, const void* src, double* dst, uint64_t count, cudaStream_t s);
 cudaError_t launch_probabilities(int P, const void* psi, double* out, uint64_t count, cudaStream_t s);
