@@ -187,7 +187,8 @@ int llg_sync(llg_state* st);
 
 /* Amplitudes to host memory (2*2^n doubles) after a flush; replaces get_numpy_view
  * (src/StateVectorOptimized.cpp:99-106) and Backend::state (src/Backend.h:44) as an explicit
- * device-to-host copy. */
+ * device-to-host copy.  Into pinned memory (llg_host_alloc, cudaHostRegister) one conversion
+ * kernel writes the host buffer directly; other memory is filled through a staging buffer. */
 int llg_copy_to_host(llg_state* st, double* out);
 /* Overwrite the amplitudes from host memory (2*2^n doubles). */
 int llg_copy_from_host(llg_state* st, const double* amps);
@@ -420,7 +421,8 @@ int64_t llg_kernel_launches(void);
 /* The state's CUDA stream (a cudaStream_t), for callers that order their own work after it. */
 int llg_get_stream(const llg_state* st, void** out);
 
-/* Pinned host memory for fast transfers (cudaHostAlloc); NULL on failure. */
+/* Pinned host memory, mapped into the device's address space, for fast transfers
+ * (cudaHostAlloc); NULL on failure. */
 void* llg_host_alloc(size_t bytes);
 void llg_host_free(void* p);
 

@@ -670,12 +670,31 @@ int llg_sync(llg_state* st) {
     return LLG_OK;
 }
 
+// Device address of pinned, mapped host memory (cudaHostAlloc / cudaHostRegister), else nullptr.
+static void* mapped_device_pointer(void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int llg_copy_to_host(llg_state* st, double* out) {
     if (!st || !out) return set_error(LLG_EINVAL, "copy_to_host: NULL argument");
     int rc = llg_flush(st);
     if (rc) return rc;
     if (st->P == LLG_F64) {
         LLG_CUDA(cudaMemcpyAsync(out, st->d_psi, st->size * 16, cudaMemcpyDeviceToHost, st->stream), "cudaMemcpyAsync(D2H)");
+        LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+        return LLG_OK;
+    }
+    // A pinned destination is written by the conversion kernel itself, over the host link: one
+    // pass at the link's rate, with no staging copy and no copy-engine step after each chunk.
+    if (void* dev_out = mapped_device_pointer(out)) {
+        rc = traced(st, LLG_PROF_READOUT, 1, "to_f64",
+                    [&] { return launch_to_f64(st->P, st->d_psi, static_cast<double*>(dev_out), st->size, st->stream); });
+        if (rc) return rc;
         LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
         return LLG_OK;
     }
@@ -851,7 +870,7 @@ int llg_renormalize(llg_state* st) {
 
 void* llg_host_alloc(size_t bytes) {
     void* p = nullptr;
-    if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess) {
+    if (cudaHostAlloc(&p, bytes, cudaHostAllocMapped) != cudaSuccess) {
         cudaGetLastError();
         return nullptr;
     }

@@ -184,6 +184,30 @@ def test_readouts_match_oracle(precision):
         st.close()
 
 
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_pinned_and_pageable_readback_agree(precision):
+    """A pinned destination is written by the conversion kernel directly; pageable memory goes
+    through 256 MiB staging chunks (two chunks at 25 qubits).  Both give the same bits."""
+    import ctypes
+
+    rng = np.random.default_rng(12)
+    for n in (5, 14, 25):
+        psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+        psi /= np.linalg.norm(psi)
+        st = llgpu.State(precision=precision, amps=psi)
+        st.apply_ops(make_ops([(OP_H, 0), (OP_RX, n - 1, 0, 0.3), (OP_CNOT, 0, n - 1)]))
+        pageable = st.state()
+        buf = llgpu.lib().llg_host_alloc(16 << n)
+        assert buf
+        try:
+            llgpu.check(llgpu.lib().llg_copy_to_host(st._h, buf))
+            pinned = np.frombuffer((ctypes.c_double * (2 << n)).from_address(buf), dtype=np.float64).view(np.complex128).copy()
+        finally:
+            llgpu.lib().llg_host_free(buf)
+        assert np.array_equal(pinned, pageable)
+        st.close()
+
+
 @pytest.mark.parametrize("precision", ["complex128", "fp64"])
 def test_every_gate_kind_both_paths(precision):
     rng = np.random.default_rng(8)
