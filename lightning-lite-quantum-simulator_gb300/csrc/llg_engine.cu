@@ -223,7 +223,9 @@ int upload_ops(llg_state* st, const std::vector<ExecOp>& ops) {
     return LLG_OK;
 }
 
-int run_tiles(llg_state* st, const std::vector<llg_op>& q) {
+// mirror (optional): the device address of a mapped host buffer that the last pass also fills;
+// *mirrored tells whether a pass did (a plan may have no pass with work)
+int run_tiles(llg_state* st, const std::vector<llg_op>& q, double* mirror = nullptr, bool* mirrored = nullptr) {
     Plan plan;
     std::string err;
     const int t = st->tile_qubits > 0 ? st->tile_qubits : default_tile(st->P);
@@ -232,12 +234,18 @@ int run_tiles(llg_state* st, const std::vector<llg_op>& q) {
     int rc = upload_ops(st, plan.ops);
     if (rc) return rc;
     st->tiles_launched = true;
-    for (const PassDesc& pd : plan.passes) {
+    size_t last = plan.passes.size();
+    for (size_t i = 0; i < plan.passes.size(); ++i)
+        if (plan.passes[i].nops > 0) last = i;
+    for (size_t i = 0; i < plan.passes.size(); ++i) {
+        const PassDesc& pd = plan.passes[i];
         if (pd.nops <= 0) continue;
+        double* m = i == last ? mirror : nullptr;
         rc = traced(st, LLG_PROF_TILE, 1, "tile kernel",
-                    [&] { return launch_tile_pass(st->P, st->d_psi, st->n, pd, st->d_ops, st->tile_threads, st->stream); });
+                    [&] { return launch_tile_pass(st->P, st->d_psi, st->n, pd, st->d_ops, st->tile_threads, st->stream, m); });
         if (rc) return rc;
     }
+    if (mirrored) *mirrored = mirror && last < plan.passes.size();
     return LLG_OK;
 }
 
@@ -682,7 +690,21 @@ static void* mapped_device_pointer(void* p) {
 
 int llg_copy_to_host(llg_state* st, double* out) {
     if (!st || !out) return set_error(LLG_EINVAL, "copy_to_host: NULL argument");
-    int rc = llg_flush(st);
+    void* const dev_out = mapped_device_pointer(out);
+    int rc;
+    // Gates still queued for tile passes: the last pass writes the host buffer as it stores its
+    // tiles, so the transfer runs under that pass's arithmetic instead of after it.
+    if (dev_out && !st->queue.empty() && st->n > 0 && st->fuse_mode == LLG_FUSE_TILE) {
+        std::vector<llg_op> q;
+        q.swap(st->queue);
+        bool mirrored = false;
+        if ((rc = run_tiles(st, q, static_cast<double*>(dev_out), &mirrored))) return rc;
+        if (mirrored) {
+            LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+            return LLG_OK;
+        }
+    }
+    rc = llg_flush(st);
     if (rc) return rc;
     if (st->P == LLG_F64) {
         LLG_CUDA(cudaMemcpyAsync(out, st->d_psi, st->size * 16, cudaMemcpyDeviceToHost, st->stream), "cudaMemcpyAsync(D2H)");
@@ -691,7 +713,7 @@ int llg_copy_to_host(llg_state* st, double* out) {
     }
     // A pinned destination is written by the conversion kernel itself, over the host link: one
     // pass at the link's rate, with no staging copy and no copy-engine step after each chunk.
-    if (void* dev_out = mapped_device_pointer(out)) {
+    if (dev_out) {
         rc = traced(st, LLG_PROF_READOUT, 1, "to_f64",
                     [&] { return launch_to_f64(st->P, st->d_psi, static_cast<double*>(dev_out), st->size, st->stream); });
         if (rc) return rc;

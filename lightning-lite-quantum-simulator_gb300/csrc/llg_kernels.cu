@@ -166,7 +166,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 }
 
 template <class P>
-__global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, PassDesc pd, const ExecOp* __restrict__ ops) {
+__global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, PassDesc pd, const ExecOp* __restrict__ ops,
+                                               double2* __restrict__ mirror) {
     using S = typename P::S;
     using K = typename P::K;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -295,10 +296,15 @@ __global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, 
                          "r"(smem_addr(tile + ((size_t)h << low))), "r"(run_bytes)
                          : "memory");
         asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // the tile is read before the CTA exits
     } else {
         for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) psi[base | hi_off[l >> low] | (l & lowmask)] = tile[l];
     }
+    // the last pass before a host readback also writes the amplitudes, as FP64, into the mapped
+    // host buffer (while the copy engine of the bulk stores still reads the tile)
+    if (mirror)
+        for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x)
+            mirror[base | hi_off[l >> low] | (l & lowmask)] = P::to_f64(P::load(tile[l]));
+    if (bulk) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // the tile is read before the CTA exits
 }
 
 // ------------------------------------------------------------------------------------------
@@ -460,7 +466,8 @@ size_t tile_smem_bytes(int t, int low) {
 }
 
 template <class P>
-cudaError_t tile_pass_t(void* vpsi, int n, const PassDesc& pd, const ExecOp* d_ops, int threads, cudaStream_t s) {
+cudaError_t tile_pass_t(void* vpsi, int n, const PassDesc& pd, const ExecOp* d_ops, int threads, double* mirror,
+                        cudaStream_t s) {
     static bool attr_set = false;
     const size_t smem = tile_smem_bytes<P>(pd.t, pd.low);
     if (!attr_set) {
@@ -471,7 +478,8 @@ cudaError_t tile_pass_t(void* vpsi, int n, const PassDesc& pd, const ExecOp* d_o
     }
     const uint64_t ntiles = 1ULL << (n - pd.t);
     if (threads <= 0) threads = pd.t >= 10 ? 512 : (pd.t >= 6 ? (1 << (pd.t - 1)) : 32);
-    k_tile<P><<<(unsigned)ntiles, threads, smem, s>>>(static_cast<typename P::S*>(vpsi), pd, d_ops);
+    k_tile<P><<<(unsigned)ntiles, threads, smem, s>>>(static_cast<typename P::S*>(vpsi), pd, d_ops,
+                                                      reinterpret_cast<double2*>(mirror));
     return cudaGetLastError();
 }
 
@@ -527,8 +535,9 @@ int tile_copy_take_error() {
     return h;
 }
 
-cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, int threads, cudaStream_t s) {
-    LLG_DISPATCH(P, return tile_pass_t<Pol>(psi, n, pd, d_ops, threads, s));
+cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, int threads, cudaStream_t s,
+                             double* mirror) {
+    LLG_DISPATCH(P, return tile_pass_t<Pol>(psi, n, pd, d_ops, threads, mirror, s));
 }
 
 template <class PA>

@@ -31,7 +31,10 @@ size_t elem_bytes(int precision);
 cudaError_t launch_init_basis(int P, void* psi, uint64_t size, uint64_t index, cudaStream_t s);
 cudaError_t launch_exec_op(int P, void* psi, int n, const ExecOp& op, cudaStream_t s);
 // threads: CTA size of the tile kernel (0: 512 for tiles of 10+ qubits, else half the tile)
-cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, int threads, cudaStream_t s);
+// mirror: nullptr, or the device address of a host buffer that also receives the pass's output as
+// FP64 (2 doubles per amplitude, full-state indexing)
+cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, int threads, cudaStream_t s,
+                             double* mirror = nullptr);
 // 1 if a tile pass's bulk load timed out since the last call (the flag is cleared)
 int tile_copy_take_error();
 cudaError_t launch_from_f64(int P, const double* src, void* dst, uint64_t count, cudaStream_t s);

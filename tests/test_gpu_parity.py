@@ -208,6 +208,34 @@ def test_pinned_and_pageable_readback_agree(precision):
         st.close()
 
 
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_readback_fused_into_last_pass(precision):
+    """get_numpy_view with gates still queued: the last tile pass writes the pinned mirror as it
+    stores its tiles.  Same bits as flushing first and converting afterwards."""
+    import quantum_sim_v3
+
+    n = 14
+    ops = workloads.layered_rotations(n, 3)
+    a = quantum_sim_v3.StateVector(n, precision)
+    a.set_fusion("tile", 10)
+    a.apply_ops(ops)
+    fused = a.get_numpy_view().copy()
+    b = quantum_sim_v3.StateVector(n, precision)
+    b.set_fusion("tile", 10)
+    b.apply_ops(ops)
+    b.flush()
+    flushed = b.get_numpy_view().copy()
+    assert np.array_equal(fused, flushed)
+    tol = 1e-12 if precision != "complex64" else 1e-5
+    assert np.max(np.abs(fused - oracle.run_ops(n, ops))) <= tol
+    assert np.array_equal(a.get_numpy_view(), fused)  # nothing queued: the plain conversion
+    # the mirror stays in step with gates applied after a fused readback
+    a.apply_ops(ops)
+    b.apply_ops(ops)
+    b.flush()
+    assert np.array_equal(a.get_numpy_view(), b.get_numpy_view())
+
+
 @pytest.mark.parametrize("precision", ["complex128", "fp64"])
 def test_every_gate_kind_both_paths(precision):
     rng = np.random.default_rng(8)
