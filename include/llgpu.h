@@ -165,6 +165,17 @@ int llg_apply_ops(llg_state* st, const llg_op* ops, int nops);
  * the block's local index.  k in [1, 5], distinct qubits in [0, n). */
 int llg_apply_matrix(llg_state* st, int k, const int* qubits, const double* m);
 
+/* Other names of four entry points above, for FFI bindings written against them:
+ *   llg_wrap_host      = llg_create_from_host (the ndarray constructor, copied, not aliased);
+ *   llg_apply_1q       = llg_apply_gate with ll::Backend validation: a qubit outside [0, n) is
+ *                        LLG_EINVAL instead of the v3 no-op (src/StateVectorBackend.h:176-186);
+ *   llg_apply_block    = llg_apply_matrix;
+ *   llg_expect_diag_zz = llg_expect_zz. */
+int llg_wrap_host(const double* amps, size_t len, int precision, llg_state** out);
+int llg_apply_1q(llg_state* st, int q, const double* m);
+int llg_apply_block(llg_state* st, int k, const int* qubits, const double* m);
+int llg_expect_diag_zz(llg_state* st, int nterms, const int* a, const int* b, const double* coeff, double* out);
+
 /* ---- density matrices (the reference's KrausChannel, src/Noise.h:85-147) ----
  * rho on n qubits lives in a state of 2n qubits: element (row, col) is amplitude
  * row + col * 2^n, so qubit q is bit q of the row and qubit n + q bit q of the column.  Create it

@@ -535,6 +535,22 @@ int llg_apply_ops(llg_state* st, const llg_op* ops, int nops) {
     return LLG_OK;
 }
 
+int llg_wrap_host(const double* amps, size_t len, int precision, llg_state** out) {
+    return llg_create_from_host(amps, len, precision, out);
+}
+
+int llg_apply_1q(llg_state* st, int q, const double* m) {
+    if (!st || !m) return set_error(LLG_EINVAL, "apply_1q: NULL argument");
+    if (int rc = check_qubit(st, q, "StateVectorBackend")) return rc;
+    return llg_apply_gate(st, q, m);
+}
+
+int llg_apply_block(llg_state* st, int k, const int* qubits, const double* m) { return llg_apply_matrix(st, k, qubits, m); }
+
+int llg_expect_diag_zz(llg_state* st, int nterms, const int* a, const int* b, const double* coeff, double* out) {
+    return llg_expect_zz(st, nterms, a, b, coeff, out);
+}
+
 int llg_apply_matrix(llg_state* st, int k, const int* qubits, const double* m) {
     if (!st || !qubits || !m) return set_error(LLG_EINVAL, "apply_matrix: NULL argument");
     if (k < 1 || k > kMaxBlockQubits || k > st->n)

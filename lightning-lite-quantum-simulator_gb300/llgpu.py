@@ -94,6 +94,10 @@ def lib() -> ctypes.CDLL:
             "llg_mcz": (i, [vp, vp, i]),
             "llg_apply_ops": (i, [vp, vp, i]),
             "llg_apply_matrix": (i, [vp, i, vp, vp]),
+            "llg_wrap_host": (i, [vp, sz, i, P(vp)]),
+            "llg_apply_1q": (i, [vp, i, vp]),
+            "llg_apply_block": (i, [vp, i, vp, vp]),
+            "llg_expect_diag_zz": (i, [vp, i, vp, vp, vp, P(d)]),
             "llg_flush": (i, [vp]),
             "llg_sync": (i, [vp]),
             "llg_copy_to_host": (i, [vp, vp]),

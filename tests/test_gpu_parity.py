@@ -236,6 +236,57 @@ def test_readback_fused_into_last_pass(precision):
     assert np.array_equal(a.get_numpy_view(), b.get_numpy_view())
 
 
+def test_alias_entry_points_match():
+    """llg_wrap_host / llg_apply_1q / llg_apply_block / llg_expect_diag_zz are the primary entry
+    points under other names; llg_apply_1q also rejects a target outside the register."""
+    import ctypes
+
+    L = llgpu.lib()
+    n = 9
+    rng = np.random.default_rng(31)
+    psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    psi /= np.linalg.norm(psi)
+    amps = np.ascontiguousarray(psi.view(np.float64))
+    g = np.array([[np.cos(0.4), -1j * np.sin(0.4)], [-1j * np.sin(0.4), np.cos(0.4)]]).reshape(-1)
+    gd = np.ascontiguousarray(g.view(np.float64))
+    m = np.linalg.qr(rng.normal(size=(8, 8)) + 1j * rng.normal(size=(8, 8)))[0]
+    md = np.ascontiguousarray(m.reshape(-1).view(np.float64))
+    qs = (ctypes.c_int * 3)(1, 4, 7)
+    a, b, c = llgpu.ring_zz_terms(n)
+    ta, tb, tc = (ctypes.c_int * len(a))(*a), (ctypes.c_int * len(b))(*b), (ctypes.c_double * len(c))(*c)
+    out = []
+    for names in (("llg_create_from_host", "llg_apply_gate", "llg_apply_matrix", "llg_expect_zz"),
+                  ("llg_wrap_host", "llg_apply_1q", "llg_apply_block", "llg_expect_diag_zz")):
+        h = ctypes.c_void_p()
+        llgpu.check(getattr(L, names[0])(amps.ctypes.data, 1 << n, 1, ctypes.byref(h)))
+        llgpu.check(getattr(L, names[1])(h, 3, gd.ctypes.data))
+        llgpu.check(getattr(L, names[2])(h, 3, qs, md.ctypes.data))
+        e = ctypes.c_double()
+        llgpu.check(getattr(L, names[3])(h, len(a), ta, tb, tc, ctypes.byref(e)))
+        st = np.zeros(2 << n)
+        llgpu.check(L.llg_copy_to_host(h, st.ctypes.data))
+        if names[1] == "llg_apply_1q":
+            assert L.llg_apply_1q(h, n, gd.ctypes.data) == llgpu.LLG_EINVAL
+            assert L.llg_apply_1q(h, -1, gd.ctypes.data) == llgpu.LLG_EINVAL
+        else:
+            assert L.llg_apply_gate(h, n, gd.ctypes.data) == 0  # v3: a target >= n is a no-op
+        llgpu.check(L.llg_destroy(h))
+        out.append((st, e.value))
+    assert np.array_equal(out[0][0], out[1][0]) and out[0][1] == out[1][1]
+    # and both are the gate, then the block (qubits[0] the low bit of its index), then the energy
+    t = psi.reshape([2] * n)  # axis j is qubit n - 1 - j
+    t = np.moveaxis(np.tensordot(g.reshape(2, 2), t, axes=([1], [n - 1 - 3])), 0, n - 1 - 3)
+    ax = [n - 1 - 7, n - 1 - 4, n - 1 - 1]
+    u = np.moveaxis(t, ax, [0, 1, 2]).reshape(8, -1)
+    t = np.moveaxis((m @ u).reshape([2, 2, 2] + [2] * (n - 3)), [0, 1, 2], ax)
+    want = t.reshape(-1)
+    assert np.max(np.abs(out[0][0].view(np.complex128) - want)) <= 1e-12
+    idx = np.arange(1 << n)
+    z = lambda q: 1 - 2 * ((idx >> q) & 1)
+    diag = sum(ck * z(ak) * (z(bk) if bk >= 0 else 1) for ak, bk, ck in zip(a, b, c))
+    assert abs(out[0][1] - float(np.sum(np.abs(want) ** 2 * diag))) <= 1e-11
+
+
 @pytest.mark.parametrize("precision", ["complex128", "fp64"])
 def test_every_gate_kind_both_paths(precision):
     rng = np.random.default_rng(8)
