@@ -171,7 +171,11 @@ __global__ void __launch_bounds__(TcShape<KQ>::kThreads, TcShape<KQ>::kMinBlocks
         float mx = 0.0f;
 #pragma unroll
         for (int i = 0; i < kPer; ++i) {
-            a[i] = sIn[(kPer * h + i) * kTcGroups + gl];
+            // stored pairs may be unnormalised (|lo| above half an ulp of hi): TwoSum makes hi the
+            // leading part, which the scale and the split into slices below rely on
+            const float4 v = sIn[(kPer * h + i) * kTcGroups + gl];
+            const df re = two_sum(v.x, v.z), im = two_sum(v.y, v.w);
+            a[i] = make_float4(re.hi, im.hi, re.lo, im.lo);
             mx = fmaxf(mx, fmaxf(fabsf(a[i].x), fabsf(a[i].y)));
         }
         if (h == 0) eg_s[gl] = 0;

@@ -107,6 +107,20 @@ __device__ __forceinline__ df df_fma(df a, df y, df x) {
     return fast_two_sum(s.hi, t);
 }
 
+// x + a*y without the final renormalisation (12 FP32 instructions): the same value as df_fma,
+// with |lo| possibly above half an ulp of hi.  Amplitudes stored this way stay exact sums hi + lo;
+// every later use takes lo in full (the cross terms of the products, TwoSum of the high parts),
+// so an operation's error stays a few 2^-46 of its inputs' scale.
+__device__ __forceinline__ df df_fma_raw(df a, df y, df x) {
+    const float p = __fmul_rn(a.hi, y.hi);
+    const float e = fmaf(a.hi, y.hi, -p);
+    const df s = two_sum(x.hi, p);
+    float t = __fadd_rn(e, x.lo);
+    t = fmaf(a.hi, y.lo, t);
+    t = fmaf(a.lo, y.hi, t);
+    return {s.hi, __fadd_rn(t, s.lo)};
+}
+
 // a*x + b*y + c*z + d*w
 __device__ __forceinline__ df df_lin4(df a, df x, df b, df y, df c, df z, df d, df w) {
     const float p1 = __fmul_rn(a.hi, x.hi);
@@ -181,6 +195,7 @@ struct PolF64 {
     __device__ static R lin2(K a, R x, K b, R y) { return fma(a, x, b * y); }
     __device__ static R lin2_raw(K a, R x, K b, R y) { return fma(a, x, b * y); }
     __device__ static R fma1(K a, R y, R x) { return fma(a, y, x); }
+    __device__ static R fma1_raw(K a, R y, R x) { return fma(a, y, x); }
     __device__ static R lin4(K a, R x, K b, R y, K c, R z, K d, R w) {
         return fma(a, x, fma(b, y, fma(c, z, d * w)));
     }
@@ -217,6 +232,7 @@ struct PolF32 {
     __device__ static R lin2(K a, R x, K b, R y) { return fmaf(a, x, b * y); }
     __device__ static R lin2_raw(K a, R x, K b, R y) { return fmaf(a, x, b * y); }
     __device__ static R fma1(K a, R y, R x) { return fmaf(a, y, x); }
+    __device__ static R fma1_raw(K a, R y, R x) { return fmaf(a, y, x); }
     __device__ static R lin4(K a, R x, K b, R y, K c, R z, K d, R w) {
         return fmaf(a, x, fmaf(b, y, fmaf(c, z, d * w)));
     }
@@ -272,6 +288,7 @@ struct PolDF64 {
     __device__ static R lin2(K a, R x, K b, R y) { return df_lin2(a, x, b, y); }
     __device__ static R lin2_raw(K a, R x, K b, R y) { return df_lin2_raw(a, x, b, y); }
     __device__ static R fma1(K a, R y, R x) { return df_fma(a, y, x); }  // x + a*y
+    __device__ static R fma1_raw(K a, R y, R x) { return df_fma_raw(a, y, x); }
     __device__ static R lin4(K a, R x, K b, R y, K c, R z, K d, R w) { return df_lin4(a, x, b, y, c, z, d, w); }
     __device__ static R add(R x, R y) { return df_add(x, y); }
     __device__ static R neg(R x) { return df_neg(x); }

@@ -56,30 +56,30 @@ struct PairMath {
             const auto ui = P::lin2(s, y0, c, ti);
             a1.re = P::lin2(ar, ur, P::kneg(ai), ui);  // ea * u
             a1.im = P::lin2(ar, ui, ai, ur);
-        } else if (KIND == EX_ZY) {  // [c, -s; s, c] diag(1, eg)
+        } else if (KIND == EX_ZY) {  // [c, -s; s, c] diag(1, eg); results stored unnormalised
             const auto gr = k[0], gi = k[1], c = k[2], s = k[3];
-            const auto tr = P::lin2(gr, x1, P::kneg(gi), y1);  // eg * a1
-            const auto ti = P::lin2(gr, y1, gi, x1);
-            a0.re = P::lin2(c, x0, P::kneg(s), tr);
-            a0.im = P::lin2(c, y0, P::kneg(s), ti);
-            a1.re = P::lin2(s, x0, c, tr);
-            a1.im = P::lin2(s, y0, c, ti);
-        } else if (KIND == EX_ZT) {  // [1, -t; t, 1] diag(1, eg)
+            const auto tr = P::lin2_raw(gr, x1, P::kneg(gi), y1);  // eg * a1
+            const auto ti = P::lin2_raw(gr, y1, gi, x1);
+            a0.re = P::lin2_raw(c, x0, P::kneg(s), tr);
+            a0.im = P::lin2_raw(c, y0, P::kneg(s), ti);
+            a1.re = P::lin2_raw(s, x0, c, tr);
+            a1.im = P::lin2_raw(s, y0, c, ti);
+        } else if (KIND == EX_ZT) {  // [1, -t; t, 1] diag(1, eg); results stored unnormalised
             const auto gr = k[0], gi = k[1], t = k[2];
             const auto zr = P::lin2_raw(gr, x1, P::kneg(gi), y1);  // z = eg * a1
             const auto zi = P::lin2_raw(gr, y1, gi, x1);
-            a0.re = P::fma1(P::kneg(t), zr, x0);
-            a0.im = P::fma1(P::kneg(t), zi, y0);
-            a1.re = P::fma1(t, x0, zr);
-            a1.im = P::fma1(t, y0, zi);
-        } else if (KIND == EX_ZC) {  // [u, -1; 1, u] diag(1, eg)
+            a0.re = P::fma1_raw(P::kneg(t), zr, x0);
+            a0.im = P::fma1_raw(P::kneg(t), zi, y0);
+            a1.re = P::fma1_raw(t, x0, zr);
+            a1.im = P::fma1_raw(t, y0, zi);
+        } else if (KIND == EX_ZC) {  // [u, -1; 1, u] diag(1, eg); results stored unnormalised
             const auto gr = k[0], gi = k[1], u = k[2];
             const auto zr = P::lin2_raw(gr, x1, P::kneg(gi), y1);
             const auto zi = P::lin2_raw(gr, y1, gi, x1);
-            a0.re = P::fma1(u, x0, P::neg(zr));
-            a0.im = P::fma1(u, y0, P::neg(zi));
-            a1.re = P::fma1(u, zr, x0);
-            a1.im = P::fma1(u, zi, y0);
+            a0.re = P::fma1_raw(u, x0, P::neg(zr));
+            a0.im = P::fma1_raw(u, y0, P::neg(zi));
+            a1.re = P::fma1_raw(u, zr, x0);
+            a1.im = P::fma1_raw(u, zi, y0);
         } else if (KIND == EX_H) {  // r [1, 1; 1, -1]
             const auto r = k[0], mr = P::kneg(k[0]);
             a0.re = P::lin2(r, x0, r, x1);
