@@ -335,19 +335,19 @@ def run_ours(args, rank, world, local):
 
 
 # FP32 lane instructions per amplitude pair of each executor op kind (0 U2, 1 RX, 2 RY, 3 H, 4 X,
-# 5 DIAG, 6 CNOT, 7 MCZ), counted from the double-float routines of the kernels: a 4-term
-# double-float dot product (df_lin4) is 43 instructions (4 FMUL + 4 FFMA product errors, 3 TwoSum
-# of 6, 8 FFMA cross terms, 6 FADD, Fast2Sum of 3), a 2-term one (df_lin2) 19; a U2 pair needs four
-# 4-term products, RX/RY/H four 2-term ones, a diagonal two 2-term ones per amplitude, a ZYZ
-# (phase-free unitary) eight 2-term ones, a carried-phase flush (13) two per amplitude pair; a CNOT
-# carrying a pushed phase multiplies a quarter of the amplitudes.  A ZY (RY after an input phase)
-# is six 2-term products stored without the final Fast2Sum (16 each), a tangent-form rotation
-# (14, 15) two such products and four x + a*y updates without it (12 each).
-# CNOT, MCZ and X otherwise move or negate data without arithmetic.
-FP32_INST_PER_PAIR = {"complex128": {0: 172, 1: 76, 2: 76, 3: 76, 4: 0, 5: 76, 6: 0, 7: 0, 11: 152, 12: 96, 13: 38, 14: 80,
+# 5 DIAG, 6 CNOT, 7 MCZ), counted from the double-float routines of the kernels.  Results are stored
+# without the closing Fast2Sum: a 4-term double-float dot product (df_lin4_raw) is 40 instructions
+# (4 FMUL + 4 FFMA product errors, 3 TwoSum of 6, 8 FFMA cross terms, 6 FADD), a 2-term one
+# (df_lin2_raw) 16, an x + a*y update (df_fma_raw) 12.  A U2 pair needs four 4-term products;
+# RX/RY/H four 2-term ones; a diagonal two 2-term ones per amplitude; a ZYZ (phase-free unitary)
+# eight; a ZY (RY after an input phase) six; a carried-phase flush (13) two per amplitude pair; a
+# tangent-form rotation (14, 15) two 2-term products and four updates.  A CNOT carrying a pushed
+# phase multiplies a quarter of the amplitudes.  CNOT, MCZ and X otherwise move or negate data
+# without arithmetic.
+FP32_INST_PER_PAIR = {"complex128": {0: 160, 1: 64, 2: 64, 3: 64, 4: 0, 5: 64, 6: 0, 7: 0, 11: 128, 12: 96, 13: 32, 14: 80,
                                      15: 80},
                       "complex64": {0: 16, 1: 8, 2: 8, 3: 8, 4: 0, 5: 8, 6: 0, 7: 0, 11: 16, 12: 12, 13: 4, 14: 8, 15: 8}}
-PHASED_CNOT_PER_PAIR = {"complex128": 19, "complex64": 2}  # a complex multiply on a quarter of the amplitudes
+PHASED_CNOT_PER_PAIR = {"complex128": 16, "complex64": 2}  # a complex multiply on a quarter of the amplitudes
 SMS, FP32_LANES_PER_SM = 152, 128
 
 

@@ -62,25 +62,14 @@ __device__ __forceinline__ df df_mul(df a, df b) {
     return fast_two_sum(p, e);
 }
 
-// a*x + b*y with one rounding of the high parts removed by TwoSum.
-__device__ __forceinline__ df df_lin2(df a, df x, df b, df y) {
-    const float p1 = __fmul_rn(a.hi, x.hi);
-    const float e1 = fmaf(a.hi, x.hi, -p1);
-    const float p2 = __fmul_rn(b.hi, y.hi);
-    const float e2 = fmaf(b.hi, y.hi, -p2);
-    const df s = two_sum(p1, p2);
-    float t = __fadd_rn(e1, e2);
-    t = fmaf(a.hi, x.lo, t);
-    t = fmaf(a.lo, x.hi, t);
-    t = fmaf(b.hi, y.lo, t);
-    t = fmaf(b.lo, y.hi, t);
-    t = __fadd_rn(t, s.lo);
-    return fast_two_sum(s.hi, t);
-}
+// The products below come in two forms.  The _raw form stops before the closing Fast2Sum: hi + lo
+// is the same value, but |lo| may exceed half an ulp of hi.  Amplitudes stored that way stay exact
+// sums hi + lo, and every later use takes lo in full (the cross terms of the products, TwoSum of
+// the high parts, hi + lo in FP64, the Dot2 and norm accumulators), so an operation's error stays
+// a few 2^-46 of its inputs' scale.  Code that splits hi and lo separately against a scale taken
+// from hi renormalises first.
 
-// a*x + b*y without the final renormalisation: hi + lo is the same value, but |lo| may exceed
-// half an ulp of hi.  Only for intermediates that feed the products of df_fma / df_lin2 (their
-// cross terms use lo in full), so the absolute error stays a few 2^-48 of the inputs' scale.
+// a*x + b*y with one rounding of the high parts removed by TwoSum (16 FP32 instructions raw)
 __device__ __forceinline__ df df_lin2_raw(df a, df x, df b, df y) {
     const float p1 = __fmul_rn(a.hi, x.hi);
     const float e1 = fmaf(a.hi, x.hi, -p1);
@@ -94,23 +83,12 @@ __device__ __forceinline__ df df_lin2_raw(df a, df x, df b, df y) {
     t = fmaf(b.lo, y.hi, t);
     return {s.hi, __fadd_rn(t, s.lo)};
 }
-
-// x + a*y (15 FP32 instructions against 19 for df_lin2)
-__device__ __forceinline__ df df_fma(df a, df y, df x) {
-    const float p = __fmul_rn(a.hi, y.hi);
-    const float e = fmaf(a.hi, y.hi, -p);
-    const df s = two_sum(x.hi, p);
-    float t = __fadd_rn(e, x.lo);
-    t = fmaf(a.hi, y.lo, t);
-    t = fmaf(a.lo, y.hi, t);
-    t = __fadd_rn(t, s.lo);
-    return fast_two_sum(s.hi, t);
+__device__ __forceinline__ df df_lin2(df a, df x, df b, df y) {
+    const df r = df_lin2_raw(a, x, b, y);
+    return fast_two_sum(r.hi, r.lo);
 }
 
-// x + a*y without the final renormalisation (12 FP32 instructions): the same value as df_fma,
-// with |lo| possibly above half an ulp of hi.  Amplitudes stored this way stay exact sums hi + lo;
-// every later use takes lo in full (the cross terms of the products, TwoSum of the high parts),
-// so an operation's error stays a few 2^-46 of its inputs' scale.
+// x + a*y (12 FP32 instructions raw, 15 renormalised, against 19 for df_lin2)
 __device__ __forceinline__ df df_fma_raw(df a, df y, df x) {
     const float p = __fmul_rn(a.hi, y.hi);
     const float e = fmaf(a.hi, y.hi, -p);
@@ -120,9 +98,13 @@ __device__ __forceinline__ df df_fma_raw(df a, df y, df x) {
     t = fmaf(a.lo, y.hi, t);
     return {s.hi, __fadd_rn(t, s.lo)};
 }
+__device__ __forceinline__ df df_fma(df a, df y, df x) {
+    const df r = df_fma_raw(a, y, x);
+    return fast_two_sum(r.hi, r.lo);
+}
 
-// a*x + b*y + c*z + d*w
-__device__ __forceinline__ df df_lin4(df a, df x, df b, df y, df c, df z, df d, df w) {
+// a*x + b*y + c*z + d*w (40 FP32 instructions raw)
+__device__ __forceinline__ df df_lin4_raw(df a, df x, df b, df y, df c, df z, df d, df w) {
     const float p1 = __fmul_rn(a.hi, x.hi);
     const float e1 = fmaf(a.hi, x.hi, -p1);
     const float p2 = __fmul_rn(b.hi, y.hi);
@@ -143,8 +125,11 @@ __device__ __forceinline__ df df_lin4(df a, df x, df b, df y, df c, df z, df d, 
     t = fmaf(c.lo, z.hi, t);
     t = fmaf(d.hi, w.lo, t);
     t = fmaf(d.lo, w.hi, t);
-    t = __fadd_rn(t, __fadd_rn(s.lo, __fadd_rn(s12.lo, s34.lo)));
-    return fast_two_sum(s.hi, t);
+    return {s.hi, __fadd_rn(t, __fadd_rn(s.lo, __fadd_rn(s12.lo, s34.lo)))};
+}
+__device__ __forceinline__ df df_lin4(df a, df x, df b, df y, df c, df z, df d, df w) {
+    const df r = df_lin4_raw(a, x, b, y, c, z, d, w);
+    return fast_two_sum(r.hi, r.lo);
 }
 
 // Dot2 accumulator (Ogita, Rump and Oishi, SIAM J. Sci. Comput. 2005): s + e carries a sum of
@@ -199,6 +184,7 @@ struct PolF64 {
     __device__ static R lin4(K a, R x, K b, R y, K c, R z, K d, R w) {
         return fma(a, x, fma(b, y, fma(c, z, d * w)));
     }
+    __device__ static R lin4_raw(K a, R x, K b, R y, K c, R z, K d, R w) { return lin4(a, x, b, y, c, z, d, w); }
     __device__ static R add(R x, R y) { return x + y; }
     __device__ static R neg(R x) { return -x; }
     __device__ static K kneg(K x) { return -x; }
@@ -236,6 +222,7 @@ struct PolF32 {
     __device__ static R lin4(K a, R x, K b, R y, K c, R z, K d, R w) {
         return fmaf(a, x, fmaf(b, y, fmaf(c, z, d * w)));
     }
+    __device__ static R lin4_raw(K a, R x, K b, R y, K c, R z, K d, R w) { return lin4(a, x, b, y, c, z, d, w); }
     __device__ static R add(R x, R y) { return x + y; }
     __device__ static R neg(R x) { return -x; }
     __device__ static K kneg(K x) { return -x; }
@@ -290,6 +277,9 @@ struct PolDF64 {
     __device__ static R fma1(K a, R y, R x) { return df_fma(a, y, x); }  // x + a*y
     __device__ static R fma1_raw(K a, R y, R x) { return df_fma_raw(a, y, x); }
     __device__ static R lin4(K a, R x, K b, R y, K c, R z, K d, R w) { return df_lin4(a, x, b, y, c, z, d, w); }
+    __device__ static R lin4_raw(K a, R x, K b, R y, K c, R z, K d, R w) {
+        return df_lin4_raw(a, x, b, y, c, z, d, w);
+    }
     __device__ static R add(R x, R y) { return df_add(x, y); }
     __device__ static R neg(R x) { return df_neg(x); }
     __device__ static K kneg(K x) { return df_neg(x); }

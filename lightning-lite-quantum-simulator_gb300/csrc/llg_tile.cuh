@@ -26,37 +26,38 @@ struct PairMath {
             k[7] = P::kneg(k[7]);
         }
     }
+    // Results are stored unnormalised (the _raw double-float forms; the same values, lo in full).
     __device__ __forceinline__ void apply(C& a0, C& a1) const {
         const auto x0 = a0.re, y0 = a0.im, x1 = a1.re, y1 = a1.im;
         if (KIND == EX_U2) {
             // k[0] = g00r, k[1] = -g00i, k[2] = g01r, k[3] = -g01i, ...
-            a0.re = P::lin4(k[0], x0, k[1], y0, k[2], x1, k[3], y1);
-            a0.im = P::lin4(k[0], y0, P::kneg(k[1]), x0, k[2], y1, P::kneg(k[3]), x1);
-            a1.re = P::lin4(k[4], x0, k[5], y0, k[6], x1, k[7], y1);
-            a1.im = P::lin4(k[4], y0, P::kneg(k[5]), x0, k[6], y1, P::kneg(k[7]), x1);
+            a0.re = P::lin4_raw(k[0], x0, k[1], y0, k[2], x1, k[3], y1);
+            a0.im = P::lin4_raw(k[0], y0, P::kneg(k[1]), x0, k[2], y1, P::kneg(k[3]), x1);
+            a1.re = P::lin4_raw(k[4], x0, k[5], y0, k[6], x1, k[7], y1);
+            a1.im = P::lin4_raw(k[4], y0, P::kneg(k[5]), x0, k[6], y1, P::kneg(k[7]), x1);
         } else if (KIND == EX_RX) {  // [c, -is; -is, c]
             const auto c = k[0], s = k[1], ms = P::kneg(k[1]);
-            a0.re = P::lin2(c, x0, s, y1);
-            a0.im = P::lin2(c, y0, ms, x1);
-            a1.re = P::lin2(s, y0, c, x1);
-            a1.im = P::lin2(ms, x0, c, y1);
+            a0.re = P::lin2_raw(c, x0, s, y1);
+            a0.im = P::lin2_raw(c, y0, ms, x1);
+            a1.re = P::lin2_raw(s, y0, c, x1);
+            a1.im = P::lin2_raw(ms, x0, c, y1);
         } else if (KIND == EX_RY) {  // [c, -s; s, c]
             const auto c = k[0], s = k[1], ms = P::kneg(k[1]);
-            a0.re = P::lin2(c, x0, ms, x1);
-            a0.im = P::lin2(c, y0, ms, y1);
-            a1.re = P::lin2(s, x0, c, x1);
-            a1.im = P::lin2(s, y0, c, y1);
+            a0.re = P::lin2_raw(c, x0, ms, x1);
+            a0.im = P::lin2_raw(c, y0, ms, y1);
+            a1.re = P::lin2_raw(s, x0, c, x1);
+            a1.im = P::lin2_raw(s, y0, c, y1);
         } else if (KIND == EX_ZYZ) {  // diag(1, ea) [c, -s; s, c] diag(1, eg)
             const auto gr = k[0], gi = k[1], c = k[2], s = k[3], ar = k[4], ai = k[5];
-            const auto tr = P::lin2(gr, x1, P::kneg(gi), y1);  // eg * a1
-            const auto ti = P::lin2(gr, y1, gi, x1);
-            a0.re = P::lin2(c, x0, P::kneg(s), tr);
-            a0.im = P::lin2(c, y0, P::kneg(s), ti);
-            const auto ur = P::lin2(s, x0, c, tr);
-            const auto ui = P::lin2(s, y0, c, ti);
-            a1.re = P::lin2(ar, ur, P::kneg(ai), ui);  // ea * u
-            a1.im = P::lin2(ar, ui, ai, ur);
-        } else if (KIND == EX_ZY) {  // [c, -s; s, c] diag(1, eg); results stored unnormalised
+            const auto tr = P::lin2_raw(gr, x1, P::kneg(gi), y1);  // eg * a1
+            const auto ti = P::lin2_raw(gr, y1, gi, x1);
+            a0.re = P::lin2_raw(c, x0, P::kneg(s), tr);
+            a0.im = P::lin2_raw(c, y0, P::kneg(s), ti);
+            const auto ur = P::lin2_raw(s, x0, c, tr);
+            const auto ui = P::lin2_raw(s, y0, c, ti);
+            a1.re = P::lin2_raw(ar, ur, P::kneg(ai), ui);  // ea * u
+            a1.im = P::lin2_raw(ar, ui, ai, ur);
+        } else if (KIND == EX_ZY) {  // [c, -s; s, c] diag(1, eg)
             const auto gr = k[0], gi = k[1], c = k[2], s = k[3];
             const auto tr = P::lin2_raw(gr, x1, P::kneg(gi), y1);  // eg * a1
             const auto ti = P::lin2_raw(gr, y1, gi, x1);
@@ -64,7 +65,7 @@ struct PairMath {
             a0.im = P::lin2_raw(c, y0, P::kneg(s), ti);
             a1.re = P::lin2_raw(s, x0, c, tr);
             a1.im = P::lin2_raw(s, y0, c, ti);
-        } else if (KIND == EX_ZT) {  // [1, -t; t, 1] diag(1, eg); results stored unnormalised
+        } else if (KIND == EX_ZT) {  // [1, -t; t, 1] diag(1, eg)
             const auto gr = k[0], gi = k[1], t = k[2];
             const auto zr = P::lin2_raw(gr, x1, P::kneg(gi), y1);  // z = eg * a1
             const auto zi = P::lin2_raw(gr, y1, gi, x1);
@@ -72,7 +73,7 @@ struct PairMath {
             a0.im = P::fma1_raw(P::kneg(t), zi, y0);
             a1.re = P::fma1_raw(t, x0, zr);
             a1.im = P::fma1_raw(t, y0, zi);
-        } else if (KIND == EX_ZC) {  // [u, -1; 1, u] diag(1, eg); results stored unnormalised
+        } else if (KIND == EX_ZC) {  // [u, -1; 1, u] diag(1, eg)
             const auto gr = k[0], gi = k[1], u = k[2];
             const auto zr = P::lin2_raw(gr, x1, P::kneg(gi), y1);
             const auto zi = P::lin2_raw(gr, y1, gi, x1);
@@ -82,10 +83,10 @@ struct PairMath {
             a1.im = P::fma1_raw(u, zi, y0);
         } else if (KIND == EX_H) {  // r [1, 1; 1, -1]
             const auto r = k[0], mr = P::kneg(k[0]);
-            a0.re = P::lin2(r, x0, r, x1);
-            a0.im = P::lin2(r, y0, r, y1);
-            a1.re = P::lin2(r, x0, mr, x1);
-            a1.im = P::lin2(r, y0, mr, y1);
+            a0.re = P::lin2_raw(r, x0, r, x1);
+            a0.im = P::lin2_raw(r, y0, r, y1);
+            a1.re = P::lin2_raw(r, x0, mr, x1);
+            a1.im = P::lin2_raw(r, y0, mr, y1);
         } else {  // EX_X
             const C t = a0;
             a0 = a1;
@@ -94,12 +95,12 @@ struct PairMath {
     }
 };
 
-// a <- d * a for a complex constant d = (dr, di)
+// a <- d * a for a complex constant d = (dr, di), stored unnormalised
 template <class P>
 __device__ __forceinline__ void cmul_const(typename P::C& a, typename P::K dr, typename P::K di, typename P::K mdi) {
     const auto x = a.re, y = a.im;
-    a.re = P::lin2(dr, x, mdi, y);
-    a.im = P::lin2(dr, y, di, x);
+    a.re = P::lin2_raw(dr, x, mdi, y);
+    a.im = P::lin2_raw(dr, y, di, x);
 }
 
 // Apply a pair op over the 2^t-amplitude shared-memory tile (pairs along local qubit q).
