@@ -364,12 +364,14 @@ size_t bwd_smem(int t, int low) {
 
 template <class P>
 cudaError_t set_smem_attrs() {
-    static bool done = false;
-    if (done) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_tile_fwd<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem<P>(kAdjTile, 4));
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_tile_bwd<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bwd_smem<P>(kAdjTile, 4));
-    if (e == cudaSuccess) done = true;
+    // once per precision (thread-safe static initialisation)
+    static const cudaError_t e = [] {
+        cudaError_t r = cudaFuncSetAttribute(k_tile_fwd<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)fwd_smem<P>(kAdjTile, 4));
+        if (r == cudaSuccess)
+            r = cudaFuncSetAttribute(k_tile_bwd<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bwd_smem<P>(kAdjTile, 4));
+        return r;
+    }();
     return e;
 }
 

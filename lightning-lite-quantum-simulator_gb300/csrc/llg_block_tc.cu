@@ -334,12 +334,9 @@ __global__ void __launch_bounds__(TcShape<KQ>::kThreads, TcShape<KQ>::kMinBlocks
 template <int KQ>
 cudaError_t launch_tc(void* psi, int n, const BlockDesc& bd, const void* d_weights, cudaStream_t s) {
     using T = TcShape<KQ>;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_block_tc<KQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::kSmem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    // once per block size (thread-safe static initialisation)
+    static const cudaError_t attr = cudaFuncSetAttribute(k_block_tc<KQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::kSmem);
+    if (attr != cudaSuccess) return attr;
     const uint64_t ntiles = (1ULL << (n - KQ)) / kTcGroups;
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);

@@ -678,10 +678,9 @@ int llg_flush(llg_state* st) {
     return st->fuse_mode == LLG_FUSE_TILE ? run_tiles(st, q) : run_streaming(st, q);
 }
 
-int llg_sync(llg_state* st) {
-    int rc = llg_flush(st);
-    if (rc) return rc;
-    LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+// After the state's stream has drained: the timeout flags of the kernels that wait on the
+// asynchronous units (tensor-core products, bulk tile loads), for the launches since the last check.
+static int device_checks(llg_state* st) {
     if (st->block_tc_launched) {
         st->block_tc_launched = false;
         if (block_tc_take_error())
@@ -692,6 +691,13 @@ int llg_sync(llg_state* st) {
         if (tile_copy_take_error()) return set_error(LLG_ECUDA, "tile pass: a bulk tile load timed out");
     }
     return LLG_OK;
+}
+
+int llg_sync(llg_state* st) {
+    int rc = llg_flush(st);
+    if (rc) return rc;
+    LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+    return device_checks(st);
 }
 
 // Device address of pinned, mapped host memory (cudaHostAlloc / cudaHostRegister), else nullptr.
@@ -717,7 +723,7 @@ int llg_copy_to_host(llg_state* st, double* out) {
         if ((rc = run_tiles(st, q, static_cast<double*>(dev_out), &mirrored))) return rc;
         if (mirrored) {
             LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
-            return LLG_OK;
+            return device_checks(st);
         }
     }
     rc = llg_flush(st);
@@ -725,7 +731,7 @@ int llg_copy_to_host(llg_state* st, double* out) {
     if (st->P == LLG_F64) {
         LLG_CUDA(cudaMemcpyAsync(out, st->d_psi, st->size * 16, cudaMemcpyDeviceToHost, st->stream), "cudaMemcpyAsync(D2H)");
         LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
-        return LLG_OK;
+        return device_checks(st);
     }
     // A pinned destination is written by the conversion kernel itself, over the host link: one
     // pass at the link's rate, with no staging copy and no copy-engine step after each chunk.
@@ -734,7 +740,7 @@ int llg_copy_to_host(llg_state* st, double* out) {
                     [&] { return launch_to_f64(st->P, st->d_psi, static_cast<double*>(dev_out), st->size, st->stream); });
         if (rc) return rc;
         LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
-        return LLG_OK;
+        return device_checks(st);
     }
     if ((rc = stage_buffers(st))) return rc;
     const size_t eb = elem_bytes(st->P);
@@ -751,7 +757,7 @@ int llg_copy_to_host(llg_state* st, double* out) {
         LLG_CUDA(cudaEventRecord(st->stage_ev[which], st->stream), "cudaEventRecord");
     }
     LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
-    return LLG_OK;
+    return device_checks(st);
 }
 
 int llg_copy_from_host(llg_state* st, const double* amps) {
@@ -801,7 +807,7 @@ int llg_probabilities(llg_state* st, double* out) {
         LLG_CUDA(cudaEventRecord(st->stage_ev[which], st->stream), "cudaEventRecord");
     }
     LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
-    return LLG_OK;
+    return device_checks(st);
 }
 
 static int build_zterms(int nterms, const int* a, const int* b, const double* coeff, int n, ZTerms& z) {
@@ -838,7 +844,7 @@ static int reduce(llg_state* st, const ZTerms& z, double* slots) {
     LLG_CUDA(cudaMemcpyAsync(slots, st->d_red, sizeof(double) * kRedSlots, cudaMemcpyDeviceToHost, st->stream),
              "cudaMemcpyAsync(D2H)");
     LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
-    return LLG_OK;
+    return device_checks(st);
 }
 
 int llg_compare(llg_state* a, llg_state* b, double* fidelity, double* max_abs_diff) {
@@ -855,6 +861,7 @@ int llg_compare(llg_state* a, llg_state* b, double* fidelity, double* max_abs_di
     LLG_CUDA(cudaMemcpyAsync(part.data(), a->d_partials, part.size() * sizeof(double), cudaMemcpyDeviceToHost, a->stream),
              "cudaMemcpyAsync(D2H)");
     LLG_CUDA(cudaStreamSynchronize(a->stream), "cudaStreamSynchronize");
+    if ((rc = device_checks(a)) || (rc = device_checks(b))) return rc;
     double re = 0.0, im = 0.0, na = 0.0, nb = 0.0, mx = 0.0;
     for (int k = 0; k < nblocks; ++k) {  // fixed order
         re += part[(size_t)k * kRedSlots];

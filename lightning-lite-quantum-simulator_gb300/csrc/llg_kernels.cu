@@ -468,14 +468,11 @@ size_t tile_smem_bytes(int t, int low) {
 template <class P>
 cudaError_t tile_pass_t(void* vpsi, int n, const PassDesc& pd, const ExecOp* d_ops, int threads, double* mirror,
                         cudaStream_t s) {
-    static bool attr_set = false;
+    // the largest dynamic shared memory of any tile, set once (thread-safe static initialisation)
+    static const cudaError_t attr = cudaFuncSetAttribute(k_tile<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                         (int)tile_smem_bytes<P>(tile_max_qubits(P::kPrecision), 4));
+    if (attr != cudaSuccess) return attr;
     const size_t smem = tile_smem_bytes<P>(pd.t, pd.low);
-    if (!attr_set) {
-        const size_t maxs = tile_smem_bytes<P>(tile_max_qubits(P::kPrecision), 4);
-        cudaError_t e = cudaFuncSetAttribute(k_tile<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxs);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
     const uint64_t ntiles = 1ULL << (n - pd.t);
     if (threads <= 0) threads = pd.t >= 10 ? 512 : (pd.t >= 6 ? (1 << (pd.t - 1)) : 32);
     k_tile<P><<<(unsigned)ntiles, threads, smem, s>>>(static_cast<typename P::S*>(vpsi), pd, d_ops,
