@@ -481,7 +481,7 @@ def run_sweep_bench(args, torch):
         # dense k-qubit blocks (llg_apply_matrix): 32 B x 2^n per application and 8 x 4^k x 2^(n-k)
         # real FLOP of complex multiply-adds
         rng = np.random.default_rng(17)
-        for k, qs in ((2, [0, n - 1]), (4, [0, 11, 20, n - 1]), (5, [0, 7, 13, 22, n - 1])):
+        for k, qs in ((2, [0, n - 1]), (3, [0, 15, n - 1]), (4, [0, 11, 20, n - 1]), (5, [0, 7, 13, 22, n - 1])):
             m, _ = np.linalg.qr(rng.normal(size=(1 << k, 1 << k)) + 1j * rng.normal(size=(1 << k, 1 << k)))
             st.apply_matrix(qs, m)  # warm-up
             st.sync()

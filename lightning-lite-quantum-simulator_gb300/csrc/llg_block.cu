@@ -2,10 +2,12 @@
 // matrix applied to every group of 2^k amplitudes that differ only in the k target qubits, the
 // fused form of python/gate_fusion.py:7-37 widened to k qubits (k <= 5).
 //
-// One warp holds 32 >> k groups, one lane per row: lane r of a group loads amplitude r (the
-// group's base index with the bits of r deposited at the target positions, bit j -> qubits[j]),
-// then forms row r of M a with the group's amplitudes broadcast by warp shuffles.  The matrix sits
-// in shared memory.  complex128 (double-float) rows are accumulated as exact products summed with
+// k <= 3 (k_group): one thread per group holds its 2^k amplitudes in registers and forms the rows
+// of M a one after another, storing each as it is done; the matrix and the 2^k target offsets are
+// read from shared memory by broadcast.  k = 4, 5 (k_block): one warp holds 32 >> k groups, one
+// lane per row: lane r of a group loads amplitude r (the group's base index with the bits of r
+// deposited at the target positions, bit j -> qubits[j]), then forms row r of M a with the group's
+// amplitudes broadcast by warp shuffles; the matrix sits in shared memory.  complex128 (double-float) rows are accumulated as exact products summed with
 // TwoSum (the Dot2 scheme of Ogita, Rump and Oishi, SIAM J. Sci. Comput. 2005) and rounded once to
 // double-float; FP64 and complex64 rows use fused multiply-adds.
 #include <cuda_runtime.h>
@@ -91,8 +93,68 @@ __global__ void __launch_bounds__(kBlockThreads) k_block(typename P::S* __restri
     }
 }
 
+template <class P, int K>
+__global__ void __launch_bounds__(kBlockThreads) k_group(typename P::S* __restrict__ psi, int n, BlockDesc bd,
+                                                         const uint64_t* __restrict__ mat) {
+    using Kt = typename P::K;
+    using C = typename P::C;
+    using D = typename DotOf<P>::T;
+    constexpr int A = 1 << K;
+    __shared__ Kt sm[2 * A * A];  // row-major (re, im)
+    __shared__ uint64_t soff[A];  // the bits of j deposited at the target qubits
+    for (int i = threadIdx.x; i < 2 * A * A; i += blockDim.x) sm[i] = P::k_from_bits(mat[i]);
+    for (int j = threadIdx.x; j < A; j += blockDim.x) {
+        uint64_t off = 0;
+        for (int b = 0; b < K; ++b)
+            if ((j >> b) & 1) off |= 1ULL << bd.q[b];
+        soff[j] = off;
+    }
+    __syncthreads();
+    const uint64_t ngroups = 1ULL << (n - K);
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += step) {
+        const uint64_t base = insert0_mask(g, bd.tmask);
+        C a[A];
+#pragma unroll
+        for (int j = 0; j < A; ++j) a[j] = P::load(psi[base | soff[j]]);
+        // rows rolled: the matrix is read from shared memory per row instead of being hoisted
+        // into registers for the whole loop over groups
+#pragma unroll 1
+        for (int r = 0; r < A; ++r) {
+            D re, im;
+#pragma unroll
+            for (int j = 0; j < A; ++j) {
+                const Kt mr = sm[2 * (r * A + j)], mi = sm[2 * (r * A + j) + 1];
+                re.add(mr, a[j].re);
+                re.add(P::kneg(mi), a[j].im);
+                im.add(mr, a[j].im);
+                im.add(mi, a[j].re);
+            }
+            C out;
+            out.re = re.value();
+            out.im = im.value();
+            psi[base | soff[r]] = P::store(out);
+        }
+    }
+}
+
+template <class P, int K>
+cudaError_t group_t(void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat, cudaStream_t s) {
+    const uint64_t ngroups = 1ULL << (n - K);
+    const uint64_t blocks = (ngroups + kBlockThreads - 1) / kBlockThreads;
+    const unsigned grid = (unsigned)(blocks < 152ULL * 8 ? blocks : 152ULL * 8);
+    k_group<P, K><<<grid, kBlockThreads, 0, s>>>(static_cast<typename P::S*>(psi), n, bd, d_mat);
+    return cudaGetLastError();
+}
+
 template <class P>
 cudaError_t block_t(void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat, cudaStream_t s) {
+    switch (bd.k) {
+        case 1: return group_t<P, 1>(psi, n, bd, d_mat, s);
+        case 2: return group_t<P, 2>(psi, n, bd, d_mat, s);
+        case 3: return group_t<P, 3>(psi, n, bd, d_mat, s);
+        default: break;
+    }
     const uint64_t ngroups = 1ULL << (n - bd.k);
     const uint64_t warps = (ngroups + (uint64_t)(32 >> bd.k) - 1) / (uint64_t)(32 >> bd.k);
     const uint64_t blocks = (warps + kBlockThreads / 32 - 1) / (kBlockThreads / 32);
