@@ -279,13 +279,14 @@ def run_ours(args, rank, world, local):
     adj = None
     if not args.no_adjoint:
         adj = run_adjoint_bench(args, torch)
-    traj = batch = zne = config1 = tsolver = None
+    traj = batch = zne = config1 = tsolver = dmat = None
     if not args.no_forms:
         traj = run_traj_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
         batch = run_batch_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
         zne = run_zne_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
         config1 = run_config1_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
         tsolver = run_tsolver_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
+        dmat = run_dm_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -330,6 +331,7 @@ def run_ours(args, rank, world, local):
         "zne": zne,
         "config1_12q": config1,
         "trajectory_solver": tsolver,
+        "density_matrix": dmat,
     }
     print(json.dumps(line), flush=True)
 
@@ -719,6 +721,77 @@ def run_zne_bench(args, torch, cpu: bool):
                                "kind": "port", "sample": f"{sample} trajectories per scale, oracle restatement of "
                                                          "NoisyBackend with folding"}
     return res
+
+
+def run_dm_bench(args, torch, cpu: bool):
+    """Density matrices (the reference's KrausChannel::apply, src/Noise.cpp:174-258): rho on n
+    qubits is a 2n-qubit state.  Amplitude damping (gamma 0.01) on every qubit is a 2-qubit block
+    Sum_k K (x) conj(K) on (q, q + n); 2-qubit depolarizing (p 0.01) on (q, q + 1) a 4-qubit block.
+    n = 10 is the reference's limit (MAX_DM_QUBITS, a 16 MiB state); n = 13 is a 1 GiB state, larger
+    than L2.  Algorithmic bytes per channel: 32 B x 4^n (every element read and written)."""
+    import llgpu
+
+    peak, _ = peaks()
+    ad = llgpu.amplitude_damping(0.01)
+    dp = llgpu.depolarizing(0.01, 2)
+    out = {"workload": "density matrices: amplitude damping on every qubit and 2-qubit depolarizing on "
+                       "neighbouring pairs, complex128"}
+    for n in (10, 13):
+        dm = llgpu.DensityMatrix(n, "complex128")
+        dm.apply_ops(llgpu.make_ops([(llgpu.OP_H, q) for q in range(n)] + [(llgpu.OP_RX, q, 0, 0.3 * q) for q in range(n)]))
+        st = dm._st
+        res = {"state_bytes": 16 << (2 * n)}
+        for name, kops, tg in (("amplitude_damping_1q", ad, [[q] for q in range(n)]),
+                               ("depolarizing_2q", dp, [[q, q + 1] for q in range(n - 1)])):
+            for t in tg[:2]:
+                dm.kraus(kops, t)  # warm-up
+            st.sync()
+            st.profile(True)
+            st.profile_read(reset=True)
+            t0 = time.perf_counter()
+            reps = 3
+            for _ in range(reps):
+                for t in tg:
+                    dm.kraus(kops, t)
+            st.sync()
+            wall = time.perf_counter() - t0
+            ms, cnt = st.profile_read(reset=True)["gate"]
+            st.profile(False)
+            per = ms / max(1, cnt) / 1e3
+            gbs = 32 * (1 << (2 * n)) / per / 1e9
+            res[name] = {"channels": reps * len(tg), "kernel_ms_per_channel": per * 1e3,
+                         "channels_per_s_wall": reps * len(tg) / wall, "gbs": gbs, "frac_of_hbm": gbs / peak,
+                         "block_qubits": 2 * len(tg[0])}
+        tr = dm.trace()
+        res["trace_minus_1"] = abs(tr - 1.0)
+        dm.close()
+        out[f"n{n}"] = res
+    if cpu:
+        # the oracle's restatement timed on one channel of each kind at the reference's size; its
+        # result is also compared with the GPU's on the same input
+        import oracle
+
+        n = 10
+        rng = np.random.default_rng(5)
+        a = rng.normal(size=(1 << n, 1 << n)) + 1j * rng.normal(size=(1 << n, 1 << n))
+        rho = a @ a.conj().T
+        rho /= np.trace(rho)
+        dm = llgpu.DensityMatrix(n, "complex128", rho=rho)
+        dm.kraus(ad, [3])
+        dm.kraus(dp, [4, 5])
+        got = dm.rho()
+        dm.close()
+        t0 = time.perf_counter()
+        want = oracle.kraus_apply(rho, n, ad, [3])
+        t1 = time.perf_counter()
+        want = oracle.kraus_apply(want, n, dp, [4, 5])
+        t2 = time.perf_counter()
+        out["max_abs_diff_vs_oracle_n10"] = float(np.max(np.abs(got - want)))
+        out["cpu_baseline"] = {"value": 2.0 / (t2 - t0), "unit": "channels/s", "cores": 1, "kind": "port",
+                               "sample": "one amplitude-damping and one 2-qubit depolarizing channel on a "
+                                         "10-qubit rho, oracle restatement of KrausChannel::apply",
+                               "ms_amplitude_damping": (t1 - t0) * 1e3, "ms_depolarizing_2q": (t2 - t1) * 1e3}
+    return out
 
 
 def run_batch_bench(args, torch, cpu: bool):
