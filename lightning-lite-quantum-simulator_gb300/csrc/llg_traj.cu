@@ -19,7 +19,10 @@
 // CTAs, rank r holding the amplitudes whose top qubit is r.  Gates and Kraus moves on the top
 // qubit read the partner's half through distributed shared memory between cluster barriers; the
 // P1 reduction sums the two halves in a fixed order on both CTAs, so both take the same decision.
-// Every cluster barrier is executed unconditionally in the same sequence by both CTAs.
+// Every cluster barrier is executed unconditionally in the same sequence by both CTAs.  An op that
+// touches only this CTA's half ends in a CTA barrier; an op that reads the partner's half starts
+// with a cluster barrier (the partner has finished its earlier writes), and the exchange words of
+// the reductions alternate between two slots.
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -169,12 +172,13 @@ struct Traj {
     __device__ void pair_gate(int q, const ExecOp& o) {
         if (!cross(q)) {
             tile_pairs<P, KIND>(s, NL >> 1, q, o);
-            group_sync<CL>();
+            __syncthreads();
             return;
         }
         const PairMath<P, KIND> m(o);
         C out[kMaxPerThread];
         int cnt = 0;
+        group_sync<CL>();  // the partner's earlier (CTA-local) writes are complete
         for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x, ++cnt) {
             C mine = P::load(s[l]), other = P::load(remote[l]);
             C a0 = rank ? other : mine, a1 = rank ? mine : other;
@@ -184,7 +188,7 @@ struct Traj {
         group_sync<CL>();  // the partner has read this CTA's half
         cnt = 0;
         for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x, ++cnt) s[l] = P::store(out[cnt]);
-        group_sync<CL>();
+        __syncthreads();
     }
 
     __device__ void gate(const ExecOp& o) {
@@ -205,7 +209,7 @@ struct Traj {
                     else cmul_const<P>(a, d0r, d0i, md0i);
                     s[l] = P::store(a);
                 }
-                group_sync<CL>();
+                __syncthreads();
                 break;
             }
             case EX_CNOT: {
@@ -223,15 +227,16 @@ struct Traj {
                             s[j | tbit] = x;
                         }
                     }
-                    group_sync<CL>();
+                    __syncthreads();
                 } else {  // target is the top qubit: swap the control = 1 halves across the CTAs
                     S out[kMaxPerThread];
                     int cnt = 0;
+                    group_sync<CL>();  // the partner's earlier writes are complete
                     for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x, ++cnt) out[cnt] = ((l >> c) & 1) ? remote[l] : s[l];
                     group_sync<CL>();
                     cnt = 0;
                     for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x, ++cnt) s[l] = out[cnt];
-                    group_sync<CL>();
+                    __syncthreads();
                 }
                 break;
             }
@@ -253,10 +258,10 @@ struct Traj {
                         s[j] = P::store(a);
                     }
                 }
-                group_sync<CL>();
+                __syncthreads();
                 break;
             }
-            default: group_sync<CL>(); break;
+            default: __syncthreads(); break;
         }
     }
 
@@ -280,11 +285,15 @@ struct Traj {
         return group_total(acc_minus(pos, neg), red, slot);
     }
 
-    // group-wide sum of one accumulator per thread, identical in every CTA of the group.  The
-    // caller separates two calls by a group barrier (the partner may still read `slot`).
-    __device__ double group_total(typename P::Acc v, typename P::Acc* red, typename P::Acc* slot) {
+    // group-wide sum of one accumulator per thread, identical in every CTA of the group.  `slot`
+    // is two exchange words used in turn: a CTA writes slot[k % 2] at call k only after the
+    // cluster barrier of call k - 1, which the partner reaches after reading call k - 2's words.
+    int sbuf = 0;
+    __device__ double group_total(typename P::Acc v, typename P::Acc* red, typename P::Acc* slot2) {
         using A = typename P::Acc;
         const A t = block_sum_acc(v, red);
+        A* slot = slot2 + sbuf;
+        sbuf ^= 1;
         if (threadIdx.x == 0) *slot = t;
         group_sync<CL>();
         double total;
@@ -322,7 +331,6 @@ struct Traj {
         double e = 0.0;
         for (int c = 0; c < ob.nclass; ++c) {
             e += ob.coef[c] * group_total(acc[c], red, slot);
-            group_sync<CL>();  // both CTAs have read the slots before the next class reuses them
         }
         return e;
     }
@@ -347,7 +355,7 @@ struct Traj {
                 s[j] = P::store(a);
             }
         }
-        group_sync<CL>();
+        __syncthreads();
     }
 
     // Pauli X on global qubit q: swap the amplitude pairs along q (across the two CTAs for the
@@ -356,6 +364,7 @@ struct Traj {
         if (cross(q)) {
             S out[kMaxPerThread];
             int cnt = 0;
+            group_sync<CL>();  // the partner's earlier writes are complete
             for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x, ++cnt) out[cnt] = remote[l];
             group_sync<CL>();  // both CTAs hold the partner's half
             cnt = 0;
@@ -369,7 +378,7 @@ struct Traj {
                 s[j1] = t;
             }
         }
-        group_sync<CL>();
+        __syncthreads();
     }
 
     // Pauli 1 = X, 2 = Y (Z then X, up to a global phase), 3 = Z
@@ -418,12 +427,13 @@ struct Traj {
                 s[j0] = P::store(t0);
                 s[j1] = P::store(t1);
             }
-            group_sync<CL>();
+            __syncthreads();
             return;
         }
         // top qubit across the cluster: rank 0 holds the bit-0 half, rank 1 the bit-1 half
         C out[kMaxPerThread];
         int cnt = 0;
+        group_sync<CL>();  // the partner's earlier writes are complete
         for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x, ++cnt) {
             C t;
             if (rank == 0) {
@@ -439,7 +449,7 @@ struct Traj {
         group_sync<CL>();
         cnt = 0;
         for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x, ++cnt) s[l] = P::store(out[cnt]);
-        group_sync<CL>();
+        __syncthreads();
     }
 };
 
@@ -491,7 +501,7 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
     using S = typename P::S;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ typename P::Acc red[32];
-    __shared__ typename P::Acc slot;
+    __shared__ typename P::Acc slot[2];  // group_total's exchange words, used in turn
     __shared__ Decision dec;
     __shared__ ObsTerms ob;  // the observable, copied once from global memory
     // uniforms of sites [u_begin, u_end): Kraus mode uni[site - u_begin] = philox_u1(site); depolarizing
@@ -567,7 +577,7 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
             for (int k = 0; k < G.nt; ++k) {
                 const int q = G.q[k];
                 if (site + 1 >= u_end) draw(site);  // AD and PD uniforms of this pair in one chunk
-                const double P1 = T.reduce(q, false, red, &slot);
+                const double P1 = T.reduce(q, false, red, slot);
                 if (threadIdx.x == 0)
                     decide<P>(P1, kp, uni[site - u_begin], uni[site + 1 - u_begin], &dec, &min_margin);
                 __syncthreads();
@@ -579,7 +589,7 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
                 site += 2;
             }
         }
-        const double z = ob.nterms > 0 ? T.observable(ob, red, &slot) : T.reduce(0, true, red, &slot);
+        const double z = ob.nterms > 0 ? T.observable(ob, red, slot) : T.reduce(0, true, red, slot);
         if (threadIdx.x == 0 && T.rank == 0) {
             z0_out[tt] = z;
             if (jumps_out) jumps_out[tt] = jumps;
