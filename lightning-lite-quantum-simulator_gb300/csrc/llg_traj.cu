@@ -456,6 +456,9 @@ struct Traj {
 // thread 0: decide one site pair (AD at a site, PD at the next) from its two uniforms, as the
 // oracle does
 template <class P>
+// The comparisons and p1 (which decides the dephasing jump) are computed exactly as the oracle
+// computes them, in IEEE double with correctly rounded division; the scale factors only rescale
+// amplitudes and use rsqrt (within 1 ulp) instead of a square root and a division.
 __device__ void decide(double P1, const KrausParams& kp, double u1, double u2, Decision* d, double* min_margin) {
     // amplitude damping
     double s_ad = 1.0 - kp.gamma * P1;
@@ -465,12 +468,12 @@ __device__ void decide(double P1, const KrausParams& kp, double u1, double u2, D
     double p1;
     if (u1 >= s_ad && tot_ad > 0.0) {
         d->ad_jump = 1;
-        d->f_ad0 = packk<P>(1.0 / sqrt(P1));
+        d->f_ad0 = packk<P>(rsqrt(P1));
         d->f_ad1 = packk<P>(0.0);
         p1 = 0.0;
     } else {
         d->ad_jump = 0;
-        const double s0 = 1.0 / sqrt(s_ad);
+        const double s0 = rsqrt(s_ad);
         d->f_ad0 = packk<P>(s0);
         d->f_ad1 = packk<P>(kp.sq1mg * s0);
         p1 = (1.0 - kp.gamma) * P1 / s_ad;
@@ -483,10 +486,10 @@ __device__ void decide(double P1, const KrausParams& kp, double u1, double u2, D
     if (u2 >= s_pd && tot_pd > 0.0) {
         d->pd_jump = 1;
         d->f_pd0 = packk<P>(0.0);
-        d->f_pd1 = packk<P>(1.0 / sqrt(p1));
+        d->f_pd1 = packk<P>(rsqrt(p1));
     } else {
         d->pd_jump = 0;
-        const double s0 = 1.0 / sqrt(s_pd);
+        const double s0 = rsqrt(s_pd);
         d->f_pd0 = packk<P>(s0);
         d->f_pd1 = packk<P>(kp.sq1ml * s0);
     }
