@@ -559,10 +559,12 @@ def run_traj_bench(args, torch, cpu: bool):
 
 def run_config1_bench(args, torch, cpu: bool):
     """The published 12-qubit workload: 1000 ops, H (p = 0.5) on a uniform qubit else CNOT on a
-    uniform distinct pair, from |0..0>, amplitudes read back.  The 64 KiB state is one shared-
-    memory tile, so the whole circuit is one launch.  Reported: device time per circuit (CUDA
-    events), end to end through quantum_sim_v3 with the op list in one call and with one Python
-    call per gate (each with the full host readback), and the published reference time."""
+    uniform distinct pair, from |0..0>, amplitudes read back.  The autotuner picks the tile width
+    (the 64 KiB state fits one tile, but 9- or 10-qubit tiles spread each pass over 8 or 4 SMs).
+    Reported: time per circuit between CUDA events on the engine's stream around reset, apply_ops
+    and flush (host planning and launches included), end to end through quantum_sim_v3 with the op
+    list in one call and with one Python call per gate (each with the full host readback), and the
+    published reference time."""
     import llgpu
     import quantum_sim_v3
     import workloads

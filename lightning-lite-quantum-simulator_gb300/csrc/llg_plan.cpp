@@ -263,7 +263,9 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
         std::fill(blocked.begin(), blocked.end(), 0);
         deferred.clear();
         included.clear();
-        for (int idx : remaining) {
+        int nblocked = 0;
+        for (size_t r = 0; r < remaining.size(); ++r) {
+            const int idx = remaining[r];
             const llg_op& op = ops[idx];
             op_qubits(op, touched, need);
             bool is_blocked = false;
@@ -281,7 +283,15 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
                 }
             }
             deferred.push_back(idx);
-            for (int q : touched) blocked[q] = 1;
+            for (int q : touched)
+                if (!blocked[q]) {
+                    blocked[q] = 1;
+                    ++nblocked;
+                }
+            if (nblocked >= n) {  // every qubit is blocked: the rest of the list is deferred as is
+                deferred.insert(deferred.end(), remaining.begin() + (std::ptrdiff_t)r + 1, remaining.end());
+                break;
+            }
         }
 
         // Fill the local set up to t qubits with the lowest unused positions so every pass has
