@@ -257,14 +257,19 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
     std::vector<int> touched, need, deferred, included;
     std::vector<char> blocked(64, 0);
 
-    while (!remaining.empty()) {
+    // remaining[head..] are the ops still to place, in order.  A pass scans a prefix of them; its
+    // deferred ops are written back right-aligned inside that prefix and head moves to the first,
+    // so the unscanned tail is never copied.
+    size_t head = 0;
+    while (head < remaining.size()) {
         uint64_t local = low_mask;
         int local_count = low;
         std::fill(blocked.begin(), blocked.end(), 0);
         deferred.clear();
         included.clear();
         int nblocked = 0;
-        for (size_t r = 0; r < remaining.size(); ++r) {
+        size_t scanned = remaining.size();
+        for (size_t r = head; r < remaining.size(); ++r) {
             const int idx = remaining[r];
             const llg_op& op = ops[idx];
             op_qubits(op, touched, need);
@@ -288,8 +293,8 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
                     blocked[q] = 1;
                     ++nblocked;
                 }
-            if (nblocked >= n) {  // every qubit is blocked: the rest of the list is deferred as is
-                deferred.insert(deferred.end(), remaining.begin() + (std::ptrdiff_t)r + 1, remaining.end());
+            if (nblocked >= n) {  // every qubit is blocked: the rest of the list stays deferred as is
+                scanned = r + 1;
                 break;
             }
         }
@@ -567,7 +572,9 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
             return false;
         }
         out.passes.push_back(pd);
-        remaining.swap(deferred);
+        size_t w = scanned;
+        for (size_t k = deferred.size(); k-- > 0;) remaining[--w] = deferred[k];
+        head = w;
     }
     if (use_zyz && !out.passes.empty()) {
         // the carried phases that reached the end, as diag(1, p) ops in the last pass; the global
