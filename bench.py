@@ -68,10 +68,9 @@ def parse_args():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    import replicas
+
+    return replicas.rank_env()
 
 
 def peaks():
@@ -253,12 +252,14 @@ def run_ours(args, rank, world, local):
     elapsed_ms = ev0.elapsed_time(ev1)
     prof = st.profile_read(reset=True)
     st.profile(False)
-    if world > 1:
-        t = torch.tensor([elapsed_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    # replicas: every rank ran the same circuit on its own state; the job's rate is all ranks'
+    # gates over the slowest rank's time
+    import replicas
+
+    value, slowest_s = replicas.job_rate(ngates * args.steps, elapsed_ms / 1e3,
+                                         torch.distributed if world > 1 else None, device="cuda")
+    elapsed_ms = slowest_s * 1e3
     ms_step = elapsed_ms / args.steps
-    value = ngates * args.steps * world / (elapsed_ms / 1e3)
 
     tile_ms, tile_n = prof["tile"] if prof["tile"][1] else prof["gate"]
     peak, peak_kind = peaks()
