@@ -112,3 +112,22 @@ def test_full_config4_ensemble():
     zo, jo, logo, _ = oracle.traj_run(14, ops, 0.01, 0.005, 2024, 0, 16, log_sites=sites)
     assert np.array_equal(log[:16], logo) and np.max(np.abs(z[:16] - zo)) <= 1e-10
     assert j.sum() > 100
+
+
+def test_shards_reproduce_the_ensemble():
+    """Trajectory i depends only on (seed, i): two shards run separately equal the single run
+    unit for unit, and replicas.traj_ensemble on one process reports the run's moments."""
+    import replicas
+
+    n, total, seed = 12, 300, 31
+    ops = workloads.noisy_layers(n, 3)
+    z_all, j_all, _, _ = llgpu.traj_run(n, ops, 0.02, 0.01, seed, total)
+    b, c = replicas.shard(total, 1, 2)
+    z_lo, j_lo, _, _ = llgpu.traj_run(n, ops, 0.02, 0.01, seed, b, begin=0)
+    z_hi, j_hi, _, _ = llgpu.traj_run(n, ops, 0.02, 0.01, seed, c, begin=b)
+    assert np.array_equal(np.concatenate([z_lo, z_hi]), z_all)
+    assert np.array_equal(np.concatenate([j_lo, j_hi]), j_all)
+    r = replicas.traj_ensemble(n, ops, 0.02, 0.01, seed, total)
+    assert r["trajectories"] == total and r["shard"] == (0, total)
+    assert abs(r["mean_z0"] - float(np.mean(z_all))) <= 1e-14
+    assert abs(r["std_error"] - float(np.std(z_all, ddof=1) / np.sqrt(total))) <= 1e-14
