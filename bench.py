@@ -742,7 +742,7 @@ def run_dm_bench(args, torch, cpu: bool):
     for n in (10, 13):
         dm = llgpu.DensityMatrix(n, "complex128")
         dm.apply_ops(llgpu.make_ops([(llgpu.OP_H, q) for q in range(n)] + [(llgpu.OP_RX, q, 0, 0.3 * q) for q in range(n)]))
-        st = dm._st
+        st = dm.state
         res = {"state_bytes": 16 << (2 * n)}
         for name, kops, tg in (("amplitude_damping_1q", ad, [[q] for q in range(n)]),
                                ("depolarizing_2q", dp, [[q, q + 1] for q in range(n - 1)])):

@@ -667,6 +667,11 @@ class DensityMatrix:
             raise ValueError("KrausChannel: operators must be 2^m x 2^m for m targets")
         check(lib().llg_dm_apply_kraus(self._st.handle, self.n, kk.shape[0], _ptr(kk), tg.size, _ptr(tg)))
 
+    @property
+    def state(self) -> "State":
+        """The 2n-qubit state that holds rho (for sync, profiling and the other State calls)."""
+        return self._st
+
     def rho(self) -> np.ndarray:
         dim = 1 << self.n
         return np.ascontiguousarray(self._st.state().reshape(dim, dim).T)
