@@ -96,6 +96,32 @@ def test_tensor_core_block_edge_values(n, k):
     st.close()
 
 
+@pytest.mark.parametrize("k", [2, 3, 4, 5])
+def test_blocks_after_cancellation(k):
+    """Pairs along qubit 0 equal to 1e-9: after H the differences are stored as unnormalised
+    double-float pairs whose low part outweighs the high part.  Every block kernel (a thread per
+    group for k <= 3, the tensor cores for k = 4, 5 on 12 qubits) must read them at full value."""
+    n = 12
+    rng = np.random.default_rng(700 + k)
+    psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    psi /= np.linalg.norm(psi)
+    even = np.arange(0, 1 << n, 2)
+    psi[even + 1] = psi[even] * (1.0 + 1e-9 * rng.normal(size=even.size))
+    st = llgpu.State(n)
+    st.load(psi)
+    st.set_fusion("tile", 10)
+    ops = llgpu.make_ops([(llgpu.OP_H, 0)])
+    st.apply_ops(ops)
+    want = oracle.run_ops(n, ops, psi)
+    qs = [0, 3, 6, 9, 11][:k]
+    m = rand_unitary(1 << k, rng)
+    st.apply_matrix(qs, m)
+    oracle.apply_matrix(want, n, qs, m)
+    got = st.state()
+    assert np.max(np.abs(got - want)) <= 1e-12 * np.max(np.abs(want))
+    st.close()
+
+
 def test_block_contract():
     st = llgpu.State(4)
     eye = np.eye(4)
