@@ -19,6 +19,13 @@ Printed as one JSON line:
                30-qubit circuit.
 `--impl reference` times that CPU implementation alone as the reference arm.
 
+Beside the headline the line carries, each with its own workload description and, where the
+oracle can run a sample of it, a CPU baseline: per-gate and dense-block sweeps against HBM
+(`gate_sweeps`), adjoint gradients against parameter shift (`adjoint`), noisy trajectories
+(`trajectories`), mixed circuit batches (`mixed_batch`), zero-noise extrapolation (`zne`), the
+12-qubit published workload (`config1_12q`), the dense trajectory solver (`trajectory_solver`) and
+density-matrix channels (`density_matrix`).  `--no-sweeps`, `--no-adjoint`, `--no-forms` skip them.
+
 Multi-GPU: the path does not shard (one state per GPU); with torchrun each rank runs an
 independent replica and `value` sums them ("replicas only", weak scaling).
 """
