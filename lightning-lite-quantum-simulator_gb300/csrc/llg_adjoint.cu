@@ -90,8 +90,8 @@ __global__ void k_coef_table(const double* __restrict__ params, int nparams, con
 
 // One gradient op fused: this thread's part of Im <lambda | P | psi> from the amplitudes before the
 // op, and the op's inverse applied to both tiles in the same loop (each pair or amplitude belongs
-// to one thread, so it reads its values before it overwrites them).  The caller's block sum
-// provides the barrier before the next op.
+// to one thread, so it reads its values before it overwrites them).  The caller reduces the
+// result and provides the barrier before the next op.
 template <class P>
 __device__ typename P::Acc tile_grad_apply(typename P::S* psi, typename P::S* lam, uint32_t tsize, uint64_t base,
                                            const ExecOp& o, const uint64_t* __restrict__ trow) {
@@ -214,8 +214,14 @@ __global__ void __launch_bounds__(512, 2) k_tile_bwd(typename P::S* __restrict__
                                                   const uint64_t* __restrict__ table, int nocc, double* __restrict__ gpart,
                                                   int tiles) {
     using S = typename P::S;
+    using A = typename P::Acc;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ typename P::Acc red[16];
+    // Gradient sums: each warp reduces its part of a parametrised op's inner product with
+    // shuffles and parks it here, so the op ends in one CTA barrier; the sums across warps are
+    // finished for up to kGradBuf ops at once, one thread per op (at most 512 threads, 16 warps).
+    constexpr int kGradBuf = 32;
+    __shared__ A gred[kGradBuf][16];
+    __shared__ int gslot[kGradBuf];
     const int t = pd.t, low = pd.low;
     const uint32_t tsize = 1u << t, nhi = 1u << (t - low);
     S* tp = reinterpret_cast<S*>(smem_raw);
@@ -240,6 +246,14 @@ __global__ void __launch_bounds__(512, 2) k_tile_bwd(typename P::S* __restrict__
         tl[l] = lam[g];
     }
     __syncthreads();
+    int ng = 0;  // buffered gradients (the same count in every thread)
+    auto flush = [&]() {  // after a barrier: the warps' partials of each buffered op, in warp order
+        if ((int)threadIdx.x < ng) {
+            A sum = gred[threadIdx.x][0];
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w) sum = acc_plus(sum, gred[threadIdx.x][w]);
+            gpart[((size_t)b * nocc + gslot[threadIdx.x]) * tiles + blockIdx.x] = acc_value(sum);
+        }
+    };
     __shared__ __align__(16) ExecOp sops[kAdjOpChunk];
     for (int k = 0; k < pd.nops; ++k) {
         if (k % kAdjOpChunk == 0) {
@@ -248,18 +262,25 @@ __global__ void __launch_bounds__(512, 2) k_tile_bwd(typename P::S* __restrict__
         }
         const ExecOp& o = sops[k % kAdjOpChunk];
         if (o.flags & OPF_GRAD) {
-            // inner product and un-application in one loop; the block sum's barriers order the
-            // tile writes before the next op.  The slot is read before them: once they are passed,
-            // the next chunk may be staged over this op's record.
-            const int slot = o.q1;
-            const auto v = block_sum_acc(tile_grad_apply<P>(tp, tl, tsize, base, o, trow), red);
-            if (threadIdx.x == 0) gpart[((size_t)b * nocc + slot) * tiles + blockIdx.x] = acc_value(v);
+            // inner product and un-application in one loop.  The slot is read before the barrier:
+            // once it is passed, the next chunk may be staged over this op's record.
+            const A v = warp_sum_acc(tile_grad_apply<P>(tp, tl, tsize, base, o, trow));
+            if ((threadIdx.x & 31) == 0) gred[ng][threadIdx.x >> 5] = v;
+            if (threadIdx.x == 0) gslot[ng] = o.q1;
+            ++ng;
+            __syncthreads();  // the tile writes before the next op, the partials before a flush
+            if (ng == kGradBuf) {
+                flush();
+                __syncthreads();  // the buffer is read before it is refilled
+                ng = 0;
+            }
             continue;
         }
         tile_apply<P>(tp, tsize, base, o, trow);
         tile_apply<P>(tl, tsize, base, o, trow);
         __syncthreads();
     }
+    flush();  // every op ended in a barrier, so the last partials are visible
     for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
         const uint64_t g = base | hi_off[l >> low] | (l & lowmask);
         psi[g] = tp[l];
