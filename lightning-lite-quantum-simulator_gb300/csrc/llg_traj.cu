@@ -51,6 +51,7 @@ using namespace llg;
 namespace {
 
 constexpr int kTrajThreads = 1024;
+constexpr int kPartWarps = kTrajThreads / 32;  // warp parts per reduction
 constexpr int kMaxPerThread = 16;  // amplitudes per thread in a cross-CTA step (2^14 / 1024)
 constexpr int kMaxGrid = 4096;     // persistent CTAs at most (per-CTA margin slots)
 constexpr int kUChunk = 512;       // noise sites whose uniforms are drawn together (one Philox call per thread)
@@ -267,7 +268,7 @@ struct Traj {
 
     // sum over the group of |a|^2 for amplitudes with (global bit q) == 1 (q < 0: all), or of
     // (1 - 2 bit0)|a|^2 when z0 is set; identical in every CTA of the group
-    __device__ double reduce(int q, bool z0, typename P::Acc* red, typename P::Acc* slot) {
+    __device__ double reduce(int q, bool z0, typename P::Acc* part2) {
         typename P::Acc pos = P::acc_zero(), neg = P::acc_zero();
         if (z0) {
             for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x) {
@@ -282,34 +283,39 @@ struct Traj {
             const uint32_t bit = 1u << q;
             for (uint32_t p = threadIdx.x; p < (NL >> 1); p += blockDim.x) pos = P::acc_norm(pos, P::load(s[ins0(p, bit) | bit]));
         }
-        return group_total(acc_minus(pos, neg), red, slot);
+        return group_total(acc_minus(pos, neg), part2);
     }
 
-    // group-wide sum of one accumulator per thread, identical in every CTA of the group.  `slot`
-    // is two exchange words used in turn: a CTA writes slot[k % 2] at call k only after the
-    // cluster barrier of call k - 1, which the partner reaches after reading call k - 2's words.
+    // group-wide sum of one accumulator per thread, returned in thread 0 (the deciding thread;
+    // other threads get 0).  Each warp parks its shuffle-reduced part in `part`, one group barrier
+    // later warp 0 adds both CTAs' parts warp by warp in rank order and reduces them, so both CTAs
+    // of a cluster get the same bits.  `part2` is two sets of kPartWarps words used in turn: a CTA
+    // writes set k % 2 at call k only after the group barrier of call k - 1, which the partner's
+    // warp 0 reaches after reading call k - 2's words.
     int sbuf = 0;
-    __device__ double group_total(typename P::Acc v, typename P::Acc* red, typename P::Acc* slot2) {
+    __device__ double group_total(typename P::Acc v, typename P::Acc* part2) {
         using A = typename P::Acc;
-        const A t = block_sum_acc(v, red);
-        A* slot = slot2 + sbuf;
+        v = warp_sum_acc(v);
+        A* part = part2 + kPartWarps * sbuf;
         sbuf ^= 1;
-        if (threadIdx.x == 0) *slot = t;
+        const int lane = threadIdx.x & 31, nw = (int)(blockDim.x >> 5);
+        if (lane == 0) part[threadIdx.x >> 5] = v;
         group_sync<CL>();
-        double total;
-        if (CL == 1) {
-            total = acc_value(*slot);
-        } else {
-            cg::cluster_group cl = cg::this_cluster();
-            const A* s0 = cl.map_shared_rank(slot, 0);
-            const A* s1 = cl.map_shared_rank(slot, 1);
-            total = acc_value(acc_plus(*s0, *s1));  // the same order on both CTAs
+        if (threadIdx.x >= 32) return 0.0;
+        A x = P::acc_zero();
+        if (lane < nw) {
+            if (CL == 1) {
+                x = part[lane];
+            } else {
+                cg::cluster_group cl = cg::this_cluster();
+                x = acc_plus(cl.map_shared_rank(part, 0)[lane], cl.map_shared_rank(part, 1)[lane]);
+            }
         }
-        return total;
+        return acc_value(warp_sum_acc(x));
     }
 
     // the observable sum_c coef_c * sum_i |a_i|^2 (tot_c - 2 odd_c(i)) over the group's state
-    __device__ double observable(const ObsTerms& ob, typename P::Acc* red, typename P::Acc* slot) {
+    __device__ double observable(const ObsTerms& ob, typename P::Acc* part2) {
         typename P::Acc acc[kObsClasses];
         int tot[kObsClasses] = {0, 0, 0};
 #pragma unroll
@@ -330,7 +336,7 @@ struct Traj {
         }
         double e = 0.0;
         for (int c = 0; c < ob.nclass; ++c) {
-            e += ob.coef[c] * group_total(acc[c], red, slot);
+            e += ob.coef[c] * group_total(acc[c], part2);
         }
         return e;
     }
@@ -503,8 +509,7 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
                                  uint8_t* __restrict__ jump_log, int64_t log_stride, double* __restrict__ margin_out) {
     using S = typename P::S;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ typename P::Acc red[32];
-    __shared__ typename P::Acc slot[2];  // group_total's exchange words, used in turn
+    __shared__ typename P::Acc part2[2 * kPartWarps];  // group_total's warp parts, two sets used in turn
     __shared__ Decision dec;
     __shared__ ObsTerms ob;  // the observable, copied once from global memory
     // uniforms of sites [u_begin, u_end): Kraus mode uni[site - u_begin] = philox_u1(site); depolarizing
@@ -580,7 +585,7 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
             for (int k = 0; k < G.nt; ++k) {
                 const int q = G.q[k];
                 if (site + 1 >= u_end) draw(site);  // AD and PD uniforms of this pair in one chunk
-                const double P1 = T.reduce(q, false, red, slot);
+                const double P1 = T.reduce(q, false, part2);
                 if (threadIdx.x == 0)
                     decide<P>(P1, kp, uni[site - u_begin], uni[site + 1 - u_begin], &dec, &min_margin);
                 __syncthreads();
@@ -592,7 +597,7 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
                 site += 2;
             }
         }
-        const double z = ob.nterms > 0 ? T.observable(ob, red, slot) : T.reduce(0, true, red, slot);
+        const double z = ob.nterms > 0 ? T.observable(ob, part2) : T.reduce(0, true, part2);
         if (threadIdx.x == 0 && T.rank == 0) {
             z0_out[tt] = z;
             if (jumps_out) jumps_out[tt] = jumps;
