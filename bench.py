@@ -318,7 +318,7 @@ def run_ours(args, rank, world, local):
                                f"passes of {tile_q} qubits", "qubits": n, "layers": args.layers, "gates": ngates,
                    "tile_passes": int(len(passes)), "tile_qubits": tile_q, "precision": args.precision,
                    "fusion": tuning, "autotune": tune,
-                   "l2": "inputs larger than L2 (16 GiB state), no flush needed"},
+                   "l2": f"inputs larger than L2 ({state_bytes / 2**30:g} GiB state), no flush needed"},
         "sweeps_per_s": len(passes) * args.steps * world / (elapsed_ms / 1e3),
         "hbm_gbs_algorithmic": len(passes) * 2 * state_bytes * args.steps * world / (elapsed_ms / 1e3) / 1e9,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
