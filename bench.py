@@ -4,7 +4,8 @@
 Workload (seeded, synthetic): a 30-qubit state from |0..0> (16 GiB of complex128), 20 layers of
 RX, RY, RZ on every qubit (angles U[0, 2pi)) plus a CNOT brickwork on (i, i+1) with alternating
 offsets -- 1800 rotations + 290 CNOTs = 2090 gates.  One step = reset the state and run the whole
-circuit through the engine (fused shared-memory tile passes, complex128 as double-float).
+circuit through the engine: fused shared-memory tile passes with carried phases and phase tables,
+complex128 in IEEE binary64 (the reference's arithmetic).
 
 Printed as one JSON line:
   value        gates/s over the whole job (logical, pre-fusion gates), device-timed with CUDA
@@ -14,17 +15,25 @@ Printed as one JSON line:
   roofline     the dominant kernel (the tile pass): algorithmic bytes per launch (32 B x 2^30
                amplitudes: one read and one write of the state) / its mean launch time, measured
                with CUDA events around every launch inside the timed region;
-  cpu_baseline the reference's per-gate algorithm (the oracle's restatement of
-               ll::StateVectorBackend, OpenMP on every host core) on the first gates of the same
-               30-qubit circuit.
-`--impl reference` times that CPU implementation alone as the reference arm.
+  fp64_roofline the bound that applies to IEEE complex128 on this GPU: the plan's algorithmic FP64
+               multiply-adds per step over the tile passes' time, against the FP64 FMA rate
+               measured live by a throughput kernel;
+  cpu_baseline the reference's CPU algorithms on the machine's host cores (the oracle's restatement,
+               checked bit-exact against the reference build): the per-gate ll::StateVectorBackend
+               path and the fused path (GateFuser.fuse_circuit + apply_gate_cache_optimized), each
+               timed per gate kind on the 30-qubit state and combined over the circuit's gate mix;
+  variants     the same circuit in double-float ("df64") and complex64, each with its rate, e2e,
+               rooflines and its error against the IEEE FP64 state (max |d amp|, relative to the
+               largest amplitude, and 1 - fidelity).
+`--impl reference` times the CPU implementation alone as the reference arm.
 
 Beside the headline the line carries, each with its own workload description and, where the
 oracle can run a sample of it, a CPU baseline: per-gate and dense-block sweeps against HBM
 (`gate_sweeps`), adjoint gradients against parameter shift (`adjoint`), noisy trajectories
 (`trajectories`), mixed circuit batches (`mixed_batch`), zero-noise extrapolation (`zne`), the
 12-qubit published workload (`config1_12q`), the dense trajectory solver (`trajectory_solver`) and
-density-matrix channels (`density_matrix`).  `--no-sweeps`, `--no-adjoint`, `--no-forms` skip them.
+density-matrix channels (`density_matrix`); `summary` at the end repeats their key figures.
+`--no-sweeps`, `--no-adjoint`, `--no-forms`, `--no-variants` skip them.
 
 Multi-GPU: the path does not shard (one state per GPU); with torchrun each rank runs an
 independent replica and `value` sums them ("replicas only", weak scaling).
@@ -51,6 +60,7 @@ import numpy as np  # noqa: E402
 
 METRIC = "30q gates/s"
 FALLBACK_HBM_GBS = 6800.0
+E2E_STEPS_MAX = 5  # the e2e loop and the variants run at most this many steps
 
 
 def parse_args():
@@ -61,13 +71,14 @@ def parse_args():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--qubits", type=int, default=30)
     ap.add_argument("--layers", type=int, default=20)
-    ap.add_argument("--precision", default="complex128")
+    ap.add_argument("--precision", default="complex128",
+                    help="complex128 (IEEE FP64, the reference's arithmetic), df64 or complex64")
     ap.add_argument("--tile", type=int, default=-1,
                     help="tile width in qubits; -1 (default): the autotuner picks width and CTA threads")
     ap.add_argument("--cta-threads", type=int, default=0, help="tile-kernel CTA threads with an explicit --tile")
-    ap.add_argument("--cpu-gates", type=int, default=12, help="gates in each CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-variants", action="store_true", help="skip the df64 / complex64 variants of the headline")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient measurement")
     ap.add_argument("--no-forms", action="store_true", help="skip the trajectory and mixed-batch measurements")
     ap.add_argument("--no-sweeps", action="store_true", help="skip the per-gate sweep roofline measurement")
@@ -141,28 +152,94 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------------------------------
-# CPU side: the reference's per-gate algorithm (oracle restatement), bounded sample
+# CPU side: the reference's algorithms (oracle restatements), timed per gate kind
 # --------------------------------------------------------------------------------------------
-def cpu_sample(n: int, ops: np.ndarray, gates: int, reps: int, warm: int):
-    """Times `gates` gates of the circuit on an n-qubit state with every host core; returns
-    (gates/s best-of, threads, seconds per sample)."""
+def circuit_mix(n: int, ops: np.ndarray) -> dict:
+    """Gate counts of the per-gate path (rotations, CNOTs) and of the reference's fused path
+    (fused 2x2s after GateFuser.fuse_circuit, CNOTs)."""
     import oracle
 
-    threads = os.cpu_count() or 1
+    kinds = ops["kind"]
+    fused = oracle.fuse_gate_list(n, ops)
+    return {"gates": int(len(ops)), "rotations": int(np.sum(np.isin(kinds, (2, 3, 4)))),
+            "cnots": int(np.sum(kinds == 5)), "fused_2x2": sum(1 for f in fused if f[0] == "u2")}
+
+
+def cpu_gate_times(n: int, threads: int, reps: int, kinds=("rx", "ry", "rz", "cnot", "u2")) -> dict:
+    """Best-of-`reps` seconds per gate of each kind on an n-qubit state with `threads` OpenMP
+    threads (after one untimed application of each): RX/RY/RZ/CNOT by the reference's per-gate
+    ll::StateVectorBackend algorithm (src/StateVectorBackend.h:61-135), U2 by
+    apply_gate_cache_optimized (src/StateVectorOptimized.cpp:56-78), as the oracle restates them.
+    Targets spread over the register: rotations on qubits 0, n/2, n-1; CNOTs on (0, 1) and
+    (n-2, n-1), the brickwork's pairs."""
+    import ctypes
+
+    import oracle
+
+    L = oracle.lib()
     oracle.set_threads(threads)
     psi = oracle.zero_state(n)
-    sample = np.ascontiguousarray(ops[:gates])
-    times = []
-    for k in range(warm + reps):
-        t0 = time.perf_counter()
-        rc = oracle.lib().orc_run_ops(psi.ctypes.data, n, sample.ctypes.data, sample.size)
-        t1 = time.perf_counter()
-        if rc:
-            raise RuntimeError("oracle rejected the sample")
-        if k >= warm:
-            times.append(t1 - t0)
-    best = min(times)
-    return gates / best, threads, best, times
+    p = psi.ctypes.data
+    u = np.linalg.qr(np.array([[0.6 + 0.1j, 0.3 - 0.2j], [-0.3 - 0.2j, 0.6 - 0.1j]]))[0].reshape(4)
+    gbuf = np.ascontiguousarray(np.stack([u.real, u.imag], axis=1).reshape(8))
+    L.orc_rx.argtypes = L.orc_ry.argtypes = L.orc_rz.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                                                  ctypes.c_double]
+    L.orc_cnot.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    qs = (0, n // 2, n - 1)
+    calls = {"rx": [lambda q=q: L.orc_rx(p, n, q, 0.7) for q in qs],
+             "ry": [lambda q=q: L.orc_ry(p, n, q, 1.1) for q in qs],
+             "rz": [lambda q=q: L.orc_rz(p, n, q, 0.4) for q in qs],
+             "cnot": [lambda: L.orc_cnot(p, n, 0, 1), lambda: L.orc_cnot(p, n, n - 2, n - 1)],
+             "u2": [lambda q=q: L.orc_apply_gate_v3(p, n, q, gbuf.ctypes.data) for q in qs]}
+    out = {}
+    for k in kinds:
+        for f in calls[k]:
+            f()  # untimed
+        best = float("inf")
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            for f in calls[k]:
+                f()
+            best = min(best, (time.perf_counter() - t0) / len(calls[k]))
+        out[k] = best
+    del psi
+    return out
+
+
+def cpu_rates(mix: dict, t: dict) -> dict:
+    """Whole-circuit gates/s of the reference's per-gate path and of its fused path, from the
+    per-kind times and the circuit's gate mix."""
+    t_rot = (t["rx"] + t["ry"] + t["rz"]) / 3.0
+    per_gate = mix["gates"] / (mix["rotations"] * t_rot + mix["cnots"] * t["cnot"])
+    fused = mix["gates"] / (mix["fused_2x2"] * t["u2"] + mix["cnots"] * t["cnot"])
+    return {"per_gate": per_gate, "fused": fused}
+
+
+def cpu_baseline(n: int, ops: np.ndarray, reps: int = 5, one_thread: bool = True) -> dict:
+    """Both reference CPU paths on every host core (best of `reps`) and on one thread (best of 1);
+    `value` is the faster all-core figure."""
+    mix = circuit_mix(n, ops)
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    t_all = cpu_gate_times(n, cores, reps)
+    r_all = cpu_rates(mix, t_all)
+    out = {"value": max(r_all.values()), "unit": "gates/s", "cores": cores, "kind": "port",
+           "path": "fused" if r_all["fused"] >= r_all["per_gate"] else "per_gate",
+           "per_gate_gates_per_s": r_all["per_gate"], "fused_gates_per_s": r_all["fused"],
+           "seconds_per_gate": t_all, "circuit_mix": mix}
+    if one_thread:
+        t_one = cpu_gate_times(n, 1, 1)
+        r_one = cpu_rates(mix, t_one)
+        out.update({"one_thread_per_gate_gates_per_s": r_one["per_gate"], "one_thread_fused_gates_per_s": r_one["fused"],
+                    "one_thread_seconds_per_gate": t_one})
+    out["sample"] = (f"each gate kind timed on the {n}-qubit state (RX/RY/RZ/U2 on qubits 0, {n // 2}, {n - 1}; CNOT "
+                     f"on (0, 1), ({n - 2}, {n - 1})), best of {reps} on {cores} threads"
+                     f"{' and best of 1 on 1 thread' if one_thread else ''} after one untimed application; "
+                     f"combined over the circuit's {mix['rotations']} rotations + {mix['cnots']} CNOTs (per-gate "
+                     f"ll::StateVectorBackend path) and {mix['fused_2x2']} fused 2x2s + {mix['cnots']} CNOTs "
+                     f"(GateFuser.fuse_circuit + apply_gate_cache_optimized); oracle restatements; "
+                     f"{time.perf_counter() - t0:.0f} s of CPU time")
+    return out
 
 
 def run_reference(args, rank, world):
@@ -171,17 +248,30 @@ def run_reference(args, rank, world):
     import workloads
 
     ops = workloads.layered_rotations(args.qubits, args.layers)
-    warm = max(1, args.warmup)
-    rate, threads, best, times = cpu_sample(args.qubits, ops, args.cpu_gates, args.steps, warm)
-    sample = (f"first {args.cpu_gates} gates of the {args.qubits}-qubit layered circuit per step, "
-              f"{args.steps} steps after {warm} warm-up; per-gate OpenMP passes of the reference algorithm")
+    mix = circuit_mix(args.qubits, ops)
+    cores = os.cpu_count() or 1
+    # warm-up steps, then K timed steps: each step times one application of every gate kind on
+    # every host core (a bounded sample of the circuit) and rates the whole circuit from it
+    for _ in range(max(1, args.warmup)):
+        cpu_gate_times(args.qubits, cores, 1)
+    rates, times = [], []
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        r = cpu_rates(mix, cpu_gate_times(args.qubits, cores, 1))
+        times.append(time.perf_counter() - t0)
+        rates.append(max(r.values()))
+    rate = statistics.median(rates)
+    sample = (f"per step: each gate kind applied once on the {args.qubits}-qubit state with {cores} threads, the "
+              f"faster of the per-gate (ll::StateVectorBackend) and fused (GateFuser + apply_gate_cache_optimized) "
+              f"paths combined over the circuit's gate mix; median of {len(rates)} steps after "
+              f"{max(1, args.warmup)} warm-up")
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "gates/s", "n_gpus": world,
-        "steps": args.steps, "warmup": warm, "ms_per_step": 1e3 * statistics.mean(times),
+        "steps": args.steps, "warmup": max(1, args.warmup), "ms_per_step": 1e3 * statistics.mean(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"{args.qubits}-qubit complex128 layered circuit ({args.layers} layers), "
-                               f"per-gate CPU sample", "qubits": args.qubits, "layers": args.layers},
-        "cpu_baseline": {"value": rate, "unit": "gates/s", "cores": threads, "kind": "port", "sample": sample},
+                               f"CPU sample per step", "qubits": args.qubits, "layers": args.layers},
+        "cpu_baseline": {"value": rate, "unit": "gates/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": "gates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -190,183 +280,46 @@ def run_reference(args, rank, world):
 # --------------------------------------------------------------------------------------------
 # GPU side
 # --------------------------------------------------------------------------------------------
-def run_ours(args, rank, world, local):
-    import __graft_entry__
-
-    __graft_entry__.build()
-    import llgpu
-    import workloads
-
-    torch = None
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    else:
-        import torch
-
-    n = args.qubits
-    ops = workloads.layered_rotations(n, args.layers)
-    ngates = len(ops)
-    st = llgpu.State(n, args.precision)
-    tune = None
-    if args.tile < 0:
-        # autotuner: two layers of the circuit on a scratch state, outside the timed region
-        tune = st.autotune(ops, sample_ops=2 * len(ops) // max(1, args.layers))
-    else:
-        st.set_fusion("tile", args.tile)
-        st.set_tile_threads(args.cta_threads)
-    tuning = st.tuning()
-    tile_q = tuning["tile_qubits"]
-    passes, xops = llgpu.plan_export(n, ops, tile_q, zyz=args.precision == "complex128")
-    if tuning["fuse_mode"] == "none":
-        passes = np.zeros(ngates)  # one streaming pass per gate
-    elem = 8 if args.precision == "complex64" else 16
-    state_bytes = elem * (1 << n)
-
-    stream = torch.cuda.ExternalStream(st.stream)
-    # warm-up
-    for _ in range(args.warmup):
-        st.reset(n)
-        st.apply_ops(ops)
-        st.flush()
-    st.sync()
-    st.profile(True)
-    st.profile_read(reset=True)
-
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-
-    launches0 = llgpu.kernel_launches()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        barrier()
-        st.sync()
-        ev0.record(stream)
-        for _ in range(args.steps):
-            st.reset(n)
-            st.apply_ops(ops)
-            st.flush()
-        ev1.record(stream)
-        st.sync()
-        torch.cuda.synchronize()
-        barrier()
-    launches = llgpu.kernel_launches() - launches0
-    elapsed_ms = ev0.elapsed_time(ev1)
-    prof = st.profile_read(reset=True)
-    st.profile(False)
-    # replicas: every rank ran the same circuit on its own state; the job's rate is all ranks'
-    # gates over the slowest rank's time
-    import replicas
-
-    value, slowest_s = replicas.job_rate(ngates * args.steps, elapsed_ms / 1e3,
-                                         torch.distributed if world > 1 else None, device="cuda")
-    elapsed_ms = slowest_s * 1e3
-    ms_step = elapsed_ms / args.steps
-
-    tile_ms, tile_n = prof["tile"] if prof["tile"][1] else prof["gate"]
-    peak, peak_kind = peaks()
-    per_launch_s = (tile_ms / tile_n) / 1e3 if tile_n else float("nan")
-    achieved = state_bytes * 2 / per_launch_s / 1e9 if tile_n else None
-    # the committed ncu capture is of the complex128 (double-float) tile pass at this workload
-    traffic = profile_traffic() if args.precision == "complex128" and n == 30 else None
-    st.close()
-
-    # end to end through the drop-in module: op records in, final amplitudes out, every step
-    e2e = None
-    if not args.no_e2e:
-        e2e = run_e2e(args, ops, xops, n, elem, world, torch)
-
-    sweeps = None
-    if not args.no_sweeps:
-        sweeps = run_sweep_bench(args, torch)
-
-    adj = None
-    if not args.no_adjoint:
-        adj = run_adjoint_bench(args, torch)
-    traj = batch = zne = config1 = tsolver = dmat = None
-    if not args.no_forms:
-        traj = run_traj_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
-        batch = run_batch_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
-        zne = run_zne_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
-        config1 = run_config1_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
-        tsolver = run_tsolver_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
-        dmat = run_dm_bench(args, torch, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
-
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        rate, threads, best, _ = cpu_sample(n, ops, args.cpu_gates, 1, 1)
-        cpu = {"value": rate, "unit": "gates/s", "cores": threads, "kind": "port",
-               "sample": f"first {args.cpu_gates} gates of the same {n}-qubit circuit, best of 1 after 1 warm-up, "
-                         f"{best:.1f} s per sample; oracle restatement of ll::StateVectorBackend (OpenMP)"}
-
-    if rank != 0:
-        return
-    clocks = clk.summary()
-    line = {
-        "metric": METRIC, "value": value, "unit": "gates/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "df64" if args.precision == "complex128" else args.precision,
-        "data": "synthetic (seeded layered circuit)",
-        "config": {"workload": f"{n}-qubit complex128 layered circuit: {args.layers} layers of RX/RY/RZ on every "
-                               f"qubit + CNOT brickwork, {ngates} gates, fused into {len(passes)} shared-memory tile "
-                               f"passes of {tile_q} qubits", "qubits": n, "layers": args.layers, "gates": ngates,
-                   "tile_passes": int(len(passes)), "tile_qubits": tile_q, "precision": args.precision,
-                   "fusion": tuning, "autotune": tune,
-                   "l2": f"inputs larger than L2 ({state_bytes / 2**30:g} GiB state), no flush needed"},
-        "sweeps_per_s": len(passes) * args.steps * world / (elapsed_ms / 1e3),
-        "hbm_gbs_algorithmic": len(passes) * 2 * state_bytes * args.steps * world / (elapsed_ms / 1e3) / 1e9,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "kernel": f"k_tile<{TILE_POLICY.get(args.precision, args.precision)}> (tile pass)",
-                     "launches": tile_n,
-                     "mean_launch_ms": tile_ms / tile_n if tile_n else None,
-                     "peak_source": f"{peak_kind} hbm_gbs"},
-        "compute_roofline": compute_roofline(args.precision, n, xops if tuning["fuse_mode"] == "tile" else [],
-                                             prof["tile"][0] / args.steps, (clocks or {}).get("sm_mhz")),
-        "kernel_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()},
-        "gpu_launches": launches,
-        "clocks": clocks,
-        "e2e": e2e,
-        "cpu_baseline": cpu,
-        "gate_sweeps": sweeps,
-        "adjoint": adj,
-        "trajectories": traj,
-        "mixed_batch": batch,
-        "zne": zne,
-        "config1_12q": config1,
-        "trajectory_solver": tsolver,
-        "density_matrix": dmat,
-    }
-    print(json.dumps(line), flush=True)
-
-
 # FP32 lane instructions per amplitude pair of each executor op kind (0 U2, 1 RX, 2 RY, 3 H, 4 X,
-# 5 DIAG, 6 CNOT, 7 MCZ), counted from the double-float routines of the kernels.  Results are stored
-# without the closing Fast2Sum: a 4-term double-float dot product (df_lin4_raw) is 40 instructions
-# (4 FMUL + 4 FFMA product errors, 3 TwoSum of 6, 8 FFMA cross terms, 6 FADD), a 2-term one
-# (df_lin2_raw) 16, an x + a*y update (df_fma_raw) 12.  A U2 pair needs four 4-term products;
-# RX/RY/H four 2-term ones; a diagonal two 2-term ones per amplitude; a ZYZ (phase-free unitary)
-# eight; a ZY (RY after an input phase) six; a carried-phase flush (13) two per amplitude pair; a
-# tangent-form rotation (14, 15) two 2-term products and four updates.  A CNOT carrying a pushed
-# phase multiplies a quarter of the amplitudes.  CNOT, MCZ and X otherwise move or negate data
-# without arithmetic.
-FP32_INST_PER_PAIR = {"complex128": {0: 160, 1: 64, 2: 64, 3: 64, 4: 0, 5: 64, 6: 0, 7: 0, 11: 128, 12: 96, 13: 32, 14: 80,
-                                     15: 80},
-                      "complex64": {0: 16, 1: 8, 2: 8, 3: 8, 4: 0, 5: 8, 6: 0, 7: 0, 11: 16, 12: 12, 13: 4, 14: 8, 15: 8}}
-PHASED_CNOT_PER_PAIR = {"complex128": 16, "complex64": 2}  # a complex multiply on a quarter of the amplitudes
+# 5 DIAG, 6 CNOT, 7 MCZ, 11 ZYZ, 12 ZY, 13 carried-phase flush, 14/15 tangent rotations with an input
+# phase, 16/17 tangent rotations whose phase a table applied, 18 phase table), counted from the
+# double-float routines of the kernels.  Results are stored without the closing Fast2Sum: a 4-term
+# double-float dot product (df_lin4_raw) is 40 instructions, a 2-term one (df_lin2_raw) 16, an
+# x + a*y update (df_fma_raw) 12.  A U2 pair needs four 4-term products; RX/RY/H four 2-term ones;
+# a diagonal two 2-term ones per amplitude; a ZYZ eight; a ZY six; a flush two per pair; a tangent
+# rotation two 2-term products and four updates, or the four updates alone after a table; a table
+# a complex product per amplitude.  A CNOT carrying a pushed phase multiplies a quarter of the
+# amplitudes.  CNOT, MCZ and X otherwise move or negate data without arithmetic.
+FP32_INST_PER_PAIR = {"df64": {0: 160, 1: 64, 2: 64, 3: 64, 4: 0, 5: 64, 6: 0, 7: 0, 11: 128, 12: 96, 13: 32, 14: 80,
+                               15: 80, 16: 48, 17: 48, 18: 64},
+                      "complex64": {0: 16, 1: 8, 2: 8, 3: 8, 4: 0, 5: 8, 6: 0, 7: 0, 11: 16, 12: 12, 13: 4, 14: 8, 15: 8,
+                                    16: 4, 17: 4, 18: 8}}
+PHASED_CNOT_PER_PAIR = {"df64": 16, "complex64": 2}  # a complex multiply on a quarter of the amplitudes
+# FP64 multiply-adds (DFMA or DMUL) per amplitude pair of each kind in IEEE complex128: a complex
+# product is four, a real 2x2 row two, a generic complex 2x2 row eight
+FP64_FMA_PER_PAIR = {0: 16, 1: 8, 2: 8, 3: 8, 4: 0, 5: 8, 6: 0, 7: 0, 11: 16, 12: 12, 13: 4, 14: 8, 15: 8, 16: 4, 17: 4,
+                     18: 8}
+FP64_PHASED_CNOT_PER_PAIR = 2
 SMS, FP32_LANES_PER_SM = 152, 128
-TILE_POLICY = {"complex128": "PolDF64", "complex64": "PolF32", "fp64": "PolF64"}
+TILE_POLICY = {"df64": "PolDF64", "complex64": "PolF32", "complex128": "PolF64", "fp64": "PolF64"}
+ELEM_BYTES = {"complex64": 8}
+
+
+def is_f64(precision: str) -> bool:
+    return precision in ("complex128", "fp64", "f64")
+
+
+def plan_for(precision: str, n: int, ops, tile_q: int):
+    import llgpu
+
+    r = llgpu.plan_export(n, ops, tile_q, zyz=True, tables=precision != "complex64")
+    return r[0], r[1]
 
 
 def compute_roofline(precision, n, xops, tile_ms_step, sm_mhz):
-    """FP32-issue roofline of the tile passes: algorithmic FP32 lane instructions per step over
-    the measured tile-pass time, against 152 SMs x 128 lanes x the sampled SM clock."""
+    """FP32-issue roofline of the tile passes (double-float and complex64): algorithmic FP32 lane
+    instructions per step over the measured tile-pass time, against 152 SMs x 128 lanes x the
+    sampled SM clock."""
     table = FP32_INST_PER_PAIR.get(precision)
     if table is None or not tile_ms_step or not len(xops):
         return None
@@ -380,10 +333,27 @@ def compute_roofline(precision, n, xops, tile_ms_step, sm_mhz):
             "fp32_inst_per_step": inst, "peak_basis": f"{SMS} SMs x {FP32_LANES_PER_SM} FP32 lanes x {mhz:.0f} MHz"}
 
 
-def profile_traffic():
-    """DRAM bytes per tile-pass launch from the committed ncu summary, if present."""
-    path = os.path.join(REPO, "profiles", "k_tile_df64_30q.md")
-    if not os.path.exists(path):
+def fp64_roofline(n, xops, tile_ms_step, fma_rate):
+    """FP64 roofline of the IEEE complex128 tile passes: the plan's FP64 multiply-adds per step
+    (FP64_FMA_PER_PAIR x 2^(n-1) pairs per op) over the tile passes' time, against the FP64 FMA
+    rate measured by the throughput kernel."""
+    if not tile_ms_step or not len(xops) or not fma_rate:
+        return None
+    per_pair = sum(FP64_FMA_PER_PAIR.get(int(k), 0) for k in xops["kind"])
+    per_pair += FP64_PHASED_CNOT_PER_PAIR * int(np.sum((xops["kind"] == 6) & ((xops["flags"] & 8) != 0)))
+    fma = per_pair * float(1 << (n - 1))
+    achieved = fma / (tile_ms_step / 1e3)
+    return {"bound": "fp64_fma", "achieved": achieved / 1e12, "peak": fma_rate / 1e12, "unit": "TFMA/s",
+            "frac": achieved / fma_rate, "fp64_fma_per_step": fma, "tflops_fp64": 2 * achieved / 1e12,
+            "peak_basis": "FP64 FMA throughput kernel (llg_fp64_fma_rate), measured in this run"}
+
+
+def profile_traffic(precision: str, n: int):
+    """DRAM bytes per tile-pass launch from the committed ncu summary of this precision's tile
+    pass, if present (scaled to a full launch there)."""
+    name = {"df64": "k_tile_df64_30q.md", "complex128": "k_tile_f64_30q.md"}.get(precision)
+    path = os.path.join(REPO, "profiles", name) if name else None
+    if n != 30 or not path or not os.path.exists(path):
         return None
     with open(path) as f:
         for line in f:
@@ -395,10 +365,253 @@ def profile_traffic():
     return None
 
 
+def measure_circuit(args, torch, precision, n, ops, steps, warmup, world, sampler_gpu=None, keep=False):
+    """Timed steps of the layered circuit at `precision`: reset, apply, flush per step, CUDA events
+    on the engine's stream, per-launch events for the tile passes.  Returns a dict (and the state
+    when keep=True)."""
+    import llgpu
+    import replicas
+
+    ngates = len(ops)
+    st = llgpu.State(n, precision)
+    tune = None
+    if args.tile < 0:
+        # autotuner: two layers of the circuit on a scratch state, outside the timed region
+        tune = st.autotune(ops, sample_ops=2 * len(ops) // max(1, args.layers))
+    else:
+        st.set_fusion("tile", args.tile)
+        st.set_tile_threads(args.cta_threads)
+    tuning = st.tuning()
+    tile_q = tuning["tile_qubits"]
+    passes, xops = plan_for(precision, n, ops, tile_q)
+    if tuning["fuse_mode"] == "none":
+        passes = np.zeros(ngates)  # one streaming pass per gate
+    state_bytes = ELEM_BYTES.get(precision, 16) * (1 << n)
+    stream = torch.cuda.ExternalStream(st.stream)
+    for _ in range(warmup):
+        st.reset(n)
+        st.apply_ops(ops)
+        st.flush()
+    st.sync()
+    st.profile(True)
+    st.profile_read(reset=True)
+    launches0 = llgpu.kernel_launches()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+
+    def timed():
+        if world > 1:
+            torch.distributed.barrier()
+        st.sync()
+        ev0.record(stream)
+        for _ in range(steps):
+            st.reset(n)
+            st.apply_ops(ops)
+            st.flush()
+        ev1.record(stream)
+        st.sync()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    clocks = None
+    if sampler_gpu is not None:
+        with ClockSampler(sampler_gpu) as clk:
+            timed()
+        clocks = clk.summary()
+    else:
+        timed()
+    launches = llgpu.kernel_launches() - launches0
+    elapsed_ms = ev0.elapsed_time(ev1)
+    prof = st.profile_read(reset=True)
+    st.profile(False)
+    value, slowest_s = replicas.job_rate(ngates * steps, elapsed_ms / 1e3, torch.distributed if world > 1 else None,
+                                         device="cuda")
+    elapsed_ms = slowest_s * 1e3
+    tile_ms, tile_n = prof["tile"] if prof["tile"][1] else prof["gate"]
+    peak, peak_kind = peaks()
+    per_launch_s = (tile_ms / tile_n) / 1e3 if tile_n else float("nan")
+    achieved = state_bytes * 2 / per_launch_s / 1e9 if tile_n else None
+    res = {
+        "value": value, "unit": "gates/s", "steps": steps, "warmup": warmup, "ms_per_step": elapsed_ms / steps,
+        "gpu_launches": launches, "tile_passes": int(len(passes)), "tile_qubits": tile_q, "fusion": tuning,
+        "autotune": tune, "state_bytes": state_bytes, "clocks": clocks,
+        "sweeps_per_s": len(passes) * steps * world / (elapsed_ms / 1e3),
+        "hbm_gbs_algorithmic": len(passes) * 2 * state_bytes * steps * world / (elapsed_ms / 1e3) / 1e9,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": profile_traffic(precision, n),
+                     "kernel": f"k_tile<{TILE_POLICY.get(precision, precision)}> (tile pass)", "launches": tile_n,
+                     "mean_launch_ms": tile_ms / tile_n if tile_n else None, "peak_source": f"{peak_kind} hbm_gbs"},
+        "kernel_ms_per_step": {k: v[0] / steps for k, v in prof.items()},
+        "_xops": xops if tuning["fuse_mode"] == "tile" else np.zeros(0, dtype=xops.dtype),
+        "_tile_ms_step": prof["tile"][0] / steps,
+    }
+    if keep:
+        return res, st
+    st.close()
+    return res
+
+
+def finish_rooflines(res, precision, n, fma_rate):
+    xops, tile_ms_step = res.pop("_xops"), res.pop("_tile_ms_step")
+    sm = (res.get("clocks") or {}).get("sm_mhz")
+    if is_f64(precision):
+        res["fp64_roofline"] = fp64_roofline(n, xops, tile_ms_step, fma_rate)
+    else:
+        res["compute_roofline"] = compute_roofline(precision, n, xops, tile_ms_step, sm)
+    return res
+
+
+def run_ours(args, rank, world, local):
+    import __graft_entry__
+
+    __graft_entry__.build()
+    import llgpu
+    import workloads
+
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        import torch
+
+    n = args.qubits
+    ops = workloads.layered_rotations(n, args.layers)
+    ngates = len(ops)
+    fma_rate = llgpu.fp64_fma_rate()
+    head, st = measure_circuit(args, torch, args.precision, n, ops, args.steps, args.warmup, world,
+                               sampler_gpu=local, keep=True)
+    head = finish_rooflines(head, args.precision, n, fma_rate)
+    clocks = head.pop("clocks")
+    elem = ELEM_BYTES.get(args.precision, 16)
+    _, xops_e2e = plan_for(args.precision, n, ops, head["tile_qubits"])
+
+    # the same circuit in the other precisions, each compared with this (FP64) final state
+    variants = None
+    if not args.no_variants and is_f64(args.precision):
+        variants = {}
+        for prec in ("df64", "complex64"):
+            vsteps = max(1, min(args.steps, E2E_STEPS_MAX))
+            v, vst = measure_circuit(args, torch, prec, n, ops, vsteps, 2, world, keep=True)
+            v = finish_rooflines(v, prec, n, fma_rate)
+            v.pop("clocks", None)
+            fid, dmax, amax = vst.compare_ex(st)
+            v["vs_fp64"] = {"max_abs_diff": dmax, "one_minus_fidelity": 1.0 - fid, "max_abs_amp": amax,
+                            "max_abs_diff_rel_to_max_amp": (dmax / amax) if amax else None}
+            vst.close()
+            if not args.no_e2e:
+                v["e2e"] = run_e2e(args, prec, ops, plan_for(prec, n, ops, v["tile_qubits"])[1], n,
+                                   ELEM_BYTES.get(prec, 16), world, torch, v["tile_qubits"])
+            variants[prec] = v
+    st.close()
+
+    # end to end through the drop-in module: op records in, final amplitudes out, every step
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, args.precision, ops, xops_e2e, n, elem, world, torch, head["tile_qubits"])
+
+    sweeps = None
+    if not args.no_sweeps:
+        sweeps = run_sweep_bench(args, torch)
+
+    adj = None
+    if not args.no_adjoint:
+        adj = run_adjoint_bench(args, torch)
+    traj = batch = zne = config1 = tsolver = dmat = None
+    cpu_ok = rank == 0 and world == 1 and not args.no_cpu_baseline
+    if not args.no_forms:
+        traj = run_traj_bench(args, torch, cpu=cpu_ok)
+        batch = run_batch_bench(args, torch, cpu=cpu_ok)
+        zne = run_zne_bench(args, torch, cpu=cpu_ok)
+        config1 = run_config1_bench(args, torch, cpu=cpu_ok)
+        tsolver = run_tsolver_bench(args, torch, cpu=cpu_ok)
+        dmat = run_dm_bench(args, torch, cpu=cpu_ok)
+
+    cpu = cpu_baseline(n, ops) if cpu_ok else None
+
+    if rank != 0:
+        return
+    dtype = {"complex128": "f64", "fp64": "f64", "f64": "f64", "df64": "df64", "complex64": "c64"}.get(args.precision,
+                                                                                                     args.precision)
+    line = {
+        "metric": METRIC, "value": head["value"], "unit": "gates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": dtype,
+        "data": "synthetic (seeded layered circuit)",
+        "config": {"workload": f"{n}-qubit complex128 layered circuit: {args.layers} layers of RX/RY/RZ on every "
+                               f"qubit + CNOT brickwork, {ngates} gates, fused into {head['tile_passes']} shared-memory "
+                               f"tile passes of {head['tile_qubits']} qubits", "qubits": n, "layers": args.layers,
+                   "gates": ngates, "tile_passes": head["tile_passes"], "tile_qubits": head["tile_qubits"],
+                   "precision": args.precision,
+                   "arithmetic": "IEEE binary64 (FP64 pipe)" if is_f64(args.precision) else args.precision,
+                   "fusion": head["fusion"], "autotune": head["autotune"],
+                   "l2": f"inputs larger than L2 ({head['state_bytes'] / 2**30:g} GiB state), no flush needed"},
+        "sweeps_per_s": head["sweeps_per_s"], "hbm_gbs_algorithmic": head["hbm_gbs_algorithmic"],
+        "roofline": head["roofline"],
+        "fp64_roofline": head.get("fp64_roofline"),
+        "compute_roofline": head.get("compute_roofline"),
+        "kernel_ms_per_step": head["kernel_ms_per_step"],
+        "gpu_launches": head["gpu_launches"],
+        "clocks": clocks,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "variants": variants,
+        "gate_sweeps": sweeps,
+        "adjoint": adj,
+        "trajectories": traj,
+        "mixed_batch": batch,
+        "zne": zne,
+        "config1_12q": config1,
+        "trajectory_solver": tsolver,
+        "density_matrix": dmat,
+    }
+    line["summary"] = summarize(line)
+    print(json.dumps(line), flush=True)
+
+
+def summarize(line: dict) -> dict:
+    """The key figure of every measured form, repeated at the end of the line."""
+    def get(d, *path):
+        for p in path:
+            if not isinstance(d, dict) or p not in d:
+                return None
+            d = d[p]
+        return d
+
+    return {
+        "headline_gates_per_s": line["value"], "dtype": line["dtype"],
+        "e2e_gates_per_s": get(line, "e2e", "value"),
+        "fp64_roofline_frac": get(line, "fp64_roofline", "frac"), "hbm_roofline_frac": get(line, "roofline", "frac"),
+        "cpu_gates_per_s": get(line, "cpu_baseline", "value"),
+        "df64_gates_per_s": get(line, "variants", "df64", "value"),
+        "df64_one_minus_fidelity": get(line, "variants", "df64", "vs_fp64", "one_minus_fidelity"),
+        "complex64_gates_per_s": get(line, "variants", "complex64", "value"),
+        "complex64_one_minus_fidelity": get(line, "variants", "complex64", "vs_fp64", "one_minus_fidelity"),
+        "adjoint_grads_per_s": get(line, "adjoint", "grads_per_s"),
+        "adjoint_speedup_vs_param_shift": get(line, "adjoint", "speedup_vs_param_shift"),
+        "adjoint_df64_grads_per_s": get(line, "adjoint", "df64", "grads_per_s"),
+        "trajectories_per_s_c128": get(line, "trajectories", "c128", "traj_per_s"),
+        "trajectories_per_s_df64": get(line, "trajectories", "df64", "traj_per_s"),
+        "trajectories_per_s_c64": get(line, "trajectories", "c64", "traj_per_s"),
+        "mixed_batch_circuits_per_s_c128": get(line, "mixed_batch", "c128", "circuits_per_s"),
+        "mixed_batch_circuits_per_s_c64": get(line, "mixed_batch", "c64", "circuits_per_s"),
+        "zne_traj_per_s": get(line, "zne", "traj_per_s"),
+    }
 def run_adjoint_bench(args, torch):
     """Adjoint gradients of the 20-qubit, 10-layer RY/RZ + CZ-ring ansatz (400 parameters,
     observable sum_i Z_i Z_{i+1} periodic) for a batch of 64 parameter sets, against the
-    parameter-shift rule evaluated on the same GPU (batched shifted circuits) for one set."""
+    parameter-shift rule evaluated on the same GPU (batched shifted circuits) for one set; in IEEE
+    complex128 (the headline) and in double-float (`df64`)."""
+    out = adjoint_once(args, torch, args.precision)
+    if is_f64(args.precision):
+        out["df64"] = adjoint_once(args, torch, "df64")
+    return out
+
+
+def adjoint_once(args, torch, precision):
     import llgpu
     import workloads
 
@@ -406,7 +619,7 @@ def run_adjoint_bench(args, torch):
     ops = workloads.hea_ansatz(n, layers)
     nparams = layers * 2 * n
     params = workloads.hea_params(n, layers, batch)
-    adj = llgpu.Adjoint(n, ops, nparams, llgpu.ring_zz_terms(n), max_batch=batch, precision=args.precision)
+    adj = llgpu.Adjoint(n, ops, nparams, llgpu.ring_zz_terms(n), max_batch=batch, precision=precision)
     stream = torch.cuda.ExternalStream(adj.stream)
     for _ in range(2):
         adj.run(params)
@@ -434,7 +647,7 @@ def run_adjoint_bench(args, torch):
             "adjoint_s_per_batch": t_adj, "param_shift_s_per_set": t_ps,
             "max_abs_grad_diff_vs_param_shift": float(np.max(np.abs(g[0] - g_ps[0]))),
             "forward_passes": info["forward_passes"], "backward_passes": info["backward_passes"],
-            "precision": args.precision}
+            "precision": precision}
 
 
 def run_sweep_bench(args, torch):
@@ -457,7 +670,7 @@ def run_sweep_bench(args, torch):
              "CZ": [(OP_CZ, 0, n - 1), (OP_CZ, 12, 13), (OP_CZ, 3, 20)]}
     bytes_per = {"CNOT": 16, "CZ": 8}
     out = {"qubits": n, "peak_gbs": peak, "peak_source": f"{peak_kind} hbm_gbs"}
-    for prec in ("complex128", "fp64"):
+    for prec in ("complex128", "df64"):
         st = llgpu.State(n, prec)
         st.set_fusion("none")
         res = {}
@@ -535,7 +748,7 @@ def run_traj_bench(args, torch, cpu: bool):
     ops = workloads.noisy_layers(n, 8)
     out = {"workload": f"{ntraj} trajectories x {n} qubits, {len(ops)} gates, {llgpu.noise_sites(ops)} noise sites "
                        f"(amplitude damping {gamma} then dephasing {lam})"}
-    for prec in ("complex128", "complex64"):
+    for prec in ("complex128", "df64", "complex64"):
         # a handle planned once; the autotuner picks cluster split and CTA threads, and every
         # launch replays the captured CUDA graph (outputs copied to host inside the timing)
         h = llgpu.Traj(n, ops, gamma, lam, ntraj, prec)
@@ -549,7 +762,7 @@ def run_traj_bench(args, torch, cpu: bool):
         t0 = time.perf_counter()
         z, j, _ = h.launch(seed, ntraj)
         dt = time.perf_counter() - t0
-        key = "c128" if prec == "complex128" else "c64"
+        key = {"complex128": "c128", "df64": "df64", "complex64": "c64"}[prec]
         out[key] = {"traj_per_s": ntraj / dt, "seconds": dt, "mean_z0": float(z.mean()),
                     "std_error": float(z.std(ddof=1) / np.sqrt(ntraj)), "jumps_per_traj": float(j.mean()),
                     "config": h.config(), "default_config": default_cfg,
@@ -817,13 +1030,13 @@ def run_batch_bench(args, torch, cpu: bool):
     ngates = int(off[-1])
     res = {"workload": f"512 circuits, n in 10..22 (total {int(np.sum(2.0 ** nq))} amplitudes), 200 gates each"}
     batches = {}
-    for prec in ("complex128", "complex64"):
+    for prec in ("complex128", "df64", "complex64"):
         tune = llgpu.batch_autotune(nq, ops, off, prec)  # tile width by measurement (cached)
         b = llgpu.Batch(nq, ops, off, prec, llgpu.TUNE_AUTO)
         stream = torch.cuda.ExternalStream(b.stream)
         b.run()  # captures the CUDA graph; later runs replay it
         dt, _ = _timed(stream, torch, b.run, reps=max(1, args.steps))
-        key = "c128" if prec == "complex128" else "c64"
+        key = {"complex128": "c128", "df64": "df64", "complex64": "c64"}[prec]
         info = b.info()
         res[key] = {"circuits_per_s": 512 / dt, "gates_per_s": ngates / dt, "seconds": dt,
                     "work_items": info["work_items"], "tile_qubits": info["tile_qubits"],
@@ -831,6 +1044,8 @@ def run_batch_bench(args, torch, cpu: bool):
         batches[key] = b
     f = batches["c64"].fidelity(batches["c128"])
     res["c64_fidelity_error"] = {"max": float(np.max(1 - f[:, 0])), "median": float(np.median(1 - f[:, 0]))}
+    f = batches["df64"].fidelity(batches["c128"])
+    res["df64_fidelity_error"] = {"max": float(np.max(1 - f[:, 0])), "median": float(np.median(1 - f[:, 0]))}
     for b in batches.values():
         b.close()
     if cpu:
@@ -848,17 +1063,17 @@ def run_batch_bench(args, torch, cpu: bool):
     return res
 
 
-def run_e2e(args, ops, xops, n, elem, world, torch):
+def run_e2e(args, precision, ops, xops, n, elem, world, torch, tile_q=12):
     import quantum_sim_v3
 
-    sv = quantum_sim_v3.StateVector(n, args.precision)
+    sv = quantum_sim_v3.StateVector(n, precision)
     if args.tile < 0:
         sv.autotune(ops, 2 * len(ops) // max(1, args.layers))  # the headline's tuning, from the cache
     else:
         sv.set_fusion("tile", args.tile)
     sv.apply_ops(ops)
     sv.get_numpy_view()  # allocates the pinned host mirror once
-    steps = max(1, args.steps)
+    steps = max(1, min(args.steps, E2E_STEPS_MAX))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
@@ -878,9 +1093,11 @@ def run_e2e(args, ops, xops, n, elem, world, torch):
     view = sv.get_numpy_view()
     c = time.perf_counter()
     del sv, view
-    return {"value": len(ops) * steps * world / (t1 - t0), "unit": "gates/s",
+    return {"value": len(ops) * steps * world / (t1 - t0), "unit": "gates/s", "steps": steps,
             "ms_per_step": 1e3 * (t1 - t0) / steps, "passes_alone_ms": 1e3 * (b - a), "readback_alone_ms": 1e3 * (c - b),
-            "h2d_bytes_per_step": int(ops.nbytes + xops.nbytes), "d2h_bytes_per_step": int((1 << n) * 16),
+            "h2d_bytes_per_step": int(xops.nbytes + int(np.sum(xops["kind"] == 18)) * 16 * (1 << tile_q)),
+            "h2d_note": "the planned executor ops and phase tables uploaded by the flush",
+            "d2h_bytes_per_step": int((1 << n) * 16),
             "api": "quantum_sim_v3.StateVector: reset, apply_ops, get_numpy_view (host copy of all amplitudes; "
                    "the last tile pass writes the pinned host mirror as it stores its tiles)"}
 

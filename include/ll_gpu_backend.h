@@ -30,8 +30,9 @@ namespace ll {
 
 class GpuBackend final : public Backend {
 public:
-    // precision: LLG_DF64 (complex128 as double-float, default), LLG_F64 or LLG_F32.
-    explicit GpuBackend(int n_qubits = 1, int precision = LLG_DF64) : precision_(precision) {
+    // precision: LLG_F64 (complex128 in IEEE binary64, the reference's arithmetic; default),
+    // LLG_DF64 (double-float, faster on this GPU) or LLG_F32 (complex64).
+    explicit GpuBackend(int n_qubits = 1, int precision = LLG_F64) : precision_(precision) {
         check(llg_create(n_qubits, precision_, &st_));
     }
     ~GpuBackend() override {
@@ -189,7 +190,7 @@ struct GpuZNEResult {
 // so results agree with the reference in distribution, not draw for draw.
 class GpuZNE {
 public:
-    explicit GpuZNE(int trajectories = 1000, int precision = LLG_DF64) : trajectories_(trajectories), precision_(precision) {
+    explicit GpuZNE(int trajectories = 1000, int precision = LLG_F64) : trajectories_(trajectories), precision_(precision) {
         if (trajectories < 1) throw std::invalid_argument("ZNE: trajectories must be >= 1");
     }
 

@@ -215,6 +215,9 @@ int llg_norm2(llg_state* st, double* out);
  * output may be NULL).  No reference counterpart: a check for parity tests at sizes whose host
  * copies would be too large. */
 int llg_compare(llg_state* a, llg_state* b, double* fidelity, double* max_abs_diff);
+/* llg_compare that also returns the largest |re| or |im| of b's amplitudes (the scale that a
+ * relative amplitude error is taken against); any output may be NULL. */
+int llg_compare_ex(llg_state* a, llg_state* b, double* fidelity, double* max_abs_diff, double* max_abs_b);
 
 /* sum_k coeff_k <Z_{a_k} Z_{b_k}>; b_k < 0 selects the single-qubit term <Z_{a_k}>.  The
  * diagonal of python/algorithms.py:141-153 (ising_diagonal) evaluated on the fly. */
@@ -431,6 +434,11 @@ int llg_profile_read(llg_state* st, double* ms, int64_t* launches, int reset);
 int64_t llg_kernel_launches(void);
 /* The state's CUDA stream (a cudaStream_t), for callers that order their own work after it. */
 int llg_get_stream(const llg_state* st, void** out);
+/* Measurement aid with no counterpart in the reference: the current device's FP64 fused
+ * multiply-add throughput, timed with CUDA events over one launch of `iters` iterations of eight
+ * independent FMA chains per thread (after one untimed launch).  The FP64 roofline of the IEEE
+ * complex128 path is taken against this number. */
+int llg_fp64_fma_rate(int iters, double* fma_per_s);
 
 /* Pinned host memory, mapped into the device's address space, for fast transfers
  * (cudaHostAlloc); NULL on failure. */
@@ -467,11 +475,21 @@ typedef struct llg_exec_op {
 
 int llg_plan_export(int n, const llg_op* ops, int nops, int tile_qubits, llg_pass_info* passes, int max_passes,
                     int* npasses, llg_exec_op* xops, int max_xops, int* nxops);
-/* The same with planner options: LLG_PLAN_ZYZ lowers fused unitary 2x2s to ZYZ ops as the
- * engine does for complex128 (double-float) states; llg_plan_export plans without it. */
+/* The same with planner options: LLG_PLAN_ZYZ lowers fused unitary 2x2s to carried-phase
+ * rotations as the engine does for complex128 and double-float states; LLG_PLAN_TABLES (with
+ * LLG_PLAN_ZYZ) also gathers their input phases and the phased CNOTs' controlled phases into
+ * phase tables (kind 18: every tile amplitude l times table entry l; kinds 16 / 17: the real
+ * rotations [1, -c2; c2, 1] and [c2, -1; 1, c2] whose input phase a table applied), as the engine
+ * does for those states.  llg_plan_export plans without either. */
 #define LLG_PLAN_ZYZ 1
+#define LLG_PLAN_TABLES 2
 int llg_plan_export_ex(int n, const llg_op* ops, int nops, int tile_qubits, int flags, llg_pass_info* passes,
                        int max_passes, int* npasses, llg_exec_op* xops, int max_xops, int* nxops);
+/* The phase tables of the same plan: (re, im) doubles, 2^tile_qubits entries per table; a kind-18
+ * op's `mask` is the index of its first entry.  Writes at most max_doubles values and the true
+ * count to *ndoubles. */
+int llg_plan_export_tables(int n, const llg_op* ops, int nops, int tile_qubits, int flags, double* tables,
+                           int64_t max_doubles, int64_t* ndoubles);
 
 #ifdef __cplusplus
 }

@@ -59,6 +59,11 @@ struct llg_state {
     size_t d_ops_cap = 0;
     ExecOp* h_ops = nullptr;
     size_t h_ops_cap = 0;
+    // phase tables of the plan (device, pinned staging), uploaded with the ops
+    uint64_t* d_tables = nullptr;
+    size_t d_tables_cap = 0;
+    uint64_t* h_tables = nullptr;
+    size_t h_tables_cap = 0;
     cudaEvent_t ops_done = nullptr;
     // dense-block matrix upload (pinned staging, reused once the previous copy has finished)
     uint64_t* d_block = nullptr;
@@ -145,7 +150,7 @@ int ensure_device_buffers(llg_state* st) {
     if (!st->stream) LLG_CUDA(cudaStreamCreateWithFlags(&st->stream, cudaStreamNonBlocking), "cudaStreamCreate");
     if (!st->ops_done) LLG_CUDA(cudaEventCreateWithFlags(&st->ops_done, cudaEventDisableTiming), "cudaEventCreate");
     if (!st->d_partials) {
-        LLG_CUDA(cudaMalloc(&st->d_partials, sizeof(double) * kRedBlocks * kRedSlots), "cudaMalloc(partials)");
+        LLG_CUDA(cudaMalloc(&st->d_partials, sizeof(double) * kRedBlocks * kPartialSlots), "cudaMalloc(partials)");
         LLG_CUDA(cudaMalloc(&st->d_red, sizeof(double) * kRedSlots), "cudaMalloc(red)");
     }
     return LLG_OK;
@@ -195,7 +200,7 @@ int run_streaming(llg_state* st, const std::vector<llg_op>& q) {
     return LLG_OK;
 }
 
-int upload_ops(llg_state* st, const std::vector<ExecOp>& ops) {
+int upload_ops(llg_state* st, const std::vector<ExecOp>& ops, const std::vector<uint64_t>* tables = nullptr) {
     const size_t count = std::max<size_t>(ops.size(), 1);
     if (count > st->d_ops_cap) {
         if (st->d_ops) {
@@ -219,6 +224,28 @@ int upload_ops(llg_state* st, const std::vector<ExecOp>& ops) {
         LLG_CUDA(cudaMemcpyAsync(st->d_ops, st->h_ops, ops.size() * sizeof(ExecOp), cudaMemcpyHostToDevice, st->stream),
                  "cudaMemcpyAsync(ops)");
     }
+    if (tables && !tables->empty()) {
+        const size_t words = tables->size();
+        if (words > st->d_tables_cap) {
+            if (st->d_tables) {
+                cudaStreamSynchronize(st->stream);
+                cudaFree(st->d_tables);
+                st->d_tables = nullptr;
+            }
+            LLG_CUDA(cudaMalloc(&st->d_tables, words * sizeof(uint64_t)), "cudaMalloc(tables)");
+            st->d_tables_cap = words;
+        }
+        if (words > st->h_tables_cap) {
+            if (st->h_tables) cudaFreeHost(st->h_tables);
+            st->h_tables = nullptr;
+            LLG_CUDA(cudaHostAlloc((void**)&st->h_tables, words * sizeof(uint64_t), cudaHostAllocDefault),
+                     "cudaHostAlloc(tables)");
+            st->h_tables_cap = words;
+        }
+        std::memcpy(st->h_tables, tables->data(), words * sizeof(uint64_t));
+        LLG_CUDA(cudaMemcpyAsync(st->d_tables, st->h_tables, words * sizeof(uint64_t), cudaMemcpyHostToDevice, st->stream),
+                 "cudaMemcpyAsync(tables)");
+    }
     LLG_CUDA(cudaEventRecord(st->ops_done, st->stream), "cudaEventRecord");
     return LLG_OK;
 }
@@ -229,9 +256,10 @@ int run_tiles(llg_state* st, const std::vector<llg_op>& q, double* mirror = null
     Plan plan;
     std::string err;
     const int t = st->tile_qubits > 0 ? st->tile_qubits : default_tile(st->P);
-    if (!plan_tiles(st->n, q.data(), (int)q.size(), std::min(t, tile_max_qubits(st->P)), st->P, plan, err))
+    if (!plan_tiles(st->n, q.data(), (int)q.size(), std::min(t, tile_max_qubits(st->P)), st->P, plan, err, false,
+                    ZYZ_DEFAULT, st->P != LLG_F32))
         return set_error(LLG_EINVAL, err);
-    int rc = upload_ops(st, plan.ops);
+    int rc = upload_ops(st, plan.ops, &plan.tables);
     if (rc) return rc;
     st->tiles_launched = true;
     size_t last = plan.passes.size();
@@ -242,7 +270,10 @@ int run_tiles(llg_state* st, const std::vector<llg_op>& q, double* mirror = null
         if (pd.nops <= 0) continue;
         double* m = i == last ? mirror : nullptr;
         rc = traced(st, LLG_PROF_TILE, 1, "tile kernel",
-                    [&] { return launch_tile_pass(st->P, st->d_psi, st->n, pd, st->d_ops, st->tile_threads, st->stream, m); });
+                    [&] {
+                        return launch_tile_pass(st->P, st->d_psi, st->n, pd, st->d_ops, st->d_tables, st->tile_threads,
+                                                st->stream, m);
+                    });
         if (rc) return rc;
     }
     if (mirrored) *mirrored = mirror && last < plan.passes.size();
@@ -382,6 +413,8 @@ int llg_destroy(llg_state* st) {
     if (st->d_psi) cudaFree(st->d_psi);
     if (st->d_ops) cudaFree(st->d_ops);
     if (st->h_ops) cudaFreeHost(st->h_ops);
+    if (st->d_tables) cudaFree(st->d_tables);
+    if (st->h_tables) cudaFreeHost(st->h_tables);
     if (st->d_partials) cudaFree(st->d_partials);
     if (st->d_red) cudaFree(st->d_red);
     for (int i = 0; i < 2; ++i) {
@@ -848,6 +881,10 @@ static int reduce(llg_state* st, const ZTerms& z, double* slots) {
 }
 
 int llg_compare(llg_state* a, llg_state* b, double* fidelity, double* max_abs_diff) {
+    return llg_compare_ex(a, b, fidelity, max_abs_diff, nullptr);
+}
+
+int llg_compare_ex(llg_state* a, llg_state* b, double* fidelity, double* max_abs_diff, double* max_abs_b) {
     if (!a || !b) return set_error(LLG_EINVAL, "compare: NULL state");
     if (a->n != b->n) return set_error(LLG_EINVAL, "compare: the states have different qubit counts");
     int rc = llg_flush(a);
@@ -857,21 +894,23 @@ int llg_compare(llg_state* a, llg_state* b, double* fidelity, double* max_abs_di
     LLG_CUDA(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
     int nblocks = 0;
     LLG_CUDA(launch_compare(a->P, a->d_psi, b->P, b->d_psi, a->size, a->d_partials, &nblocks, a->stream), "compare kernel");
-    std::vector<double> part((size_t)nblocks * kRedSlots);
+    std::vector<double> part((size_t)nblocks * kCmpSlots);
     LLG_CUDA(cudaMemcpyAsync(part.data(), a->d_partials, part.size() * sizeof(double), cudaMemcpyDeviceToHost, a->stream),
              "cudaMemcpyAsync(D2H)");
     LLG_CUDA(cudaStreamSynchronize(a->stream), "cudaStreamSynchronize");
     if ((rc = device_checks(a)) || (rc = device_checks(b))) return rc;
-    double re = 0.0, im = 0.0, na = 0.0, nb = 0.0, mx = 0.0;
+    double re = 0.0, im = 0.0, na = 0.0, nb = 0.0, mx = 0.0, mb = 0.0;
     for (int k = 0; k < nblocks; ++k) {  // fixed order
-        re += part[(size_t)k * kRedSlots];
-        im += part[(size_t)k * kRedSlots + 1];
-        na += part[(size_t)k * kRedSlots + 2];
-        nb += part[(size_t)k * kRedSlots + 3];
-        mx = std::max(mx, part[(size_t)k * kRedSlots + 4]);
+        re += part[(size_t)k * kCmpSlots];
+        im += part[(size_t)k * kCmpSlots + 1];
+        na += part[(size_t)k * kCmpSlots + 2];
+        nb += part[(size_t)k * kCmpSlots + 3];
+        mx = std::max(mx, part[(size_t)k * kCmpSlots + 4]);
+        mb = std::max(mb, part[(size_t)k * kCmpSlots + 5]);
     }
     if (fidelity) *fidelity = (na > 0.0 && nb > 0.0) ? (re * re + im * im) / (na * nb) : 0.0;
     if (max_abs_diff) *max_abs_diff = mx;
+    if (max_abs_b) *max_abs_b = mb;
     return LLG_OK;
 }
 
@@ -957,6 +996,12 @@ int llg_profile_read(llg_state* st, double* ms, int64_t* launches, int reset) {
 
 int64_t llg_kernel_launches(void) { return g_launches.load(); }
 
+int llg_fp64_fma_rate(int iters, double* fma_per_s) {
+    if (!fma_per_s || iters < 1) return set_error(LLG_EINVAL, "fp64_fma_rate: bad argument");
+    LLG_CUDA(fp64_fma_rate(iters, fma_per_s), "fp64_fma_rate");
+    return LLG_OK;
+}
+
 int llg_get_stream(const llg_state* st, void** out) {
     if (!st || !out) return set_error(LLG_EINVAL, "get_stream: NULL argument");
     *out = (void*)st->stream;
@@ -968,9 +1013,11 @@ int llg_plan_export(int n, const llg_op* ops, int nops, int tile_qubits, llg_pas
     return llg_plan_export_ex(n, ops, nops, tile_qubits, 0, passes, max_passes, npasses, xops, max_xops, nxops);
 }
 
-int llg_plan_export_ex(int n, const llg_op* ops, int nops, int tile_qubits, int flags, llg_pass_info* passes,
-                       int max_passes, int* npasses, llg_exec_op* xops, int max_xops, int* nxops) {
-    if (n < 1 || n > kMaxQubits || nops < 0 || (nops > 0 && !ops) || !npasses || !nxops)
+}  // extern "C"
+
+namespace {
+int export_plan(int n, const llg_op* ops, int nops, int tile_qubits, int flags, Plan& plan) {
+    if (n < 1 || n > kMaxQubits || nops < 0 || (nops > 0 && !ops))
         return set_error(LLG_EINVAL, "plan_export: bad argument");
     if (tile_qubits < 1 || tile_qubits > 14) return set_error(LLG_EINVAL, "plan_export: tile_qubits out of range");
     llg_state tmp;
@@ -979,10 +1026,35 @@ int llg_plan_export_ex(int n, const llg_op* ops, int nops, int tile_qubits, int 
         int rc = validate_op(&tmp, ops[i], "plan_export");
         if (rc) return rc;
     }
-    Plan plan;
     std::string err;
-    if (!plan_tiles(n, ops, nops, tile_qubits, LLG_F64, plan, err, false, (flags & LLG_PLAN_ZYZ) ? ZYZ_ON : ZYZ_OFF))
+    if (!plan_tiles(n, ops, nops, tile_qubits, LLG_F64, plan, err, false, (flags & LLG_PLAN_ZYZ) ? ZYZ_ON : ZYZ_OFF,
+                    (flags & LLG_PLAN_TABLES) != 0))
         return set_error(LLG_EINVAL, err);
+    return LLG_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int llg_plan_export_tables(int n, const llg_op* ops, int nops, int tile_qubits, int flags, double* tables,
+                           int64_t max_doubles, int64_t* ndoubles) {
+    if (!ndoubles) return set_error(LLG_EINVAL, "plan_export_tables: NULL count");
+    Plan plan;
+    int rc = export_plan(n, ops, nops, tile_qubits, flags, plan);
+    if (rc) return rc;
+    *ndoubles = (int64_t)plan.tables.size();
+    if (tables)
+        for (int64_t i = 0; i < (int64_t)plan.tables.size() && i < max_doubles; ++i)
+            std::memcpy(&tables[i], &plan.tables[(size_t)i], sizeof(double));
+    return LLG_OK;
+}
+
+int llg_plan_export_ex(int n, const llg_op* ops, int nops, int tile_qubits, int flags, llg_pass_info* passes,
+                       int max_passes, int* npasses, llg_exec_op* xops, int max_xops, int* nxops) {
+    if (!npasses || !nxops) return set_error(LLG_EINVAL, "plan_export: bad argument");
+    Plan plan;
+    int rc = export_plan(n, ops, nops, tile_qubits, flags, plan);
+    if (rc) return rc;
     *npasses = (int)plan.passes.size();
     *nxops = (int)plan.ops.size();
     if (passes)

@@ -43,6 +43,16 @@ enum ExecKind : int32_t {
     // c[0..1] = cos g, sin g.  92 FP32 instructions per double-float pair against 114 for EX_ZY.
     EX_ZT = 14,
     EX_ZC = 15,
+    // EX_ZT / EX_ZC whose input phase diag(1, e^{ig}) was moved into a phase table (EX_PTAB) that
+    // runs earlier in the pass: the real rotations a0' = a0 - t a1, a1' = a1 + t a0 (EX_RT,
+    // c[2] = t) and a0' = u a0 - a1, a1' = a0 + u a1 (EX_RC, c[2] = u): 4 FMA per pair
+    EX_RT = 16,
+    EX_RC = 17,
+    // multiply every tile amplitude l by the phase-table entry T[l] (a diagonal of the tile's
+    // local qubits: the product of the input phases, controlled phases and carried phases the
+    // planner gathered there); the table starts at entry `mask` of the plan's table buffer and
+    // has 2^t entries of (re, im) coefficient slots
+    EX_PTAB = 18,
 };
 
 // Flags of a tile op.
@@ -86,6 +96,9 @@ struct Plan {
     std::vector<PassDesc> passes;
     std::vector<ExecOp> ops;
     std::vector<int> source_index;  // for each ExecOp, index of the llg_op it came from (-1: fused)
+    // phase tables of the EX_PTAB ops: 2^t entries each, two coefficient slots (re, im) per
+    // entry, packed for the plan's precision like ExecOp::c
+    std::vector<uint64_t> tables;
 };
 
 // Lower and plan a gate list into tile passes (llg_plan.cpp).  Returns false with `err` set on
@@ -93,10 +106,14 @@ struct Plan {
 // With use_params, rotations whose `param` >= 0 are kept unfused and lowered to EX_*_P ops whose
 // q1 is the op's occurrence slot (the index of that op among all parametrised ops, in order).
 // With zyz, fused unitary 2x2s are lowered to EX_ZYZ and their global phases folded into the
-// first EX_U2 of the plan (default: on for double-float states without parametrised ops).
+// first EX_U2 of the plan (default: on for double-float and FP64 states without parametrised ops).
 enum PlanZyz : int { ZYZ_DEFAULT = -1, ZYZ_OFF = 0, ZYZ_ON = 1 };
+// With tables, runs of diagonal factors inside a pass (the input phases of carried-phase
+// rotations, the controlled phases of phased CNOTs, carried phases flushed at the end) are
+// gathered into EX_PTAB phase tables where a table replaces more than two complex multiplies per
+// amplitude pair; only kernels that execute EX_PTAB (the engine's tile pass) may run such plans.
 bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int precision, Plan& out, std::string& err,
-                bool use_params = false, int zyz = ZYZ_DEFAULT);
+                bool use_params = false, int zyz = ZYZ_DEFAULT, bool tables = false);
 
 // Lower one gate record to executor ops with GLOBAL qubit indices (streaming path).
 bool lower_op(int n, const llg_op& op, int precision, std::vector<ExecOp>& out, std::string& err);

@@ -167,7 +167,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 
 template <class P>
 __global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, PassDesc pd, const ExecOp* __restrict__ ops,
-                                               double2* __restrict__ mirror) {
+                                               const uint64_t* __restrict__ tables, double2* __restrict__ mirror) {
     using S = typename P::S;
     using K = typename P::K;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -239,6 +239,9 @@ __global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, 
             case EX_ZY: tile_pairs<P, EX_ZY>(tile, tsize >> 1, o.q0, o); break;
             case EX_ZT: tile_pairs<P, EX_ZT>(tile, tsize >> 1, o.q0, o); break;
             case EX_ZC: tile_pairs<P, EX_ZC>(tile, tsize >> 1, o.q0, o); break;
+            case EX_RT: tile_pairs<P, EX_RT>(tile, tsize >> 1, o.q0, o); break;
+            case EX_RC: tile_pairs<P, EX_RC>(tile, tsize >> 1, o.q0, o); break;
+            case EX_PTAB: tile_ptab<P>(tile, tsize, o, tables); break;
             case EX_PHASE1: tile_phase1<P>(tile, tsize, base, o); break;
             case EX_RX: tile_pairs<P, EX_RX>(tile, tsize >> 1, o.q0, o); break;
             case EX_RY: tile_pairs<P, EX_RY>(tile, tsize >> 1, o.q0, o); break;
@@ -408,7 +411,7 @@ template <class PA, class PB>
 __global__ void __launch_bounds__(kThreads) k_compare(const typename PA::S* __restrict__ a, const typename PB::S* __restrict__ b,
                                                       uint64_t size, double* __restrict__ partials) {
     __shared__ double sh[kThreads / 32];
-    double re = 0.0, im = 0.0, na = 0.0, nb = 0.0, mx = 0.0;
+    double re = 0.0, im = 0.0, na = 0.0, nb = 0.0, mx = 0.0, mb = 0.0;
     const uint64_t step = (uint64_t)gridDim.x * kThreads;
     for (uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x; i < size; i += step) {
         const double2 x = PA::to_f64(PA::load(a[i])), y = PB::to_f64(PB::load(b[i]));
@@ -417,15 +420,18 @@ __global__ void __launch_bounds__(kThreads) k_compare(const typename PA::S* __re
         na = fma(x.x, x.x, fma(x.y, x.y, na));
         nb = fma(y.x, y.x, fma(y.y, y.y, nb));
         mx = fmax(mx, fmax(fabs(x.x - y.x), fabs(x.y - y.y)));
+        mb = fmax(mb, fmax(fabs(y.x), fabs(y.y)));
     }
     const double v[4] = {re, im, na, nb};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const double t = block_sum(v[k], sh);
-        if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kRedSlots + k] = t;
+        if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kCmpSlots + k] = t;
     }
     const double m = block_max(mx, sh);
-    if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kRedSlots + 4] = m;
+    if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kCmpSlots + 4] = m;
+    const double m2 = block_max(mb, sh);
+    if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kCmpSlots + 5] = m2;
 }
 
 __global__ void k_finish(const double* __restrict__ partials, int nblocks, double* __restrict__ out) {
@@ -435,6 +441,21 @@ __global__ void k_finish(const double* __restrict__ partials, int nblocks, doubl
     double r = 0.0;
     for (int b = 0; b < nblocks; ++b) r += partials[(size_t)b * kRedSlots + s];
     out[s] = r;
+}
+
+// FP64 FMA throughput probe: eight independent dependency chains per thread keep the FP64
+// pipe's latency covered; the sum is stored only if it takes an impossible value, so the compiler
+// keeps every FMA and nothing is written.
+__global__ void __launch_bounds__(256) k_dfma_rate(double* out, int iters, double m, double c) {
+    double a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = 1.0 + 1e-3 * (threadIdx.x + k);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = fma(a[k], m, c);
+    }
+    const double s = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+    if (s == -1.0) out[0] = s;
 }
 
 template <class P>
@@ -466,8 +487,8 @@ size_t tile_smem_bytes(int t, int low) {
 }
 
 template <class P>
-cudaError_t tile_pass_t(void* vpsi, int n, const PassDesc& pd, const ExecOp* d_ops, int threads, double* mirror,
-                        cudaStream_t s) {
+cudaError_t tile_pass_t(void* vpsi, int n, const PassDesc& pd, const ExecOp* d_ops, const uint64_t* d_tables, int threads,
+                        double* mirror, cudaStream_t s) {
     // the largest dynamic shared memory of any tile, set once (thread-safe static initialisation)
     static const cudaError_t attr = cudaFuncSetAttribute(k_tile<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                          (int)tile_smem_bytes<P>(tile_max_qubits(P::kPrecision), 4));
@@ -475,7 +496,7 @@ cudaError_t tile_pass_t(void* vpsi, int n, const PassDesc& pd, const ExecOp* d_o
     const size_t smem = tile_smem_bytes<P>(pd.t, pd.low);
     const uint64_t ntiles = 1ULL << (n - pd.t);
     if (threads <= 0) threads = pd.t >= 10 ? 512 : (pd.t >= 6 ? (1 << (pd.t - 1)) : 32);
-    k_tile<P><<<(unsigned)ntiles, threads, smem, s>>>(static_cast<typename P::S*>(vpsi), pd, d_ops,
+    k_tile<P><<<(unsigned)ntiles, threads, smem, s>>>(static_cast<typename P::S*>(vpsi), pd, d_ops, d_tables,
                                                       reinterpret_cast<double2*>(mirror));
     return cudaGetLastError();
 }
@@ -522,6 +543,28 @@ cudaError_t launch_exec_op(int P, void* psi, int n, const ExecOp& op, cudaStream
     LLG_DISPATCH(P, return exec_op_t<Pol>(psi, n, op, s));
 }
 
+cudaError_t fp64_fma_rate(int iters, double* fma_per_s) {
+    const unsigned grid = (unsigned)sm_count() * 8;
+    cudaStream_t s = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return e;
+    cudaEvent_t a = nullptr, b = nullptr;
+    if ((e = cudaEventCreate(&a)) == cudaSuccess && (e = cudaEventCreate(&b)) == cudaSuccess) {
+        k_dfma_rate<<<grid, 256, 0, s>>>(nullptr, iters / 8 + 1, 0.9999999, 1e-9);
+        cudaEventRecord(a, s);
+        k_dfma_rate<<<grid, 256, 0, s>>>(nullptr, iters, 0.9999999, 1e-9);
+        cudaEventRecord(b, s);
+        e = cudaEventSynchronize(b);
+        float ms = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+        if (e == cudaSuccess) *fma_per_s = (double)grid * 256.0 * 8.0 * (double)iters / (ms * 1e-3);
+    }
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    cudaStreamDestroy(s);
+    return e;
+}
+
 int tile_copy_take_error() {
     int h = 0;
     cudaMemcpyFromSymbol(&h, g_tile_copy_error, sizeof(int));
@@ -532,9 +575,9 @@ int tile_copy_take_error() {
     return h;
 }
 
-cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, int threads, cudaStream_t s,
-                             double* mirror) {
-    LLG_DISPATCH(P, return tile_pass_t<Pol>(psi, n, pd, d_ops, threads, mirror, s));
+cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, const uint64_t* d_tables,
+                             int threads, cudaStream_t s, double* mirror) {
+    LLG_DISPATCH(P, return tile_pass_t<Pol>(psi, n, pd, d_ops, d_tables, threads, mirror, s));
 }
 
 template <class PA>

@@ -22,8 +22,11 @@ struct ZTerms {
     double coef[kMaxZClasses];
 };
 
-// Per-block partial results of a reduction: up to kRedSlots doubles per block.
+// Per-block partial results of a reduction: up to kRedSlots doubles per block (kCmpSlots for the
+// two-state comparison); the engine's partial buffer holds kRedBlocks x kPartialSlots doubles.
 constexpr int kRedSlots = 1 + kMaxZClasses;
+constexpr int kCmpSlots = 6;
+constexpr int kPartialSlots = 8;
 constexpr int kRedBlocks = 1024;
 
 size_t elem_bytes(int precision);
@@ -33,8 +36,10 @@ cudaError_t launch_exec_op(int P, void* psi, int n, const ExecOp& op, cudaStream
 // threads: CTA size of the tile kernel (0: 512 for tiles of 10+ qubits, else half the tile)
 // mirror: nullptr, or the device address of a host buffer that also receives the pass's output as
 // FP64 (2 doubles per amplitude, full-state indexing)
-cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, int threads, cudaStream_t s,
-                             double* mirror = nullptr);
+// d_tables: the plan's phase tables (Plan::tables on the device), or nullptr for a plan without
+// EX_PTAB ops
+cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, const uint64_t* d_tables,
+                             int threads, cudaStream_t s, double* mirror = nullptr);
 // 1 if a tile pass's bulk load timed out since the last call (the flag is cleared)
 int tile_copy_take_error();
 cudaError_t launch_from_f64(int P, const double* src, void* dst, uint64_t count, cudaStream_t s);
@@ -46,12 +51,15 @@ cudaError_t launch_scale(int P, void* psi, uint64_t count, double factor, cudaSt
 cudaError_t launch_reduce_z(int P, const void* psi, int n, const ZTerms& terms, double* d_partials, double* d_out,
                             cudaStream_t s);
 
-// Two states of equal size, any precisions: per block (kRedSlots doubles each) Re <a|b>, Im <a|b>,
-// <a|a>, <b|b> and max |a_i - b_i| (re and im parts); *nblocks = blocks written
+// Two states of equal size, any precisions: per block (kCmpSlots doubles each) Re <a|b>, Im <a|b>,
+// <a|a>, <b|b>, max |a_i - b_i| and max |b_i| (over re and im parts); *nblocks = blocks written
 cudaError_t launch_compare(int PA, const void* a, int PB, const void* b, uint64_t size, double* partials, int* nblocks,
                            cudaStream_t s);
 
 int tile_max_qubits(int P);
+
+// FP64 FMA operations per second of the current device (one timed launch of `iters` iterations)
+cudaError_t fp64_fma_rate(int iters, double* fma_per_s);
 
 // dense k-qubit block (llg_block.cu): bit j of a row/column index is qubit q[j]; the matrix is
 // 2 * 4^k coefficient slots, row-major (re, im), packed for the state's precision

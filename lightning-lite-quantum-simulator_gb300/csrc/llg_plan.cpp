@@ -182,6 +182,259 @@ struct Pending {
 
 }  // namespace
 
+// The double held by a coefficient slot packed for LLG_F64.
+static double coef_value(uint64_t bits) {
+    double v;
+    std::memcpy(&v, &bits, sizeof(v));
+    return v;
+}
+
+// ------------------------------------------------------------------------------------------
+// Phase tables.  A diagonal factor commutes with every op that leaves the Z basis of its qubits
+// alone, so inside a pass it may slide to any slot between the ops that do not.  Three kinds of
+// diagonal factors are gathered:
+//   * the input phase diag(1, e^{ig}) of a carried-phase rotation (EX_ZT / EX_ZC / EX_ZY); it may
+//     move earlier, back to the previous op that mixes its qubit;
+//   * the controlled phase of a phased CNOT (control local), applied after the CNOT's swap; it
+//     may move later, up to the next op that mixes its control or target;
+//   * a local carried-phase flush (EX_PHASE1) or diagonal (EX_DIAG), in both directions.
+// Each factor has an interval of slots (slot s = just before op s).  The fewest points that
+// stab every interval are chosen greedily (intervals by right end); a point becomes one EX_PTAB
+// when its factors save more complex multiplies per amplitude pair than the table costs (2: one
+// multiply per amplitude), and the rotations it serves become the real forms EX_RT / EX_RC /
+// EX_RY.  The table's entry l is the product of the point's factors at the tile's local index l.
+// ------------------------------------------------------------------------------------------
+namespace {
+
+struct DiagFactor {
+    int kind;       // 0 rotation input phase, 1 controlled phase, 2 one-qubit diagonal op
+    int op;         // index of the op in the pass
+    int q0, q1;     // local qubits: the phase's qubit; for 1 the control and the target
+    std::complex<double> v0, v1;  // kind 2: the values on bit 0 and bit 1; else v1 only
+    int lo, hi;     // slots it may move to
+    double saves;   // complex multiplies per amplitude pair when applied on its own
+    int point = -1;
+};
+
+// Does an op mix the Z basis of local qubit q (is it an op a diagonal on q cannot pass)?
+bool mixes(const ExecOp& e, int q) {
+    switch (e.kind) {
+        case EX_CNOT: return e.q1 == q;
+        case EX_DIAG:
+        case EX_PHASE1:
+        case EX_MCZ:
+        case EX_RZ_P:
+        case EX_PTAB: return false;
+        default: return e.q0 == q;  // every other kind is a non-diagonal op on its target q0
+    }
+}
+
+}  // namespace
+
+static void gather_phase_tables(Plan& out) {
+    using cd = std::complex<double>;
+    std::vector<ExecOp> ops;
+    std::vector<int> src;
+    ops.reserve(out.ops.size());
+    src.reserve(out.ops.size());
+    for (PassDesc& pd : out.passes) {
+        const int b = pd.op_begin, m = pd.nops, t = pd.t;
+        // Reorder the pass by ASAP depth (an op's depth is one more than the deepest earlier op
+        // sharing a qubit with it; ops keep their order within a depth).  Ops on shared qubits keep
+        // their relative order, so the product is unchanged, and the rotations of one depth become
+        // adjacent: one table point can then serve all of them.
+        {
+            std::vector<int> depth(m), last(t + 64, 0);
+            auto res = [&](const ExecOp& x, std::vector<int>& r) {  // local q -> q, global q -> t + q
+                r.clear();
+                const bool nl = (x.flags & OPF_NONLOCAL_Q0) != 0;
+                switch (x.kind) {
+                    case EX_CNOT:
+                        r.push_back(nl ? t + x.q0 : x.q0);
+                        r.push_back(x.q1);
+                        break;
+                    case EX_MCZ:
+                        for (int q = 0; q < t; ++q)
+                            if (x.mask >> q & 1) r.push_back(q);
+                        for (int q = 0; q < 64; ++q)
+                            if (x.nl_mask >> q & 1) r.push_back(t + q);
+                        break;
+                    default: r.push_back(nl ? t + x.q0 : x.q0); break;
+                }
+            };
+            std::vector<int> r;
+            for (int i = 0; i < m; ++i) {
+                res(out.ops[b + i], r);
+                int d = 0;
+                for (int q : r) d = std::max(d, last[q]);
+                depth[i] = d + 1;
+                for (int q : r) last[q] = d + 1;
+            }
+            std::vector<int> ord(m);
+            for (int i = 0; i < m; ++i) ord[i] = i;
+            std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) { return depth[a] < depth[c]; });
+            std::vector<ExecOp> tmp(m);
+            std::vector<int> tsrc(m);
+            for (int i = 0; i < m; ++i) {
+                tmp[i] = out.ops[b + ord[i]];
+                tsrc[i] = out.source_index[b + ord[i]];
+            }
+            for (int i = 0; i < m; ++i) {
+                out.ops[b + i] = tmp[i];
+                out.source_index[b + i] = tsrc[i];
+            }
+        }
+        const ExecOp* e = out.ops.data() + b;
+        std::vector<DiagFactor> fs;
+        auto last_mix = [&](int i, int q) {  // last op before i that mixes q (-1: none)
+            for (int j = i - 1; j >= 0; --j)
+                if (mixes(e[j], q)) return j;
+            return -1;
+        };
+        auto next_mix = [&](int i, int qa, int qb) {  // first op after i that mixes qa or qb (m: none)
+            for (int j = i + 1; j < m; ++j)
+                if (mixes(e[j], qa) || (qb >= 0 && mixes(e[j], qb))) return j;
+            return m;
+        };
+        for (int i = 0; i < m; ++i) {
+            const ExecOp& x = e[i];
+            DiagFactor f{};
+            f.op = i;
+            if ((x.kind == EX_ZT || x.kind == EX_ZC || x.kind == EX_ZY) &&
+                !(coef_value(x.c[0]) == 1.0 && coef_value(x.c[1]) == 0.0)) {
+                f.kind = 0;
+                f.q0 = x.q0;
+                f.v1 = cd(coef_value(x.c[0]), coef_value(x.c[1]));
+                f.lo = last_mix(i, x.q0) + 1;
+                f.hi = i;
+                f.saves = 1.0;  // a1 times e^{ig}: one multiply per pair
+            } else if (x.kind == EX_CNOT && (x.flags & OPF_PHASE) && !(x.flags & OPF_NONLOCAL_Q0)) {
+                f.kind = 1;
+                f.q0 = x.q0;
+                f.q1 = x.q1;
+                f.v1 = cd(coef_value(x.c[0]), coef_value(x.c[1]));
+                f.lo = i + 1;
+                f.hi = next_mix(i, x.q0, x.q1);
+                f.saves = 0.5;  // a quarter of the amplitudes
+            } else if ((x.kind == EX_PHASE1 || x.kind == EX_DIAG) && !(x.flags & OPF_NONLOCAL_Q0)) {
+                f.kind = 2;
+                f.q0 = x.q0;
+                if (x.kind == EX_PHASE1) {
+                    f.v0 = 1.0;
+                    f.v1 = cd(coef_value(x.c[0]), coef_value(x.c[1]));
+                    f.saves = 1.0;
+                } else {
+                    f.v0 = cd(coef_value(x.c[0]), coef_value(x.c[1]));
+                    f.v1 = cd(coef_value(x.c[2]), coef_value(x.c[3]));
+                    f.saves = 2.0;
+                }
+                f.lo = last_mix(i, x.q0) + 1;
+                f.hi = next_mix(i, x.q0, -1);
+            } else {
+                continue;
+            }
+            fs.push_back(f);
+        }
+        // greedy stabbing by right end, then keep the points that pay for their table
+        std::vector<int> order(fs.size());
+        for (size_t k = 0; k < fs.size(); ++k) order[k] = (int)k;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return fs[a].hi < fs[c].hi; });
+        std::vector<int> pts;      // slot of each point
+        std::vector<double> gain;  // multiplies saved per pair
+        for (int k : order) {
+            if (pts.empty() || pts.back() < fs[k].lo) {
+                pts.push_back(fs[k].hi);
+                gain.push_back(0.0);
+            }
+            fs[k].point = (int)pts.size() - 1;
+            gain.back() += fs[k].saves;
+        }
+        std::vector<char> keep(pts.size());
+        for (size_t p = 0; p < pts.size(); ++p) keep[p] = gain[p] > 2.0;
+        // tables of the kept points
+        std::vector<long> table_of(pts.size(), -1);
+        const size_t entries = (size_t)1 << t;
+        for (size_t p = 0; p < pts.size(); ++p) {
+            if (!keep[p]) continue;
+            std::vector<cd> qv(t, cd(1.0, 0.0)), q0v(t, cd(1.0, 0.0));  // per-qubit bit-1 / bit-0 factors
+            std::vector<const DiagFactor*> cps;
+            for (const DiagFactor& f : fs) {
+                if (f.point != (int)p) continue;
+                if (f.kind == 1) cps.push_back(&f);
+                else {
+                    qv[f.q0] *= f.v1;
+                    if (f.kind == 2) q0v[f.q0] *= f.v0;
+                }
+            }
+            std::vector<cd> tab(entries);
+            tab[0] = 1.0;
+            for (int q = 0; q < t; ++q) {  // doubling: entries with bit q set from those without
+                const size_t half = (size_t)1 << q;
+                const bool scale0 = !(q0v[q].real() == 1.0 && q0v[q].imag() == 0.0);
+                for (size_t l = 0; l < half; ++l) {
+                    tab[l | half] = tab[l] * qv[q];
+                    if (scale0) tab[l] *= q0v[q];
+                }
+            }
+            for (const DiagFactor* f : cps) {
+                const size_t both = ((size_t)1 << f->q0) | ((size_t)1 << f->q1);
+                for (size_t l = 0; l < entries; ++l)
+                    if ((l & both) == both) tab[l] *= f->v1;
+            }
+            table_of[p] = (long)(out.tables.size() / 2);
+            for (const cd& v : tab) {
+                out.tables.push_back(pack_coef(LLG_F64, v.real()));
+                out.tables.push_back(pack_coef(LLG_F64, v.imag()));
+            }
+        }
+        // rewrite the pass
+        std::vector<int> pt_at(m + 1, -1);
+        for (size_t p = 0; p < pts.size(); ++p)
+            if (keep[p]) pt_at[pts[p]] = (int)p;
+        std::vector<int> absorbed(m, 0);  // 1: factor moved into a table
+        for (const DiagFactor& f : fs)
+            if (keep[f.point]) absorbed[f.op] = 1;
+        const int begin = (int)ops.size();
+        for (int i = 0; i <= m; ++i) {
+            if (pt_at[i] >= 0) {
+                ExecOp tp = blank(EX_PTAB);
+                tp.mask = (uint64_t)table_of[pt_at[i]];
+                ops.push_back(tp);
+                src.push_back(-1);
+            }
+            if (i == m) break;
+            ExecOp x = e[i];
+            if (absorbed[i]) {
+                switch (x.kind) {
+                    case EX_ZT:
+                    case EX_ZC:
+                        x.kind = x.kind == EX_ZT ? EX_RT : EX_RC;
+                        x.c[0] = pack_coef(LLG_F64, 1.0);
+                        x.c[1] = 0;
+                        break;
+                    case EX_ZY:  // RY(b) with the pass scale folded into (c, s)
+                        x.kind = EX_RY;
+                        x.c[0] = x.c[2];
+                        x.c[1] = x.c[3];
+                        x.c[2] = x.c[3] = 0;
+                        break;
+                    case EX_CNOT:
+                        x.flags &= ~OPF_PHASE;
+                        x.c[0] = x.c[1] = 0;
+                        break;
+                    default: continue;  // EX_PHASE1 / EX_DIAG: wholly in the table
+                }
+            }
+            ops.push_back(x);
+            src.push_back(out.source_index[b + i]);
+        }
+        pd.op_begin = begin;
+        pd.nops = (int)ops.size() - begin;
+    }
+    out.ops.swap(ops);
+    out.source_index.swap(src);
+}
+
 static bool is_param_op(const llg_op& op, bool use_params) {
     return use_params && op.param >= 0 && (op.kind == LLG_OP_RX || op.kind == LLG_OP_RY || op.kind == LLG_OP_RZ);
 }
@@ -218,11 +471,14 @@ static bool split_zyz(const double* m, std::complex<double>& z, double& c, doubl
 }
 
 bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan& out, std::string& err,
-                bool use_params, int zyz) {
+                bool use_params, int zyz, bool tables) {
     out.passes.clear();
     out.ops.clear();
     out.source_index.clear();
-    const bool use_zyz = zyz == ZYZ_DEFAULT ? (P == LLG_DF64 && !use_params) : zyz == ZYZ_ON;
+    out.tables.clear();
+    // coefficients are planned as FP64 bits and packed for the state's precision at the end
+    constexpr int PP = LLG_F64;
+    const bool use_zyz = zyz == ZYZ_DEFAULT ? ((P == LLG_DF64 || P == LLG_F64) && !use_params) : zyz == ZYZ_ON;
     // the phase carrier: the plan's first EX_U2, which also applies the global phases dropped by
     // every EX_ZYZ (a scalar factor commutes with every op, so any op of the flush may carry it)
     int carrier = -1;
@@ -403,14 +659,14 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
                     e = blank(EX_ZY);
                     e.q0 = q;
                     const double v[4] = {eg.real(), eg.imag(), sigma * c, sigma * sn};
-                    for (int k = 0; k < 4; ++k) e.c[k] = pack_coef(P, v[k]);
+                    for (int k = 0; k < 4; ++k) e.c[k] = pack_coef(PP, v[k]);
                     sigma = 1.0;
                     last_t = -1;
                 } else {
                     e = blank(tan_form ? EX_ZT : EX_ZC);
                     e.q0 = q;
                     const double v[3] = {eg.real(), eg.imag(), tan_form ? sn / c : c / sn};
-                    for (int k = 0; k < 3; ++k) e.c[k] = pack_coef(P, v[k]);
+                    for (int k = 0; k < 3; ++k) e.c[k] = pack_coef(PP, v[k]);
                     sigma *= f;
                     last_t = (int)out.ops.size();
                     last_f = f;
@@ -421,13 +677,13 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
                 emit_raw(e, src);
                 return;
             }
-            for (int k = 0; k < 8; ++k) e.c[k] = pack_coef(P, m[k]);
+            for (int k = 0; k < 8; ++k) e.c[k] = pack_coef(PP, m[k]);
             emit_raw(e, src);
         };
         auto emit_lowered = [&](const llg_op& gop, int src) -> bool {
             if (!use_zyz) {
                 std::vector<ExecOp> tmp;
-                if (!lower_op(n, gop, P, tmp, err)) return false;
+                if (!lower_op(n, gop, PP, tmp, err)) return false;
                 for (ExecOp& e : tmp) emit_raw(e, src);
                 return true;
             }
@@ -461,14 +717,14 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
                 case LLG_OP_U2: emit_u2(gop.m, q, src); return true;
                 case LLG_OP_CNOT: {
                     std::vector<ExecOp> tmp;
-                    if (!lower_op(n, gop, P, tmp, err)) return false;
+                    if (!lower_op(n, gop, PP, tmp, err)) return false;
                     const cd p = ph[gop.q1];
                     if (!is_one(p)) {
                         ph[gop.q0] *= p;
                         const cd cp = 1.0 / (p * p);
                         tmp[0].flags |= OPF_PHASE;
-                        tmp[0].c[0] = pack_coef(P, cp.real());
-                        tmp[0].c[1] = pack_coef(P, cp.imag());
+                        tmp[0].c[0] = pack_coef(PP, cp.real());
+                        tmp[0].c[1] = pack_coef(PP, cp.imag());
                     }
                     emit_raw(tmp[0], src);
                     return true;
@@ -476,7 +732,7 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
                 default: break;  // cz, mcz: diagonal, they commute with the carried phases
             }
             std::vector<ExecOp> tmp;
-            if (!lower_op(n, gop, P, tmp, err)) return false;
+            if (!lower_op(n, gop, PP, tmp, err)) return false;
             for (ExecOp& e : tmp) emit_raw(e, src);
             return true;
         };
@@ -503,10 +759,10 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
                 std::vector<ExecOp> tmp;
                 ExecOp e = blank(EX_DIAG);
                 e.q0 = q;
-                e.c[0] = pack_coef(P, p.m[0]);
-                e.c[1] = pack_coef(P, p.m[1]);
-                e.c[2] = pack_coef(P, p.m[6]);
-                e.c[3] = pack_coef(P, p.m[7]);
+                e.c[0] = pack_coef(PP, p.m[0]);
+                e.c[1] = pack_coef(PP, p.m[1]);
+                e.c[2] = pack_coef(PP, p.m[6]);
+                e.c[3] = pack_coef(PP, p.m[7]);
                 if (to_local[q] >= 0) e.q0 = to_local[q];
                 else e.flags |= OPF_NONLOCAL_Q0;
                 out.ops.push_back(e);
@@ -564,7 +820,7 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
             const double g = sigma / last_f;
             e.kind = EX_ZY;
             const double v[4] = {last_g.real(), last_g.imag(), g * last_c, g * last_s};
-            for (int k = 0; k < 4; ++k) e.c[k] = pack_coef(P, v[k]);
+            for (int k = 0; k < 4; ++k) e.c[k] = pack_coef(PP, v[k]);
         }
         pd.nops = (int)out.ops.size() - pd.op_begin;
         if (included.empty()) {
@@ -592,8 +848,8 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
         for (int q = 0; q < n; ++q) {
             if (is_one(ph[q])) continue;
             ExecOp e = blank(EX_PHASE1);
-            e.c[0] = pack_coef(P, ph[q].real());
-            e.c[1] = pack_coef(P, ph[q].imag());
+            e.c[0] = pack_coef(PP, ph[q].real());
+            e.c[1] = pack_coef(PP, ph[q].imag());
             if (to_local[q] >= 0) e.q0 = to_local[q];
             else {
                 e.q0 = q;
@@ -605,8 +861,8 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
         if (carrier < 0 && !is_one(phase)) {
             ExecOp e = blank(EX_DIAG);  // local qubit 0 of the tile, both entries the phase
             e.q0 = 0;
-            e.c[0] = e.c[2] = pack_coef(P, phase.real());
-            e.c[1] = e.c[3] = pack_coef(P, phase.imag());
+            e.c[0] = e.c[2] = pack_coef(PP, phase.real());
+            e.c[1] = e.c[3] = pack_coef(PP, phase.imag());
             append(e);
             phase = 1.0;
         }
@@ -614,9 +870,15 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
     if (carrier >= 0 && (phase.real() != 1.0 || phase.imag() != 0.0)) {
         for (int r = 0; r < 4; ++r) {
             const std::complex<double> v = phase * std::complex<double>(carrier_m[2 * r], carrier_m[2 * r + 1]);
-            out.ops[carrier].c[2 * r] = pack_coef(P, v.real());
-            out.ops[carrier].c[2 * r + 1] = pack_coef(P, v.imag());
+            out.ops[carrier].c[2 * r] = pack_coef(PP, v.real());
+            out.ops[carrier].c[2 * r + 1] = pack_coef(PP, v.imag());
         }
+    }
+    if (tables) gather_phase_tables(out);
+    if (P != PP) {
+        for (ExecOp& e : out.ops)
+            for (uint64_t& c : e.c) c = pack_coef(P, coef_value(c));
+        for (uint64_t& c : out.tables) c = pack_coef(P, coef_value(c));
     }
     return true;
 }

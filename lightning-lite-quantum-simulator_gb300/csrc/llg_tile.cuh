@@ -81,6 +81,18 @@ struct PairMath {
             a0.im = P::fma1_raw(u, y0, P::neg(zi));
             a1.re = P::fma1_raw(u, zr, x0);
             a1.im = P::fma1_raw(u, zi, y0);
+        } else if (KIND == EX_RT) {  // [1, -t; t, 1] (input phase applied by a phase table)
+            const auto t = k[2], mt = P::kneg(k[2]);
+            a0.re = P::fma1_raw(mt, x1, x0);
+            a0.im = P::fma1_raw(mt, y1, y0);
+            a1.re = P::fma1_raw(t, x0, x1);
+            a1.im = P::fma1_raw(t, y0, y1);
+        } else if (KIND == EX_RC) {  // [u, -1; 1, u]
+            const auto u = k[2];
+            a0.re = P::fma1_raw(u, x0, P::neg(x1));
+            a0.im = P::fma1_raw(u, y0, P::neg(y1));
+            a1.re = P::fma1_raw(u, x1, x0);
+            a1.im = P::fma1_raw(u, y1, y0);
         } else if (KIND == EX_H) {  // r [1, 1; 1, -1]
             const auto r = k[0], mr = P::kneg(k[0]);
             a0.re = P::lin2_raw(r, x0, r, x1);
@@ -142,6 +154,22 @@ __device__ __forceinline__ void tile_phase1(typename P::S* tile, uint32_t tsize,
     }
 }
 
+// EX_PTAB: every amplitude l of the tile times the phase-table entry T[l] (the table starts at
+// entry o.mask of `tables`; two coefficient slots (re, im) per entry, read through the L2 cache)
+template <class P>
+__device__ __forceinline__ void tile_ptab(typename P::S* tile, uint32_t tsize, const ExecOp& o,
+                                          const uint64_t* __restrict__ tables) {
+    using K = typename P::K;
+    const ulonglong2* tb = reinterpret_cast<const ulonglong2*>(tables) + o.mask;
+    for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
+        const ulonglong2 w = __ldg(tb + l);
+        const K tr = P::k_from_bits(w.x), ti = P::k_from_bits(w.y);
+        auto a = P::load(tile[l]);
+        cmul_const<P>(a, tr, ti, P::kneg(ti));
+        tile[l] = P::store(a);
+    }
+}
+
 // CNOT (control q0, possibly a tile-uniform global qubit; target q1 local); with OPF_PHASE the
 // amplitudes that end with control = target = 1 are then multiplied by c[0] + i c[1]
 template <class P>
@@ -199,6 +227,8 @@ __device__ void tile_apply(typename P::S* tile, uint32_t tsize, uint64_t base, c
         case EX_ZY: tile_pairs<P, EX_ZY>(tile, tsize >> 1, o.q0, o); break;
         case EX_ZT: tile_pairs<P, EX_ZT>(tile, tsize >> 1, o.q0, o); break;
         case EX_ZC: tile_pairs<P, EX_ZC>(tile, tsize >> 1, o.q0, o); break;
+        case EX_RT: tile_pairs<P, EX_RT>(tile, tsize >> 1, o.q0, o); break;
+        case EX_RC: tile_pairs<P, EX_RC>(tile, tsize >> 1, o.q0, o); break;
         case EX_PHASE1: tile_phase1<P>(tile, tsize, base, o); break;
         case EX_RX: tile_pairs<P, EX_RX>(tile, tsize >> 1, o.q0, o); break;
         case EX_RY: tile_pairs<P, EX_RY>(tile, tsize >> 1, o.q0, o); break;

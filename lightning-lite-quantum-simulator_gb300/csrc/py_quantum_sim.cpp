@@ -42,14 +42,15 @@ void check(int rc) {
 }
 
 int parse_precision(const std::string& p) {
-    if (p == "complex128" || p == "df64" || p == "c128") return LLG_DF64;
-    if (p == "fp64" || p == "f64") return LLG_F64;
+    if (p == "df64") return LLG_DF64;
+    if (p == "complex128" || p == "c128" || p == "fp64" || p == "f64") return LLG_F64;
     if (p == "complex64" || p == "c64" || p == "f32") return LLG_F32;
-    throw py::value_error("precision must be 'complex128' (double-float, default), 'fp64' or 'complex64'");
+    throw py::value_error("precision must be 'complex128' (IEEE FP64, default; alias 'fp64'), 'df64' (double-float) "
+                          "or 'complex64'");
 }
 
 const char* precision_name(int p) {
-    return p == LLG_F64 ? "fp64" : (p == LLG_F32 ? "complex64" : "complex128");
+    return p == LLG_F64 ? "complex128" : (p == LLG_F32 ? "complex64" : "df64");
 }
 
 // A 2x2 gate given as any sequence of 4 complex-castable entries (the reference takes a list).

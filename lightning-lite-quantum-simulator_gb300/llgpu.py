@@ -27,7 +27,9 @@ OP_H, OP_X, OP_RX, OP_RY, OP_RZ, OP_CNOT, OP_MCZ, OP_CZ, OP_U2 = range(9)
 PROF_CLASSES = 4
 PROF_NAMES = ("tile", "gate", "init", "readout")
 
-PRECISIONS = {"fp64": LLG_F64, "complex128": LLG_DF64, "df64": LLG_DF64, "complex64": LLG_F32}
+# "complex128" is the reference's arithmetic: IEEE binary64 (LLG_F64).  "df64" keeps each real part as an
+# fp32 pair (about 48 significant bits, faster on this GPU's FP32 pipe); "complex64" is FP32.
+PRECISIONS = {"complex128": LLG_F64, "fp64": LLG_F64, "f64": LLG_F64, "df64": LLG_DF64, "complex64": LLG_F32}
 
 # numpy view of llg_op (96 bytes)
 OP_DTYPE = np.dtype([
@@ -110,9 +112,11 @@ def lib() -> ctypes.CDLL:
             "llg_host_free": (None, [vp]),
             "llg_plan_export": (i, [i, vp, i, i, vp, i, P(i), vp, i, P(i)]),
             "llg_plan_export_ex": (i, [i, vp, i, i, i, vp, i, P(i), vp, i, P(i)]),
+            "llg_plan_export_tables": (i, [i, vp, i, i, i, vp, ctypes.c_int64, P(ctypes.c_int64)]),
             "llg_profile": (i, [vp, i]),
             "llg_profile_read": (i, [vp, vp, vp, i]),
             "llg_kernel_launches": (ctypes.c_int64, []),
+            "llg_fp64_fma_rate": (i, [i, P(d)]),
             "llg_get_stream": (i, [vp, P(vp)]),
             "llg_expect_zz_noalloc": (i, [vp, i, i, i, vp, vp, vp, vp, vp]),
             "llg_adjoint_create": (i, [i, vp, i, i, i, i, i, vp, vp, vp, P(vp)]),
@@ -135,6 +139,7 @@ def lib() -> ctypes.CDLL:
             "llg_batch_config": (i, [vp, P(i), P(i), P(i)]),
             "llg_set_tile_threads": (i, [vp, i]),
             "llg_compare": (i, [vp, vp, P(d), P(d)]),
+            "llg_compare_ex": (i, [vp, vp, P(d), P(d), P(d)]),
             "llg_get_tuning": (i, [vp, P(i), P(i), P(i)]),
             "llg_autotune": (i, [vp, vp, i, i, vp]),
             "llg_tune_cache_clear": (None, []),
@@ -345,6 +350,13 @@ class State:
         check(lib().llg_compare(self._h, other._h, ctypes.byref(f), ctypes.byref(d)))
         return f.value, d.value
 
+    def compare_ex(self, other: "State") -> tuple[float, float, float]:
+        """compare() plus the largest |re| or |im| of `other`'s amplitudes (the scale of a relative
+        error)."""
+        f, d, m = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(lib().llg_compare_ex(self._h, other._h, ctypes.byref(f), ctypes.byref(d), ctypes.byref(m)))
+        return f.value, d.value, m.value
+
     def expect_zz(self, a: Sequence[int], b: Sequence[int], coeff: Sequence[float]) -> float:
         aa = np.ascontiguousarray(a, dtype=np.int32)
         bb = np.ascontiguousarray(b, dtype=np.int32)
@@ -380,13 +392,16 @@ class State:
 # planner introspection (host only)
 # ---------------------------------------------------------------------------------------------
 PLAN_ZYZ = 1
+PLAN_TABLES = 2
 
 
-def plan_export(n: int, ops: np.ndarray, tile_qubits: int, zyz: bool = False):
+def plan_export(n: int, ops: np.ndarray, tile_qubits: int, zyz: bool = False, tables: bool = False):
     """Host-side plan of `ops` (passes, executor ops; coefficients as doubles).  zyz=True plans
-    as the engine does for complex128 states (fused unitary 2x2s as ZYZ ops)."""
+    as the engine does for complex128 states (fused unitary 2x2s as carried-phase rotations);
+    tables=True (with zyz) also gathers diagonal factors into phase tables, and the result gains a
+    third item: the tables as a complex array (2^tile_qubits entries per table)."""
     ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
-    flags = PLAN_ZYZ if zyz else 0
+    flags = (PLAN_ZYZ if zyz else 0) | (PLAN_TABLES if tables else 0)
     npasses, nx = ctypes.c_int(), ctypes.c_int()
     check(lib().llg_plan_export_ex(n, _ptr(ops) if ops.size else None, ops.size, tile_qubits, flags, None, 0,
                                    ctypes.byref(npasses), None, 0, ctypes.byref(nx)))
@@ -394,7 +409,22 @@ def plan_export(n: int, ops: np.ndarray, tile_qubits: int, zyz: bool = False):
     xops = np.zeros(max(nx.value, 1), dtype=XOP_DTYPE)
     check(lib().llg_plan_export_ex(n, _ptr(ops) if ops.size else None, ops.size, tile_qubits, flags, _ptr(passes),
                                    passes.size, ctypes.byref(npasses), _ptr(xops), xops.size, ctypes.byref(nx)))
-    return passes, xops[: nx.value]
+    if not tables:
+        return passes, xops[: nx.value]
+    nd = ctypes.c_int64()
+    check(lib().llg_plan_export_tables(n, _ptr(ops) if ops.size else None, ops.size, tile_qubits, flags, None, 0,
+                                       ctypes.byref(nd)))
+    tab = np.zeros(max(nd.value, 2), dtype=np.float64)
+    check(lib().llg_plan_export_tables(n, _ptr(ops) if ops.size else None, ops.size, tile_qubits, flags, _ptr(tab),
+                                       tab.size, ctypes.byref(nd)))
+    return passes, xops[: nx.value], tab[: nd.value].view(np.complex128)
+
+
+def fp64_fma_rate(iters: int = 1 << 16) -> float:
+    """FP64 fused multiply-adds per second of the current device (a timed throughput kernel)."""
+    v = ctypes.c_double()
+    check(lib().llg_fp64_fma_rate(iters, ctypes.byref(v)))
+    return v.value
 
 
 def ring_zz_terms(n: int):

@@ -10,6 +10,10 @@
   src/Mitigation.h.
   It needs the reference tree and pybind11 headers, so it only runs where both exist.
 
+Where the reference tree lies: the environment variable LLG_REFERENCE_ROOT, else DEFAULT_REF (the
+place this recipe reads it from on the build machine).  ``reference_root()`` returns None where
+neither holds the tree (the GPU machine): the reference build and the tests that need the tree skip.
+
 Run ``python oracle/build_oracle.py [--ref]``.
 """
 from __future__ import annotations
@@ -24,6 +28,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
 DEFAULT_REF = "/root/reference"
+REF_ENV = "LLG_REFERENCE_ROOT"
 
 
 def _run(cmd: list[str]) -> None:
@@ -55,13 +60,26 @@ def build_oracle(force: bool = False) -> str:
     return out
 
 
-def ref_available(ref: str = DEFAULT_REF) -> bool:
-    return os.path.isfile(os.path.join(ref, "src", "StateVectorBackend.h"))
+def _is_tree(ref: str | None) -> bool:
+    return bool(ref) and os.path.isfile(os.path.join(ref, "src", "StateVectorBackend.h"))
 
 
-def build_ref(ref: str = DEFAULT_REF, force: bool = False) -> dict[str, str]:
+def reference_root() -> str | None:
+    """The reference tree (LLG_REFERENCE_ROOT, else DEFAULT_REF), or None where it is absent."""
+    for ref in (os.environ.get(REF_ENV), DEFAULT_REF):
+        if _is_tree(ref):
+            return ref
+    return None
+
+
+def ref_available(ref: str | None = None) -> bool:
+    return _is_tree(ref) if ref else reference_root() is not None
+
+
+def build_ref(ref: str | None = None, force: bool = False) -> dict[str, str]:
     """Compile the reference's own sources into oracle/_ref (only where the tree exists)."""
-    if not ref_available(ref):
+    ref = ref or reference_root()
+    if not _is_tree(ref):
         raise FileNotFoundError(f"reference sources not found under {ref}")
     import pybind11  # only needed here, where the reference is built
 

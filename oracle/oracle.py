@@ -349,3 +349,41 @@ def lindblad_exact(h, channels, rho0, duration: float, steps: int) -> np.ndarray
     out = np.zeros_like(r0)
     lib().orc_lindblad_exact(d, _p(hh), len(channels), _p(ls), _p(gs), _p(r0), duration, steps, _p(out))
     return out
+
+
+def fuse_gate_list(n: int, ops: np.ndarray):
+    """The reference's own fused CPU path for an op list: runs of consecutive single-qubit gates
+    on one target merged into one 2x2, the later gate on the left (GateFuser.fuse_circuit,
+    python/gate_fusion.py:15-37, as benchmarks/benchmark_fusion.py:36-50 feeds it to
+    apply_gate_cache_optimized); CNOT / CZ / MCZ records stay as they are and end a run.
+    Returns a list of ("u2", target, 2x2 matrix) and ("op", record) items."""
+    out = []
+    for op in ops:
+        k = int(op["kind"])
+        if k in (0, 1, 2, 3, 4, 8):  # H, X, RX, RY, RZ, U2
+            m = _op_matrix(op)
+            q = int(op["q0"])
+            if out and out[-1][0] == "u2" and out[-1][1] == q:
+                out[-1] = ("u2", q, m @ out[-1][2])
+            else:
+                out.append(("u2", q, m))
+        else:
+            out.append(("op", op))
+    return out
+
+
+def _op_matrix(op) -> np.ndarray:
+    k, t = int(op["kind"]), float(op["theta"])
+    c, s = np.cos(0.5 * t), np.sin(0.5 * t)
+    r = 1.0 / np.sqrt(2.0)
+    if k == 0:
+        return np.array([[r, r], [r, -r]], dtype=complex)
+    if k == 1:
+        return np.array([[0, 1], [1, 0]], dtype=complex)
+    if k == 2:
+        return np.array([[c, -1j * s], [-1j * s, c]])
+    if k == 3:
+        return np.array([[c, -s], [s, c]], dtype=complex)
+    if k == 4:
+        return np.diag([np.exp(-0.5j * t), np.exp(0.5j * t)])
+    return np.asarray(op["m"], dtype=np.float64).view(np.complex128).reshape(2, 2)

@@ -1,6 +1,7 @@
 """Writes the golden fixtures in this directory by running the REFERENCE's own code.
 
-Runs only where the reference tree is present (it is read at /root/reference, never copied):
+Runs only where the reference tree is present (found by oracle/build_oracle.py's
+reference_root(); it is read in place, never copied):
   * oracle/_ref/libref.so -- ll::ReferenceBackend, ll::StateVectorBackend, ll::Grover,
     ll::VQE::prepare, ll::NoisyBackend and ll::ZNE compiled from the reference headers
     (oracle/build_oracle.py --ref);
@@ -22,11 +23,12 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference"
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 sys.path.insert(0, os.path.join(REPO, "lightning-lite-quantum-simulator_gb300"))
 
 import build_oracle  # noqa: E402
+
+REF = build_oracle.reference_root()
 import workloads  # noqa: E402
 from llgpu import OP_DTYPE  # noqa: E402
 

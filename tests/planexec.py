@@ -24,6 +24,10 @@ def _matrix(x) -> np.ndarray:
     if k == 15:  # [u, -1; 1, u] diag(1, eg)
         eg, u = c[0] + 1j * c[1], c[2]
         return np.array([[u, -1], [1, u]], dtype=complex) @ np.diag([1, eg])
+    if k == 16:  # [1, -t; t, 1] (input phase applied by a phase table)
+        return np.array([[1, -c[2]], [c[2], 1]], dtype=complex)
+    if k == 17:  # [u, -1; 1, u]
+        return np.array([[c[2], -1], [1, c[2]]], dtype=complex)
     if k == 11:  # diag(1, ea) [c, -s; s, c] diag(1, eg)
         eg, ea = c[0] + 1j * c[1], c[4] + 1j * c[5]
         ry = np.array([[c[2], -c[3]], [c[3], c[2]]], dtype=complex)
@@ -39,7 +43,7 @@ def _pair(tile: np.ndarray, q: int, m: np.ndarray) -> None:
     v[:, :, 1, :] = m[1, 0] * a0 + m[1, 1] * a1
 
 
-def execute(psi: np.ndarray, n: int, passes: np.ndarray, xops: np.ndarray) -> np.ndarray:
+def execute(psi: np.ndarray, n: int, passes: np.ndarray, xops: np.ndarray, tables: np.ndarray | None = None) -> np.ndarray:
     psi = psi.copy()
     for p in passes:
         lm = int(p["local_mask"])
@@ -58,8 +62,11 @@ def execute(psi: np.ndarray, n: int, passes: np.ndarray, xops: np.ndarray) -> np
         lidx = np.arange(1 << t)
         for x in xops[p["op_begin"]:p["op_begin"] + p["nops"]]:
             k, q0, q1, fl = int(x["kind"]), int(x["q0"]), int(x["q1"]), int(x["flags"])
-            if k <= 4 or k in (11, 12, 14, 15):
+            if k <= 4 or k in (11, 12, 14, 15, 16, 17):
                 _pair(tile, q0, _matrix(x))
+            elif k == 18:  # phase table: tile amplitude l times entry l
+                off = int(x["mask"])
+                tile *= tables[off:off + (1 << t)][None, :]
             elif k == 13:  # diag(1, ph) on q0 (tile-uniform when q0 is not local)
                 ph = x["c"][0] + 1j * x["c"][1]
                 if fl & 1:

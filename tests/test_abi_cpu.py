@@ -225,3 +225,57 @@ def test_thirty_qubit_plan_is_compact(built):
     assert all(bin(int(p["local_mask"])).count("1") == 12 for p in passes)
     assert all(int(p["local_mask"]) & 0xF == 0xF for p in passes)
     assert len(passes) < 60
+
+
+def _plan_exec(n, ops, tile, tables):
+    r = llgpu.plan_export(n, ops, tile, zyz=True, tables=tables)
+    return r, execute(oracle.zero_state(n), n, r[0], r[1], r[2] if tables else None)
+
+
+@pytest.mark.parametrize("n,tile", [(6, 5), (9, 6), (10, 7), (11, 5)])
+def test_phase_table_plans_reproduce_the_oracle(built, n, tile):
+    # random circuits over every gate kind (non-unitary 2x2s, MCZ masks, CNOTs with non-local
+    # controls): gathering diagonal factors into phase tables keeps the plan's product
+    rng = np.random.default_rng(300 + n)
+    ops = random_ops(n, 300, rng)
+    (passes, xops, tab), got = _plan_exec(n, ops, tile, True)
+    want = oracle.run_ops(n, ops)
+    assert np.max(np.abs(got - want)) <= 1e-12 * max(1.0, np.max(np.abs(want)))
+    # every table op points at a whole table of 2^t unit-modulus entries
+    for p in passes:
+        for x in xops[p["op_begin"]:p["op_begin"] + p["nops"]]:
+            if int(x["kind"]) == 18:
+                ent = tab[int(x["mask"]):int(x["mask"]) + (1 << int(p["t"]))]
+                assert ent.size == 1 << int(p["t"]) and np.allclose(np.abs(ent), 1.0, atol=1e-14)
+
+
+def test_phase_tables_on_the_layered_circuit(built, golden):
+    g = golden("config2_layered")
+    for n, ops in zip(g["n"], split(g["ops"], g["offsets"])):
+        n = int(n)
+        for tile in (5, 8):
+            (passes, xops, tab), got = _plan_exec(n, ops, tile, True)
+            assert np.max(np.abs(got - oracle.run_ops(n, ops))) < 1e-12
+
+
+def _fp64_mults_per_pair(xops):
+    # FP64 multiply-adds per amplitude pair of each executor kind (phased CNOT: a quarter of the
+    # amplitudes times a complex constant)
+    cost = {0: 16, 1: 8, 2: 8, 3: 8, 5: 8, 11: 16, 12: 12, 13: 4, 14: 8, 15: 8, 16: 4, 17: 4, 18: 8}
+    c = sum(cost.get(int(k), 0) for k in xops["kind"])
+    return c + 2 * int(np.sum((xops["kind"] == 6) & ((xops["flags"] & 8) != 0)))
+
+
+def test_phase_tables_halve_the_rotation_arithmetic(built):
+    # the 30-qubit headline recipe with 12-qubit tiles: rotations lose their complex input-phase
+    # product (8 -> 4 multiply-adds per pair) and phased CNOTs their controlled phase; the tables
+    # that take them over cost less than what they replace
+    n = 30
+    ops = workloads.layered_rotations(n, layers=20)
+    plain = llgpu.plan_export(n, ops, 12, zyz=True)
+    passes, xops, tab = llgpu.plan_export(n, ops, 12, zyz=True, tables=True)
+    assert len(passes) == len(plain[0])
+    kinds = np.bincount(xops["kind"], minlength=19)
+    assert kinds[16] + kinds[17] > 500 and kinds[18] > 0
+    assert _fp64_mults_per_pair(xops) < 0.7 * _fp64_mults_per_pair(plain[1])
+    assert tab.size == kinds[18] << 12

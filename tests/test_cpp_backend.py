@@ -7,10 +7,12 @@ import subprocess
 import numpy as np
 import pytest
 
+import build_oracle
 import llgpu
 from conftest import PKG, REPO
 
-REF_SRC = "/root/reference/src"
+_REF = build_oracle.reference_root()
+REF_SRC = os.path.join(_REF, "src") if _REF else ""
 CPP = os.path.join(REPO, "tests", "cpp")
 BUILD = os.path.join(PKG, "_build", "cpp_tests")
 
@@ -25,7 +27,7 @@ def compile_driver(src: str, out: str, iface: str) -> str:
     return exe
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference tree not present on this machine")
+@pytest.mark.skipif(not REF_SRC, reason="reference tree not present on this machine")
 def test_reference_algorithms_compile_against_gpu_backend(built):
     exe = compile_driver("reference_algorithms_on_gpu.cpp", "ref_alg_gpu", REF_SRC)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
@@ -45,7 +47,7 @@ def test_restated_interface_matches_reference_signatures():
     ours = open(os.path.join(CPP, "iface", "Backend.h")).read()
     sigs = sorted(set(re.findall(r"virtual ([^;{]+?)\s*=\s*0;", ours)))
     assert len(sigs) == 11
-    if os.path.isdir(REF_SRC):
+    if REF_SRC:
         ref = open(os.path.join(REF_SRC, "Backend.h")).read()
         ref_block = ref[ref.index("class Backend {"):ref.index("};", ref.index("class Backend {"))]
         ref_sigs = sorted(set(re.findall(r"virtual ([^;{]+?)\s*=\s*0;", ref_block)))

@@ -23,7 +23,7 @@ def _built(built):
     assert llgpu.device_count() > 0
 
 
-@pytest.mark.parametrize("precision", ["complex128", "fp64"])
+@pytest.mark.parametrize("precision", ["df64", "fp64"])
 def test_hea_gradients_match_reference_parameter_shift(golden, precision):
     g = golden("hea_param_shift")
     n = int(g["n"])

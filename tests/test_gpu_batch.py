@@ -47,7 +47,7 @@ def random_batch(count, lo, hi, depth, seed):
     return np.array(nq), np.concatenate(circuits), offsets, circuits
 
 
-@pytest.mark.parametrize("precision,tol", [("complex128", 1e-12), ("fp64", 1e-12), ("complex64", 5e-5)])
+@pytest.mark.parametrize("precision,tol", [("df64", 1e-12), ("fp64", 1e-12), ("complex64", 5e-5)])
 @pytest.mark.parametrize("tile", [5, 0])
 def test_batch_matches_oracle(precision, tol, tile):
     nq, ops, off, circuits = random_batch(30, 2, 14, 80, seed=31)
@@ -62,7 +62,7 @@ def test_batch_matches_oracle(precision, tol, tile):
 
 def test_fidelity_of_complex64_batch():
     nq, ops, off, _ = random_batch(20, 4, 15, 120, seed=5)
-    b128 = llgpu.Batch(nq, ops, off, "complex128")
+    b128 = llgpu.Batch(nq, ops, off, "df64")
     b64 = llgpu.Batch(nq, ops, off, "complex64")
     b128.run()
     b64.run()
@@ -77,7 +77,7 @@ def test_fidelity_of_complex64_batch():
 def test_bounded_wait_reports_timeout():
     # 2 circuits of 8 qubits with 5-qubit tiles: 8 tiles per pass, several passes
     nq, ops, off, _ = random_batch(2, 8, 8, 60, seed=2)
-    b = llgpu.Batch(nq, ops, off, "complex128", 5)
+    b = llgpu.Batch(nq, ops, off, "df64", 5)
     assert b.info()["total_passes"] > 2
     b.run()
     # work items are ordered by pass round: item 16 is a pass-1 tile of circuit 0
@@ -85,7 +85,7 @@ def test_bounded_wait_reports_timeout():
     with pytest.raises(llgpu.LLGError, match="waited past its limit"):
         b.run(spin_limit=20000)
     b.close()
-    b2 = llgpu.Batch(nq, ops, off, "complex128", 5)  # the context is still usable
+    b2 = llgpu.Batch(nq, ops, off, "df64", 5)  # the context is still usable
     b2.run()
     b2.close()
 
@@ -94,7 +94,7 @@ def test_full_config5_batch():
     """512 circuits, n uniform in 10..22, 200 gates each; complex64 vs complex128 fidelity per
     circuit; circuits up to 16 qubits against the oracle."""
     nq, ops, off = workloads.mixed_batch(512, 10, 22, 200)
-    b128 = llgpu.Batch(nq, ops, off, "complex128")
+    b128 = llgpu.Batch(nq, ops, off, "df64")
     b64 = llgpu.Batch(nq, ops, off, "complex64")
     b128.run()
     b64.run()

@@ -10,7 +10,7 @@ import oracle
 import workloads
 
 pytestmark = pytest.mark.gpu
-TOL = {"complex128": 1e-12, "fp64": 1e-12, "complex64": 5e-5}
+TOL = {"df64": 1e-12, "fp64": 1e-12, "complex64": 5e-5}
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -23,7 +23,7 @@ def rand_unitary(d, rng):
     return q * (np.diag(r) / np.abs(np.diag(r)))
 
 
-@pytest.mark.parametrize("precision", ["complex128", "fp64", "complex64"])
+@pytest.mark.parametrize("precision", ["df64", "fp64", "complex64"])
 @pytest.mark.parametrize("n,k", [(4, 1), (6, 2), (8, 3), (11, 4), (13, 5), (5, 5), (3, 2), (16, 5)])
 def test_block_matches_oracle(precision, n, k):
     ops = workloads.layered_rotations(n, 2, seed=n)

@@ -26,7 +26,7 @@ def random_cptp(m, nk, rng):
     return [q[k * d:(k + 1) * d] for k in range(nk)]
 
 
-@pytest.mark.parametrize("precision,tol", [("complex128", 1e-12), ("fp64", 1e-12), ("complex64", 5e-6)])
+@pytest.mark.parametrize("precision,tol", [("df64", 1e-12), ("fp64", 1e-12), ("complex64", 5e-6)])
 @pytest.mark.parametrize("n", [3, 5, 7])
 def test_rho_matches_oracle(precision, tol, n):
     rng = np.random.default_rng(40 + n)

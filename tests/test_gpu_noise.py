@@ -15,7 +15,7 @@ from llgpu import OP_CNOT, OP_H, OP_RX, OP_RY, OP_RZ, make_ops
 pytestmark = pytest.mark.gpu
 
 TERMS3 = [(0, 1, 1.0), (2, -1, 0.5)]
-TOL = {"complex128": 1e-12, "fp64": 1e-12, "complex64": 2e-5}
+TOL = {"df64": 1e-12, "fp64": 1e-12, "complex64": 2e-5}
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -23,7 +23,7 @@ def _built(built):
     assert llgpu.device_count() > 0
 
 
-@pytest.mark.parametrize("precision", ["complex128", "fp64", "complex64"])
+@pytest.mark.parametrize("precision", ["df64", "fp64", "complex64"])
 @pytest.mark.parametrize("scale", [1, 3])
 def test_pauli_choices_match_the_oracle(golden, precision, scale):
     ops = golden("noisy_zne")["three_ops"]
@@ -35,7 +35,7 @@ def test_pauli_choices_match_the_oracle(golden, precision, scale):
     h.close()
 
 
-@pytest.mark.parametrize("n,precision", [(14, "complex128"), (14, "complex64"), (10, "complex128")])
+@pytest.mark.parametrize("n,precision", [(14, "df64"), (14, "complex64"), (10, "df64")])
 def test_wide_states_with_cross_cta_paulis(n, precision):
     # 14-qubit complex128 states span a 2-CTA cluster: Paulis on the top qubit cross CTAs
     ops = workloads.noisy_layers(n, 2)
@@ -45,7 +45,7 @@ def test_wide_states_with_cross_cta_paulis(n, precision):
     want, wpaulis = oracle.noisy_run(n, ops, 0.02, 3, 7, 0, 64, terms)
     assert np.array_equal(paulis, wpaulis) and paulis.sum() > 50
     assert np.max(np.abs(obs - want)) <= TOL[precision]
-    if n == 14 and precision == "complex128":
+    if n == 14 and precision == "df64":
         assert h.config()["cluster"] == 2
     h.close()
 
@@ -80,7 +80,7 @@ def test_depolarizing_decay_closed_forms():
         h.close()
 
 
-@pytest.mark.parametrize("precision", ["complex128", "complex64"])
+@pytest.mark.parametrize("precision", ["df64", "complex64"])
 def test_zne_matches_the_oracle(golden, precision):
     ops = golden("noisy_zne")["three_ops"]
     r = llgpu.zne(3, ops, 0.03, [1, 3, 5], 2000, 77, TERMS3, precision)

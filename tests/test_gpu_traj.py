@@ -35,7 +35,7 @@ def check_exact(n, ops, gamma, lam, seed, count, precision, begin=0):
     return z, j
 
 
-@pytest.mark.parametrize("precision", ["complex128", "fp64"])
+@pytest.mark.parametrize("precision", ["df64", "fp64"])
 def test_config4_circuit_jumps_bit_exact_14_qubits(precision):
     # 14 qubits of complex128 need a 2-CTA cluster: exercises the cross-CTA paths
     ops = workloads.noisy_layers(14, 8)
@@ -46,7 +46,7 @@ def test_config4_circuit_jumps_bit_exact_14_qubits(precision):
 @pytest.mark.parametrize("n", [3, 7, 10])
 def test_strong_noise_jumps_bit_exact(n):
     ops = workloads.noisy_layers(n, 3, seed=n)
-    check_exact(n, ops, 0.25, 0.15, seed=77, count=256, precision="complex128")
+    check_exact(n, ops, 0.25, 0.15, seed=77, count=256, precision="df64")
 
 
 def test_every_gate_kind_and_cross_cta_sites():
@@ -71,7 +71,7 @@ def test_every_gate_kind_and_cross_cta_sites():
     # make sure the top qubit (the one split across the cluster) is hit as target and control
     recs += [(OP_H, 13), (OP_CNOT, 13, 2), (OP_CNOT, 4, 13), (OP_RZ, 13, 0, 0.3), (OP_CZ, 13, 0)]
     ops = make_ops(recs)
-    check_exact(n, ops, 0.3, 0.2, seed=9, count=32, precision="complex128")
+    check_exact(n, ops, 0.3, 0.2, seed=9, count=32, precision="df64")
 
 
 def test_trajectory_ranges_are_reproducible():
@@ -86,7 +86,7 @@ def test_mean_matches_density_matrix():
     ops = workloads.noisy_layers(n, 3, seed=6)
     gamma, lam = 0.1, 0.05
     exact = oracle.density_z0(n, ops, gamma, lam)
-    for precision in ("complex128", "complex64"):
+    for precision in ("df64", "complex64"):
         z, _, _, _ = llgpu.traj_run(n, ops, gamma, lam, 123, 8192, precision=precision)
         se = z.std(ddof=1) / np.sqrt(z.size)
         assert abs(z.mean() - exact) < 5 * se, (precision, z.mean(), exact, se)

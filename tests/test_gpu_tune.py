@@ -19,7 +19,7 @@ def _built(built):
     assert llgpu.device_count() > 0
 
 
-@pytest.mark.parametrize("precision", ["complex128", "complex64"])
+@pytest.mark.parametrize("precision", ["df64", "complex64"])
 def test_state_autotune_then_parity(precision):
     llgpu.tune_cache_clear()
     n = 16
@@ -35,7 +35,7 @@ def test_state_autotune_then_parity(precision):
     else:
         assert tun["fuse_mode"] == "none"
     st.apply_ops(ops)
-    tol = 1e-12 if precision == "complex128" else 5e-5
+    tol = 1e-12 if precision == "df64" else 5e-5
     assert np.max(np.abs(st.state() - oracle.run_ops(n, ops))) <= tol
     # the same circuit shape again is a cache hit (angles do not matter)
     ops2 = ops.copy()
@@ -51,7 +51,7 @@ def test_state_autotune_then_parity(precision):
 def test_tile_threads_parity(tile, threads):
     n = 14
     ops = workloads.layered_rotations(n, 3)
-    st = llgpu.State(n, "complex128")
+    st = llgpu.State(n, "df64")
     st.set_fusion("tile", tile)
     st.set_tile_threads(threads)
     st.apply_ops(ops)
@@ -63,7 +63,7 @@ def test_tile_threads_parity(tile, threads):
     st.close()
 
 
-@pytest.mark.parametrize("n,precision", [(10, "complex128"), (14, "complex128"), (14, "complex64"), (9, "fp64")])
+@pytest.mark.parametrize("n,precision", [(10, "df64"), (14, "df64"), (14, "complex64"), (9, "fp64")])
 def test_traj_handle_replays_match_one_shot(n, precision):
     ops = workloads.noisy_layers(n, 3)
     seed = 77
@@ -81,7 +81,7 @@ def test_traj_handle_replays_match_one_shot(n, precision):
     h.close()
 
 
-@pytest.mark.parametrize("n,precision", [(14, "complex128"), (14, "complex64"), (11, "complex128")])
+@pytest.mark.parametrize("n,precision", [(14, "df64"), (14, "complex64"), (11, "df64")])
 def test_traj_autotune_keeps_decisions(n, precision):
     llgpu.tune_cache_clear()
     ops = workloads.noisy_layers(n, 3)
@@ -90,7 +90,7 @@ def test_traj_autotune_keeps_decisions(n, precision):
     res = h.autotune()
     cfg = h.config()
     assert res["candidates"] >= 1 and cfg["cluster"] == res["cluster"] and cfg["cta_threads"] == res["cta_threads"]
-    if n == 14 and precision == "complex128":
+    if n == 14 and precision == "df64":
         assert cfg["cluster"] == 2  # 256 KiB of amplitudes never fit one CTA
     z, j, _ = h.launch(5, 400)
     # jump choices are the same; <Z0> differs only by the reduction order of the tuned shape
@@ -112,9 +112,9 @@ def test_batch_autotune_parity():
     llgpu.tune_cache_clear()
     rng = np.random.default_rng(9)
     nq, ops, off = workloads.mixed_batch(24, 8, 14, 60, seed=int(rng.integers(1 << 30)))
-    res = llgpu.batch_autotune(nq, ops, off, "complex128")
+    res = llgpu.batch_autotune(nq, ops, off, "df64")
     assert res["candidates"] >= 2 and 8 <= res["tile_qubits"] <= 13
-    b = llgpu.Batch(nq, ops, off, "complex128", llgpu.TUNE_AUTO)
+    b = llgpu.Batch(nq, ops, off, "df64", llgpu.TUNE_AUTO)
     assert b.info()["tile_qubits"] == res["tile_qubits"]
     for _ in range(2):  # graph replay
         b.run()

@@ -16,7 +16,7 @@ import llgpu
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp64": 1e-12, "complex128": 1e-12, "complex64": 1e-6}
+TOL = {"fp64": 1e-12, "df64": 1e-12, "complex64": 1e-6}
 
 
 def device_layout(psi: np.ndarray, precision: str) -> np.ndarray:
@@ -48,7 +48,7 @@ def test_noalloc_expectation_matches_existing_entry_point(built):
     a, b, c = a + [0, 5], b + [-1, -1], c + [0.5, -0.25]
     rng = np.random.default_rng(2718)
     stream = torch.cuda.current_stream().cuda_stream
-    for precision in ("fp64", "complex128", "complex64"):
+    for precision in ("fp64", "df64", "complex64"):
         for _ in range(2):  # two calls in a row share the scratch array
             psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
             psi /= np.linalg.norm(psi)
