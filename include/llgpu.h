@@ -220,8 +220,17 @@ int llg_compare(llg_state* a, llg_state* b, double* fidelity, double* max_abs_di
 int llg_compare_ex(llg_state* a, llg_state* b, double* fidelity, double* max_abs_diff, double* max_abs_b);
 
 /* sum_k coeff_k <Z_{a_k} Z_{b_k}>; b_k < 0 selects the single-qubit term <Z_{a_k}>.  The
- * diagonal of python/algorithms.py:141-153 (ising_diagonal) evaluated on the fly. */
+ * diagonal of python/algorithms.py:139-152 (ising_diagonal) evaluated on the fly: any number of
+ * terms with any coefficients (up to 64 terms with at most 4 distinct values run a kernel that
+ * counts parities per coefficient class; anything larger, e.g. an SK model's all-to-all
+ * couplings, runs a chunked kernel whose cost per amplitude does not grow with the terms). */
 int llg_expect_zz(llg_state* st, int nterms, const int* a, const int* b, const double* coeff, double* out);
+
+/* sum_i |a_i|^2 diag[i] for a full 2^n diagonal: the reference's energy = probabilities() . diag
+ * (python/algorithms.py:172-181, run_vqe(hamiltonian_diag=...)).  on_device = 0: `diag` is host
+ * memory, copied to a device buffer the state keeps; else it is device memory of the state's
+ * device, read in place. */
+int llg_expect_diagonal(llg_state* st, const double* diag, int on_device, double* out);
 
 /* No counterpart in the reference.  llg_expect_zz for callers that cannot allocate GPU memory:
  * callers whose device memory belongs to another allocator (a framework that reserves most of
@@ -485,6 +494,10 @@ int llg_plan_export(int n, const llg_op* ops, int nops, int tile_qubits, llg_pas
 #define LLG_PLAN_TABLES 2
 int llg_plan_export_ex(int n, const llg_op* ops, int nops, int tile_qubits, int flags, llg_pass_info* passes,
                        int max_passes, int* npasses, llg_exec_op* xops, int max_xops, int* nxops);
+/* The eigenvalue d(i) of the diagonal observable sum_k coeff_k Z_{a_k} Z_{b_k} (b_k < 0: Z_{a_k}) for
+ * every basis index i < 2^n, computed on the host by the same chunked decomposition the GPU
+ * kernel uses (n <= 26).  For tests. */
+int llg_diag_export(int n, int nterms, const int* a, const int* b, const double* coeff, double* out);
 /* The phase tables of the same plan: (re, im) doubles, 2^tile_qubits entries per table; a kind-18
  * op's `mask` is the index of its first entry.  Writes at most max_doubles values and the true
  * count to *ndoubles. */

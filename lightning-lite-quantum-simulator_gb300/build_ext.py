@@ -1,5 +1,5 @@
 """Builds the engine in-tree: libllgpu.so (CUDA kernels + C ABI, sm_103a) and the pybind11 drop-in
-modules quantum_sim_v3 / quantum_sim_v2 that sit on top of it.
+modules quantum_sim_v3 / quantum_sim_v2 / quantum_sim_algorithms that sit on top of it.
 
 Compiles each translation unit in parallel with nvcc (-gencode arch=compute_103a,code=sm_103a) or
 g++, links with nvcc.  pybind11 headers come from the ones PyTorch ships (torch/include), so the
@@ -28,8 +28,8 @@ CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-I" + INCLUDE, "-I" + CSRC]
 
 CU_SOURCES = ["llg_kernels.cu", "llg_engine.cu", "llg_noalloc.cu", "llg_adjoint.cu", "llg_traj.cu", "llg_batch.cu",
               "llg_tune.cu", "llg_block.cu", "llg_block_tc.cu",
-              "llg_tsolver.cu"]
-CXX_SOURCES = ["llg_plan.cpp"]
+              "llg_tsolver.cu", "llg_diag.cu"]
+CXX_SOURCES = ["llg_plan.cpp", "llg_diag_host.cpp"]
 
 LIB = os.path.join(HERE, "libllgpu.so")
 
@@ -100,18 +100,19 @@ def build(force: bool = False, jobs: int = 8) -> str:
     # pybind11 drop-in modules over the C ABI
     ext = sysconfig.get_config_var("EXT_SUFFIX")
     py_inc = sysconfig.get_paths()["include"]
-    pb_src = os.path.join(CSRC, "py_quantum_sim.cpp")
-    if os.path.exists(pb_src):
-        pb_inc = torch_pybind_include()
-        mods = []
-        for mod, define in (("quantum_sim_v3", "LLG_MODULE_V3"), ("quantum_sim_v2", "LLG_MODULE_V2")):
-            out = os.path.join(HERE, mod + ext)
-            if force or _newer(out, [pb_src, LIB] + hdrs):
-                mods.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fvisibility=hidden", "-D" + define,
-                             "-I" + INCLUDE, "-I" + py_inc, "-I" + pb_inc, pb_src, "-o", out, "-L" + HERE, "-lllgpu",
-                             "-Wl,-rpath,$ORIGIN"])
-        with ThreadPoolExecutor(max_workers=2) as ex:
-            list(ex.map(_run, mods))
+    pb_inc = torch_pybind_include()
+    mods = []
+    for mod, src, define in (("quantum_sim_v3", "py_quantum_sim.cpp", "LLG_MODULE_V3"),
+                             ("quantum_sim_v2", "py_quantum_sim.cpp", "LLG_MODULE_V2"),
+                             ("quantum_sim_algorithms", "py_algorithms.cpp", "LLG_MODULE_ALGORITHMS")):
+        pb_src = os.path.join(CSRC, src)
+        out = os.path.join(HERE, mod + ext)
+        if force or _newer(out, [pb_src, LIB] + hdrs):
+            mods.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fvisibility=hidden", "-D" + define,
+                         "-I" + INCLUDE, "-I" + py_inc, "-I" + pb_inc, pb_src, "-o", out, "-L" + HERE, "-lllgpu",
+                         "-Wl,-rpath,$ORIGIN"])
+    with ThreadPoolExecutor(max_workers=3) as ex:
+        list(ex.map(_run, mods))
     return LIB
 
 

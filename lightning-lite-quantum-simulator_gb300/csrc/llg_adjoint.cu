@@ -25,6 +25,7 @@
 #include "../../include/llgpu.h"
 #include "llg_common.cuh"
 #include "llg_internal.h"
+#include "llg_diag_launch.h"
 #include "llg_launch.h"
 #include "llg_tile.cuh"
 
@@ -220,7 +221,7 @@ __global__ void __launch_bounds__(512, 2) k_tile_bwd(typename P::S* __restrict__
     // shuffles and parks it here, so the op ends in one CTA barrier; the sums across warps are
     // finished for up to kGradBuf ops at once, one thread per op (at most 512 threads, 16 warps).
     constexpr int kGradBuf = 32;
-    __shared__ A gred[kGradBuf][16];
+    __shared__ double gred[kGradBuf][16];  // per-warp parts, converted to IEEE double
     __shared__ int gslot[kGradBuf];
     const int t = pd.t, low = pd.low;
     const uint32_t tsize = 1u << t, nhi = 1u << (t - low);
@@ -249,9 +250,9 @@ __global__ void __launch_bounds__(512, 2) k_tile_bwd(typename P::S* __restrict__
     int ng = 0;  // buffered gradients (the same count in every thread)
     auto flush = [&]() {  // after a barrier: the warps' partials of each buffered op, in warp order
         if ((int)threadIdx.x < ng) {
-            A sum = gred[threadIdx.x][0];
-            for (int w = 1; w < (int)(blockDim.x >> 5); ++w) sum = acc_plus(sum, gred[threadIdx.x][w]);
-            gpart[((size_t)b * nocc + gslot[threadIdx.x]) * tiles + blockIdx.x] = acc_value(sum);
+            double sum = gred[threadIdx.x][0];
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w) sum += gred[threadIdx.x][w];
+            gpart[((size_t)b * nocc + gslot[threadIdx.x]) * tiles + blockIdx.x] = sum;
         }
     };
     __shared__ __align__(16) ExecOp sops[kAdjOpChunk];
@@ -264,7 +265,8 @@ __global__ void __launch_bounds__(512, 2) k_tile_bwd(typename P::S* __restrict__
         if (o.flags & OPF_GRAD) {
             // inner product and un-application in one loop.  The slot is read before the barrier:
             // once it is passed, the next chunk may be staged over this op's record.
-            const A v = warp_sum_acc(tile_grad_apply<P>(tp, tl, tsize, base, o, trow));
+            // the warp's sum in the accumulator's format, then IEEE double across warps and tiles
+            const double v = acc_value(warp_sum_acc(tile_grad_apply<P>(tp, tl, tsize, base, o, trow)));
             if ((threadIdx.x & 31) == 0) gred[ng][threadIdx.x >> 5] = v;
             if (threadIdx.x == 0) gslot[ng] = o.q1;
             ++ng;
@@ -286,78 +288,6 @@ __global__ void __launch_bounds__(512, 2) k_tile_bwd(typename P::S* __restrict__
         psi[g] = tp[l];
         lam[g] = tl[l];
     }
-}
-
-// lambda = O psi (if lam != nullptr) and per-block energy partials, grid (kEBlocksPerState, batch)
-template <class P>
-__global__ void __launch_bounds__(kThreads) k_energy_lambda(const typename P::S* __restrict__ psi_all,
-                                                            typename P::S* __restrict__ lam_all, int n, ZTerms z,
-                                                            double* __restrict__ epart) {
-    using K = typename P::K;
-    __shared__ typename P::Acc sh[kThreads / 32];
-    const uint64_t b = blockIdx.y;
-    const uint64_t size = 1ULL << n;
-    const typename P::S* psi = psi_all + b * size;
-    typename P::S* lam = lam_all ? lam_all + b * size : nullptr;
-    int tot[kMaxZClasses] = {0, 0, 0, 0};
-    for (int k = 0; k < z.nterms; ++k) tot[z.cls[k]] += 1;
-    K cf[kMaxZClasses];
-#pragma unroll
-    for (int c = 0; c < kMaxZClasses; ++c) cf[c] = P::k_from_bits(0);
-    for (int c = 0; c < z.nclass; ++c) {
-        const double v = z.coef[c];
-        if (P::kPrecision == 0) cf[c] = P::k_from_bits((uint64_t)__double_as_longlong(v));
-        else if (P::kPrecision == 2) cf[c] = P::k_from_bits((uint64_t)__float_as_uint(__double2float_rn(v)));
-        else {
-            const df d = double_to_df(v);
-            cf[c] = P::k_from_bits((uint64_t)__float_as_uint(d.hi) | ((uint64_t)__float_as_uint(d.lo) << 32));
-        }
-    }
-    typename P::Acc acc[kMaxZClasses];
-#pragma unroll
-    for (int c = 0; c < kMaxZClasses; ++c) acc[c] = P::acc_zero();
-    const uint64_t step = (uint64_t)gridDim.x * kThreads;
-    for (uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x; i < size; i += step) {
-        const auto a = P::load(psi[i]);
-        int odd[kMaxZClasses] = {0, 0, 0, 0};
-        for (int k = 0; k < z.nterms; ++k) {
-            int par = (int)((i >> z.a[k]) & 1);
-            if (z.b[k] >= 0) par ^= (int)((i >> z.b[k]) & 1);
-            odd[z.cls[k]] += par;
-        }
-        typename P::R dre = P::zero(), dim_unused = P::zero();
-        (void)dim_unused;
-#pragma unroll
-        for (int c = 0; c < kMaxZClasses; ++c) {
-            if (c >= z.nclass) break;
-            const float m = (float)(tot[c] - 2 * odd[c]);  // sum over the class of the +-1 eigenvalues
-            acc[c] = P::acc_norm_w(acc[c], a, m);
-            if (lam) dre = P::add(dre, P::mulk(cf[c], P::r_from_float(m)));
-        }
-        if (lam) {
-            typename P::C out;
-            out.re = P::mulk(dre, a.re);
-            out.im = P::mulk(dre, a.im);
-            lam[i] = P::store(out);
-        }
-    }
-#pragma unroll
-    for (int c = 0; c < kMaxZClasses; ++c) {
-        const auto v = block_sum_acc(acc[c], sh);
-        if (threadIdx.x == 0) epart[((size_t)b * gridDim.x + blockIdx.x) * kMaxZClasses + c] = acc_value(v);
-    }
-}
-
-__global__ void k_energy_finish(const double* __restrict__ epart, int blocks, int batch, ZTerms z, double* __restrict__ energies) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= batch) return;
-    double e = 0.0;
-    for (int c = 0; c < z.nclass; ++c) {
-        double w = 0.0;
-        for (int k = 0; k < blocks; ++k) w += epart[((size_t)b * blocks + k) * kMaxZClasses + c];
-        e += z.coef[c] * w;
-    }
-    energies[b] = e;
 }
 
 // grads[b][k] = sum over the occurrences of parameter k (CSR list) and tiles, fixed order
@@ -422,7 +352,8 @@ int threads_for(int t, int fixed) {
 struct llg_adjoint {
     int n = 0, P = LLG_DF64, nparams = 0, max_batch = 0, nocc = 0, tiles = 1;
     int threads = 0;  // CTA threads of the tile passes (0: 256 for tiles of 10+ qubits)
-    ZTerms z;
+    DiagObsHost obs;   // the observable: any number of Z / ZZ terms with any coefficients
+    void* d_obs = nullptr;
     Plan fwd;
     std::vector<PassDesc> bwd_passes;
     std::vector<ExecOp> bwd_ops;
@@ -525,14 +456,13 @@ int run_forward(llg_adjoint* h, int batch, bool make_lambda, const int* ckpt_eve
                      "checkpoint");
         }
     }
-    const dim3 eg(kEBlocksPerState, (unsigned)batch);
-    k_energy_lambda<P><<<eg, kThreads, 0, s>>>(static_cast<const typename P::S*>(h->d_psi),
-                                               make_lambda ? static_cast<typename P::S*>(h->d_lam) : nullptr, h->n, h->z,
-                                               h->d_epart);
-    ADJ_CUDA(cudaGetLastError(), "energy");
-    k_energy_finish<<<(batch + 127) / 128, 128, 0, s>>>(h->d_epart, kEBlocksPerState, batch, h->z, h->d_energy);
-    ADJ_CUDA(cudaGetLastError(), "energy finish");
-    (void)size;
+    // lambda = O psi and the energies: the observable's chunked kernel, one chunk of up to 2^12
+    // amplitudes per block at a time
+    const uint64_t chunks = size >> h->obs.L;
+    const int eblocks = (int)std::min<uint64_t>(kEBlocksPerState, chunks);
+    ADJ_CUDA(launch_lambda_diag(h->P, h->d_psi, make_lambda ? h->d_lam : nullptr, diag_obs_view(h->obs, h->d_obs), batch,
+                                eblocks, h->d_epart, h->d_energy, s),
+             "energy");
     return LLG_OK;
 }
 
@@ -648,35 +578,19 @@ int llg_adjoint_create(int n, const llg_op* ops, int nops, int nparams, int max_
         return set_error(LLG_EINVAL, "adjoint_create: bad sizes");
     if (precision != LLG_F64 && precision != LLG_DF64 && precision != LLG_F32)
         return set_error(LLG_EINVAL, "adjoint_create: unknown precision");
-    if (nterms < 1 || nterms > kMaxZTerms || !za || !zb || !zcoeff)
-        return set_error(LLG_EINVAL, "adjoint_create: observable needs 1.." + std::to_string(kMaxZTerms) + " terms");
+    if (nterms < 1 || !za || !zb || !zcoeff) return set_error(LLG_EINVAL, "adjoint_create: observable needs 1 or more terms");
     llg_adjoint* h = new llg_adjoint();
     h->n = n;
     h->P = precision;
     h->nparams = nparams;
     h->max_batch = max_batch;
     // observable
-    std::memset(&h->z, 0, sizeof(h->z));
-    h->z.nterms = nterms;
-    for (int k = 0; k < nterms; ++k) {
-        if (za[k] < 0 || za[k] >= n || zb[k] >= n || zb[k] == za[k] || !std::isfinite(zcoeff[k])) {
+    {
+        std::string oerr;
+        if (!build_diag_obs(n, nterms, za, zb, zcoeff, h->obs, oerr)) {
             delete h;
-            return set_error(LLG_EINVAL, "adjoint_create: bad observable term " + std::to_string(k));
+            return set_error(LLG_EINVAL, "adjoint_create: " + oerr);
         }
-        int c = -1;
-        for (int j = 0; j < h->z.nclass; ++j)
-            if (h->z.coef[j] == zcoeff[k]) c = j;
-        if (c < 0) {
-            if (h->z.nclass == kMaxZClasses) {
-                delete h;
-                return set_error(LLG_EINVAL, "adjoint_create: at most 4 distinct observable coefficients");
-            }
-            c = h->z.nclass++;
-            h->z.coef[c] = zcoeff[k];
-        }
-        h->z.a[k] = za[k];
-        h->z.b[k] = zb[k] < 0 ? -1 : zb[k];
-        h->z.cls[k] = c;
     }
     // validate ops (bad qubits, angles; parameter indices)
     for (int i = 0; i < nops; ++i) {
@@ -735,7 +649,11 @@ int llg_adjoint_create(int n, const llg_op* ops, int nops, int nparams, int max_
     if (!rc) rc = dmalloc(&h->d_csr_occ, h->nocc, "csr");
     if (!rc) rc = dmalloc(&h->d_params, (size_t)max_batch * std::max(nparams, 1), "params");
     if (!rc) rc = dmalloc(&h->d_gpart, (size_t)max_batch * h->nocc * h->tiles, "gradient partials");
-    if (!rc) rc = dmalloc(&h->d_epart, (size_t)max_batch * kEBlocksPerState * kMaxZClasses, "energy partials");
+    if (!rc) rc = dmalloc(&h->d_epart, (size_t)max_batch * kEBlocksPerState, "energy partials");
+    if (!rc) rc = dmalloc((char**)&h->d_obs, h->obs.bytes.size(), "observable");
+    if (!rc)
+        rc = cudaMemcpy(h->d_obs, h->obs.bytes.data(), h->obs.bytes.size(), cudaMemcpyHostToDevice)
+                 ? set_error(LLG_ECUDA, "adjoint_create: observable upload") : LLG_OK;
     if (!rc) rc = dmalloc(&h->d_energy, max_batch, "energies");
     if (!rc) rc = dmalloc(&h->d_grad, (size_t)max_batch * std::max(nparams, 1), "gradients");
     if (!rc) rc = dmalloc(&h->d_row_set, max_batch, "rows");
@@ -767,7 +685,7 @@ int llg_adjoint_destroy(llg_adjoint* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     void* ptrs[] = {h->d_psi, h->d_lam, h->d_fwd_ops, h->d_bwd_ops, h->d_table, h->d_occ_param, h->d_csr_ptr,
                     h->d_csr_occ, h->d_params, h->d_gpart, h->d_epart, h->d_energy, h->d_grad, h->d_row_set,
-                    h->d_shift_occ, h->d_shift_val};
+                    h->d_shift_occ, h->d_shift_val, h->d_obs};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (void* p : h->ckpt) cudaFree(p);

@@ -198,11 +198,14 @@ struct PolF64 {
     // acc + re(conj(x) * y) and acc + im(conj(x) * y)
     __device__ static Acc acc_dot_re(Acc a, const C& x, const C& y) { return fma(x.re, y.re, fma(x.im, y.im, a)); }
     __device__ static Acc acc_dot_im(Acc a, const C& x, const C& y) { return fma(x.re, y.im, fma(-x.im, y.re, a)); }
+    // acc + d * |c|^2 for a real weight d given in double (a diagonal observable's eigenvalue)
+    __device__ static Acc acc_norm_d(Acc a, const C& c, double d) { return fma(d, fma(c.re, c.re, c.im * c.im), a); }
     __device__ static double acc_to_double(Acc a) { return a; }
     __device__ static Acc acc_from_double(double a) { return a; }
     __device__ static C from_f64(double2 v) { return {v.x, v.y}; }
     __device__ static double2 to_f64(const C& c) { return make_double2(c.re, c.im); }
     __device__ static K k_from_bits(uint64_t b) { return __longlong_as_double((long long)b); }
+    __device__ static K k_from_double(double d) { return d; }
     __device__ static R r_from_float(float f) { return (double)f; }
 };
 
@@ -255,11 +258,19 @@ struct PolF32 {
     __device__ static Acc acc_dot_im(Acc a, const C& x, const C& y) {
         return df_add(a, df_lin2(df{x.re, 0.f}, df{y.im, 0.f}, df{-x.im, 0.f}, df{y.re, 0.f}));
     }
+    __device__ static Acc acc_norm_d(Acc a, const C& c, double d) {
+        const float p = __fmul_rn(c.re, c.re), q = __fmul_rn(c.im, c.im);
+        const float ep = fmaf(c.re, c.re, -p), eq = fmaf(c.im, c.im, -q);
+        const df s = two_sum(p, q);
+        const df v = fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(ep, eq)));
+        return df_add(a, df_mul(v, double_to_df(d)));
+    }
     __device__ static double acc_to_double(Acc a) { return df_to_double(a); }
     __device__ static Acc acc_from_double(double a) { return double_to_df(a); }
     __device__ static C from_f64(double2 v) { return {__double2float_rn(v.x), __double2float_rn(v.y)}; }
     __device__ static double2 to_f64(const C& c) { return make_double2((double)c.re, (double)c.im); }
     __device__ static K k_from_bits(uint64_t b) { return __uint_as_float((uint32_t)b); }
+    __device__ static K k_from_double(double d) { return __double2float_rn(d); }
     __device__ static R r_from_float(float f) { return f; }
 };
 
@@ -295,6 +306,9 @@ struct PolDF64 {
     __device__ static Acc acc_dot_im(Acc a, const C& x, const C& y) {
         return df_add(a, df_lin2(x.re, y.im, df_neg(x.im), y.re));
     }
+    __device__ static Acc acc_norm_d(Acc a, const C& c, double d) {
+        return df_add(a, df_mul(df_sqsum(c.re, c.im), double_to_df(d)));
+    }
     __device__ static double acc_to_double(Acc a) { return df_to_double(a); }
     __device__ static Acc acc_from_double(double a) { return double_to_df(a); }
     __device__ static C from_f64(double2 v) { return {double_to_df(v.x), double_to_df(v.y)}; }
@@ -302,6 +316,7 @@ struct PolDF64 {
     __device__ static K k_from_bits(uint64_t b) {
         return df{__uint_as_float((uint32_t)b), __uint_as_float((uint32_t)(b >> 32))};
     }
+    __device__ static K k_from_double(double d) { return double_to_df(d); }
     __device__ static R r_from_float(float f) { return df{f, 0.0f}; }
 };
 

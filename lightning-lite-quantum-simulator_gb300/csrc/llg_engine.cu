@@ -14,6 +14,8 @@
 
 #include "../../include/llgpu.h"
 #include "llg_common_host.h"
+#include "llg_diag.h"
+#include "llg_diag_launch.h"
 #include "llg_internal.h"
 #include "llg_launch.h"
 
@@ -78,6 +80,12 @@ struct llg_state {
     // reductions
     double* d_partials = nullptr;
     double* d_red = nullptr;
+    // the last general diagonal observable (llg_diag.h), its device copy, and a full diagonal
+    DiagObsHost obs;
+    void* d_obs = nullptr;
+    size_t d_obs_cap = 0;
+    double* d_diag = nullptr;
+    uint64_t d_diag_size = 0;
     // transfer staging (two chunks of complex128 = double2)
     double* d_stage[2] = {nullptr, nullptr};
     cudaEvent_t stage_ev[2] = {nullptr, nullptr};
@@ -417,6 +425,8 @@ int llg_destroy(llg_state* st) {
     if (st->h_tables) cudaFreeHost(st->h_tables);
     if (st->d_partials) cudaFree(st->d_partials);
     if (st->d_red) cudaFree(st->d_red);
+    if (st->d_obs) cudaFree(st->d_obs);
+    if (st->d_diag) cudaFree(st->d_diag);
     for (int i = 0; i < 2; ++i) {
         if (st->d_stage[i]) cudaFree(st->d_stage[i]);
         if (st->stage_ev[i]) cudaEventDestroy(st->stage_ev[i]);
@@ -843,6 +853,23 @@ int llg_probabilities(llg_state* st, double* out) {
     return device_checks(st);
 }
 
+// The class-counting kernel takes up to kMaxZTerms terms with up to kMaxZClasses distinct
+// coefficient values; it counts parities per class in integers.
+static bool fits_class_kernel(int nterms, const double* coeff) {
+    if (nterms < 0 || nterms > kMaxZTerms) return false;
+    double seen[kMaxZClasses];
+    int ns = 0;
+    for (int k = 0; k < nterms; ++k) {
+        bool found = false;
+        for (int j = 0; j < ns; ++j) found |= seen[j] == coeff[k];
+        if (!found) {
+            if (ns == kMaxZClasses) return false;
+            seen[ns++] = coeff[k];
+        }
+    }
+    return true;
+}
+
 static int build_zterms(int nterms, const int* a, const int* b, const double* coeff, int n, ZTerms& z) {
     if (nterms < 0 || nterms > kMaxZTerms)
         return set_error(LLG_EINVAL, "expect_zz: at most " + std::to_string(kMaxZTerms) + " terms");
@@ -925,11 +952,61 @@ int llg_norm2(llg_state* st, double* out) {
     return LLG_OK;
 }
 
+// sum_i |a_i|^2 d(i) for a general diagonal observable: out[0] the energy, out[1] the norm^2
+static int reduce_diag(llg_state* st, const DiagObs& o, double* out2) {
+    int rc = llg_flush(st);
+    if (rc) return rc;
+    if ((rc = ensure_device_buffers(st))) return rc;
+    rc = traced(st, LLG_PROF_READOUT, 2, "diagonal observable",
+                [&] { return launch_expect_diag(st->P, st->d_psi, o, st->d_partials, st->d_red, st->stream); });
+    if (rc) return rc;
+    LLG_CUDA(cudaMemcpyAsync(out2, st->d_red, 2 * sizeof(double), cudaMemcpyDeviceToHost, st->stream),
+             "cudaMemcpyAsync(D2H)");
+    LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+    return device_checks(st);
+}
+
+// The observable's layout on the device (rebuilt and uploaded only when the terms change).
+static int upload_obs(llg_state* st, int nterms, const int* a, const int* b, const double* coeff, DiagObs* view) {
+    if (!diag_obs_same(st->obs, st->n, nterms, a, b, coeff)) {
+        std::string err;
+        DiagObsHost h;
+        if (!build_diag_obs(st->n, nterms, a, b, coeff, h, err)) return set_error(LLG_EINVAL, "expect_zz: " + err);
+        int rc = ensure_device_buffers(st);
+        if (rc) return rc;
+        if (h.bytes.size() > st->d_obs_cap) {
+            LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+            if (st->d_obs) cudaFree(st->d_obs);
+            st->d_obs = nullptr;
+            st->d_obs_cap = 0;
+            LLG_CUDA(cudaMalloc(&st->d_obs, h.bytes.size()), "cudaMalloc(observable)");
+            st->d_obs_cap = h.bytes.size();
+        }
+        // ordered on the stream after any kernel still reading the previous observable
+        LLG_CUDA(cudaMemcpyAsync(st->d_obs, h.bytes.data(), h.bytes.size(), cudaMemcpyHostToDevice, st->stream),
+                 "cudaMemcpyAsync(observable)");
+        LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");  // h's bytes are freed below
+        st->obs = std::move(h);
+    }
+    *view = diag_obs_view(st->obs, st->d_obs);
+    return LLG_OK;
+}
+
 int llg_expect_zz(llg_state* st, int nterms, const int* a, const int* b, const double* coeff, double* out) {
     if (!st || !out || (nterms > 0 && (!a || !b || !coeff))) return set_error(LLG_EINVAL, "expect_zz: NULL argument");
+    int rc;
+    if (!fits_class_kernel(nterms, coeff)) {
+        // more terms or coefficient values than the class-counting kernel takes: the general
+        // chunked kernel (any number of terms, any coefficients)
+        DiagObs o;
+        if ((rc = upload_obs(st, nterms, a, b, coeff, &o))) return rc;
+        double r[2];
+        if ((rc = reduce_diag(st, o, r))) return rc;
+        *out = r[0];
+        return LLG_OK;
+    }
     ZTerms z;
-    int rc = build_zterms(nterms, a, b, coeff, st->n, z);
-    if (rc) return rc;
+    if ((rc = build_zterms(nterms, a, b, coeff, st->n, z))) return rc;
     double slots[kRedSlots];
     if ((rc = reduce(st, z, slots))) return rc;
     // sum_k c_k <Z..> = sum_c c_c * (count_c * N - 2 W_c)
@@ -940,6 +1017,44 @@ int llg_expect_zz(llg_state* st, int nterms, const int* a, const int* b, const d
         e += z.coef[c] * (cnt * slots[0] - 2.0 * slots[1 + c]);
     }
     *out = e;
+    return LLG_OK;
+}
+
+int llg_expect_diagonal(llg_state* st, const double* diag, int on_device, double* out) {
+    if (!st || !diag || !out) return set_error(LLG_EINVAL, "expect_diagonal: NULL argument");
+    int rc = ensure_device_buffers(st);
+    if (rc) return rc;
+    const double* d = diag;
+    if (!on_device) {
+        if (st->d_diag_size != st->size) {
+            LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+            if (st->d_diag) cudaFree(st->d_diag);
+            st->d_diag = nullptr;
+            st->d_diag_size = 0;
+            cudaError_t e = cudaMalloc(&st->d_diag, st->size * sizeof(double));
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                return set_error(LLG_ENOMEM, std::string("expect_diagonal: cannot allocate the diagonal: ") +
+                                                 cudaGetErrorString(e));
+            }
+            st->d_diag_size = st->size;
+        }
+        LLG_CUDA(cudaMemcpyAsync(st->d_diag, diag, st->size * sizeof(double), cudaMemcpyHostToDevice, st->stream),
+                 "cudaMemcpyAsync(diagonal)");
+        d = st->d_diag;
+    } else {
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, diag) != cudaSuccess) cudaGetLastError();
+        else if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
+            return set_error(LLG_EINVAL, "expect_diagonal: on_device set but diag is not device memory");
+    }
+    DiagObs o;
+    std::memset(&o, 0, sizeof(o));
+    o.n = st->n;
+    o.diag = d;
+    double r[2];
+    if ((rc = reduce_diag(st, o, r))) return rc;
+    *out = r[0];
     return LLG_OK;
 }
 
@@ -1035,6 +1150,15 @@ int export_plan(int n, const llg_op* ops, int nops, int tile_qubits, int flags, 
 }  // namespace
 
 extern "C" {
+
+int llg_diag_export(int n, int nterms, const int* a, const int* b, const double* coeff, double* out) {
+    if (n < 1 || n > 26 || !out) return set_error(LLG_EINVAL, "diag_export: bad argument");
+    DiagObsHost h;
+    std::string err;
+    if (!build_diag_obs(n, nterms, a, b, coeff, h, err)) return set_error(LLG_EINVAL, "diag_export: " + err);
+    diag_obs_eval_host(h, out);
+    return LLG_OK;
+}
 
 int llg_plan_export_tables(int n, const llg_op* ops, int nops, int tile_qubits, int flags, double* tables,
                            int64_t max_doubles, int64_t* ndoubles) {

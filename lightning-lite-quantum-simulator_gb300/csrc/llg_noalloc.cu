@@ -15,7 +15,13 @@
 //
 // Contract:
 //  * The first call on a device resolves that device's scratch address (cudaGetSymbolAddress);
-//    make that first call before any stream capture on that device.
+//    make that first call before any stream capture on that device.  The address is cached per
+//    device for the life of the process: it stays valid while the device's primary context lives,
+//    so a caller that resets the device (cudaDeviceReset) must not use this entry point afterwards.
+//  * d_amps and d_out must be memory of the current device (or managed memory); device memory of
+//    another GPU is rejected with LLG_EINVAL.
+//  * The call reports a CUDA error left pending by earlier work (cudaPeekAtLastError) as
+//    LLG_ECUDA before launching anything, and does not clear it.
 //  * Every call shares the one scratch array and it keeps the last call's contents.  Each call
 //    writes every partial row it later reads, so nothing has to start at zero; but calls whose
 //    kernels overlap on the GPU (different streams, or different host threads) race on the array.
@@ -136,13 +142,15 @@ int scratch_address(double** out) {
     return LLG_OK;
 }
 
-bool device_reachable(const void* p) {
+// Device memory of the current device, or managed memory.
+bool device_reachable(const void* p, int dev) {
     cudaPointerAttributes at;
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-        cudaGetLastError();
+        cudaGetLastError();  // the error this query itself raised (an unregistered host pointer)
         return false;
     }
-    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+    if (at.type == cudaMemoryTypeManaged) return true;
+    return at.type == cudaMemoryTypeDevice && at.device == dev;
 }
 
 template <class P>
@@ -198,8 +206,16 @@ extern "C" int llg_expect_zz_noalloc(const void* d_amps, int n_qubits, int preci
         z.b[k] = b[k] < 0 ? -1 : b[k];
         z.cls[k] = c;
     }
-    if (!device_reachable(d_amps) || !device_reachable(d_out))
-        return set_error(LLG_EINVAL, "expect_zz_noalloc: d_amps and d_out must be device (or managed) memory");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_error(LLG_ECUDA, std::string("expect_zz_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
+    e = cudaPeekAtLastError();
+    if (e != cudaSuccess)
+        return set_error(LLG_ECUDA, std::string("expect_zz_noalloc: a CUDA error is pending from earlier work: ") +
+                                        cudaGetErrorString(e));
+    if (!device_reachable(d_amps, dev) || !device_reachable(d_out, dev))
+        return set_error(LLG_EINVAL, "expect_zz_noalloc: d_amps and d_out must be device memory of the current device "
+                                     "(or managed memory)");
     double* scratch = nullptr;
     int rc = scratch_address(&scratch);
     if (rc) return rc;

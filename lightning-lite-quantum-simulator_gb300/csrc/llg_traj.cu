@@ -268,7 +268,7 @@ struct Traj {
 
     // sum over the group of |a|^2 for amplitudes with (global bit q) == 1 (q < 0: all), or of
     // (1 - 2 bit0)|a|^2 when z0 is set; identical in every CTA of the group
-    __device__ double reduce(int q, bool z0, typename P::Acc* part2) {
+    __device__ double reduce(int q, bool z0, double* part2) {
         typename P::Acc pos = P::acc_zero(), neg = P::acc_zero();
         if (z0) {
             for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x) {
@@ -293,29 +293,31 @@ struct Traj {
     // writes set k % 2 at call k only after the group barrier of call k - 1, which the partner's
     // warp 0 reaches after reading call k - 2's words.
     int sbuf = 0;
-    __device__ double group_total(typename P::Acc v, typename P::Acc* part2) {
-        using A = typename P::Acc;
-        v = warp_sum_acc(v);
-        A* part = part2 + kPartWarps * sbuf;
+    // The warp stage runs in the accumulator's format (double-float on the FP32 pipe for
+    // double-float and complex64 states); the warp's sum is then converted once, and the stages
+    // across warps and CTAs add IEEE doubles.
+    __device__ double group_total(typename P::Acc v, double* part2) {
+        const double wsum = acc_value(warp_sum_acc(v));
+        double* part = part2 + kPartWarps * sbuf;
         sbuf ^= 1;
         const int lane = threadIdx.x & 31, nw = (int)(blockDim.x >> 5);
-        if (lane == 0) part[threadIdx.x >> 5] = v;
+        if (lane == 0) part[threadIdx.x >> 5] = wsum;
         group_sync<CL>();
         if (threadIdx.x >= 32) return 0.0;
-        A x = P::acc_zero();
+        double x = 0.0;
         if (lane < nw) {
             if (CL == 1) {
                 x = part[lane];
             } else {
                 cg::cluster_group cl = cg::this_cluster();
-                x = acc_plus(cl.map_shared_rank(part, 0)[lane], cl.map_shared_rank(part, 1)[lane]);
+                x = cl.map_shared_rank(part, 0)[lane] + cl.map_shared_rank(part, 1)[lane];
             }
         }
-        return acc_value(warp_sum_acc(x));
+        return warp_sum_dbl(x);
     }
 
     // the observable sum_c coef_c * sum_i |a_i|^2 (tot_c - 2 odd_c(i)) over the group's state
-    __device__ double observable(const ObsTerms& ob, typename P::Acc* part2) {
+    __device__ double observable(const ObsTerms& ob, double* part2) {
         typename P::Acc acc[kObsClasses];
         int tot[kObsClasses] = {0, 0, 0};
 #pragma unroll
@@ -509,7 +511,7 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
                                  uint8_t* __restrict__ jump_log, int64_t log_stride, double* __restrict__ margin_out) {
     using S = typename P::S;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ typename P::Acc part2[2 * kPartWarps];  // group_total's warp parts, two sets used in turn
+    __shared__ double part2[2 * kPartWarps];  // group_total's warp parts (double), two sets used in turn
     __shared__ Decision dec;
     __shared__ ObsTerms ob;  // the observable, copied once from global memory
     // uniforms of sites [u_begin, u_end): Kraus mode uni[site - u_begin] = philox_u1(site); depolarizing

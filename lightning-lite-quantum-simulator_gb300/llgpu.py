@@ -107,6 +107,8 @@ def lib() -> ctypes.CDLL:
             "llg_probabilities": (i, [vp, vp]),
             "llg_norm2": (i, [vp, P(d)]),
             "llg_expect_zz": (i, [vp, i, vp, vp, vp, P(d)]),
+            "llg_expect_diagonal": (i, [vp, vp, i, P(d)]),
+            "llg_diag_export": (i, [i, i, vp, vp, vp, vp]),
             "llg_renormalize": (i, [vp]),
             "llg_host_alloc": (vp, [sz]),
             "llg_host_free": (None, [vp]),
@@ -357,6 +359,22 @@ class State:
         check(lib().llg_compare_ex(self._h, other._h, ctypes.byref(f), ctypes.byref(d), ctypes.byref(m)))
         return f.value, d.value, m.value
 
+    def expect_diagonal(self, diag) -> float:
+        """sum_i |a_i|^2 diag[i] for a full diagonal: a numpy array of 2^n doubles (copied to the
+        device) or a CUDA array with __cuda_array_interface__ (a torch tensor, read in place)."""
+        cai = getattr(diag, "__cuda_array_interface__", None)
+        v = ctypes.c_double()
+        if cai is not None:
+            if tuple(cai["shape"]) != (self.size,) or cai["typestr"] != "<f8" or cai.get("strides") not in (None, (8,)):
+                raise ValueError("the diagonal must be a contiguous float64 vector of 2^n entries")
+            check(lib().llg_expect_diagonal(self._h, ctypes.c_void_p(cai["data"][0]), 1, ctypes.byref(v)))
+        else:
+            d = np.ascontiguousarray(diag, dtype=np.float64)
+            if d.shape != (self.size,):
+                raise ValueError("the diagonal must have 2^n entries")
+            check(lib().llg_expect_diagonal(self._h, _ptr(d), 0, ctypes.byref(v)))
+        return v.value
+
     def expect_zz(self, a: Sequence[int], b: Sequence[int], coeff: Sequence[float]) -> float:
         aa = np.ascontiguousarray(a, dtype=np.int32)
         bb = np.ascontiguousarray(b, dtype=np.int32)
@@ -425,6 +443,36 @@ def fp64_fma_rate(iters: int = 1 << 16) -> float:
     v = ctypes.c_double()
     check(lib().llg_fp64_fma_rate(iters, ctypes.byref(v)))
     return v.value
+
+
+def diag_export(n: int, a, b, coeff) -> np.ndarray:
+    """The observable's eigenvalue per basis index by the GPU kernel's chunked decomposition,
+    computed on the host (tests)."""
+    aa = np.ascontiguousarray(a, dtype=np.int32)
+    bb = np.ascontiguousarray(b, dtype=np.int32)
+    cc = np.ascontiguousarray(coeff, dtype=np.float64)
+    out = np.empty(1 << n, dtype=np.float64)
+    check(lib().llg_diag_export(n, aa.size, _ptr(aa), _ptr(bb), _ptr(cc), _ptr(out)))
+    return out
+
+
+def ising_terms(n: int, zz=(), z=()):
+    """(a, b, coeff) lists of H = sum J_ij Z_i Z_j + sum h_i Z_i with the arguments of the
+    reference's ising_diagonal (python/algorithms.py:139-152): zz a list of (i, j, J), z a list of
+    (i, h).  llg_expect_zz evaluates them without the 2^n diagonal."""
+    a, b, c = [], [], []
+    for i, j, v in zz:
+        a.append(int(i))
+        b.append(int(j))
+        c.append(float(v))
+    for i, v in z:
+        a.append(int(i))
+        b.append(-1)
+        c.append(float(v))
+    for q in a + [x for x in b if x >= 0]:
+        if not 0 <= q < n:
+            raise ValueError(f"qubit {q} outside [0, {n})")
+    return a, b, c
 
 
 def ring_zz_terms(n: int):

@@ -3,7 +3,7 @@
 //
 // Built by oracle/build_oracle.py with -I<reference>/src into oracle/_ref/libref.so, directly
 // from the reference's headers where they lie: src/Backend.h (ReferenceBackend),
-// src/StateVectorBackend.h (StateVectorBackend), src/Algorithms.h (Grover, VQE::prepare) and
+// src/StateVectorBackend.h (StateVectorBackend), src/Algorithms.h (Grover, QAOA, VQE) and
 // src/Mitigation.h (NoisyBackend, ZNE).
 // Nothing from the reference is copied here; this file only drives its classes.
 
@@ -231,6 +231,54 @@ int ref_zne(int n, const orc_op* ops, int nops, double p, uint64_t seed, const d
         return 1;
     } catch (const std::runtime_error&) {
         return 3;
+    } catch (...) {
+        return 2;
+    }
+}
+
+// ll::QAOA::run on StateVectorBackend (Algorithms.h:156-191): edges (ei[k], ej[k], w[k]), p layers.
+// probs: 2^n_nodes doubles.
+int ref_qaoa(int n_nodes, int nedges, const int* ei, const int* ej, const double* w, int p, const double* gammas,
+             const double* betas, double* probs, double* best_cut) {
+    try {
+        ll::Graph g;
+        g.n_nodes = n_nodes;
+        for (int k = 0; k < nedges; ++k) g.edges.emplace_back(ei[k], ej[k], w[k]);
+        ll::StateVectorBackend be(1);
+        const ll::QAOAResult r = ll::QAOA::run(be, g, std::vector<double>(gammas, gammas + p),
+                                               std::vector<double>(betas, betas + p));
+        std::memcpy(probs, r.probabilities.data(), r.probabilities.size() * sizeof(double));
+        *best_cut = r.best_cut;
+        return 0;
+    } catch (const std::invalid_argument&) {
+        return 1;
+    } catch (...) {
+        return 2;
+    }
+}
+
+// ll::VQE::optimize on StateVectorBackend (Algorithms.h:255-307) with the energy function the
+// reference's run_vqe builds from a diagonal (python/algorithms.py:172-181): prepare, then
+// probabilities() . diag, here with diag = sum_k c_k Z_a Z_b.  params: n * layers doubles out;
+// probs: the best state's probabilities (2^n doubles).
+int ref_vqe_optimize(int n, int layers, uint64_t seed, int max_iter, double lr, int nterms, const int* za, const int* zb,
+                     const double* zc, double* energy, double* params, int* iterations, double* probs) {
+    try {
+        ll::VQE vqe(n, layers, seed);
+        ll::StateVectorBackend be(1);
+        auto fn = [&](const std::vector<double>& th) {
+            vqe.prepare(be, th);
+            return zz_observable(be, nterms, za, zb, zc);
+        };
+        const ll::VQEResult r = vqe.optimize(be, fn, max_iter, lr);
+        *energy = r.energy;
+        std::memcpy(params, r.params.data(), r.params.size() * sizeof(double));
+        *iterations = r.iterations;
+        const auto p = be.probabilities();
+        std::memcpy(probs, p.data(), p.size() * sizeof(double));
+        return 0;
+    } catch (const std::invalid_argument&) {
+        return 1;
     } catch (...) {
         return 2;
     }

@@ -49,6 +49,8 @@ def load_ref():
     L.ref_vqe_prepare.argtypes = [i, i, vp, vp]
     L.ref_noisy_obs.argtypes = [i, vp, i, d, i, u64, i, i, vp, vp, vp, vp]
     L.ref_zne.argtypes = [i, vp, i, d, u64, vp, i, i, i, vp, vp, vp, vp]
+    L.ref_qaoa.argtypes = [i, i, vp, vp, vp, i, vp, vp, vp, ctypes.POINTER(d)]
+    L.ref_vqe_optimize.argtypes = [i, i, u64, i, d, i, vp, vp, vp, ctypes.POINTER(d), vp, ctypes.POINTER(i), vp]
     mods = {}
     for name in ("quantum_sim_v3", "quantum_sim_v2"):
         path = [p for k, p in paths.items() if k.startswith(name)][0]
@@ -328,6 +330,56 @@ def gen_noise(L):
     np.savez_compressed(os.path.join(HERE, "noisy_zne.npz"), **out)
 
 
+def algorithm_cases():
+    """QAOA graphs and VQE problems for the algorithm fixtures (shared with the tests)."""
+    rng = np.random.default_rng(77)
+    ring4 = (4, [(0, 1, 1.0), (1, 2, 1.0), (2, 3, 1.0), (3, 0, 1.0)])
+    w6 = (6, [(i, j, float(np.round(rng.uniform(0.2, 2.0), 3))) for i in range(6) for j in range(i + 1, 6)
+              if rng.uniform() < 0.6])
+    w10 = (10, [(i, (i + 1) % 10, 1.0) for i in range(10)] + [(i, (i + 3) % 10, 0.5) for i in range(0, 10, 2)])
+    qaoa = [("ring4_p1", ring4, [0.4], [0.3]), ("w6_p2", w6, [0.3, 0.7], [0.5, 0.2]),
+            ("w10_p3", w10, [0.2, 0.5, 0.8], [0.6, 0.4, 0.1])]
+    sk5 = [(i, j, float(np.round(rng.normal() / np.sqrt(5), 4))) for i in range(5) for j in range(i + 1, 5)]
+    vqe = [("ring4_l2", 4, 2, 1, 12, 0.1, [(i, (i + 1) % 4, 1.0) for i in range(4)], []),
+           ("sk5_l2", 5, 2, 7, 10, 0.05, sk5, [(i, 0.3 * (i - 2)) for i in range(5)])]
+    return qaoa, vqe
+
+
+def gen_algorithms(L):
+    # Algorithms.h's QAOA::run (src/Algorithms.h:156-191) and VQE::optimize (:255-307) on
+    # ll::StateVectorBackend, for the drop-in algorithms module on the GPU backend
+    out = {}
+    qaoa, vqe = algorithm_cases()
+    for label, (n, edges), gammas, betas in qaoa:
+        ei = np.array([e[0] for e in edges], dtype=np.int32)
+        ej = np.array([e[1] for e in edges], dtype=np.int32)
+        w = np.array([e[2] for e in edges], dtype=np.float64)
+        g = np.array(gammas, dtype=np.float64)
+        b = np.array(betas, dtype=np.float64)
+        probs = np.zeros(1 << n)
+        cut = ctypes.c_double()
+        rc = L.ref_qaoa(n, ei.size, ei.ctypes.data, ej.ctypes.data, w.ctypes.data, g.size, g.ctypes.data,
+                        b.ctypes.data, probs.ctypes.data, ctypes.byref(cut))
+        assert rc == 0
+        out[f"qaoa_{label}_probs"] = probs
+        out[f"qaoa_{label}_best_cut"] = cut.value
+    for label, n, layers, seed, iters, lr, zz, z in vqe:
+        a = np.array([t[0] for t in zz] + [t[0] for t in z], dtype=np.int32)
+        bb = np.array([t[1] for t in zz] + [-1] * len(z), dtype=np.int32)
+        c = np.array([t[2] for t in zz] + [t[1] for t in z], dtype=np.float64)
+        params = np.zeros(n * layers)
+        probs = np.zeros(1 << n)
+        e, it = ctypes.c_double(), ctypes.c_int()
+        rc = L.ref_vqe_optimize(n, layers, seed, iters, lr, a.size, a.ctypes.data, bb.ctypes.data, c.ctypes.data,
+                                ctypes.byref(e), params.ctypes.data, ctypes.byref(it), probs.ctypes.data)
+        assert rc == 0
+        out[f"vqe_{label}_energy"] = e.value
+        out[f"vqe_{label}_params"] = params
+        out[f"vqe_{label}_iterations"] = it.value
+        out[f"vqe_{label}_probs"] = probs
+    np.savez_compressed(os.path.join(HERE, "algorithms.npz"), **out)
+
+
 def main():
     L, mods = load_ref()
     gen_random_2024(L)
@@ -339,6 +391,7 @@ def main():
     gen_vqe(L)
     gen_hea(L)
     gen_noise(L)
+    gen_algorithms(L)
     print("fixtures written to", HERE)
 
 

@@ -279,3 +279,46 @@ def test_phase_tables_halve_the_rotation_arithmetic(built):
     assert kinds[16] + kinds[17] > 500 and kinds[18] > 0
     assert _fp64_mults_per_pair(xops) < 0.7 * _fp64_mults_per_pair(plain[1])
     assert tab.size == kinds[18] << 12
+
+
+def _ising_diagonal(n, zz, z):
+    # the reference's ising_diagonal (python/algorithms.py:139-152), restated in numpy
+    idx = np.arange(1 << n, dtype=np.int64)
+    s = [1.0 - 2.0 * ((idx >> q) & 1) for q in range(n)]
+    d = np.zeros(idx.size)
+    for i, j, c in zz:
+        d += c * s[i] * s[j]
+    for i, h in z:
+        d += h * s[i]
+    return d
+
+
+@pytest.mark.parametrize("n", [1, 5, 12, 13, 17])
+def test_general_observable_decomposition(built, n):
+    # any number of Z / ZZ terms with any coefficients (all-to-all couplings, fields, repeated
+    # pairs): the chunked decomposition the GPU kernel uses gives ising_diagonal's values
+    rng = np.random.default_rng(40 + n)
+    zz = [(i, j, float(rng.normal())) for i in range(n) for j in range(i + 1, n)]
+    zz += [(j, i, 0.5) for i, j, _ in zz[:3]]  # the same pair twice, in either order
+    z = [(i, float(rng.normal())) for i in range(n)]
+    a, b, c = llgpu.ising_terms(n, zz, z)
+    got = llgpu.diag_export(n, a, b, c)
+    want = _ising_diagonal(n, zz, z)
+    assert np.max(np.abs(got - want)) <= 1e-12 * max(1.0, np.max(np.abs(want)))
+
+
+def test_general_observable_rejects_bad_terms(built):
+    for a, b, c in (([0], [0], [1.0]), ([3], [-1], [1.0]), ([0], [1], [float("nan")]), ([-1], [0], [1.0])):
+        with pytest.raises(ValueError):
+            llgpu.diag_export(3, a, b, c)
+
+
+def test_algorithms_module_without_a_gpu(built):
+    import quantum_sim_algorithms as alg
+
+    g = alg.Graph(4, [(0, 1, 1.0), (1, 2, 2.0)])
+    g.add_edge(2, 3, 0.5)
+    assert alg.QAOA.cut_value(g, 0b0101) == 3.5 and len(g.edges) == 3
+    if llgpu.device_count() == 0:
+        with pytest.raises(RuntimeError):
+            alg.make_gpu_backend(3)  # no CPU fallback

@@ -28,15 +28,24 @@ def compile_driver(src: str, out: str, iface: str) -> str:
 
 
 @pytest.mark.skipif(not REF_SRC, reason="reference tree not present on this machine")
-def test_reference_algorithms_compile_against_gpu_backend(built):
+def test_reference_algorithms_compile_against_gpu_backend(built, golden):
     exe = compile_driver("reference_algorithms_on_gpu.cpp", "ref_alg_gpu", REF_SRC)
-    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    v = golden("vqe_param_shift")
+    theta = v["n4_l2_theta"]
+    r = subprocess.run([exe] + [repr(float(t)) for t in theta], capture_output=True, text=True, timeout=120)
     if llgpu.device_count() == 0:
         assert r.returncode == 4 and "runtime_error" in r.stderr  # loud failure, no CPU fallback
-    else:
-        assert r.returncode == 0, r.stderr
-        it, mi, p = r.stdout.split("\n")[0].split()[1:]
-        assert int(it) == 12 and int(mi) == 85 and abs(float(p) - 0.99994704) < 5e-9
+        return
+    assert r.returncode == 0, r.stderr
+    lines = {ln.split()[0]: ln.split()[1:] for ln in r.stdout.strip().split("\n")}
+    it, mi, p = lines["grover"]
+    assert int(it) == 12 and int(mi) == 85 and abs(float(p) - 0.99994704) < 5e-9
+    a = golden("algorithms")
+    q = [float(x) for x in lines["qaoa"]]
+    assert q[0] == float(a["qaoa_ring4_p1_best_cut"])
+    assert np.max(np.abs(np.array(q[1:]) - a["qaoa_ring4_p1_probs"])) <= 1e-12
+    probs = np.array([float(x) for x in lines["vqe"]])
+    assert np.max(np.abs(probs - np.abs(v["n4_l2_state"]) ** 2)) <= 1e-12
 
 
 def test_restated_interface_matches_reference_signatures():

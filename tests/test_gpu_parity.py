@@ -370,3 +370,36 @@ def test_twenty_qubit_layered_vs_oracle():
     got = run_gpu(n, ops, "complex64", "tile")
     fid = abs(np.vdot(want, got)) ** 2
     assert 1 - fid < 1e-9
+
+
+def _sk_terms(n, seed):
+    # Sherrington-Kirkpatrick couplings J_ij ~ N(0, 1/n) on every pair plus random fields: more
+    # terms and distinct coefficients than the class-counting kernel takes
+    rng = np.random.default_rng(seed)
+    zz = [(i, j, float(rng.normal() / np.sqrt(n))) for i in range(n) for j in range(i + 1, n)]
+    z = [(i, float(rng.normal())) for i in range(n)]
+    return llgpu.ising_terms(n, zz, z)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_sk_energy_matches_oracle(precision):
+    # a 20-qubit SK-model energy (190 couplings + 20 fields) through llg_expect_zz's general
+    # kernel, and the same diagonal as a full 2^n vector through llg_expect_diagonal (host and
+    # device copies), against the oracle's term-by-term sum
+    n = 20
+    a, b, c = _sk_terms(n, 5)
+    ops = workloads.layered_rotations(n, layers=2, seed=9)
+    psi = oracle.run_ops(n, ops)
+    want = oracle.expect_zz(psi, n, a, b, c)
+    st = llgpu.State(precision=precision, amps=psi)
+    tol = 1e-11 if precision != "complex64" else 1e-5
+    assert abs(st.expect_zz(a, b, c) - want) <= tol
+    assert abs(st.expect_zz(a, b, c) - want) <= tol  # the cached device layout
+    d = llgpu.diag_export(n, a, b, c)
+    assert abs(st.expect_diagonal(d) - want) <= tol
+    torch = pytest.importorskip("torch")
+    assert abs(st.expect_diagonal(torch.from_numpy(d).cuda()) - want) <= tol
+    # a small observable still takes the class-counting kernel, after the large one
+    ra, rb, rc = llgpu.ring_zz_terms(n)
+    assert abs(st.expect_zz(ra, rb, rc) - oracle.expect_zz(psi, n, ra, rb, rc)) <= tol
+    st.close()

@@ -66,14 +66,35 @@ def test_noalloc_expectation_matches_existing_entry_point(built):
             assert abs(got[1] - want_norm) <= TOL[precision]
 
 
+def test_noalloc_large_then_small_call(built):
+    # a 22-qubit state fills every one of the 1024 scratch rows (the grid cap binds and the blocks
+    # stride past it); a 12-qubit call right after it on the same stream reads only its own rows
+    torch = pytest.importorskip("torch")
+    stream = torch.cuda.current_stream().cuda_stream
+    rng = np.random.default_rng(99)
+    for n in (22, 12):
+        a, b, c = llgpu.ring_zz_terms(n)
+        psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+        psi /= np.linalg.norm(psi)
+        st = llgpu.State(precision="fp64", amps=psi)
+        want, want_norm = st.expect_zz(a, b, c), st.norm2()
+        st.close()
+        d_amps = torch.from_numpy(device_layout(psi, "fp64")).cuda()
+        d_out = torch.full((2,), float("nan"), dtype=torch.float64, device="cuda")
+        assert call_noalloc(d_amps.data_ptr(), n, "fp64", a, b, c, d_out.data_ptr(), stream) == 0, llgpu.last_error()
+        torch.cuda.synchronize()
+        got = d_out.cpu().numpy()
+        assert abs(got[0] - want) <= TOL["fp64"] and abs(got[1] - want_norm) <= TOL["fp64"], (n, got, want)
+
+
 def test_noalloc_rejects_sizes_beyond_its_limits(built):
     torch = pytest.importorskip("torch")
     d = torch.zeros(8, dtype=torch.float64, device="cuda")
     out = torch.zeros(2, dtype=torch.float64, device="cuda")
     assert call_noalloc(d.data_ptr(), 35, "fp64", [0], [-1], [1.0], out.data_ptr(), None) == llgpu.LLG_EINVAL
     assert "n_qubits" in llgpu.last_error()
-    many = list(range(65))
     assert call_noalloc(d.data_ptr(), 2, "fp64", [0] * 65, [-1] * 65, [1.0] * 65, out.data_ptr(), None) == llgpu.LLG_EINVAL
+    assert "terms" in llgpu.last_error()
     host = np.zeros(8)
     assert call_noalloc(host.ctypes.data, 2, "fp64", [0], [-1], [1.0], out.data_ptr(), None) == llgpu.LLG_EINVAL
-    del many
+    assert "device" in llgpu.last_error()
