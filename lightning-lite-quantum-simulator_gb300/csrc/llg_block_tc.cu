@@ -62,8 +62,6 @@ struct TcShape {
     static_assert(6 * kReals <= kTmemCols, "accumulators fit the allocation");
 };
 
-__device__ int g_block_tc_error = 0;
-
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 // tcgen05 shared-memory descriptor, no swizzle: start, leading (K-direction core) byte offset,
@@ -95,7 +93,7 @@ __device__ __forceinline__ df df_add_f(df a, float b) {
 template <int KQ>
 __global__ void __launch_bounds__(TcShape<KQ>::kThreads, TcShape<KQ>::kMinBlocks)
     k_block_tc(float4* __restrict__ psi, int n, BlockDesc bd, const uint16_t* __restrict__ wslices,
-               const int32_t* __restrict__ wexp) {
+               const int32_t* __restrict__ wexp, int* __restrict__ err_flag) {
     using T = TcShape<KQ>;
     constexpr int kAmps = T::kAmps, kReals = T::kReals, kPer = T::kPer;
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -262,7 +260,7 @@ __global__ void __launch_bounds__(TcShape<KQ>::kThreads, TcShape<KQ>::kMinBlocks
         if (abort_s) {
             // report, then give the products in flight a second bounded wait before the
             // accumulators are freed
-            if (tid == 0) atomicExch(&g_block_tc_error, 1);
+            if (tid == 0) atomicExch(err_flag, 1);
             done = 0;
             for (long it = 0; it < kTcWaitLimit && !done; ++it)
                 asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
@@ -332,7 +330,7 @@ __global__ void __launch_bounds__(TcShape<KQ>::kThreads, TcShape<KQ>::kMinBlocks
 }
 
 template <int KQ>
-cudaError_t launch_tc(void* psi, int n, const BlockDesc& bd, const void* d_weights, cudaStream_t s) {
+cudaError_t launch_tc(void* psi, int n, const BlockDesc& bd, const void* d_weights, int* err_flag, cudaStream_t s) {
     using T = TcShape<KQ>;
     // once per block size (thread-safe static initialisation)
     static const cudaError_t attr = cudaFuncSetAttribute(k_block_tc<KQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::kSmem);
@@ -346,7 +344,7 @@ cudaError_t launch_tc(void* psi, int n, const BlockDesc& bd, const void* d_weigh
     const uint16_t* w = static_cast<const uint16_t*>(d_weights);
     const int32_t* ex = reinterpret_cast<const int32_t*>(static_cast<const unsigned char*>(d_weights) +
                                                           (size_t)kTcSlices * T::kWSliceBytes);
-    k_block_tc<KQ><<<grid, T::kThreads, T::kSmem, s>>>(static_cast<float4*>(psi), n, bd, w, ex);
+    k_block_tc<KQ><<<grid, T::kThreads, T::kSmem, s>>>(static_cast<float4*>(psi), n, bd, w, ex, err_flag);
     return cudaGetLastError();
 }
 
@@ -399,19 +397,8 @@ size_t block_tc_weight_bytes(int k) {
 
 bool block_tc_eligible(int P, int n, int k) { return P == LLG_DF64 && (k == 4 || k == 5) && n >= k + 7; }
 
-cudaError_t launch_block_tc(void* psi, int n, const BlockDesc& bd, const void* d_weights, cudaStream_t s) {
-    return bd.k == 5 ? launch_tc<5>(psi, n, bd, d_weights, s) : launch_tc<4>(psi, n, bd, d_weights, s);
-}
-
-// 1 if a tensor-core block kernel timed out waiting for its products since the last call
-int block_tc_take_error() {
-    int h = 0;
-    cudaMemcpyFromSymbol(&h, g_block_tc_error, sizeof(int));
-    if (h) {
-        const int zero = 0;
-        cudaMemcpyToSymbol(g_block_tc_error, &zero, sizeof(int));
-    }
-    return h;
+cudaError_t launch_block_tc(void* psi, int n, const BlockDesc& bd, const void* d_weights, int* err_flag, cudaStream_t s) {
+    return bd.k == 5 ? launch_tc<5>(psi, n, bd, d_weights, err_flag, s) : launch_tc<4>(psi, n, bd, d_weights, err_flag, s);
 }
 
 }  // namespace llg

@@ -77,6 +77,8 @@ struct llg_state {
     unsigned char* h_block_tc = nullptr;
     bool block_tc_launched = false;
     bool tiles_launched = false;  // a tile pass ran since the last sync (its load-timeout flag to check)
+    // this state's timeout flags on the device: [0] a bulk tile load, [1] tensor-core products
+    int* d_flags = nullptr;
     // reductions
     double* d_partials = nullptr;
     double* d_red = nullptr;
@@ -160,6 +162,10 @@ int ensure_device_buffers(llg_state* st) {
     if (!st->d_partials) {
         LLG_CUDA(cudaMalloc(&st->d_partials, sizeof(double) * kRedBlocks * kPartialSlots), "cudaMalloc(partials)");
         LLG_CUDA(cudaMalloc(&st->d_red, sizeof(double) * kRedSlots), "cudaMalloc(red)");
+    }
+    if (!st->d_flags) {
+        LLG_CUDA(cudaMalloc(&st->d_flags, 2 * sizeof(int)), "cudaMalloc(flags)");
+        LLG_CUDA(cudaMemsetAsync(st->d_flags, 0, 2 * sizeof(int), st->stream), "cudaMemsetAsync(flags)");
     }
     return LLG_OK;
 }
@@ -280,7 +286,7 @@ int run_tiles(llg_state* st, const std::vector<llg_op>& q, double* mirror = null
         rc = traced(st, LLG_PROF_TILE, 1, "tile kernel",
                     [&] {
                         return launch_tile_pass(st->P, st->d_psi, st->n, pd, st->d_ops, st->d_tables, st->tile_threads,
-                                                st->stream, m);
+                                                st->d_flags, st->stream, m);
                     });
         if (rc) return rc;
     }
@@ -425,6 +431,7 @@ int llg_destroy(llg_state* st) {
     if (st->h_tables) cudaFreeHost(st->h_tables);
     if (st->d_partials) cudaFree(st->d_partials);
     if (st->d_red) cudaFree(st->d_red);
+    if (st->d_flags) cudaFree(st->d_flags);
     if (st->d_obs) cudaFree(st->d_obs);
     if (st->d_diag) cudaFree(st->d_diag);
     for (int i = 0; i < 2; ++i) {
@@ -634,7 +641,7 @@ int llg_apply_matrix(llg_state* st, int k, const int* qubits, const double* m) {
         st->block_pending = true;
         st->block_tc_launched = true;
         return traced(st, LLG_PROF_GATE, 1, "block kernel (tensor cores)",
-                      [&] { return launch_block_tc(st->d_psi, st->n, bd, st->d_block_tc, st->stream); });
+                      [&] { return launch_block_tc(st->d_psi, st->n, bd, st->d_block_tc, st->d_flags, st->stream); });
     }
     for (int i = 0; i < slots; ++i) st->h_block[i] = pack_coef(st->P, m[i]);
     LLG_CUDA(cudaMemcpyAsync(st->d_block, st->h_block, slots * sizeof(uint64_t), cudaMemcpyHostToDevice, st->stream),
@@ -723,16 +730,17 @@ int llg_flush(llg_state* st) {
 
 // After the state's stream has drained: the timeout flags of the kernels that wait on the
 // asynchronous units (tensor-core products, bulk tile loads), for the launches since the last check.
+// The flags are this state's own, read and cleared on its own stream.
 static int device_checks(llg_state* st) {
-    if (st->block_tc_launched) {
-        st->block_tc_launched = false;
-        if (block_tc_take_error())
-            return set_error(LLG_ECUDA, "apply_matrix: a tensor-core block kernel timed out waiting for its products");
-    }
-    if (st->tiles_launched) {
-        st->tiles_launched = false;
-        if (tile_copy_take_error()) return set_error(LLG_ECUDA, "tile pass: a bulk tile load timed out");
-    }
+    if (!st->block_tc_launched && !st->tiles_launched) return LLG_OK;
+    const bool tc = st->block_tc_launched, tiles = st->tiles_launched;
+    st->block_tc_launched = st->tiles_launched = false;
+    int h[2] = {0, 0};
+    LLG_CUDA(cudaMemcpyAsync(h, st->d_flags, sizeof(h), cudaMemcpyDeviceToHost, st->stream), "cudaMemcpyAsync(flags)");
+    LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+    if (h[0] || h[1]) LLG_CUDA(cudaMemsetAsync(st->d_flags, 0, sizeof(h), st->stream), "cudaMemsetAsync(flags)");
+    if (tc && h[1]) return set_error(LLG_ECUDA, "apply_matrix: a tensor-core block kernel timed out waiting for its products");
+    if (tiles && h[0]) return set_error(LLG_ECUDA, "tile pass: a bulk tile load timed out");
     return LLG_OK;
 }
 

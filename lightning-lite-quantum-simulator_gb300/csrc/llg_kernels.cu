@@ -10,6 +10,7 @@
 //    shared memory in 2^low-amplitude contiguous runs, applies a list of ops there, writes back.
 //  * conversions to/from complex128, |a|^2, scaling, and deterministic two-stage reductions
 //    (fixed grid, per-block partials, one FP64 pass over the partials).
+#include <atomic>
 #include <cstdio>
 
 #include "llg_common.cuh"
@@ -22,15 +23,24 @@ namespace {
 
 constexpr int kThreads = 256;
 
-int g_sms = 0;
+// SM count of each device, read once per device (the current device at launch time)
+constexpr int kMaxDevices = 64;
+std::atomic<int> g_sms[kMaxDevices];
 int sm_count() {
-    if (g_sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_sms <= 0) g_sms = 1;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        return 1;
     }
-    return g_sms;
+    int v = g_sms[dev].load(std::memory_order_relaxed);
+    if (v <= 0) {
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) {
+            cudaGetLastError();
+            v = 1;
+        }
+        g_sms[dev].store(v, std::memory_order_relaxed);
+    }
+    return v;
 }
 
 unsigned grid_for(uint64_t items, int per_thread) {
@@ -151,8 +161,6 @@ __global__ void __launch_bounds__(kThreads) k_mcz(typename P::S* __restrict__ ps
 constexpr int kOpChunk = 32;  // op records staged per shared-memory chunk in k_tile
 constexpr long kTileCopyWaitLimit = 1L << 24;  // mbarrier polls before a tile load is reported as timed out
 
-__device__ int g_tile_copy_error = 0;
-
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 // bounded wait for phase `parity` of an mbarrier; false if it did not complete
@@ -167,7 +175,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 
 template <class P>
 __global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, PassDesc pd, const ExecOp* __restrict__ ops,
-                                               const uint64_t* __restrict__ tables, double2* __restrict__ mirror) {
+                                               const uint64_t* __restrict__ tables, double2* __restrict__ mirror,
+                                               int* __restrict__ err_flag) {
     using S = typename P::S;
     using K = typename P::K;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -209,7 +218,7 @@ __global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, 
                 "l"(psi + (base | hi_off[h])), "r"(run_bytes), "r"(smem_addr(&tile_bar))
                 : "memory");
         loaded = mbar_wait(&tile_bar, 0);
-        if (!loaded && threadIdx.x == 0) atomicExch(&g_tile_copy_error, 1);
+        if (!loaded && threadIdx.x == 0) atomicExch(err_flag, 1);
     } else {
         for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) tile[l] = psi[base | hi_off[l >> low] | (l & lowmask)];
     }
@@ -488,7 +497,7 @@ size_t tile_smem_bytes(int t, int low) {
 
 template <class P>
 cudaError_t tile_pass_t(void* vpsi, int n, const PassDesc& pd, const ExecOp* d_ops, const uint64_t* d_tables, int threads,
-                        double* mirror, cudaStream_t s) {
+                        double* mirror, int* err_flag, cudaStream_t s) {
     // the largest dynamic shared memory of any tile, set once (thread-safe static initialisation)
     static const cudaError_t attr = cudaFuncSetAttribute(k_tile<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                          (int)tile_smem_bytes<P>(tile_max_qubits(P::kPrecision), 4));
@@ -497,7 +506,7 @@ cudaError_t tile_pass_t(void* vpsi, int n, const PassDesc& pd, const ExecOp* d_o
     const uint64_t ntiles = 1ULL << (n - pd.t);
     if (threads <= 0) threads = pd.t >= 10 ? 512 : (pd.t >= 6 ? (1 << (pd.t - 1)) : 32);
     k_tile<P><<<(unsigned)ntiles, threads, smem, s>>>(static_cast<typename P::S*>(vpsi), pd, d_ops, d_tables,
-                                                      reinterpret_cast<double2*>(mirror));
+                                                      reinterpret_cast<double2*>(mirror), err_flag);
     return cudaGetLastError();
 }
 
@@ -565,19 +574,9 @@ cudaError_t fp64_fma_rate(int iters, double* fma_per_s) {
     return e;
 }
 
-int tile_copy_take_error() {
-    int h = 0;
-    cudaMemcpyFromSymbol(&h, g_tile_copy_error, sizeof(int));
-    if (h) {
-        const int zero = 0;
-        cudaMemcpyToSymbol(g_tile_copy_error, &zero, sizeof(int));
-    }
-    return h;
-}
-
 cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, const uint64_t* d_tables,
-                             int threads, cudaStream_t s, double* mirror) {
-    LLG_DISPATCH(P, return tile_pass_t<Pol>(psi, n, pd, d_ops, d_tables, threads, mirror, s));
+                             int threads, int* err_flag, cudaStream_t s, double* mirror) {
+    LLG_DISPATCH(P, return tile_pass_t<Pol>(psi, n, pd, d_ops, d_tables, threads, mirror, err_flag, s));
 }
 
 template <class PA>

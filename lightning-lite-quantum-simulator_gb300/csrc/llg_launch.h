@@ -37,11 +37,10 @@ cudaError_t launch_exec_op(int P, void* psi, int n, const ExecOp& op, cudaStream
 // mirror: nullptr, or the device address of a host buffer that also receives the pass's output as
 // FP64 (2 doubles per amplitude, full-state indexing)
 // d_tables: the plan's phase tables (Plan::tables on the device), or nullptr for a plan without
-// EX_PTAB ops
+// EX_PTAB ops; err_flag: a device int of the caller's that a CTA sets to 1 when its bulk tile load
+// does not complete within the wait limit (the CTA then stores nothing)
 cudaError_t launch_tile_pass(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, const uint64_t* d_tables,
-                             int threads, cudaStream_t s, double* mirror = nullptr);
-// 1 if a tile pass's bulk load timed out since the last call (the flag is cleared)
-int tile_copy_take_error();
+                             int threads, int* err_flag, cudaStream_t s, double* mirror = nullptr);
 cudaError_t launch_from_f64(int P, const double* src, void* dst, uint64_t count, cudaStream_t s);
 cudaError_t launch_to_f64(int P, const void* src, double* dst, uint64_t count, cudaStream_t s);
 cudaError_t launch_probabilities(int P, const void* psi, double* out, uint64_t count, cudaStream_t s);
@@ -75,12 +74,11 @@ cudaError_t launch_block(int P, void* psi, int n, const BlockDesc& bd, const uin
 // 4- and 5-qubit blocks on double-float states of at least k + 7 qubits on the tensor cores
 // (llg_block_tc.cu): the host slices the matrix (2 * 4^k doubles, row-major re/im) into
 // block_tc_weight_bytes(k) of device input; a kernel whose products do not arrive within its
-// wait limit sets a flag that block_tc_take_error() returns (and clears)
+// wait limit sets *err_flag (a device int of the caller's) to 1
 bool block_tc_eligible(int P, int n, int k);
 size_t block_tc_weight_bytes(int k);
 void block_tc_prepare(int k, const double* m, void* weights);
-cudaError_t launch_block_tc(void* psi, int n, const BlockDesc& bd, const void* d_weights, cudaStream_t s);
-int block_tc_take_error();
+cudaError_t launch_block_tc(void* psi, int n, const BlockDesc& bd, const void* d_weights, int* err_flag, cudaStream_t s);
 
 // process-wide tuning cache (llg_tune.cu), keyed by an FNV-1a hash of the workload's shape
 uint64_t tune_hash(uint64_t h, uint64_t v);

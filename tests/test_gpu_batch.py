@@ -91,20 +91,41 @@ def test_bounded_wait_reports_timeout():
 
 
 def test_full_config5_batch():
-    """512 circuits, n uniform in 10..22, 200 gates each; complex64 vs complex128 fidelity per
-    circuit; circuits up to 16 qubits against the oracle."""
+    """512 circuits, n uniform in 10..22, 200 gates each, in IEEE complex128, double-float and
+    complex64: every circuit of up to 18 qubits against the oracle (the oracle runs them on every
+    host core), the rest of the complex128 batch against the double-float one, and complex64 against
+    complex128 per circuit."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+
     nq, ops, off = workloads.mixed_batch(512, 10, 22, 200)
-    b128 = llgpu.Batch(nq, ops, off, "df64")
+    b128 = llgpu.Batch(nq, ops, off, "complex128")
+    bdf = llgpu.Batch(nq, ops, off, "df64")
     b64 = llgpu.Batch(nq, ops, off, "complex64")
-    b128.run()
-    b64.run()
+    for b in (b128, bdf, b64):
+        b.run()
     f = b64.fidelity(b128)
     assert np.all(np.abs(f[:, 2] - 1) < 1e-11)
     assert np.all(1 - f[:, 0] < 1e-8)
-    checked = 0
-    for i in range(512):
-        if nq[i] <= 16 and checked < 6:
-            want = oracle.run_ops(int(nq[i]), ops[off[i]:off[i + 1]])
-            assert np.max(np.abs(b128.state(i) - want)) <= 1e-12
-            checked += 1
-    assert checked == 6
+    fd = bdf.fidelity(b128)
+    assert np.all(1 - fd[:, 0] < 1e-13)
+    small = [i for i in range(512) if nq[i] <= 18]
+    assert len(small) > 250
+    oracle.set_threads(1)
+    # oracle runs in worker processes started with spawn (the GPU context stays in this process)
+    with cf.ProcessPoolExecutor(max_workers=min(16, mp.cpu_count()), mp_context=mp.get_context("spawn")) as ex:
+        wants = list(ex.map(_oracle_circuit, [(int(nq[i]), ops[off[i]:off[i + 1]]) for i in small], chunksize=8))
+    for i, want in zip(small, wants):
+        assert np.max(np.abs(b128.state(i) - want)) <= 1e-12, i
+        assert np.max(np.abs(bdf.state(i) - want)) <= 1e-12, i
+    oracle.set_threads(oracle.max_threads())
+    for b in (b128, bdf, b64):
+        b.close()
+
+
+def _oracle_circuit(args):
+    import oracle as orc
+
+    orc.set_threads(1)
+    n, o = args
+    return orc.run_ops(n, o)

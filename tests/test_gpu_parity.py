@@ -403,3 +403,30 @@ def test_sk_energy_matches_oracle(precision):
     ra, rb, rc = llgpu.ring_zz_terms(n)
     assert abs(st.expect_zz(ra, rb, rc) - oracle.expect_zz(psi, n, ra, rb, rc)) <= tol
     st.close()
+
+
+def test_apply_fused_gate_list():
+    # GateFuser.fuse_circuit output fed to StateVector.apply_fused (python/gate_fusion.py:15-37,
+    # benchmarks/benchmark_fusion.py:36-50): the fused list gives the unfused circuit's state
+    import quantum_sim_v3
+    from gate_fusion import GATES, GateFuser
+
+    rng = np.random.default_rng(44)
+    n = 12
+    gates = []
+    for _ in range(400):
+        q = int(rng.integers(n))
+        if rng.uniform() < 0.5:
+            gates.append((q, GATES[["X", "H", "S", "T"][int(rng.integers(4))]]))
+        else:
+            u = np.linalg.qr(rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2)))[0]
+            gates.append((q, list(u.reshape(4))))
+    fused = GateFuser.fuse_circuit(gates)
+    assert len(fused) < len(gates)
+    want = oracle.zero_state(n)
+    for q, g in gates:
+        oracle.apply_gate_v3(want, n, q, g)
+    for precision in ("complex128", "df64"):
+        sv = quantum_sim_v3.StateVector(n, precision)
+        sv.apply_fused(fused)
+        assert np.max(np.abs(sv.get_numpy_view() - want)) <= 1e-12, precision
