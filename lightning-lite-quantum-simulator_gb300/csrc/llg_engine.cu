@@ -779,17 +779,18 @@ int llg_copy_to_host(llg_state* st, double* out) {
     }
     rc = llg_flush(st);
     if (rc) return rc;
-    if (st->P == LLG_F64) {
-        LLG_CUDA(cudaMemcpyAsync(out, st->d_psi, st->size * 16, cudaMemcpyDeviceToHost, st->stream), "cudaMemcpyAsync(D2H)");
-        LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
-        return device_checks(st);
-    }
-    // A pinned destination is written by the conversion kernel itself, over the host link: one
-    // pass at the link's rate, with no staging copy and no copy-engine step after each chunk.
+    // A pinned destination is written by the conversion kernel itself (a plain copy for FP64
+    // states), over the host link: one pass at the link's rate, with no staging copy and no
+    // copy-engine step after each chunk.
     if (dev_out) {
         rc = traced(st, LLG_PROF_READOUT, 1, "to_f64",
                     [&] { return launch_to_f64(st->P, st->d_psi, static_cast<double*>(dev_out), st->size, st->stream); });
         if (rc) return rc;
+        LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
+        return device_checks(st);
+    }
+    if (st->P == LLG_F64) {  // pageable destination, same layout: one copy
+        LLG_CUDA(cudaMemcpyAsync(out, st->d_psi, st->size * 16, cudaMemcpyDeviceToHost, st->stream), "cudaMemcpyAsync(D2H)");
         LLG_CUDA(cudaStreamSynchronize(st->stream), "cudaStreamSynchronize");
         return device_checks(st);
     }
