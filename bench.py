@@ -309,10 +309,14 @@ def is_f64(precision: str) -> bool:
     return precision in ("complex128", "fp64", "f64")
 
 
-def plan_for(precision: str, n: int, ops, tile_q: int):
+def plan_for(precision: str, n: int, ops, tile_q: int, regs: bool = False):
+    """The plan the engine runs: carried phases and phase tables for 16-byte precisions, the plain
+    lowering for complex64 shared-memory tiles, register programs for register-tiled passes."""
     import llgpu
 
-    r = llgpu.plan_export(n, ops, tile_q, zyz=True, tables=precision != "complex64")
+    if regs:
+        return llgpu.plan_export(n, ops, tile_q, zyz=True, regs=True)
+    r = llgpu.plan_export(n, ops, tile_q, zyz=precision != "complex64", tables=precision != "complex64")
     return r[0], r[1]
 
 
@@ -383,7 +387,7 @@ def measure_circuit(args, torch, precision, n, ops, steps, warmup, world, sample
         st.set_tile_threads(args.cta_threads)
     tuning = st.tuning()
     tile_q = tuning["tile_qubits"]
-    passes, xops = plan_for(precision, n, ops, tile_q)
+    passes, xops = plan_for(precision, n, ops, tile_q, tuning["fuse_mode"] == "reg")
     if tuning["fuse_mode"] == "none":
         passes = np.zeros(ngates)  # one streaming pass per gate
     state_bytes = ELEM_BYTES.get(precision, 16) * (1 << n)
@@ -440,10 +444,12 @@ def measure_circuit(args, torch, precision, n, ops, steps, warmup, world, sample
         "hbm_gbs_algorithmic": len(passes) * 2 * state_bytes * steps * world / (elapsed_ms / 1e3) / 1e9,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": profile_traffic(precision, n),
-                     "kernel": f"k_tile<{TILE_POLICY.get(precision, precision)}> (tile pass)", "launches": tile_n,
+                     "kernel": (f"k_tile_reg<{TILE_POLICY.get(precision, precision)}> (register-tiled pass)"
+                                if tuning["fuse_mode"] == "reg" else f"k_tile<{TILE_POLICY.get(precision, precision)}> (tile pass)"),
+                     "launches": tile_n,
                      "mean_launch_ms": tile_ms / tile_n if tile_n else None, "peak_source": f"{peak_kind} hbm_gbs"},
         "kernel_ms_per_step": {k: v[0] / steps for k, v in prof.items()},
-        "_xops": xops if tuning["fuse_mode"] == "tile" else np.zeros(0, dtype=xops.dtype),
+        "_xops": xops if tuning["fuse_mode"] != "none" else np.zeros(0, dtype=xops.dtype),
         "_tile_ms_step": prof["tile"][0] / steps,
     }
     if keep:
@@ -487,7 +493,7 @@ def run_ours(args, rank, world, local):
     head = finish_rooflines(head, args.precision, n, fma_rate)
     clocks = head.pop("clocks")
     elem = ELEM_BYTES.get(args.precision, 16)
-    _, xops_e2e = plan_for(args.precision, n, ops, head["tile_qubits"])
+    _, xops_e2e = plan_for(args.precision, n, ops, head["tile_qubits"], head["fusion"]["fuse_mode"] == "reg")
 
     # the same circuit in the other precisions, each compared with this (FP64) final state
     variants = None
@@ -503,7 +509,7 @@ def run_ours(args, rank, world, local):
                             "max_abs_diff_rel_to_max_amp": (dmax / amax) if amax else None}
             vst.close()
             if not args.no_e2e:
-                v["e2e"] = run_e2e(args, prec, ops, plan_for(prec, n, ops, v["tile_qubits"])[1], n,
+                v["e2e"] = run_e2e(args, prec, ops, plan_for(prec, n, ops, v["tile_qubits"], v["fusion"]["fuse_mode"] == "reg")[1], n,
                                    ELEM_BYTES.get(prec, 16), world, torch, v["tile_qubits"])
             variants[prec] = v
     st.close()

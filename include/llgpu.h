@@ -49,6 +49,8 @@ extern "C" {
 /* ---- fusion modes for the pending-gate queue ---- */
 #define LLG_FUSE_NONE 0 /* one streaming kernel per gate: the reference's own algorithm */
 #define LLG_FUSE_TILE 1 /* shared-memory tile passes over chosen qubit sets (cache blocking) */
+#define LLG_FUSE_REG 2  /* register-tiled passes: complex64 states, tiles of 9..13 qubits held in
+                           registers (16 amplitudes per thread), shared memory only between layouts */
 
 /* ---- gate record (96 bytes).  Kinds 0..6 are the Op kinds of the reference's random-circuit
  * test, tests/test_backends.cpp:78-83 (h, x, rx, ry, rz, cnot, mcz). ---- */
@@ -492,6 +494,11 @@ int llg_plan_export(int n, const llg_op* ops, int nops, int tile_qubits, llg_pas
  * does for those states.  llg_plan_export plans without either. */
 #define LLG_PLAN_ZYZ 1
 #define LLG_PLAN_TABLES 2
+/* LLG_PLAN_REGS: the register programs of the register-tiled pass (kind 19 switches the layout:
+ * register positions in mask, 4 bits each; thread-index positions in nl_mask; 1-qubit ops name a
+ * register slot in q0, CNOTs their target slot in q1 and, with flags bit 4, a control slot in q0),
+ * as the engine runs complex64 states (tables are not combined with it). */
+#define LLG_PLAN_REGS 4
 int llg_plan_export_ex(int n, const llg_op* ops, int nops, int tile_qubits, int flags, llg_pass_info* passes,
                        int max_passes, int* npasses, llg_exec_op* xops, int max_xops, int* nxops);
 /* The eigenvalue d(i) of the diagonal observable sum_k coeff_k Z_{a_k} Z_{b_k} (b_k < 0: Z_{a_k}) for

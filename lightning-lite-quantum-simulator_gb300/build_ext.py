@@ -28,7 +28,7 @@ CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-I" + INCLUDE, "-I" + CSRC]
 
 CU_SOURCES = ["llg_kernels.cu", "llg_engine.cu", "llg_noalloc.cu", "llg_adjoint.cu", "llg_traj.cu", "llg_batch.cu",
               "llg_tune.cu", "llg_block.cu", "llg_block_tc.cu",
-              "llg_tsolver.cu", "llg_diag.cu"]
+              "llg_tsolver.cu", "llg_diag.cu", "llg_tile_reg.cu"]
 CXX_SOURCES = ["llg_plan.cpp", "llg_diag_host.cpp"]
 
 LIB = os.path.join(HERE, "libllgpu.so")

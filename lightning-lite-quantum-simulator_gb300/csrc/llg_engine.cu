@@ -270,9 +270,12 @@ int run_tiles(llg_state* st, const std::vector<llg_op>& q, double* mirror = null
     Plan plan;
     std::string err;
     const int t = st->tile_qubits > 0 ? st->tile_qubits : default_tile(st->P);
-    if (!plan_tiles(st->n, q.data(), (int)q.size(), std::min(t, tile_max_qubits(st->P)), st->P, plan, err, false,
-                    ZYZ_DEFAULT, st->P != LLG_F32))
+    // register-tiled passes on registers of 9+ qubits (smaller ones keep the shared-memory tiles)
+    const bool reg = st->fuse_mode == LLG_FUSE_REG && std::min(st->n, std::min(t, 13)) >= 9;
+    if (!plan_tiles(st->n, q.data(), (int)q.size(), reg ? std::min(t, 13) : std::min(t, tile_max_qubits(st->P)), st->P,
+                    plan, err, false, reg ? ZYZ_ON : ZYZ_DEFAULT, !reg && st->P != LLG_F32))
         return set_error(LLG_EINVAL, err);
+    if (reg) to_register_program(plan);
     int rc = upload_ops(st, plan.ops, &plan.tables);
     if (rc) return rc;
     st->tiles_launched = true;
@@ -285,6 +288,7 @@ int run_tiles(llg_state* st, const std::vector<llg_op>& q, double* mirror = null
         double* m = i == last ? mirror : nullptr;
         rc = traced(st, LLG_PROF_TILE, 1, "tile kernel",
                     [&] {
+                        if (reg) return launch_tile_reg(st->P, st->d_psi, st->n, pd, st->d_ops, st->stream, m);
                         return launch_tile_pass(st->P, st->d_psi, st->n, pd, st->d_ops, st->d_tables, st->tile_threads,
                                                 st->d_flags, st->stream, m);
                     });
@@ -484,7 +488,10 @@ int llg_get_precision(const llg_state* st, int* out) {
 
 int llg_set_fusion(llg_state* st, int mode, int tile_qubits) {
     if (!st) return set_error(LLG_EINVAL, "llg_set_fusion: NULL state");
-    if (mode != LLG_FUSE_NONE && mode != LLG_FUSE_TILE) return set_error(LLG_EINVAL, "llg_set_fusion: unknown mode");
+    if (mode != LLG_FUSE_NONE && mode != LLG_FUSE_TILE && mode != LLG_FUSE_REG)
+        return set_error(LLG_EINVAL, "llg_set_fusion: unknown mode");
+    if (mode == LLG_FUSE_REG && (st->P != LLG_F32 || (tile_qubits != 0 && (tile_qubits < 9 || tile_qubits > 13))))
+        return set_error(LLG_EINVAL, "llg_set_fusion: register-tiled passes take complex64 states and tiles of 9..13 qubits");
     if (tile_qubits < 0 || tile_qubits > tile_max_qubits(st->P) || (tile_qubits > 0 && tile_qubits < 5))
         return set_error(LLG_EINVAL, "llg_set_fusion: tile_qubits must be 0 or in [5, " +
                                          std::to_string(tile_max_qubits(st->P)) + "]");
@@ -725,7 +732,7 @@ int llg_flush(llg_state* st) {
     std::vector<llg_op> q;
     q.swap(st->queue);
     if (st->n == 0) return LLG_OK;
-    return st->fuse_mode == LLG_FUSE_TILE ? run_tiles(st, q) : run_streaming(st, q);
+    return st->fuse_mode != LLG_FUSE_NONE ? run_tiles(st, q) : run_streaming(st, q);
 }
 
 // After the state's stream has drained: the timeout flags of the kernels that wait on the
@@ -767,7 +774,7 @@ int llg_copy_to_host(llg_state* st, double* out) {
     int rc;
     // Gates still queued for tile passes: the last pass writes the host buffer as it stores its
     // tiles, so the transfer runs under that pass's arithmetic instead of after it.
-    if (dev_out && !st->queue.empty() && st->n > 0 && st->fuse_mode == LLG_FUSE_TILE) {
+    if (dev_out && !st->queue.empty() && st->n > 0 && st->fuse_mode != LLG_FUSE_NONE) {
         std::vector<llg_op> q;
         q.swap(st->queue);
         bool mirrored = false;
@@ -1152,8 +1159,12 @@ int export_plan(int n, const llg_op* ops, int nops, int tile_qubits, int flags, 
     }
     std::string err;
     if (!plan_tiles(n, ops, nops, tile_qubits, LLG_F64, plan, err, false, (flags & LLG_PLAN_ZYZ) ? ZYZ_ON : ZYZ_OFF,
-                    (flags & LLG_PLAN_TABLES) != 0))
+                    (flags & LLG_PLAN_TABLES) != 0 && (flags & LLG_PLAN_REGS) == 0))
         return set_error(LLG_EINVAL, err);
+    if (flags & LLG_PLAN_REGS) {
+        if (tile_qubits < 9) return set_error(LLG_EINVAL, "plan_export: register programs need tiles of 9+ qubits");
+        to_register_program(plan);
+    }
     return LLG_OK;
 }
 }  // namespace

@@ -53,6 +53,11 @@ enum ExecKind : int32_t {
     // planner gathered there); the table starts at entry `mask` of the plan's table buffer and
     // has 2^t entries of (re, im) coefficient slots
     EX_PTAB = 18,
+    // register-tiled passes (to_register_program): switch the tile's register layout.  Each thread
+    // holds 16 amplitudes whose local indices vary over 4 "register" positions (mask: 4 x 4 bits)
+    // and are fixed by the thread index over the other t - 4 positions (nl_mask: 4 bits per thread
+    // index bit, in order; q0 = t - 4).  The tile moves through shared memory once per layout.
+    EX_LAYOUT = 19,
 };
 
 // Flags of a tile op.
@@ -62,6 +67,7 @@ enum : int32_t {
     OPF_GRAD = 4,         // backward pass: accumulate Im<lambda|P|psi> before applying the op
     OPF_PHASE = 8,        // EX_CNOT: multiply the amplitudes with control = target = 1 after the swap
                           // by c[0] + i c[1] (a carried target phase pushed through the CNOT)
+    OPF_SLOT_Q0 = 16,     // register program: q0 (a CNOT control, a diagonal's qubit) is a register slot
 };
 
 // One executor op.  In a tile pass q0/q1/mask are LOCAL (tile) indices unless flagged; `nl_mask`
@@ -114,6 +120,14 @@ enum PlanZyz : int { ZYZ_DEFAULT = -1, ZYZ_OFF = 0, ZYZ_ON = 1 };
 // amplitude pair; only kernels that execute EX_PTAB (the engine's tile pass) may run such plans.
 bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int precision, Plan& out, std::string& err,
                 bool use_params = false, int zyz = ZYZ_DEFAULT, bool tables = false);
+
+// Rewrites a tile plan (without EX_PTAB ops) as register programs for the register-tiled pass
+// kernel (tile widths 9..13): EX_LAYOUT ops are inserted so that the target of every non-diagonal
+// 1-qubit op and every CNOT is a register position when it runs; those ops then name register
+// slots 0..3 in q0 (CNOT: the target in q1, the control as a slot with OPF_SLOT_Q0, else a local
+// position or a global qubit as before).  Every pass starts and ends in the layout whose register
+// positions are the top four tile positions.  Returns the number of layout changes.
+int to_register_program(Plan& plan);
 
 // Lower one gate record to executor ops with GLOBAL qubit indices (streaming path).
 bool lower_op(int n, const llg_op& op, int precision, std::vector<ExecOp>& out, std::string& err);

@@ -57,6 +57,11 @@ cudaError_t launch_compare(int PA, const void* a, int PB, const void* b, uint64_
 
 int tile_max_qubits(int P);
 
+// register-tiled pass (llg_tile_reg.cu) over a register program (to_register_program): complex64
+// states, pd.t in [9, 13]; 2^(t-4) threads per CTA
+cudaError_t launch_tile_reg(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, cudaStream_t s,
+                            double* mirror = nullptr);
+
 // FP64 FMA operations per second of the current device (one timed launch of `iters` iterations)
 cudaError_t fp64_fma_rate(int iters, double* fma_per_s);
 

@@ -435,6 +435,134 @@ static void gather_phase_tables(Plan& out) {
     out.source_index.swap(src);
 }
 
+// ------------------------------------------------------------------------------------------
+// Register programs.  A thread of the register-tiled kernel holds 16 amplitudes of the tile: the
+// ones whose local index varies over 4 register positions, its thread index fixing the others.
+// An op whose target is a register position runs in registers; a layout change moves the tile
+// through shared memory once.  Layouts are chosen greedily: when an op's target is not a register
+// position, the next four distinct targets of the pass (in op order, from this op on) become the
+// register positions.  The thread-index bits go to the other positions, the first four to
+// positions of four different residues mod 4 where possible: the kernel's shared-memory swizzle
+// folds every 4-bit group of a local index into its low 4 bits, so such lanes hit distinct banks.
+// ------------------------------------------------------------------------------------------
+namespace {
+
+// the local position an op needs in a register (-1: none)
+int reg_need(const ExecOp& e) {
+    switch (e.kind) {
+        case EX_CNOT: return e.q1;
+        case EX_DIAG:
+        case EX_PHASE1:
+        case EX_MCZ: return -1;
+        default: return e.q0;
+    }
+}
+
+ExecOp layout_op(int t, const int regs[4]) {
+    ExecOp e = blank(EX_LAYOUT);
+    uint64_t rm = 0;
+    bool is_reg[kMaxTileQubits + 2] = {};
+    for (int j = 0; j < 4; ++j) {
+        rm |= (uint64_t)regs[j] << (4 * j);
+        is_reg[regs[j]] = true;
+    }
+    // thread-index bits: first four at distinct residues mod 4 (lowest first), then the rest ascending
+    std::vector<int> order;
+    bool used[kMaxTileQubits + 2] = {};
+    bool res_used[4] = {false, false, false, false};
+    for (int p = 0; p < t && order.size() < 4; ++p)
+        if (!is_reg[p] && !res_used[p & 3]) {
+            order.push_back(p);
+            used[p] = true;
+            res_used[p & 3] = true;
+        }
+    for (int p = 0; p < t; ++p)
+        if (!is_reg[p] && !used[p]) order.push_back(p);
+    uint64_t tm = 0;
+    for (size_t k = 0; k < order.size(); ++k) tm |= (uint64_t)order[k] << (4 * k);
+    e.mask = rm;
+    e.nl_mask = tm;
+    e.q0 = t - 4;
+    return e;
+}
+
+}  // namespace
+
+int to_register_program(Plan& out) {
+    std::vector<ExecOp> ops;
+    std::vector<int> src;
+    int changes = 0;
+    for (PassDesc& pd : out.passes) {
+        const int t = pd.t, b = pd.op_begin, m = pd.nops;
+        int base_regs[4], regs[4];
+        for (int j = 0; j < 4; ++j) base_regs[j] = regs[j] = t - 4 + j;
+        auto slot_of = [&](int q) {
+            for (int j = 0; j < 4; ++j)
+                if (regs[j] == q) return j;
+            return -1;
+        };
+        const int begin = (int)ops.size();
+        for (int i = 0; i < m; ++i) {
+            ExecOp x = out.ops[b + i];
+            const int q = reg_need(x);
+            if (q >= 0 && slot_of(q) < 0) {
+                // the next four distinct targets from here on
+                std::vector<int> want;
+                for (int k = i; k < m && want.size() < 4; ++k) {
+                    const int w = reg_need(out.ops[b + k]);
+                    if (w >= 0 && std::find(want.begin(), want.end(), w) == want.end()) want.push_back(w);
+                }
+                for (int j = 0; j < 4 && want.size() < 4; ++j)  // keep current registers in the free slots
+                    if (std::find(want.begin(), want.end(), regs[j]) == want.end()) want.push_back(regs[j]);
+                std::sort(want.begin(), want.end());
+                for (int j = 0; j < 4; ++j) regs[j] = want[j];
+                ops.push_back(layout_op(t, regs));
+                src.push_back(-1);
+                ++changes;
+            }
+            switch (x.kind) {
+                case EX_CNOT: {
+                    x.q1 = slot_of(x.q1);
+                    if (!(x.flags & OPF_NONLOCAL_Q0)) {
+                        const int c = slot_of(x.q0);
+                        if (c >= 0) {
+                            x.q0 = c;
+                            x.flags |= OPF_SLOT_Q0;
+                        }
+                    }
+                    break;
+                }
+                case EX_DIAG:
+                case EX_PHASE1:
+                    if (!(x.flags & OPF_NONLOCAL_Q0)) {
+                        const int c = slot_of(x.q0);
+                        if (c >= 0) {
+                            x.q0 = c;
+                            x.flags |= OPF_SLOT_Q0;
+                        }
+                    }
+                    break;
+                case EX_MCZ: break;
+                default: x.q0 = slot_of(x.q0); break;
+            }
+            ops.push_back(x);
+            src.push_back(out.source_index[b + i]);
+        }
+        bool same = true;
+        for (int j = 0; j < 4; ++j) same &= regs[j] == base_regs[j];
+        if (!same) {
+            ops.push_back(layout_op(t, base_regs));
+            src.push_back(-1);
+            ++changes;
+        }
+        pd.op_begin = begin;
+        pd.nops = (int)ops.size() - begin;
+    }
+    out.ops.swap(ops);
+    out.source_index.swap(src);
+    return changes;
+}
+
 static bool is_param_op(const llg_op& op, bool use_params) {
     return use_params && op.param >= 0 && (op.kind == LLG_OP_RX || op.kind == LLG_OP_RY || op.kind == LLG_OP_RZ);
 }

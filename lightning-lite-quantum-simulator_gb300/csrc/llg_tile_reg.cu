@@ -1,0 +1,260 @@
+// llg_tile_reg.cu -- register-tiled pass: the tile of a pass lives in registers, 16 amplitudes per
+// thread, and moves through shared memory only when the register layout changes (the register
+// programs of to_register_program, llg_plan.cpp).
+//
+// In the shared-memory tile pass every op reads and writes each amplitude pair in shared memory
+// and ends in a barrier; for complex64 (8 FMA per rotation pair) that traffic, the index arithmetic
+// and the barriers bound the pass.  Here a thread holds the amplitudes whose tile-local indices
+// vary over 4 register positions; an op on a register position is pure register arithmetic with
+// the pair pattern fixed at compile time, diagonal ops and CNOT controls on any position read the
+// thread's index bits, and a layout change is one shared-memory round trip (write, barrier, read)
+// for a run of ops.  The tile is read from and written to HBM directly from registers in the base
+// layout (thread-index bits on the low positions: 16 lanes cover one 128-byte run).
+//
+// Shared memory is swizzled: local index l lives at slot l ^ fold(l >> 4), fold XOR-ing the 4-bit
+// groups together.  A lane bit on position p toggles slot bit (p mod 4); the planner puts the first
+// four lane bits on positions of distinct residues, so a half-warp's 16 accesses hit 16 distinct
+// 8-byte bank pairs.
+#include <cuda_runtime.h>
+
+#include "llg_common.cuh"
+#include "llg_internal.h"
+#include "llg_launch.h"
+#include "llg_tile.cuh"
+
+namespace llg {
+
+namespace {
+
+constexpr int kRA = 16;         // amplitudes per thread
+constexpr int kROpChunk = 32;   // op records staged per shared-memory chunk
+
+__device__ __forceinline__ uint32_t swz(uint32_t l) {
+    const uint32_t x = l >> 4;
+    return l ^ ((x ^ (x >> 4) ^ (x >> 8)) & 15u);
+}
+
+// local-index offset of register amplitude e: bit j of e at register position j
+__device__ __forceinline__ uint32_t reg_off(const uint32_t rb[4], int e) {
+    return ((e & 1) ? rb[0] : 0u) | ((e & 2) ? rb[1] : 0u) | ((e & 4) ? rb[2] : 0u) | ((e & 8) ? rb[3] : 0u);
+}
+
+template <class P, int J, int KIND>
+__device__ __forceinline__ void reg_pairs_j(typename P::C (&a)[kRA], const ExecOp& o) {
+    const PairMath<P, KIND> m(o);
+#pragma unroll
+    for (int e = 0; e < kRA; ++e)
+        if (!(e & (1 << J))) m.apply(a[e], a[e | (1 << J)]);
+}
+
+template <class P, int KIND>
+__device__ __forceinline__ void reg_pairs(typename P::C (&a)[kRA], const ExecOp& o) {
+    switch (o.q0) {
+        case 0: reg_pairs_j<P, 0, KIND>(a, o); break;
+        case 1: reg_pairs_j<P, 1, KIND>(a, o); break;
+        case 2: reg_pairs_j<P, 2, KIND>(a, o); break;
+        default: reg_pairs_j<P, 3, KIND>(a, o); break;
+    }
+}
+
+// CNOT with target slot J: the control is a register slot (OPF_SLOT_Q0), a thread-index position
+// or a global qubit outside the tile; with OPF_PHASE the amplitudes that end at control = target
+// = 1 are multiplied by c[0] + i c[1]
+template <class P, int J>
+__device__ __forceinline__ void reg_cnot_j(typename P::C (&a)[kRA], const ExecOp& o, uint32_t tb, uint64_t base) {
+    using K = typename P::K;
+    using C = typename P::C;
+    const bool phased = (o.flags & OPF_PHASE) != 0;
+    const K pr = P::k_from_bits(o.c[0]), pi = P::k_from_bits(o.c[1]), mpi = P::kneg(pi);
+    if (o.flags & OPF_SLOT_Q0) {
+        const int k = o.q0;
+#pragma unroll
+        for (int e = 0; e < kRA; ++e)
+            if (!(e & (1 << J)) && ((e >> k) & 1)) {
+                C x = a[e];
+                a[e] = a[e | (1 << J)];
+                if (phased) cmul_const<P>(x, pr, pi, mpi);
+                a[e | (1 << J)] = x;
+            }
+        return;
+    }
+    const bool on = (o.flags & OPF_NONLOCAL_Q0) ? ((base >> o.q0) & 1) : ((tb >> o.q0) & 1);
+    if (!on) return;
+#pragma unroll
+    for (int e = 0; e < kRA; ++e)
+        if (!(e & (1 << J))) {
+            C x = a[e];
+            a[e] = a[e | (1 << J)];
+            if (phased) cmul_const<P>(x, pr, pi, mpi);
+            a[e | (1 << J)] = x;
+        }
+}
+
+template <class P>
+__device__ __forceinline__ void reg_cnot(typename P::C (&a)[kRA], const ExecOp& o, uint32_t tb, uint64_t base) {
+    switch (o.q1) {
+        case 0: reg_cnot_j<P, 0>(a, o, tb, base); break;
+        case 1: reg_cnot_j<P, 1>(a, o, tb, base); break;
+        case 2: reg_cnot_j<P, 2>(a, o, tb, base); break;
+        default: reg_cnot_j<P, 3>(a, o, tb, base); break;
+    }
+}
+
+// diag(d0, d1) (EX_DIAG) or diag(1, ph) (EX_PHASE1) on a register slot, a thread-index position or
+// a global qubit
+template <class P>
+__device__ __forceinline__ void reg_diag(typename P::C (&a)[kRA], const ExecOp& o, uint32_t tb, uint64_t base) {
+    using K = typename P::K;
+    const bool ph1 = o.kind == EX_PHASE1;
+    const K d1r = P::k_from_bits(ph1 ? o.c[0] : o.c[2]), d1i = P::k_from_bits(ph1 ? o.c[1] : o.c[3]);
+    const K d0r = ph1 ? P::k_from_bits(0) : P::k_from_bits(o.c[0]), d0i = ph1 ? P::k_from_bits(0) : P::k_from_bits(o.c[1]);
+    const K md1i = P::kneg(d1i), md0i = P::kneg(d0i);
+    if (o.flags & OPF_SLOT_Q0) {
+        const int j = o.q0;
+#pragma unroll
+        for (int e = 0; e < kRA; ++e) {
+            if ((e >> j) & 1) cmul_const<P>(a[e], d1r, d1i, md1i);
+            else if (!ph1) cmul_const<P>(a[e], d0r, d0i, md0i);
+        }
+        return;
+    }
+    const bool one = (o.flags & OPF_NONLOCAL_Q0) ? ((base >> o.q0) & 1) : ((tb >> o.q0) & 1);
+    if (ph1 && !one) return;
+    const K dr = one ? d1r : d0r, di = one ? d1i : d0i, mdi = one ? md1i : md0i;
+#pragma unroll
+    for (int e = 0; e < kRA; ++e) cmul_const<P>(a[e], dr, di, mdi);
+}
+
+// negate the amplitudes with every bit of the local mask set (and every global bit of nl_mask)
+template <class P>
+__device__ __forceinline__ void reg_mcz(typename P::C (&a)[kRA], const ExecOp& o, uint32_t tb, const uint32_t rb[4],
+                                        uint64_t base) {
+    if ((base & o.nl_mask) != o.nl_mask) return;
+    const uint32_t lm = (uint32_t)o.mask;
+#pragma unroll
+    for (int e = 0; e < kRA; ++e)
+        if (((tb | reg_off(rb, e)) & lm) == lm) {
+            a[e].re = P::neg(a[e].re);
+            a[e].im = P::neg(a[e].im);
+        }
+}
+
+// thread-index bits of this thread in a layout: bit k of threadIdx.x at position (tm >> 4k) & 15
+__device__ __forceinline__ uint32_t thread_bits(uint64_t tm, int nthr) {
+    uint32_t tb = 0;
+    for (int k = 0; k < nthr; ++k)
+        if ((threadIdx.x >> k) & 1) tb |= 1u << ((tm >> (4 * k)) & 15);
+    return tb;
+}
+
+template <class P>
+__global__ void __launch_bounds__(512, 1) k_tile_reg(typename P::S* __restrict__ psi, PassDesc pd,
+                                                    const ExecOp* __restrict__ ops, double2* __restrict__ mirror) {
+    using S = typename P::S;
+    using C = typename P::C;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int t = pd.t, low = pd.low;
+    const uint32_t tsize = 1u << t, nhi = 1u << (t - low);
+    S* sm = reinterpret_cast<S*>(smem_raw);
+    uint64_t* hi_off = reinterpret_cast<uint64_t*>(smem_raw + (size_t)tsize * sizeof(S));
+    __shared__ __align__(16) ExecOp sops[kROpChunk];
+
+    const uint64_t base = insert0_mask((uint64_t)blockIdx.x, pd.local_mask);
+    for (uint32_t h = threadIdx.x; h < nhi; h += blockDim.x) {
+        uint64_t off = 0;
+        for (int j = 0; j < t - low; ++j)
+            if ((h >> j) & 1) off |= 1ULL << pd.hi_pos[j];
+        hi_off[h] = off;
+    }
+    __syncthreads();
+    const uint32_t lowmask = (1u << low) - 1;
+    // base layout: register positions t-4 .. t-1, thread-index bits on positions 0 .. t-5 in order
+    uint32_t rb[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) rb[j] = 1u << (t - 4 + j);
+    uint32_t tb = threadIdx.x;
+    C a[kRA];
+#pragma unroll
+    for (int e = 0; e < kRA; ++e) {
+        const uint32_t l = tb | reg_off(rb, e);
+        a[e] = P::load(psi[base | hi_off[l >> low] | (l & lowmask)]);
+    }
+
+    constexpr int kWords = (int)(sizeof(ExecOp) / 16);
+    for (int k = 0; k < pd.nops; ++k) {
+        if (k % kROpChunk == 0) {
+            const int cnt = min(kROpChunk, pd.nops - k);
+            __syncthreads();  // every thread is done with the previous chunk
+            const uint4* src = reinterpret_cast<const uint4*>(ops + pd.op_begin + k);
+            for (int w = threadIdx.x; w < cnt * kWords; w += blockDim.x) reinterpret_cast<uint4*>(sops)[w] = src[w];
+            __syncthreads();
+        }
+        const ExecOp& o = sops[k % kROpChunk];
+        switch (o.kind) {
+            case EX_U2: reg_pairs<P, EX_U2>(a, o); break;
+            case EX_ZYZ: reg_pairs<P, EX_ZYZ>(a, o); break;
+            case EX_ZY: reg_pairs<P, EX_ZY>(a, o); break;
+            case EX_ZT: reg_pairs<P, EX_ZT>(a, o); break;
+            case EX_ZC: reg_pairs<P, EX_ZC>(a, o); break;
+            case EX_RT: reg_pairs<P, EX_RT>(a, o); break;
+            case EX_RC: reg_pairs<P, EX_RC>(a, o); break;
+            case EX_RX: reg_pairs<P, EX_RX>(a, o); break;
+            case EX_RY: reg_pairs<P, EX_RY>(a, o); break;
+            case EX_H: reg_pairs<P, EX_H>(a, o); break;
+            case EX_X: reg_pairs<P, EX_X>(a, o); break;
+            case EX_CNOT: reg_cnot<P>(a, o, tb, base); break;
+            case EX_DIAG:
+            case EX_PHASE1: reg_diag<P>(a, o, tb, base); break;
+            case EX_MCZ: reg_mcz<P>(a, o, tb, rb, base); break;
+            case EX_LAYOUT: {
+                __syncthreads();  // the previous layout's reads of sm are done
+#pragma unroll
+                for (int e = 0; e < kRA; ++e) sm[swz(tb | reg_off(rb, e))] = P::store(a[e]);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) rb[j] = 1u << ((o.mask >> (4 * j)) & 15);
+                tb = thread_bits(o.nl_mask, o.q0);
+                __syncthreads();
+#pragma unroll
+                for (int e = 0; e < kRA; ++e) a[e] = P::load(sm[swz(tb | reg_off(rb, e))]);
+                break;
+            }
+            default: break;
+        }
+    }
+    // the program ends in the base layout: store from registers (and, for the last pass before a
+    // readback, the FP64 copy into the mapped host buffer)
+#pragma unroll
+    for (int e = 0; e < kRA; ++e) {
+        const uint32_t l = tb | reg_off(rb, e);
+        const uint64_t g = base | hi_off[l >> low] | (l & lowmask);
+        psi[g] = P::store(a[e]);
+        if (mirror) mirror[g] = P::to_f64(a[e]);
+    }
+}
+
+template <class P>
+cudaError_t tile_reg_t(void* vpsi, int n, const PassDesc& pd, const ExecOp* d_ops, double* mirror, cudaStream_t s) {
+    using S = typename P::S;
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_tile_reg<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(((size_t)1 << 13) * sizeof(S) + ((size_t)1 << 9) * sizeof(uint64_t)));
+    if (attr != cudaSuccess) return attr;
+    if (pd.t < 9 || pd.t > 13) return cudaErrorInvalidValue;
+    const size_t smem = ((size_t)1 << pd.t) * sizeof(S) + ((size_t)1 << (pd.t - pd.low)) * sizeof(uint64_t);
+    const unsigned threads = 1u << (pd.t - 4);
+    const uint64_t ntiles = 1ULL << (n - pd.t);
+    k_tile_reg<P><<<(unsigned)ntiles, threads, smem, s>>>(static_cast<S*>(vpsi), pd, d_ops, reinterpret_cast<double2*>(mirror));
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_tile_reg(int P, void* psi, int n, const PassDesc& pd, const ExecOp* d_ops, cudaStream_t s,
+                            double* mirror) {
+    switch (P) {
+        case LLG_F32: return tile_reg_t<PolF32>(psi, n, pd, d_ops, mirror, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace llg

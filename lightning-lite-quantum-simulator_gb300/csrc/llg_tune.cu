@@ -129,6 +129,8 @@ int llg_autotune(llg_state* st, const llg_op* ops, int nops, int sample_ops, llg
         for (int t = std::max(5, std::min(8, tmax)); t <= tmax; ++t)
             for (int th : {256, 512, 1024})
                 if (th == 256 || (th == 512 && t >= 10) || (th == 1024 && small && t >= 11)) cands.push_back({LLG_FUSE_TILE, t, th});
+        if (P == LLG_F32)  // register-tiled passes (2^(t-4) threads per CTA)
+            for (int t = 9; t <= std::min(n, 13); ++t) cands.push_back({LLG_FUSE_REG, t, 0});
         llg_state* tmp = nullptr;
         int rc = llg_create(n, P, &tmp);
         if (rc) return set_error(rc, "autotune: cannot create the scratch state (a second state of the same size)");

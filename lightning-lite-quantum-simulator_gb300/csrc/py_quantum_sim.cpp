@@ -177,8 +177,9 @@ public:
     void set_fusion(const std::string& mode, int tile_qubits) {
         int m;
         if (mode == "tile") m = LLG_FUSE_TILE;
+        else if (mode == "reg") m = LLG_FUSE_REG;
         else if (mode == "none") m = LLG_FUSE_NONE;
-        else throw py::value_error("fusion mode must be 'tile' or 'none'");
+        else throw py::value_error("fusion mode must be 'tile', 'reg' or 'none'");
         check(llg_set_fusion(st_, m, tile_qubits));
     }
 
@@ -190,7 +191,7 @@ public:
         llg_tune_result r;
         check(llg_autotune(st_, static_cast<const llg_op*>(ops.data()), n, sample_ops, &r));
         py::dict d;
-        d["fuse_mode"] = r.fuse_mode == LLG_FUSE_TILE ? "tile" : "none";
+        d["fuse_mode"] = r.fuse_mode == LLG_FUSE_TILE ? "tile" : (r.fuse_mode == LLG_FUSE_REG ? "reg" : "none");
         d["tile_qubits"] = r.tile_qubits;
         d["cta_threads"] = r.cta_threads;
         d["candidates"] = r.candidates;

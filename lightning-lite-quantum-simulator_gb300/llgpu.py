@@ -21,7 +21,9 @@ LIB_PATH = os.path.join(HERE, "libllgpu.so")
 # status codes / enums (include/llgpu.h)
 LLG_OK, LLG_EINVAL, LLG_ERUNTIME, LLG_ENOMEM, LLG_ECUDA, LLG_ETIMEOUT = range(6)
 LLG_F64, LLG_DF64, LLG_F32 = 0, 1, 2
-LLG_FUSE_NONE, LLG_FUSE_TILE = 0, 1
+LLG_FUSE_NONE, LLG_FUSE_TILE, LLG_FUSE_REG = 0, 1, 2
+FUSE_MODES = {"none": LLG_FUSE_NONE, "tile": LLG_FUSE_TILE, "reg": LLG_FUSE_REG}
+FUSE_NAMES = {v: k for k, v in FUSE_MODES.items()}
 OP_H, OP_X, OP_RX, OP_RY, OP_RZ, OP_CNOT, OP_MCZ, OP_CZ, OP_U2 = range(9)
 
 PROF_CLASSES = 4
@@ -273,7 +275,11 @@ class State:
         return v.value
 
     def set_fusion(self, mode: str = "tile", tile_qubits: int = 0) -> None:
-        check(lib().llg_set_fusion(self._h, LLG_FUSE_TILE if mode == "tile" else LLG_FUSE_NONE, tile_qubits))
+        """mode: "tile" (shared-memory tile passes), "reg" (register-tiled passes, complex64) or
+        "none" (one streaming kernel per gate)."""
+        if mode not in FUSE_MODES:
+            raise ValueError("fusion mode must be 'tile', 'reg' or 'none'")
+        check(lib().llg_set_fusion(self._h, FUSE_MODES[mode], tile_qubits))
 
     def set_tile_threads(self, threads: int) -> None:
         check(lib().llg_set_tile_threads(self._h, threads))
@@ -281,8 +287,7 @@ class State:
     def tuning(self) -> dict:
         m, t, th = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         check(lib().llg_get_tuning(self._h, ctypes.byref(m), ctypes.byref(t), ctypes.byref(th)))
-        return {"fuse_mode": "tile" if m.value == LLG_FUSE_TILE else "none", "tile_qubits": t.value,
-                "cta_threads": th.value}
+        return {"fuse_mode": FUSE_NAMES.get(m.value, "none"), "tile_qubits": t.value, "cta_threads": th.value}
 
     def autotune(self, ops: np.ndarray, sample_ops: int = 0) -> dict:
         """Time candidate (fusion mode, tile width, CTA threads) settings on a scratch state with
@@ -411,15 +416,17 @@ class State:
 # ---------------------------------------------------------------------------------------------
 PLAN_ZYZ = 1
 PLAN_TABLES = 2
+PLAN_REGS = 4
 
 
-def plan_export(n: int, ops: np.ndarray, tile_qubits: int, zyz: bool = False, tables: bool = False):
+def plan_export(n: int, ops: np.ndarray, tile_qubits: int, zyz: bool = False, tables: bool = False,
+                regs: bool = False):
     """Host-side plan of `ops` (passes, executor ops; coefficients as doubles).  zyz=True plans
     as the engine does for complex128 states (fused unitary 2x2s as carried-phase rotations);
     tables=True (with zyz) also gathers diagonal factors into phase tables, and the result gains a
     third item: the tables as a complex array (2^tile_qubits entries per table)."""
     ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
-    flags = (PLAN_ZYZ if zyz else 0) | (PLAN_TABLES if tables else 0)
+    flags = (PLAN_ZYZ if zyz else 0) | (PLAN_TABLES if tables else 0) | (PLAN_REGS if regs else 0)
     npasses, nx = ctypes.c_int(), ctypes.c_int()
     check(lib().llg_plan_export_ex(n, _ptr(ops) if ops.size else None, ops.size, tile_qubits, flags, None, 0,
                                    ctypes.byref(npasses), None, 0, ctypes.byref(nx)))

@@ -43,6 +43,37 @@ def _pair(tile: np.ndarray, q: int, m: np.ndarray) -> None:
     v[:, :, 1, :] = m[1, 0] * a0 + m[1, 1] * a1
 
 
+def unregister(passes: np.ndarray, xops: np.ndarray) -> np.ndarray:
+    """A register program (kind 19 layout ops, register slots in the op records) turned back into
+    the tile program it encodes: slots replaced by the layout's local positions, layout ops kept
+    as no-ops (kind -1).  Also checks the layouts: four distinct register positions, and thread
+    positions covering the rest of the tile."""
+    out = xops.copy()
+    for p in passes:
+        t = int(p["t"])
+        regs = list(range(t - 4, t))
+        for i in range(int(p["op_begin"]), int(p["op_begin"]) + int(p["nops"])):
+            x = out[i]
+            k = int(x["kind"])
+            if k == 19:
+                regs = [(int(x["mask"]) >> (4 * j)) & 15 for j in range(4)]
+                thr = [(int(x["nl_mask"]) >> (4 * j)) & 15 for j in range(int(x["q0"]))]
+                assert int(x["q0"]) == t - 4 and sorted(regs + thr) == list(range(t)), (regs, thr)
+                out[i]["kind"] = -1
+            elif k == 6:
+                out[i]["q1"] = regs[int(x["q1"])]
+                if int(x["flags"]) & 16:
+                    out[i]["q0"] = regs[int(x["q0"])]
+            elif k in (5, 13):
+                if int(x["flags"]) & 16:
+                    out[i]["q0"] = regs[int(x["q0"])]
+            elif k != 7:
+                assert 0 <= int(x["q0"]) < 4
+                out[i]["q0"] = regs[int(x["q0"])]
+        assert regs == list(range(t - 4, t))  # every pass ends in the base layout
+    return out
+
+
 def execute(psi: np.ndarray, n: int, passes: np.ndarray, xops: np.ndarray, tables: np.ndarray | None = None) -> np.ndarray:
     psi = psi.copy()
     for p in passes:
@@ -62,6 +93,8 @@ def execute(psi: np.ndarray, n: int, passes: np.ndarray, xops: np.ndarray, table
         lidx = np.arange(1 << t)
         for x in xops[p["op_begin"]:p["op_begin"] + p["nops"]]:
             k, q0, q1, fl = int(x["kind"]), int(x["q0"]), int(x["q1"]), int(x["flags"])
+            if k == -1:
+                continue
             if k <= 4 or k in (11, 12, 14, 15, 16, 17):
                 _pair(tile, q0, _matrix(x))
             elif k == 18:  # phase table: tile amplitude l times entry l

@@ -430,3 +430,43 @@ def test_apply_fused_gate_list():
         sv = quantum_sim_v3.StateVector(n, precision)
         sv.apply_fused(fused)
         assert np.max(np.abs(sv.get_numpy_view() - want)) <= 1e-12, precision
+
+
+@pytest.mark.parametrize("tile", [9, 11, 13])
+def test_register_tiled_passes(golden, tile):
+    # complex64 register-tiled passes (16 amplitudes per thread, shared memory only between
+    # layouts) against the oracle: every gate kind, non-local CNOT controls and MCZ masks, the
+    # layered recipe, and the readback fused into the last pass
+    import quantum_sim_v3
+
+    rng = np.random.default_rng(70 + tile)
+    n = 15
+    recs = []
+    for _ in range(300):
+        k = rng.integers(9)
+        q = int(rng.integers(n))
+        if k == 0:
+            recs.append((OP_H, q))
+        elif k == 1:
+            recs.append((OP_X, q))
+        elif k < 5:
+            recs.append(((OP_RX, OP_RY, OP_RZ)[k - 2], q, 0, float(rng.uniform(0, 2 * np.pi))))
+        elif k < 7:
+            a, b = rng.choice(n, 2, replace=False)
+            recs.append(((OP_CNOT, OP_CZ)[k - 5], int(a), int(b)))
+        elif k == 7:
+            recs.append((OP_MCZ, 0, 0, 0.0, int(rng.integers(1, 1 << n))))
+        else:
+            u, _ = np.linalg.qr(rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2)))
+            recs.append((OP_U2, q, 0, 0.0, None, u.reshape(4)))
+    for ops in (make_ops(recs), workloads.layered_rotations(n, layers=6, seed=tile)):
+        want = oracle.run_ops(n, ops)
+        got = run_gpu(n, ops, "complex64", "reg", tile)
+        assert np.max(np.abs(got - want)) <= 5e-5
+        sv = quantum_sim_v3.StateVector(n, "complex64")
+        sv.set_fusion("reg", tile)
+        sv.apply_ops(ops)
+        view = sv.get_numpy_view().copy()  # gates queued: the last pass also writes the host mirror
+        assert np.max(np.abs(view - want)) <= 5e-5
+    with pytest.raises(ValueError):
+        llgpu.State(12, "df64").set_fusion("reg", 12)
