@@ -1,0 +1,117 @@
+"""Small workloads, one kernel family each, for ncu captures (the commands that made the summaries
+under profiles/ name this script).  Each case runs its kernel a few times on a state larger than
+the 129 MB L2 but of a few GB at most, so a capture of one to three launches ends in seconds.
+
+    python profile_cases.py <case> [<case> ...]       cases: see CASES
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+import numpy as np  # noqa: E402
+
+import llgpu  # noqa: E402
+import workloads  # noqa: E402
+
+
+def tile_f64():
+    """IEEE complex128 tile passes with phase tables: the 30-qubit recipe's circuit at 26 qubits
+    (1 GiB), 11-qubit tiles and 256 threads (the tuner's choice at 30 qubits)."""
+    n = 26
+    st = llgpu.State(n, "complex128")
+    st.set_fusion("tile", 11)
+    st.set_tile_threads(256)
+    st.apply_ops(workloads.layered_rotations(n, 4))
+    st.sync()
+    st.close()
+
+
+def tile_reg_c64():
+    """complex64 register-tiled passes, 27 qubits (1 GiB), 13-qubit tiles."""
+    n = 27
+    st = llgpu.State(n, "complex64")
+    st.set_fusion("reg", 13)
+    st.apply_ops(workloads.layered_rotations(n, 4))
+    st.sync()
+    st.close()
+
+
+def tile_c64():
+    """complex64 shared-memory tile passes, 27 qubits, 13-qubit tiles (the register kernel's baseline)."""
+    n = 27
+    st = llgpu.State(n, "complex64")
+    st.set_fusion("tile", 13)
+    st.apply_ops(workloads.layered_rotations(n, 4))
+    st.sync()
+    st.close()
+
+
+def streaming():
+    """Per-gate streaming kernels on a 27-qubit complex128 state (2 GiB): CNOT (control 3, target
+    20), CZ / MCZ (3, 20), RY on qubit 13."""
+    n = 27
+    st = llgpu.State(n, "complex128")
+    st.set_fusion("none")
+    st.apply_ops(llgpu.make_ops([(llgpu.OP_CNOT, 3, 20)] * 3 + [(llgpu.OP_CZ, 3, 20)] * 3 +
+                                [(llgpu.OP_RY, 13, 0, 0.4)] * 3))
+    st.sync()
+    st.close()
+
+
+def reductions():
+    """Observable reductions on a 27-qubit complex128 state: the class-counting kernel (ring ZZ,
+    27 terms) and the chunked kernel (all-to-all couplings, 351 terms + 27 fields)."""
+    n = 27
+    st = llgpu.State(n, "complex128")
+    st.apply_ops(workloads.layered_rotations(n, 1))
+    a, b, c = llgpu.ring_zz_terms(n)
+    rng = np.random.default_rng(3)
+    zz = [(i, j, float(rng.normal())) for i in range(n) for j in range(i + 1, n)]
+    z = [(i, float(rng.normal())) for i in range(n)]
+    sa, sb, sc = llgpu.ising_terms(n, zz, z)
+    for _ in range(3):
+        st.expect_zz(a, b, c)
+        st.expect_zz(sa, sb, sc)
+    st.close()
+
+
+def readback():
+    """The host readback of a 26-qubit complex128 state into pinned memory (the conversion /
+    copy kernel writing the mapped host buffer)."""
+    import quantum_sim_v3
+
+    n = 26
+    sv = quantum_sim_v3.StateVector(n)
+    sv.h(0)
+    for _ in range(3):
+        sv.get_numpy_view()
+        sv.h(1)
+        sv.flush()
+
+
+def tsolve():
+    """The dense trajectory solver at dim 1024 (10 qubits), 256 trajectories of 20 steps."""
+    rng = np.random.default_rng(11)
+    d = 1024
+    a = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    h = (a + a.conj().T) / (4 * np.sqrt(d))
+    s = llgpu.TrajectorySolver(10)
+    s.set_hamiltonian(h)
+    sm = np.array([[0, 1], [0, 0]], dtype=complex)
+    s.add_lindblad(np.kron(np.eye(d // 2), sm), 0.4)
+    psi0 = rng.normal(size=d) + 1j * rng.normal(size=d)
+    s.states(psi0, 0.4, 0.02, 256, "PROJECTOR", seed=5)
+    s.close()
+
+
+CASES = {"tile_f64": tile_f64, "tile_reg_c64": tile_reg_c64, "tile_c64": tile_c64, "streaming": streaming,
+         "reductions": reductions, "readback": readback, "tsolve": tsolve}
+
+if __name__ == "__main__":
+    for name in sys.argv[1:]:
+        CASES[name]()
+    print("profile cases done:", " ".join(sys.argv[1:]))
