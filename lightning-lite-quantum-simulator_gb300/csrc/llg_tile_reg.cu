@@ -57,37 +57,56 @@ __device__ __forceinline__ void reg_pairs(typename P::C (&a)[kRA], const ExecOp&
     }
 }
 
-// CNOT with target slot J: the control is a register slot (OPF_SLOT_Q0), a thread-index position
-// or a global qubit outside the tile; with OPF_PHASE the amplitudes that end at control = target
-// = 1 are multiplied by c[0] + i c[1]
-template <class P, int J>
-__device__ __forceinline__ void reg_cnot_j(typename P::C (&a)[kRA], const ExecOp& o, uint32_t tb, uint64_t base) {
-    using K = typename P::K;
+// CNOT with target slot J and control slot K, both in registers: the swaps are register renames
+// fixed at compile time; with OPF_PHASE the amplitudes that end at control = target = 1 are
+// multiplied by c[0] + i c[1]
+template <class P, int J, int K>
+__device__ __forceinline__ void reg_cnot_jk(typename P::C (&a)[kRA], const ExecOp& o) {
+    using Kt = typename P::K;
     using C = typename P::C;
     const bool phased = (o.flags & OPF_PHASE) != 0;
-    const K pr = P::k_from_bits(o.c[0]), pi = P::k_from_bits(o.c[1]), mpi = P::kneg(pi);
-    if (o.flags & OPF_SLOT_Q0) {
-        const int k = o.q0;
+    const Kt pr = P::k_from_bits(o.c[0]), pi = P::k_from_bits(o.c[1]), mpi = P::kneg(pi);
 #pragma unroll
-        for (int e = 0; e < kRA; ++e)
-            if (!(e & (1 << J)) && ((e >> k) & 1)) {
-                C x = a[e];
-                a[e] = a[e | (1 << J)];
-                if (phased) cmul_const<P>(x, pr, pi, mpi);
-                a[e | (1 << J)] = x;
-            }
-        return;
-    }
-    const bool on = (o.flags & OPF_NONLOCAL_Q0) ? ((base >> o.q0) & 1) : ((tb >> o.q0) & 1);
-    if (!on) return;
+    for (int e = 0; e < kRA; ++e)
+        if (!(e & (1 << J)) && (e & (1 << K))) {
+            const C x = a[e];
+            a[e] = a[e | (1 << J)];
+            a[e | (1 << J)] = x;
+            if (phased) cmul_const<P>(a[e | (1 << J)], pr, pi, mpi);
+        }
+}
+
+// CNOT with target slot J whose control is uniform for this thread (a thread-index position) or
+// for the tile (a global qubit): all of the thread's pairs on J, or none
+template <class P, int J>
+__device__ __forceinline__ void reg_cnot_uniform(typename P::C (&a)[kRA], const ExecOp& o) {
+    using Kt = typename P::K;
+    using C = typename P::C;
+    const bool phased = (o.flags & OPF_PHASE) != 0;
+    const Kt pr = P::k_from_bits(o.c[0]), pi = P::k_from_bits(o.c[1]), mpi = P::kneg(pi);
 #pragma unroll
     for (int e = 0; e < kRA; ++e)
         if (!(e & (1 << J))) {
-            C x = a[e];
+            const C x = a[e];
             a[e] = a[e | (1 << J)];
-            if (phased) cmul_const<P>(x, pr, pi, mpi);
             a[e | (1 << J)] = x;
+            if (phased) cmul_const<P>(a[e | (1 << J)], pr, pi, mpi);
         }
+}
+
+template <class P, int J>
+__device__ __forceinline__ void reg_cnot_j(typename P::C (&a)[kRA], const ExecOp& o, uint32_t tb, uint64_t base) {
+    if (o.flags & OPF_SLOT_Q0) {
+        switch (o.q0) {
+            case 0: if (J != 0) reg_cnot_jk<P, J, (J == 0 ? 1 : 0)>(a, o); break;
+            case 1: if (J != 1) reg_cnot_jk<P, J, (J == 1 ? 0 : 1)>(a, o); break;
+            case 2: if (J != 2) reg_cnot_jk<P, J, (J == 2 ? 0 : 2)>(a, o); break;
+            default: if (J != 3) reg_cnot_jk<P, J, (J == 3 ? 0 : 3)>(a, o); break;
+        }
+        return;
+    }
+    const bool on = (o.flags & OPF_NONLOCAL_Q0) ? ((base >> o.q0) & 1) : ((tb >> o.q0) & 1);
+    if (on) reg_cnot_uniform<P, J>(a, o);
 }
 
 template <class P>
@@ -100,27 +119,42 @@ __device__ __forceinline__ void reg_cnot(typename P::C (&a)[kRA], const ExecOp& 
     }
 }
 
-// diag(d0, d1) (EX_DIAG) or diag(1, ph) (EX_PHASE1) on a register slot, a thread-index position or
-// a global qubit
+// diag(d0, d1) (EX_DIAG) or diag(1, ph) (EX_PHASE1) on register slot J
+template <class P, int J>
+__device__ __forceinline__ void reg_diag_j(typename P::C (&a)[kRA], const ExecOp& o) {
+    using K = typename P::K;
+    const bool ph1 = o.kind == EX_PHASE1;
+    const K d1r = P::k_from_bits(ph1 ? o.c[0] : o.c[2]), d1i = P::k_from_bits(ph1 ? o.c[1] : o.c[3]), md1i = P::kneg(d1i);
+#pragma unroll
+    for (int e = 0; e < kRA; ++e)
+        if (e & (1 << J)) cmul_const<P>(a[e], d1r, d1i, md1i);
+    if (!ph1) {
+        const K d0r = P::k_from_bits(o.c[0]), d0i = P::k_from_bits(o.c[1]), md0i = P::kneg(d0i);
+#pragma unroll
+        for (int e = 0; e < kRA; ++e)
+            if (!(e & (1 << J))) cmul_const<P>(a[e], d0r, d0i, md0i);
+    }
+}
+
+// the same on a register slot, a thread-index position or a global qubit (the last two: one
+// factor for all the thread's amplitudes)
 template <class P>
 __device__ __forceinline__ void reg_diag(typename P::C (&a)[kRA], const ExecOp& o, uint32_t tb, uint64_t base) {
     using K = typename P::K;
-    const bool ph1 = o.kind == EX_PHASE1;
-    const K d1r = P::k_from_bits(ph1 ? o.c[0] : o.c[2]), d1i = P::k_from_bits(ph1 ? o.c[1] : o.c[3]);
-    const K d0r = ph1 ? P::k_from_bits(0) : P::k_from_bits(o.c[0]), d0i = ph1 ? P::k_from_bits(0) : P::k_from_bits(o.c[1]);
-    const K md1i = P::kneg(d1i), md0i = P::kneg(d0i);
     if (o.flags & OPF_SLOT_Q0) {
-        const int j = o.q0;
-#pragma unroll
-        for (int e = 0; e < kRA; ++e) {
-            if ((e >> j) & 1) cmul_const<P>(a[e], d1r, d1i, md1i);
-            else if (!ph1) cmul_const<P>(a[e], d0r, d0i, md0i);
+        switch (o.q0) {
+            case 0: reg_diag_j<P, 0>(a, o); break;
+            case 1: reg_diag_j<P, 1>(a, o); break;
+            case 2: reg_diag_j<P, 2>(a, o); break;
+            default: reg_diag_j<P, 3>(a, o); break;
         }
         return;
     }
+    const bool ph1 = o.kind == EX_PHASE1;
     const bool one = (o.flags & OPF_NONLOCAL_Q0) ? ((base >> o.q0) & 1) : ((tb >> o.q0) & 1);
     if (ph1 && !one) return;
-    const K dr = one ? d1r : d0r, di = one ? d1i : d0i, mdi = one ? md1i : md0i;
+    const int s = (one && !ph1) ? 2 : 0;  // EX_DIAG: d1 in c[2..3]; EX_PHASE1: the phase in c[0..1]
+    const K dr = P::k_from_bits(o.c[s]), di = P::k_from_bits(o.c[s + 1]), mdi = P::kneg(di);
 #pragma unroll
     for (int e = 0; e < kRA; ++e) cmul_const<P>(a[e], dr, di, mdi);
 }
@@ -207,15 +241,28 @@ __global__ void __launch_bounds__(512, 1) k_tile_reg(typename P::S* __restrict__
             case EX_PHASE1: reg_diag<P>(a, o, tb, base); break;
             case EX_MCZ: reg_mcz<P>(a, o, tb, rb, base); break;
             case EX_LAYOUT: {
+                // the swizzle is linear over the index bits (XOR), and tb and the register offsets
+                // occupy disjoint bits: slot(tb | off) = slot(tb) ^ slot(off), with slot(off) the XOR
+                // of the register positions' slots selected by e
                 __syncthreads();  // the previous layout's reads of sm are done
+                {
+                    const uint32_t st = swz(tb), s0 = swz(rb[0]), s1 = swz(rb[1]), s2 = swz(rb[2]), s3 = swz(rb[3]);
 #pragma unroll
-                for (int e = 0; e < kRA; ++e) sm[swz(tb | reg_off(rb, e))] = P::store(a[e]);
+                    for (int e = 0; e < kRA; ++e)
+                        sm[st ^ ((e & 1) ? s0 : 0u) ^ ((e & 2) ? s1 : 0u) ^ ((e & 4) ? s2 : 0u) ^ ((e & 8) ? s3 : 0u)] =
+                            P::store(a[e]);
+                }
 #pragma unroll
                 for (int j = 0; j < 4; ++j) rb[j] = 1u << ((o.mask >> (4 * j)) & 15);
                 tb = thread_bits(o.nl_mask, o.q0);
                 __syncthreads();
+                {
+                    const uint32_t st = swz(tb), s0 = swz(rb[0]), s1 = swz(rb[1]), s2 = swz(rb[2]), s3 = swz(rb[3]);
 #pragma unroll
-                for (int e = 0; e < kRA; ++e) a[e] = P::load(sm[swz(tb | reg_off(rb, e))]);
+                    for (int e = 0; e < kRA; ++e)
+                        a[e] = P::load(sm[st ^ ((e & 1) ? s0 : 0u) ^ ((e & 2) ? s1 : 0u) ^ ((e & 4) ? s2 : 0u) ^
+                                          ((e & 8) ? s3 : 0u)]);
+                }
                 break;
             }
             default: break;
