@@ -129,6 +129,21 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int precisi
 // positions are the top four tile positions.  Returns the number of layout changes.
 int to_register_program(Plan& plan);
 
+// Dense dispatch codes of register-program ops, in flags >> kRegCodeShift: one jump table in the
+// kernel selects the kind and its register slots together.
+constexpr int kRegCodeShift = 8;
+enum RegCode : int32_t {
+    RC_PAIR = 1,           // + 4 * (index of the kind in U2, ZYZ, ZY, ZT, ZC, RT, RC, RX, RY, H, X) + slot
+    RC_CNOT_SLOT = 45,     // + 4 * target slot + control slot
+    RC_CNOT_UNIFORM = 61,  // + target slot (control a thread-index position or a global qubit)
+    RC_DIAG_SLOT = 65,     // + slot
+    RC_PHASE_SLOT = 69,    // + slot
+    RC_DIAG_UNIFORM = 73,  // EX_DIAG / EX_PHASE1 on a thread-index position or a global qubit
+    RC_MCZ = 74,
+    RC_LAYOUT = 75,
+};
+int32_t reg_dispatch_code(const ExecOp& x);
+
 // Lower one gate record to executor ops with GLOBAL qubit indices (streaming path).
 bool lower_op(int n, const llg_op& op, int precision, std::vector<ExecOp>& out, std::string& err);
 

@@ -458,6 +458,28 @@ int reg_need(const ExecOp& e) {
     }
 }
 
+}  // namespace
+
+// The register kernel's dense dispatch code of an encoded op (RegCode in llg_internal.h).
+int32_t reg_dispatch_code(const ExecOp& x) {
+    static const int kinds[] = {EX_U2, EX_ZYZ, EX_ZY, EX_ZT, EX_ZC, EX_RT, EX_RC, EX_RX, EX_RY, EX_H, EX_X};
+    switch (x.kind) {
+        case EX_CNOT:
+            if (x.flags & OPF_SLOT_Q0) return RC_CNOT_SLOT + 4 * x.q1 + x.q0;
+            return RC_CNOT_UNIFORM + x.q1;
+        case EX_DIAG: return (x.flags & OPF_SLOT_Q0) ? RC_DIAG_SLOT + x.q0 : RC_DIAG_UNIFORM;
+        case EX_PHASE1: return (x.flags & OPF_SLOT_Q0) ? RC_PHASE_SLOT + x.q0 : RC_DIAG_UNIFORM;
+        case EX_MCZ: return RC_MCZ;
+        case EX_LAYOUT: return RC_LAYOUT;
+        default:
+            for (int k = 0; k < (int)(sizeof(kinds) / sizeof(kinds[0])); ++k)
+                if (kinds[k] == x.kind) return RC_PAIR + 4 * k + x.q0;
+            return 0;
+    }
+}
+
+namespace {
+
 ExecOp layout_op(int t, const int regs[4]) {
     ExecOp e = blank(EX_LAYOUT);
     uint64_t rm = 0;
@@ -483,6 +505,7 @@ ExecOp layout_op(int t, const int regs[4]) {
     e.mask = rm;
     e.nl_mask = tm;
     e.q0 = t - 4;
+    e.flags = RC_LAYOUT << kRegCodeShift;
     return e;
 }
 
@@ -545,6 +568,7 @@ int to_register_program(Plan& out) {
                 case EX_MCZ: break;
                 default: x.q0 = slot_of(x.q0); break;
             }
+            x.flags |= reg_dispatch_code(x) << kRegCodeShift;
             ops.push_back(x);
             src.push_back(out.source_index[b + i]);
         }

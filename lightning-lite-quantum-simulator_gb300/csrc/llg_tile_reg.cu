@@ -224,23 +224,47 @@ __global__ void __launch_bounds__(512, 1) k_tile_reg(typename P::S* __restrict__
             __syncthreads();
         }
         const ExecOp& o = sops[k % kROpChunk];
-        switch (o.kind) {
-            case EX_U2: reg_pairs<P, EX_U2>(a, o); break;
-            case EX_ZYZ: reg_pairs<P, EX_ZYZ>(a, o); break;
-            case EX_ZY: reg_pairs<P, EX_ZY>(a, o); break;
-            case EX_ZT: reg_pairs<P, EX_ZT>(a, o); break;
-            case EX_ZC: reg_pairs<P, EX_ZC>(a, o); break;
-            case EX_RT: reg_pairs<P, EX_RT>(a, o); break;
-            case EX_RC: reg_pairs<P, EX_RC>(a, o); break;
-            case EX_RX: reg_pairs<P, EX_RX>(a, o); break;
-            case EX_RY: reg_pairs<P, EX_RY>(a, o); break;
-            case EX_H: reg_pairs<P, EX_H>(a, o); break;
-            case EX_X: reg_pairs<P, EX_X>(a, o); break;
-            case EX_CNOT: reg_cnot<P>(a, o, tb, base); break;
-            case EX_DIAG:
-            case EX_PHASE1: reg_diag<P>(a, o, tb, base); break;
-            case EX_MCZ: reg_mcz<P>(a, o, tb, rb, base); break;
-            case EX_LAYOUT: {
+        // one jump table over (kind, register slots): the planner's dense dispatch code
+#define LLG_RP(KI, KIND)                                                          \
+    case RC_PAIR + 4 * KI + 0: reg_pairs_j<P, 0, KIND>(a, o); break;              \
+    case RC_PAIR + 4 * KI + 1: reg_pairs_j<P, 1, KIND>(a, o); break;              \
+    case RC_PAIR + 4 * KI + 2: reg_pairs_j<P, 2, KIND>(a, o); break;              \
+    case RC_PAIR + 4 * KI + 3: reg_pairs_j<P, 3, KIND>(a, o); break;
+#define LLG_RCN(J, K) \
+    case RC_CNOT_SLOT + 4 * J + K: reg_cnot_jk<P, J, K>(a, o); break;
+        switch (o.flags >> kRegCodeShift) {
+            LLG_RP(0, EX_U2)
+            LLG_RP(1, EX_ZYZ)
+            LLG_RP(2, EX_ZY)
+            LLG_RP(3, EX_ZT)
+            LLG_RP(4, EX_ZC)
+            LLG_RP(5, EX_RT)
+            LLG_RP(6, EX_RC)
+            LLG_RP(7, EX_RX)
+            LLG_RP(8, EX_RY)
+            LLG_RP(9, EX_H)
+            LLG_RP(10, EX_X)
+            LLG_RCN(0, 1) LLG_RCN(0, 2) LLG_RCN(0, 3)
+            LLG_RCN(1, 0) LLG_RCN(1, 2) LLG_RCN(1, 3)
+            LLG_RCN(2, 0) LLG_RCN(2, 1) LLG_RCN(2, 3)
+            LLG_RCN(3, 0) LLG_RCN(3, 1) LLG_RCN(3, 2)
+            case RC_CNOT_UNIFORM + 0:
+            case RC_CNOT_UNIFORM + 1:
+            case RC_CNOT_UNIFORM + 2:
+            case RC_CNOT_UNIFORM + 3: reg_cnot<P>(a, o, tb, base); break;
+            case RC_DIAG_SLOT + 0:
+            case RC_PHASE_SLOT + 0: reg_diag_j<P, 0>(a, o); break;
+            case RC_DIAG_SLOT + 1:
+            case RC_PHASE_SLOT + 1: reg_diag_j<P, 1>(a, o); break;
+            case RC_DIAG_SLOT + 2:
+            case RC_PHASE_SLOT + 2: reg_diag_j<P, 2>(a, o); break;
+            case RC_DIAG_SLOT + 3:
+            case RC_PHASE_SLOT + 3: reg_diag_j<P, 3>(a, o); break;
+            case RC_DIAG_UNIFORM: reg_diag<P>(a, o, tb, base); break;
+            case RC_MCZ: reg_mcz<P>(a, o, tb, rb, base); break;
+#undef LLG_RP
+#undef LLG_RCN
+            case RC_LAYOUT: {
                 // the swizzle is linear over the index bits (XOR), and tb and the register offsets
                 // occupy disjoint bits: slot(tb | off) = slot(tb) ^ slot(off), with slot(off) the XOR
                 // of the register positions' slots selected by e
