@@ -32,6 +32,9 @@ def test_state_autotune_then_parity(precision):
     if res["fuse_mode"] == llgpu.LLG_FUSE_TILE:
         assert tun["fuse_mode"] == "tile" and tun["tile_qubits"] == res["tile_qubits"]
         assert tun["cta_threads"] == res["cta_threads"]
+    elif res["fuse_mode"] == llgpu.LLG_FUSE_REG:  # complex64 only: the register-tiled pass
+        assert precision == "complex64"
+        assert tun["fuse_mode"] == "reg" and tun["tile_qubits"] == res["tile_qubits"]
     else:
         assert tun["fuse_mode"] == "none"
     st.apply_ops(ops)
