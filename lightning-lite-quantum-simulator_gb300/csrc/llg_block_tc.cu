@@ -11,20 +11,25 @@
 // where every slice is an integer of magnitude <= 256, exact in bf16.  The 21 slice products
 // with i + j <= 5 are accumulated by diagonal d = i + j into six fp32 accumulators in tensor
 // memory.  A product of two slices is below 2^16 and 64 of them below 2^22, so each diagonal sum
-// is an integer below 2^24 and the fp32 accumulation is exact (K = 32 leaves a factor 2 spare).  The epilogue recombines
-//     D = 2^(e_g + e_r - 16) sum_d 2^(-8 d) D_d
-// into double-float.  Dropped terms (i + j >= 6) and the final rounding stay near 2^-46 of each
-// group's largest amplitude.
+// is an integer below 2^24 and the fp32 accumulation is exact (K = 32 leaves a factor 2 spare).
+// Diagonals 0, 1 and 2 get an accumulator each; 3, 4 and 5 share one, filled by Horner's rule with
+// the MMA's input scale (D = A B + 2^-8 D on the first product of a diagonal): it holds
+// D_3 + 2^-8 D_4 + 2^-16 D_5, rounded at fp32 precision of D_3's scale.  The epilogue recombines
+//     D = 2^(e_g + e_r - 16) (D_0 + 2^-8 D_1 + 2^-16 D_2 + 2^-24 D_345)
+// into double-float, the first three terms exactly.  Dropped terms (i + j >= 6) and the
+// rounding stay near 2^-46 of each group's largest amplitude.
 //
-// Persistent CTAs (k = 5: one of 512 threads per SM; k = 4: two of 256).  Per tile: every thread
-// takes its 8 amplitudes from
-// shared memory (copied asynchronously while the previous tile was in the tensor cores), the
-// group scales come from the largest high part, slices go to shared memory in the no-swizzle
-// K-major core-matrix layout, one thread issues the 21 x K/16 MMAs (M = 128 groups, N = 2A, K = 16
-// per instruction) and commits them to an mbarrier, all threads wait (bounded), read the
-// accumulators with tcgen05.ld, recombine and stage the amplitudes in shared memory, and store
-// them.  The gate's slices are prepared on the host in double (exact) and copied to shared
-// memory once per CTA.
+// Persistent CTAs (k = 5: one of 512 threads per SM; k = 4: two of 256), pipelined by one tile:
+// tensor memory holds two accumulator sets, and while the tensor cores compute tile i into one,
+// the threads recombine tile i - 1 from the other and store it.  Per tile: every thread takes its
+// 8 amplitudes from shared memory (copied asynchronously during the previous tile), the group
+// scales come from the largest high part, the next tile's copies start, the threads wait
+// (bounded) until the tensor cores have finished tile i - 1 (they read the slice buffer), write
+// the slices in the no-swizzle K-major core-matrix layout, and one thread issues the 21 x K/16
+// MMAs (M = 128 groups, N = 2A, K = 16 per instruction) and commits them to an mbarrier.  Then
+// the epilogue of tile i - 1: tcgen05.ld of its accumulators, recombination, and stores straight
+// from registers (a warp's lanes hold 32 consecutive groups).  The gate's slices are prepared on
+// the host in double (exact) and copied to shared memory once per CTA.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -43,6 +48,7 @@ namespace {
 
 constexpr int kTcGroups = 128;            // groups per tile (the MMA's M)
 constexpr int kTcSlices = 6;              // 8-bit slices per operand
+constexpr int kTcAcc = 4;                 // accumulators per set: diagonals 0, 1, 2 and 3..5
 constexpr long kTcWaitLimit = 1L << 26;   // mbarrier polls before the kernel reports a timeout
 
 // shapes of the k = 4 and k = 5 kernels
@@ -55,11 +61,13 @@ struct TcShape {
     static constexpr int kPer = kTcGroups * kAmps / kThreads;      // amplitudes per thread (8)
     static constexpr int kSliceBytes = kTcGroups * kReals * 2;     // one state slice, bf16
     static constexpr int kWSliceBytes = kReals * kReals * 2;       // one gate slice, bf16
-    static constexpr int kTmemCols = KQ == 5 ? 512 : 256;          // six accumulators, power of two
+    static constexpr int kSetCols = kTcAcc * kReals;               // one accumulator set
+    static constexpr int kTmemCols = 2 * kSetCols;                 // two sets (512 / 256: powers of two)
     static constexpr size_t kSmem =
         (size_t)kTcSlices * (kSliceBytes + kWSliceBytes) + (size_t)kTcGroups * kAmps * sizeof(float4);
     static_assert(kPer == 8, "one 8-wide core of real and one of imaginary parts per thread");
-    static_assert(6 * kReals <= kTmemCols, "accumulators fit the allocation");
+    static_assert(kTmemCols == 512 || kTmemCols == 256, "a power-of-two allocation of at most 512 columns");
+    static_assert(kTmemCols * kMinBlocks <= 512, "the CTAs of an SM fit its tensor memory");
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -97,13 +105,14 @@ __global__ void __launch_bounds__(TcShape<KQ>::kThreads, TcShape<KQ>::kMinBlocks
     using T = TcShape<KQ>;
     constexpr int kAmps = T::kAmps, kReals = T::kReals, kPer = T::kPer;
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* sA = smem;                                  // kTcSlices state slices (also the output stage)
+    unsigned char* sA = smem;                                  // kTcSlices state slices
     unsigned char* sW = smem + kTcSlices * T::kSliceBytes;     // kTcSlices gate slices
     // the next tile's amplitudes, [amplitude][group] so that a warp's 32 groups are 32 consecutive
     // float4s (a [group][amplitude] layout puts them kAmps * 16 bytes apart: 32-way bank conflicts)
     float4* sIn = reinterpret_cast<float4*>(sW + kTcSlices * T::kWSliceBytes);
     __shared__ uint64_t toff[kAmps];
-    __shared__ int32_t eg_s[kTcGroups];
+    // group exponents, three tiles in turn: a tile's row is zeroed two tiles after its epilogue read it
+    __shared__ int32_t eg_s[3][kTcGroups];
     __shared__ int32_t er_s[kReals];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_s;
@@ -160,10 +169,76 @@ __global__ void __launch_bounds__(TcShape<KQ>::kThreads, TcShape<KQ>::kMinBlocks
     __syncthreads();  // toff
     if ((uint64_t)blockIdx.x < ntiles) prefetch(blockIdx.x);
 
-    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    // bounded wait for the products committed with parity `ph`; false: the limit ran out
+    auto wait_mma = [&](uint32_t ph) {
+        uint32_t done = 0;
+        for (long it = 0; it < kTcWaitLimit && !done; ++it)
+            asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                         : "=r"(done)
+                         : "r"(smem_u32(&mbar)), "r"(ph));
+        return done != 0;
+    };
+    // recombine the tile in accumulator set `set` and store it: warp w reads lanes 32 (w & 3) ..
+    // +31 (its groups) and the real and imaginary columns of amplitudes 8 (w >> 2) .. +7, so that
+    // each thread writes whole amplitudes, a warp 32 consecutive groups per amplitude
+    auto epilogue = [&](uint64_t tile, int set, int egb) {
+        const int row = 32 * (warp & 3) + lane;
+        const int a0 = 8 * (warp >> 2);
+        const int eg = eg_s[egb][row] - 1000;  // stored with the atomicMax offset
+        df out[2][8];
+#pragma unroll
+        for (int part = 0; part < 2; ++part) {
+            uint32_t v[kTcAcc][8];
+#pragma unroll
+            for (int d = 0; d < kTcAcc; ++d) {
+                const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) +
+                                       (uint32_t)(set * T::kSetCols + d * kReals + kAmps * part + a0);
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                             : "=r"(v[d][0]), "=r"(v[d][1]), "=r"(v[d][2]), "=r"(v[d][3]), "=r"(v[d][4]), "=r"(v[d][5]),
+                               "=r"(v[d][6]), "=r"(v[d][7])
+                             : "r"(taddr));
+            }
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                // D_0 + 2^-8 D_1 + 2^-16 D_2 exactly, 2^-24 D_345 rounded once (below 2^-46)
+                const float d0 = __uint_as_float(v[0][c]), d1 = __uint_as_float(v[1][c]) * 0x1p-8f;
+                const float d2 = __uint_as_float(v[2][c]) * 0x1p-16f;
+                const float t = __uint_as_float(v[3][c]) * 0x1p-24f;
+                df acc = two_sum(d0, d1);
+                acc = df_add_f(acc, d2);
+                acc = fast_two_sum(acc.hi, __fadd_rn(acc.lo, t));
+                // 2^(e_g + e_r - 16), split in two factors so that each stays a normal float
+                const int et = eg + er_s[kAmps * part + a0 + c] - 16;
+                const int e1 = max(min(et, 100), -100), e2 = max(min(et - e1, 100), -126);
+                const float f1 = pow2f(e1), f2 = pow2f(e2);
+                out[part][c] = {acc.hi * f1 * f2, acc.lo * f1 * f2};
+            }
+        }
+        const uint64_t base = insert0_mask(tile * kTcGroups + (uint64_t)row, bd.tmask);
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+            psi[base | toff[a0 + c]] = make_float4(out[0][c].hi, out[1][c].hi, out[0][c].lo, out[1][c].lo);
+        // the accumulator set is read: the next MMAs into it may follow the next barrier
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    };
+    // one MMA: D (+)= A B, with D first scaled by 2^-8 when `scale` is set
+    auto mma = [&](uint32_t dcol, uint64_t da, uint64_t dw, uint32_t acc, bool scale) {
+        if (scale)
+            asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p, 8;\n}" ::"r"(
+                             dcol),
+                         "l"(da), "l"(dw), "r"(idesc), "r"(acc));
+        else
+            asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
+                             dcol),
+                         "l"(da), "l"(dw), "r"(idesc), "r"(acc));
+    };
+
+    uint64_t prev_tile = 0;
+    bool have_prev = false;
+    int set = 0, egb = 0;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, set ^= 1, egb = egb == 2 ? 0 : egb + 1) {
         // ---- this thread's amplitudes of group gl (its own copies), the group's scale ----
-        const uint64_t g = tile * kTcGroups + (uint64_t)gl;
-        const uint64_t base = insert0_mask(g, bd.tmask);
         asm volatile("cp.async.wait_group 0;" ::: "memory");
         float4 a[kPer];
         float mx = 0.0f;
@@ -176,16 +251,35 @@ __global__ void __launch_bounds__(TcShape<KQ>::kThreads, TcShape<KQ>::kMinBlocks
             a[i] = make_float4(re.hi, im.hi, re.lo, im.lo);
             mx = fmaxf(mx, fmaxf(fabsf(a[i].x), fabsf(a[i].y)));
         }
-        if (h == 0) eg_s[gl] = 0;
+        // eg_s[egb] was last read by the epilogue of tile i - 3, during tile i - 1: the barriers of
+        // the tile in between separate that read from this write
+        if (h == 0) eg_s[egb][gl] = 0;
         __syncthreads();
         // all |x| < 2^e with e from the high parts' largest exponent; clamped so that the scale
         // factors 2^(8 - e) and 2^(32 - e) below stay normal floats (groups under 2^-94 keep their
         // absolute error below 2^-134 instead of a relative one)
         int e = (int)((__float_as_uint(mx) >> 23) & 0xFF) - 126;
         e = max(e, -94);
-        atomicMax(&eg_s[gl], e + 1000);  // the group's threads agree on the largest exponent
+        atomicMax(&eg_s[egb][gl], e + 1000);  // the group's threads agree on the largest exponent
         __syncthreads();
-        e = eg_s[gl] - 1000;
+        e = eg_s[egb][gl] - 1000;
+        // every thread has read its amplitudes out of sIn: start the next tile's copies
+        if (tile + gridDim.x < ntiles) prefetch(tile + gridDim.x);
+        // ---- the previous tile's products must be done before its slices are overwritten ----
+        if (have_prev) {
+            if (!wait_mma(phase)) abort_s = 1;
+            __syncthreads();
+            if (abort_s) {
+                // report, then give the products in flight a second bounded wait before the
+                // accumulators are freed
+                if (tid == 0) atomicExch(err_flag, 1);
+                wait_mma(phase);
+                have_prev = false;
+                break;
+            }
+            phase ^= 1;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        }
         // ---- six 8-bit slices per real, into the core-matrix layout ----
         {
             const float sc = pow2f(8 - e), sclo = pow2f(32 - e);
@@ -224,103 +318,49 @@ __global__ void __launch_bounds__(TcShape<KQ>::kThreads, TcShape<KQ>::kMinBlocks
                         make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
             }
         }
-        // every thread has read its amplitudes out of sIn: start the next tile's copies
-        if (tile + gridDim.x < ntiles) prefetch(tile + gridDim.x);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
+        __syncthreads();  // the slices are written; the epilogue two tiles back has read this set
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // ---- 21 slice products (i + j <= 5) into six accumulators, K / 16 steps each ----
+        // ---- 21 slice products (i + j <= 5) into four accumulators of this set, K / 16 steps each ----
         if (tid == 0) {
-            for (int d = 0; d < kTcSlices; ++d) {
-                uint32_t acc = 0;
+            const uint32_t tset = tmem + (uint32_t)(set * T::kSetCols);
+            auto diagonal = [&](int d, uint32_t dcol, bool first_fresh) {
+                bool first = true;
                 for (int i = 0; i <= d; ++i) {
                     const int j = d - i;
                     for (int ks = 0; ks < kReals / 16; ++ks) {
                         const uint64_t da = tc_desc(smem_u32(sA + i * T::kSliceBytes) + ks * 256, lbo, sbo);
                         const uint64_t dw = tc_desc(smem_u32(sW + j * T::kWSliceBytes) + ks * 256, lbo, sbo);
-                        asm volatile(
-                            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
-                                tmem + (uint32_t)(d * kReals)),
-                            "l"(da), "l"(dw), "r"(idesc), "r"(acc));
-                        acc = 1;
+                        // a diagonal's first product starts the accumulator (first_fresh) or scales
+                        // the diagonals above it by 2^-8 (Horner)
+                        mma(dcol, da, dw, (first && first_fresh) ? 0u : 1u, first && !first_fresh);
+                        first = false;
                     }
                 }
-            }
+            };
+            for (int d = 0; d < 3; ++d) diagonal(d, tset + (uint32_t)(d * kReals), true);
+            diagonal(5, tset + (uint32_t)(3 * kReals), true);
+            diagonal(4, tset + (uint32_t)(3 * kReals), false);
+            diagonal(3, tset + (uint32_t)(3 * kReals), false);
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(&mbar)));
         }
-        // ---- bounded wait for the products ----
-        uint32_t done = 0;
-        for (long it = 0; it < kTcWaitLimit && !done; ++it)
-            asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
-                         : "=r"(done)
-                         : "r"(smem_u32(&mbar)), "r"(phase));
-        if (!done) abort_s = 1;
+        // ---- the previous tile's epilogue, under this tile's products ----
+        if (have_prev) epilogue(prev_tile, set ^ 1, egb == 0 ? 2 : egb - 1);
+        prev_tile = tile;
+        have_prev = true;
+    }
+    // the last tile
+    if (have_prev) {
+        if (!wait_mma(phase)) abort_s = 1;
         __syncthreads();
         if (abort_s) {
-            // report, then give the products in flight a second bounded wait before the
-            // accumulators are freed
             if (tid == 0) atomicExch(err_flag, 1);
-            done = 0;
-            for (long it = 0; it < kTcWaitLimit && !done; ++it)
-                asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
-                             : "=r"(done)
-                             : "r"(smem_u32(&mbar)), "r"(phase));
-            break;
+            wait_mma(phase);
+        } else {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            epilogue(prev_tile, set ^ 1, egb == 0 ? 2 : egb - 1);
         }
-        phase ^= 1;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // ---- epilogue: warp w reads lanes 32 (w & 3) .. +31 (its groups) and the real and imaginary
-        // columns of amplitudes 8 (w >> 2) .. +7, so that each thread writes whole amplitudes ----
-        {
-            const int row = 32 * (warp & 3) + lane;
-            const int a0 = 8 * (warp >> 2);
-            const int eg = eg_s[row] - 1000;  // stored with the atomicMax offset
-            float4* stage = reinterpret_cast<float4*>(sA);  // [amplitude][group]; the MMAs are done
-            df out[2][8];
-#pragma unroll
-            for (int part = 0; part < 2; ++part) {
-                uint32_t v[kTcSlices][8];
-#pragma unroll
-                for (int d = 0; d < kTcSlices; ++d) {
-                    const uint32_t taddr =
-                        tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(d * kReals + kAmps * part + a0);
-                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                                 : "=r"(v[d][0]), "=r"(v[d][1]), "=r"(v[d][2]), "=r"(v[d][3]), "=r"(v[d][4]), "=r"(v[d][5]),
-                                   "=r"(v[d][6]), "=r"(v[d][7])
-                                 : "r"(taddr));
-                }
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-                for (int c = 0; c < 8; ++c) {
-                    // D_0 + 2^-8 D_1 + 2^-16 D_2 exactly, the rest rounded once (below 2^-46)
-                    const float d0 = __uint_as_float(v[0][c]), d1 = __uint_as_float(v[1][c]) * 0x1p-8f;
-                    const float d2 = __uint_as_float(v[2][c]) * 0x1p-16f;
-                    float t = fmaf(__uint_as_float(v[5][c]), 0x1p-40f, __uint_as_float(v[4][c]) * 0x1p-32f);
-                    t = fmaf(__uint_as_float(v[3][c]), 0x1p-24f, t);
-                    df acc = two_sum(d0, d1);
-                    acc = df_add_f(acc, d2);
-                    acc = fast_two_sum(acc.hi, __fadd_rn(acc.lo, t));
-                    // 2^(e_g + e_r - 16), split in two factors so that each stays a normal float
-                    const int et = eg + er_s[kAmps * part + a0 + c] - 16;
-                    const int e1 = max(min(et, 100), -100), e2 = max(min(et - e1, 100), -126);
-                    const float f1 = pow2f(e1), f2 = pow2f(e2);
-                    out[part][c] = {acc.hi * f1 * f2, acc.lo * f1 * f2};
-                }
-            }
-#pragma unroll
-            for (int c = 0; c < 8; ++c)
-                stage[(a0 + c) * kTcGroups + row] = make_float4(out[0][c].hi, out[1][c].hi, out[0][c].lo, out[1][c].lo);
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        // ---- store ----
-        {
-            const float4* stage = reinterpret_cast<const float4*>(sA);
-#pragma unroll
-            for (int i = 0; i < kPer; ++i) psi[base | toff[kPer * h + i]] = stage[(kPer * h + i) * kTcGroups + gl];
-        }
-        __syncthreads();  // the stage is the next tile's slice area
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");  // no copy left in flight on any exit
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

@@ -108,7 +108,21 @@ def tsolve():
     s.close()
 
 
-CASES = {"tile_f64": tile_f64, "tile_reg_c64": tile_reg_c64, "tile_c64": tile_c64, "streaming": streaming,
+def block_tc():
+    """A dense 5-qubit block on a 26-qubit double-float state (1 GiB) on the tensor cores: a random
+    32x32 unitary on qubits (0, 7, 13, 22, 25), applied three times after a layer of H."""
+    n = 26
+    st = llgpu.State(n, "df64")
+    st.apply_ops(llgpu.make_ops([(llgpu.OP_H, q) for q in range(n)]))
+    rng = np.random.default_rng(17)
+    m = np.linalg.qr(rng.normal(size=(32, 32)) + 1j * rng.normal(size=(32, 32)))[0]
+    for _ in range(3):
+        st.apply_matrix([0, 7, 13, 22, 25], m)
+    st.sync()
+    st.close()
+
+
+CASES = {"tile_f64": tile_f64, "block_tc": block_tc, "tile_reg_c64": tile_reg_c64, "tile_c64": tile_c64, "streaming": streaming,
          "reductions": reductions, "readback": readback, "tsolve": tsolve}
 
 if __name__ == "__main__":
