@@ -315,9 +315,13 @@ def plan_for(precision: str, n: int, ops, tile_q: int, regs: bool = False):
     import llgpu
 
     if regs:
-        return llgpu.plan_export(n, ops, tile_q, zyz=True, regs=True)
-    r = llgpu.plan_export(n, ops, tile_q, zyz=precision != "complex64", tables=precision != "complex64")
-    return r[0], r[1]
+        p, x = llgpu.plan_export(n, ops, tile_q, zyz=True, regs=True)
+        return p, x, 0
+    if precision == "complex64":
+        p, x = llgpu.plan_export(n, ops, tile_q, zyz=False)
+        return p, x, 0
+    p, x, tab = llgpu.plan_export(n, ops, tile_q, zyz=True, tables=True)
+    return p, x, int(tab.nbytes)
 
 
 def compute_roofline(precision, n, xops, tile_ms_step, sm_mhz):
@@ -387,7 +391,7 @@ def measure_circuit(args, torch, precision, n, ops, steps, warmup, world, sample
         st.set_tile_threads(args.cta_threads)
     tuning = st.tuning()
     tile_q = tuning["tile_qubits"]
-    passes, xops = plan_for(precision, n, ops, tile_q, tuning["fuse_mode"] == "reg")
+    passes, xops, table_bytes = plan_for(precision, n, ops, tile_q, tuning["fuse_mode"] == "reg")
     if tuning["fuse_mode"] == "none":
         passes = np.zeros(ngates)  # one streaming pass per gate
     state_bytes = ELEM_BYTES.get(precision, 16) * (1 << n)
@@ -439,6 +443,7 @@ def measure_circuit(args, torch, precision, n, ops, steps, warmup, world, sample
     res = {
         "value": value, "unit": "gates/s", "steps": steps, "warmup": warmup, "ms_per_step": elapsed_ms / steps,
         "gpu_launches": launches, "tile_passes": int(len(passes)), "tile_qubits": tile_q, "fusion": tuning,
+        "phase_table_bytes": table_bytes,
         "autotune": tune, "state_bytes": state_bytes, "clocks": clocks,
         "sweeps_per_s": len(passes) * steps * world / (elapsed_ms / 1e3),
         "hbm_gbs_algorithmic": len(passes) * 2 * state_bytes * steps * world / (elapsed_ms / 1e3) / 1e9,
@@ -493,7 +498,7 @@ def run_ours(args, rank, world, local):
     head = finish_rooflines(head, args.precision, n, fma_rate)
     clocks = head.pop("clocks")
     elem = ELEM_BYTES.get(args.precision, 16)
-    _, xops_e2e = plan_for(args.precision, n, ops, head["tile_qubits"], head["fusion"]["fuse_mode"] == "reg")
+    _, xops_e2e, tables_e2e = plan_for(args.precision, n, ops, head["tile_qubits"], head["fusion"]["fuse_mode"] == "reg")
 
     # the same circuit in the other precisions, each compared with this (FP64) final state
     variants = None
@@ -509,15 +514,15 @@ def run_ours(args, rank, world, local):
                             "max_abs_diff_rel_to_max_amp": (dmax / amax) if amax else None}
             vst.close()
             if not args.no_e2e:
-                v["e2e"] = run_e2e(args, prec, ops, plan_for(prec, n, ops, v["tile_qubits"], v["fusion"]["fuse_mode"] == "reg")[1], n,
-                                   ELEM_BYTES.get(prec, 16), world, torch, v["tile_qubits"])
+                _, vx, vtab = plan_for(prec, n, ops, v["tile_qubits"], v["fusion"]["fuse_mode"] == "reg")
+                v["e2e"] = run_e2e(args, prec, ops, vx, vtab, n, ELEM_BYTES.get(prec, 16), world, torch)
             variants[prec] = v
     st.close()
 
     # end to end through the drop-in module: op records in, final amplitudes out, every step
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(args, args.precision, ops, xops_e2e, n, elem, world, torch, head["tile_qubits"])
+        e2e = run_e2e(args, args.precision, ops, xops_e2e, tables_e2e, n, elem, world, torch)
 
     sweeps = None
     if not args.no_sweeps:
@@ -1069,7 +1074,7 @@ def run_batch_bench(args, torch, cpu: bool):
     return res
 
 
-def run_e2e(args, precision, ops, xops, n, elem, world, torch, tile_q=12):
+def run_e2e(args, precision, ops, xops, table_bytes, n, elem, world, torch):
     import quantum_sim_v3
 
     sv = quantum_sim_v3.StateVector(n, precision)
@@ -1101,7 +1106,7 @@ def run_e2e(args, precision, ops, xops, n, elem, world, torch, tile_q=12):
     del sv, view
     return {"value": len(ops) * steps * world / (t1 - t0), "unit": "gates/s", "steps": steps,
             "ms_per_step": 1e3 * (t1 - t0) / steps, "passes_alone_ms": 1e3 * (b - a), "readback_alone_ms": 1e3 * (c - b),
-            "h2d_bytes_per_step": int(xops.nbytes + int(np.sum(xops["kind"] == 18)) * 16 * (1 << tile_q)),
+            "h2d_bytes_per_step": int(xops.nbytes + table_bytes),
             "h2d_note": "the planned executor ops and phase tables uploaded by the flush",
             "d2h_bytes_per_step": int((1 << n) * 16),
             "api": "quantum_sim_v3.StateVector: reset, apply_ops, get_numpy_view (host copy of all amplitudes; "
