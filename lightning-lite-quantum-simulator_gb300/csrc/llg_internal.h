@@ -51,9 +51,7 @@ enum ExecKind : int32_t {
     // multiply every tile amplitude l by the phase-table entry T[l] (a diagonal of the tile's
     // local qubits: the product of the input phases, controlled phases and carried phases the
     // planner gathered there); the table starts at entry `mask` of the plan's table buffer and
-    // has 2^t entries of (re, im) coefficient slots.  When nl_mask is set (controlled phases whose
-    // control is outside the tile), 2^popcount(nl_mask) tables follow one another and a tile uses
-    // variant v, bit j of v the tile's bit of the j-th lowest qubit of nl_mask
+    // has 2^t entries of (re, im) coefficient slots
     EX_PTAB = 18,
     // register-tiled passes (to_register_program): switch the tile's register layout.  Each thread
     // holds 16 amplitudes whose local indices vary over 4 "register" positions (mask: 4 x 4 bits)

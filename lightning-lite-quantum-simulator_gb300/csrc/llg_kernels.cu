@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, 
             case EX_ZC: tile_pairs<P, EX_ZC>(tile, tsize >> 1, o.q0, o); break;
             case EX_RT: tile_pairs<P, EX_RT>(tile, tsize >> 1, o.q0, o); break;
             case EX_RC: tile_pairs<P, EX_RC>(tile, tsize >> 1, o.q0, o); break;
-            case EX_PTAB: tile_ptab<P>(tile, tsize, base, o, tables); break;
+            case EX_PTAB: tile_ptab<P>(tile, tsize, o, tables); break;
             case EX_PHASE1: tile_phase1<P>(tile, tsize, base, o); break;
             case EX_RX: tile_pairs<P, EX_RX>(tile, tsize >> 1, o.q0, o); break;
             case EX_RY: tile_pairs<P, EX_RY>(tile, tsize >> 1, o.q0, o); break;

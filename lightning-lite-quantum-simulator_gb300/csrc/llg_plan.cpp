@@ -206,13 +206,8 @@ static double coef_value(uint64_t bits) {
 // ------------------------------------------------------------------------------------------
 namespace {
 
-// Controlled phases whose control lies outside the tile: a table point holding such factors has
-// one table variant per combination of their control bits (at most this many distinct controls).
-constexpr int kMaxTableCtrl = 5;
-
 struct DiagFactor {
-    int kind;       // 0 rotation input phase, 1 controlled phase, 2 one-qubit diagonal op,
-                    // 3 controlled phase with a global control outside the tile (q0 global)
+    int kind;       // 0 rotation input phase, 1 controlled phase, 2 one-qubit diagonal op
     int op;         // index of the op in the pass
     int q0, q1;     // local qubits: the phase's qubit; for 1 the control and the target
     std::complex<double> v0, v1;  // kind 2: the values on bit 0 and bit 1; else v1 only
@@ -235,12 +230,6 @@ bool mixes(const ExecOp& e, int q) {
 }
 
 }  // namespace
-
-// complex product by the schoolbook formula (std::complex's operator* goes through a library
-// call that rechecks for infinities; the table entries are unit-modulus and finite)
-static inline std::complex<double> cmul(const std::complex<double>& a, const std::complex<double>& b) {
-    return {a.real() * b.real() - a.imag() * b.imag(), a.real() * b.imag() + a.imag() * b.real()};
-}
 
 static void gather_phase_tables(Plan& out) {
     using cd = std::complex<double>;
@@ -327,14 +316,6 @@ static void gather_phase_tables(Plan& out) {
                 f.lo = i + 1;
                 f.hi = next_mix(i, x.q0, x.q1);
                 f.saves = 0.5;  // a quarter of the amplitudes
-            } else if (x.kind == EX_CNOT && (x.flags & OPF_PHASE)) {  // control outside the tile
-                f.kind = 3;
-                f.q0 = x.q0;
-                f.q1 = x.q1;
-                f.v1 = cd(coef_value(x.c[0]), coef_value(x.c[1]));
-                f.lo = i + 1;
-                f.hi = next_mix(i, x.q1, -1);
-                f.saves = 0.5;  // the target-1 half of the tiles whose control bit is set
             } else if ((x.kind == EX_PHASE1 || x.kind == EX_DIAG) && !(x.flags & OPF_NONLOCAL_Q0)) {
                 f.kind = 2;
                 f.q0 = x.q0;
@@ -368,22 +349,6 @@ static void gather_phase_tables(Plan& out) {
             fs[k].point = (int)pts.size() - 1;
             gain.back() += fs[k].saves;
         }
-        // at most kMaxTableCtrl distinct outside controls per point (2^k table variants); the
-        // factors of any further control stay on their CNOTs
-        std::vector<std::vector<int>> ctrls(pts.size());
-        for (DiagFactor& f : fs) {
-            if (f.kind != 3) continue;
-            std::vector<int>& c = ctrls[f.point];
-            if (std::find(c.begin(), c.end(), f.q0) == c.end()) {
-                if ((int)c.size() == kMaxTableCtrl) {
-                    gain[f.point] -= f.saves;
-                    f.point = -1;
-                    continue;
-                }
-                c.push_back(f.q0);
-            }
-        }
-        for (auto& c : ctrls) std::sort(c.begin(), c.end());
         std::vector<char> keep(pts.size());
         for (size_t p = 0; p < pts.size(); ++p) keep[p] = gain[p] > 2.0;
         // tables of the kept points
@@ -392,11 +357,10 @@ static void gather_phase_tables(Plan& out) {
         for (size_t p = 0; p < pts.size(); ++p) {
             if (!keep[p]) continue;
             std::vector<cd> qv(t, cd(1.0, 0.0)), q0v(t, cd(1.0, 0.0));  // per-qubit bit-1 / bit-0 factors
-            std::vector<const DiagFactor*> cps, ccps;
+            std::vector<const DiagFactor*> cps;
             for (const DiagFactor& f : fs) {
                 if (f.point != (int)p) continue;
                 if (f.kind == 1) cps.push_back(&f);
-                else if (f.kind == 3) ccps.push_back(&f);
                 else {
                     qv[f.q0] *= f.v1;
                     if (f.kind == 2) q0v[f.q0] *= f.v0;
@@ -408,49 +372,19 @@ static void gather_phase_tables(Plan& out) {
                 const size_t half = (size_t)1 << q;
                 const bool scale0 = !(q0v[q].real() == 1.0 && q0v[q].imag() == 0.0);
                 for (size_t l = 0; l < half; ++l) {
-                    tab[l | half] = cmul(tab[l], qv[q]);
-                    if (scale0) tab[l] = cmul(tab[l], q0v[q]);
+                    tab[l | half] = tab[l] * qv[q];
+                    if (scale0) tab[l] *= q0v[q];
                 }
             }
             for (const DiagFactor* f : cps) {
                 const size_t both = ((size_t)1 << f->q0) | ((size_t)1 << f->q1);
                 for (size_t l = 0; l < entries; ++l)
-                    if ((l & both) == both) tab[l] = cmul(tab[l], f->v1);
+                    if ((l & both) == both) tab[l] *= f->v1;
             }
             table_of[p] = (long)(out.tables.size() / 2);
-            // variant v: the outside controls ctrls[p][j] with bit j of v set are 1 in the tile.
-            // Built by doubling: variant v | 2^j is variant v times control j's factor, the product
-            // of its controlled phases on their targets' 1 halves (one pass over the entries).
-            const int nc = (int)ctrls[p].size(), nv = 1 << nc;
-            std::vector<cd> fac((size_t)nc * entries);
-            for (int j = 0; j < nc; ++j) {
-                std::vector<cd> tv(t, cd(1.0, 0.0));  // the factor on target bit 1, per local qubit
-                for (const DiagFactor* f : ccps)
-                    if (f->q0 == ctrls[p][j]) tv[f->q1] = cmul(tv[f->q1], f->v1);
-                cd* fj = fac.data() + (size_t)j * entries;
-                fj[0] = 1.0;
-                for (int q = 0; q < t; ++q) {
-                    const size_t half = (size_t)1 << q;
-                    for (size_t l = 0; l < half; ++l) fj[l | half] = cmul(fj[l], tv[q]);
-                }
-            }
-            // F64 coefficient slots hold the doubles' bits: the variants are built in place
-            const size_t at = out.tables.size();
-            out.tables.resize(at + 2 * (size_t)nv * entries);
-            uint64_t* dst0 = out.tables.data() + at;
-            std::memcpy(dst0, tab.data(), entries * sizeof(cd));
-            for (int v = 1; v < nv; ++v) {
-                const int j = 31 - __builtin_clz((unsigned)v);  // highest bit of v
-                const uint64_t* src = dst0 + 2 * (size_t)(v ^ (1 << j)) * entries;
-                uint64_t* dst = dst0 + 2 * (size_t)v * entries;
-                const cd* fj = fac.data() + (size_t)j * entries;
-                for (size_t l = 0; l < entries; ++l) {
-                    double a[2], r[2];
-                    std::memcpy(a, src + 2 * l, sizeof(a));
-                    r[0] = a[0] * fj[l].real() - a[1] * fj[l].imag();
-                    r[1] = a[0] * fj[l].imag() + a[1] * fj[l].real();
-                    std::memcpy(dst + 2 * l, r, sizeof(r));
-                }
+            for (const cd& v : tab) {
+                out.tables.push_back(pack_coef(LLG_F64, v.real()));
+                out.tables.push_back(pack_coef(LLG_F64, v.imag()));
             }
         }
         // rewrite the pass
@@ -459,13 +393,12 @@ static void gather_phase_tables(Plan& out) {
             if (keep[p]) pt_at[pts[p]] = (int)p;
         std::vector<int> absorbed(m, 0);  // 1: factor moved into a table
         for (const DiagFactor& f : fs)
-            if (f.point >= 0 && keep[f.point]) absorbed[f.op] = 1;
+            if (keep[f.point]) absorbed[f.op] = 1;
         const int begin = (int)ops.size();
         for (int i = 0; i <= m; ++i) {
             if (pt_at[i] >= 0) {
                 ExecOp tp = blank(EX_PTAB);
                 tp.mask = (uint64_t)table_of[pt_at[i]];
-                for (int c : ctrls[pt_at[i]]) tp.nl_mask |= 1ULL << c;
                 ops.push_back(tp);
                 src.push_back(-1);
             }

@@ -157,13 +157,10 @@ __device__ __forceinline__ void tile_phase1(typename P::S* tile, uint32_t tsize,
 // EX_PTAB: every amplitude l of the tile times the phase-table entry T[l] (the table starts at
 // entry o.mask of `tables`; two coefficient slots (re, im) per entry, read through the L2 cache)
 template <class P>
-__device__ __forceinline__ void tile_ptab(typename P::S* tile, uint32_t tsize, uint64_t base, const ExecOp& o,
+__device__ __forceinline__ void tile_ptab(typename P::S* tile, uint32_t tsize, const ExecOp& o,
                                           const uint64_t* __restrict__ tables) {
     using K = typename P::K;
-    // the variant of this tile: its bits of the outside controls, lowest qubit first
-    uint64_t variant = 0, m = o.nl_mask;
-    for (int j = 0; m; ++j, m &= m - 1) variant |= ((base >> (__ffsll((long long)m) - 1)) & 1ULL) << j;
-    const ulonglong2* tb = reinterpret_cast<const ulonglong2*>(tables) + o.mask + variant * tsize;
+    const ulonglong2* tb = reinterpret_cast<const ulonglong2*>(tables) + o.mask;
     for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
         const ulonglong2 w = __ldg(tb + l);
         const K tr = P::k_from_bits(w.x), ti = P::k_from_bits(w.y);

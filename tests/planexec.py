@@ -97,12 +97,9 @@ def execute(psi: np.ndarray, n: int, passes: np.ndarray, xops: np.ndarray, table
                 continue
             if k <= 4 or k in (11, 12, 14, 15, 16, 17):
                 _pair(tile, q0, _matrix(x))
-            elif k == 18:  # phase table: tile amplitude l times entry l (of the tile's variant)
-                off, ctl = int(x["mask"]), [q for q in range(64) if int(x["nl_mask"]) >> q & 1]
-                var = np.zeros(bases.size, dtype=np.int64)
-                for j, q in enumerate(ctl):
-                    var |= ((bases >> q) & 1) << j
-                tile *= tables[off + (var[:, None] << t) + lidx[None, :]]
+            elif k == 18:  # phase table: tile amplitude l times entry l
+                off = int(x["mask"])
+                tile *= tables[off:off + (1 << t)][None, :]
             elif k == 13:  # diag(1, ph) on q0 (tile-uniform when q0 is not local)
                 ph = x["c"][0] + 1j * x["c"][1]
                 if fl & 1:

@@ -278,7 +278,7 @@ def test_phase_tables_halve_the_rotation_arithmetic(built):
     kinds = np.bincount(xops["kind"], minlength=19)
     assert kinds[16] + kinds[17] > 500 and kinds[18] > 0
     assert _fp64_mults_per_pair(xops) < 0.7 * _fp64_mults_per_pair(plain[1])
-    assert tab.size >= kinds[18] << 12  # variants for controlled phases with outside controls
+    assert tab.size == kinds[18] << 12
 
 
 def _ising_diagonal(n, zz, z):
