@@ -385,7 +385,7 @@ def measure_circuit(args, torch, precision, n, ops, steps, warmup, world, sample
     tune = None
     if args.tile < 0:
         # autotuner: two layers of the circuit on a scratch state, outside the timed region
-        tune = st.autotune(ops, sample_ops=2 * len(ops) // max(1, args.layers))
+        tune = st.autotune(ops, sample_ops=4 * len(ops) // max(1, args.layers))
     else:
         st.set_fusion("tile", args.tile)
         st.set_tile_threads(args.cta_threads)
@@ -608,9 +608,14 @@ def summarize(line: dict) -> dict:
         "trajectories_per_s_df64": get(line, "trajectories", "df64", "traj_per_s"),
         "trajectories_per_s_c64": get(line, "trajectories", "c64", "traj_per_s"),
         "mixed_batch_circuits_per_s_c128": get(line, "mixed_batch", "c128", "circuits_per_s"),
+        "mixed_batch_circuits_per_s_df64": get(line, "mixed_batch", "df64", "circuits_per_s"),
         "mixed_batch_circuits_per_s_c64": get(line, "mixed_batch", "c64", "circuits_per_s"),
         "zne_traj_per_s": get(line, "zne", "traj_per_s"),
+        "block5_tensor_core_hbm_frac": get(line, "gate_sweeps", "df64", "block5", "frac"),
+        "dm_depolarizing_2q_df64_hbm_frac": get(line, "density_matrix", "df64_n13", "depolarizing_2q", "frac_of_hbm"),
     }
+
+
 def run_adjoint_bench(args, torch):
     """Adjoint gradients of the 20-qubit, 10-layer RY/RZ + CZ-ring ansatz (400 parameters,
     observable sum_i Z_i Z_{i+1} periodic) for a batch of 64 parameter sets, against the
@@ -972,9 +977,10 @@ def run_dm_bench(args, torch, cpu: bool):
     ad = llgpu.amplitude_damping(0.01)
     dp = llgpu.depolarizing(0.01, 2)
     out = {"workload": "density matrices: amplitude damping on every qubit and 2-qubit depolarizing on "
-                       "neighbouring pairs, complex128"}
-    for n in (10, 13):
-        dm = llgpu.DensityMatrix(n, "complex128")
+                       "neighbouring pairs, complex128 (IEEE FP64); df64_n13: the 13-qubit case in double-float, "
+                       "whose 2-qubit channels run on the tensor cores"}
+    for prec, n in (("complex128", 10), ("complex128", 13), ("df64", 13)):
+        dm = llgpu.DensityMatrix(n, prec)
         dm.apply_ops(llgpu.make_ops([(llgpu.OP_H, q) for q in range(n)] + [(llgpu.OP_RX, q, 0, 0.3 * q) for q in range(n)]))
         st = dm.state
         res = {"state_bytes": 16 << (2 * n)}
@@ -1002,7 +1008,7 @@ def run_dm_bench(args, torch, cpu: bool):
         tr = dm.trace()
         res["trace_minus_1"] = abs(tr - 1.0)
         dm.close()
-        out[f"n{n}"] = res
+        out[f"n{n}" if prec == "complex128" else f"{prec}_n{n}"] = res
     if cpu:
         # the oracle's restatement timed on one channel of each kind at the reference's size; its
         # result is also compared with the GPU's on the same input
@@ -1079,7 +1085,7 @@ def run_e2e(args, precision, ops, xops, table_bytes, n, elem, world, torch):
 
     sv = quantum_sim_v3.StateVector(n, precision)
     if args.tile < 0:
-        sv.autotune(ops, 2 * len(ops) // max(1, args.layers))  # the headline's tuning, from the cache
+        sv.autotune(ops, 4 * len(ops) // max(1, args.layers))  # the headline's tuning, from the cache
     else:
         sv.set_fusion("tile", args.tile)
     sv.apply_ops(ops)
