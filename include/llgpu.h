@@ -238,13 +238,16 @@ int llg_expect_diagonal(llg_state* st, const double* diag, int on_device, double
  * callers whose device memory belongs to another allocator (a framework that reserves most of
  * the GPU up front) and callers in latency-critical loops where cudaMalloc/cudaFree would
  * synchronise the device.  The caller passes the amplitudes (d_amps: 2^n elements in the
- * `precision` layout, device or managed memory it owns) and d_out (2 device doubles, receiving
+ * `precision` layout, memory of the current device or managed memory; another device's memory is
+ * LLG_EINVAL) and d_out (2 device doubles, receiving
  * [sum_k coeff_k <Z..>, sum |a|^2]); kernels are enqueued on `stream` (a cudaStream_t, NULL for
  * the default stream) and the call returns without waiting.  Nothing is allocated: the partial
  * sums go to a fixed 40 KiB device array inside the library (1024 blocks x 5 doubles), held by
  * every GPU that loads it until exit.  The first call on a device resolves that array's address
  * and should come before any stream capture on that device.  All calls share the array; each
- * call writes every partial it reads, but calls that overlap on the GPU race.  Limits:
+ * call writes every partial it reads, but calls that overlap on the GPU race.  The array's
+ * address is cached per device for the process: do not call this after cudaDeviceReset.  A CUDA
+ * error already pending before the call is returned as LLG_ECUDA without launching.  Limits:
  * n_qubits in [1, 34], at most 64 terms with at most 4 distinct coefficients. */
 int llg_expect_zz_noalloc(const void* d_amps, int n_qubits, int precision, int nterms, const int* a, const int* b,
                           const double* coeff, double* d_out, void* stream);
