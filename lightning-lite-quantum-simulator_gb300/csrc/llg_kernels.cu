@@ -173,6 +173,96 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     return done != 0;
 }
 
+// complex64 tiles: two amplitudes per 16-byte shared-memory access.  For a target q >= 1 the
+// amplitudes 2f and 2f + 1 share every bit but bit 0, so the float4 at f pairs with the float4 at
+// f | 2^(q-1): two pairs per two loads and two stores, one index computation.  For q = 0 a float4
+// is one pair.  Needs the tile 16-byte aligned (k_tile's dynamic shared memory is).
+template <class P, int KIND>
+__device__ __forceinline__ void tile_pairs_f32x2(typename P::S* tile, uint32_t tsize, int q, const ExecOp& o) {
+    static_assert(sizeof(typename P::S) == 8, "complex64 tiles only");
+    const PairMath<P, KIND> m(o);
+    float4* t4 = reinterpret_cast<float4*>(tile);
+    if (q == 0) {
+        for (uint32_t f = threadIdx.x; f < (tsize >> 1); f += blockDim.x) {
+            const float4 v = t4[f];
+            auto a0 = P::load(make_float2(v.x, v.y));
+            auto a1 = P::load(make_float2(v.z, v.w));
+            m.apply(a0, a1);
+            const float2 s0 = P::store(a0), s1 = P::store(a1);
+            t4[f] = make_float4(s0.x, s0.y, s1.x, s1.y);
+        }
+        return;
+    }
+    const uint32_t fbit = 1u << (q - 1);
+    for (uint32_t p = threadIdx.x; p < (tsize >> 2); p += blockDim.x) {
+        const uint32_t f0 = ins0(p, fbit), f1 = f0 | fbit;
+        const float4 u = t4[f0], v = t4[f1];
+        auto a0 = P::load(make_float2(u.x, u.y)), b0 = P::load(make_float2(u.z, u.w));
+        auto a1 = P::load(make_float2(v.x, v.y)), b1 = P::load(make_float2(v.z, v.w));
+        m.apply(a0, a1);
+        m.apply(b0, b1);
+        const float2 sa0 = P::store(a0), sb0 = P::store(b0), sa1 = P::store(a1), sb1 = P::store(b1);
+        t4[f0] = make_float4(sa0.x, sa0.y, sb0.x, sb0.y);
+        t4[f1] = make_float4(sa1.x, sa1.y, sb1.x, sb1.y);
+    }
+}
+
+// complex64 CNOT with control and target on tile bits >= 1 (or a tile-uniform control): the swaps
+// move float4s (two amplitudes that differ in bit 0 only); with OPF_PHASE the float4 that ends at
+// control = target = 1 is multiplied by c[0] + i c[1].  False: not this form, nothing done.
+template <class P>
+__device__ __forceinline__ bool tile_cnot_f32x2(typename P::S* tile, uint32_t tsize, uint64_t base, const ExecOp& o) {
+    static_assert(sizeof(typename P::S) == 8, "complex64 tiles only");
+    using K = typename P::K;
+    const int tq = o.q1;
+    const bool nonlocal = (o.flags & OPF_NONLOCAL_Q0) != 0;
+    if (tsize < 8 || tq == 0 || (!nonlocal && o.q0 == 0)) return false;
+    const bool phased = (o.flags & OPF_PHASE) != 0;
+    const K pr = P::k_from_bits(o.c[0]), pi = P::k_from_bits(o.c[1]), mpi = P::kneg(pi);
+    float4* t4 = reinterpret_cast<float4*>(tile);
+    const uint32_t tb = 1u << (tq - 1);
+    auto moved = [&](float4 v) {  // the phase on both amplitudes of a float4 landing at (1, 1)
+        if (!phased) return v;
+        auto a = P::load(make_float2(v.x, v.y)), b = P::load(make_float2(v.z, v.w));
+        cmul_const<P>(a, pr, pi, mpi);
+        cmul_const<P>(b, pr, pi, mpi);
+        const float2 sa = P::store(a), sb = P::store(b);
+        return make_float4(sa.x, sa.y, sb.x, sb.y);
+    };
+    if (nonlocal) {
+        if (!((base >> o.q0) & 1)) return true;
+        for (uint32_t p = threadIdx.x; p < (tsize >> 2); p += blockDim.x) {
+            const uint32_t f0 = ins0(p, tb), f1 = f0 | tb;
+            const float4 x = t4[f0];
+            t4[f0] = t4[f1];
+            t4[f1] = moved(x);
+        }
+        return true;
+    }
+    const int c = o.q0;
+    const uint32_t cb = 1u << (c - 1);
+    const uint32_t lo = cb < tb ? cb : tb, hi = cb < tb ? tb : cb;
+    for (uint32_t r = threadIdx.x; r < (tsize >> 3); r += blockDim.x) {
+        const uint32_t f = ins0(ins0(r, lo), hi) | cb;
+        const float4 x = t4[f];
+        t4[f] = t4[f | tb];
+        t4[f | tb] = moved(x);
+    }
+    return true;
+}
+
+// the pair ops of k_tile: complex64 through the two-amplitude form, the 16-byte formats as is
+template <class P, int KIND>
+__device__ __forceinline__ void tile_pairs_k(typename P::S* tile, uint32_t tsize, int q, const ExecOp& o) {
+    if constexpr (sizeof(typename P::S) == 8) {
+        if (tsize >= 4) {
+            tile_pairs_f32x2<P, KIND>(tile, tsize, q, o);
+            return;
+        }
+    }
+    tile_pairs<P, KIND>(tile, tsize >> 1, q, o);
+}
+
 template <class P>
 __global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, PassDesc pd, const ExecOp* __restrict__ ops,
                                                const uint64_t* __restrict__ tables, double2* __restrict__ mirror,
@@ -243,19 +333,19 @@ __global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, 
         const ExecOp& o = sops[k % kOpChunk];
         const int kind = o.kind;
         switch (kind) {
-            case EX_U2: tile_pairs<P, EX_U2>(tile, tsize >> 1, o.q0, o); break;
-            case EX_ZYZ: tile_pairs<P, EX_ZYZ>(tile, tsize >> 1, o.q0, o); break;
-            case EX_ZY: tile_pairs<P, EX_ZY>(tile, tsize >> 1, o.q0, o); break;
-            case EX_ZT: tile_pairs<P, EX_ZT>(tile, tsize >> 1, o.q0, o); break;
-            case EX_ZC: tile_pairs<P, EX_ZC>(tile, tsize >> 1, o.q0, o); break;
-            case EX_RT: tile_pairs<P, EX_RT>(tile, tsize >> 1, o.q0, o); break;
-            case EX_RC: tile_pairs<P, EX_RC>(tile, tsize >> 1, o.q0, o); break;
+            case EX_U2: tile_pairs_k<P, EX_U2>(tile, tsize, o.q0, o); break;
+            case EX_ZYZ: tile_pairs_k<P, EX_ZYZ>(tile, tsize, o.q0, o); break;
+            case EX_ZY: tile_pairs_k<P, EX_ZY>(tile, tsize, o.q0, o); break;
+            case EX_ZT: tile_pairs_k<P, EX_ZT>(tile, tsize, o.q0, o); break;
+            case EX_ZC: tile_pairs_k<P, EX_ZC>(tile, tsize, o.q0, o); break;
+            case EX_RT: tile_pairs_k<P, EX_RT>(tile, tsize, o.q0, o); break;
+            case EX_RC: tile_pairs_k<P, EX_RC>(tile, tsize, o.q0, o); break;
             case EX_PTAB: tile_ptab<P>(tile, tsize, o, tables); break;
             case EX_PHASE1: tile_phase1<P>(tile, tsize, base, o); break;
-            case EX_RX: tile_pairs<P, EX_RX>(tile, tsize >> 1, o.q0, o); break;
-            case EX_RY: tile_pairs<P, EX_RY>(tile, tsize >> 1, o.q0, o); break;
-            case EX_H: tile_pairs<P, EX_H>(tile, tsize >> 1, o.q0, o); break;
-            case EX_X: tile_pairs<P, EX_X>(tile, tsize >> 1, o.q0, o); break;
+            case EX_RX: tile_pairs_k<P, EX_RX>(tile, tsize, o.q0, o); break;
+            case EX_RY: tile_pairs_k<P, EX_RY>(tile, tsize, o.q0, o); break;
+            case EX_H: tile_pairs_k<P, EX_H>(tile, tsize, o.q0, o); break;
+            case EX_X: tile_pairs_k<P, EX_X>(tile, tsize, o.q0, o); break;
             case EX_DIAG: {
                 const K d0r = P::k_from_bits(o.c[0]), d0i = P::k_from_bits(o.c[1]);
                 const K d1r = P::k_from_bits(o.c[2]), d1i = P::k_from_bits(o.c[3]);
@@ -280,7 +370,12 @@ __global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, 
                 }
                 break;
             }
-            case EX_CNOT: tile_cnot<P>(tile, tsize, base, o); break;
+            case EX_CNOT:
+                if constexpr (sizeof(S) == 8) {
+                    if (tile_cnot_f32x2<P>(tile, tsize, base, o)) break;
+                }
+                tile_cnot<P>(tile, tsize, base, o);
+                break;
             case EX_MCZ: {
                 if ((base & o.nl_mask) == o.nl_mask) {
                     const uint32_t lm = (uint32_t)o.mask;
