@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(kThreads) k_mcz(typename P::S* __restrict__ ps
 // ------------------------------------------------------------------------------------------
 // tile pass
 // ------------------------------------------------------------------------------------------
-constexpr int kOpChunk = 32;  // op records staged per shared-memory chunk in k_tile
+constexpr int kOpChunk = kTileOpChunk;  // op records staged per shared-memory chunk in k_tile
 constexpr long kTileCopyWaitLimit = 1L << 24;  // mbarrier polls before a tile load is reported as timed out
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -249,6 +249,107 @@ __device__ __forceinline__ bool tile_cnot_f32x2(typename P::S* tile, uint32_t ts
         t4[f | tb] = moved(x);
     }
     return true;
+}
+
+// ------------------------------------------------------------------------------------------
+// EX_GROUP (group_tile_ops): a run of ops on three local qubits g0 < g1 < g2 runs on octets.  A
+// thread loads the 8 amplitudes over those qubits (register e holds local index i0 | bits of e on
+// g0, g1, g2), applies every op of the run in registers with its pair pattern fixed at compile
+// time, and stores them: one shared-memory round trip and one barrier for the run instead of one
+// per op.
+// ------------------------------------------------------------------------------------------
+template <class P, int KIND, int J>
+__device__ __forceinline__ void octet_pairs(typename P::C (&a)[8], const ExecOp& o) {
+    const PairMath<P, KIND> m(o);
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+        if (!(e & (1 << J))) m.apply(a[e], a[e | (1 << J)]);
+}
+
+template <class P, int KIND>
+__device__ __forceinline__ void octet_pairs_slot(typename P::C (&a)[8], int j, const ExecOp& o) {
+    if (j == 0) octet_pairs<P, KIND, 0>(a, o);
+    else if (j == 1) octet_pairs<P, KIND, 1>(a, o);
+    else octet_pairs<P, KIND, 2>(a, o);
+}
+
+// CNOT with target slot J and control slot K (K < 0: a tile-uniform global control, `on`); with
+// OPF_PHASE the amplitude that lands at control = target = 1 is multiplied by c[0] + i c[1]
+template <class P, int J, int K>
+__device__ __forceinline__ void octet_cnot(typename P::C (&a)[8], const ExecOp& o, bool on) {
+    using Kt = typename P::K;
+    using C = typename P::C;
+    if (K < 0 && !on) return;
+    constexpr int KB = K < 0 ? 0 : (1 << (K < 0 ? 0 : K));
+    const bool phased = (o.flags & OPF_PHASE) != 0;
+    const Kt pr = P::k_from_bits(o.c[0]), pi = P::k_from_bits(o.c[1]), mpi = P::kneg(pi);
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+        if (!(e & (1 << J)) && (K < 0 || (e & KB))) {
+            const C x = a[e];
+            a[e] = a[e | (1 << J)];
+            a[e | (1 << J)] = x;
+            if (phased) cmul_const<P>(a[e | (1 << J)], pr, pi, mpi);
+        }
+}
+
+template <class P>
+__device__ __forceinline__ void octet_cnot_slots(typename P::C (&a)[8], int jt, int jc, const ExecOp& o, bool on) {
+    switch (jt * 4 + (jc + 1)) {  // jc = -1: global control
+        case 0: octet_cnot<P, 0, -1>(a, o, on); break;
+        case 2: octet_cnot<P, 0, 1>(a, o, on); break;
+        case 3: octet_cnot<P, 0, 2>(a, o, on); break;
+        case 4: octet_cnot<P, 1, -1>(a, o, on); break;
+        case 5: octet_cnot<P, 1, 0>(a, o, on); break;
+        case 7: octet_cnot<P, 1, 2>(a, o, on); break;
+        case 8: octet_cnot<P, 2, -1>(a, o, on); break;
+        case 9: octet_cnot<P, 2, 0>(a, o, on); break;
+        case 10: octet_cnot<P, 2, 1>(a, o, on); break;
+        default: break;
+    }
+}
+
+template <class P>
+__device__ __forceinline__ void tile_group(typename P::S* tile, uint32_t tsize, uint64_t base, const ExecOp& h,
+                                           const ExecOp* sub) {
+    using C = typename P::C;
+    const uint32_t m = (uint32_t)h.mask;
+    const uint32_t b0 = m & (0u - m), m1 = m ^ b0, b1 = m1 & (0u - m1), b2 = m1 ^ b1;
+    const int g0 = __ffs(b0) - 1, g1 = __ffs(b1) - 1;
+    const int nsub = h.q0;
+    auto slot = [&](int q) { return q == g0 ? 0 : (q == g1 ? 1 : 2); };
+    for (uint32_t r = threadIdx.x; r < (tsize >> 3); r += blockDim.x) {
+        const uint32_t i0 = ins0(ins0(ins0(r, b0), b1), b2);
+        C a[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+            a[e] = P::load(tile[i0 | ((e & 1) ? b0 : 0u) | ((e & 2) ? b1 : 0u) | ((e & 4) ? b2 : 0u)]);
+        for (int s = 0; s < nsub; ++s) {
+            const ExecOp& o = sub[s];
+            switch (o.kind) {
+                case EX_U2: octet_pairs_slot<P, EX_U2>(a, slot(o.q0), o); break;
+                case EX_ZYZ: octet_pairs_slot<P, EX_ZYZ>(a, slot(o.q0), o); break;
+                case EX_ZY: octet_pairs_slot<P, EX_ZY>(a, slot(o.q0), o); break;
+                case EX_ZT: octet_pairs_slot<P, EX_ZT>(a, slot(o.q0), o); break;
+                case EX_ZC: octet_pairs_slot<P, EX_ZC>(a, slot(o.q0), o); break;
+                case EX_RT: octet_pairs_slot<P, EX_RT>(a, slot(o.q0), o); break;
+                case EX_RC: octet_pairs_slot<P, EX_RC>(a, slot(o.q0), o); break;
+                case EX_RX: octet_pairs_slot<P, EX_RX>(a, slot(o.q0), o); break;
+                case EX_RY: octet_pairs_slot<P, EX_RY>(a, slot(o.q0), o); break;
+                case EX_H: octet_pairs_slot<P, EX_H>(a, slot(o.q0), o); break;
+                case EX_X: octet_pairs_slot<P, EX_X>(a, slot(o.q0), o); break;
+                case EX_CNOT: {
+                    const bool global = (o.flags & OPF_NONLOCAL_Q0) != 0;
+                    octet_cnot_slots<P>(a, slot(o.q1), global ? -1 : slot(o.q0), o, global && ((base >> o.q0) & 1));
+                    break;
+                }
+                default: break;
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+            tile[i0 | ((e & 1) ? b0 : 0u) | ((e & 2) ? b1 : 0u) | ((e & 4) ? b2 : 0u)] = P::store(a[e]);
+    }
 }
 
 // the pair ops of k_tile: complex64 through the two-amplitude form, the 16-byte formats as is
@@ -375,6 +476,19 @@ __global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, 
                     if (tile_cnot_f32x2<P>(tile, tsize, base, o)) break;
                 }
                 tile_cnot<P>(tile, tsize, base, o);
+                break;
+            case EX_GROUP:
+                // complex64 tiles run the group on octets; anywhere else (or for a header that
+                // does not fit its chunk or the tile) the header is a no-op and its ops run one
+                // by one, which is the same product
+                if constexpr (sizeof(S) == 8) {
+                    const uint32_t gm = (uint32_t)o.mask;
+                    if (o.q0 >= 1 && (k % kOpChunk) + o.q0 < kOpChunk && (o.mask >> 32) == 0 && __popc(gm) == 3 &&
+                        gm < tsize) {
+                        tile_group<P>(tile, tsize, base, o, &sops[(k % kOpChunk) + 1]);
+                        k += o.q0;
+                    }
+                }
                 break;
             case EX_MCZ: {
                 if ((base & o.nl_mask) == o.nl_mask) {
