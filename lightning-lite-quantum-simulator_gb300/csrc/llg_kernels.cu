@@ -258,25 +258,29 @@ __device__ __forceinline__ bool tile_cnot_f32x2(typename P::S* tile, uint32_t ts
 // time, and stores them: one shared-memory round trip and one barrier for the run instead of one
 // per op.
 // ------------------------------------------------------------------------------------------
-template <class P, int KIND, int J>
-__device__ __forceinline__ void octet_pairs(typename P::C (&a)[8], const ExecOp& o) {
+// Each thread holds NO octets (the tile's octets split evenly over the CTA), so an op's record is
+// read and dispatched once per thread, not once per octet.
+template <class P, int KIND, int J, int NO>
+__device__ __forceinline__ void octet_pairs(typename P::C (&a)[NO][8], const ExecOp& o) {
     const PairMath<P, KIND> m(o);
 #pragma unroll
-    for (int e = 0; e < 8; ++e)
-        if (!(e & (1 << J))) m.apply(a[e], a[e | (1 << J)]);
+    for (int n = 0; n < NO; ++n)
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+            if (!(e & (1 << J))) m.apply(a[n][e], a[n][e | (1 << J)]);
 }
 
-template <class P, int KIND>
-__device__ __forceinline__ void octet_pairs_slot(typename P::C (&a)[8], int j, const ExecOp& o) {
-    if (j == 0) octet_pairs<P, KIND, 0>(a, o);
-    else if (j == 1) octet_pairs<P, KIND, 1>(a, o);
-    else octet_pairs<P, KIND, 2>(a, o);
+template <class P, int KIND, int NO>
+__device__ __forceinline__ void octet_pairs_slot(typename P::C (&a)[NO][8], int j, const ExecOp& o) {
+    if (j == 0) octet_pairs<P, KIND, 0, NO>(a, o);
+    else if (j == 1) octet_pairs<P, KIND, 1, NO>(a, o);
+    else octet_pairs<P, KIND, 2, NO>(a, o);
 }
 
 // CNOT with target slot J and control slot K (K < 0: a tile-uniform global control, `on`); with
 // OPF_PHASE the amplitude that lands at control = target = 1 is multiplied by c[0] + i c[1]
-template <class P, int J, int K>
-__device__ __forceinline__ void octet_cnot(typename P::C (&a)[8], const ExecOp& o, bool on) {
+template <class P, int J, int K, int NO>
+__device__ __forceinline__ void octet_cnot(typename P::C (&a)[NO][8], const ExecOp& o, bool on) {
     using Kt = typename P::K;
     using C = typename P::C;
     if (K < 0 && !on) return;
@@ -284,72 +288,76 @@ __device__ __forceinline__ void octet_cnot(typename P::C (&a)[8], const ExecOp& 
     const bool phased = (o.flags & OPF_PHASE) != 0;
     const Kt pr = P::k_from_bits(o.c[0]), pi = P::k_from_bits(o.c[1]), mpi = P::kneg(pi);
 #pragma unroll
-    for (int e = 0; e < 8; ++e)
-        if (!(e & (1 << J)) && (K < 0 || (e & KB))) {
-            const C x = a[e];
-            a[e] = a[e | (1 << J)];
-            a[e | (1 << J)] = x;
-            if (phased) cmul_const<P>(a[e | (1 << J)], pr, pi, mpi);
-        }
+    for (int n = 0; n < NO; ++n)
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+            if (!(e & (1 << J)) && (K < 0 || (e & KB))) {
+                const C x = a[n][e];
+                a[n][e] = a[n][e | (1 << J)];
+                a[n][e | (1 << J)] = x;
+                if (phased) cmul_const<P>(a[n][e | (1 << J)], pr, pi, mpi);
+            }
 }
 
-template <class P>
-__device__ __forceinline__ void octet_cnot_slots(typename P::C (&a)[8], int jt, int jc, const ExecOp& o, bool on) {
+template <class P, int NO>
+__device__ __forceinline__ void octet_cnot_slots(typename P::C (&a)[NO][8], int jt, int jc, const ExecOp& o, bool on) {
     switch (jt * 4 + (jc + 1)) {  // jc = -1: global control
-        case 0: octet_cnot<P, 0, -1>(a, o, on); break;
-        case 2: octet_cnot<P, 0, 1>(a, o, on); break;
-        case 3: octet_cnot<P, 0, 2>(a, o, on); break;
-        case 4: octet_cnot<P, 1, -1>(a, o, on); break;
-        case 5: octet_cnot<P, 1, 0>(a, o, on); break;
-        case 7: octet_cnot<P, 1, 2>(a, o, on); break;
-        case 8: octet_cnot<P, 2, -1>(a, o, on); break;
-        case 9: octet_cnot<P, 2, 0>(a, o, on); break;
-        case 10: octet_cnot<P, 2, 1>(a, o, on); break;
+        case 0: octet_cnot<P, 0, -1, NO>(a, o, on); break;
+        case 2: octet_cnot<P, 0, 1, NO>(a, o, on); break;
+        case 3: octet_cnot<P, 0, 2, NO>(a, o, on); break;
+        case 4: octet_cnot<P, 1, -1, NO>(a, o, on); break;
+        case 5: octet_cnot<P, 1, 0, NO>(a, o, on); break;
+        case 7: octet_cnot<P, 1, 2, NO>(a, o, on); break;
+        case 8: octet_cnot<P, 2, -1, NO>(a, o, on); break;
+        case 9: octet_cnot<P, 2, 0, NO>(a, o, on); break;
+        case 10: octet_cnot<P, 2, 1, NO>(a, o, on); break;
         default: break;
     }
 }
 
-template <class P>
-__device__ __forceinline__ void tile_group(typename P::S* tile, uint32_t tsize, uint64_t base, const ExecOp& h,
-                                           const ExecOp* sub) {
+// the run on octets r = threadIdx.x + n * blockDim.x, n < NO (NO * blockDim.x octets in all)
+template <class P, int NO>
+__device__ __forceinline__ void tile_group(typename P::S* tile, uint64_t base, const ExecOp& h, const ExecOp* sub) {
     using C = typename P::C;
     const uint32_t m = (uint32_t)h.mask;
     const uint32_t b0 = m & (0u - m), m1 = m ^ b0, b1 = m1 & (0u - m1), b2 = m1 ^ b1;
     const int g0 = __ffs(b0) - 1, g1 = __ffs(b1) - 1;
-    const int nsub = h.q0;
     auto slot = [&](int q) { return q == g0 ? 0 : (q == g1 ? 1 : 2); };
-    for (uint32_t r = threadIdx.x; r < (tsize >> 3); r += blockDim.x) {
-        const uint32_t i0 = ins0(ins0(ins0(r, b0), b1), b2);
-        C a[8];
+    auto at = [&](int n, int e) {
+        const uint32_t r = threadIdx.x + (uint32_t)n * blockDim.x;
+        return ins0(ins0(ins0(r, b0), b1), b2) | ((e & 1) ? b0 : 0u) | ((e & 2) ? b1 : 0u) | ((e & 4) ? b2 : 0u);
+    };
+    C a[NO][8];
 #pragma unroll
-        for (int e = 0; e < 8; ++e)
-            a[e] = P::load(tile[i0 | ((e & 1) ? b0 : 0u) | ((e & 2) ? b1 : 0u) | ((e & 4) ? b2 : 0u)]);
-        for (int s = 0; s < nsub; ++s) {
-            const ExecOp& o = sub[s];
-            switch (o.kind) {
-                case EX_U2: octet_pairs_slot<P, EX_U2>(a, slot(o.q0), o); break;
-                case EX_ZYZ: octet_pairs_slot<P, EX_ZYZ>(a, slot(o.q0), o); break;
-                case EX_ZY: octet_pairs_slot<P, EX_ZY>(a, slot(o.q0), o); break;
-                case EX_ZT: octet_pairs_slot<P, EX_ZT>(a, slot(o.q0), o); break;
-                case EX_ZC: octet_pairs_slot<P, EX_ZC>(a, slot(o.q0), o); break;
-                case EX_RT: octet_pairs_slot<P, EX_RT>(a, slot(o.q0), o); break;
-                case EX_RC: octet_pairs_slot<P, EX_RC>(a, slot(o.q0), o); break;
-                case EX_RX: octet_pairs_slot<P, EX_RX>(a, slot(o.q0), o); break;
-                case EX_RY: octet_pairs_slot<P, EX_RY>(a, slot(o.q0), o); break;
-                case EX_H: octet_pairs_slot<P, EX_H>(a, slot(o.q0), o); break;
-                case EX_X: octet_pairs_slot<P, EX_X>(a, slot(o.q0), o); break;
-                case EX_CNOT: {
-                    const bool global = (o.flags & OPF_NONLOCAL_Q0) != 0;
-                    octet_cnot_slots<P>(a, slot(o.q1), global ? -1 : slot(o.q0), o, global && ((base >> o.q0) & 1));
-                    break;
-                }
-                default: break;
+    for (int n = 0; n < NO; ++n)
+#pragma unroll
+        for (int e = 0; e < 8; ++e) a[n][e] = P::load(tile[at(n, e)]);
+    for (int s = 0; s < h.q0; ++s) {
+        const ExecOp& o = sub[s];
+        switch (o.kind) {
+            case EX_U2: octet_pairs_slot<P, EX_U2, NO>(a, slot(o.q0), o); break;
+            case EX_ZYZ: octet_pairs_slot<P, EX_ZYZ, NO>(a, slot(o.q0), o); break;
+            case EX_ZY: octet_pairs_slot<P, EX_ZY, NO>(a, slot(o.q0), o); break;
+            case EX_ZT: octet_pairs_slot<P, EX_ZT, NO>(a, slot(o.q0), o); break;
+            case EX_ZC: octet_pairs_slot<P, EX_ZC, NO>(a, slot(o.q0), o); break;
+            case EX_RT: octet_pairs_slot<P, EX_RT, NO>(a, slot(o.q0), o); break;
+            case EX_RC: octet_pairs_slot<P, EX_RC, NO>(a, slot(o.q0), o); break;
+            case EX_RX: octet_pairs_slot<P, EX_RX, NO>(a, slot(o.q0), o); break;
+            case EX_RY: octet_pairs_slot<P, EX_RY, NO>(a, slot(o.q0), o); break;
+            case EX_H: octet_pairs_slot<P, EX_H, NO>(a, slot(o.q0), o); break;
+            case EX_X: octet_pairs_slot<P, EX_X, NO>(a, slot(o.q0), o); break;
+            case EX_CNOT: {
+                const bool global = (o.flags & OPF_NONLOCAL_Q0) != 0;
+                octet_cnot_slots<P, NO>(a, slot(o.q1), global ? -1 : slot(o.q0), o, global && ((base >> o.q0) & 1));
+                break;
             }
+            default: break;
         }
-#pragma unroll
-        for (int e = 0; e < 8; ++e)
-            tile[i0 | ((e & 1) ? b0 : 0u) | ((e & 2) ? b1 : 0u) | ((e & 4) ? b2 : 0u)] = P::store(a[e]);
     }
+#pragma unroll
+    for (int n = 0; n < NO; ++n)
+#pragma unroll
+        for (int e = 0; e < 8; ++e) tile[at(n, e)] = P::store(a[n][e]);
 }
 
 // the pair ops of k_tile: complex64 through the two-amplitude form, the 16-byte formats as is
@@ -364,8 +372,14 @@ __device__ __forceinline__ void tile_pairs_k(typename P::S* tile, uint32_t tsize
     tile_pairs<P, KIND>(tile, tsize >> 1, q, o);
 }
 
+// CTA size limit of k_tile: complex64 tiles keep up to 4 octets of a run in registers per thread
 template <class P>
-__global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, PassDesc pd, const ExecOp* __restrict__ ops,
+struct TileMaxThreads {
+    static constexpr int value = sizeof(typename P::S) == 8 ? 512 : 1024;
+};
+
+template <class P>
+__global__ void __launch_bounds__(TileMaxThreads<P>::value) k_tile(typename P::S* __restrict__ psi, PassDesc pd, const ExecOp* __restrict__ ops,
                                                const uint64_t* __restrict__ tables, double2* __restrict__ mirror,
                                                int* __restrict__ err_flag) {
     using S = typename P::S;
@@ -483,9 +497,12 @@ __global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, 
                 // by one, which is the same product
                 if constexpr (sizeof(S) == 8) {
                     const uint32_t gm = (uint32_t)o.mask;
+                    const uint32_t per = (tsize >> 3) / blockDim.x;  // octets per thread
                     if (o.q0 >= 1 && (k % kOpChunk) + o.q0 < kOpChunk && (o.mask >> 32) == 0 && __popc(gm) == 3 &&
-                        gm < tsize) {
-                        tile_group<P>(tile, tsize, base, o, &sops[(k % kOpChunk) + 1]);
+                        gm < tsize && per * blockDim.x == (tsize >> 3) && (per == 1 || per == 2)) {
+                        const ExecOp* sub = &sops[(k % kOpChunk) + 1];
+                        if (per == 2) tile_group<P, 2>(tile, base, o, sub);
+                        else tile_group<P, 1>(tile, base, o, sub);
                         k += o.q0;
                     }
                 }
@@ -714,6 +731,7 @@ cudaError_t tile_pass_t(void* vpsi, int n, const PassDesc& pd, const ExecOp* d_o
     const size_t smem = tile_smem_bytes<P>(pd.t, pd.low);
     const uint64_t ntiles = 1ULL << (n - pd.t);
     if (threads <= 0) threads = pd.t >= 10 ? 512 : (pd.t >= 6 ? (1 << (pd.t - 1)) : 32);
+    threads = std::min(threads, TileMaxThreads<P>::value);
     k_tile<P><<<(unsigned)ntiles, threads, smem, s>>>(static_cast<typename P::S*>(vpsi), pd, d_ops, d_tables,
                                                       reinterpret_cast<double2*>(mirror), err_flag);
     return cudaGetLastError();
