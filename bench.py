@@ -311,15 +311,14 @@ def is_f64(precision: str) -> bool:
 
 def plan_for(precision: str, n: int, ops, tile_q: int, regs: bool = False):
     """The plan the engine runs: carried phases and phase tables for 16-byte precisions, carried
-    phases and op groups for complex64 shared-memory tiles, register programs for register-tiled
-    passes."""
+    phases alone for complex64 shared-memory tiles, register programs for register-tiled passes."""
     import llgpu
 
     if regs:
         p, x = llgpu.plan_export(n, ops, tile_q, zyz=True, regs=True)
         return p, x, 0
     if precision == "complex64":
-        p, x = llgpu.plan_export(n, ops, tile_q, zyz=True, groups=True)
+        p, x = llgpu.plan_export(n, ops, tile_q, zyz=True)
         return p, x, 0
     p, x, tab = llgpu.plan_export(n, ops, tile_q, zyz=True, tables=True)
     return p, x, int(tab.nbytes)

@@ -270,13 +270,13 @@ int run_tiles(llg_state* st, const std::vector<llg_op>& q, double* mirror = null
     Plan plan;
     std::string err;
     const int t = st->tile_qubits > 0 ? st->tile_qubits : default_tile(st->P);
-    // register-tiled passes on registers of 9+ qubits (smaller ones keep the shared-memory tiles)
+    // register-tiled passes on registers of 9+ qubits (smaller ones keep the shared-memory tiles);
+    // every precision plans carried-phase tangent rotations, the 16-byte ones also phase tables
     const bool reg = st->fuse_mode == LLG_FUSE_REG && std::min(st->n, std::min(t, 13)) >= 9;
     if (!plan_tiles(st->n, q.data(), (int)q.size(), reg ? std::min(t, 13) : std::min(t, tile_max_qubits(st->P)), st->P,
-                    plan, err, false, (reg || st->P == LLG_F32) ? ZYZ_ON : ZYZ_DEFAULT, !reg && st->P != LLG_F32))
+                    plan, err, false, ZYZ_ON, !reg && st->P != LLG_F32))
         return set_error(LLG_EINVAL, err);
     if (reg) to_register_program(plan);
-    else if (st->P == LLG_F32) group_tile_ops(plan);
     int rc = upload_ops(st, plan.ops, &plan.tables);
     if (rc) return rc;
     st->tiles_launched = true;
@@ -1165,9 +1165,6 @@ int export_plan(int n, const llg_op* ops, int nops, int tile_qubits, int flags, 
     if (flags & LLG_PLAN_REGS) {
         if (tile_qubits < 9) return set_error(LLG_EINVAL, "plan_export: register programs need tiles of 9+ qubits");
         to_register_program(plan);
-    } else if (flags & LLG_PLAN_GROUPS) {
-        if (flags & LLG_PLAN_TABLES) return set_error(LLG_EINVAL, "plan_export: groups are not combined with tables");
-        group_tile_ops(plan);
     }
     return LLG_OK;
 }

@@ -58,17 +58,7 @@ enum ExecKind : int32_t {
     // and are fixed by the thread index over the other t - 4 positions (nl_mask: 4 bits per thread
     // index bit, in order; q0 = t - 4).  The tile moves through shared memory once per layout.
     EX_LAYOUT = 19,
-    // op group (group_tile_ops): the next q0 ops act only on the three local qubits of `mask` (a
-    // CNOT's control may also be a global qubit).  A thread loads an octet of amplitudes over
-    // those qubits into registers, applies the q0 ops there in order and stores it: one
-    // shared-memory round trip and one barrier for the run.  A group never straddles a chunk of
-    // kTileOpChunk staged op records.
-    EX_GROUP = 20,
 };
-
-// op records the tile kernel stages through shared memory at a time (chunks start at multiples of
-// this within a pass)
-constexpr int kTileOpChunk = 32;
 
 // Flags of a tile op.
 enum : int32_t {
@@ -138,13 +128,6 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int precisi
 // position or a global qubit as before).  Every pass starts and ends in the layout whose register
 // positions are the top four tile positions.  Returns the number of layout changes.
 int to_register_program(Plan& plan);
-
-// Rewrites a tile plan (complex64 engine passes) with EX_GROUP runs: inside a pass, ops that act
-// on at most three local qubits are gathered greedily, an op joining a run only if it commutes
-// with every op it moves past (their qubits are disjoint); every other op keeps its order.  Pair
-// ops (U2, RX, RY, H, X, ZYZ, ZY, ZT, ZC, RT, RC) and CNOTs (control local or global) can join.
-// Returns the number of ops placed in groups.
-int group_tile_ops(Plan& plan);
 
 // Dense dispatch codes of register-program ops, in flags >> kRegCodeShift: one jump table in the
 // kernel selects the kind and its register slots together.

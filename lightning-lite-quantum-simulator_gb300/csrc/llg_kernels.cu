@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(kThreads) k_mcz(typename P::S* __restrict__ ps
 // ------------------------------------------------------------------------------------------
 // tile pass
 // ------------------------------------------------------------------------------------------
-constexpr int kOpChunk = kTileOpChunk;  // op records staged per shared-memory chunk in k_tile
+constexpr int kOpChunk = 32;  // op records staged per shared-memory chunk in k_tile
 constexpr long kTileCopyWaitLimit = 1L << 24;  // mbarrier polls before a tile load is reported as timed out
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -173,213 +173,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     return done != 0;
 }
 
-// complex64 tiles: two amplitudes per 16-byte shared-memory access.  For a target q >= 1 the
-// amplitudes 2f and 2f + 1 share every bit but bit 0, so the float4 at f pairs with the float4 at
-// f | 2^(q-1): two pairs per two loads and two stores, one index computation.  For q = 0 a float4
-// is one pair.  Needs the tile 16-byte aligned (k_tile's dynamic shared memory is).
-template <class P, int KIND>
-__device__ __forceinline__ void tile_pairs_f32x2(typename P::S* tile, uint32_t tsize, int q, const ExecOp& o) {
-    static_assert(sizeof(typename P::S) == 8, "complex64 tiles only");
-    const PairMath<P, KIND> m(o);
-    float4* t4 = reinterpret_cast<float4*>(tile);
-    if (q == 0) {
-        for (uint32_t f = threadIdx.x; f < (tsize >> 1); f += blockDim.x) {
-            const float4 v = t4[f];
-            auto a0 = P::load(make_float2(v.x, v.y));
-            auto a1 = P::load(make_float2(v.z, v.w));
-            m.apply(a0, a1);
-            const float2 s0 = P::store(a0), s1 = P::store(a1);
-            t4[f] = make_float4(s0.x, s0.y, s1.x, s1.y);
-        }
-        return;
-    }
-    const uint32_t fbit = 1u << (q - 1);
-    for (uint32_t p = threadIdx.x; p < (tsize >> 2); p += blockDim.x) {
-        const uint32_t f0 = ins0(p, fbit), f1 = f0 | fbit;
-        const float4 u = t4[f0], v = t4[f1];
-        auto a0 = P::load(make_float2(u.x, u.y)), b0 = P::load(make_float2(u.z, u.w));
-        auto a1 = P::load(make_float2(v.x, v.y)), b1 = P::load(make_float2(v.z, v.w));
-        m.apply(a0, a1);
-        m.apply(b0, b1);
-        const float2 sa0 = P::store(a0), sb0 = P::store(b0), sa1 = P::store(a1), sb1 = P::store(b1);
-        t4[f0] = make_float4(sa0.x, sa0.y, sb0.x, sb0.y);
-        t4[f1] = make_float4(sa1.x, sa1.y, sb1.x, sb1.y);
-    }
-}
-
-// complex64 CNOT with control and target on tile bits >= 1 (or a tile-uniform control): the swaps
-// move float4s (two amplitudes that differ in bit 0 only); with OPF_PHASE the float4 that ends at
-// control = target = 1 is multiplied by c[0] + i c[1].  False: not this form, nothing done.
 template <class P>
-__device__ __forceinline__ bool tile_cnot_f32x2(typename P::S* tile, uint32_t tsize, uint64_t base, const ExecOp& o) {
-    static_assert(sizeof(typename P::S) == 8, "complex64 tiles only");
-    using K = typename P::K;
-    const int tq = o.q1;
-    const bool nonlocal = (o.flags & OPF_NONLOCAL_Q0) != 0;
-    if (tsize < 8 || tq == 0 || (!nonlocal && o.q0 == 0)) return false;
-    const bool phased = (o.flags & OPF_PHASE) != 0;
-    const K pr = P::k_from_bits(o.c[0]), pi = P::k_from_bits(o.c[1]), mpi = P::kneg(pi);
-    float4* t4 = reinterpret_cast<float4*>(tile);
-    const uint32_t tb = 1u << (tq - 1);
-    auto moved = [&](float4 v) {  // the phase on both amplitudes of a float4 landing at (1, 1)
-        if (!phased) return v;
-        auto a = P::load(make_float2(v.x, v.y)), b = P::load(make_float2(v.z, v.w));
-        cmul_const<P>(a, pr, pi, mpi);
-        cmul_const<P>(b, pr, pi, mpi);
-        const float2 sa = P::store(a), sb = P::store(b);
-        return make_float4(sa.x, sa.y, sb.x, sb.y);
-    };
-    if (nonlocal) {
-        if (!((base >> o.q0) & 1)) return true;
-        for (uint32_t p = threadIdx.x; p < (tsize >> 2); p += blockDim.x) {
-            const uint32_t f0 = ins0(p, tb), f1 = f0 | tb;
-            const float4 x = t4[f0];
-            t4[f0] = t4[f1];
-            t4[f1] = moved(x);
-        }
-        return true;
-    }
-    const int c = o.q0;
-    const uint32_t cb = 1u << (c - 1);
-    const uint32_t lo = cb < tb ? cb : tb, hi = cb < tb ? tb : cb;
-    for (uint32_t r = threadIdx.x; r < (tsize >> 3); r += blockDim.x) {
-        const uint32_t f = ins0(ins0(r, lo), hi) | cb;
-        const float4 x = t4[f];
-        t4[f] = t4[f | tb];
-        t4[f | tb] = moved(x);
-    }
-    return true;
-}
-
-// ------------------------------------------------------------------------------------------
-// EX_GROUP (group_tile_ops): a run of ops on three local qubits g0 < g1 < g2 runs on octets.  A
-// thread loads the 8 amplitudes over those qubits (register e holds local index i0 | bits of e on
-// g0, g1, g2), applies every op of the run in registers with its pair pattern fixed at compile
-// time, and stores them: one shared-memory round trip and one barrier for the run instead of one
-// per op.
-// ------------------------------------------------------------------------------------------
-// Each thread holds NO octets (the tile's octets split evenly over the CTA), so an op's record is
-// read and dispatched once per thread, not once per octet.
-template <class P, int KIND, int J, int NO>
-__device__ __forceinline__ void octet_pairs(typename P::C (&a)[NO][8], const ExecOp& o) {
-    const PairMath<P, KIND> m(o);
-#pragma unroll
-    for (int n = 0; n < NO; ++n)
-#pragma unroll
-        for (int e = 0; e < 8; ++e)
-            if (!(e & (1 << J))) m.apply(a[n][e], a[n][e | (1 << J)]);
-}
-
-template <class P, int KIND, int NO>
-__device__ __forceinline__ void octet_pairs_slot(typename P::C (&a)[NO][8], int j, const ExecOp& o) {
-    if (j == 0) octet_pairs<P, KIND, 0, NO>(a, o);
-    else if (j == 1) octet_pairs<P, KIND, 1, NO>(a, o);
-    else octet_pairs<P, KIND, 2, NO>(a, o);
-}
-
-// CNOT with target slot J and control slot K (K < 0: a tile-uniform global control, `on`); with
-// OPF_PHASE the amplitude that lands at control = target = 1 is multiplied by c[0] + i c[1]
-template <class P, int J, int K, int NO>
-__device__ __forceinline__ void octet_cnot(typename P::C (&a)[NO][8], const ExecOp& o, bool on) {
-    using Kt = typename P::K;
-    using C = typename P::C;
-    if (K < 0 && !on) return;
-    constexpr int KB = K < 0 ? 0 : (1 << (K < 0 ? 0 : K));
-    const bool phased = (o.flags & OPF_PHASE) != 0;
-    const Kt pr = P::k_from_bits(o.c[0]), pi = P::k_from_bits(o.c[1]), mpi = P::kneg(pi);
-#pragma unroll
-    for (int n = 0; n < NO; ++n)
-#pragma unroll
-        for (int e = 0; e < 8; ++e)
-            if (!(e & (1 << J)) && (K < 0 || (e & KB))) {
-                const C x = a[n][e];
-                a[n][e] = a[n][e | (1 << J)];
-                a[n][e | (1 << J)] = x;
-                if (phased) cmul_const<P>(a[n][e | (1 << J)], pr, pi, mpi);
-            }
-}
-
-template <class P, int NO>
-__device__ __forceinline__ void octet_cnot_slots(typename P::C (&a)[NO][8], int jt, int jc, const ExecOp& o, bool on) {
-    switch (jt * 4 + (jc + 1)) {  // jc = -1: global control
-        case 0: octet_cnot<P, 0, -1, NO>(a, o, on); break;
-        case 2: octet_cnot<P, 0, 1, NO>(a, o, on); break;
-        case 3: octet_cnot<P, 0, 2, NO>(a, o, on); break;
-        case 4: octet_cnot<P, 1, -1, NO>(a, o, on); break;
-        case 5: octet_cnot<P, 1, 0, NO>(a, o, on); break;
-        case 7: octet_cnot<P, 1, 2, NO>(a, o, on); break;
-        case 8: octet_cnot<P, 2, -1, NO>(a, o, on); break;
-        case 9: octet_cnot<P, 2, 0, NO>(a, o, on); break;
-        case 10: octet_cnot<P, 2, 1, NO>(a, o, on); break;
-        default: break;
-    }
-}
-
-// the run on octets r = threadIdx.x + n * blockDim.x, n < NO (NO * blockDim.x octets in all)
-template <class P, int NO>
-__device__ __forceinline__ void tile_group(typename P::S* tile, uint64_t base, const ExecOp& h, const ExecOp* sub) {
-    using C = typename P::C;
-    const uint32_t m = (uint32_t)h.mask;
-    const uint32_t b0 = m & (0u - m), m1 = m ^ b0, b1 = m1 & (0u - m1), b2 = m1 ^ b1;
-    const int g0 = __ffs(b0) - 1, g1 = __ffs(b1) - 1;
-    auto slot = [&](int q) { return q == g0 ? 0 : (q == g1 ? 1 : 2); };
-    auto at = [&](int n, int e) {
-        const uint32_t r = threadIdx.x + (uint32_t)n * blockDim.x;
-        return ins0(ins0(ins0(r, b0), b1), b2) | ((e & 1) ? b0 : 0u) | ((e & 2) ? b1 : 0u) | ((e & 4) ? b2 : 0u);
-    };
-    C a[NO][8];
-#pragma unroll
-    for (int n = 0; n < NO; ++n)
-#pragma unroll
-        for (int e = 0; e < 8; ++e) a[n][e] = P::load(tile[at(n, e)]);
-    for (int s = 0; s < h.q0; ++s) {
-        const ExecOp& o = sub[s];
-        switch (o.kind) {
-            case EX_U2: octet_pairs_slot<P, EX_U2, NO>(a, slot(o.q0), o); break;
-            case EX_ZYZ: octet_pairs_slot<P, EX_ZYZ, NO>(a, slot(o.q0), o); break;
-            case EX_ZY: octet_pairs_slot<P, EX_ZY, NO>(a, slot(o.q0), o); break;
-            case EX_ZT: octet_pairs_slot<P, EX_ZT, NO>(a, slot(o.q0), o); break;
-            case EX_ZC: octet_pairs_slot<P, EX_ZC, NO>(a, slot(o.q0), o); break;
-            case EX_RT: octet_pairs_slot<P, EX_RT, NO>(a, slot(o.q0), o); break;
-            case EX_RC: octet_pairs_slot<P, EX_RC, NO>(a, slot(o.q0), o); break;
-            case EX_RX: octet_pairs_slot<P, EX_RX, NO>(a, slot(o.q0), o); break;
-            case EX_RY: octet_pairs_slot<P, EX_RY, NO>(a, slot(o.q0), o); break;
-            case EX_H: octet_pairs_slot<P, EX_H, NO>(a, slot(o.q0), o); break;
-            case EX_X: octet_pairs_slot<P, EX_X, NO>(a, slot(o.q0), o); break;
-            case EX_CNOT: {
-                const bool global = (o.flags & OPF_NONLOCAL_Q0) != 0;
-                octet_cnot_slots<P, NO>(a, slot(o.q1), global ? -1 : slot(o.q0), o, global && ((base >> o.q0) & 1));
-                break;
-            }
-            default: break;
-        }
-    }
-#pragma unroll
-    for (int n = 0; n < NO; ++n)
-#pragma unroll
-        for (int e = 0; e < 8; ++e) tile[at(n, e)] = P::store(a[n][e]);
-}
-
-// the pair ops of k_tile: complex64 through the two-amplitude form, the 16-byte formats as is
-template <class P, int KIND>
-__device__ __forceinline__ void tile_pairs_k(typename P::S* tile, uint32_t tsize, int q, const ExecOp& o) {
-    if constexpr (sizeof(typename P::S) == 8) {
-        if (tsize >= 4) {
-            tile_pairs_f32x2<P, KIND>(tile, tsize, q, o);
-            return;
-        }
-    }
-    tile_pairs<P, KIND>(tile, tsize >> 1, q, o);
-}
-
-// CTA size limit of k_tile: complex64 tiles keep up to 4 octets of a run in registers per thread
-template <class P>
-struct TileMaxThreads {
-    static constexpr int value = sizeof(typename P::S) == 8 ? 512 : 1024;
-};
-
-template <class P>
-__global__ void __launch_bounds__(TileMaxThreads<P>::value) k_tile(typename P::S* __restrict__ psi, PassDesc pd, const ExecOp* __restrict__ ops,
+__global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, PassDesc pd, const ExecOp* __restrict__ ops,
                                                const uint64_t* __restrict__ tables, double2* __restrict__ mirror,
                                                int* __restrict__ err_flag) {
     using S = typename P::S;
@@ -448,19 +243,19 @@ __global__ void __launch_bounds__(TileMaxThreads<P>::value) k_tile(typename P::S
         const ExecOp& o = sops[k % kOpChunk];
         const int kind = o.kind;
         switch (kind) {
-            case EX_U2: tile_pairs_k<P, EX_U2>(tile, tsize, o.q0, o); break;
-            case EX_ZYZ: tile_pairs_k<P, EX_ZYZ>(tile, tsize, o.q0, o); break;
-            case EX_ZY: tile_pairs_k<P, EX_ZY>(tile, tsize, o.q0, o); break;
-            case EX_ZT: tile_pairs_k<P, EX_ZT>(tile, tsize, o.q0, o); break;
-            case EX_ZC: tile_pairs_k<P, EX_ZC>(tile, tsize, o.q0, o); break;
-            case EX_RT: tile_pairs_k<P, EX_RT>(tile, tsize, o.q0, o); break;
-            case EX_RC: tile_pairs_k<P, EX_RC>(tile, tsize, o.q0, o); break;
+            case EX_U2: tile_pairs<P, EX_U2>(tile, tsize >> 1, o.q0, o); break;
+            case EX_ZYZ: tile_pairs<P, EX_ZYZ>(tile, tsize >> 1, o.q0, o); break;
+            case EX_ZY: tile_pairs<P, EX_ZY>(tile, tsize >> 1, o.q0, o); break;
+            case EX_ZT: tile_pairs<P, EX_ZT>(tile, tsize >> 1, o.q0, o); break;
+            case EX_ZC: tile_pairs<P, EX_ZC>(tile, tsize >> 1, o.q0, o); break;
+            case EX_RT: tile_pairs<P, EX_RT>(tile, tsize >> 1, o.q0, o); break;
+            case EX_RC: tile_pairs<P, EX_RC>(tile, tsize >> 1, o.q0, o); break;
             case EX_PTAB: tile_ptab<P>(tile, tsize, o, tables); break;
             case EX_PHASE1: tile_phase1<P>(tile, tsize, base, o); break;
-            case EX_RX: tile_pairs_k<P, EX_RX>(tile, tsize, o.q0, o); break;
-            case EX_RY: tile_pairs_k<P, EX_RY>(tile, tsize, o.q0, o); break;
-            case EX_H: tile_pairs_k<P, EX_H>(tile, tsize, o.q0, o); break;
-            case EX_X: tile_pairs_k<P, EX_X>(tile, tsize, o.q0, o); break;
+            case EX_RX: tile_pairs<P, EX_RX>(tile, tsize >> 1, o.q0, o); break;
+            case EX_RY: tile_pairs<P, EX_RY>(tile, tsize >> 1, o.q0, o); break;
+            case EX_H: tile_pairs<P, EX_H>(tile, tsize >> 1, o.q0, o); break;
+            case EX_X: tile_pairs<P, EX_X>(tile, tsize >> 1, o.q0, o); break;
             case EX_DIAG: {
                 const K d0r = P::k_from_bits(o.c[0]), d0i = P::k_from_bits(o.c[1]);
                 const K d1r = P::k_from_bits(o.c[2]), d1i = P::k_from_bits(o.c[3]);
@@ -485,28 +280,7 @@ __global__ void __launch_bounds__(TileMaxThreads<P>::value) k_tile(typename P::S
                 }
                 break;
             }
-            case EX_CNOT:
-                if constexpr (sizeof(S) == 8) {
-                    if (tile_cnot_f32x2<P>(tile, tsize, base, o)) break;
-                }
-                tile_cnot<P>(tile, tsize, base, o);
-                break;
-            case EX_GROUP:
-                // complex64 tiles run the group on octets; anywhere else (or for a header that
-                // does not fit its chunk or the tile) the header is a no-op and its ops run one
-                // by one, which is the same product
-                if constexpr (sizeof(S) == 8) {
-                    const uint32_t gm = (uint32_t)o.mask;
-                    const uint32_t per = (tsize >> 3) / blockDim.x;  // octets per thread
-                    if (o.q0 >= 1 && (k % kOpChunk) + o.q0 < kOpChunk && (o.mask >> 32) == 0 && __popc(gm) == 3 &&
-                        gm < tsize && per * blockDim.x == (tsize >> 3) && (per == 1 || per == 2)) {
-                        const ExecOp* sub = &sops[(k % kOpChunk) + 1];
-                        if (per == 2) tile_group<P, 2>(tile, base, o, sub);
-                        else tile_group<P, 1>(tile, base, o, sub);
-                        k += o.q0;
-                    }
-                }
-                break;
+            case EX_CNOT: tile_cnot<P>(tile, tsize, base, o); break;
             case EX_MCZ: {
                 if ((base & o.nl_mask) == o.nl_mask) {
                     const uint32_t lm = (uint32_t)o.mask;
@@ -731,7 +505,6 @@ cudaError_t tile_pass_t(void* vpsi, int n, const PassDesc& pd, const ExecOp* d_o
     const size_t smem = tile_smem_bytes<P>(pd.t, pd.low);
     const uint64_t ntiles = 1ULL << (n - pd.t);
     if (threads <= 0) threads = pd.t >= 10 ? 512 : (pd.t >= 6 ? (1 << (pd.t - 1)) : 32);
-    threads = std::min(threads, TileMaxThreads<P>::value);
     k_tile<P><<<(unsigned)ntiles, threads, smem, s>>>(static_cast<typename P::S*>(vpsi), pd, d_ops, d_tables,
                                                       reinterpret_cast<double2*>(mirror), err_flag);
     return cudaGetLastError();

@@ -587,112 +587,6 @@ int to_register_program(Plan& out) {
     return changes;
 }
 
-// ------------------------------------------------------------------------------------------
-// Op groups.  In a shared-memory tile pass every op moves the whole tile through shared memory
-// and ends in a barrier; for complex64 that traffic bounds the pass.  A run of ops that act on at
-// most three local qubits can instead run on octets of amplitudes held in registers (EX_GROUP):
-// one round trip and one barrier per run.  Runs are gathered greedily in pass order: an op joins
-// the open run if its qubits keep the run within three and it commutes with every op it moves
-// past (disjoint qubits); ops that cannot join block all local qubits.
-// ------------------------------------------------------------------------------------------
-namespace {
-
-// the local qubits an op needs inside a group (0: the op cannot join one)
-uint32_t group_qubits(const ExecOp& e) {
-    switch (e.kind) {
-        case EX_U2:
-        case EX_RX:
-        case EX_RY:
-        case EX_H:
-        case EX_X:
-        case EX_ZYZ:
-        case EX_ZY:
-        case EX_ZT:
-        case EX_ZC:
-        case EX_RT:
-        case EX_RC: return (e.flags & OPF_NONLOCAL_Q0) ? 0u : 1u << e.q0;
-        case EX_CNOT: return (e.flags & OPF_NONLOCAL_Q0) ? 1u << e.q1 : (1u << e.q0) | (1u << e.q1);
-        default: return 0u;
-    }
-}
-
-}  // namespace
-
-int group_tile_ops(Plan& out) {
-    std::vector<ExecOp> ops;
-    std::vector<int> src;
-    ops.reserve(out.ops.size() + out.ops.size() / 2);
-    src.reserve(out.ops.size() + out.ops.size() / 2);
-    int grouped = 0;
-    for (PassDesc& pd : out.passes) {
-        const int b = pd.op_begin, m = pd.nops, t = pd.t;
-        const int begin = (int)ops.size();
-        auto emit = [&](int i) {
-            ops.push_back(out.ops[b + i]);
-            src.push_back(out.source_index[b + i]);
-        };
-        if (t < 3 || t > 31) {
-            for (int i = 0; i < m; ++i) emit(i);
-            pd.op_begin = begin;
-            continue;
-        }
-        const uint32_t all_local = (uint32_t)((1ULL << t) - 1);
-        std::vector<char> done(m, 0);
-        std::vector<int> members;
-        for (int i = 0; i < m; ++i) {
-            if (done[i]) continue;
-            done[i] = 1;
-            members.assign(1, i);
-            uint32_t g = group_qubits(out.ops[b + i]);
-            if (g) {
-                uint32_t blocked = 0;
-                for (int j = i + 1; j < m && blocked != all_local; ++j) {
-                    if (done[j]) continue;
-                    const uint32_t gj = group_qubits(out.ops[b + j]);
-                    if (gj && !(gj & blocked) && __builtin_popcount(g | gj) <= 3) {
-                        g |= gj;
-                        done[j] = 1;
-                        members.push_back(j);
-                    } else {
-                        blocked |= gj ? gj : all_local;
-                    }
-                }
-            }
-            if (members.size() < 2) {
-                emit(i);
-                continue;
-            }
-            for (int q = 0; __builtin_popcount(g) < 3; ++q) g |= 1u << q;  // three qubits: pad with free positions
-            // emit the run, split where it would straddle a chunk of staged op records
-            size_t k = 0;
-            while (k < members.size()) {
-                const int room = kTileOpChunk - ((int)ops.size() - begin) % kTileOpChunk;
-                const int left = (int)(members.size() - k);
-                if (left >= 2 && room >= 3) {
-                    const int c = std::min(left, room - 1);
-                    ExecOp h = blank(EX_GROUP);
-                    h.mask = g;
-                    h.q0 = c;
-                    ops.push_back(h);
-                    src.push_back(-1);
-                    for (int u = 0; u < c; ++u) emit(members[k + u]);
-                    k += c;
-                    grouped += c;
-                } else {
-                    const int c = left >= 2 ? std::min(left, room) : 1;  // plain ops to the chunk's end
-                    for (int u = 0; u < c; ++u) emit(members[k + u]);
-                    k += c;
-                }
-            }
-        }
-        pd.op_begin = begin;
-        pd.nops = (int)ops.size() - begin;
-    }
-    out.ops.swap(ops);
-    out.source_index.swap(src);
-    return grouped;
-}
-
 static bool is_param_op(const llg_op& op, bool use_params) {
     return use_params && op.param >= 0 && (op.kind == LLG_OP_RX || op.kind == LLG_OP_RY || op.kind == LLG_OP_RZ);
 }

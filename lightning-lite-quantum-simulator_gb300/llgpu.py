@@ -417,19 +417,16 @@ class State:
 PLAN_ZYZ = 1
 PLAN_TABLES = 2
 PLAN_REGS = 4
-PLAN_GROUPS = 8
 
 
 def plan_export(n: int, ops: np.ndarray, tile_qubits: int, zyz: bool = False, tables: bool = False,
-                regs: bool = False, groups: bool = False):
+                regs: bool = False):
     """Host-side plan of `ops` (passes, executor ops; coefficients as doubles).  zyz=True plans
     as the engine does for complex128 states (fused unitary 2x2s as carried-phase rotations);
     tables=True (with zyz) also gathers diagonal factors into phase tables, and the result gains a
-    third item: the tables as a complex array (2^tile_qubits entries per table); groups=True adds
-    the op groups of complex64 tile passes (kind 20), regs=True gives register programs."""
+    third item: the tables as a complex array (2^tile_qubits entries per table)."""
     ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
-    flags = ((PLAN_ZYZ if zyz else 0) | (PLAN_TABLES if tables else 0) | (PLAN_REGS if regs else 0) |
-             (PLAN_GROUPS if groups else 0))
+    flags = (PLAN_ZYZ if zyz else 0) | (PLAN_TABLES if tables else 0) | (PLAN_REGS if regs else 0)
     npasses, nx = ctypes.c_int(), ctypes.c_int()
     check(lib().llg_plan_export_ex(n, _ptr(ops) if ops.size else None, ops.size, tile_qubits, flags, None, 0,
                                    ctypes.byref(npasses), None, 0, ctypes.byref(nx)))

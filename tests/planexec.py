@@ -74,38 +74,6 @@ def unregister(passes: np.ndarray, xops: np.ndarray) -> np.ndarray:
     return out
 
 
-GROUP_KINDS = (0, 1, 2, 3, 4, 11, 12, 14, 15, 16, 17)  # pair ops that may join an op group
-TILE_OP_CHUNK = 32  # op records the tile kernel stages at a time
-
-
-def check_groups(passes: np.ndarray, xops: np.ndarray) -> int:
-    """The invariants the tile kernel relies on for kind-20 op groups: three local qubits in the
-    mask, q0 >= 1 member ops right after the header, each a pair op on one of the three qubits or
-    a CNOT whose target (and local control) is one of them, and header plus members inside one
-    chunk of TILE_OP_CHUNK records.  Returns the number of grouped ops."""
-    grouped = 0
-    for p in passes:
-        b, m, t = int(p["op_begin"]), int(p["nops"]), int(p["t"])
-        i = 0
-        while i < m:
-            x = xops[b + i]
-            if int(x["kind"]) == 20:
-                g, c = int(x["mask"]), int(x["q0"])
-                assert bin(g).count("1") == 3 and g < (1 << t), (g, t)
-                assert c >= 1 and i + c < m and i // TILE_OP_CHUNK == (i + c) // TILE_OP_CHUNK, (i, c)
-                for y in xops[b + i + 1:b + i + 1 + c]:
-                    k, q0, q1, fl = int(y["kind"]), int(y["q0"]), int(y["q1"]), int(y["flags"])
-                    if k == 6:
-                        assert g >> q1 & 1 and (fl & 1 or g >> q0 & 1), (k, q0, q1, fl, g)
-                    else:
-                        assert k in GROUP_KINDS and not fl & 1 and g >> q0 & 1, (k, q0, fl, g)
-                grouped += c
-                i += c + 1
-            else:
-                i += 1
-    return grouped
-
-
 def execute(psi: np.ndarray, n: int, passes: np.ndarray, xops: np.ndarray, tables: np.ndarray | None = None) -> np.ndarray:
     psi = psi.copy()
     for p in passes:
@@ -125,7 +93,7 @@ def execute(psi: np.ndarray, n: int, passes: np.ndarray, xops: np.ndarray, table
         lidx = np.arange(1 << t)
         for x in xops[p["op_begin"]:p["op_begin"] + p["nops"]]:
             k, q0, q1, fl = int(x["kind"]), int(x["q0"]), int(x["q1"]), int(x["flags"])
-            if k in (-1, 20):  # a layout op of a register program, an op group's header
+            if k == -1:
                 continue
             if k <= 4 or k in (11, 12, 14, 15, 16, 17):
                 _pair(tile, q0, _matrix(x))

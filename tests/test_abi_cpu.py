@@ -15,7 +15,7 @@ import oracle
 import workloads
 from conftest import REPO, split
 from llgpu import OP_CNOT, OP_CZ, OP_DTYPE, OP_H, OP_MCZ, OP_RX, OP_RY, OP_RZ, OP_U2, OP_X, make_ops
-from planexec import check_groups, execute, unregister
+from planexec import execute, unregister
 
 
 def header_symbols():
@@ -111,34 +111,6 @@ def test_plan_of_random_2024_circuits(built, golden):
         passes, xops = llgpu.plan_export(n, ops, 3)
         got = execute(oracle.zero_state(n), n, passes, xops)
         assert np.max(np.abs(got - oracle.run_ops(n, ops))) < 1e-12
-
-
-@pytest.mark.parametrize("n,tile", [(8, 5), (10, 7), (12, 9), (14, 13)])
-def test_op_groups_reproduce_the_oracle(built, n, tile):
-    # complex64 tile passes run runs of ops on three local qubits as register octets (kind 20):
-    # ops move only past ops on disjoint qubits, so the grouped plan's product is unchanged
-    rng = np.random.default_rng(300 + n)
-    for ops in (random_ops(n, 300, rng), workloads.layered_rotations(n, 6, seed=n)):
-        passes, xops = llgpu.plan_export(n, ops, tile, zyz=True, groups=True)
-        grouped = check_groups(passes, xops)
-        assert grouped > len(xops) // 3  # most ops run inside groups
-        got = execute(oracle.zero_state(n), n, passes, xops)
-        assert np.max(np.abs(got - oracle.run_ops(n, ops))) < 1e-12
-
-
-def test_op_groups_respect_the_op_chunks(built):
-    # a 30-qubit layered circuit: many passes, groups split where they would cross a chunk of 32
-    # staged op records; a pass without room keeps its ops plain
-    ops = workloads.layered_rotations(30, 20)
-    passes, xops = llgpu.plan_export(30, ops, 13, zyz=True, groups=True)
-    p0, x0 = llgpu.plan_export(30, ops, 13, zyz=True)
-    assert len(passes) == len(p0)
-    grouped = check_groups(passes, xops)
-    kinds = xops["kind"]
-    assert int(np.sum(kinds != 20)) == len(x0)  # the same ops plus one header per group
-    assert grouped > 0.8 * len(x0) and int(np.sum(kinds == 20)) < len(x0) / 4  # several ops per group
-    with pytest.raises(ValueError):
-        llgpu.plan_export(12, ops[:10], 9, zyz=True, tables=True, groups=True)
 
 
 @pytest.mark.parametrize("tile", [9, 11, 13])
