@@ -20,10 +20,10 @@ import workloads  # noqa: E402
 
 def tile_f64():
     """IEEE complex128 tile passes with phase tables: the 30-qubit recipe's circuit at 26 qubits
-    (1 GiB), 11-qubit tiles and 256 threads (the tuner's choice at 30 qubits)."""
+    (1 GiB), 12-qubit tiles and 256 threads (the tuner's choice at 30 qubits)."""
     n = 26
     st = llgpu.State(n, "complex128")
-    st.set_fusion("tile", 11)
+    st.set_fusion("tile", 12)
     st.set_tile_threads(256)
     st.apply_ops(workloads.layered_rotations(n, 4))
     st.sync()
