@@ -181,9 +181,8 @@ __global__ void __launch_bounds__(TcShape<KQ>::kThreads, TcShape<KQ>::kMinBlocks
     // recombine the tile in accumulator set `set` and store it: warp w reads lanes 32 (w & 3) ..
     // +31 (its groups) and the real and imaginary columns of amplitudes 8 (w >> 2) .. +7, so that
     // each thread writes whole amplitudes, a warp 32 consecutive groups per amplitude
-    auto epilogue = [&](uint64_t tile, int set, int egb) {
+    auto epilogue = [&](uint64_t tile, int set, int egb, int a0) {
         const int row = 32 * (warp & 3) + lane;
-        const int a0 = 8 * (warp >> 2);
         const int eg = eg_s[egb][row] - 1000;  // stored with the atomicMax offset
         df out[2][8];
 #pragma unroll
@@ -325,13 +324,16 @@ __global__ void __launch_bounds__(TcShape<KQ>::kThreads, TcShape<KQ>::kMinBlocks
         // ---- 21 slice products (i + j <= 5) into four accumulators of this set, K / 16 steps each ----
         if (tid == 0) {
             const uint32_t tset = tmem + (uint32_t)(set * T::kSetCols);
+            const uint64_t da0 = tc_desc(smem_u32(sA), lbo, sbo), dw0 = tc_desc(smem_u32(sW), lbo, sbo);
             auto diagonal = [&](int d, uint32_t dcol, bool first_fresh) {
                 bool first = true;
                 for (int i = 0; i <= d; ++i) {
                     const int j = d - i;
                     for (int ks = 0; ks < kReals / 16; ++ks) {
-                        const uint64_t da = tc_desc(smem_u32(sA + i * T::kSliceBytes) + ks * 256, lbo, sbo);
-                        const uint64_t dw = tc_desc(smem_u32(sW + j * T::kWSliceBytes) + ks * 256, lbo, sbo);
+                        // the start address is the descriptor's low field (bytes / 16, below 2^14 for
+                        // any shared-memory address): offsets add to it directly
+                        const uint64_t da = da0 + (uint64_t)((i * T::kSliceBytes + ks * 256) >> 4);
+                        const uint64_t dw = dw0 + (uint64_t)((j * T::kWSliceBytes + ks * 256) >> 4);
                         // a diagonal's first product starts the accumulator (first_fresh) or scales
                         // the diagonals above it by 2^-8 (Horner)
                         mma(dcol, da, dw, (first && first_fresh) ? 0u : 1u, first && !first_fresh);
@@ -345,8 +347,15 @@ __global__ void __launch_bounds__(TcShape<KQ>::kThreads, TcShape<KQ>::kMinBlocks
             diagonal(3, tset + (uint32_t)(3 * kReals), false);
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(&mbar)));
         }
-        // ---- the previous tile's epilogue, under this tile's products ----
-        if (have_prev) epilogue(prev_tile, set ^ 1, egb == 0 ? 2 : egb - 1);
+        // ---- the previous tile's epilogue, under this tile's products.  Warp 0 issued the
+        // products; its share of the epilogue (lanes 0-31, amplitudes 0-7) goes to warp 4, which
+        // reads the same tensor-memory lanes, so that the issue does not delay the next barrier ----
+        if (have_prev) {
+            const int egp = egb == 0 ? 2 : egb - 1;
+            if (warp != 0) epilogue(prev_tile, set ^ 1, egp, 8 * (warp >> 2));
+            if (warp == 4) epilogue(prev_tile, set ^ 1, egp, 0);
+            if (warp == 0) asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        }
         prev_tile = tile;
         have_prev = true;
     }
@@ -359,7 +368,7 @@ __global__ void __launch_bounds__(TcShape<KQ>::kThreads, TcShape<KQ>::kMinBlocks
             wait_mma(phase);
         } else {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            epilogue(prev_tile, set ^ 1, egb == 0 ? 2 : egb - 1);
+            epilogue(prev_tile, set ^ 1, egb == 0 ? 2 : egb - 1, 8 * (warp >> 2));
         }
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");  // no copy left in flight on any exit
