@@ -55,7 +55,8 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(typename P::S* __restri
                                                          const PassDesc* __restrict__ passes, const ExecOp* __restrict__ ops,
                                                          const Item* __restrict__ items, long long nitems,
                                                          unsigned long long* __restrict__ next, unsigned* __restrict__ completed,
-                                                         int* __restrict__ err, long long spin_limit) {
+                                                         int* __restrict__ err, long long spin_limit,
+                                                         const uint64_t* __restrict__ tables) {
     using S = typename P::S;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ long long s_item;
@@ -110,7 +111,7 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(typename P::S* __restri
                     for (int q = threadIdx.x; q < cnt * kWords; q += blockDim.x) reinterpret_cast<uint4*>(sops)[q] = src[q];
                     __syncthreads();
                 }
-                tile_apply<P>(tile, tsize, base, sops[k % kBatchOpChunk], nullptr);
+                tile_apply<P>(tile, tsize, base, sops[k % kBatchOpChunk], nullptr, tables);
                 __syncthreads();
             }
             for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) psi[base | hi_off[l >> low] | (l & lowmask)] = tile[l];
@@ -195,6 +196,7 @@ struct llg_batch {
     std::vector<CircDesc> circs;
     std::vector<PassDesc> passes;
     std::vector<ExecOp> ops;
+    std::vector<uint64_t> tables;  // phase tables of every circuit's plan, (re, im) slots per entry
     std::vector<Item> items;
     uint64_t total_amps = 0;
     cudaStream_t stream = nullptr;
@@ -202,6 +204,7 @@ struct llg_batch {
     CircDesc* d_circs = nullptr;
     PassDesc* d_passes = nullptr;
     ExecOp* d_ops = nullptr;
+    uint64_t* d_tables = nullptr;
     Item* d_items = nullptr;
     unsigned long long* d_next = nullptr;
     unsigned* d_completed = nullptr;
@@ -247,7 +250,7 @@ cudaError_t enqueue_batch(llg_batch* b, long long spin_limit) {
     if ((e = cudaMemsetAsync(b->d_err, 0, sizeof(int), s))) return e;
     k_batch<P><<<b->grid, b->threads, b->smem, s>>>(static_cast<typename P::S*>(b->d_arena), b->d_circs, b->d_passes,
                                                        b->d_ops, b->d_items, (long long)b->items.size(), b->d_next,
-                                                       b->d_completed, b->d_err, spin_limit);
+                                                       b->d_completed, b->d_err, spin_limit, b->d_tables);
     return cudaGetLastError();
 }
 
@@ -315,7 +318,10 @@ static int batch_build(int count, const int* n_qubits, const llg_op* ops, const 
         }
         Plan plan;
         std::string err;
-        if (!plan_tiles(n, ops + o0, (int)(o1 - o0), tile, precision, plan, err)) {
+        // 16-byte precisions gather diagonal factors into phase tables (one table buffer for the
+        // batch; each circuit's EX_PTAB offsets are shifted to its part of it)
+        if (!plan_tiles(n, ops + o0, (int)(o1 - o0), tile, precision, plan, err, false, ZYZ_DEFAULT,
+                        precision != LLG_F32)) {
             delete b;
             return set_error(LLG_EINVAL, "batch_create: " + err);
         }
@@ -329,6 +335,10 @@ static int batch_build(int count, const int* n_qubits, const llg_op* ops, const 
             pd.op_begin += (int)b->ops.size();
             b->passes.push_back(pd);
         }
+        const uint64_t table_base = b->tables.size() / 2;  // entries of (re, im) slots
+        for (ExecOp& x : plan.ops)
+            if (x.kind == EX_PTAB) x.mask += table_base;
+        b->tables.insert(b->tables.end(), plan.tables.begin(), plan.tables.end());
         b->ops.insert(b->ops.end(), plan.ops.begin(), plan.ops.end());
         b->circs.push_back(cd);
         b->total_amps += 1ULL << n;
@@ -355,6 +365,7 @@ static int batch_build(int count, const int* n_qubits, const llg_op* ops, const 
     alloc((void**)&b->d_circs, b->circs.size() * sizeof(CircDesc), "circuit table");
     alloc((void**)&b->d_passes, b->passes.size() * sizeof(PassDesc), "pass table");
     alloc((void**)&b->d_ops, b->ops.size() * sizeof(ExecOp), "op table");
+    if (!b->tables.empty()) alloc((void**)&b->d_tables, b->tables.size() * sizeof(uint64_t), "phase tables");
     alloc((void**)&b->d_items, b->items.size() * sizeof(Item), "work queue");
     alloc((void**)&b->d_next, sizeof(unsigned long long), "queue head");
     alloc((void**)&b->d_completed, count * sizeof(unsigned), "counters");
@@ -366,6 +377,7 @@ static int batch_build(int count, const int* n_qubits, const llg_op* ops, const 
     up(b->d_circs, b->circs.data(), b->circs.size() * sizeof(CircDesc));
     up(b->d_passes, b->passes.data(), b->passes.size() * sizeof(PassDesc));
     up(b->d_ops, b->ops.data(), b->ops.size() * sizeof(ExecOp));
+    if (b->d_tables) up(b->d_tables, b->tables.data(), b->tables.size() * sizeof(uint64_t));
     up(b->d_items, b->items.data(), b->items.size() * sizeof(Item));
     if (rc) {
         llg_batch_destroy(b);
@@ -476,7 +488,8 @@ int llg_batch_destroy(llg_batch* b) {
     if (!b) return LLG_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
     drop_graph(b);
-    void* ptrs[] = {b->d_arena, b->d_circs, b->d_passes, b->d_ops, b->d_items, b->d_next, b->d_completed, b->d_err};
+    void* ptrs[] = {b->d_arena, b->d_circs, b->d_passes, b->d_ops, b->d_tables, b->d_items, b->d_next, b->d_completed,
+                    b->d_err};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->stream) cudaStreamDestroy(b->stream);

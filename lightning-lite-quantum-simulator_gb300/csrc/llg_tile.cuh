@@ -218,7 +218,7 @@ __device__ __forceinline__ void tile_cnot(typename P::S* tile, uint32_t tsize, u
 // ------------------------------------------------------------------------------------------
 template <class P>
 __device__ void tile_apply(typename P::S* tile, uint32_t tsize, uint64_t base, const ExecOp& o,
-                           const uint64_t* __restrict__ trow) {
+                           const uint64_t* __restrict__ trow, const uint64_t* __restrict__ tables = nullptr) {
     using K = typename P::K;
     using S = typename P::S;
     switch (o.kind) {
@@ -229,6 +229,9 @@ __device__ void tile_apply(typename P::S* tile, uint32_t tsize, uint64_t base, c
         case EX_ZC: tile_pairs<P, EX_ZC>(tile, tsize >> 1, o.q0, o); break;
         case EX_RT: tile_pairs<P, EX_RT>(tile, tsize >> 1, o.q0, o); break;
         case EX_RC: tile_pairs<P, EX_RC>(tile, tsize >> 1, o.q0, o); break;
+        case EX_PTAB:  // plans with phase tables run only where the kernel passes them
+            if (tables) tile_ptab<P>(tile, tsize, o, tables);
+            break;
         case EX_PHASE1: tile_phase1<P>(tile, tsize, base, o); break;
         case EX_RX: tile_pairs<P, EX_RX>(tile, tsize >> 1, o.q0, o); break;
         case EX_RY: tile_pairs<P, EX_RY>(tile, tsize >> 1, o.q0, o); break;
