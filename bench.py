@@ -624,6 +624,13 @@ def run_adjoint_bench(args, torch):
     out = adjoint_once(args, torch, args.precision)
     if is_f64(args.precision):
         out["df64"] = adjoint_once(args, torch, "df64")
+        # the double-float gradients against the IEEE FP64 ones, relative to the largest gradient
+        g64, gdf = out.pop("_grads"), out["df64"].pop("_grads")
+        scale = float(np.max(np.abs(g64)))
+        out["df64"]["vs_fp64"] = {"max_abs_grad_diff": float(np.max(np.abs(gdf - g64))),
+                                  "max_abs_grad_diff_rel_to_max_grad": float(np.max(np.abs(gdf - g64))) / scale
+                                  if scale else None}
+    out.pop("_grads", None)
     return out
 
 
@@ -663,7 +670,7 @@ def adjoint_once(args, torch, precision):
             "adjoint_s_per_batch": t_adj, "param_shift_s_per_set": t_ps,
             "max_abs_grad_diff_vs_param_shift": float(np.max(np.abs(g[0] - g_ps[0]))),
             "forward_passes": info["forward_passes"], "backward_passes": info["backward_passes"],
-            "precision": precision}
+            "precision": precision, "_grads": np.array(g)}
 
 
 def run_sweep_bench(args, torch):
@@ -782,8 +789,15 @@ def run_traj_bench(args, torch, cpu: bool):
         out[key] = {"traj_per_s": ntraj / dt, "seconds": dt, "mean_z0": float(z.mean()),
                     "std_error": float(z.std(ddof=1) / np.sqrt(ntraj)), "jumps_per_traj": float(j.mean()),
                     "config": h.config(), "default_config": default_cfg,
-                    "default_traj_per_s": ntraj / dt_default, "autotune": tune}
+                    "default_traj_per_s": ntraj / dt_default, "autotune": tune, "_z": z}
         h.close()
+    # every trajectory's <Z0> in double-float and complex64 against IEEE complex128 (same Philox
+    # draws, so the same jumps unless a decision margin is below the arithmetic's error)
+    z128 = out["c128"].pop("_z")
+    for key in ("df64", "c64"):
+        zk = out[key].pop("_z")
+        out[key]["vs_fp64"] = {"max_abs_z0_diff": float(np.max(np.abs(zk - z128))),
+                               "mean_z0_diff": float(abs(zk.mean() - z128.mean()))}
     if cpu:
         import oracle
 
