@@ -293,7 +293,7 @@ def run_reference(args, rank, world):
 FP32_INST_PER_PAIR = {"df64": {0: 160, 1: 64, 2: 64, 3: 64, 4: 0, 5: 64, 6: 0, 7: 0, 11: 128, 12: 96, 13: 32, 14: 80,
                                15: 80, 16: 48, 17: 48, 18: 64},
                       "complex64": {0: 16, 1: 8, 2: 8, 3: 8, 4: 0, 5: 8, 6: 0, 7: 0, 11: 16, 12: 12, 13: 4, 14: 8, 15: 8,
-                                    16: 4, 17: 4, 18: 8}}
+                                    16: 4, 17: 4, 18: 8, 20: 32, 21: 16}}
 PHASED_CNOT_PER_PAIR = {"df64": 16, "complex64": 2}  # a complex multiply on a quarter of the amplitudes
 # FP64 multiply-adds (DFMA or DMUL) per amplitude pair of each kind in IEEE complex128: a complex
 # product is four, a real 2x2 row two, a generic complex 2x2 row eight
@@ -310,16 +310,16 @@ def is_f64(precision: str) -> bool:
 
 
 def plan_for(precision: str, n: int, ops, tile_q: int, regs: bool = False):
-    """The plan the engine runs: carried phases and phase tables for 16-byte precisions, carried
-    phases alone for complex64 shared-memory tiles, register programs for register-tiled passes."""
+    """The plan the engine runs: carried phases and phase tables for 16-byte precisions, two-qubit
+    blocks for complex64 shared-memory tiles, register programs for register-tiled passes."""
     import llgpu
 
     if regs:
         p, x = llgpu.plan_export(n, ops, tile_q, zyz=True, regs=True)
         return p, x, 0
     if precision == "complex64":
-        p, x = llgpu.plan_export(n, ops, tile_q, zyz=True)
-        return p, x, 0
+        p, x, tab = llgpu.plan_export(n, ops, tile_q, fuse2=True)
+        return p, x, int(tab.nbytes)
     p, x, tab = llgpu.plan_export(n, ops, tile_q, zyz=True, tables=True)
     return p, x, int(tab.nbytes)
 

@@ -502,6 +502,10 @@ int llg_plan_export(int n, const llg_op* ops, int nops, int tile_qubits, llg_pas
  * register slot in q0, CNOTs their target slot in q1 and, with flags bit 4, a control slot in q0),
  * as the engine runs complex64 states (tables are not combined with it). */
 #define LLG_PLAN_REGS 4
+/* LLG_PLAN_FUSE2: two-qubit blocks as the engine plans complex64 shared-memory passes (kind 20: a
+ * 4x4 matrix on local qubits q0 (index bit 0) and q1 (index bit 1), 16 entries from table entry
+ * `mask`, row-major); alone, without the other options. */
+#define LLG_PLAN_FUSE2 8
 int llg_plan_export_ex(int n, const llg_op* ops, int nops, int tile_qubits, int flags, llg_pass_info* passes,
                        int max_passes, int* npasses, llg_exec_op* xops, int max_xops, int* nxops);
 /* The eigenvalue d(i) of the diagonal observable sum_k coeff_k Z_{a_k} Z_{b_k} (b_k < 0: Z_{a_k}) for

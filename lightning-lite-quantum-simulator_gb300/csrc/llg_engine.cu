@@ -270,11 +270,14 @@ int run_tiles(llg_state* st, const std::vector<llg_op>& q, double* mirror = null
     Plan plan;
     std::string err;
     const int t = st->tile_qubits > 0 ? st->tile_qubits : default_tile(st->P);
-    // register-tiled passes on registers of 9+ qubits (smaller ones keep the shared-memory tiles);
-    // every precision plans carried-phase tangent rotations, the 16-byte ones also phase tables
+    // register-tiled passes on registers of 9+ qubits (smaller ones keep the shared-memory tiles).
+    // The 16-byte precisions plan carried-phase tangent rotations and phase tables (their passes
+    // are arithmetic-bound); complex64 shared-memory passes, bound by shared-memory traffic, merge
+    // each CNOT with its neighbouring one-qubit ops into a 4x4 block instead
     const bool reg = st->fuse_mode == LLG_FUSE_REG && std::min(st->n, std::min(t, 13)) >= 9;
+    const bool f32_tiles = !reg && st->P == LLG_F32;
     if (!plan_tiles(st->n, q.data(), (int)q.size(), reg ? std::min(t, 13) : std::min(t, tile_max_qubits(st->P)), st->P,
-                    plan, err, false, ZYZ_ON, !reg && st->P != LLG_F32))
+                    plan, err, false, f32_tiles ? ZYZ_OFF : ZYZ_ON, !reg && st->P != LLG_F32, f32_tiles))
         return set_error(LLG_EINVAL, err);
     if (reg) to_register_program(plan);
     int rc = upload_ops(st, plan.ops, &plan.tables);
@@ -1159,8 +1162,10 @@ int export_plan(int n, const llg_op* ops, int nops, int tile_qubits, int flags, 
         if (rc) return rc;
     }
     std::string err;
+    if ((flags & LLG_PLAN_FUSE2) && (flags & (LLG_PLAN_ZYZ | LLG_PLAN_TABLES | LLG_PLAN_REGS)))
+        return set_error(LLG_EINVAL, "plan_export: two-qubit blocks are planned alone");
     if (!plan_tiles(n, ops, nops, tile_qubits, LLG_F64, plan, err, false, (flags & LLG_PLAN_ZYZ) ? ZYZ_ON : ZYZ_OFF,
-                    (flags & LLG_PLAN_TABLES) != 0 && (flags & LLG_PLAN_REGS) == 0))
+                    (flags & LLG_PLAN_TABLES) != 0 && (flags & LLG_PLAN_REGS) == 0, (flags & LLG_PLAN_FUSE2) != 0))
         return set_error(LLG_EINVAL, err);
     if (flags & LLG_PLAN_REGS) {
         if (tile_qubits < 9) return set_error(LLG_EINVAL, "plan_export: register programs need tiles of 9+ qubits");

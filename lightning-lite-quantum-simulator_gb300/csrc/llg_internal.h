@@ -58,6 +58,16 @@ enum ExecKind : int32_t {
     // and are fixed by the thread index over the other t - 4 positions (nl_mask: 4 bits per thread
     // index bit, in order; q0 = t - 4).  The tile moves through shared memory once per layout.
     EX_LAYOUT = 19,
+    // a dense two-qubit block (fuse_two_qubit): a CNOT together with the one-qubit ops next to it on
+    // its two qubits, as one 4x4 matrix on local qubits q0 (index bit 0) and q1 (index bit 1); the
+    // 16 entries (row-major, (re, im) coefficient slots) start at entry `mask` of the plan's table
+    // buffer.  One shared-memory round trip for up to five ops.
+    EX_U4 = 20,
+    // a CNOT whose control q0 is a global qubit (outside the tile), merged with the one-qubit ops
+    // next to it on its local target q1 (fuse_two_qubit): a 2x2 on q1 chosen by the control bit of
+    // the tile's base index, entries (row-major, (re, im) slots) at table entry `mask` (control 0)
+    // and `mask` + 4 (control 1)
+    EX_U2C = 21,
 };
 
 // Flags of a tile op.
@@ -118,8 +128,12 @@ enum PlanZyz : int { ZYZ_DEFAULT = -1, ZYZ_OFF = 0, ZYZ_ON = 1 };
 // rotations, the controlled phases of phased CNOTs, carried phases flushed at the end) are
 // gathered into EX_PTAB phase tables where a table replaces more than two complex multiplies per
 // amplitude pair; only kernels that execute EX_PTAB (the engine's tile pass) may run such plans.
+// With fuse2, every CNOT whose control and target are local is merged with the one-qubit ops that
+// can move next to it on those qubits (the last before it and the first after it on each, when
+// they are pair or diagonal ops) into an EX_U4 block; only kernels that execute EX_U4 (the
+// engine's tile pass) may run such plans.  Not combined with zyz or tables.
 bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int precision, Plan& out, std::string& err,
-                bool use_params = false, int zyz = ZYZ_DEFAULT, bool tables = false);
+                bool use_params = false, int zyz = ZYZ_DEFAULT, bool tables = false, bool fuse2 = false);
 
 // Rewrites a tile plan (without EX_PTAB ops) as register programs for the register-tiled pass
 // kernel (tile widths 9..13): EX_LAYOUT ops are inserted so that the target of every non-diagonal
@@ -128,6 +142,9 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int precisi
 // position or a global qubit as before).  Every pass starts and ends in the layout whose register
 // positions are the top four tile positions.  Returns the number of layout changes.
 int to_register_program(Plan& plan);
+
+// The EX_U4 fusion of plan_tiles(fuse2): returns the number of one-qubit ops merged into blocks.
+int fuse_two_qubit(Plan& plan);
 
 // Dense dispatch codes of register-program ops, in flags >> kRegCodeShift: one jump table in the
 // kernel selects the kind and its register slots together.

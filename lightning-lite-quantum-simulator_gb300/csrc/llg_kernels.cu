@@ -173,6 +173,44 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     return done != 0;
 }
 
+// EX_U4 (fuse_two_qubit) on a complex64 tile: the 4x4 block on local qubits q0 (index bit 0) and
+// q1 (index bit 1), one quad of amplitudes per thread and iteration; the 16 complex entries are
+// read once per thread (the table is L2/L1-resident: 128 bytes per block)
+template <class P>
+__device__ __forceinline__ void tile_u4_f32(typename P::S* tile, uint32_t tsize, const ExecOp& o,
+                                            const uint64_t* __restrict__ tables) {
+    static_assert(sizeof(typename P::S) == 8, "complex64 tiles only");
+    const uint64_t* mt = tables + 2 * o.mask;
+    float mr[16], mi[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        mr[i] = P::k_from_bits(__ldg(mt + 2 * i));
+        mi[i] = P::k_from_bits(__ldg(mt + 2 * i + 1));
+    }
+    const uint32_t bx = 1u << o.q0, by = 1u << o.q1;
+    const uint32_t lo = bx < by ? bx : by, hi = bx < by ? by : bx;
+    float2* t2 = reinterpret_cast<float2*>(tile);
+    for (uint32_t r = threadIdx.x; r < (tsize >> 2); r += blockDim.x) {
+        const uint32_t j0 = ins0(ins0(r, lo), hi);
+        const uint32_t idx[4] = {j0, j0 | bx, j0 | by, j0 | bx | by};
+        float2 v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) v[k] = t2[idx[k]];
+#pragma unroll
+        for (int row = 0; row < 4; ++row) {
+            float re = 0.0f, im = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                re = fmaf(mr[row * 4 + k], v[k].x, re);
+                re = fmaf(-mi[row * 4 + k], v[k].y, re);
+                im = fmaf(mr[row * 4 + k], v[k].y, im);
+                im = fmaf(mi[row * 4 + k], v[k].x, im);
+            }
+            t2[idx[row]] = make_float2(re, im);
+        }
+    }
+}
+
 template <class P>
 __global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, PassDesc pd, const ExecOp* __restrict__ ops,
                                                const uint64_t* __restrict__ tables, double2* __restrict__ mirror,
@@ -281,6 +319,17 @@ __global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, 
                 break;
             }
             case EX_CNOT: tile_cnot<P>(tile, tsize, base, o); break;
+            case EX_U4:  // emitted for complex64 plans only
+                if constexpr (sizeof(S) == 8) tile_u4_f32<P>(tile, tsize, o, tables);
+                break;
+            case EX_U2C: {  // the 2x2 for this tile's control bit, applied as a generic pair op
+                ExecOp u = o;
+                const uint64_t* mt = tables + 2 * (o.mask + 4 * ((base >> o.q0) & 1));
+#pragma unroll
+                for (int i = 0; i < 8; ++i) u.c[i] = __ldg(mt + i);
+                tile_pairs<P, EX_U2>(tile, tsize >> 1, o.q1, u);
+                break;
+            }
             case EX_MCZ: {
                 if ((base & o.nl_mask) == o.nl_mask) {
                     const uint32_t lm = (uint32_t)o.mask;

@@ -587,6 +587,189 @@ int to_register_program(Plan& out) {
     return changes;
 }
 
+// ------------------------------------------------------------------------------------------
+// Two-qubit blocks.  A CNOT on local qubits c, t and the one-qubit ops next to it on c and t (the
+// last op before it on each qubit and the first after it, when those are pair or local diagonal
+// ops: nothing between them and the CNOT touches their qubit, so they may move to it) become one
+// 4x4 matrix M = (A_c x A_t) CNOT (B_c x B_t), applied as EX_U4 in one shared-memory round trip.
+// Coefficients are FP64 bits here (packed for the state's precision by plan_tiles afterwards).
+// ------------------------------------------------------------------------------------------
+namespace {
+
+using cd2 = std::complex<double>;
+
+// the 2x2 of a one-qubit executor op on a local qubit (false: not such an op)
+bool op_2x2(const ExecOp& e, cd2 m[4]) {
+    if (e.flags & OPF_NONLOCAL_Q0) return false;
+    auto c = [&](int i) { return coef_value(e.c[i]); };
+    switch (e.kind) {
+        case EX_U2:
+            for (int r = 0; r < 4; ++r) m[r] = cd2(c(2 * r), c(2 * r + 1));
+            return true;
+        case EX_RX: m[0] = m[3] = c(0); m[1] = m[2] = cd2(0.0, -c(1)); return true;
+        case EX_RY: m[0] = m[3] = c(0); m[1] = -c(1); m[2] = c(1); return true;
+        case EX_H: m[0] = m[1] = m[2] = c(0); m[3] = -c(0); return true;
+        case EX_X: m[0] = m[3] = 0.0; m[1] = m[2] = 1.0; return true;
+        case EX_DIAG: m[0] = cd2(c(0), c(1)); m[1] = m[2] = 0.0; m[3] = cd2(c(2), c(3)); return true;
+        default: return false;
+    }
+}
+
+bool touches(const ExecOp& e, int q) {
+    switch (e.kind) {
+        case EX_CNOT: return e.q1 == q || (!(e.flags & OPF_NONLOCAL_Q0) && e.q0 == q);
+        case EX_U4: return e.q0 == q || e.q1 == q;
+        case EX_U2C: return e.q1 == q;
+        case EX_MCZ: return (e.mask >> q) & 1;
+        default: return !(e.flags & OPF_NONLOCAL_Q0) && e.q0 == q;
+    }
+}
+
+// M <- (U on index bit p) M, for 4x4 row-major M
+void left_1q(cd2 M[16], const cd2 u[4], int p) {
+    cd2 R[16];
+    for (int r = 0; r < 4; ++r)
+        for (int col = 0; col < 4; ++col) {
+            const int br = (r >> p) & 1, r0 = r & ~(1 << p);
+            R[r * 4 + col] = u[br * 2 + 0] * M[(r0) * 4 + col] + u[br * 2 + 1] * M[(r0 | (1 << p)) * 4 + col];
+        }
+    for (int i = 0; i < 16; ++i) M[i] = R[i];
+}
+
+}  // namespace
+
+int fuse_two_qubit(Plan& out) {
+    int fused = 0;
+    for (PassDesc& pd : out.passes) {
+        const int b = pd.op_begin, m = pd.nops;
+        std::vector<char> gone(m, 0);
+        for (int i = 0; i < m; ++i) {
+            ExecOp& x = out.ops[b + i];
+            if (x.kind != EX_CNOT) continue;
+            if (x.flags & OPF_NONLOCAL_Q0) {
+                // global control: only the target's neighbours can join; one 2x2 per control value
+                const int tq = x.q1;
+                int bj = -1, aj = -1;
+                cd2 ub[4], ua[4];
+                for (int j = i - 1; j >= 0; --j) {
+                    if (gone[j] || !touches(out.ops[b + j], tq)) continue;
+                    if (op_2x2(out.ops[b + j], ub)) bj = j;
+                    break;
+                }
+                for (int j = i + 1; j < m; ++j) {
+                    if (gone[j] || !touches(out.ops[b + j], tq)) continue;
+                    if (op_2x2(out.ops[b + j], ua)) aj = j;
+                    break;
+                }
+                if (bj < 0 && aj < 0) continue;
+                const cd2 one(1.0, 0.0), zero(0.0, 0.0);
+                const cd2 ph = (x.flags & OPF_PHASE) ? cd2(coef_value(x.c[0]), coef_value(x.c[1])) : one;
+                cd2 B[4] = {one, zero, zero, one}, A[4] = {one, zero, zero, one};
+                if (bj >= 0) std::copy(ub, ub + 4, B);
+                if (aj >= 0) std::copy(ua, ua + 4, A);
+                // control 0: A B; control 1: A diag(1, ph) X B (a phased CNOT multiplies target 1)
+                const cd2 X1[4] = {zero, one, ph, zero};
+                auto mul = [](const cd2* p, const cd2* q, cd2* r) {
+                    r[0] = p[0] * q[0] + p[1] * q[2];
+                    r[1] = p[0] * q[1] + p[1] * q[3];
+                    r[2] = p[2] * q[0] + p[3] * q[2];
+                    r[3] = p[2] * q[1] + p[3] * q[3];
+                };
+                cd2 M0[4], XB[4], M1[4];
+                mul(A, B, M0);
+                mul(X1, B, XB);
+                mul(A, XB, M1);
+                ExecOp u = blank(EX_U2C);
+                u.q0 = x.q0;
+                u.q1 = tq;
+                u.flags = OPF_NONLOCAL_Q0;
+                u.mask = out.tables.size() / 2;
+                for (const cd2* mm : {M0, M1})
+                    for (int r = 0; r < 4; ++r) {
+                        out.tables.push_back(pack_coef(LLG_F64, mm[r].real()));
+                        out.tables.push_back(pack_coef(LLG_F64, mm[r].imag()));
+                    }
+                x = u;
+                if (bj >= 0) gone[bj] = 1, ++fused;
+                if (aj >= 0) gone[aj] = 1, ++fused;
+                continue;
+            }
+            const int q[2] = {x.q0, x.q1};  // index bit 0: the control, bit 1: the target
+            int before[2] = {-1, -1}, after[2] = {-1, -1};
+            cd2 ub[2][4], ua[2][4];
+            for (int k = 0; k < 2; ++k) {
+                for (int j = i - 1; j >= 0; --j) {
+                    if (gone[j] || !touches(out.ops[b + j], q[k])) continue;
+                    if (op_2x2(out.ops[b + j], ub[k])) before[k] = j;
+                    break;
+                }
+                for (int j = i + 1; j < m; ++j) {
+                    if (gone[j] || !touches(out.ops[b + j], q[k])) continue;
+                    if (op_2x2(out.ops[b + j], ua[k])) after[k] = j;
+                    break;
+                }
+            }
+            if (before[0] < 0 && before[1] < 0 && after[0] < 0 && after[1] < 0) continue;
+            cd2 M[16];
+            for (int r = 0; r < 16; ++r) M[r] = 0.0;
+            // CNOT: |c, t> -> |c, t ^ c>, index k = c + 2 t; a phased CNOT then multiplies |1, 1>
+            const cd2 ph = (x.flags & OPF_PHASE) ? cd2(coef_value(x.c[0]), coef_value(x.c[1])) : cd2(1.0, 0.0);
+            M[0 * 4 + 0] = 1.0;
+            M[2 * 4 + 2] = 1.0;
+            M[3 * 4 + 1] = ph;   // |1,0> -> |1,1>
+            M[1 * 4 + 3] = 1.0;  // |1,1> -> |1,0>
+            cd2 Mb[16];
+            for (int r = 0; r < 16; ++r) Mb[r] = (r % 5 == 0) ? cd2(1.0, 0.0) : cd2(0.0, 0.0);
+            for (int k = 0; k < 2; ++k)
+                if (before[k] >= 0) left_1q(Mb, ub[k], k);
+            // M <- M Mb
+            cd2 R[16];
+            for (int r = 0; r < 4; ++r)
+                for (int col = 0; col < 4; ++col) {
+                    cd2 v = 0.0;
+                    for (int k = 0; k < 4; ++k) v += M[r * 4 + k] * Mb[k * 4 + col];
+                    R[r * 4 + col] = v;
+                }
+            for (int k = 0; k < 2; ++k)
+                if (after[k] >= 0) left_1q(R, ua[k], k);
+            ExecOp u = blank(EX_U4);
+            u.q0 = q[0];
+            u.q1 = q[1];
+            u.mask = out.tables.size() / 2;
+            for (int r = 0; r < 16; ++r) {
+                out.tables.push_back(pack_coef(LLG_F64, R[r].real()));
+                out.tables.push_back(pack_coef(LLG_F64, R[r].imag()));
+            }
+            x = u;
+            for (int k = 0; k < 2; ++k) {
+                if (before[k] >= 0) gone[before[k]] = 1, ++fused;
+                if (after[k] >= 0) gone[after[k]] = 1, ++fused;
+            }
+        }
+        // compact the pass
+        int w = b;
+        for (int i = 0; i < m; ++i)
+            if (!gone[i]) {
+                out.ops[w] = out.ops[b + i];
+                out.source_index[w] = out.source_index[b + i];
+                ++w;
+            }
+        pd.nops = w - b;
+    }
+    // close the gaps between passes
+    std::vector<ExecOp> ops;
+    std::vector<int> src;
+    for (PassDesc& pd : out.passes) {
+        const int begin = (int)ops.size();
+        ops.insert(ops.end(), out.ops.begin() + pd.op_begin, out.ops.begin() + pd.op_begin + pd.nops);
+        src.insert(src.end(), out.source_index.begin() + pd.op_begin, out.source_index.begin() + pd.op_begin + pd.nops);
+        pd.op_begin = begin;
+    }
+    out.ops.swap(ops);
+    out.source_index.swap(src);
+    return fused;
+}
+
 static bool is_param_op(const llg_op& op, bool use_params) {
     return use_params && op.param >= 0 && (op.kind == LLG_OP_RX || op.kind == LLG_OP_RY || op.kind == LLG_OP_RZ);
 }
@@ -623,7 +806,7 @@ static bool split_zyz(const double* m, std::complex<double>& z, double& c, doubl
 }
 
 bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan& out, std::string& err,
-                bool use_params, int zyz, bool tables) {
+                bool use_params, int zyz, bool tables, bool fuse2) {
     out.passes.clear();
     out.ops.clear();
     out.source_index.clear();
@@ -1027,6 +1210,7 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
         }
     }
     if (tables) gather_phase_tables(out);
+    if (fuse2 && !use_zyz && !tables) fuse_two_qubit(out);
     if (P != PP) {
         for (ExecOp& e : out.ops)
             for (uint64_t& c : e.c) c = pack_coef(P, coef_value(c));

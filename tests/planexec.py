@@ -97,6 +97,23 @@ def execute(psi: np.ndarray, n: int, passes: np.ndarray, xops: np.ndarray, table
                 continue
             if k <= 4 or k in (11, 12, 14, 15, 16, 17):
                 _pair(tile, q0, _matrix(x))
+            elif k == 20:  # 4x4 block on (q0, q1): 16 table entries from `mask`, row-major
+                off = int(x["mask"])
+                mm = tables[off:off + 16].reshape(4, 4)
+                v = tile.reshape(tile.shape[0], -1)
+                b0 = ((lidx >> q0) & 1) + 2 * ((lidx >> q1) & 1)
+                base_idx = lidx[b0 == 0]
+                cols = [base_idx, base_idx | (1 << q0), base_idx | (1 << q1), base_idx | (1 << q0) | (1 << q1)]
+                vals = [v[:, c].copy() for c in cols]
+                for r in range(4):
+                    v[:, cols[r]] = sum(mm[r, k2] * vals[k2] for k2 in range(4))
+            elif k == 21:  # 2x2 on q1 chosen by the tile's global control bit q0
+                off = int(x["mask"])
+                sel = ((bases >> q0) & 1).astype(bool)
+                for s_, val in ((~sel, 0), (sel, 1)):
+                    sub = tile[s_]
+                    _pair(sub, q1, tables[off + 4 * val:off + 4 * val + 4].reshape(2, 2))
+                    tile[s_] = sub
             elif k == 18:  # phase table: tile amplitude l times entry l
                 off = int(x["mask"])
                 tile *= tables[off:off + (1 << t)][None, :]

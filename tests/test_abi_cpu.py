@@ -113,6 +113,32 @@ def test_plan_of_random_2024_circuits(built, golden):
         assert np.max(np.abs(got - oracle.run_ops(n, ops))) < 1e-12
 
 
+@pytest.mark.parametrize("n,tile", [(6, 5), (9, 6), (12, 9), (14, 13)])
+def test_two_qubit_blocks_reproduce_the_oracle(built, n, tile):
+    # complex64 tile passes merge each local CNOT with its neighbouring one-qubit ops into a 4x4
+    # block (kind 20): the plan's product is unchanged
+    rng = np.random.default_rng(500 + n)
+    for ops in (random_ops(n, 300, rng), workloads.layered_rotations(n, 6, seed=n)):
+        passes, xops, tab = llgpu.plan_export(n, ops, tile, fuse2=True)
+        p0, x0 = llgpu.plan_export(n, ops, tile)
+        blocks, cblocks = int(np.sum(xops["kind"] == 20)), int(np.sum(xops["kind"] == 21))
+        assert blocks > 0 and len(xops) < len(x0)
+        assert tab.size == 16 * blocks + 8 * cblocks
+        got = execute(oracle.zero_state(n), n, passes, xops, tab)
+        assert np.max(np.abs(got - oracle.run_ops(n, ops))) < 1e-12
+    with pytest.raises(ValueError):
+        llgpu.plan_export(n, ops, tile, fuse2=True, zyz=True)
+
+
+def test_two_qubit_blocks_on_the_layered_circuit(built):
+    # 30 qubits, 13-qubit tiles: most one-qubit ops move into the blocks of the brickwork's CNOTs
+    ops = workloads.layered_rotations(30, 20)
+    p0, x0 = llgpu.plan_export(30, ops, 13)
+    passes, xops, tab = llgpu.plan_export(30, ops, 13, fuse2=True)
+    assert len(passes) == len(p0)
+    assert len(xops) < 0.6 * len(x0)
+
+
 @pytest.mark.parametrize("tile", [9, 11, 13])
 def test_register_programs_reproduce_the_oracle(built, tile):
     n = 16
