@@ -367,9 +367,12 @@ def test_twenty_qubit_layered_vs_oracle():
     for fusion in ("tile", "none"):
         got = run_gpu(n, ops, "df64", fusion)
         assert np.max(np.abs(got - want)) <= 1e-12
+    # complex64: the direction to 1e-9 in fidelity; the norm drifts at the level of fp32 rounding
+    # of the gates' coefficients (a slightly non-unitary matrix applied to every amplitude)
     got = run_gpu(n, ops, "complex64", "tile")
-    fid = abs(np.vdot(want, got)) ** 2
-    assert 1 - fid < 1e-9
+    norm = np.vdot(got, got).real
+    fid = abs(np.vdot(want, got)) ** 2 / norm
+    assert 1 - fid < 1e-9 and abs(norm - 1) < 1e-5
 
 
 def _sk_terms(n, seed):
