@@ -152,8 +152,12 @@ __global__ void __launch_bounds__(TcShape<KQ>::kThreads, TcShape<KQ>::kMinBlocks
     const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kReals >> 3) << 17) |
                            ((uint32_t)(kTcGroups >> 4) << 24);
     const uint32_t lbo = 128, sbo = (kReals / 8) * 128;
-    const int gl = tid & (kTcGroups - 1);  // the group this thread loads, slices and stores
-    const int h = tid >> 7;                // which kPer of its kAmps amplitudes
+    // a group's kAmps / kPer threads sit in one warp: G consecutive lanes take G groups, the next G
+    // lanes the same groups' next kPer amplitudes, and so on, so the group's scale is a shuffle
+    // reduction (the slice stores of a warp still fill whole core-matrix rows)
+    constexpr int kH = kAmps / kPer, kG = 32 / kH;
+    const int gl = (tid % kG) + kG * (tid >> 5);  // the group this thread loads, slices and stores
+    const int h = (tid / kG) % kH;                 // which kPer of its kAmps amplitudes
     uint32_t phase = 0;
     // a thread's amplitudes of a tile go to sIn[(kPer h + i) * 128 + gl] by asynchronous copies,
     // issued one tile ahead so that their latency hides behind the products and the epilogue
@@ -183,7 +187,7 @@ __global__ void __launch_bounds__(TcShape<KQ>::kThreads, TcShape<KQ>::kMinBlocks
     // each thread writes whole amplitudes, a warp 32 consecutive groups per amplitude
     auto epilogue = [&](uint64_t tile, int set, int egb, int a0) {
         const int row = 32 * (warp & 3) + lane;
-        const int eg = eg_s[egb][row] - 1000;  // stored with the atomicMax offset
+        const int eg = eg_s[egb][row] - 1000;  // stored with an offset of 1000
         df out[2][8];
 #pragma unroll
         for (int part = 0; part < 2; ++part) {
@@ -250,35 +254,34 @@ __global__ void __launch_bounds__(TcShape<KQ>::kThreads, TcShape<KQ>::kMinBlocks
             a[i] = make_float4(re.hi, im.hi, re.lo, im.lo);
             mx = fmaxf(mx, fmaxf(fabsf(a[i].x), fabsf(a[i].y)));
         }
-        // eg_s[egb] was last read by the epilogue of tile i - 3, during tile i - 1: the barriers of
-        // the tile in between separate that read from this write
-        if (h == 0) eg_s[egb][gl] = 0;
-        __syncthreads();
+        // the group's threads agree on the largest high part (lanes kG, 2 kG, ... apart)
+#pragma unroll
+        for (int off = kG; off < 32; off <<= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
         // all |x| < 2^e with e from the high parts' largest exponent; clamped so that the scale
         // factors 2^(8 - e) and 2^(32 - e) below stay normal floats (groups under 2^-94 keep their
         // absolute error below 2^-134 instead of a relative one)
         int e = (int)((__float_as_uint(mx) >> 23) & 0xFF) - 126;
         e = max(e, -94);
-        atomicMax(&eg_s[egb][gl], e + 1000);  // the group's threads agree on the largest exponent
+        // for the epilogue of this tile (during the next one, after this tile's slicing barrier);
+        // eg_s[egb] was last read by the epilogue of tile i - 3, during tile i - 1
+        if (h == 0) eg_s[egb][gl] = e + 1000;
+        // ---- the previous tile's products must be done before its slices are overwritten; the
+        // barrier also ends every thread's reads of sIn before the next tile's copies start ----
+        if (have_prev && !wait_mma(phase)) abort_s = 1;
         __syncthreads();
-        e = eg_s[egb][gl] - 1000;
-        // every thread has read its amplitudes out of sIn: start the next tile's copies
-        if (tile + gridDim.x < ntiles) prefetch(tile + gridDim.x);
-        // ---- the previous tile's products must be done before its slices are overwritten ----
+        if (abort_s) {
+            // report, then give the products in flight a second bounded wait before the
+            // accumulators are freed
+            if (tid == 0) atomicExch(err_flag, 1);
+            wait_mma(phase);
+            have_prev = false;
+            break;
+        }
         if (have_prev) {
-            if (!wait_mma(phase)) abort_s = 1;
-            __syncthreads();
-            if (abort_s) {
-                // report, then give the products in flight a second bounded wait before the
-                // accumulators are freed
-                if (tid == 0) atomicExch(err_flag, 1);
-                wait_mma(phase);
-                have_prev = false;
-                break;
-            }
             phase ^= 1;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         }
+        if (tile + gridDim.x < ntiles) prefetch(tile + gridDim.x);
         // ---- six 8-bit slices per real, into the core-matrix layout ----
         {
             const float sc = pow2f(8 - e), sclo = pow2f(32 - e);
