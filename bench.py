@@ -320,7 +320,7 @@ def plan_for(precision: str, n: int, ops, tile_q: int, regs: bool = False):
     if precision == "complex64":
         p, x, tab = llgpu.plan_export(n, ops, tile_q, fuse2=True)
         return p, x, int(tab.nbytes)
-    p, x, tab = llgpu.plan_export(n, ops, tile_q, zyz=True, tables=True)
+    p, x, tab = llgpu.plan_export(n, ops, tile_q, zyz=True, tables=True, df64=precision == "df64")
     return p, x, int(tab.nbytes)
 
 

@@ -506,6 +506,10 @@ int llg_plan_export(int n, const llg_op* ops, int nops, int tile_qubits, llg_pas
  * 4x4 matrix on local qubits q0 (index bit 0) and q1 (index bit 1), 16 entries from table entry
  * `mask`, row-major); alone, without the other options. */
 #define LLG_PLAN_FUSE2 8
+/* LLG_PLAN_DF64: with LLG_PLAN_ZYZ, the plan a double-float state gets (the tangent rotations'
+ * dropped scale is absorbed before it reaches 2^-40 instead of 2^-300); the coefficients are
+ * exported as doubles either way. */
+#define LLG_PLAN_DF64 16
 int llg_plan_export_ex(int n, const llg_op* ops, int nops, int tile_qubits, int flags, llg_pass_info* passes,
                        int max_passes, int* npasses, llg_exec_op* xops, int max_xops, int* nxops);
 /* The eigenvalue d(i) of the diagonal observable sum_k coeff_k Z_{a_k} Z_{b_k} (b_k < 0: Z_{a_k}) for

@@ -1164,9 +1164,24 @@ int export_plan(int n, const llg_op* ops, int nops, int tile_qubits, int flags, 
     std::string err;
     if ((flags & LLG_PLAN_FUSE2) && (flags & (LLG_PLAN_ZYZ | LLG_PLAN_TABLES | LLG_PLAN_REGS)))
         return set_error(LLG_EINVAL, "plan_export: two-qubit blocks are planned alone");
-    if (!plan_tiles(n, ops, nops, tile_qubits, LLG_F64, plan, err, false, (flags & LLG_PLAN_ZYZ) ? ZYZ_ON : ZYZ_OFF,
+    const int prec = (flags & LLG_PLAN_DF64) ? LLG_DF64 : LLG_F64;
+    if (!plan_tiles(n, ops, nops, tile_qubits, prec, plan, err, false, (flags & LLG_PLAN_ZYZ) ? ZYZ_ON : ZYZ_OFF,
                     (flags & LLG_PLAN_TABLES) != 0 && (flags & LLG_PLAN_REGS) == 0, (flags & LLG_PLAN_FUSE2) != 0))
         return set_error(LLG_EINVAL, err);
+    if (prec == LLG_DF64) {
+        // back from the fp32 (hi, lo) slots of a double-float plan to doubles (hi + lo is exact)
+        auto unpack = [](uint64_t& c) {
+            float h, l;
+            const uint32_t bh = (uint32_t)c, bl = (uint32_t)(c >> 32);
+            std::memcpy(&h, &bh, 4);
+            std::memcpy(&l, &bl, 4);
+            const double v = (double)h + (double)l;
+            std::memcpy(&c, &v, 8);
+        };
+        for (ExecOp& e : plan.ops)
+            for (uint64_t& c : e.c) unpack(c);
+        for (uint64_t& c : plan.tables) unpack(c);
+    }
     if (flags & LLG_PLAN_REGS) {
         if (tile_qubits < 9) return set_error(LLG_EINVAL, "plan_export: register programs need tiles of 9+ qubits");
         to_register_program(plan);

@@ -28,8 +28,11 @@
 
 namespace llg {
 
-// Smallest |product of dropped rotation factors| a pass may carry before a full EX_ZY absorbs it.
-constexpr double kMinPassScale = 0x1p-40;
+// Smallest |product of dropped rotation factors| a flush may carry before a full EX_ZY absorbs it:
+// double-float amplitudes then stay within 2^40 of their true scale (FP32 range to 2^127), IEEE
+// double ones within 2^300 (range to 2^1023).
+constexpr double kMinScaleDF64 = 0x1p-40;
+constexpr double kMinScaleF64 = 0x1p-300;
 
 bool is_single_qubit(int kind) {
     return kind == LLG_OP_H || kind == LLG_OP_X || kind == LLG_OP_RX || kind == LLG_OP_RY || kind == LLG_OP_RZ ||
@@ -848,6 +851,18 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
     std::vector<int> touched, need, deferred, included;
     std::vector<char> blocked(64, 0);
 
+    // Rotations as EX_ZT / EX_ZC leave the amplitudes divided by sigma, the product of their
+    // dropped factors f (|f| >= 1/sqrt 2 each).  Sigma is carried across the passes of the flush:
+    // one full EX_ZY absorbs it mid-flush when |sigma| would fall below min_scale, and at the end
+    // the flush's last EX_ZT / EX_ZC is rewritten as that EX_ZY, so the flush stores true
+    // amplitudes (every op after it is unitary and scale-free).  A pass boundary is no absorption
+    // point: tiles hold amplitudes scaled by the same 1 / sigma everywhere in the register.
+    const double min_scale = P == LLG_F64 ? kMinScaleF64 : kMinScaleDF64;
+    double sigma = 1.0;
+    int last_t = -1;  // index in out.ops of the last EX_ZT / EX_ZC since sigma was 1
+    double last_f = 1.0, last_c = 1.0, last_s = 0.0;
+    std::complex<double> last_g(1.0, 0.0);
+
     // remaining[head..] are the ops still to place, in order.  A pass scans a prefix of them; its
     // deferred ops are written back right-aligned inside that prefix and head moves to the first,
     // so the unscanned tail is never copied.
@@ -917,15 +932,6 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
 
         // Peephole fusion of same-qubit 1-qubit runs, then lowering to local indices.
         std::vector<Pending> pend(n);
-        // Rotations as EX_ZT / EX_ZC leave the pass's amplitudes divided by sigma, the product of
-        // their dropped factors f (|f| >= 1/sqrt 2 each).  One full EX_ZY absorbs sigma: mid-pass
-        // when |sigma| would fall below 2^-40 (amplitudes stay below 2^40 of their true scale), and
-        // at the end of the pass the last EX_ZT / EX_ZC is rewritten as that EX_ZY, so every pass
-        // stores true amplitudes.
-        double sigma = 1.0;
-        int last_t = -1;             // index in out.ops of the last EX_ZT / EX_ZC since sigma was 1
-        double last_f = 1.0, last_c = 1.0, last_s = 0.0;
-        std::complex<double> last_g(1.0, 0.0);
         // local indices for one executor op (global qubits in), then append it
         auto emit_raw = [&](ExecOp e, int src) {
             switch (e.kind) {
@@ -990,7 +996,7 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
                 phase *= z;
                 const bool tan_form = std::fabs(c) >= std::fabs(sn);
                 const double f = tan_form ? c : sn;
-                if (std::fabs(sigma * f) < kMinPassScale) {  // absorb sigma here: a full EX_ZY
+                if (std::fabs(sigma * f) < min_scale) {  // absorb sigma here: a full EX_ZY
                     e = blank(EX_ZY);
                     e.q0 = q;
                     const double v[4] = {eg.real(), eg.imag(), sigma * c, sigma * sn};
@@ -1148,15 +1154,6 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
         for (int q = 0; q < n; ++q)
             if (!flush_pending(q)) return false;
 
-        if (last_t >= 0 && sigma != 1.0) {
-            // the pass's last EX_ZT / EX_ZC becomes the EX_ZY that absorbs sigma: before it the
-            // amplitudes carry 1 / (sigma / last_f), so its rotation is scaled by sigma / last_f
-            ExecOp& e = out.ops[last_t];
-            const double g = sigma / last_f;
-            e.kind = EX_ZY;
-            const double v[4] = {last_g.real(), last_g.imag(), g * last_c, g * last_s};
-            for (int k = 0; k < 4; ++k) e.c[k] = pack_coef(PP, v[k]);
-        }
         pd.nops = (int)out.ops.size() - pd.op_begin;
         if (included.empty()) {
             err = "planner made no progress";
@@ -1166,6 +1163,15 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
         size_t w = scanned;
         for (size_t k = deferred.size(); k-- > 0;) remaining[--w] = deferred[k];
         head = w;
+    }
+    if (last_t >= 0 && sigma != 1.0) {
+        // the flush's last EX_ZT / EX_ZC becomes the EX_ZY that absorbs sigma: before it the
+        // amplitudes carry 1 / (sigma / last_f), so its rotation is scaled by sigma / last_f
+        ExecOp& e = out.ops[last_t];
+        const double g = sigma / last_f;
+        e.kind = EX_ZY;
+        const double v[4] = {last_g.real(), last_g.imag(), g * last_c, g * last_s};
+        for (int k = 0; k < 4; ++k) e.c[k] = pack_coef(PP, v[k]);
     }
     if (use_zyz && !out.passes.empty()) {
         // the carried phases that reached the end, as diag(1, p) ops in the last pass; the global

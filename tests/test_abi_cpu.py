@@ -156,8 +156,8 @@ def test_zyz_plan_carries_the_global_phase_in_one_u2(built):
     passes, xops = llgpu.plan_export(n, ops, 8, zyz=True)
     kinds = np.bincount(xops["kind"], minlength=16)
     # rotations as RY diag(1, g) over their dropped cos / sin factor (kinds 14, 15), output phases
-    # carried; one full RY per pass (kind 12) absorbs the pass's factors
-    assert kinds[0] == 1 and kinds[14] + kinds[15] > 50 and kinds[12] <= len(passes)
+    # carried; one full RY (kind 12) absorbs the flush's dropped factors
+    assert kinds[0] == 1 and kinds[14] + kinds[15] > 50 and kinds[12] == 1
     assert kinds[5] == 0  # every RZ folded into carried phases
     phased = (xops["kind"] == 6) & ((xops["flags"] & 8) != 0)
     assert phased.sum() > 10  # carried target phases pushed through CNOTs
@@ -184,12 +184,12 @@ def test_zyz_keeps_non_unitary_gates_generic(built):
     assert np.max(np.abs(got - want)) <= 1e-12 * max(1.0, np.max(np.abs(want)))
 
 
-def _pass_scales(passes, xops):
-    """Per pass: the smallest running product of the factors dropped by kind 14/15 ops since the
-    last full rotation (kind 12), and the product left at the end of the pass."""
-    out = []
+def _flush_scales(passes, xops):
+    """The smallest running product of the factors dropped by kind 14/15 ops since the last full
+    rotation (kind 12), over the whole flush (the product carries across passes), and the product
+    left at the end of the flush."""
+    sig, low = 1.0, 1.0
     for p in passes:
-        sig, low = 1.0, 1.0
         for x in xops[p["op_begin"]:p["op_begin"] + p["nops"]]:
             k = int(x["kind"])
             if k in (14, 15):
@@ -197,26 +197,30 @@ def _pass_scales(passes, xops):
                 low = min(low, sig)
             elif k == 12:
                 sig = 1.0
-        out.append((low, sig))
-    return out
+    return low, sig
 
 
-def test_tangent_rotations_renormalise_each_pass(built):
-    # one 8-qubit pass of 600 rotations: the dropped factors (|f| >= 1/sqrt 2 each) would shrink
-    # to ~2^-300; full rotations absorb them before 2^-40 and at the end of every pass
+@pytest.mark.parametrize("df64,floor", [(False, 2.0 ** -300), (True, 2.0 ** -40)])
+def test_tangent_rotations_renormalise_per_flush(built, df64, floor):
+    # 600 rotations on 8 qubits: the dropped factors (|f| >= 1/sqrt 2 each) shrink the running
+    # scale; full rotations absorb it before the precision's floor (2^-40 for double-float, 2^-300
+    # for IEEE double) and once at the end of the flush, whatever the pass boundaries
     n = 8
     ops = workloads.layered_rotations(n, layers=75)
     for tile in (8, 5):
-        passes, xops = llgpu.plan_export(n, ops, tile, zyz=True)
+        passes, xops = llgpu.plan_export(n, ops, tile, zyz=True, df64=df64)
         if tile == 8:
             assert len(passes) == 1
         kinds = np.bincount(xops["kind"], minlength=16)
-        # one full rotation per pass, plus one per ~60 or more rotations inside a long pass
-        assert 0 < kinds[12] <= len(passes) + (kinds[14] + kinds[15]) // 60
-        for low, end in _pass_scales(passes, xops):
-            assert low >= 2.0 ** -40.5 and end == 1.0
+        ntan = kinds[14] + kinds[15]
+        # one full rotation at the end, plus one per ~60 or more tangent rotations for double-float
+        assert 0 < kinds[12] <= 1 + (ntan // 60 if df64 else 0)
+        low, end = _flush_scales(passes, xops)
+        assert low >= floor / np.sqrt(2.0) and end == 1.0
         got = execute(oracle.zero_state(n), n, passes, xops)
         assert np.max(np.abs(got - oracle.run_ops(n, ops))) < 1e-12
+    if df64:
+        return
     # angles near 0 and pi/2 (tangent and cotangent forms, |coefficient| <= 1), and exactly pi
     rng = np.random.default_rng(5)
     recs = []
