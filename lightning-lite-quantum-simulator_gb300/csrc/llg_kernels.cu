@@ -211,8 +211,11 @@ __device__ __forceinline__ void tile_u4_f32(typename P::S* tile, uint32_t tsize,
     }
 }
 
-template <class P>
-__global__ void __launch_bounds__(1024) k_tile(typename P::S* __restrict__ psi, PassDesc pd, const ExecOp* __restrict__ ops,
+// MAXT: the largest CTA the instantiation runs.  1024 caps a thread at 64 registers; the 256-thread
+// form keeps three CTAs per SM (the shared-memory limit of 12- and 13-qubit tiles) and may use 85,
+// enough for a two-qubit block's 16 complex coefficients to stay in registers across its quads.
+template <class P, int MAXT>
+__global__ void __launch_bounds__(MAXT, MAXT == 256 ? 3 : 1) k_tile(typename P::S* __restrict__ psi, PassDesc pd, const ExecOp* __restrict__ ops,
                                                const uint64_t* __restrict__ tables, double2* __restrict__ mirror,
                                                int* __restrict__ err_flag) {
     using S = typename P::S;
@@ -547,15 +550,24 @@ size_t tile_smem_bytes(int t, int low) {
 template <class P>
 cudaError_t tile_pass_t(void* vpsi, int n, const PassDesc& pd, const ExecOp* d_ops, const uint64_t* d_tables, int threads,
                         double* mirror, int* err_flag, cudaStream_t s) {
-    // the largest dynamic shared memory of any tile, set once (thread-safe static initialisation)
-    static const cudaError_t attr = cudaFuncSetAttribute(k_tile<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                         (int)tile_smem_bytes<P>(tile_max_qubits(P::kPrecision), 4));
+    // the largest dynamic shared memory of any tile, set once per instantiation (thread-safe static
+    // initialisation)
+    const int max_smem = (int)tile_smem_bytes<P>(tile_max_qubits(P::kPrecision), 4);
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_tile<P, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
+    static const cudaError_t attr256 =
+        cudaFuncSetAttribute(k_tile<P, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
     if (attr != cudaSuccess) return attr;
+    if (attr256 != cudaSuccess) return attr256;
     const size_t smem = tile_smem_bytes<P>(pd.t, pd.low);
     const uint64_t ntiles = 1ULL << (n - pd.t);
     if (threads <= 0) threads = pd.t >= 10 ? 512 : (pd.t >= 6 ? (1 << (pd.t - 1)) : 32);
-    k_tile<P><<<(unsigned)ntiles, threads, smem, s>>>(static_cast<typename P::S*>(vpsi), pd, d_ops, d_tables,
-                                                      reinterpret_cast<double2*>(mirror), err_flag);
+    if (threads <= 256)
+        k_tile<P, 256><<<(unsigned)ntiles, threads, smem, s>>>(static_cast<typename P::S*>(vpsi), pd, d_ops, d_tables,
+                                                               reinterpret_cast<double2*>(mirror), err_flag);
+    else
+        k_tile<P, 1024><<<(unsigned)ntiles, threads, smem, s>>>(static_cast<typename P::S*>(vpsi), pd, d_ops, d_tables,
+                                                                reinterpret_cast<double2*>(mirror), err_flag);
     return cudaGetLastError();
 }
 
