@@ -611,6 +611,8 @@ def summarize(line: dict) -> dict:
         "mixed_batch_circuits_per_s_df64": get(line, "mixed_batch", "df64", "circuits_per_s"),
         "mixed_batch_circuits_per_s_c64": get(line, "mixed_batch", "c64", "circuits_per_s"),
         "zne_traj_per_s": get(line, "zne", "traj_per_s"),
+        "complex128_gate_sweep_hbm_frac": {k: round(v["frac"], 3) for k, v in (get(line, "gate_sweeps", "complex128") or {}).items()
+                                           if isinstance(v, dict) and "frac" in v and not k.startswith("block")} or None,
         "block5_tensor_core_hbm_frac": get(line, "gate_sweeps", "df64", "block5", "frac"),
         "dm_depolarizing_2q_df64_hbm_frac": get(line, "density_matrix", "df64_n13", "depolarizing_2q", "frac_of_hbm"),
     }
@@ -692,13 +694,25 @@ def run_sweep_bench(args, torch):
              "CNOT": [(OP_CNOT, 0, n - 1), (OP_CNOT, n - 1, 0), (OP_CNOT, 12, 13), (OP_CNOT, 3, 20)],
              "CZ": [(OP_CZ, 0, n - 1), (OP_CZ, 12, 13), (OP_CZ, 3, 20)]}
     bytes_per = {"CNOT": 16, "CZ": 8}
-    out = {"qubits": n, "peak_gbs": peak, "peak_source": f"{peak_kind} hbm_gbs"}
+    out = {"qubits": n, "peak_gbs": peak, "peak_source": f"{peak_kind} hbm_gbs",
+           "bytes_basis": "amplitudes each launch reads and writes (32 B x 2^n for a pair pass, 16 B x 2^n for "
+                          "the IEEE complex128 RZ, which rewrites only the |1> half, 16 / 8 B x 2^n for CNOT / CZ)"}
     for prec in ("complex128", "df64"):
         st = llgpu.State(n, prec)
         st.set_fusion("none")
         res = {}
         for name, recs in kinds.items():
             ops = make_ops(recs)
+            if prec == "complex128" and name not in bytes_per:
+                # IEEE complex128 flushes run the per-gate lowering that carries the gates' real
+                # factors (and RZ's global phase) and absorbs them in one op of the flush: its
+                # launches move the bytes of the ops it exports
+                _, xs = llgpu.plan_export(n, ops, n, stream=True)
+                sweep_bytes = sum(16 if int(k) == 13 else 32 for k in xs["kind"]) * (1 << n) / len(xs)
+                flush_ops = {str(int(k)): int(c) for k, c in zip(*np.unique(xs["kind"], return_counts=True))}
+            else:
+                sweep_bytes = bytes_per.get(name, 32) * (1 << n)
+                flush_ops = None
             st.apply_ops(ops)  # warm-up
             st.sync()
             st.profile(True)
@@ -709,8 +723,10 @@ def run_sweep_bench(args, torch):
             ms, cnt = st.profile_read(reset=True)["gate"]
             st.profile(False)
             per = ms / cnt / 1e3
-            gbs = bytes_per.get(name, 32) * (1 << n) / per / 1e9
+            gbs = sweep_bytes / per / 1e9
             res[name] = {"ms_per_sweep": per * 1e3, "gbs": gbs, "frac": gbs / peak}
+            if flush_ops:
+                res[name]["flush_ops_by_kind"] = flush_ops
             if name in bytes_per:
                 # per (control, target): with qubit 0 among the touched bits, touched and untouched
                 # amplitudes share every 32-byte sector, so DRAM moves twice the algorithmic bytes

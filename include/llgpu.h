@@ -510,6 +510,12 @@ int llg_plan_export(int n, const llg_op* ops, int nops, int tile_qubits, llg_pas
  * dropped scale is absorbed before it reaches 2^-40 instead of 2^-300); the coefficients are
  * exported as doubles either way. */
 #define LLG_PLAN_DF64 16
+/* LLG_PLAN_STREAM: alone, the per-gate lowering an IEEE complex128 state runs without fusion (one
+ * pass per op over the whole register, exported as a single pass of t = n): RX / RY / H without
+ * their real factors (kinds 22 / 23: [1, -i c2; -i c2, 1] and [c2, -i; -i, c2]; 16 / 17 as above;
+ * 24: [1, 1; 1, -1]), RZ as diag(1, e^{it}) (kind 13), the factors and RZ's global phase
+ * absorbed once per flush by rewriting one op to its full form (kinds 0, 1, 2, 3 or 5). */
+#define LLG_PLAN_STREAM 32
 int llg_plan_export_ex(int n, const llg_op* ops, int nops, int tile_qubits, int flags, llg_pass_info* passes,
                        int max_passes, int* npasses, llg_exec_op* xops, int max_xops, int* nxops);
 /* The eigenvalue d(i) of the diagonal observable sum_k coeff_k Z_{a_k} Z_{b_k} (b_k < 0: Z_{a_k}) for

@@ -186,6 +186,7 @@ struct PolF64 {
     }
     __device__ static R lin4_raw(K a, R x, K b, R y, K c, R z, K d, R w) { return lin4(a, x, b, y, c, z, d, w); }
     __device__ static R add(R x, R y) { return x + y; }
+    __device__ static R sub(R x, R y) { return x - y; }
     // the sign bit flipped on the integer pipe (the same bits as IEEE negation); a plain -x that is
     // not folded into a multiply-add runs on the FP64 pipe, this GPU's scarcest
     __device__ static R neg(R x) { return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL); }
@@ -229,6 +230,7 @@ struct PolF32 {
     }
     __device__ static R lin4_raw(K a, R x, K b, R y, K c, R z, K d, R w) { return lin4(a, x, b, y, c, z, d, w); }
     __device__ static R add(R x, R y) { return x + y; }
+    __device__ static R sub(R x, R y) { return x - y; }
     __device__ static R neg(R x) { return -x; }
     __device__ static K kneg(K x) { return -x; }
     __device__ static R mulk(K a, R x) { return a * x; }
@@ -294,6 +296,7 @@ struct PolDF64 {
         return df_lin4_raw(a, x, b, y, c, z, d, w);
     }
     __device__ static R add(R x, R y) { return df_add(x, y); }
+    __device__ static R sub(R x, R y) { return df_sub(x, y); }
     __device__ static R neg(R x) { return df_neg(x); }
     __device__ static K kneg(K x) { return df_neg(x); }
     __device__ static R mulk(K a, R x) { return df_mul(a, x); }

@@ -202,6 +202,17 @@ int stage_buffers(llg_state* st) {
 int run_streaming(llg_state* st, const std::vector<llg_op>& q) {
     std::vector<ExecOp> lowered;
     std::string err;
+    if (st->P == LLG_F64) {
+        // IEEE complex128: one pass per gate, the gates' real factors and RZ's global phase
+        // carried through the flush and absorbed once (4 FP64 operations per pair, not 8)
+        if (!lower_stream_f64(st->n, q.data(), (int)q.size(), lowered, err)) return set_error(LLG_EINVAL, err);
+        for (const ExecOp& e : lowered) {
+            int rc = traced(st, LLG_PROF_GATE, 1, "gate kernel",
+                            [&] { return launch_exec_op(st->P, st->d_psi, st->n, e, st->stream); });
+            if (rc) return rc;
+        }
+        return LLG_OK;
+    }
     for (const llg_op& op : q) {
         lowered.clear();
         if (!lower_op(st->n, op, st->P, lowered, err)) return set_error(LLG_EINVAL, err);
@@ -1162,6 +1173,22 @@ int export_plan(int n, const llg_op* ops, int nops, int tile_qubits, int flags, 
         if (rc) return rc;
     }
     std::string err;
+    if (flags & LLG_PLAN_STREAM) {
+        // the per-gate lowering of an IEEE complex128 flush, as one pass over the whole register
+        if (flags & ~LLG_PLAN_STREAM) return set_error(LLG_EINVAL, "plan_export: the streaming lowering is exported alone");
+        plan.passes.clear();
+        plan.ops.clear();
+        plan.tables.clear();
+        if (!lower_stream_f64(n, ops, nops, plan.ops, err)) return set_error(LLG_EINVAL, err);
+        PassDesc pd;
+        std::memset(&pd, 0, sizeof(pd));
+        pd.local_mask = n >= 64 ? ~0ULL : ((1ULL << n) - 1);
+        pd.t = n;
+        pd.low = n;
+        pd.nops = (int)plan.ops.size();
+        plan.passes.push_back(pd);
+        return LLG_OK;
+    }
     if ((flags & LLG_PLAN_FUSE2) && (flags & (LLG_PLAN_ZYZ | LLG_PLAN_TABLES | LLG_PLAN_REGS)))
         return set_error(LLG_EINVAL, "plan_export: two-qubit blocks are planned alone");
     const int prec = (flags & LLG_PLAN_DF64) ? LLG_DF64 : LLG_F64;

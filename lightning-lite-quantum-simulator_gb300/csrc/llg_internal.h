@@ -68,6 +68,14 @@ enum ExecKind : int32_t {
     // the tile's base index, entries (row-major, (re, im) slots) at table entry `mask` (control 0)
     // and `mask` + 4 (control 1)
     EX_U2C = 21,
+    // Streaming forms for IEEE complex128 per-gate flushes (lower_stream_f64): the gate without
+    // its real factor f, which the flush carries and absorbs once (4 FP64 operations per pair
+    // instead of 8).  RX(b) = f [1, -it; -it, 1] (EX_RXT, c[2] = t = tan b/2, f = cos b/2) or
+    // f [u, -i; -i, u] (EX_RXC, c[2] = u = cot b/2, f = sin b/2); H = 2^-1/2 [1, 1; 1, -1]
+    // (EX_HS: sums and differences only).
+    EX_RXT = 22,
+    EX_RXC = 23,
+    EX_HS = 24,
 };
 
 // Flags of a tile op.
@@ -142,6 +150,15 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int precisi
 // position or a global qubit as before).  Every pass starts and ends in the layout whose register
 // positions are the top four tile positions.  Returns the number of layout changes.
 int to_register_program(Plan& plan);
+
+// Per-gate lowering of a flush for IEEE complex128 states on the streaming path (one pass per
+// gate): RX / RY / H in their scale-free forms (EX_RXT, EX_RXC, EX_RT, EX_RC, EX_HS) with the
+// dropped real factors carried, RZ as its global phase (carried) times diag(1, e^{it}) on the
+// |1> half (EX_PHASE1).  The carried factor is absorbed once: into a generic 2x2 of the flush
+// when there is one, else the real part into the last scale-free op (rewritten as its full form)
+// and the phase into the last EX_PHASE1 (rewritten as an EX_DIAG over the whole state); the real
+// part also whenever it would fall below 2^-300.  Other gates lower as lower_op does.
+bool lower_stream_f64(int n, const llg_op* ops, int nops, std::vector<ExecOp>& out, std::string& err);
 
 // The EX_U4 fusion of plan_tiles(fuse2): returns the number of one-qubit ops merged into blocks.
 int fuse_two_qubit(Plan& plan);

@@ -98,6 +98,29 @@ __global__ void __launch_bounds__(kThreads) k_diag(typename P::S* __restrict__ p
     }
 }
 
+// diag(1, p) on qubit q: only the amplitudes with bit q set are read and written (p = c[0] + i c[1])
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_phase1(typename P::S* __restrict__ psi, uint64_t half, int q, ExecOp op) {
+    using K = typename P::K;
+    const K pr = P::k_from_bits(op.c[0]), pi = P::k_from_bits(op.c[1]), mpi = P::kneg(pi);
+    const uint64_t bit = 1ULL << q;
+    const uint64_t step = (uint64_t)gridDim.x * kThreads * 2;
+    for (uint64_t base = (uint64_t)blockIdx.x * kThreads * 2 + threadIdx.x; base < half; base += step) {
+        const uint64_t pB = base + kThreads;
+        const bool hasB = pB < half;
+        const uint64_t iA = insert0(base, q) | bit, iB = insert0(hasB ? pB : base, q) | bit;
+        auto a = P::load(psi[iA]);
+        typename P::C b;
+        if (hasB) b = P::load(psi[iB]);
+        cmul_const<P>(a, pr, pi, mpi);
+        psi[iA] = P::store(a);
+        if (hasB) {
+            cmul_const<P>(b, pr, pi, mpi);
+            psi[iB] = P::store(b);
+        }
+    }
+}
+
 // CNOT: swap (c=1, t=0) <-> (c=1, t=1) over the N/4 quads (src/StateVectorBackend.h:109-135).
 // kStreamItems quads per thread per step, all loads issued before the stores (memory-level
 // parallelism for a kernel that does no arithmetic).
@@ -530,6 +553,12 @@ cudaError_t exec_op_t(void* vpsi, int n, const ExecOp& op, cudaStream_t s) {
         case EX_RY: k_pairs<P, EX_RY><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
         case EX_H: k_pairs<P, EX_H><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
         case EX_X: k_pairs<P, EX_X><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
+        case EX_RT: k_pairs<P, EX_RT><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
+        case EX_RC: k_pairs<P, EX_RC><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
+        case EX_RXT: k_pairs<P, EX_RXT><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
+        case EX_RXC: k_pairs<P, EX_RXC><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
+        case EX_HS: k_pairs<P, EX_HS><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
+        case EX_PHASE1: k_phase1<P><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
         case EX_DIAG: k_diag<P><<<grid_for(size, 1), kThreads, 0, s>>>(psi, size, op.q0, op); break;
         case EX_CNOT: k_cnot<P><<<grid_for(size / 4, kStreamItems), kThreads, 0, s>>>(psi, size / 4, op.q0, op.q1); break;
         case EX_MCZ: {

@@ -1225,4 +1225,112 @@ bool plan_tiles(int n, const llg_op* ops, int nops, int tile_qubits, int P, Plan
     return true;
 }
 
+bool lower_stream_f64(int n, const llg_op* ops, int nops, std::vector<ExecOp>& out, std::string& err) {
+    using cd = std::complex<double>;
+    constexpr int PP = LLG_F64;
+    double r = 1.0;      // carried real factor: the state is r w times what the kernels hold
+    cd w(1.0, 0.0);      // carried global phase (from RZ)
+    int last_real = -1;  // index in out of the last scale-free op (absorbs r)
+    int last_phase = -1; // index in out of the last EX_PHASE1 (absorbs w)
+    int last_u2 = -1;    // index in out of a generic 2x2 (absorbs r w for free)
+    // the scale-free op at index i rewritten as its full form times the real factor g
+    auto absorb_real = [&](int i, double g) {
+        ExecOp& e = out[i];
+        const double a = coef_value(e.c[2]);
+        double c = g, sn = g;
+        switch (e.kind) {
+            case EX_RT: sn = g * a; e.kind = EX_RY; break;   // g [1, -t; t, 1] = RY-form (g, g t)
+            case EX_RC: c = g * a; e.kind = EX_RY; break;    // g [u, -1; 1, u] = RY-form (g u, g)
+            case EX_RXT: sn = g * a; e.kind = EX_RX; break;  // g [1, -it; -it, 1] = RX-form (g, g t)
+            case EX_RXC: c = g * a; e.kind = EX_RX; break;   // g [u, -i; -i, u] = RX-form (g u, g)
+            default: e.kind = EX_H; break;                   // g [1, 1; 1, -1]
+        }
+        std::memset(e.c, 0, sizeof(e.c));
+        e.c[0] = pack_coef(PP, c);
+        e.c[1] = pack_coef(PP, sn);
+    };
+    for (int i = 0; i < nops; ++i) {
+        const llg_op& op = ops[i];
+        const double c = std::cos(0.5 * op.theta), s = std::sin(0.5 * op.theta);
+        ExecOp e;
+        std::memset(&e, 0, sizeof(e));
+        e.q0 = op.q0;
+        switch (op.kind) {
+            case LLG_OP_RX:
+            case LLG_OP_RY: {
+                const bool tan_form = std::fabs(c) >= std::fabs(s);
+                const bool rx = op.kind == LLG_OP_RX;
+                e.kind = tan_form ? (rx ? EX_RXT : EX_RT) : (rx ? EX_RXC : EX_RC);
+                e.c[2] = pack_coef(PP, tan_form ? s / c : c / s);
+                r *= tan_form ? c : s;
+                last_real = (int)out.size();
+                out.push_back(e);
+                break;
+            }
+            case LLG_OP_H:
+                e.kind = EX_HS;
+                r *= 1.0 / std::sqrt(2.0);
+                last_real = (int)out.size();
+                out.push_back(e);
+                break;
+            case LLG_OP_RZ: {  // diag(e^-it/2, e^it/2) = e^-it/2 diag(1, e^it)
+                w *= cd(c, -s);
+                const cd p(std::cos(op.theta), std::sin(op.theta));
+                e.kind = EX_PHASE1;
+                e.c[0] = pack_coef(PP, p.real());
+                e.c[1] = pack_coef(PP, p.imag());
+                last_phase = (int)out.size();
+                out.push_back(e);
+                break;
+            }
+            default: {
+                const size_t before = out.size();
+                if (!lower_op(n, op, PP, out, err)) return false;
+                for (size_t k = before; k < out.size(); ++k)
+                    if (out[k].kind == EX_U2) last_u2 = (int)k;
+                break;
+            }
+        }
+        // amplitudes held at 1 / r of their size: keep them within 2^300 (FP64 range to 2^1023)
+        if (std::fabs(r) < 0x1p-300 && last_real >= 0) {
+            absorb_real(last_real, r);
+            r = 1.0;
+            last_real = -1;
+        }
+    }
+    if (r == 1.0 && w == cd(1.0, 0.0)) return true;
+    if (last_u2 >= 0) {  // a scalar times a generic 2x2: free
+        const cd z = r * w;
+        ExecOp& e = out[last_u2];
+        for (int k = 0; k < 4; ++k) {
+            const cd v = z * cd(coef_value(e.c[2 * k]), coef_value(e.c[2 * k + 1]));
+            e.c[2 * k] = pack_coef(PP, v.real());
+            e.c[2 * k + 1] = pack_coef(PP, v.imag());
+        }
+        return true;
+    }
+    if (r != 1.0) {
+        if (last_real < 0) {
+            err = "stream lowering: a carried factor without a scale-free op";
+            return false;
+        }
+        absorb_real(last_real, r);
+    }
+    if (w != cd(1.0, 0.0)) {
+        if (last_phase < 0) {
+            err = "stream lowering: a carried phase without a phase op";
+            return false;
+        }
+        ExecOp& e = out[last_phase];  // w diag(1, p) = diag(w, w p) over the whole state
+        const cd p(coef_value(e.c[0]), coef_value(e.c[1]));
+        const cd d1 = w * p;
+        e.kind = EX_DIAG;
+        e.c[0] = pack_coef(PP, w.real());
+        e.c[1] = pack_coef(PP, w.imag());
+        e.c[2] = pack_coef(PP, d1.real());
+        e.c[3] = pack_coef(PP, d1.imag());
+    }
+    return true;
+}
+
 }  // namespace llg

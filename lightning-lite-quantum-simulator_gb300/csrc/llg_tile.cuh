@@ -93,6 +93,23 @@ struct PairMath {
             a0.im = P::fma1_raw(u, y0, P::neg(y1));
             a1.re = P::fma1_raw(u, x1, x0);
             a1.im = P::fma1_raw(u, y1, y0);
+        } else if (KIND == EX_RXT) {  // [1, -it; -it, 1]
+            const auto t = k[2], mt = P::kneg(k[2]);
+            a0.re = P::fma1_raw(t, y1, x0);
+            a0.im = P::fma1_raw(mt, x1, y0);
+            a1.re = P::fma1_raw(t, y0, x1);
+            a1.im = P::fma1_raw(mt, x0, y1);
+        } else if (KIND == EX_RXC) {  // [u, -i; -i, u]
+            const auto u = k[2];
+            a0.re = P::fma1_raw(u, x0, y1);
+            a0.im = P::fma1_raw(u, y0, P::neg(x1));
+            a1.re = P::fma1_raw(u, x1, y0);
+            a1.im = P::fma1_raw(u, y1, P::neg(x0));
+        } else if (KIND == EX_HS) {  // [1, 1; 1, -1]
+            a0.re = P::add(x0, x1);
+            a0.im = P::add(y0, y1);
+            a1.re = P::sub(x0, x1);
+            a1.im = P::sub(y0, y1);
         } else if (KIND == EX_H) {  // r [1, 1; 1, -1]
             const auto r = k[0], mr = P::kneg(k[0]);
             a0.re = P::lin2_raw(r, x0, r, x1);

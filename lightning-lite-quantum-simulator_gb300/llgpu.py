@@ -419,19 +419,21 @@ PLAN_TABLES = 2
 PLAN_REGS = 4
 PLAN_FUSE2 = 8
 PLAN_DF64 = 16
+PLAN_STREAM = 32
 
 
 def plan_export(n: int, ops: np.ndarray, tile_qubits: int, zyz: bool = False, tables: bool = False,
-                regs: bool = False, fuse2: bool = False, df64: bool = False):
+                regs: bool = False, fuse2: bool = False, df64: bool = False, stream: bool = False):
     """Host-side plan of `ops` (passes, executor ops; coefficients as doubles).  zyz=True plans
     as the engine does for complex128 states (fused unitary 2x2s as carried-phase rotations);
     tables=True (with zyz) also gathers diagonal factors into phase tables, and the result gains a
     third item: the tables as a complex array (2^tile_qubits entries per table); fuse2=True plans the
     two-qubit blocks of complex64 tile passes (kind 20, 16 table entries each) and also returns the
-    tables; df64=True plans as for a double-float state (IEEE complex128 otherwise)."""
+    tables; df64=True plans as for a double-float state (IEEE complex128 otherwise); stream=True
+    returns the per-gate lowering of an unfused IEEE complex128 flush as one whole-register pass."""
     ops = np.ascontiguousarray(ops, dtype=OP_DTYPE)
     flags = ((PLAN_ZYZ if zyz else 0) | (PLAN_TABLES if tables else 0) | (PLAN_REGS if regs else 0) |
-             (PLAN_FUSE2 if fuse2 else 0) | (PLAN_DF64 if df64 else 0))
+             (PLAN_FUSE2 if fuse2 else 0) | (PLAN_DF64 if df64 else 0) | (PLAN_STREAM if stream else 0))
     npasses, nx = ctypes.c_int(), ctypes.c_int()
     check(lib().llg_plan_export_ex(n, _ptr(ops) if ops.size else None, ops.size, tile_qubits, flags, None, 0,
                                    ctypes.byref(npasses), None, 0, ctypes.byref(nx)))

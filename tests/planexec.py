@@ -28,6 +28,12 @@ def _matrix(x) -> np.ndarray:
         return np.array([[1, -c[2]], [c[2], 1]], dtype=complex)
     if k == 17:  # [u, -1; 1, u]
         return np.array([[c[2], -1], [1, c[2]]], dtype=complex)
+    if k == 22:  # [1, -it; -it, 1]
+        return np.array([[1, -1j * c[2]], [-1j * c[2], 1]])
+    if k == 23:  # [u, -i; -i, u]
+        return np.array([[c[2], -1j], [-1j, c[2]]])
+    if k == 24:  # [1, 1; 1, -1]
+        return np.array([[1, 1], [1, -1]], dtype=complex)
     if k == 11:  # diag(1, ea) [c, -s; s, c] diag(1, eg)
         eg, ea = c[0] + 1j * c[1], c[4] + 1j * c[5]
         ry = np.array([[c[2], -c[3]], [c[3], c[2]]], dtype=complex)
@@ -95,7 +101,7 @@ def execute(psi: np.ndarray, n: int, passes: np.ndarray, xops: np.ndarray, table
             k, q0, q1, fl = int(x["kind"]), int(x["q0"]), int(x["q1"]), int(x["flags"])
             if k == -1:
                 continue
-            if k <= 4 or k in (11, 12, 14, 15, 16, 17):
+            if k <= 4 or k in (11, 12, 14, 15, 16, 17, 22, 23, 24):
                 _pair(tile, q0, _matrix(x))
             elif k == 20:  # 4x4 block on (q0, q1): 16 table entries from `mask`, row-major
                 off = int(x["mask"])

@@ -362,3 +362,38 @@ def test_algorithms_module_without_a_gpu(built):
     if llgpu.device_count() == 0:
         with pytest.raises(RuntimeError):
             alg.make_gpu_backend(3)  # no CPU fallback
+
+
+def test_stream_lowering_reproduces_the_oracle(built):
+    # IEEE complex128 per-gate flushes: scale-free RX / RY / H, RZ as diag(1, e^it) on the |1> half,
+    # the carried factor and phase absorbed once (into a generic 2x2 when there is one)
+    rng = np.random.default_rng(77)
+    for n, with_u2 in ((6, True), (7, False), (9, False), (10, True)):
+        ops = random_ops(n, 300, rng)
+        if not with_u2:
+            ops = ops[ops["kind"] != OP_U2]
+        passes, xops = llgpu.plan_export(n, ops, n, stream=True)
+        assert len(passes) == 1 and len(xops) >= len(ops)
+        kinds = np.bincount(xops["kind"], minlength=25)
+        assert kinds[22] + kinds[23] + kinds[16] + kinds[17] + kinds[24] > 0 and kinds[13] > 0
+        # full forms: none left without a generic 2x2 to take the scalar, else one real op and one
+        # whole-state diagonal
+        full = int(kinds[1] + kinds[2] + kinds[3] + kinds[5])
+        assert full == 0 if with_u2 else full == 2
+        got = execute(oracle.zero_state(n), n, passes, xops)
+        assert np.max(np.abs(got - oracle.run_ops(n, ops))) < 1e-12
+
+
+def test_stream_lowering_absorbs_before_the_floor(built):
+    # 700 rotations at |cos| = |sin| = 2^-1/2 shrink the carried factor to 2^-350: it is absorbed
+    # before 2^-300 and once at the end
+    n = 3
+    recs = [((OP_RX, OP_RY)[k % 2], k % n, 0, np.pi / 2 + (1e-3 if k % 3 else -1e-3)) for k in range(700)]
+    ops = make_ops(recs)
+    passes, xops = llgpu.plan_export(n, ops, n, stream=True)
+    kinds = np.bincount(xops["kind"], minlength=25)
+    assert kinds[1] + kinds[2] == 2  # one mid-flush absorption, one at the end
+    got = execute(oracle.zero_state(n), n, passes, xops)
+    assert np.max(np.abs(got - oracle.run_ops(n, ops))) < 1e-12
+    with pytest.raises(ValueError):
+        llgpu.plan_export(n, ops, n, stream=True, zyz=True)
