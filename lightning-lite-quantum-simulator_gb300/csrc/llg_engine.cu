@@ -1165,7 +1165,8 @@ namespace {
 int export_plan(int n, const llg_op* ops, int nops, int tile_qubits, int flags, Plan& plan) {
     if (n < 1 || n > kMaxQubits || nops < 0 || (nops > 0 && !ops))
         return set_error(LLG_EINVAL, "plan_export: bad argument");
-    if (tile_qubits < 1 || tile_qubits > 14) return set_error(LLG_EINVAL, "plan_export: tile_qubits out of range");
+    if ((tile_qubits < 1 || tile_qubits > 14) && !(flags & LLG_PLAN_STREAM))
+        return set_error(LLG_EINVAL, "plan_export: tile_qubits out of range");
     llg_state tmp;
     tmp.n = n;
     for (int i = 0; i < nops; ++i) {
