@@ -76,6 +76,12 @@ enum ExecKind : int32_t {
     EX_RXT = 22,
     EX_RXC = 23,
     EX_HS = 24,
+    // A unitary 2x2 z diag(1, ea) RY(b) diag(1, eg) in the same streaming lowering, without z and
+    // the rotation's real factor: diag(1, ea) [1, -t; t, 1] diag(1, eg) (EX_ZTZ, c[2] = t) or
+    // diag(1, ea) [u, -1; 1, u] diag(1, eg) (EX_ZCZ, c[2] = u); c[0..1] = eg, c[4..5] = ea.
+    // 12 FP64 operations per pair against 16 for the generic form.
+    EX_ZTZ = 25,
+    EX_ZCZ = 26,
 };
 
 // Flags of a tile op.
@@ -154,10 +160,13 @@ int to_register_program(Plan& plan);
 // Per-gate lowering of a flush for IEEE complex128 states on the streaming path (one pass per
 // gate): RX / RY / H in their scale-free forms (EX_RXT, EX_RXC, EX_RT, EX_RC, EX_HS) with the
 // dropped real factors carried, RZ as its global phase (carried) times diag(1, e^{it}) on the
-// |1> half (EX_PHASE1).  The carried factor is absorbed once: into a generic 2x2 of the flush
-// when there is one, else the real part into the last scale-free op (rewritten as its full form)
-// and the phase into the last EX_PHASE1 (rewritten as an EX_DIAG over the whole state); the real
-// part also whenever it would fall below 2^-300.  Other gates lower as lower_op does.
+// |1> half (EX_PHASE1), unitary 2x2s as EX_ZTZ / EX_ZCZ with their global phase and real factor
+// carried.  The carried factor is absorbed once: into a generic (non-unitary) 2x2 of the flush
+// when there is one; else, when the phase has no EX_PHASE1 to take it, both into the last
+// EX_ZTZ / EX_ZCZ (rewritten as a generic 2x2); else the real part into the last scale-free op
+// (rewritten as its full form) and the phase into the last EX_PHASE1 (rewritten as an EX_DIAG
+// over the whole state).  The real part is also absorbed whenever it would fall below 2^-300.
+// Other gates lower as lower_op does.
 bool lower_stream_f64(int n, const llg_op* ops, int nops, std::vector<ExecOp>& out, std::string& err);
 
 // The EX_U4 fusion of plan_tiles(fuse2): returns the number of one-qubit ops merged into blocks.

@@ -558,6 +558,9 @@ cudaError_t exec_op_t(void* vpsi, int n, const ExecOp& op, cudaStream_t s) {
         case EX_RXT: k_pairs<P, EX_RXT><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
         case EX_RXC: k_pairs<P, EX_RXC><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
         case EX_HS: k_pairs<P, EX_HS><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
+        case EX_ZTZ: k_pairs<P, EX_ZTZ><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
+        case EX_ZCZ: k_pairs<P, EX_ZCZ><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
+        case EX_ZYZ: k_pairs<P, EX_ZYZ><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
         case EX_PHASE1: k_phase1<P><<<grid_for(size / 2, 2), kThreads, 0, s>>>(psi, size / 2, op.q0, op); break;
         case EX_DIAG: k_diag<P><<<grid_for(size, 1), kThreads, 0, s>>>(psi, size, op.q0, op); break;
         case EX_CNOT: k_cnot<P><<<grid_for(size / 4, kStreamItems), kThreads, 0, s>>>(psi, size / 4, op.q0, op.q1); break;

@@ -1233,11 +1233,20 @@ bool lower_stream_f64(int n, const llg_op* ops, int nops, std::vector<ExecOp>& o
     int last_real = -1;  // index in out of the last scale-free op (absorbs r)
     int last_phase = -1; // index in out of the last EX_PHASE1 (absorbs w)
     int last_u2 = -1;    // index in out of a generic 2x2 (absorbs r w for free)
+    int last_zyz = -1;   // index in out of the last EX_ZTZ / EX_ZCZ (or the EX_ZYZ it became)
     // the scale-free op at index i rewritten as its full form times the real factor g
     auto absorb_real = [&](int i, double g) {
         ExecOp& e = out[i];
         const double a = coef_value(e.c[2]);
         double c = g, sn = g;
+        if (e.kind == EX_ZTZ || e.kind == EX_ZCZ) {  // diag(1, ea) g T diag(1, eg) = EX_ZYZ (c, s)
+            if (e.kind == EX_ZTZ) sn = g * a;
+            else c = g * a;
+            e.kind = EX_ZYZ;
+            e.c[2] = pack_coef(PP, c);
+            e.c[3] = pack_coef(PP, sn);
+            return;
+        }
         switch (e.kind) {
             case EX_RT: sn = g * a; e.kind = EX_RY; break;   // g [1, -t; t, 1] = RY-form (g, g t)
             case EX_RC: c = g * a; e.kind = EX_RY; break;    // g [u, -1; 1, u] = RY-form (g u, g)
@@ -1248,6 +1257,26 @@ bool lower_stream_f64(int n, const llg_op* ops, int nops, std::vector<ExecOp>& o
         std::memset(e.c, 0, sizeof(e.c));
         e.c[0] = pack_coef(PP, c);
         e.c[1] = pack_coef(PP, sn);
+    };
+    // the 2x2 of a unitary-form op (EX_ZTZ, EX_ZCZ, EX_ZYZ): diag(1, ea) R diag(1, eg)
+    auto zyz_matrix = [&](const ExecOp& e, cd m[4]) {
+        const cd eg(coef_value(e.c[0]), coef_value(e.c[1])), ea(coef_value(e.c[4]), coef_value(e.c[5]));
+        const double a = coef_value(e.c[2]);
+        double r00 = 1.0, r01 = -a, r10 = a, r11 = 1.0;  // EX_ZTZ: [1, -t; t, 1]
+        if (e.kind == EX_ZCZ) {
+            r00 = r11 = a;
+            r01 = -1.0;
+            r10 = 1.0;
+        } else if (e.kind == EX_ZYZ) {
+            const double sn = coef_value(e.c[3]);
+            r00 = r11 = a;
+            r01 = -sn;
+            r10 = sn;
+        }
+        m[0] = r00;
+        m[1] = r01 * eg;
+        m[2] = ea * r10;
+        m[3] = ea * r11 * eg;
     };
     for (int i = 0; i < nops; ++i) {
         const llg_op& op = ops[i];
@@ -1283,6 +1312,27 @@ bool lower_stream_f64(int n, const llg_op* ops, int nops, std::vector<ExecOp>& o
                 out.push_back(e);
                 break;
             }
+            case LLG_OP_U2: {
+                cd z, ea, eg;
+                double cc = 0.0, ss = 0.0;
+                if (split_zyz(op.m, z, cc, ss, ea, eg)) {  // z diag(1, ea) [cc, -ss; ss, cc] diag(1, eg)
+                    const bool tan_form = cc >= ss;         // cc, ss >= 0
+                    e.kind = tan_form ? EX_ZTZ : EX_ZCZ;
+                    e.c[0] = pack_coef(PP, eg.real());
+                    e.c[1] = pack_coef(PP, eg.imag());
+                    e.c[2] = pack_coef(PP, tan_form ? ss / cc : cc / ss);
+                    e.c[4] = pack_coef(PP, ea.real());
+                    e.c[5] = pack_coef(PP, ea.imag());
+                    r *= tan_form ? cc : ss;
+                    w *= z;
+                    last_real = last_zyz = (int)out.size();
+                    out.push_back(e);
+                    break;
+                }
+                if (!lower_op(n, op, PP, out, err)) return false;  // not unitary: the generic form
+                last_u2 = (int)out.size() - 1;
+                break;
+            }
             default: {
                 const size_t before = out.size();
                 if (!lower_op(n, op, PP, out, err)) return false;
@@ -1304,6 +1354,23 @@ bool lower_stream_f64(int n, const llg_op* ops, int nops, std::vector<ExecOp>& o
         ExecOp& e = out[last_u2];
         for (int k = 0; k < 4; ++k) {
             const cd v = z * cd(coef_value(e.c[2 * k]), coef_value(e.c[2 * k + 1]));
+            e.c[2 * k] = pack_coef(PP, v.real());
+            e.c[2 * k + 1] = pack_coef(PP, v.imag());
+        }
+        return true;
+    }
+    if (w != cd(1.0, 0.0) && last_phase < 0 && last_zyz >= 0) {
+        // a phase from unitary 2x2s and no phase op to take it: the last of them becomes the
+        // generic 2x2 r w diag(1, ea) R diag(1, eg)
+        ExecOp& e = out[last_zyz];
+        cd m[4];
+        zyz_matrix(e, m);
+        const int q = e.q0;
+        std::memset(&e, 0, sizeof(e));
+        e.kind = EX_U2;
+        e.q0 = q;
+        for (int k = 0; k < 4; ++k) {
+            const cd v = r * w * m[k];
             e.c[2 * k] = pack_coef(PP, v.real());
             e.c[2 * k + 1] = pack_coef(PP, v.imag());
         }

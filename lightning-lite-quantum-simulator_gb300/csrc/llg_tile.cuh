@@ -105,6 +105,26 @@ struct PairMath {
             a0.im = P::fma1_raw(u, y0, P::neg(x1));
             a1.re = P::fma1_raw(u, x1, y0);
             a1.im = P::fma1_raw(u, y1, P::neg(x0));
+        } else if (KIND == EX_ZTZ) {  // diag(1, ea) [1, -t; t, 1] diag(1, eg)
+            const auto gr = k[0], gi = k[1], t = k[2], mt = P::kneg(k[2]), ar = k[4], ai = k[5];
+            const auto zr = P::lin2_raw(gr, x1, P::kneg(gi), y1);  // z = eg a1
+            const auto zi = P::lin2_raw(gr, y1, gi, x1);
+            a0.re = P::fma1_raw(mt, zr, x0);
+            a0.im = P::fma1_raw(mt, zi, y0);
+            const auto ur = P::fma1_raw(t, x0, zr);
+            const auto ui = P::fma1_raw(t, y0, zi);
+            a1.re = P::lin2_raw(ar, ur, P::kneg(ai), ui);  // ea u
+            a1.im = P::lin2_raw(ar, ui, ai, ur);
+        } else if (KIND == EX_ZCZ) {  // diag(1, ea) [u, -1; 1, u] diag(1, eg)
+            const auto gr = k[0], gi = k[1], u = k[2], ar = k[4], ai = k[5];
+            const auto zr = P::lin2_raw(gr, x1, P::kneg(gi), y1);
+            const auto zi = P::lin2_raw(gr, y1, gi, x1);
+            a0.re = P::fma1_raw(u, x0, P::neg(zr));
+            a0.im = P::fma1_raw(u, y0, P::neg(zi));
+            const auto vr = P::fma1_raw(u, zr, x0);
+            const auto vi = P::fma1_raw(u, zi, y0);
+            a1.re = P::lin2_raw(ar, vr, P::kneg(ai), vi);
+            a1.im = P::lin2_raw(ar, vi, ai, vr);
         } else if (KIND == EX_HS) {  // [1, 1; 1, -1]
             a0.re = P::add(x0, x1);
             a0.im = P::add(y0, y1);

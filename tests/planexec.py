@@ -32,6 +32,10 @@ def _matrix(x) -> np.ndarray:
         return np.array([[1, -1j * c[2]], [-1j * c[2], 1]])
     if k == 23:  # [u, -i; -i, u]
         return np.array([[c[2], -1j], [-1j, c[2]]])
+    if k in (25, 26):  # diag(1, ea) [1, -t; t, 1] diag(1, eg) / diag(1, ea) [u, -1; 1, u] diag(1, eg)
+        eg, ea, a = c[0] + 1j * c[1], c[4] + 1j * c[5], c[2]
+        r = np.array([[1, -a], [a, 1]] if k == 25 else [[a, -1], [1, a]], dtype=complex)
+        return np.diag([1, ea]) @ r @ np.diag([1, eg])
     if k == 24:  # [1, 1; 1, -1]
         return np.array([[1, 1], [1, -1]], dtype=complex)
     if k == 11:  # diag(1, ea) [c, -s; s, c] diag(1, eg)
@@ -101,7 +105,7 @@ def execute(psi: np.ndarray, n: int, passes: np.ndarray, xops: np.ndarray, table
             k, q0, q1, fl = int(x["kind"]), int(x["q0"]), int(x["q1"]), int(x["flags"])
             if k == -1:
                 continue
-            if k <= 4 or k in (11, 12, 14, 15, 16, 17, 22, 23, 24):
+            if k <= 4 or k in (11, 12, 14, 15, 16, 17, 22, 23, 24, 25, 26):
                 _pair(tile, q0, _matrix(x))
             elif k == 20:  # 4x4 block on (q0, q1): 16 table entries from `mask`, row-major
                 off = int(x["mask"])

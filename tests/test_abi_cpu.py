@@ -374,14 +374,28 @@ def test_stream_lowering_reproduces_the_oracle(built):
             ops = ops[ops["kind"] != OP_U2]
         passes, xops = llgpu.plan_export(n, ops, n, stream=True)
         assert len(passes) == 1 and len(xops) >= len(ops)
-        kinds = np.bincount(xops["kind"], minlength=25)
+        kinds = np.bincount(xops["kind"], minlength=27)
         assert kinds[22] + kinds[23] + kinds[16] + kinds[17] + kinds[24] > 0 and kinds[13] > 0
-        # full forms: none left without a generic 2x2 to take the scalar, else one real op and one
-        # whole-state diagonal
-        full = int(kinds[1] + kinds[2] + kinds[3] + kinds[5])
-        assert full == 0 if with_u2 else full == 2
+        # unitary 2x2s as phase-rotation-phase without their factor (kinds 25 / 26)
+        assert (kinds[25] + kinds[26] > 0) == with_u2
+        # full forms: at most one real op (or the unitary form it absorbs into) and one
+        # whole-state diagonal take the carried factor and phase
+        full = int(kinds[0] + kinds[1] + kinds[2] + kinds[3] + kinds[5] + kinds[11])
+        assert full <= 2
         got = execute(oracle.zero_state(n), n, passes, xops)
         assert np.max(np.abs(got - oracle.run_ops(n, ops))) < 1e-12
+    # a flush of unitary 2x2s alone: four scale-free forms, the last one the generic 2x2 that
+    # takes the carried factor and phase; a non-unitary 2x2 takes them for free
+    for recs in ([(OP_U2, q, 0, 0.0, None, np.linalg.qr(rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2)))[0].reshape(4))
+                  for q in (0, 1, 2, 3, 4)],
+                 [(OP_U2, 2, 0, 0.0, None, np.array([1.0, 0.5, 0.25j, 2.0]))] +
+                 [(OP_RY, q, 0, 0.3 + q) for q in range(5)] + [(OP_RZ, 1, 0, 0.7)]):
+        ops = make_ops(recs)
+        passes, xops = llgpu.plan_export(5, ops, 5, stream=True)
+        kinds = np.bincount(xops["kind"], minlength=27)
+        got = execute(oracle.zero_state(5), 5, passes, xops)
+        assert np.max(np.abs(got - oracle.run_ops(5, ops))) < 1e-12
+        assert kinds[0] == 1 and kinds[1] + kinds[2] + kinds[3] + kinds[5] + kinds[11] == 0
 
 
 def test_stream_lowering_absorbs_before_the_floor(built):
