@@ -138,6 +138,85 @@ __global__ void __launch_bounds__(kBlockThreads) k_group(typename P::S* __restri
     }
 }
 
+// A sparse block (k <= 4): a thread per group as in k_group, but row r sums only over the columns
+// whose entry is nonzero (bit c of nz.rows[r]); an entry with a zero imaginary part (bit c of
+// nz.real[r]) costs two real multiply-adds instead of four.  The masks are the same for every
+// thread, so the tests branch uniformly.  Superoperators of noise channels (Kraus sums on a
+// density matrix's row and column qubits) have 1-4 nonzero real entries per row of 4 or 16.
+template <class P, int K>
+__global__ void __launch_bounds__(kBlockThreads) k_group_sparse(typename P::S* __restrict__ psi, int n, BlockDesc bd,
+                                                                const uint64_t* __restrict__ mat, BlockSparsity nz) {
+    using Kt = typename P::K;
+    using C = typename P::C;
+    constexpr int A = 1 << K;
+    __shared__ Kt sm[2 * A * A];  // row-major (re, im)
+    __shared__ uint64_t soff[A];
+    __shared__ uint32_t srows[A], sreal[A];
+    for (int i = threadIdx.x; i < 2 * A * A; i += blockDim.x) sm[i] = P::k_from_bits(mat[i]);
+    for (int j = threadIdx.x; j < A; j += blockDim.x) {
+        uint64_t off = 0;
+        for (int b = 0; b < K; ++b)
+            if ((j >> b) & 1) off |= 1ULL << bd.q[b];
+        soff[j] = off;
+        srows[j] = nz.rows[j];
+        sreal[j] = nz.real[j];
+    }
+    __syncthreads();
+    const uint64_t ngroups = 1ULL << (n - K);
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += step) {
+        const uint64_t base = insert0_mask(g, bd.tmask);
+        C a[A];
+#pragma unroll
+        for (int j = 0; j < A; ++j) a[j] = P::load(psi[base | soff[j]]);
+        // rows rolled: the entries are read from shared memory per row, not hoisted into
+        // registers for the whole loop over groups
+#pragma unroll 1
+        for (int r = 0; r < A; ++r) {
+            const uint32_t rows = srows[r], reals = sreal[r];
+            auto re = P::zero(), im = P::zero();
+#pragma unroll
+            for (int j = 0; j < A; ++j) {
+                if (!((rows >> j) & 1)) continue;
+                const Kt mr = sm[2 * (r * A + j)];
+                re = P::fma1(mr, a[j].re, re);
+                im = P::fma1(mr, a[j].im, im);
+                if (!((reals >> j) & 1)) {
+                    const Kt mi = sm[2 * (r * A + j) + 1];
+                    re = P::fma1(P::kneg(mi), a[j].im, re);
+                    im = P::fma1(mi, a[j].re, im);
+                }
+            }
+            C out;
+            out.re = re;
+            out.im = im;
+            psi[base | soff[r]] = P::store(out);
+        }
+    }
+}
+
+template <class P, int K>
+cudaError_t group_sparse_t(void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat, const BlockSparsity& nz,
+                           cudaStream_t s) {
+    const uint64_t ngroups = 1ULL << (n - K);
+    const uint64_t blocks = (ngroups + kBlockThreads - 1) / kBlockThreads;
+    const unsigned grid = (unsigned)(blocks < 152ULL * 8 ? blocks : 152ULL * 8);
+    k_group_sparse<P, K><<<grid, kBlockThreads, 0, s>>>(static_cast<typename P::S*>(psi), n, bd, d_mat, nz);
+    return cudaGetLastError();
+}
+
+template <class P>
+cudaError_t block_sparse_t(void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat, const BlockSparsity& nz,
+                           cudaStream_t s) {
+    switch (bd.k) {
+        case 1: return group_sparse_t<P, 1>(psi, n, bd, d_mat, nz, s);
+        case 2: return group_sparse_t<P, 2>(psi, n, bd, d_mat, nz, s);
+        case 3: return group_sparse_t<P, 3>(psi, n, bd, d_mat, nz, s);
+        case 4: return group_sparse_t<P, 4>(psi, n, bd, d_mat, nz, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 template <class P, int K>
 cudaError_t group_t(void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat, cudaStream_t s) {
     const uint64_t ngroups = 1ULL << (n - K);
@@ -164,6 +243,15 @@ cudaError_t block_t(void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat
 }
 
 }  // namespace
+
+cudaError_t launch_block_sparse(int P, void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat,
+                                const BlockSparsity& nz, cudaStream_t s) {
+    switch (P) {
+        case LLG_F64: return block_sparse_t<PolF64>(psi, n, bd, d_mat, nz, s);
+        case LLG_F32: return block_sparse_t<PolF32>(psi, n, bd, d_mat, nz, s);
+        default: return block_sparse_t<PolDF64>(psi, n, bd, d_mat, nz, s);
+    }
+}
 
 cudaError_t launch_block(int P, void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat, cudaStream_t s) {
     switch (P) {

@@ -649,6 +649,29 @@ int llg_apply_matrix(llg_state* st, int k, const int* qubits, const double* m) {
         LLG_CUDA(cudaEventCreateWithFlags(&st->block_done, cudaEventDisableTiming), "cudaEventCreate");
     }
     if (st->block_pending) LLG_CUDA(cudaEventSynchronize(st->block_done), "block staging");
+    // a mostly-zero block (noise-channel superoperators) runs only its nonzero entries: two
+    // multiply-adds per real entry, four per complex one, against four per entry dense
+    BlockSparsity nz;
+    std::memset(&nz, 0, sizeof(nz));
+    int sparse_cost = 0;
+    const int dim = 1 << k;
+    for (int r = 0; r < dim; ++r)
+        for (int c = 0; c < dim; ++c) {
+            const double re = m[2 * (r * dim + c)], im = m[2 * (r * dim + c) + 1];
+            if (re == 0.0 && im == 0.0) continue;
+            nz.rows[r] |= 1u << c;
+            if (im == 0.0) nz.real[r] |= 1u << c;
+            sparse_cost += im == 0.0 ? 2 : 4;
+        }
+    if (k <= 4 && 2 * sparse_cost <= 4 * dim * dim) {
+        for (int i = 0; i < slots; ++i) st->h_block[i] = pack_coef(st->P, m[i]);
+        LLG_CUDA(cudaMemcpyAsync(st->d_block, st->h_block, slots * sizeof(uint64_t), cudaMemcpyHostToDevice, st->stream),
+                 "cudaMemcpyAsync(block)");
+        LLG_CUDA(cudaEventRecord(st->block_done, st->stream), "cudaEventRecord");
+        st->block_pending = true;
+        return traced(st, LLG_PROF_GATE, 1, "block kernel (sparse)",
+                      [&] { return launch_block_sparse(st->P, st->d_psi, st->n, bd, st->d_block, nz, st->stream); });
+    }
     if (block_tc_eligible(st->P, st->n, k)) {
         const size_t wb = block_tc_weight_bytes(k);
         if (!st->d_block_tc) {

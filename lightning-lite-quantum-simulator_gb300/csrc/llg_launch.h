@@ -75,6 +75,14 @@ struct BlockDesc {
     uint64_t tmask;
 };
 cudaError_t launch_block(int P, void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat, cudaStream_t s);
+// Which entries of a block of k <= 4 qubits are nonzero (bit c of rows[r]) and real (bit c of
+// real[r]); the block kernel then sums row r over those columns only.
+struct BlockSparsity {
+    uint32_t rows[16];
+    uint32_t real[16];
+};
+cudaError_t launch_block_sparse(int P, void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat,
+                                const BlockSparsity& nz, cudaStream_t s);
 
 // 4- and 5-qubit blocks on double-float states of at least k + 7 qubits on the tensor cores
 // (llg_block_tc.cu): the host slices the matrix (2 * 4^k doubles, row-major re/im) into

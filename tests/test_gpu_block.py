@@ -43,6 +43,33 @@ def test_block_matches_oracle(precision, n, k):
     st2.close()
 
 
+@pytest.mark.parametrize("precision", ["df64", "fp64", "complex64"])
+@pytest.mark.parametrize("n,k", [(5, 1), (9, 2), (10, 3), (13, 4)])
+def test_sparse_block_matches_oracle(precision, n, k):
+    # blocks with at most a quarter of their cost in nonzero entries run the sparse kernel: real and
+    # complex entries, an empty row, a full row
+    ops = workloads.layered_rotations(n, 2, seed=n)
+    st = llgpu.State(n, precision)
+    st.apply_ops(ops)
+    want = oracle.run_ops(n, ops)
+    rng = np.random.default_rng(50 * n + k)
+    d = 1 << k
+    for rep in range(3):
+        m = np.zeros((d, d), dtype=complex)
+        for r in range(d):
+            for c in rng.choice(d, size=min(d, 1 + (r % 2)), replace=False):
+                m[r, c] = rng.normal() + (1j * rng.normal() if (r + c) % 3 == 0 else 0.0)
+        m[d - 1, :] = 0.0
+        if k == 1:
+            m[0, :] = [0.6, 0.0]
+        qs = [int(x) for x in rng.choice(n, size=k, replace=False)]
+        st.apply_matrix(qs, m)
+        oracle.apply_matrix(want, n, qs, m)
+    scale = max(1.0, float(np.max(np.abs(want))))
+    assert np.max(np.abs(st.state() - want)) <= TOL[precision] * scale
+    st.close()
+
+
 def test_non_unitary_block_and_high_qubits():
     rng = np.random.default_rng(3)
     n = 20
