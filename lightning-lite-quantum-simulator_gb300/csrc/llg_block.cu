@@ -169,9 +169,12 @@ __global__ void __launch_bounds__(kBlockThreads) k_group_sparse(typename P::S* _
         C a[A];
 #pragma unroll
         for (int j = 0; j < A; ++j) a[j] = P::load(psi[base | soff[j]]);
-        // rows rolled: the entries are read from shared memory per row, not hoisted into
-        // registers for the whole loop over groups
-#pragma unroll 1
+        // rows unrolled by a few: independent accumulation chains for the FP64 pipe, the entries
+        // still read from shared memory per row rather than hoisted into registers for the whole
+        // loop over groups (two rows at a time for 16-amplitude groups, whose inputs take 64
+        // registers in FP64)
+        constexpr int kRowUnroll = K == 4 ? 2 : 4;
+#pragma unroll kRowUnroll
         for (int r = 0; r < A; ++r) {
             const uint32_t rows = srows[r], reals = sreal[r];
             auto re = P::zero(), im = P::zero();
