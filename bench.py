@@ -526,7 +526,7 @@ def run_ours(args, rank, world, local):
 
     sweeps = None
     if not args.no_sweeps:
-        sweeps = run_sweep_bench(args, torch)
+        sweeps = run_sweep_bench(args, torch, fma_rate)
 
     adj = None
     if not args.no_adjoint:
@@ -675,7 +675,7 @@ def adjoint_once(args, torch, precision):
             "precision": precision, "_grads": np.array(g)}
 
 
-def run_sweep_bench(args, torch):
+def run_sweep_bench(args, torch, fma_rate=None):
     """Per-gate streaming sweeps on the 30-qubit state (the reference's one-pass-per-gate method):
     each gate kind on several target qubits, timed per launch with CUDA events on the engine's
     stream.  Algorithmic bytes per sweep: 32 B x 2^n for 1-qubit gates (read + write every
@@ -759,8 +759,11 @@ def run_sweep_bench(args, torch):
             st.profile(False)
             per = ms / cnt / 1e3
             gbs = 32 * (1 << n) / per / 1e9
-            res[f"block{k}"] = {"ms_per_sweep": per * 1e3, "gbs": gbs, "frac": gbs / peak,
-                                "tflops": 8 * (4 ** k) * (1 << (n - k)) / per / 1e12, "qubits": qs}
+            tflops = 8 * (4 ** k) * (1 << (n - k)) / per / 1e12
+            res[f"block{k}"] = {"ms_per_sweep": per * 1e3, "gbs": gbs, "frac": gbs / peak, "tflops": tflops, "qubits": qs}
+            if prec == "complex128" and fma_rate:
+                # the dense FP64 forms are bound by the FP64 pipe: 2 FLOP per multiply-add
+                res[f"block{k}"]["fp64_frac"] = tflops * 1e12 / (2 * fma_rate)
         st.close()
         out[prec] = res
     return out

@@ -400,16 +400,334 @@ cudaError_t launch_tc(void* psi, int n, const BlockDesc& bd, const void* d_weigh
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------------------------------
+// IEEE complex128 (FP64) states, k = 4: the same pipeline with eight slices per operand and an
+// exact recombination, so the products leave the FP64 pipe altogether.
+//   * A real x of a group whose largest biased exponent is e_g is the 62-bit fixed-point integer
+//     X = m 2^(9 - e_g + e) (m the 53-bit significand, e its exponent; truncated below 2^-61 of the
+//     group's scale), split into eight balanced base-256 digits: x = 2^(e_g - 1028) sum_s d_s
+//     2^(-8 s), |d_s| <= 128, exact in bf16.  The gate's rows are split on the host the same way
+//     (eight slices capture a double exactly).
+//   * The 36 slice products with i + j <= 7 go by diagonal into six accumulators: d = 0..4 one each
+//     (a diagonal has at most eight products of 32 terms, each below 2^14: below 2^22, exact in
+//     fp32), d = 5, 6, 7 shared by Horner's rule through the MMA's input scale.
+//   * Epilogue: every exact diagonal becomes an integer by the 1.5 * 2^23 magic addition, the
+//     Horner accumulator is rounded to an integer at 2^-40 of D_0's unit, the six combine exactly
+//     in a 64-bit integer (below 2^60), which is converted to double once (the only rounding of
+//     the product, apart from the slicing's 2^-61 truncation and the dropped diagonals near 2^-64)
+//     and scaled by 2^(e_g + e_r - 1075) through its exponent field.
+// One CTA of 256 threads per SM: two accumulator sets of 6 x 32 columns take 384 of the 512
+// columns of tensor memory.
+// ------------------------------------------------------------------------------------------
+constexpr int kTcSlicesF64 = 8;
+constexpr int kTcAccF64 = 6;
+
+template <int KQ>
+struct TcShapeF64 {
+    static constexpr int kAmps = 1 << KQ;
+    static constexpr int kReals = 2 * kAmps;
+    static constexpr int kThreads = 256;
+    static constexpr int kPer = kTcGroups * kAmps / kThreads;
+    static constexpr int kSliceBytes = kTcGroups * kReals * 2;
+    static constexpr int kWSliceBytes = kReals * kReals * 2;
+    static constexpr int kSetCols = kTcAccF64 * kReals;
+    static constexpr int kTmemCols = 512;
+    static constexpr size_t kSmemUsed =
+        (size_t)kTcSlicesF64 * (kSliceBytes + kWSliceBytes) + (size_t)kTcGroups * kAmps * sizeof(double2);
+    // padded past half of the SM's shared memory: a second CTA on the SM would wait for the
+    // first one's tensor-memory columns for its whole run
+    static constexpr size_t kSmem = kSmemUsed > 120 * 1024 ? kSmemUsed : 120 * 1024;
+    static_assert(KQ == 4, "the eight-slice FP64 form fits shared memory for 4-qubit blocks");
+    static_assert(kPer == 8, "one 8-wide core of real and one of imaginary parts per thread");
+    static_assert(2 * kSetCols <= kTmemCols, "two accumulator sets in the allocation");
+};
+
+// bf16 bits of a small integer d (|d| <= 256): the float d built by the magic addition, whose value
+// has at most 8 significant bits, keeps its high half exactly
+__device__ __forceinline__ uint32_t bf16_of_int(int d) {
+    const float f = __int_as_float(0x4B400000 + d) - 12582912.0f;
+    return __float_as_uint(f) >> 16;
+}
+
+// the eight digits of x against the group exponent eg (see above), most significant first
+__device__ __forceinline__ void slice_f64(double x, int eg, uint32_t (&bits)[kTcSlicesF64]) {
+    const long long b = __double_as_longlong(x);
+    const int ex = (int)((b >> 52) & 0x7FF);
+    const long long m = (b & 0xFFFFFFFFFFFFFLL) | (ex ? (1LL << 52) : 0LL);
+    const int sh = 9 - (eg - (ex ? ex : 1));
+    long long X = sh >= 0 ? (m << sh) : (sh > -63 ? (m >> -sh) : 0LL);
+    if (b < 0) X = -X;
+#pragma unroll
+    for (int s = kTcSlicesF64 - 1; s > 0; --s) {
+        const int d = (int)(signed char)(X & 0xFF);
+        X = (X - d) >> 8;
+        bits[s] = bf16_of_int(d);
+    }
+    bits[0] = bf16_of_int((int)X);
+}
+
+// an exact fp32 integer v (|v| < 2^22), or v rounded to the nearest integer, as an int
+__device__ __forceinline__ int int_of_f32(float v) { return __float_as_int(v + 12582912.0f) - 0x4B400000; }
+
+template <int KQ>
+__global__ void __launch_bounds__(TcShapeF64<KQ>::kThreads, 1)
+    k_block_tc_f64(double2* __restrict__ psi, int n, BlockDesc bd, const uint16_t* __restrict__ wslices,
+                   const int32_t* __restrict__ wexp, int* __restrict__ err_flag) {
+    using T = TcShapeF64<KQ>;
+    constexpr int kAmps = T::kAmps, kReals = T::kReals, kPer = T::kPer;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* sA = smem;                                   // kTcSlicesF64 state slices
+    unsigned char* sW = smem + kTcSlicesF64 * T::kSliceBytes;   // kTcSlicesF64 gate slices
+    double2* sIn = reinterpret_cast<double2*>(sW + kTcSlicesF64 * T::kWSliceBytes);  // [amplitude][group]
+    __shared__ uint64_t toff[kAmps];
+    __shared__ int32_t eg_s[3][kTcGroups];
+    __shared__ int32_t er_s[kReals];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_s;
+    __shared__ int abort_s;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    for (int j = tid; j < kAmps; j += blockDim.x) {
+        uint64_t o = 0;
+        for (int b = 0; b < KQ; ++b)
+            if ((j >> b) & 1) o |= 1ULL << bd.q[b];
+        toff[j] = o;
+    }
+    for (int r = tid; r < kReals; r += blockDim.x) er_s[r] = wexp[r];
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(wslices);
+        uint4* dst = reinterpret_cast<uint4*>(sW);
+        for (int i = tid; i < kTcSlicesF64 * T::kWSliceBytes / 16; i += blockDim.x) dst[i] = src[i];
+    }
+    if (tid == 0) {
+        abort_s = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_s)),
+                     "r"(T::kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_s;
+
+    const uint64_t ngroups = 1ULL << (n - KQ);
+    const uint64_t ntiles = ngroups / kTcGroups;
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kReals >> 3) << 17) |
+                           ((uint32_t)(kTcGroups >> 4) << 24);
+    const uint32_t lbo = 128, sbo = (kReals / 8) * 128;
+    constexpr int kH = kAmps / kPer, kG = 32 / kH;
+    const int gl = (tid % kG) + kG * (tid >> 5);
+    const int h = (tid / kG) % kH;
+    uint32_t phase = 0;
+    auto prefetch = [&](uint64_t tile) {
+        const uint64_t b = insert0_mask(tile * kTcGroups + (uint64_t)gl, bd.tmask);
+#pragma unroll
+        for (int i = 0; i < kPer; ++i)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(&sIn[(kPer * h + i) * kTcGroups + gl])),
+                         "l"(psi + (b | toff[kPer * h + i]))
+                         : "memory");
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    __syncthreads();  // toff
+    if ((uint64_t)blockIdx.x < ntiles) prefetch(blockIdx.x);
+
+    auto wait_mma = [&](uint32_t ph) {
+        uint32_t done = 0;
+        for (long it = 0; it < kTcWaitLimit && !done; ++it)
+            asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                         : "=r"(done)
+                         : "r"(smem_u32(&mbar)), "r"(ph));
+        return done != 0;
+    };
+    // warp w reads tensor-memory lanes 32 (w & 3) .. +31 (its groups) and amplitudes 8 (w >> 2) .. +7
+    auto epilogue = [&](uint64_t tile, int set, int egb, int a0) {
+        const int row = 32 * (warp & 3) + lane;
+        const int eg = eg_s[egb][row];
+        double out[2][8];
+#pragma unroll
+        for (int part = 0; part < 2; ++part) {
+            uint32_t v[kTcAccF64][8];
+#pragma unroll
+            for (int d = 0; d < kTcAccF64; ++d) {
+                const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) +
+                                       (uint32_t)(set * T::kSetCols + d * kReals + kAmps * part + a0);
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                             : "=r"(v[d][0]), "=r"(v[d][1]), "=r"(v[d][2]), "=r"(v[d][3]), "=r"(v[d][4]), "=r"(v[d][5]),
+                               "=r"(v[d][6]), "=r"(v[d][7])
+                             : "r"(taddr));
+            }
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                // 2^40 sum_d 2^(-8 d) D_d as one integer: D_0..D_4 exact, D_567 rounded at 2^-40
+                long long acc = (long long)int_of_f32(__uint_as_float(v[5][c]));
+#pragma unroll
+                for (int d = 0; d < 5; ++d) acc += (long long)int_of_f32(__uint_as_float(v[d][c])) << (40 - 8 * d);
+                double r = __ll2double_rn(acc);
+                // times 2^(e_g - 1028) 2^(e_r - 7) 2^-40 through the exponent field
+                const int et = eg + er_s[kAmps * part + a0 + c] - 1075;
+                const long long rb = __double_as_longlong(r);
+                const int ef = (int)((rb >> 52) & 0x7FF), ne = ef + et;
+                if (ef != 0 && ne >= 1 && ne <= 2046) r = __longlong_as_double(rb + ((long long)et << 52));
+                else if (r != 0.0) r = ldexp(r, et);
+                out[part][c] = r;
+            }
+        }
+        const uint64_t base = insert0_mask(tile * kTcGroups + (uint64_t)row, bd.tmask);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) psi[base | toff[a0 + c]] = make_double2(out[0][c], out[1][c]);
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    };
+    auto mma = [&](uint32_t dcol, uint64_t da, uint64_t dw, uint32_t acc, bool scale) {
+        if (scale)
+            asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p, 8;\n}" ::"r"(
+                             dcol),
+                         "l"(da), "l"(dw), "r"(idesc), "r"(acc));
+        else
+            asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
+                             dcol),
+                         "l"(da), "l"(dw), "r"(idesc), "r"(acc));
+    };
+
+    uint64_t prev_tile = 0;
+    bool have_prev = false;
+    int set = 0, egb = 0;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, set ^= 1, egb = egb == 2 ? 0 : egb + 1) {
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        double2 a[kPer];
+        int mx = 0;
+#pragma unroll
+        for (int i = 0; i < kPer; ++i) {
+            a[i] = sIn[(kPer * h + i) * kTcGroups + gl];
+            mx = max(mx, (int)((__double_as_longlong(a[i].x) >> 52) & 0x7FF));
+            mx = max(mx, (int)((__double_as_longlong(a[i].y) >> 52) & 0x7FF));
+        }
+#pragma unroll
+        for (int off = kG; off < 32; off <<= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+        const int eg = max(mx, 1);  // subnormal and zero groups take the smallest normal scale
+        if (h == 0) eg_s[egb][gl] = eg;
+        if (have_prev && !wait_mma(phase)) abort_s = 1;
+        __syncthreads();
+        if (abort_s) {
+            if (tid == 0) atomicExch(err_flag, 1);
+            wait_mma(phase);
+            have_prev = false;
+            break;
+        }
+        if (have_prev) {
+            phase ^= 1;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        }
+        if (tile + gridDim.x < ntiles) prefetch(tile + gridDim.x);
+        // ---- eight balanced 8-bit slices per real, into the core-matrix layout ----
+#pragma unroll
+        for (int part = 0; part < 2; ++part) {
+            uint32_t packed[kTcSlicesF64][4];
+#pragma unroll
+            for (int i2 = 0; i2 < 4; ++i2) {
+                uint32_t b0[kTcSlicesF64], b1[kTcSlicesF64];
+                slice_f64(part ? a[2 * i2].y : a[2 * i2].x, eg, b0);
+                slice_f64(part ? a[2 * i2 + 1].y : a[2 * i2 + 1].x, eg, b1);
+#pragma unroll
+                for (int s = 0; s < kTcSlicesF64; ++s) packed[s][i2] = b0[s] | (b1[s] << 16);
+            }
+            const int c0 = kAmps * part + kPer * h;
+#pragma unroll
+            for (int s = 0; s < kTcSlicesF64; ++s)
+                *reinterpret_cast<uint4*>(sA + s * T::kSliceBytes + core_off(gl, c0, kReals)) =
+                    make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // ---- 36 slice products (i + j <= 7): diagonals 0..4 one accumulator each, 5..7 one by Horner ----
+        if (tid == 0) {
+            const uint32_t tset = tmem + (uint32_t)(set * T::kSetCols);
+            const uint64_t da0 = tc_desc(smem_u32(sA), lbo, sbo), dw0 = tc_desc(smem_u32(sW), lbo, sbo);
+            auto diagonal = [&](int d, uint32_t dcol, bool first_fresh) {
+                bool first = true;
+                for (int i = 0; i <= d; ++i) {
+                    const int j = d - i;
+                    if (i >= kTcSlicesF64 || j >= kTcSlicesF64) continue;
+                    for (int ks = 0; ks < kReals / 16; ++ks) {
+                        const uint64_t da = da0 + (uint64_t)((i * T::kSliceBytes + ks * 256) >> 4);
+                        const uint64_t dw = dw0 + (uint64_t)((j * T::kWSliceBytes + ks * 256) >> 4);
+                        mma(dcol, da, dw, (first && first_fresh) ? 0u : 1u, first && !first_fresh);
+                        first = false;
+                    }
+                }
+            };
+            for (int d = 0; d < 5; ++d) diagonal(d, tset + (uint32_t)(d * kReals), true);
+            diagonal(7, tset + (uint32_t)(5 * kReals), true);
+            diagonal(6, tset + (uint32_t)(5 * kReals), false);
+            diagonal(5, tset + (uint32_t)(5 * kReals), false);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(&mbar)));
+        }
+        if (have_prev) {
+            const int egp = egb == 0 ? 2 : egb - 1;
+            if (warp != 0) epilogue(prev_tile, set ^ 1, egp, 8 * (warp >> 2));
+            if (warp == 4) epilogue(prev_tile, set ^ 1, egp, 0);
+            if (warp == 0) asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        }
+        prev_tile = tile;
+        have_prev = true;
+    }
+    if (have_prev) {
+        if (!wait_mma(phase)) abort_s = 1;
+        __syncthreads();
+        if (abort_s) {
+            if (tid == 0) atomicExch(err_flag, 1);
+            wait_mma(phase);
+        } else {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            epilogue(prev_tile, set ^ 1, egb == 0 ? 2 : egb - 1, 8 * (warp >> 2));
+        }
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(T::kTmemCols));
+}
+
+template <int KQ>
+cudaError_t launch_tc_f64(void* psi, int n, const BlockDesc& bd, const void* d_weights, int* err_flag, cudaStream_t s) {
+    using T = TcShapeF64<KQ>;
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_block_tc_f64<KQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::kSmem);
+    if (attr != cudaSuccess) return attr;
+    const uint64_t ntiles = (1ULL << (n - KQ)) / kTcGroups;
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned grid = (unsigned)(ntiles < (uint64_t)sms ? ntiles : (uint64_t)sms);
+    const uint16_t* w = static_cast<const uint16_t*>(d_weights);
+    const int32_t* ex = reinterpret_cast<const int32_t*>(static_cast<const unsigned char*>(d_weights) +
+                                                          (size_t)kTcSlicesF64 * T::kWSliceBytes);
+    k_block_tc_f64<KQ><<<grid, T::kThreads, T::kSmem, s>>>(static_cast<double2*>(psi), n, bd, w, ex, err_flag);
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 // Host side: the gate's real form in slices (exact in double), in the kernel's layout:
 // kTcSlices slices of 2A x 2A bf16, then 2A row exponents.
-void block_tc_prepare(int k, const double* m, void* weights) {
+namespace {
+// The gate's real form, row r split as W[r][c] = 2^(e_r - top) sum_j w_j[r][c] 2^(-8 j) into
+// `slices` slices (|w_0| < 2^top; later slices are balanced remainders of magnitude <= 128, so
+// eight slices hold a double exactly), in the kernel's core-matrix layout, then the 2A row
+// exponents.
+void prepare_slices(int k, const double* m, void* weights, int slices, int top) {
     const int amps = 1 << k, reals = 2 * amps;
     const size_t wslice = (size_t)reals * reals * 2;
     unsigned char* out = static_cast<unsigned char*>(weights);
-    int32_t* wexp = reinterpret_cast<int32_t*>(out + kTcSlices * wslice);
-    std::memset(out, 0, kTcSlices * wslice);
+    int32_t* wexp = reinterpret_cast<int32_t*>(out + slices * wslice);
+    std::memset(out, 0, slices * wslice);
     std::vector<double> w(reals);
     for (int r = 0; r < reals; ++r) {
         const int orow = r & (amps - 1), oim = r >> k;
@@ -429,8 +747,8 @@ void block_tc_prepare(int k, const double* m, void* weights) {
         if (e == -1000) e = 0;
         wexp[r] = e;
         for (int c = 0; c < reals; ++c) {
-            double v = std::ldexp(w[c], 8 - e);
-            for (int s = 0; s < kTcSlices; ++s) {
+            double v = std::ldexp(w[c], top - e);
+            for (int s = 0; s < slices; ++s) {
                 const double q = std::nearbyint(v);
                 v = (v - q) * 256.0;
                 const float f = (float)q;  // an integer of magnitude <= 256: exact in bf16
@@ -441,15 +759,25 @@ void block_tc_prepare(int k, const double* m, void* weights) {
         }
     }
 }
+}  // namespace
 
-size_t block_tc_weight_bytes(int k) {
-    const size_t reals = (size_t)2 << k;
-    return kTcSlices * reals * reals * 2 + reals * sizeof(int32_t);
+void block_tc_prepare(int P, int k, const double* m, void* weights) {
+    if (P == LLG_F64) prepare_slices(k, m, weights, kTcSlicesF64, 7);
+    else prepare_slices(k, m, weights, kTcSlices, 8);
 }
 
-bool block_tc_eligible(int P, int n, int k) { return P == LLG_DF64 && (k == 4 || k == 5) && n >= k + 7; }
+size_t block_tc_weight_bytes(int P, int k) {
+    const size_t reals = (size_t)2 << k;
+    return (P == LLG_F64 ? kTcSlicesF64 : kTcSlices) * reals * reals * 2 + reals * sizeof(int32_t);
+}
 
-cudaError_t launch_block_tc(void* psi, int n, const BlockDesc& bd, const void* d_weights, int* err_flag, cudaStream_t s) {
+bool block_tc_eligible(int P, int n, int k) {
+    return (P == LLG_DF64 && (k == 4 || k == 5) && n >= k + 7) || (P == LLG_F64 && k == 4 && n >= k + 7);
+}
+
+cudaError_t launch_block_tc(int P, void* psi, int n, const BlockDesc& bd, const void* d_weights, int* err_flag,
+                            cudaStream_t s) {
+    if (P == LLG_F64) return launch_tc_f64<4>(psi, n, bd, d_weights, err_flag, s);
     return bd.k == 5 ? launch_tc<5>(psi, n, bd, d_weights, err_flag, s) : launch_tc<4>(psi, n, bd, d_weights, err_flag, s);
 }
 

@@ -673,20 +673,20 @@ int llg_apply_matrix(llg_state* st, int k, const int* qubits, const double* m) {
                       [&] { return launch_block_sparse(st->P, st->d_psi, st->n, bd, st->d_block, nz, st->stream); });
     }
     if (block_tc_eligible(st->P, st->n, k)) {
-        const size_t wb = block_tc_weight_bytes(k);
+        const size_t wb = block_tc_weight_bytes(st->P, k);
         if (!st->d_block_tc) {
-            const size_t cap = block_tc_weight_bytes(kMaxBlockQubits);
+            const size_t cap = std::max(block_tc_weight_bytes(LLG_DF64, kMaxBlockQubits), block_tc_weight_bytes(LLG_F64, 4));
             LLG_CUDA(cudaMalloc(&st->d_block_tc, cap), "cudaMalloc(block weights)");
             LLG_CUDA(cudaHostAlloc((void**)&st->h_block_tc, cap, cudaHostAllocDefault), "cudaHostAlloc(block weights)");
         }
-        block_tc_prepare(k, m, st->h_block_tc);
+        block_tc_prepare(st->P, k, m, st->h_block_tc);
         LLG_CUDA(cudaMemcpyAsync(st->d_block_tc, st->h_block_tc, wb, cudaMemcpyHostToDevice, st->stream),
                  "cudaMemcpyAsync(block weights)");
         LLG_CUDA(cudaEventRecord(st->block_done, st->stream), "cudaEventRecord");
         st->block_pending = true;
         st->block_tc_launched = true;
         return traced(st, LLG_PROF_GATE, 1, "block kernel (tensor cores)",
-                      [&] { return launch_block_tc(st->d_psi, st->n, bd, st->d_block_tc, st->d_flags, st->stream); });
+                      [&] { return launch_block_tc(st->P, st->d_psi, st->n, bd, st->d_block_tc, st->d_flags, st->stream); });
     }
     for (int i = 0; i < slots; ++i) st->h_block[i] = pack_coef(st->P, m[i]);
     LLG_CUDA(cudaMemcpyAsync(st->d_block, st->h_block, slots * sizeof(uint64_t), cudaMemcpyHostToDevice, st->stream),

@@ -89,9 +89,10 @@ cudaError_t launch_block_sparse(int P, void* psi, int n, const BlockDesc& bd, co
 // block_tc_weight_bytes(k) of device input; a kernel whose products do not arrive within its
 // wait limit sets *err_flag (a device int of the caller's) to 1
 bool block_tc_eligible(int P, int n, int k);
-size_t block_tc_weight_bytes(int k);
-void block_tc_prepare(int k, const double* m, void* weights);
-cudaError_t launch_block_tc(void* psi, int n, const BlockDesc& bd, const void* d_weights, int* err_flag, cudaStream_t s);
+size_t block_tc_weight_bytes(int P, int k);
+void block_tc_prepare(int P, int k, const double* m, void* weights);
+cudaError_t launch_block_tc(int P, void* psi, int n, const BlockDesc& bd, const void* d_weights, int* err_flag,
+                            cudaStream_t s);
 
 // process-wide tuning cache (llg_tune.cu), keyed by an FNV-1a hash of the workload's shape
 uint64_t tune_hash(uint64_t h, uint64_t v);

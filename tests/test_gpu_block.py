@@ -86,11 +86,13 @@ def test_non_unitary_block_and_high_qubits():
     st.close()
 
 
+@pytest.mark.parametrize("precision", ["df64", "fp64"])
 @pytest.mark.parametrize("n,k", [(12, 5), (14, 5), (11, 4), (13, 4)])
-def test_tensor_core_block_edge_values(n, k):
-    # 4- and 5-qubit blocks on double-float states of k + 7 or more qubits run on the tensor cores
-    # (exact 8-bit slices against a scale per group of 2^k amplitudes): zero groups, tiny groups,
-    # 20 orders of magnitude inside one group, a non-unitary matrix with large entries and a zero row
+def test_tensor_core_block_edge_values(precision, n, k):
+    # 4- and 5-qubit blocks on double-float states, and 4-qubit blocks on IEEE complex128 states,
+    # of k + 7 or more qubits run on the tensor cores (exact 8-bit slices against a scale per group
+    # of 2^k amplitudes: six for double-float, eight for FP64): zero groups, tiny groups, 20 orders
+    # of magnitude inside one group, a non-unitary matrix with large entries and a zero row
     rng = np.random.default_rng(40 + n + k)
     psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
     qs = [0, 3, n - 5, n - 2, n - 1][5 - k:]
@@ -102,7 +104,7 @@ def test_tensor_core_block_edge_values(n, k):
     psi[[free[1] | o for o in offs]] *= 1e-25                    # a tiny group
     psi[[free[2] | o for o in offs[1:]]] *= 1e-20                # one large amplitude, the rest tiny
     psi[free[3] | offs[5]] = 3.0 - 4.0j
-    st = llgpu.State(n)
+    st = llgpu.State(n, precision)
     st.load(psi)
     want = psi.copy()
     m = (rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))) * 4.0
@@ -123,18 +125,20 @@ def test_tensor_core_block_edge_values(n, k):
     st.close()
 
 
+@pytest.mark.parametrize("precision", ["df64", "fp64"])
 @pytest.mark.parametrize("k", [2, 3, 4, 5])
-def test_blocks_after_cancellation(k):
+def test_blocks_after_cancellation(precision, k):
     """Pairs along qubit 0 equal to 1e-9: after H the differences are stored as unnormalised
-    double-float pairs whose low part outweighs the high part.  Every block kernel (a thread per
-    group for k <= 3, the tensor cores for k = 4, 5 on 12 qubits) must read them at full value."""
+    double-float pairs whose low part outweighs the high part (double-float), or as doubles 1e-9
+    below their neighbours (FP64).  Every block kernel (a thread per group for k <= 3, the tensor
+    cores for k = 4, 5 on 12 qubits) must read them at full value."""
     n = 12
     rng = np.random.default_rng(700 + k)
     psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
     psi /= np.linalg.norm(psi)
     even = np.arange(0, 1 << n, 2)
     psi[even + 1] = psi[even] * (1.0 + 1e-9 * rng.normal(size=even.size))
-    st = llgpu.State(n)
+    st = llgpu.State(n, precision)
     st.load(psi)
     st.set_fusion("tile", 10)
     ops = llgpu.make_ops([(llgpu.OP_H, 0)])
