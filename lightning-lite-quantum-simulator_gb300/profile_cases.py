@@ -122,7 +122,36 @@ def block_tc():
     st.close()
 
 
-CASES = {"tile_f64": tile_f64, "block_tc": block_tc, "tile_reg_c64": tile_reg_c64, "tile_c64": tile_c64, "streaming": streaming,
+def block_tc_f64():
+    """A dense 4-qubit block on a 26-qubit IEEE complex128 state (1 GiB) on the tensor cores (eight
+    exact slices): a random 16x16 unitary on qubits (0, 7, 13, 25), three times after a layer of H."""
+    n = 26
+    st = llgpu.State(n, "complex128")
+    st.apply_ops(llgpu.make_ops([(llgpu.OP_H, q) for q in range(n)]))
+    rng = np.random.default_rng(19)
+    m = np.linalg.qr(rng.normal(size=(16, 16)) + 1j * rng.normal(size=(16, 16)))[0]
+    for _ in range(3):
+        st.apply_matrix([0, 7, 13, 25], m)
+    st.sync()
+    st.close()
+
+
+def dm_sparse():
+    """Noise channels on a 13-qubit IEEE complex128 density matrix (a 26-qubit state, 1 GiB) through
+    the sparse block kernel: amplitude damping on qubits 0..2, then 2-qubit depolarizing on
+    (3, 4), (5, 6)."""
+    dm = llgpu.DensityMatrix(13, "complex128")
+    dm.apply_ops(llgpu.make_ops([(llgpu.OP_H, q) for q in range(13)]))
+    ad, dp = llgpu.amplitude_damping(0.01), llgpu.depolarizing(0.01, 2)
+    for q in range(3):
+        dm.kraus(ad, [q])
+    for q in (3, 5):
+        dm.kraus(dp, [q, q + 1])
+    dm.state.sync()
+    dm.close()
+
+
+CASES = {"tile_f64": tile_f64, "block_tc": block_tc, "block_tc_f64": block_tc_f64, "dm_sparse": dm_sparse, "tile_reg_c64": tile_reg_c64, "tile_c64": tile_c64, "streaming": streaming,
          "reductions": reductions, "readback": readback, "tsolve": tsolve}
 
 if __name__ == "__main__":
