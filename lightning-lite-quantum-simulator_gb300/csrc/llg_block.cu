@@ -138,56 +138,69 @@ __global__ void __launch_bounds__(kBlockThreads) k_group(typename P::S* __restri
     }
 }
 
-// A sparse block (k <= 4): a thread per group as in k_group, but row r sums only over the columns
-// whose entry is nonzero (bit c of nz.rows[r]); an entry with a zero imaginary part (bit c of
-// nz.real[r]) costs two real multiply-adds instead of four.  The masks are the same for every
-// thread, so the tests branch uniformly.  Superoperators of noise channels (Kraus sums on a
-// density matrix's row and column qubits) have 1-4 nonzero real entries per row of 4 or 16.
-template <class P, int K>
+// A sparse block (k <= 4): a thread per group as in k_group, but row r sums only over its nonzero
+// entries, listed once per CTA in shared memory.  Every loop runs exactly over the nonzeros with a
+// trip count that is the same on every thread, and a real matrix (REAL: every nonzero entry real,
+// as in the superoperators of amplitude damping, dephasing and depolarizing channels) has an
+// instantiation without the imaginary-part multiply-adds: on this GPU a predicated-off FP64
+// instruction still takes the FP64 pipe, and the first form of this kernel, which skipped zero and
+// imaginary terms by uniform tests, issued twice the FP64 instructions it executed.  The group's
+// amplitudes are staged column-major in shared memory, where the rows read them by column index.
+template <class P, int K, bool REAL>
 __global__ void __launch_bounds__(kBlockThreads) k_group_sparse(typename P::S* __restrict__ psi, int n, BlockDesc bd,
                                                                 const uint64_t* __restrict__ mat, BlockSparsity nz) {
     using Kt = typename P::K;
+    using S = typename P::S;
     using C = typename P::C;
     constexpr int A = 1 << K;
-    __shared__ Kt sm[2 * A * A];  // row-major (re, im)
+    extern __shared__ __align__(16) unsigned char smem_sparse[];
+    S* buf = reinterpret_cast<S*>(smem_sparse);  // [column][thread]
+    __shared__ Kt sre[A * A], sim[A * A];        // the nonzero entries of each row, in row order
+    __shared__ uint8_t scol[A * A];
+    __shared__ int sbeg[A + 1];
     __shared__ uint64_t soff[A];
-    __shared__ uint32_t srows[A], sreal[A];
-    for (int i = threadIdx.x; i < 2 * A * A; i += blockDim.x) sm[i] = P::k_from_bits(mat[i]);
+    if (threadIdx.x == 0) {
+        int cnt = 0;
+        for (int r = 0; r < A; ++r) {
+            sbeg[r] = cnt;
+            for (int c = 0; c < A; ++c)
+                if ((nz.rows[r] >> c) & 1) {
+                    scol[cnt] = (uint8_t)c;
+                    sre[cnt] = P::k_from_bits(mat[2 * (r * A + c)]);
+                    sim[cnt] = P::k_from_bits(mat[2 * (r * A + c) + 1]);
+                    ++cnt;
+                }
+        }
+        sbeg[A] = cnt;
+    }
     for (int j = threadIdx.x; j < A; j += blockDim.x) {
         uint64_t off = 0;
         for (int b = 0; b < K; ++b)
             if ((j >> b) & 1) off |= 1ULL << bd.q[b];
         soff[j] = off;
-        srows[j] = nz.rows[j];
-        sreal[j] = nz.real[j];
     }
     __syncthreads();
     const uint64_t ngroups = 1ULL << (n - K);
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += step) {
+    const int tid = threadIdx.x;
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + tid; g < ngroups; g += step) {
         const uint64_t base = insert0_mask(g, bd.tmask);
-        C a[A];
+        // the group into this thread's column of the staging buffer (only this thread reads it)
 #pragma unroll
-        for (int j = 0; j < A; ++j) a[j] = P::load(psi[base | soff[j]]);
-        // rows rolled: the entries are read from shared memory per row, not hoisted into
-        // registers for the whole loop over groups.  (Measured against two alternatives on
-        // 13-qubit density matrices: two or four rows in flight per thread, and per-row lists of
-        // nonzero columns over a shared-memory copy of the group; both were no faster in FP64 and
-        // 15-35 % slower in double-float.)
+        for (int j = 0; j < A; ++j) buf[j * kBlockThreads + tid] = psi[base | soff[j]];
 #pragma unroll 1
         for (int r = 0; r < A; ++r) {
-            const uint32_t rows = srows[r], reals = sreal[r];
             auto re = P::zero(), im = P::zero();
-#pragma unroll
-            for (int j = 0; j < A; ++j) {
-                if (!((rows >> j) & 1)) continue;
-                const Kt mr = sm[2 * (r * A + j)];
-                re = P::fma1(mr, a[j].re, re);
-                im = P::fma1(mr, a[j].im, im);
-                if (!((reals >> j) & 1)) {
-                    const Kt mi = sm[2 * (r * A + j) + 1];
-                    re = P::fma1(P::kneg(mi), a[j].im, re);
-                    im = P::fma1(mi, a[j].re, im);
+            const int e1 = sbeg[r + 1];
+            for (int e = sbeg[r]; e < e1; ++e) {
+                const C x = P::load(buf[scol[e] * kBlockThreads + tid]);
+                const Kt mr = sre[e];
+                re = P::fma1(mr, x.re, re);
+                im = P::fma1(mr, x.im, im);
+                if (!REAL) {
+                    const Kt mi = sim[e];
+                    re = P::fma1(P::kneg(mi), x.im, re);
+                    im = P::fma1(mi, x.re, im);
                 }
             }
             C out;
@@ -198,24 +211,36 @@ __global__ void __launch_bounds__(kBlockThreads) k_group_sparse(typename P::S* _
     }
 }
 
-template <class P, int K>
+template <class P, int K, bool REAL>
 cudaError_t group_sparse_t(void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat, const BlockSparsity& nz,
                            cudaStream_t s) {
     const uint64_t ngroups = 1ULL << (n - K);
     const uint64_t blocks = (ngroups + kBlockThreads - 1) / kBlockThreads;
     const unsigned grid = (unsigned)(blocks < 152ULL * 8 ? blocks : 152ULL * 8);
-    k_group_sparse<P, K><<<grid, kBlockThreads, 0, s>>>(static_cast<typename P::S*>(psi), n, bd, d_mat, nz);
+    const size_t smem = (size_t)(1 << K) * kBlockThreads * sizeof(typename P::S);
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_group_sparse<P, K, REAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (attr != cudaSuccess) return attr;
+    k_group_sparse<P, K, REAL><<<grid, kBlockThreads, smem, s>>>(static_cast<typename P::S*>(psi), n, bd, d_mat, nz);
     return cudaGetLastError();
+}
+
+template <class P, int K>
+cudaError_t group_sparse_k(void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat, const BlockSparsity& nz,
+                           cudaStream_t s) {
+    bool real = true;
+    for (int r = 0; r < (1 << K); ++r) real = real && nz.real[r] == nz.rows[r];
+    return real ? group_sparse_t<P, K, true>(psi, n, bd, d_mat, nz, s) : group_sparse_t<P, K, false>(psi, n, bd, d_mat, nz, s);
 }
 
 template <class P>
 cudaError_t block_sparse_t(void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat, const BlockSparsity& nz,
                            cudaStream_t s) {
     switch (bd.k) {
-        case 1: return group_sparse_t<P, 1>(psi, n, bd, d_mat, nz, s);
-        case 2: return group_sparse_t<P, 2>(psi, n, bd, d_mat, nz, s);
-        case 3: return group_sparse_t<P, 3>(psi, n, bd, d_mat, nz, s);
-        case 4: return group_sparse_t<P, 4>(psi, n, bd, d_mat, nz, s);
+        case 1: return group_sparse_k<P, 1>(psi, n, bd, d_mat, nz, s);
+        case 2: return group_sparse_k<P, 2>(psi, n, bd, d_mat, nz, s);
+        case 3: return group_sparse_k<P, 3>(psi, n, bd, d_mat, nz, s);
+        case 4: return group_sparse_k<P, 4>(psi, n, bd, d_mat, nz, s);
         default: return cudaErrorInvalidValue;
     }
 }

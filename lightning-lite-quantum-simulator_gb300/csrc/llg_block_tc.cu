@@ -416,8 +416,8 @@ cudaError_t launch_tc(void* psi, int n, const BlockDesc& bd, const void* d_weigh
 //     in a 64-bit integer (below 2^60), which is converted to double once (the only rounding of
 //     the product, apart from the slicing's 2^-61 truncation and the dropped diagonals near 2^-64)
 //     and scaled by 2^(e_g + e_r - 1075) through its exponent field.
-// One CTA of 256 threads per SM: two accumulator sets of 6 x 32 columns take 384 of the 512
-// columns of tensor memory.
+// One CTA of 512 threads per SM, four amplitudes per thread: two accumulator sets of 6 x 32
+// columns take 384 of the 512 columns of tensor memory.
 // ------------------------------------------------------------------------------------------
 constexpr int kTcSlicesF64 = 8;
 constexpr int kTcAccF64 = 6;
@@ -426,8 +426,9 @@ template <int KQ>
 struct TcShapeF64 {
     static constexpr int kAmps = 1 << KQ;
     static constexpr int kReals = 2 * kAmps;
-    static constexpr int kThreads = 256;
-    static constexpr int kPer = kTcGroups * kAmps / kThreads;
+    static constexpr int kThreads = 512;
+    static constexpr int kPer = kTcGroups * kAmps / kThreads;  // amplitudes per thread (4)
+    static constexpr int kEpi = kAmps / (kThreads / 128);      // amplitudes per warp in the epilogue (4)
     static constexpr int kSliceBytes = kTcGroups * kReals * 2;
     static constexpr int kWSliceBytes = kReals * kReals * 2;
     static constexpr int kSetCols = kTcAccF64 * kReals;
@@ -438,7 +439,7 @@ struct TcShapeF64 {
     // first one's tensor-memory columns for its whole run
     static constexpr size_t kSmem = kSmemUsed > 120 * 1024 ? kSmemUsed : 120 * 1024;
     static_assert(KQ == 4, "the eight-slice FP64 form fits shared memory for 4-qubit blocks");
-    static_assert(kPer == 8, "one 8-wide core of real and one of imaginary parts per thread");
+    static_assert(kPer == 4 && kEpi == 4, "half an 8-wide core row of real and of imaginary parts per thread");
     static_assert(2 * kSetCols <= kTmemCols, "two accumulator sets in the allocation");
 };
 
@@ -543,26 +544,27 @@ __global__ void __launch_bounds__(TcShapeF64<KQ>::kThreads, 1)
                          : "r"(smem_u32(&mbar)), "r"(ph));
         return done != 0;
     };
-    // warp w reads tensor-memory lanes 32 (w & 3) .. +31 (its groups) and amplitudes 8 (w >> 2) .. +7
+    // warp w reads tensor-memory lanes 32 (w & 3) .. +31 (its groups) and amplitudes
+    // kEpi (w >> 2) .. + kEpi - 1
+    constexpr int kEpi = T::kEpi;
     auto epilogue = [&](uint64_t tile, int set, int egb, int a0) {
         const int row = 32 * (warp & 3) + lane;
         const int eg = eg_s[egb][row];
-        double out[2][8];
+        double out[2][kEpi];
 #pragma unroll
         for (int part = 0; part < 2; ++part) {
-            uint32_t v[kTcAccF64][8];
+            uint32_t v[kTcAccF64][kEpi];
 #pragma unroll
             for (int d = 0; d < kTcAccF64; ++d) {
                 const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) +
                                        (uint32_t)(set * T::kSetCols + d * kReals + kAmps * part + a0);
-                asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                             : "=r"(v[d][0]), "=r"(v[d][1]), "=r"(v[d][2]), "=r"(v[d][3]), "=r"(v[d][4]), "=r"(v[d][5]),
-                               "=r"(v[d][6]), "=r"(v[d][7])
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                             : "=r"(v[d][0]), "=r"(v[d][1]), "=r"(v[d][2]), "=r"(v[d][3])
                              : "r"(taddr));
             }
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-            for (int c = 0; c < 8; ++c) {
+            for (int c = 0; c < kEpi; ++c) {
                 // 2^40 sum_d 2^(-8 d) D_d as one integer: D_0..D_4 exact, D_567 rounded at 2^-40
                 long long acc = (long long)int_of_f32(__uint_as_float(v[5][c]));
 #pragma unroll
@@ -579,7 +581,7 @@ __global__ void __launch_bounds__(TcShapeF64<KQ>::kThreads, 1)
         }
         const uint64_t base = insert0_mask(tile * kTcGroups + (uint64_t)row, bd.tmask);
 #pragma unroll
-        for (int c = 0; c < 8; ++c) psi[base | toff[a0 + c]] = make_double2(out[0][c], out[1][c]);
+        for (int c = 0; c < kEpi; ++c) psi[base | toff[a0 + c]] = make_double2(out[0][c], out[1][c]);
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     };
     auto mma = [&](uint32_t dcol, uint64_t da, uint64_t dw, uint32_t acc, bool scale) {
@@ -623,12 +625,13 @@ __global__ void __launch_bounds__(TcShapeF64<KQ>::kThreads, 1)
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         }
         if (tile + gridDim.x < ntiles) prefetch(tile + gridDim.x);
-        // ---- eight balanced 8-bit slices per real, into the core-matrix layout ----
+        // ---- eight balanced 8-bit slices per real, into the core-matrix layout (half a core row
+        // of 8 bytes per thread and slice) ----
 #pragma unroll
         for (int part = 0; part < 2; ++part) {
-            uint32_t packed[kTcSlicesF64][4];
+            uint32_t packed[kTcSlicesF64][kPer / 2];
 #pragma unroll
-            for (int i2 = 0; i2 < 4; ++i2) {
+            for (int i2 = 0; i2 < kPer / 2; ++i2) {
                 uint32_t b0[kTcSlicesF64], b1[kTcSlicesF64];
                 slice_f64(part ? a[2 * i2].y : a[2 * i2].x, eg, b0);
                 slice_f64(part ? a[2 * i2 + 1].y : a[2 * i2 + 1].x, eg, b1);
@@ -638,8 +641,8 @@ __global__ void __launch_bounds__(TcShapeF64<KQ>::kThreads, 1)
             const int c0 = kAmps * part + kPer * h;
 #pragma unroll
             for (int s = 0; s < kTcSlicesF64; ++s)
-                *reinterpret_cast<uint4*>(sA + s * T::kSliceBytes + core_off(gl, c0, kReals)) =
-                    make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
+                *reinterpret_cast<uint2*>(sA + s * T::kSliceBytes + core_off(gl, c0, kReals)) =
+                    make_uint2(packed[s][0], packed[s][1]);
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -670,7 +673,7 @@ __global__ void __launch_bounds__(TcShapeF64<KQ>::kThreads, 1)
         }
         if (have_prev) {
             const int egp = egb == 0 ? 2 : egb - 1;
-            if (warp != 0) epilogue(prev_tile, set ^ 1, egp, 8 * (warp >> 2));
+            if (warp != 0) epilogue(prev_tile, set ^ 1, egp, kEpi * (warp >> 2));
             if (warp == 4) epilogue(prev_tile, set ^ 1, egp, 0);
             if (warp == 0) asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         }
@@ -685,7 +688,7 @@ __global__ void __launch_bounds__(TcShapeF64<KQ>::kThreads, 1)
             wait_mma(phase);
         } else {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            epilogue(prev_tile, set ^ 1, egb == 0 ? 2 : egb - 1, 8 * (warp >> 2));
+            epilogue(prev_tile, set ^ 1, egb == 0 ? 2 : egb - 1, kEpi * (warp >> 2));
         }
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");
