@@ -73,8 +73,37 @@ def torch_pybind_include() -> str:
     return inc
 
 
+class _BuildLock:
+    """An exclusive lock on a file in the build folder: builds started at the same time (a test
+    run and a bench, two processes importing the package) wait for each other instead of writing
+    the same objects and library at once; the later one then finds everything up to date."""
+
+    def __init__(self, path: str):
+        self.path = path
+        self.fd = -1
+
+    def __enter__(self):
+        import fcntl
+
+        self.fd = os.open(self.path, os.O_CREAT | os.O_RDWR, 0o644)
+        fcntl.flock(self.fd, fcntl.LOCK_EX)
+        return self
+
+    def __exit__(self, *exc):
+        import fcntl
+
+        fcntl.flock(self.fd, fcntl.LOCK_UN)
+        os.close(self.fd)
+        return False
+
+
 def build(force: bool = False, jobs: int = 8) -> str:
     os.makedirs(OBJ, exist_ok=True)
+    with _BuildLock(os.path.join(OBJ, ".build.lock")):
+        return _build_locked(force, jobs)
+
+
+def _build_locked(force: bool, jobs: int) -> str:
     hdrs = _headers()
     tasks = []
     objs = []

@@ -151,7 +151,30 @@ def dm_sparse():
     dm.close()
 
 
-CASES = {"tile_f64": tile_f64, "block_tc": block_tc, "block_tc_f64": block_tc_f64, "dm_sparse": dm_sparse, "tile_reg_c64": tile_reg_c64, "tile_c64": tile_c64, "streaming": streaming,
+def traj_f64():
+    """IEEE complex128 noisy trajectories: 512 trajectories of the 14-qubit, 8-layer RX/RY +
+    CNOT-chain circuit with amplitude damping and dephasing sites (one launch of the default
+    configuration)."""
+    ops = workloads.noisy_layers(14, 8)
+    h = llgpu.Traj(14, ops, 0.01, 0.005, 512, "complex128")
+    h.launch(2024, 512)
+    h.launch(2024, 512)
+    h.close()
+
+
+def adjoint_f64():
+    """IEEE complex128 adjoint gradients: the 20-qubit, 10-layer RY/RZ + CZ-ring ansatz, a batch of
+    8 parameter sets (128 MiB per buffer)."""
+    n, layers, batch = 20, 10, 8
+    adj = llgpu.Adjoint(n, workloads.hea_ansatz(n, layers), 2 * n * layers, llgpu.ring_zz_terms(n), max_batch=batch,
+                        precision="complex128")
+    params = workloads.hea_params(n, layers, batch)
+    adj.run(params)
+    adj.run(params)
+    adj.close()
+
+
+CASES = {"tile_f64": tile_f64, "traj_f64": traj_f64, "adjoint_f64": adjoint_f64, "block_tc": block_tc, "block_tc_f64": block_tc_f64, "dm_sparse": dm_sparse, "tile_reg_c64": tile_reg_c64, "tile_c64": tile_c64, "streaming": streaming,
          "reductions": reductions, "readback": readback, "tsolve": tsolve}
 
 if __name__ == "__main__":

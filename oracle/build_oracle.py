@@ -48,8 +48,31 @@ def oracle_lib_path() -> str:
     return os.path.join(BUILD, "liboracle.so")
 
 
+def _locked(path: str):
+    """An exclusive file lock: concurrent builds of the oracle wait for each other."""
+    import contextlib
+    import fcntl
+
+    @contextlib.contextmanager
+    def lock():
+        fd = os.open(path, os.O_CREAT | os.O_RDWR, 0o644)
+        try:
+            fcntl.flock(fd, fcntl.LOCK_EX)
+            yield
+        finally:
+            fcntl.flock(fd, fcntl.LOCK_UN)
+            os.close(fd)
+
+    return lock()
+
+
 def build_oracle(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
+    with _locked(os.path.join(BUILD, ".build.lock")):
+        return _build_oracle_locked(force)
+
+
+def _build_oracle_locked(force: bool) -> str:
     srcs = [os.path.join(HERE, f) for f in ("sv_oracle.c", "traj_oracle.c", "adjoint_oracle.c", "noise_oracle.c", "dm_oracle.c", "tsolver_oracle.c")]
     out = oracle_lib_path()
     if force or _stale(out, srcs + [os.path.join(HERE, "sv_oracle.h")]):
