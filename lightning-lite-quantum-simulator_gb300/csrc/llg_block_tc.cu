@@ -425,22 +425,25 @@ constexpr int kTcAccF64 = 6;
 template <int KQ>
 struct TcShapeF64 {
     static constexpr int kAmps = 1 << KQ;
-    static constexpr int kReals = 2 * kAmps;
-    static constexpr int kThreads = 512;
+    static constexpr int kReals = 2 * kAmps;                   // the MMA's K and N (32 / 16)
+    static constexpr int kThreads = KQ == 4 ? 512 : 256;
+    static constexpr int kCtas = KQ == 4 ? 1 : 2;              // CTAs per SM
     static constexpr int kPer = kTcGroups * kAmps / kThreads;  // amplitudes per thread (4)
     static constexpr int kEpi = kAmps / (kThreads / 128);      // amplitudes per warp in the epilogue (4)
     static constexpr int kSliceBytes = kTcGroups * kReals * 2;
     static constexpr int kWSliceBytes = kReals * kReals * 2;
     static constexpr int kSetCols = kTcAccF64 * kReals;
-    static constexpr int kTmemCols = 512;
+    static constexpr int kTmemCols = 512 / kCtas;
     static constexpr size_t kSmemUsed =
         (size_t)kTcSlicesF64 * (kSliceBytes + kWSliceBytes) + (size_t)kTcGroups * kAmps * sizeof(double2);
-    // padded past half of the SM's shared memory: a second CTA on the SM would wait for the
-    // first one's tensor-memory columns for its whole run
-    static constexpr size_t kSmem = kSmemUsed > 120 * 1024 ? kSmemUsed : 120 * 1024;
-    static_assert(KQ == 4, "the eight-slice FP64 form fits shared memory for 4-qubit blocks");
+    // padded so that no more than kCtas CTAs share an SM: one more would wait for the others'
+    // tensor-memory columns for its whole run
+    static constexpr size_t kSmemFloor = (size_t)(228 * 1024) / (kCtas + 1) + 1024;
+    static constexpr size_t kSmem = kSmemUsed > kSmemFloor ? kSmemUsed : kSmemFloor;
+    static_assert(KQ == 3 || KQ == 4, "the eight-slice FP64 form fits shared memory for 3- and 4-qubit blocks");
     static_assert(kPer == 4 && kEpi == 4, "half an 8-wide core row of real and of imaginary parts per thread");
     static_assert(2 * kSetCols <= kTmemCols, "two accumulator sets in the allocation");
+    static_assert(kSmem * kCtas <= 227 * 1024, "kCtas CTAs fit an SM's shared memory");
 };
 
 // bf16 bits of a small integer d (|d| <= 256): the float d built by the magic addition, whose value
@@ -471,7 +474,7 @@ __device__ __forceinline__ void slice_f64(double x, int eg, uint32_t (&bits)[kTc
 __device__ __forceinline__ int int_of_f32(float v) { return __float_as_int(v + 12582912.0f) - 0x4B400000; }
 
 template <int KQ>
-__global__ void __launch_bounds__(TcShapeF64<KQ>::kThreads, 1)
+__global__ void __launch_bounds__(TcShapeF64<KQ>::kThreads, TcShapeF64<KQ>::kCtas)
     k_block_tc_f64(double2* __restrict__ psi, int n, BlockDesc bd, const uint16_t* __restrict__ wslices,
                    const int32_t* __restrict__ wexp, int* __restrict__ err_flag) {
     using T = TcShapeF64<KQ>;
@@ -708,7 +711,8 @@ cudaError_t launch_tc_f64(void* psi, int n, const BlockDesc& bd, const void* d_w
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const unsigned grid = (unsigned)(ntiles < (uint64_t)sms ? ntiles : (uint64_t)sms);
+    const uint64_t cap = (uint64_t)sms * T::kCtas;
+    const unsigned grid = (unsigned)(ntiles < cap ? ntiles : cap);
     const uint16_t* w = static_cast<const uint16_t*>(d_weights);
     const int32_t* ex = reinterpret_cast<const int32_t*>(static_cast<const unsigned char*>(d_weights) +
                                                           (size_t)kTcSlicesF64 * T::kWSliceBytes);
@@ -775,12 +779,13 @@ size_t block_tc_weight_bytes(int P, int k) {
 }
 
 bool block_tc_eligible(int P, int n, int k) {
-    return (P == LLG_DF64 && (k == 4 || k == 5) && n >= k + 7) || (P == LLG_F64 && k == 4 && n >= k + 7);
+    return (P == LLG_DF64 && (k == 4 || k == 5) && n >= k + 7) || (P == LLG_F64 && (k == 3 || k == 4) && n >= k + 7);
 }
 
 cudaError_t launch_block_tc(int P, void* psi, int n, const BlockDesc& bd, const void* d_weights, int* err_flag,
                             cudaStream_t s) {
-    if (P == LLG_F64) return launch_tc_f64<4>(psi, n, bd, d_weights, err_flag, s);
+    if (P == LLG_F64)
+        return bd.k == 3 ? launch_tc_f64<3>(psi, n, bd, d_weights, err_flag, s) : launch_tc_f64<4>(psi, n, bd, d_weights, err_flag, s);
     return bd.k == 5 ? launch_tc<5>(psi, n, bd, d_weights, err_flag, s) : launch_tc<4>(psi, n, bd, d_weights, err_flag, s);
 }
 

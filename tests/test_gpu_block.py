@@ -87,12 +87,12 @@ def test_non_unitary_block_and_high_qubits():
 
 
 @pytest.mark.parametrize("precision", ["df64", "fp64"])
-@pytest.mark.parametrize("n,k", [(12, 5), (14, 5), (11, 4), (13, 4)])
+@pytest.mark.parametrize("n,k", [(12, 5), (14, 5), (11, 4), (13, 4), (10, 3), (12, 3)])
 def test_tensor_core_block_edge_values(precision, n, k):
-    # 4- and 5-qubit blocks on double-float states, and 4-qubit blocks on IEEE complex128 states,
-    # of k + 7 or more qubits run on the tensor cores (exact 8-bit slices against a scale per group
-    # of 2^k amplitudes: six for double-float, eight for FP64): zero groups, tiny groups, 20 orders
-    # of magnitude inside one group, a non-unitary matrix with large entries and a zero row
+    # 4- and 5-qubit blocks on double-float states, and 3- and 4-qubit blocks on IEEE complex128
+    # states, of k + 7 or more qubits run on the tensor cores (exact 8-bit slices against a scale
+    # per group of 2^k amplitudes: six for double-float, eight for FP64): zero groups, tiny groups,
+    # 20 orders of magnitude inside one group, a non-unitary matrix with large entries and a zero row
     rng = np.random.default_rng(40 + n + k)
     psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
     qs = [0, 3, n - 5, n - 2, n - 1][5 - k:]
@@ -109,7 +109,7 @@ def test_tensor_core_block_edge_values(precision, n, k):
     want = psi.copy()
     m = (rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))) * 4.0
     m[7, :] = 0.0
-    m[:, 9] *= 1e-12
+    m[:, min(9, d - 2)] *= 1e-12
     st.apply_matrix(qs, m)
     oracle.apply_matrix(want, n, qs, m)
     u = rand_unitary(d, rng)
