@@ -613,6 +613,8 @@ def summarize(line: dict) -> dict:
         "zne_traj_per_s": get(line, "zne", "traj_per_s"),
         "complex128_gate_sweep_hbm_frac": {k: round(v["frac"], 3) for k, v in (get(line, "gate_sweeps", "complex128") or {}).items()
                                            if isinstance(v, dict) and "frac" in v and not k.startswith("block")} or None,
+        "complex128_dense_block_ms": {k: round(v["ms_per_sweep"], 2) for k, v in (get(line, "gate_sweeps", "complex128") or {}).items()
+                                      if k.startswith("block")} or None,
         "block5_tensor_core_hbm_frac": get(line, "gate_sweeps", "df64", "block5", "frac"),
         "dm_depolarizing_2q_df64_hbm_frac": get(line, "density_matrix", "df64_n13", "depolarizing_2q", "frac_of_hbm"),
     }

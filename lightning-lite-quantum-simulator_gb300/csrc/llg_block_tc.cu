@@ -701,6 +701,233 @@ __global__ void __launch_bounds__(TcShapeF64<KQ>::kThreads, TcShapeF64<KQ>::kCta
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(T::kTmemCols));
 }
 
+// IEEE complex128, k = 5: the same arithmetic as k_block_tc_f64 on 32-amplitude groups (K = N = 64).
+// Six accumulators of 64 columns take 384 of the 512 columns, so there is one set and a tile's
+// products and epilogue run one after the other; eight 16 KB state slices and eight 8 KB gate
+// slices take 192 KB, so the next tile is prefetched into registers (eight 16-byte loads per
+// thread, issued before the products) instead of a shared-memory buffer.
+struct TcShapeF64x5 {
+    static constexpr int kAmps = 32, kReals = 64, kThreads = 512;
+    static constexpr int kPer = kTcGroups * kAmps / kThreads;  // 8
+    static constexpr int kEpi = kAmps / (kThreads / 128);      // 8
+    static constexpr int kSliceBytes = kTcGroups * kReals * 2;
+    static constexpr int kWSliceBytes = kReals * kReals * 2;
+    static constexpr int kTmemCols = 512;
+    static constexpr size_t kSmem = (size_t)kTcSlicesF64 * (kSliceBytes + kWSliceBytes);
+    static_assert(kTcAccF64 * kReals <= kTmemCols, "one accumulator set");
+    static_assert(kSmem <= 200 * 1024, "slices fit shared memory");
+};
+
+__global__ void __launch_bounds__(TcShapeF64x5::kThreads, 1)
+    k_block_tc_f64x5(double2* __restrict__ psi, int n, BlockDesc bd, const uint16_t* __restrict__ wslices,
+                     const int32_t* __restrict__ wexp, int* __restrict__ err_flag) {
+    using T = TcShapeF64x5;
+    constexpr int KQ = 5, kAmps = T::kAmps, kReals = T::kReals, kPer = T::kPer, kEpi = T::kEpi;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* sA = smem;
+    unsigned char* sW = smem + kTcSlicesF64 * T::kSliceBytes;
+    __shared__ uint64_t toff[kAmps];
+    __shared__ int32_t eg_s[2][kTcGroups];  // by tile parity: a row is rewritten two tiles later
+    __shared__ int32_t er_s[kReals];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_s;
+    __shared__ int abort_s;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    for (int j = tid; j < kAmps; j += blockDim.x) {
+        uint64_t o = 0;
+        for (int b = 0; b < KQ; ++b)
+            if ((j >> b) & 1) o |= 1ULL << bd.q[b];
+        toff[j] = o;
+    }
+    for (int r = tid; r < kReals; r += blockDim.x) er_s[r] = wexp[r];
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(wslices);
+        uint4* dst = reinterpret_cast<uint4*>(sW);
+        for (int i = tid; i < kTcSlicesF64 * T::kWSliceBytes / 16; i += blockDim.x) dst[i] = src[i];
+    }
+    if (tid == 0) {
+        abort_s = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_s)),
+                     "r"(T::kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_s;
+
+    const uint64_t ngroups = 1ULL << (n - KQ);
+    const uint64_t ntiles = ngroups / kTcGroups;
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kReals >> 3) << 17) |
+                           ((uint32_t)(kTcGroups >> 4) << 24);
+    const uint32_t lbo = 128, sbo = (kReals / 8) * 128;
+    constexpr int kH = kAmps / kPer, kG = 32 / kH;
+    const int gl = (tid % kG) + kG * (tid >> 5);
+    const int h = (tid / kG) % kH;
+    uint32_t phase = 0;
+    double2 nxt[kPer];
+    auto prefetch = [&](uint64_t tile) {
+        const uint64_t b = insert0_mask(tile * kTcGroups + (uint64_t)gl, bd.tmask);
+#pragma unroll
+        for (int i = 0; i < kPer; ++i) nxt[i] = __ldcg(psi + (b | toff[kPer * h + i]));
+    };
+    __syncthreads();  // toff
+    if ((uint64_t)blockIdx.x < ntiles) prefetch(blockIdx.x);
+
+    auto wait_mma = [&](uint32_t ph) {
+        uint32_t done = 0;
+        for (long it = 0; it < kTcWaitLimit && !done; ++it)
+            asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                         : "=r"(done)
+                         : "r"(smem_u32(&mbar)), "r"(ph));
+        return done != 0;
+    };
+    auto mma = [&](uint32_t dcol, uint64_t da, uint64_t dw, uint32_t acc, bool scale) {
+        if (scale)
+            asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p, 8;\n}" ::"r"(
+                             dcol),
+                         "l"(da), "l"(dw), "r"(idesc), "r"(acc));
+        else
+            asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
+                             dcol),
+                         "l"(da), "l"(dw), "r"(idesc), "r"(acc));
+    };
+
+    int par = 0;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, par ^= 1) {
+        double2 a[kPer];
+        int mx = 0;
+#pragma unroll
+        for (int i = 0; i < kPer; ++i) {
+            a[i] = nxt[i];
+            mx = max(mx, (int)((__double_as_longlong(a[i].x) >> 52) & 0x7FF));
+            mx = max(mx, (int)((__double_as_longlong(a[i].y) >> 52) & 0x7FF));
+        }
+#pragma unroll
+        for (int off = kG; off < 32; off <<= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+        const int eg = max(mx, 1);
+        if (h == 0) eg_s[par][gl] = eg;  // read by this tile's epilogue, after the barrier below
+        if (tile + gridDim.x < ntiles) prefetch(tile + gridDim.x);
+        // ---- eight balanced 8-bit slices per real (the previous tile's products are done) ----
+#pragma unroll
+        for (int part = 0; part < 2; ++part) {
+            uint32_t packed[kTcSlicesF64][kPer / 2];
+#pragma unroll
+            for (int i2 = 0; i2 < kPer / 2; ++i2) {
+                uint32_t b0[kTcSlicesF64], b1[kTcSlicesF64];
+                slice_f64(part ? a[2 * i2].y : a[2 * i2].x, eg, b0);
+                slice_f64(part ? a[2 * i2 + 1].y : a[2 * i2 + 1].x, eg, b1);
+#pragma unroll
+                for (int s = 0; s < kTcSlicesF64; ++s) packed[s][i2] = b0[s] | (b1[s] << 16);
+            }
+            const int c0 = kAmps * part + kPer * h;
+#pragma unroll
+            for (int s = 0; s < kTcSlicesF64; ++s)
+                *reinterpret_cast<uint4*>(sA + s * T::kSliceBytes + core_off(gl, c0, kReals)) =
+                    make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();  // slices and exponents written; the previous epilogue has read the accumulators
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (abort_s) break;  // written before the barrier: the same on every thread
+        if (tid == 0) {
+            const uint64_t da0 = tc_desc(smem_u32(sA), lbo, sbo), dw0 = tc_desc(smem_u32(sW), lbo, sbo);
+            auto diagonal = [&](int d, uint32_t dcol, bool first_fresh) {
+                bool first = true;
+                for (int i = 0; i <= d; ++i) {
+                    const int j = d - i;
+                    if (i >= kTcSlicesF64 || j >= kTcSlicesF64) continue;
+                    for (int ks = 0; ks < kReals / 16; ++ks) {
+                        const uint64_t da = da0 + (uint64_t)((i * T::kSliceBytes + ks * 256) >> 4);
+                        const uint64_t dw = dw0 + (uint64_t)((j * T::kWSliceBytes + ks * 256) >> 4);
+                        mma(dcol, da, dw, (first && first_fresh) ? 0u : 1u, first && !first_fresh);
+                        first = false;
+                    }
+                }
+            };
+            for (int d = 0; d < 5; ++d) diagonal(d, tmem + (uint32_t)(d * kReals), true);
+            diagonal(7, tmem + (uint32_t)(5 * kReals), true);
+            diagonal(6, tmem + (uint32_t)(5 * kReals), false);
+            diagonal(5, tmem + (uint32_t)(5 * kReals), false);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(&mbar)));
+        }
+        if (!wait_mma(phase)) abort_s = 1;
+        phase ^= 1;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // ---- epilogue: warp w, tensor-memory lanes 32 (w & 3) .. +31, amplitudes kEpi (w >> 2) .. ----
+        {
+            const int row = 32 * (warp & 3) + lane;
+            const int a0 = kEpi * (warp >> 2);
+            const int egr = eg_s[par][row];
+            double out[2][kEpi];
+#pragma unroll
+            for (int part = 0; part < 2; ++part) {
+                uint32_t v[kTcAccF64][kEpi];
+#pragma unroll
+                for (int d = 0; d < kTcAccF64; ++d) {
+                    const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(d * kReals + kAmps * part + a0);
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                                 : "=r"(v[d][0]), "=r"(v[d][1]), "=r"(v[d][2]), "=r"(v[d][3]), "=r"(v[d][4]), "=r"(v[d][5]),
+                                   "=r"(v[d][6]), "=r"(v[d][7])
+                                 : "r"(taddr));
+                }
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int c = 0; c < kEpi; ++c) {
+                    long long acc = (long long)int_of_f32(__uint_as_float(v[5][c]));
+#pragma unroll
+                    for (int d = 0; d < 5; ++d) acc += (long long)int_of_f32(__uint_as_float(v[d][c])) << (40 - 8 * d);
+                    double r = __ll2double_rn(acc);
+                    const int et = egr + er_s[kAmps * part + a0 + c] - 1075;
+                    const long long rb = __double_as_longlong(r);
+                    const int ef = (int)((rb >> 52) & 0x7FF), ne = ef + et;
+                    if (ef != 0 && ne >= 1 && ne <= 2046) r = __longlong_as_double(rb + ((long long)et << 52));
+                    else if (r != 0.0) r = ldexp(r, et);
+                    out[part][c] = r;
+                }
+            }
+            if (!abort_s) {
+                const uint64_t base = insert0_mask(tile * kTcGroups + (uint64_t)row, bd.tmask);
+#pragma unroll
+                for (int c = 0; c < kEpi; ++c) psi[base | toff[a0 + c]] = make_double2(out[0][c], out[1][c]);
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (abort_s) {
+        // report, then give products still in flight a second bounded wait before the columns are freed
+        if (tid == 0) atomicExch(err_flag, 1);
+        wait_mma(phase ^ 1);
+    }
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(T::kTmemCols));
+}
+
+cudaError_t launch_tc_f64x5(void* psi, int n, const BlockDesc& bd, const void* d_weights, int* err_flag, cudaStream_t s) {
+    using T = TcShapeF64x5;
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_block_tc_f64x5, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::kSmem);
+    if (attr != cudaSuccess) return attr;
+    const uint64_t ntiles = (1ULL << (n - 5)) / kTcGroups;
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned grid = (unsigned)(ntiles < (uint64_t)sms ? ntiles : (uint64_t)sms);
+    const uint16_t* w = static_cast<const uint16_t*>(d_weights);
+    const int32_t* ex = reinterpret_cast<const int32_t*>(static_cast<const unsigned char*>(d_weights) +
+                                                          (size_t)kTcSlicesF64 * T::kWSliceBytes);
+    k_block_tc_f64x5<<<grid, T::kThreads, T::kSmem, s>>>(static_cast<double2*>(psi), n, bd, w, ex, err_flag);
+    return cudaGetLastError();
+}
+
 template <int KQ>
 cudaError_t launch_tc_f64(void* psi, int n, const BlockDesc& bd, const void* d_weights, int* err_flag, cudaStream_t s) {
     using T = TcShapeF64<KQ>;
@@ -779,13 +1006,15 @@ size_t block_tc_weight_bytes(int P, int k) {
 }
 
 bool block_tc_eligible(int P, int n, int k) {
-    return (P == LLG_DF64 && (k == 4 || k == 5) && n >= k + 7) || (P == LLG_F64 && (k == 3 || k == 4) && n >= k + 7);
+    return (P == LLG_DF64 && (k == 4 || k == 5) && n >= k + 7) || (P == LLG_F64 && k >= 3 && k <= 5 && n >= k + 7);
 }
 
 cudaError_t launch_block_tc(int P, void* psi, int n, const BlockDesc& bd, const void* d_weights, int* err_flag,
                             cudaStream_t s) {
-    if (P == LLG_F64)
+    if (P == LLG_F64) {
+        if (bd.k == 5) return launch_tc_f64x5(psi, n, bd, d_weights, err_flag, s);
         return bd.k == 3 ? launch_tc_f64<3>(psi, n, bd, d_weights, err_flag, s) : launch_tc_f64<4>(psi, n, bd, d_weights, err_flag, s);
+    }
     return bd.k == 5 ? launch_tc<5>(psi, n, bd, d_weights, err_flag, s) : launch_tc<4>(psi, n, bd, d_weights, err_flag, s);
 }
 
