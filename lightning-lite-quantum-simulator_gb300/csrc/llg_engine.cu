@@ -675,10 +675,14 @@ int llg_apply_matrix(llg_state* st, int k, const int* qubits, const double* m) {
     if (block_tc_eligible(st->P, st->n, k)) {
         const size_t wb = block_tc_weight_bytes(st->P, k);
         if (!st->d_block_tc) {
-            const size_t cap = std::max(block_tc_weight_bytes(LLG_DF64, kMaxBlockQubits), block_tc_weight_bytes(LLG_F64, 4));
+            // the largest weight set of any precision (the eight-slice FP64 one)
+            const size_t cap = std::max(block_tc_weight_bytes(LLG_DF64, kMaxBlockQubits),
+                                        block_tc_weight_bytes(LLG_F64, kMaxBlockQubits));
             LLG_CUDA(cudaMalloc(&st->d_block_tc, cap), "cudaMalloc(block weights)");
             LLG_CUDA(cudaHostAlloc((void**)&st->h_block_tc, cap, cudaHostAllocDefault), "cudaHostAlloc(block weights)");
         }
+        if (wb > std::max(block_tc_weight_bytes(LLG_DF64, kMaxBlockQubits), block_tc_weight_bytes(LLG_F64, kMaxBlockQubits)))
+            return set_error(LLG_ERUNTIME, "apply_matrix: block weights larger than their staging buffer");
         block_tc_prepare(st->P, k, m, st->h_block_tc);
         LLG_CUDA(cudaMemcpyAsync(st->d_block_tc, st->h_block_tc, wb, cudaMemcpyHostToDevice, st->stream),
                  "cudaMemcpyAsync(block weights)");
