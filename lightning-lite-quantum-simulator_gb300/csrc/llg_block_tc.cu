@@ -405,17 +405,18 @@ cudaError_t launch_tc(void* psi, int n, const BlockDesc& bd, const void* d_weigh
 // exact recombination, so the products leave the FP64 pipe altogether.
 //   * A real x of a group whose largest biased exponent is e_g is the 62-bit fixed-point integer
 //     X = m 2^(9 - e_g + e) (m the 53-bit significand, e its exponent; truncated below 2^-61 of the
-//     group's scale), split into eight balanced base-256 digits: x = 2^(e_g - 1028) sum_s d_s
-//     2^(-8 s), |d_s| <= 128, exact in bf16.  The gate's rows are split on the host the same way
-//     (eight slices capture a double exactly).
+//     group's scale), split into its signed top byte and seven unsigned bytes:
+//     x = 2^(e_g - 1028) sum_s d_s 2^(-8 s), d_0 in [-64, 64], d_1..7 in [0, 255], all exact in
+//     bf16.  The gate's rows are split on the host into balanced digits of magnitude <= 128 (eight
+//     slices capture a double exactly).
 //   * The 36 slice products with i + j <= 7 go by diagonal into six accumulators: d = 0..4 one each
-//     (a diagonal has at most eight products of 32 terms, each below 2^14: below 2^22, exact in
+//     (a diagonal has at most eight products of 32 terms, each below 2^15: below 2^23, exact in
 //     fp32), d = 5, 6, 7 shared by Horner's rule through the MMA's input scale.
-//   * Epilogue: every exact diagonal becomes an integer by the 1.5 * 2^23 magic addition, the
-//     Horner accumulator is rounded to an integer at 2^-40 of D_0's unit, the six combine exactly
-//     in a 64-bit integer (below 2^60), which is converted to double once (the only rounding of
-//     the product, apart from the slicing's 2^-61 truncation and the dropped diagonals near 2^-64)
-//     and scaled by 2^(e_g + e_r - 1075) through its exponent field.
+//   * Epilogue: every exact diagonal becomes an integer (round-to-nearest conversion), the Horner
+//     accumulator is rounded to an integer at 2^-40 of D_0's unit, the six combine exactly in a
+//     64-bit integer (below 2^61), which is converted to double once (the only rounding of the
+//     product, apart from the slicing's 2^-61 truncation and the dropped diagonals near 2^-64) and
+//     scaled by 2^(e_g + e_r - 1075) through its exponent field.
 // One CTA of 512 threads per SM, four amplitudes per thread: two accumulator sets of 6 x 32
 // columns take 384 of the 512 columns of tensor memory.
 // ------------------------------------------------------------------------------------------
@@ -453,7 +454,9 @@ __device__ __forceinline__ uint32_t bf16_of_int(int d) {
     return __float_as_uint(f) >> 16;
 }
 
-// the eight digits of x against the group exponent eg (see above), most significant first
+// the eight digits of x against the group exponent eg (see above), most significant first: the
+// signed top byte of the 62-bit integer X and its seven low bytes unsigned (X = t 2^56 +
+// sum_s u_s 2^(8 (7 - s)), u_s in [0, 255], |t| <= 64), read straight from X's two 32-bit words
 __device__ __forceinline__ void slice_f64(double x, int eg, uint32_t (&bits)[kTcSlicesF64]) {
     const long long b = __double_as_longlong(x);
     const int ex = (int)((b >> 52) & 0x7FF);
@@ -461,17 +464,16 @@ __device__ __forceinline__ void slice_f64(double x, int eg, uint32_t (&bits)[kTc
     const int sh = 9 - (eg - (ex ? ex : 1));
     long long X = sh >= 0 ? (m << sh) : (sh > -63 ? (m >> -sh) : 0LL);
     if (b < 0) X = -X;
+    const uint32_t lo = (uint32_t)X, hi = (uint32_t)((unsigned long long)X >> 32);
+    bits[0] = bf16_of_int((int)hi >> 24);
 #pragma unroll
-    for (int s = kTcSlicesF64 - 1; s > 0; --s) {
-        const int d = (int)(signed char)(X & 0xFF);
-        X = (X - d) >> 8;
-        bits[s] = bf16_of_int(d);
-    }
-    bits[0] = bf16_of_int((int)X);
+    for (int s = 1; s < 4; ++s) bits[s] = bf16_of_int((int)((hi >> (24 - 8 * s)) & 0xFF));
+#pragma unroll
+    for (int s = 4; s < kTcSlicesF64; ++s) bits[s] = bf16_of_int((int)((lo >> (56 - 8 * s)) & 0xFF));
 }
 
-// an exact fp32 integer v (|v| < 2^22), or v rounded to the nearest integer, as an int
-__device__ __forceinline__ int int_of_f32(float v) { return __float_as_int(v + 12582912.0f) - 0x4B400000; }
+// an fp32 integer value v (|v| < 2^24: every diagonal sum), or v rounded to the nearest integer
+__device__ __forceinline__ int int_of_f32(float v) { return __float2int_rn(v); }
 
 template <int KQ>
 __global__ void __launch_bounds__(TcShapeF64<KQ>::kThreads, TcShapeF64<KQ>::kCtas)

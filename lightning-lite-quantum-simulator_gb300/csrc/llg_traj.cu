@@ -143,7 +143,10 @@ __device__ __forceinline__ uint64_t packk(double x) {
 
 // shared decision record written by thread 0
 struct Decision {
-    uint64_t f_ad0, f_ad1, f_pd0, f_pd1;  // packed scale factors
+    // packed scale factors of the pair: g0 = f_ad0 f_pd0 for the |0> amplitudes (or the |1>
+    // amplitudes moved down by an amplitude-damping jump), g1 = f_ad1 f_pd1 for the |1> ones, each
+    // product formed once in double so that a site pair costs one multiply per real instead of two
+    uint64_t g0, g1;
     int ad_jump, pd_jump;
     double p1;
 };
@@ -397,8 +400,7 @@ struct Traj {
 
     // amplitude damping then phase damping on qubit q, decisions in *d (already filled)
     __device__ void kraus_apply(int q, const Decision* d) {
-        const K fa0 = P::k_from_bits(d->f_ad0), fa1 = P::k_from_bits(d->f_ad1);
-        const K fp0 = P::k_from_bits(d->f_pd0), fp1 = P::k_from_bits(d->f_pd1);
+        const K g0 = P::k_from_bits(d->g0), g1 = P::k_from_bits(d->g1);
         const int adj = d->ad_jump, pdj = d->pd_jump;
         auto scale = [](C a, K f) {
             C r;
@@ -419,19 +421,13 @@ struct Traj {
                 C a0 = P::load(s[j0]), a1 = P::load(s[j1]);
                 C t0, t1;
                 if (adj) {
-                    t0 = scale(a1, fa0);
+                    t0 = scale(a1, g0);
                     t1 = zero();
                 } else {
-                    t0 = scale(a0, fa0);
-                    t1 = scale(a1, fa1);
+                    t0 = scale(a0, g0);
+                    t1 = scale(a1, g1);
                 }
-                if (pdj) {
-                    t0 = zero();
-                    t1 = scale(t1, fp1);
-                } else {
-                    t0 = scale(t0, fp0);
-                    t1 = scale(t1, fp1);
-                }
+                if (pdj) t0 = zero();
                 s[j0] = P::store(t0);
                 s[j1] = P::store(t1);
             }
@@ -445,12 +441,10 @@ struct Traj {
         for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x, ++cnt) {
             C t;
             if (rank == 0) {
-                t = adj ? scale(P::load(remote[l]), fa0) : scale(P::load(s[l]), fa0);
-                t = pdj ? zero() : scale(t, fp0);
+                t = adj ? scale(P::load(remote[l]), g0) : scale(P::load(s[l]), g0);
+                if (pdj) t = zero();
             } else {
-                t = adj ? zero() : scale(P::load(s[l]), fa1);
-                t = scale(t, fp1);
-                if (pdj && adj) t = zero();
+                t = adj ? zero() : scale(P::load(s[l]), g1);
             }
             out[cnt] = t;
         }
@@ -473,17 +467,17 @@ __device__ void decide(double P1, const KrausParams& kp, double u1, double u2, D
     const double tot_ad = kp.gamma * P1;
     double m = fabs(u1 - s_ad);
     if (m < *min_margin) *min_margin = m;
-    double p1;
+    double p1, fa0, fa1, fp0, fp1;
     if (u1 >= s_ad && tot_ad > 0.0) {
         d->ad_jump = 1;
-        d->f_ad0 = packk<P>(rsqrt(P1));
-        d->f_ad1 = packk<P>(0.0);
+        fa0 = rsqrt(P1);
+        fa1 = 0.0;
         p1 = 0.0;
     } else {
         d->ad_jump = 0;
         const double s0 = rsqrt(s_ad);
-        d->f_ad0 = packk<P>(s0);
-        d->f_ad1 = packk<P>(kp.sq1mg * s0);
+        fa0 = s0;
+        fa1 = kp.sq1mg * s0;
         p1 = (1.0 - kp.gamma) * P1 / s_ad;
     }
     // phase damping
@@ -493,14 +487,16 @@ __device__ void decide(double P1, const KrausParams& kp, double u1, double u2, D
     if (m < *min_margin) *min_margin = m;
     if (u2 >= s_pd && tot_pd > 0.0) {
         d->pd_jump = 1;
-        d->f_pd0 = packk<P>(0.0);
-        d->f_pd1 = packk<P>(rsqrt(p1));
+        fp0 = 0.0;
+        fp1 = rsqrt(p1);
     } else {
         d->pd_jump = 0;
         const double s0 = rsqrt(s_pd);
-        d->f_pd0 = packk<P>(s0);
-        d->f_pd1 = packk<P>(kp.sq1ml * s0);
+        fp0 = s0;
+        fp1 = kp.sq1ml * s0;
     }
+    d->g0 = packk<P>(fa0 * fp0);
+    d->g1 = packk<P>(fa1 * fp1);
     d->p1 = p1;
 }
 
