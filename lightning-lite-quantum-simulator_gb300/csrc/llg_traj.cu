@@ -62,6 +62,10 @@ struct TrajGate {
     int32_t nt;     // touched qubits, in noise-site order
     int32_t q[6];
     int32_t pair;   // depolarizing mode: 1 = one 2-qubit site over (q[0], q[1]), 0 = a 1-qubit site per qubit
+    // Kraus mode: the real factor the op leaves out (RX / RY in their scale-free forms, EX_RXT,
+    // EX_RXC, EX_RT, EX_RC; 1 otherwise).  The state is then held at 1 / f of its size until the
+    // noise site that follows the gate, whose P(1) and renormalising factors take f into account.
+    double f;
 };
 
 constexpr int kObsTerms = 16;
@@ -200,6 +204,10 @@ struct Traj {
             case EX_U2: pair_gate<EX_U2>(o.q0, o); break;
             case EX_RX: pair_gate<EX_RX>(o.q0, o); break;
             case EX_RY: pair_gate<EX_RY>(o.q0, o); break;
+            case EX_RT: pair_gate<EX_RT>(o.q0, o); break;
+            case EX_RC: pair_gate<EX_RC>(o.q0, o); break;
+            case EX_RXT: pair_gate<EX_RXT>(o.q0, o); break;
+            case EX_RXC: pair_gate<EX_RXC>(o.q0, o); break;
             case EX_H: pair_gate<EX_H>(o.q0, o); break;
             case EX_X: pair_gate<EX_X>(o.q0, o); break;
             case EX_DIAG: {
@@ -461,7 +469,12 @@ template <class P>
 // The comparisons and p1 (which decides the dephasing jump) are computed exactly as the oracle
 // computes them, in IEEE double with correctly rounded division; the scale factors only rescale
 // amplitudes and use rsqrt (within 1 ulp) instead of a square root and a division.
-__device__ void decide(double P1, const KrausParams& kp, double u1, double u2, Decision* d, double* min_margin) {
+// sig: the factor the held state is short of its true size (scale-free rotations since the last
+// site); P1_held is the held state's P(1), so the true one is sig^2 P1_held, and the factors that
+// renormalise the held amplitudes carry sig.
+__device__ void decide(double P1_held, double sig, const KrausParams& kp, double u1, double u2, Decision* d,
+                       double* min_margin) {
+    const double P1 = sig == 1.0 ? P1_held : sig * sig * P1_held;
     // amplitude damping
     double s_ad = 1.0 - kp.gamma * P1;
     const double tot_ad = kp.gamma * P1;
@@ -495,8 +508,8 @@ __device__ void decide(double P1, const KrausParams& kp, double u1, double u2, D
         fp0 = s0;
         fp1 = kp.sq1ml * s0;
     }
-    d->g0 = packk<P>(fa0 * fp0);
-    d->g1 = packk<P>(fa1 * fp1);
+    d->g0 = packk<P>(fa0 * fp0 * sig);
+    d->g1 = packk<P>(fa1 * fp1 * sig);
     d->p1 = p1;
 }
 
@@ -545,6 +558,7 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
         group_sync<CL>();
         uint64_t site = 0;
         uint32_t jumps = 0;
+        double sig = 1.0;  // the held state is 1 / sig of its true size (the same on every thread)
         u_begin = u_end = 0;
         auto draw = [&](uint64_t first) {  // every thread, at the same site
             __syncthreads();
@@ -559,6 +573,7 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
         for (int g = 0; g < ngates; ++g) {
             const TrajGate& G = gates[g];
             T.gate(G.op);
+            sig *= G.f;
             if (kp.mode == NOISE_DEPOL) {
                 // decisions do not depend on the state: every thread draws the same uniforms, so
                 // the branch is uniform and needs no broadcast
@@ -585,7 +600,8 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
                 if (site + 1 >= u_end) draw(site);  // AD and PD uniforms of this pair in one chunk
                 const double P1 = T.reduce(q, false, part2);
                 if (threadIdx.x == 0)
-                    decide<P>(P1, kp, uni[site - u_begin], uni[site + 1 - u_begin], &dec, &min_margin);
+                    decide<P>(P1, sig, kp, uni[site - u_begin], uni[site + 1 - u_begin], &dec, &min_margin);
+                sig = 1.0;  // the Kraus pass below stores the true, renormalised state
                 __syncthreads();
                 const int code = dec.ad_jump | (dec.pd_jump << 1);
                 T.kraus_apply(q, &dec);
@@ -595,7 +611,8 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
                 site += 2;
             }
         }
-        const double z = ob.nterms > 0 ? T.observable(ob, part2) : T.reduce(0, true, part2);
+        double z = ob.nterms > 0 ? T.observable(ob, part2) : T.reduce(0, true, part2);
+        if (sig != 1.0) z *= sig * sig;  // a scale-free rotation with no site after it
         if (threadIdx.x == 0 && T.rank == 0) {
             z0_out[tt] = z;
             if (jumps_out) jumps_out[tt] = jumps;
@@ -818,6 +835,21 @@ bool build_gates(int n, const llg_op* ops, int nops, int precision, int mode, in
             }
             std::memset(&g[v], 0, sizeof(TrajGate));
             g[v].op = lowered[0];
+            g[v].f = 1.0;
+            if (mode == NOISE_KRAUS && (o.kind == LLG_OP_RX || o.kind == LLG_OP_RY)) {
+                // the scale-free form: every Kraus-mode gate is followed by its noise sites, whose
+                // renormalisation absorbs the factor (4 multiply-adds per pair instead of 8)
+                const double th = (v ? inv : o).theta;
+                const double c = std::cos(0.5 * th), sn = std::sin(0.5 * th);
+                const bool tan_form = std::fabs(c) >= std::fabs(sn);
+                ExecOp e;
+                std::memset(&e, 0, sizeof(e));
+                e.kind = o.kind == LLG_OP_RX ? (tan_form ? EX_RXT : EX_RXC) : (tan_form ? EX_RT : EX_RC);
+                e.q0 = o.q0;
+                e.c[2] = pack_coef(precision, tan_form ? sn / c : c / sn);
+                g[v].op = e;
+                g[v].f = tan_form ? c : sn;
+            }
             if (o.kind == LLG_OP_CNOT || o.kind == LLG_OP_CZ) {
                 g[v].nt = 2;
                 g[v].q[0] = o.q0;
