@@ -836,9 +836,11 @@ bool build_gates(int n, const llg_op* ops, int nops, int precision, int mode, in
             std::memset(&g[v], 0, sizeof(TrajGate));
             g[v].op = lowered[0];
             g[v].f = 1.0;
-            if (mode == NOISE_KRAUS && (o.kind == LLG_OP_RX || o.kind == LLG_OP_RY)) {
+            if (mode == NOISE_KRAUS && precision == LLG_F64 && (o.kind == LLG_OP_RX || o.kind == LLG_OP_RY)) {
                 // the scale-free form: every Kraus-mode gate is followed by its noise sites, whose
-                // renormalisation absorbs the factor (4 multiply-adds per pair instead of 8)
+                // renormalisation absorbs the factor (4 FP64 multiply-adds per pair instead of 8;
+                // IEEE complex128 10.8k -> 12.7k trajectories/s; the barrier-bound double-float and
+                // complex64 kernels measured 2-3 % slower with it, so they keep the full forms)
                 const double th = (v ? inv : o).theta;
                 const double c = std::cos(0.5 * th), sn = std::sin(0.5 * th);
                 const bool tan_form = std::fabs(c) >= std::fabs(sn);
