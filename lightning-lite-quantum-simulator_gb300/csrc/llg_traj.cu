@@ -406,6 +406,18 @@ struct Traj {
         if (which == 1 || which == 2) pauli_x(q);
     }
 
+    // every held amplitude times f (this CTA's slice; each CTA of a cluster scales its own)
+    __device__ void rescale(double f) {
+        const K fk = P::k_from_double(f);
+        for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x) {
+            C a = P::load(s[l]);
+            a.re = P::mulk(fk, a.re);
+            a.im = P::mulk(fk, a.im);
+            s[l] = P::store(a);
+        }
+        __syncthreads();
+    }
+
     // amplitude damping then phase damping on qubit q, decisions in *d (already filled)
     __device__ void kraus_apply(int q, const Decision* d) {
         const K g0 = P::k_from_bits(d->g0), g1 = P::k_from_bits(d->g1);
@@ -575,6 +587,12 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
             T.gate(G.op);
             sig *= G.f;
             if (kp.mode == NOISE_DEPOL) {
+                // unitary sites: the factor is carried to the observable; the held state is
+                // rescaled before it could leave the FP64 range (2^300 above its true size)
+                if (fabs(sig) < 0x1p-300) {
+                    T.rescale(sig);
+                    sig = 1.0;
+                }
                 // decisions do not depend on the state: every thread draws the same uniforms, so
                 // the branch is uniform and needs no broadcast
                 if (!(kp.gamma > 0.0)) continue;
@@ -836,11 +854,13 @@ bool build_gates(int n, const llg_op* ops, int nops, int precision, int mode, in
             std::memset(&g[v], 0, sizeof(TrajGate));
             g[v].op = lowered[0];
             g[v].f = 1.0;
-            if (mode == NOISE_KRAUS && precision == LLG_F64 && (o.kind == LLG_OP_RX || o.kind == LLG_OP_RY)) {
-                // the scale-free form: every Kraus-mode gate is followed by its noise sites, whose
-                // renormalisation absorbs the factor (4 FP64 multiply-adds per pair instead of 8;
-                // IEEE complex128 10.8k -> 12.7k trajectories/s; the barrier-bound double-float and
-                // complex64 kernels measured 2-3 % slower with it, so they keep the full forms)
+            if (precision == LLG_F64 && (o.kind == LLG_OP_RX || o.kind == LLG_OP_RY)) {
+                // the scale-free form (4 FP64 multiply-adds per pair instead of 8): in Kraus mode
+                // every gate is followed by its noise sites, whose renormalisation absorbs the
+                // factor; in depolarizing mode the sites are unitary Paulis and the factor is
+                // carried to the observable (IEEE complex128 Kraus trajectories 10.8k -> 12.7k per
+                // second; the barrier-bound double-float and complex64 kernels measured 2-3 %
+                // slower with it, so they keep the full forms)
                 const double th = (v ? inv : o).theta;
                 const double c = std::cos(0.5 * th), sn = std::sin(0.5 * th);
                 const bool tan_form = std::fabs(c) >= std::fabs(sn);
