@@ -268,7 +268,7 @@ int llg_adjoint_create(int n, const llg_op* ops, int nops, int nparams, int max_
                        const int* za, const int* zb, const double* zcoeff, llg_adjoint** out);
 int llg_adjoint_destroy(llg_adjoint* h);
 int llg_adjoint_info(const llg_adjoint* h, int* fwd_passes, int* bwd_passes, int* n_param_ops);
-/* Threads per CTA of the forward and reverse tile passes: 0 (default: 256 for tiles of 10+
+/* Threads per CTA of the forward and reverse tile passes: 0 (default: 128 for tiles of 8+
  * qubits) or a multiple of 32 in [32, 512]. */
 int llg_adjoint_set_threads(llg_adjoint* h, int threads);
 

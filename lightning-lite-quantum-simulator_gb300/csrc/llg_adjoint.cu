@@ -58,11 +58,79 @@ constexpr int kThreads = 256;
 constexpr int kEBlocksPerState = 64;
 
 // ------------------------------------------------------------------------------------------
+// IEEE complex128: parametrised RX / RY in scale-free form.  This GPU retires 2 FP64
+// multiply-adds per clock per SM, and the pair passes of these kernels are bound by that pipe.
+// The table row of an RX / RY occurrence holds (v, f) and a form byte: form 0 (|sin| <= |cos|)
+// v = tan(theta/2), f = cos(theta/2), and the rotation is f [1, -v; v, 1] (RY) or
+// f [1, -iv; -iv, 1] (RX); form 1 v = cot(theta/2), f = sin(theta/2), and it is f [v, -1; 1, v]
+// or f [v, -i; -i, v].  The tile applies the bracket, one multiply-add per real component instead
+// of two, and the kernel multiplies f into the tile's running factor F: the tile holds the
+// amplitudes divided by F, and its store multiplies F back in, so states between passes (and
+// checkpoints) are exact-scaled.  The inverse negates v, and in form 1 f too
+// (RY(-theta) = (-s) [-u, -1; 1, -u]).  An inner product of psi and lambda tiles, which share F,
+// is F^2 times that of the stored values.  |f| >= 1/sqrt(2), so |F| falls below 2^kMinTileExp
+// only after some 600 rotations in one pass; the tile is then rescaled in place.
+// ------------------------------------------------------------------------------------------
+constexpr int kMinTileExp = -300;
+
+struct RotSF {
+    double v, f;
+    bool cform;
+};
+
+// (negations flip the sign bit on the integer pipe)
+__device__ __forceinline__ RotSF rot_sf(const ExecOp& o, const uint64_t* __restrict__ trow, const uint8_t* __restrict__ frow) {
+    constexpr uint64_t kSign = 0x8000000000000000ULL;
+    RotSF r;
+    r.cform = frow[o.q1] != 0;
+    const bool inv = (o.flags & OPF_ADJOINT) != 0;
+    r.v = __longlong_as_double((long long)(trow[2 * o.q1] ^ (inv ? kSign : 0)));
+    r.f = __longlong_as_double((long long)(trow[2 * o.q1 + 1] ^ (inv && r.cform ? kSign : 0)));
+    return r;
+}
+
+// |F| < 2^kMinTileExp, from the exponent field (no FP64 instruction)
+__device__ __forceinline__ bool below_min_scale(double F) {
+    return ((__double_as_longlong(F) >> 52) & 0x7ff) < 1023 + kMinTileExp;
+}
+
+// the bracket of a scale-free rotation on one tile
+__device__ __forceinline__ void tile_rot_sf(double2* tile, uint32_t tsize, const ExecOp& o, const RotSF& r) {
+    ExecOp e = o;
+    e.c[2] = (uint64_t)__double_as_longlong(r.v);
+    if (o.kind == EX_RY_P) {
+        if (r.cform) tile_pairs<PolF64, EX_RC>(tile, tsize >> 1, o.q0, e);
+        else tile_pairs<PolF64, EX_RT>(tile, tsize >> 1, o.q0, e);
+    } else {
+        if (r.cform) tile_pairs<PolF64, EX_RXC>(tile, tsize >> 1, o.q0, e);
+        else tile_pairs<PolF64, EX_RXT>(tile, tsize >> 1, o.q0, e);
+    }
+}
+
+__device__ __forceinline__ void tile_scale(double2* tile, uint32_t tsize, double F) {
+    for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
+        double2 a = tile[l];
+        a.x *= F;
+        a.y *= F;
+        tile[l] = a;
+    }
+}
+
+__device__ __forceinline__ bool is_rot_p(int kind) { return kind == EX_RX_P || kind == EX_RY_P; }
+
+// the weight of tile_grad_apply's sum: IEEE complex128 RZ sums only the q = 1 half (-2 x)
+template <class P>
+__device__ __forceinline__ double grad_weight(int kind) {
+    return (P::kPrecision == LLG_F64 && kind == EX_RZ_P) ? -2.0 : 1.0;
+}
+
+// ------------------------------------------------------------------------------------------
 // coefficient table: table[row][j] = (cos(theta/2), sin(theta/2)) packed for the precision; for an
 // RZ occurrence (cos theta, sin theta): RZ runs as diag(1, e^{i theta}) without its global phase
 // e^{-i theta/2}.  psi and lambda pick up the same phases through both sweeps, so energies
 // <psi|O|psi> and gradients Im <lambda|P|psi> are unchanged, and RZ costs one complex product on
-// half of the amplitudes instead of one on every amplitude.
+// half of the amplitudes instead of one on every amplitude.  In IEEE complex128 an RX / RY entry
+// holds the scale-free (v, f) instead, with its form byte in form[row][j].
 // ------------------------------------------------------------------------------------------
 template <class P>
 __device__ uint64_t pack_dev(double x) {
@@ -75,7 +143,8 @@ __device__ uint64_t pack_dev(double x) {
 template <class P>
 __global__ void k_coef_table(const double* __restrict__ params, int nparams, const int* __restrict__ occ_param, int nocc,
                              int rows, const int* __restrict__ row_set, const int* __restrict__ shift_occ,
-                             const double* __restrict__ shift_val, uint64_t* __restrict__ table) {
+                             const double* __restrict__ shift_val, uint64_t* __restrict__ table,
+                             uint8_t* __restrict__ form) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= rows * nocc) return;
     const int r = idx / nocc, j = idx % nocc;
@@ -85,8 +154,48 @@ __global__ void k_coef_table(const double* __restrict__ params, int nparams, con
     if (shift_occ && shift_occ[r] == j) theta += shift_val[r];
     double s, c;
     sincos((code & 1) ? theta : 0.5 * theta, &s, &c);
+    if (P::kPrecision == LLG_F64 && !(code & 1)) {  // RX / RY: the scale-free (v, f) and its form
+        const bool cform = fabs(s) > fabs(c);
+        table[2 * (size_t)idx] = pack_dev<P>(cform ? c / s : s / c);
+        table[2 * (size_t)idx + 1] = pack_dev<P>(cform ? s : c);
+        form[idx] = cform ? 1 : 0;
+        return;
+    }
     table[2 * (size_t)idx] = pack_dev<P>(c);
     table[2 * (size_t)idx + 1] = pack_dev<P>(s);
+    if (form) form[idx] = 0;
+}
+
+// A rotation's part of the gradient and its inverse on both tiles: Y (YDOT) accumulates
+// Re(conj(l1) p0) - Re(conj(l0) p1), X accumulates Im(conj(l0) p1) + Im(conj(l1) p0).  In IEEE
+// complex128 the subtracted terms enter one accumulator through negated multiply-add operands
+// (no separate FP64 subtraction).
+template <class P, int KIND, bool YDOT>
+__device__ __forceinline__ typename P::Acc grad_pairs(typename P::S* psi, typename P::S* lam, uint32_t tsize, uint32_t bit,
+                                                      const PairMath<P, KIND>& m) {
+    using C = typename P::C;
+    constexpr bool kOne = P::kPrecision == LLG_F64;
+    typename P::Acc pos = P::acc_zero(), neg = P::acc_zero();
+    for (uint32_t pp = threadIdx.x; pp < (tsize >> 1); pp += blockDim.x) {
+        const uint32_t j0 = ins0(pp, bit), j1 = j0 | bit;
+        C p0 = P::load(psi[j0]), p1 = P::load(psi[j1]), q0 = P::load(lam[j0]), q1 = P::load(lam[j1]);
+        if (YDOT) {
+            pos = P::acc_dot_re(pos, q1, p0);
+            if constexpr (kOne) pos = fma(-q0.re, p1.re, fma(-q0.im, p1.im, pos));
+            else neg = P::acc_dot_re(neg, q0, p1);
+        } else {
+            pos = P::acc_dot_im(pos, q0, p1);
+            pos = P::acc_dot_im(pos, q1, p0);
+        }
+        m.apply(p0, p1);
+        m.apply(q0, q1);
+        psi[j0] = P::store(p0);
+        psi[j1] = P::store(p1);
+        lam[j0] = P::store(q0);
+        lam[j1] = P::store(q1);
+    }
+    if constexpr (kOne) return pos;
+    else return YDOT ? acc_minus(pos, neg) : pos;
 }
 
 // One gradient op fused: this thread's part of Im <lambda | P | psi> from the amplitudes before the
@@ -95,7 +204,8 @@ __global__ void k_coef_table(const double* __restrict__ params, int nparams, con
 // result and provides the barrier before the next op.
 template <class P>
 __device__ typename P::Acc tile_grad_apply(typename P::S* psi, typename P::S* lam, uint32_t tsize, uint64_t base,
-                                           const ExecOp& o, const uint64_t* __restrict__ trow) {
+                                           const ExecOp& o, const uint64_t* __restrict__ trow,
+                                           const uint8_t* __restrict__ frow) {
     using K = typename P::K;
     using C = typename P::C;
     typename P::Acc pos = P::acc_zero(), neg = P::acc_zero();
@@ -106,6 +216,9 @@ __device__ typename P::Acc tile_grad_apply(typename P::S* psi, typename P::S* la
         const K ms0 = P::kneg(s0);
         if (o.flags & OPF_NONLOCAL_Q0) {
             const bool one = (base >> o.q0) & 1;
+            if constexpr (P::kPrecision == LLG_F64) {
+                if (!one) return pos;  // the q = 0 half: no contribution, no change (see below)
+            }
             for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
                 C p = P::load(psi[l]), q = P::load(lam[l]);
                 pos = P::acc_dot_im(pos, q, p);
@@ -116,9 +229,26 @@ __device__ typename P::Acc tile_grad_apply(typename P::S* psi, typename P::S* la
                     lam[l] = P::store(q);
                 }
             }
-            return one ? acc_minus(P::acc_zero(), pos) : pos;
+            if constexpr (P::kPrecision == LLG_F64) return pos;  // weighted -2 by the caller
+            else return one ? acc_minus(P::acc_zero(), pos) : pos;
         }
         const uint32_t bit = 1u << o.q0;
+        if constexpr (P::kPrecision == LLG_F64) {
+            // <lambda|psi> = <psi_N|O|psi_N> is real at every step of the reverse sweep (both
+            // vectors go through the same unitaries, O is a real diagonal), so summed over all
+            // tiles Im <lambda|Z|psi> = -2 sum_{q = 1} Im(conj(l) p): the q = 0 half is not read.
+            // The sum is returned unweighted; the caller applies grad_weight's -2.
+            for (uint32_t pp = threadIdx.x; pp < (tsize >> 1); pp += blockDim.x) {
+                const uint32_t j1 = ins0(pp, bit) | bit;
+                C p1 = P::load(psi[j1]), q1 = P::load(lam[j1]);
+                pos = P::acc_dot_im(pos, q1, p1);
+                cmul_const<P>(p1, c0, s0, ms0);
+                cmul_const<P>(q1, c0, s0, ms0);
+                psi[j1] = P::store(p1);
+                lam[j1] = P::store(q1);
+            }
+            return pos;
+        }
         for (uint32_t pp = threadIdx.x; pp < (tsize >> 1); pp += blockDim.x) {
             const uint32_t j0 = ins0(pp, bit), j1 = j0 | bit;
             const C p0 = P::load(psi[j0]), q0 = P::load(lam[j0]);
@@ -132,41 +262,28 @@ __device__ typename P::Acc tile_grad_apply(typename P::S* psi, typename P::S* la
         }
         return acc_minus(pos, neg);
     }
-    ExecOp r = o;  // RX / RY with the (possibly negated) sine of the table row
-    r.c[0] = trow[2 * o.q1];
     const uint32_t bit = 1u << o.q0;
-    if (o.kind == EX_RY_P) {
-        PairMath<P, EX_RY> m(r);
-        m.k[1] = s0;
-        for (uint32_t pp = threadIdx.x; pp < (tsize >> 1); pp += blockDim.x) {
-            const uint32_t j0 = ins0(pp, bit), j1 = j0 | bit;
-            C p0 = P::load(psi[j0]), p1 = P::load(psi[j1]), q0 = P::load(lam[j0]), q1 = P::load(lam[j1]);
-            pos = P::acc_dot_re(pos, q1, p0);  // Y: Re(conj(l1) p0) - Re(conj(l0) p1)
-            neg = P::acc_dot_re(neg, q0, p1);
-            m.apply(p0, p1);
-            m.apply(q0, q1);
-            psi[j0] = P::store(p0);
-            psi[j1] = P::store(p1);
-            lam[j0] = P::store(q0);
-            lam[j1] = P::store(q1);
-        }
+    if constexpr (P::kPrecision == LLG_F64) {  // the scale-free brackets (the caller carries f)
+        const RotSF rs = rot_sf(o, trow, frow);
+        ExecOp e = o;
+        e.c[2] = (uint64_t)__double_as_longlong(rs.v);
+        if (o.kind == EX_RY_P)
+            return rs.cform ? grad_pairs<P, EX_RC, true>(psi, lam, tsize, bit, PairMath<P, EX_RC>(e))
+                            : grad_pairs<P, EX_RT, true>(psi, lam, tsize, bit, PairMath<P, EX_RT>(e));
+        return rs.cform ? grad_pairs<P, EX_RXC, false>(psi, lam, tsize, bit, PairMath<P, EX_RXC>(e))
+                        : grad_pairs<P, EX_RXT, false>(psi, lam, tsize, bit, PairMath<P, EX_RXT>(e));
     } else {
+        ExecOp r = o;  // RX / RY with the (possibly negated) sine of the table row
+        r.c[0] = trow[2 * o.q1];
+        if (o.kind == EX_RY_P) {
+            PairMath<P, EX_RY> m(r);
+            m.k[1] = s0;
+            return grad_pairs<P, EX_RY, true>(psi, lam, tsize, bit, m);
+        }
         PairMath<P, EX_RX> m(r);
         m.k[1] = s0;
-        for (uint32_t pp = threadIdx.x; pp < (tsize >> 1); pp += blockDim.x) {
-            const uint32_t j0 = ins0(pp, bit), j1 = j0 | bit;
-            C p0 = P::load(psi[j0]), p1 = P::load(psi[j1]), q0 = P::load(lam[j0]), q1 = P::load(lam[j1]);
-            pos = P::acc_dot_im(pos, q0, p1);  // X: Im(conj(l0) p1) + Im(conj(l1) p0)
-            pos = P::acc_dot_im(pos, q1, p0);
-            m.apply(p0, p1);
-            m.apply(q0, q1);
-            psi[j0] = P::store(p0);
-            psi[j1] = P::store(p1);
-            lam[j0] = P::store(q0);
-            lam[j1] = P::store(q1);
-        }
+        return grad_pairs<P, EX_RX, false>(psi, lam, tsize, bit, m);
     }
-    return acc_minus(pos, neg);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -175,7 +292,7 @@ __device__ typename P::Acc tile_grad_apply(typename P::S* psi, typename P::S* la
 template <class P>
 __global__ void __launch_bounds__(512) k_tile_fwd(typename P::S* __restrict__ psi_all, int n, PassDesc pd,
                                                   const ExecOp* __restrict__ ops, const uint64_t* __restrict__ table,
-                                                  int nocc) {
+                                                  const uint8_t* __restrict__ form, int nocc) {
     using S = typename P::S;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int t = pd.t, low = pd.low;
@@ -185,6 +302,7 @@ __global__ void __launch_bounds__(512) k_tile_fwd(typename P::S* __restrict__ ps
     const uint64_t b = blockIdx.y;
     S* psi = psi_all + (b << n);
     const uint64_t* trow = table + b * (uint64_t)nocc * 2;
+    const uint8_t* frow = form + b * (uint64_t)nocc;
     const uint64_t base = insert0_mask((uint64_t)blockIdx.x, pd.local_mask);
     for (uint32_t h = threadIdx.x; h < nhi; h += blockDim.x) {
         uint64_t off = 0;
@@ -197,23 +315,46 @@ __global__ void __launch_bounds__(512) k_tile_fwd(typename P::S* __restrict__ ps
     for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) tile[l] = psi[base | hi_off[l >> low] | (l & lowmask)];
     __syncthreads();
     __shared__ __align__(16) ExecOp sops[kAdjOpChunk];
+    double F = 1.0;  // IEEE complex128: the tile holds the amplitudes divided by F
     for (int k = 0; k < pd.nops; ++k) {
         if (k % kAdjOpChunk == 0) {
             stage_ops(sops, ops, pd.op_begin + k, min(kAdjOpChunk, pd.nops - k));
             __syncthreads();
         }
-        tile_apply<P>(tile, tsize, base, sops[k % kAdjOpChunk], trow);
+        const ExecOp& o = sops[k % kAdjOpChunk];
+        if constexpr (P::kPrecision == LLG_F64) {
+            if (is_rot_p(o.kind)) {
+                const RotSF rs = rot_sf(o, trow, frow);
+                tile_rot_sf(tile, tsize, o, rs);
+                F *= rs.f;
+                __syncthreads();
+                if (below_min_scale(F)) {
+                    tile_scale(tile, tsize, F);
+                    F = 1.0;
+                    __syncthreads();
+                }
+                continue;
+            }
+        }
+        tile_apply<P>(tile, tsize, base, o, trow);
         __syncthreads();
     }
-    for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) psi[base | hi_off[l >> low] | (l & lowmask)] = tile[l];
+    for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
+        S a = tile[l];
+        if constexpr (P::kPrecision == LLG_F64) {
+            a.x *= F;
+            a.y *= F;
+        }
+        psi[base | hi_off[l >> low] | (l & lowmask)] = a;
+    }
 }
 
 // batched backward tile pass over psi and lambda; gpart[b][occ][tile]
 template <class P>
-__global__ void __launch_bounds__(512, 2) k_tile_bwd(typename P::S* __restrict__ psi_all, typename P::S* __restrict__ lam_all,
+__global__ void __maxnreg__(80) k_tile_bwd(typename P::S* __restrict__ psi_all, typename P::S* __restrict__ lam_all,
                                                   int n, PassDesc pd, const ExecOp* __restrict__ ops,
-                                                  const uint64_t* __restrict__ table, int nocc, double* __restrict__ gpart,
-                                                  int tiles) {
+                                                  const uint64_t* __restrict__ table, const uint8_t* __restrict__ form,
+                                                  int nocc, double* __restrict__ gpart, int tiles) {
     using S = typename P::S;
     using A = typename P::Acc;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -222,6 +363,7 @@ __global__ void __launch_bounds__(512, 2) k_tile_bwd(typename P::S* __restrict__
     // finished for up to kGradBuf ops at once, one thread per op (at most 512 threads, 16 warps).
     constexpr int kGradBuf = 32;
     __shared__ double gred[kGradBuf][16];  // per-warp parts, converted to IEEE double
+    __shared__ double gscale[kGradBuf];    // each buffered sum's weight (F^2 and grad_weight)
     __shared__ int gslot[kGradBuf];
     const int t = pd.t, low = pd.low;
     const uint32_t tsize = 1u << t, nhi = 1u << (t - low);
@@ -232,6 +374,7 @@ __global__ void __launch_bounds__(512, 2) k_tile_bwd(typename P::S* __restrict__
     S* psi = psi_all + (b << n);
     S* lam = lam_all + (b << n);
     const uint64_t* trow = table + b * (uint64_t)nocc * 2;
+    const uint8_t* frow = form + b * (uint64_t)nocc;
     const uint64_t base = insert0_mask((uint64_t)blockIdx.x, pd.local_mask);
     for (uint32_t h = threadIdx.x; h < nhi; h += blockDim.x) {
         uint64_t off = 0;
@@ -252,10 +395,11 @@ __global__ void __launch_bounds__(512, 2) k_tile_bwd(typename P::S* __restrict__
         if ((int)threadIdx.x < ng) {
             double sum = gred[threadIdx.x][0];
             for (int w = 1; w < (int)(blockDim.x >> 5); ++w) sum += gred[threadIdx.x][w];
-            gpart[((size_t)b * nocc + gslot[threadIdx.x]) * tiles + blockIdx.x] = sum;
+            gpart[((size_t)b * nocc + gslot[threadIdx.x]) * tiles + blockIdx.x] = sum * gscale[threadIdx.x];
         }
     };
     __shared__ __align__(16) ExecOp sops[kAdjOpChunk];
+    double F = 1.0;  // IEEE complex128: both tiles hold their amplitudes divided by F
     for (int k = 0; k < pd.nops; ++k) {
         if (k % kAdjOpChunk == 0) {
             stage_ops(sops, ops, pd.op_begin + k, min(kAdjOpChunk, pd.nops - k));
@@ -266,9 +410,15 @@ __global__ void __launch_bounds__(512, 2) k_tile_bwd(typename P::S* __restrict__
             // inner product and un-application in one loop.  The slot is read before the barrier:
             // once it is passed, the next chunk may be staged over this op's record.
             // the warp's sum in the accumulator's format, then IEEE double across warps and tiles
-            const double v = acc_value(warp_sum_acc(tile_grad_apply<P>(tp, tl, tsize, base, o, trow)));
+            const double v = acc_value(warp_sum_acc(tile_grad_apply<P>(tp, tl, tsize, base, o, trow, frow)));
             if ((threadIdx.x & 31) == 0) gred[ng][threadIdx.x >> 5] = v;
-            if (threadIdx.x == 0) gslot[ng] = o.q1;
+            if (threadIdx.x == 0) {
+                gslot[ng] = o.q1;
+                gscale[ng] = P::kPrecision == LLG_F64 ? grad_weight<P>(o.kind) * (F * F) : 1.0;  // F before the op
+            }
+            if constexpr (P::kPrecision == LLG_F64) {
+                if (is_rot_p(o.kind)) F *= rot_sf(o, trow, frow).f;
+            }
             ++ng;
             __syncthreads();  // the tile writes before the next op, the partials before a flush
             if (ng == kGradBuf) {
@@ -276,17 +426,32 @@ __global__ void __launch_bounds__(512, 2) k_tile_bwd(typename P::S* __restrict__
                 __syncthreads();  // the buffer is read before it is refilled
                 ng = 0;
             }
-            continue;
+        } else {
+            tile_apply<P>(tp, tsize, base, o, trow);
+            tile_apply<P>(tl, tsize, base, o, trow);
+            __syncthreads();
         }
-        tile_apply<P>(tp, tsize, base, o, trow);
-        tile_apply<P>(tl, tsize, base, o, trow);
-        __syncthreads();
+        if constexpr (P::kPrecision == LLG_F64) {
+            if (below_min_scale(F)) {  // uniform across the CTA; the last op ended in a barrier
+                tile_scale(tp, tsize, F);
+                tile_scale(tl, tsize, F);
+                F = 1.0;
+                __syncthreads();
+            }
+        }
     }
     flush();  // every op ended in a barrier, so the last partials are visible
     for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
         const uint64_t g = base | hi_off[l >> low] | (l & lowmask);
-        psi[g] = tp[l];
-        lam[g] = tl[l];
+        S a = tp[l], c = tl[l];
+        if constexpr (P::kPrecision == LLG_F64) {
+            a.x *= F;
+            a.y *= F;
+            c.x *= F;
+            c.y *= F;
+        }
+        psi[g] = a;
+        lam[g] = c;
     }
 }
 
@@ -339,9 +504,12 @@ __global__ void k_set_rows(typename P::S* psi, int n, int batch) {
 
 int threads_for(int t, int fixed) {
     if (fixed > 0) return fixed;
-    // 256 threads for 10+-qubit tiles: more CTAs per SM than 512 (measured 101k against 80k
-    // gradients/s on the 20-qubit, 400-parameter ansatz)
-    return t >= 10 ? 256 : (t >= 6 ? (1 << (t - 1)) : 32);
+    // 128 threads for 8+-qubit tiles.  The passes are bound by the FP64 pipe (complex128) or the
+    // FP32 pipe (double-float), which a few warps per scheduler keep busy; fewer threads per tile
+    // mean fewer warps per gradient reduction and per barrier (measured on the 20-qubit,
+    // 400-parameter ansatz, batch 64: 65.3k against 63.3k gradients/s at 256 threads in complex128,
+    // 155k against 151k in double-float; 512 threads were slower still)
+    return t >= 8 ? 128 : (t >= 6 ? (1 << (t - 1)) : 32);
 }
 
 }  // namespace
@@ -364,6 +532,7 @@ struct llg_adjoint {
     ExecOp* d_fwd_ops = nullptr;
     ExecOp* d_bwd_ops = nullptr;
     uint64_t* d_table = nullptr;
+    uint8_t* d_form = nullptr;  // IEEE complex128: the scale-free form of each RX / RY table entry
     int* d_occ_param = nullptr;
     int* d_csr_ptr = nullptr;
     int* d_csr_occ = nullptr;
@@ -448,7 +617,7 @@ int run_forward(llg_adjoint* h, int batch, bool make_lambda, const int* ckpt_eve
         const PassDesc& pd = h->fwd.passes[j];
         const dim3 grid((unsigned)(1ULL << (h->n - pd.t)), (unsigned)batch);
         k_tile_fwd<P><<<grid, threads_for(pd.t, h->threads), fwd_smem<P>(pd.t, pd.low), s>>>(
-            static_cast<typename P::S*>(h->d_psi), h->n, pd, h->d_fwd_ops, h->d_table, h->nocc);
+            static_cast<typename P::S*>(h->d_psi), h->n, pd, h->d_fwd_ops, h->d_table, h->d_form, h->nocc);
         ADJ_CUDA(cudaGetLastError(), "forward tile pass");
         if (C > 0 && (j + 1) % C == 0 && j + 1 < h->fwd.passes.size()) {
             const size_t m = (j + 1) / C - 1;
@@ -475,7 +644,7 @@ int run_backward(llg_adjoint* h, int batch, int C) {
         const dim3 grid((unsigned)(1ULL << (h->n - pd.t)), (unsigned)batch);
         k_tile_bwd<P><<<grid, threads_for(pd.t, h->threads), bwd_smem<P>(pd.t, pd.low), s>>>(
             static_cast<typename P::S*>(h->d_psi), static_cast<typename P::S*>(h->d_lam), h->n, pd, h->d_bwd_ops,
-            h->d_table, h->nocc, h->d_gpart, h->tiles);
+            h->d_table, h->d_form, h->nocc, h->d_gpart, h->tiles);
         ADJ_CUDA(cudaGetLastError(), "backward tile pass");
         // backward pass j undoes forward pass fj = np - 1 - j; psi is now the state after fj forward
         // passes; restart it from the checkpoint taken there, if any
@@ -501,17 +670,20 @@ int build_table(llg_adjoint* h, int rows, bool shifted) {
         case LLG_F64:
             k_coef_table<PolF64><<<blocks, 256, 0, h->stream>>>(h->d_params, h->nparams, h->d_occ_param, h->nocc, rows,
                                                                 shifted ? h->d_row_set : nullptr,
-                                                                shifted ? h->d_shift_occ : nullptr, h->d_shift_val, h->d_table);
+                                                                shifted ? h->d_shift_occ : nullptr, h->d_shift_val, h->d_table,
+                                                                h->d_form);
             break;
         case LLG_F32:
             k_coef_table<PolF32><<<blocks, 256, 0, h->stream>>>(h->d_params, h->nparams, h->d_occ_param, h->nocc, rows,
                                                                 shifted ? h->d_row_set : nullptr,
-                                                                shifted ? h->d_shift_occ : nullptr, h->d_shift_val, h->d_table);
+                                                                shifted ? h->d_shift_occ : nullptr, h->d_shift_val, h->d_table,
+                                                                h->d_form);
             break;
         default:
             k_coef_table<PolDF64><<<blocks, 256, 0, h->stream>>>(h->d_params, h->nparams, h->d_occ_param, h->nocc, rows,
                                                                  shifted ? h->d_row_set : nullptr,
-                                                                 shifted ? h->d_shift_occ : nullptr, h->d_shift_val, h->d_table);
+                                                                 shifted ? h->d_shift_occ : nullptr, h->d_shift_val, h->d_table,
+                                                                 h->d_form);
     }
     ADJ_CUDA(cudaGetLastError(), "coefficient table");
     return LLG_OK;
@@ -644,6 +816,7 @@ int llg_adjoint_create(int n, const llg_op* ops, int nops, int nparams, int max_
     if (!rc) rc = dmalloc(&h->d_fwd_ops, h->fwd.ops.size(), "ops");
     if (!rc) rc = dmalloc(&h->d_bwd_ops, h->bwd_ops.size(), "ops");
     if (!rc) rc = dmalloc(&h->d_table, (size_t)max_batch * h->nocc * 2, "coefficient table");
+    if (!rc) rc = dmalloc(&h->d_form, (size_t)max_batch * h->nocc, "coefficient table");
     if (!rc) rc = dmalloc(&h->d_occ_param, h->nocc, "occurrence map");
     if (!rc) rc = dmalloc(&h->d_csr_ptr, nparams + 1, "csr");
     if (!rc) rc = dmalloc(&h->d_csr_occ, h->nocc, "csr");
@@ -683,7 +856,7 @@ int llg_adjoint_create(int n, const llg_op* ops, int nops, int nparams, int max_
 int llg_adjoint_destroy(llg_adjoint* h) {
     if (!h) return LLG_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
-    void* ptrs[] = {h->d_psi, h->d_lam, h->d_fwd_ops, h->d_bwd_ops, h->d_table, h->d_occ_param, h->d_csr_ptr,
+    void* ptrs[] = {h->d_psi, h->d_lam, h->d_fwd_ops, h->d_bwd_ops, h->d_table, h->d_form, h->d_occ_param, h->d_csr_ptr,
                     h->d_csr_occ, h->d_params, h->d_gpart, h->d_epart, h->d_energy, h->d_grad, h->d_row_set,
                     h->d_shift_occ, h->d_shift_val, h->d_obs};
     for (void* p : ptrs)

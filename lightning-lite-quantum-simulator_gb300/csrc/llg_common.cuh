@@ -190,7 +190,7 @@ struct PolF64 {
     // the sign bit flipped on the integer pipe (the same bits as IEEE negation); a plain -x that is
     // not folded into a multiply-add runs on the FP64 pipe, this GPU's scarcest
     __device__ static R neg(R x) { return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL); }
-    __device__ static K kneg(K x) { return -x; }
+    __device__ static K kneg(K x) { return neg(x); }
     __device__ static R mulk(K a, R x) { return a * x; }
     __device__ static R zero() { return 0.0; }
     __device__ static Acc acc_zero() { return 0.0; }

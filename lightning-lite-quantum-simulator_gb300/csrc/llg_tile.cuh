@@ -275,7 +275,7 @@ __device__ void tile_apply(typename P::S* tile, uint32_t tsize, uint64_t base, c
         case EX_H: tile_pairs<P, EX_H>(tile, tsize >> 1, o.q0, o); break;
         case EX_X: tile_pairs<P, EX_X>(tile, tsize >> 1, o.q0, o); break;
         case EX_RX_P:
-        case EX_RY_P: {
+        case EX_RY_P: {  // (the adjoint kernels run IEEE complex128 occurrences in scale-free form)
             ExecOp r = o;
             r.c[0] = trow[2 * o.q1];
             const K s = P::k_from_bits(trow[2 * o.q1 + 1]);

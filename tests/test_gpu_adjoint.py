@@ -99,6 +99,32 @@ def test_mixed_circuit_adjoint_vs_oracle_and_gpu_parameter_shift():
     adj.close()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "df64"])
+def test_long_rotation_pass_rescales(precision):
+    """720 parametrised RX / RY in one tile pass, angles near pi/2 and 3pi/2 (both tangent and
+    cotangent forms, either sign): the IEEE complex128 kernels' running factor of dropped cosines
+    falls below 2^-300 and the tiles are rescaled in place, in the forward and the reverse sweep."""
+    rng = np.random.default_rng(31)
+    n, nrot = 5, 720
+    recs = []
+    for k in range(nrot):
+        recs.append(((OP_RX, OP_RY)[k % 2], int(rng.integers(n)), 0, 0.0, None, None, k))
+        if k % 9 == 8:
+            a, b = rng.choice(n, 2, replace=False)
+            recs.append(((OP_CNOT, OP_CZ)[k % 2], int(a), int(b)))
+    ops = make_ops(recs)
+    params = np.where(rng.random((2, nrot)) < 0.5, np.pi / 2, -1.5 * np.pi) + rng.uniform(-0.1, 0.1, (2, nrot))
+    obs = ([0, 1, 2], [1, -1, 4], [1.0, -0.5, 0.75])
+    adj = llgpu.Adjoint(n, ops, nrot, obs, max_batch=2, precision=precision)
+    assert adj.info()["forward_passes"] == 1
+    e, gr = adj.run(params)
+    for b in range(2):
+        e_o, g_o = oracle.param_shift(n, ops, params[b], *obs)
+        assert abs(e[b] - e_o) <= 1e-10
+        assert np.max(np.abs(gr[b] - g_o)) <= 1e-10
+    adj.close()
+
+
 def test_checkpointed_reverse_sweep_agrees():
     rng = np.random.default_rng(4)
     n = 16
