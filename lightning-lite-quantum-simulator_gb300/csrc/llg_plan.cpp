@@ -1232,6 +1232,7 @@ bool lower_stream_f64(int n, const llg_op* ops, int nops, std::vector<ExecOp>& o
     cd w(1.0, 0.0);      // carried global phase (from RZ)
     int last_real = -1;  // index in out of the last scale-free op (absorbs r)
     int last_phase = -1; // index in out of the last EX_PHASE1 (absorbs w)
+    int phase_q0 = -1;   // index in out of an EX_PHASE1 on qubit 0 (absorbs w first, see below)
     int last_u2 = -1;    // index in out of a generic 2x2 (absorbs r w for free)
     int last_zyz = -1;   // index in out of the last EX_ZTZ / EX_ZCZ (or the EX_ZYZ it became)
     // the scale-free op at index i rewritten as its full form times the real factor g
@@ -1309,6 +1310,7 @@ bool lower_stream_f64(int n, const llg_op* ops, int nops, std::vector<ExecOp>& o
                 e.c[0] = pack_coef(PP, p.real());
                 e.c[1] = pack_coef(PP, p.imag());
                 last_phase = (int)out.size();
+                if (op.q0 == 0) phase_q0 = last_phase;
                 out.push_back(e);
                 break;
             }
@@ -1388,7 +1390,10 @@ bool lower_stream_f64(int n, const llg_op* ops, int nops, std::vector<ExecOp>& o
             err = "stream lowering: a carried phase without a phase op";
             return false;
         }
-        ExecOp& e = out[last_phase];  // w diag(1, p) = diag(w, w p) over the whole state
+        // w diag(1, p) = diag(w, w p) over the whole state.  A phase on qubit 0 takes it when there
+        // is one: its |1> amplitudes share every 32-byte sector with |0> ones, so its half-state
+        // pass already moves the whole state, and the other phases keep their half-state passes.
+        ExecOp& e = out[phase_q0 >= 0 ? phase_q0 : last_phase];
         const cd p(coef_value(e.c[0]), coef_value(e.c[1]));
         const cd d1 = w * p;
         e.kind = EX_DIAG;

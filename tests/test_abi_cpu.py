@@ -398,6 +398,23 @@ def test_stream_lowering_reproduces_the_oracle(built):
         assert kinds[0] == 1 and kinds[1] + kinds[2] + kinds[3] + kinds[5] + kinds[11] == 0
 
 
+def test_stream_lowering_phase_on_qubit_0_takes_the_global_phase(built):
+    # five RZs: the one on qubit 0 (whose half-state pass moves every sector anyway) becomes the
+    # whole-state diagonal, the others stay half-state phases
+    n = 8
+    rng = np.random.default_rng(5)
+    psi0 = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    psi0 /= np.linalg.norm(psi0)
+    for targets in ((0, 3, 5, 6, 7), (4, 0, 7), (3, 5, 7)):
+        ops = make_ops([(OP_RZ, q, 0, 0.3 + 0.4 * q) for q in targets])
+        passes, xops = llgpu.plan_export(n, ops, n, stream=True)
+        kinds = xops["kind"].tolist()
+        diag = [int(xops["q0"][i]) for i, k in enumerate(kinds) if k == 5]  # EX_DIAG
+        assert kinds.count(13) == len(targets) - 1 and diag == [0 if 0 in targets else targets[-1]]
+        got = execute(psi0, n, passes, xops)
+        assert np.max(np.abs(got - oracle.run_ops(n, ops, psi0.copy()))) < 1e-12
+
+
 def test_stream_lowering_absorbs_before_the_floor(built):
     # 700 rotations at |cos| = |sin| = 2^-1/2 shrink the carried factor to 2^-350: it is absorbed
     # before 2^-300 and once at the end
