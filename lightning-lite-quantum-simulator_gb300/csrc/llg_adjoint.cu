@@ -58,62 +58,81 @@ constexpr int kThreads = 256;
 constexpr int kEBlocksPerState = 64;
 
 // ------------------------------------------------------------------------------------------
-// IEEE complex128: parametrised RX / RY in scale-free form.  This GPU retires 2 FP64
-// multiply-adds per clock per SM, and the pair passes of these kernels are bound by that pipe.
-// The table row of an RX / RY occurrence holds (v, f) and a form byte: form 0 (|sin| <= |cos|)
-// v = tan(theta/2), f = cos(theta/2), and the rotation is f [1, -v; v, 1] (RY) or
-// f [1, -iv; -iv, 1] (RX); form 1 v = cot(theta/2), f = sin(theta/2), and it is f [v, -1; 1, v]
-// or f [v, -i; -i, v].  The tile applies the bracket, one multiply-add per real component instead
-// of two, and the kernel multiplies f into the tile's running factor F: the tile holds the
-// amplitudes divided by F, and its store multiplies F back in, so states between passes (and
-// checkpoints) are exact-scaled.  The inverse negates v, and in form 1 f too
+// Parametrised RX / RY in scale-free form (IEEE complex128 and double-float).  The FP64 passes
+// are bound by this GPU's FP64 pipe (2 multiply-adds per clock per SM), the double-float ones by
+// instruction issue.  The table row of an RX / RY occurrence holds (v, f) and a form byte: form 0
+// (|sin| <= |cos|) v = tan(theta/2), f = cos(theta/2), and the rotation is f [1, -v; v, 1] (RY)
+// or f [1, -iv; -iv, 1] (RX); form 1 v = cot(theta/2), f = sin(theta/2), and it is
+// f [v, -1; 1, v] or f [v, -i; -i, v].  v is packed in the state's format, f is an IEEE double.
+// The tile applies the bracket, one multiply-add per real component instead of two, and the
+// kernel multiplies f into the tile's running factor F (a double): the tile holds the amplitudes
+// divided by F, and its store multiplies F back in, so states between passes (and checkpoints)
+// are exact-scaled.  The inverse negates v, and in form 1 f too
 // (RY(-theta) = (-s) [-u, -1; 1, -u]).  An inner product of psi and lambda tiles, which share F,
-// is F^2 times that of the stored values.  |f| >= 1/sqrt(2), so |F| falls below 2^kMinTileExp
-// only after some 600 rotations in one pass; the tile is then rescaled in place.
+// is F^2 times that of the stored values.  |f| >= 1/sqrt(2); when |F| falls below 2^kMinExp
+// (2^-300 in FP64; 2^-40 in double-float, whose floats reach 2^-126) the tiles are rescaled in
+// place.  complex64 keeps the full forms.
 // ------------------------------------------------------------------------------------------
-constexpr int kMinTileExp = -300;
+template <class P>
+constexpr bool kScaleFree = P::kPrecision == LLG_F64 || P::kPrecision == LLG_DF64;
+
+template <class P>
+constexpr int kMinExp = P::kPrecision == LLG_F64 ? -300 : -40;
 
 struct RotSF {
-    double v, f;
+    uint64_t v;  // packed in the state's format
+    double f;
     bool cform;
 };
 
-// (negations flip the sign bit on the integer pipe)
+// (negations flip sign bits on the integer pipe)
+template <class P>
 __device__ __forceinline__ RotSF rot_sf(const ExecOp& o, const uint64_t* __restrict__ trow, const uint8_t* __restrict__ frow) {
     constexpr uint64_t kSign = 0x8000000000000000ULL;
+    constexpr uint64_t kSignV = P::kPrecision == LLG_F64 ? kSign : 0x8000000080000000ULL;  // double-float: hi and lo
     RotSF r;
     r.cform = frow[o.q1] != 0;
     const bool inv = (o.flags & OPF_ADJOINT) != 0;
-    r.v = __longlong_as_double((long long)(trow[2 * o.q1] ^ (inv ? kSign : 0)));
+    r.v = trow[2 * o.q1] ^ (inv ? kSignV : 0);
     r.f = __longlong_as_double((long long)(trow[2 * o.q1 + 1] ^ (inv && r.cform ? kSign : 0)));
     return r;
 }
 
-// |F| < 2^kMinTileExp, from the exponent field (no FP64 instruction)
+// |F| < 2^kMinExp, from the exponent field (no FP64 instruction)
+template <class P>
 __device__ __forceinline__ bool below_min_scale(double F) {
-    return ((__double_as_longlong(F) >> 52) & 0x7ff) < 1023 + kMinTileExp;
+    return ((__double_as_longlong(F) >> 52) & 0x7ff) < 1023 + kMinExp<P>;
 }
 
 // the bracket of a scale-free rotation on one tile
-__device__ __forceinline__ void tile_rot_sf(double2* tile, uint32_t tsize, const ExecOp& o, const RotSF& r) {
+template <class P>
+__device__ __forceinline__ void tile_rot_sf(typename P::S* tile, uint32_t tsize, const ExecOp& o, const RotSF& r) {
     ExecOp e = o;
-    e.c[2] = (uint64_t)__double_as_longlong(r.v);
+    e.c[2] = r.v;
     if (o.kind == EX_RY_P) {
-        if (r.cform) tile_pairs<PolF64, EX_RC>(tile, tsize >> 1, o.q0, e);
-        else tile_pairs<PolF64, EX_RT>(tile, tsize >> 1, o.q0, e);
+        if (r.cform) tile_pairs<P, EX_RC>(tile, tsize >> 1, o.q0, e);
+        else tile_pairs<P, EX_RT>(tile, tsize >> 1, o.q0, e);
     } else {
-        if (r.cform) tile_pairs<PolF64, EX_RXC>(tile, tsize >> 1, o.q0, e);
-        else tile_pairs<PolF64, EX_RXT>(tile, tsize >> 1, o.q0, e);
+        if (r.cform) tile_pairs<P, EX_RXC>(tile, tsize >> 1, o.q0, e);
+        else tile_pairs<P, EX_RXT>(tile, tsize >> 1, o.q0, e);
     }
 }
 
-__device__ __forceinline__ void tile_scale(double2* tile, uint32_t tsize, double F) {
-    for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
-        double2 a = tile[l];
-        a.x *= F;
-        a.y *= F;
-        tile[l] = a;
-    }
+// F != 1 from its bits (no FP64 instruction)
+__device__ __forceinline__ bool is_not_one(double F) { return __double_as_longlong(F) != 0x3FF0000000000000LL; }
+
+template <class P>
+__device__ __forceinline__ typename P::S scaled(typename P::S x, double F) {
+    const typename P::K k = P::k_from_double(F);
+    typename P::C a = P::load(x);
+    a.re = P::mulk(k, a.re);
+    a.im = P::mulk(k, a.im);
+    return P::store(a);
+}
+
+template <class P>
+__device__ __forceinline__ void tile_scale(typename P::S* tile, uint32_t tsize, double F) {
+    for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) tile[l] = scaled<P>(tile[l], F);
 }
 
 __device__ __forceinline__ bool is_rot_p(int kind) { return kind == EX_RX_P || kind == EX_RY_P; }
@@ -129,8 +148,8 @@ __device__ __forceinline__ double grad_weight(int kind) {
 // RZ occurrence (cos theta, sin theta): RZ runs as diag(1, e^{i theta}) without its global phase
 // e^{-i theta/2}.  psi and lambda pick up the same phases through both sweeps, so energies
 // <psi|O|psi> and gradients Im <lambda|P|psi> are unchanged, and RZ costs one complex product on
-// half of the amplitudes instead of one on every amplitude.  In IEEE complex128 an RX / RY entry
-// holds the scale-free (v, f) instead, with its form byte in form[row][j].
+// half of the amplitudes instead of one on every amplitude.  In IEEE complex128 and double-float
+// an RX / RY entry holds the scale-free (v, f) instead, with its form byte in form[row][j].
 // ------------------------------------------------------------------------------------------
 template <class P>
 __device__ uint64_t pack_dev(double x) {
@@ -154,10 +173,10 @@ __global__ void k_coef_table(const double* __restrict__ params, int nparams, con
     if (shift_occ && shift_occ[r] == j) theta += shift_val[r];
     double s, c;
     sincos((code & 1) ? theta : 0.5 * theta, &s, &c);
-    if (P::kPrecision == LLG_F64 && !(code & 1)) {  // RX / RY: the scale-free (v, f) and its form
+    if (kScaleFree<P> && !(code & 1)) {  // RX / RY: the scale-free (v, f) and its form
         const bool cform = fabs(s) > fabs(c);
         table[2 * (size_t)idx] = pack_dev<P>(cform ? c / s : s / c);
-        table[2 * (size_t)idx + 1] = pack_dev<P>(cform ? s : c);
+        table[2 * (size_t)idx + 1] = (uint64_t)__double_as_longlong(cform ? s : c);  // f stays a double
         form[idx] = cform ? 1 : 0;
         return;
     }
@@ -263,10 +282,10 @@ __device__ typename P::Acc tile_grad_apply(typename P::S* psi, typename P::S* la
         return acc_minus(pos, neg);
     }
     const uint32_t bit = 1u << o.q0;
-    if constexpr (P::kPrecision == LLG_F64) {  // the scale-free brackets (the caller carries f)
-        const RotSF rs = rot_sf(o, trow, frow);
+    if constexpr (kScaleFree<P>) {  // the scale-free brackets (the caller carries f)
+        const RotSF rs = rot_sf<P>(o, trow, frow);
         ExecOp e = o;
-        e.c[2] = (uint64_t)__double_as_longlong(rs.v);
+        e.c[2] = rs.v;
         if (o.kind == EX_RY_P)
             return rs.cform ? grad_pairs<P, EX_RC, true>(psi, lam, tsize, bit, PairMath<P, EX_RC>(e))
                             : grad_pairs<P, EX_RT, true>(psi, lam, tsize, bit, PairMath<P, EX_RT>(e));
@@ -315,21 +334,21 @@ __global__ void __launch_bounds__(512) k_tile_fwd(typename P::S* __restrict__ ps
     for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) tile[l] = psi[base | hi_off[l >> low] | (l & lowmask)];
     __syncthreads();
     __shared__ __align__(16) ExecOp sops[kAdjOpChunk];
-    double F = 1.0;  // IEEE complex128: the tile holds the amplitudes divided by F
+    double F = 1.0;  // scale-free formats: the tile holds the amplitudes divided by F
     for (int k = 0; k < pd.nops; ++k) {
         if (k % kAdjOpChunk == 0) {
             stage_ops(sops, ops, pd.op_begin + k, min(kAdjOpChunk, pd.nops - k));
             __syncthreads();
         }
         const ExecOp& o = sops[k % kAdjOpChunk];
-        if constexpr (P::kPrecision == LLG_F64) {
+        if constexpr (kScaleFree<P>) {
             if (is_rot_p(o.kind)) {
-                const RotSF rs = rot_sf(o, trow, frow);
-                tile_rot_sf(tile, tsize, o, rs);
+                const RotSF rs = rot_sf<P>(o, trow, frow);
+                tile_rot_sf<P>(tile, tsize, o, rs);
                 F *= rs.f;
                 __syncthreads();
-                if (below_min_scale(F)) {
-                    tile_scale(tile, tsize, F);
+                if (below_min_scale<P>(F)) {
+                    tile_scale<P>(tile, tsize, F);
                     F = 1.0;
                     __syncthreads();
                 }
@@ -339,12 +358,10 @@ __global__ void __launch_bounds__(512) k_tile_fwd(typename P::S* __restrict__ ps
         tile_apply<P>(tile, tsize, base, o, trow);
         __syncthreads();
     }
+    const bool rescale = kScaleFree<P> && is_not_one(F);  // uniform across the CTA
     for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
         S a = tile[l];
-        if constexpr (P::kPrecision == LLG_F64) {
-            a.x *= F;
-            a.y *= F;
-        }
+        if (rescale) a = scaled<P>(a, F);
         psi[base | hi_off[l >> low] | (l & lowmask)] = a;
     }
 }
@@ -399,7 +416,7 @@ __global__ void __maxnreg__(80) k_tile_bwd(typename P::S* __restrict__ psi_all, 
         }
     };
     __shared__ __align__(16) ExecOp sops[kAdjOpChunk];
-    double F = 1.0;  // IEEE complex128: both tiles hold their amplitudes divided by F
+    double F = 1.0;  // scale-free formats: both tiles hold their amplitudes divided by F
     for (int k = 0; k < pd.nops; ++k) {
         if (k % kAdjOpChunk == 0) {
             stage_ops(sops, ops, pd.op_begin + k, min(kAdjOpChunk, pd.nops - k));
@@ -414,10 +431,10 @@ __global__ void __maxnreg__(80) k_tile_bwd(typename P::S* __restrict__ psi_all, 
             if ((threadIdx.x & 31) == 0) gred[ng][threadIdx.x >> 5] = v;
             if (threadIdx.x == 0) {
                 gslot[ng] = o.q1;
-                gscale[ng] = P::kPrecision == LLG_F64 ? grad_weight<P>(o.kind) * (F * F) : 1.0;  // F before the op
+                gscale[ng] = kScaleFree<P> ? grad_weight<P>(o.kind) * (F * F) : 1.0;  // F before the op
             }
-            if constexpr (P::kPrecision == LLG_F64) {
-                if (is_rot_p(o.kind)) F *= rot_sf(o, trow, frow).f;
+            if constexpr (kScaleFree<P>) {
+                if (is_rot_p(o.kind)) F *= rot_sf<P>(o, trow, frow).f;
             }
             ++ng;
             __syncthreads();  // the tile writes before the next op, the partials before a flush
@@ -431,24 +448,23 @@ __global__ void __maxnreg__(80) k_tile_bwd(typename P::S* __restrict__ psi_all, 
             tile_apply<P>(tl, tsize, base, o, trow);
             __syncthreads();
         }
-        if constexpr (P::kPrecision == LLG_F64) {
-            if (below_min_scale(F)) {  // uniform across the CTA; the last op ended in a barrier
-                tile_scale(tp, tsize, F);
-                tile_scale(tl, tsize, F);
+        if constexpr (kScaleFree<P>) {
+            if (below_min_scale<P>(F)) {  // uniform across the CTA; the last op ended in a barrier
+                tile_scale<P>(tp, tsize, F);
+                tile_scale<P>(tl, tsize, F);
                 F = 1.0;
                 __syncthreads();
             }
         }
     }
     flush();  // every op ended in a barrier, so the last partials are visible
+    const bool rescale = kScaleFree<P> && is_not_one(F);  // uniform across the CTA
     for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
         const uint64_t g = base | hi_off[l >> low] | (l & lowmask);
         S a = tp[l], c = tl[l];
-        if constexpr (P::kPrecision == LLG_F64) {
-            a.x *= F;
-            a.y *= F;
-            c.x *= F;
-            c.y *= F;
+        if (rescale) {
+            a = scaled<P>(a, F);
+            c = scaled<P>(c, F);
         }
         psi[g] = a;
         lam[g] = c;
