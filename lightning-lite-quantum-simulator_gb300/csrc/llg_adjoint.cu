@@ -54,7 +54,6 @@ __device__ __forceinline__ void stage_ops(ExecOp* sops, const ExecOp* __restrict
     const uint4* src = reinterpret_cast<const uint4*>(ops + first);
     for (int w = threadIdx.x; w < cnt * kWords; w += blockDim.x) reinterpret_cast<uint4*>(sops)[w] = src[w];
 }
-constexpr int kThreads = 256;
 constexpr int kEBlocksPerState = 64;
 
 // ------------------------------------------------------------------------------------------
@@ -67,7 +66,7 @@ constexpr int kEBlocksPerState = 64;
 // The tile applies the bracket, one multiply-add per real component instead of two, and the
 // kernel multiplies f into the tile's running factor F (a double): the tile holds the amplitudes
 // divided by F, and its store multiplies F back in, so states between passes (and checkpoints)
-// are exact-scaled.  The inverse negates v, and in form 1 f too
+// are at their true scale.  The inverse negates v, and in form 1 f too
 // (RY(-theta) = (-s) [-u, -1; 1, -u]).  An inner product of psi and lambda tiles, which share F,
 // is F^2 times that of the stored values.  |f| >= 1/sqrt(2); when |F| falls below 2^kMinExp
 // (2^-300 in FP64; 2^-40 in double-float, whose floats reach 2^-126) the tiles are rescaled in
