@@ -266,19 +266,20 @@ __device__ typename P::Acc tile_grad_apply(typename P::S* psi, typename P::S* la
                 lam[j1] = P::store(q1);
             }
             return pos;
+        } else {
+            for (uint32_t pp = threadIdx.x; pp < (tsize >> 1); pp += blockDim.x) {
+                const uint32_t j0 = ins0(pp, bit), j1 = j0 | bit;
+                const C p0 = P::load(psi[j0]), q0 = P::load(lam[j0]);
+                C p1 = P::load(psi[j1]), q1 = P::load(lam[j1]);
+                pos = P::acc_dot_im(pos, q0, p0);
+                neg = P::acc_dot_im(neg, q1, p1);
+                cmul_const<P>(p1, c0, s0, ms0);
+                cmul_const<P>(q1, c0, s0, ms0);
+                psi[j1] = P::store(p1);
+                lam[j1] = P::store(q1);
+            }
+            return acc_minus(pos, neg);
         }
-        for (uint32_t pp = threadIdx.x; pp < (tsize >> 1); pp += blockDim.x) {
-            const uint32_t j0 = ins0(pp, bit), j1 = j0 | bit;
-            const C p0 = P::load(psi[j0]), q0 = P::load(lam[j0]);
-            C p1 = P::load(psi[j1]), q1 = P::load(lam[j1]);
-            pos = P::acc_dot_im(pos, q0, p0);
-            neg = P::acc_dot_im(neg, q1, p1);
-            cmul_const<P>(p1, c0, s0, ms0);
-            cmul_const<P>(q1, c0, s0, ms0);
-            psi[j1] = P::store(p1);
-            lam[j1] = P::store(q1);
-        }
-        return acc_minus(pos, neg);
     }
     const uint32_t bit = 1u << o.q0;
     if constexpr (kScaleFree<P>) {  // the scale-free brackets (the caller carries f)
