@@ -152,8 +152,21 @@ struct Decision {
     // product formed once in double so that a site pair costs one multiply per real instead of two
     uint64_t g0, g1;
     int ad_jump, pd_jump;
+    // IEEE complex128 without a jump: the |0> amplitudes' factor f_ad0 f_pd0 sig is carried
+    // (sig_next) instead of applied, and only the |1> amplitudes are scaled, by
+    // g1 = f_ad1 f_pd1 / (f_ad0 f_pd0) = sqrt(1 - gamma) sqrt(1 - lambda): one multiply per real of
+    // half of the state instead of one per real of all of it
+    int carry;
+    double sig_next;  // the held state's factor after the pair (1 unless carry)
     double p1;
 };
+
+// |x| < 2^-300 or |x| >= 2^300 (x not 0), from the exponent field: no FP64 instruction in the
+// per-gate path
+__device__ __forceinline__ bool outside_2pow300(double x) {
+    const int e = (int)((__double_as_longlong(x) >> 52) & 0x7ff) - 1023;
+    return e < -300 || e >= 300;
+}
 
 // barrier for the trajectory's CTA group
 template <int CL>
@@ -434,6 +447,19 @@ struct Traj {
             r.im = P::zero();
             return r;
         };
+        if (d->carry) {  // no jump, the |0> factor carried: the |1> amplitudes times g1
+            if (!cross(q)) {
+                const uint32_t bit = 1u << q;
+                for (uint32_t p = threadIdx.x; p < (NL >> 1); p += blockDim.x) {
+                    const uint32_t j1 = ins0(p, bit) | bit;
+                    s[j1] = P::store(scale(P::load(s[j1]), g1));
+                }
+            } else if (rank == 1) {  // the cluster's bit-1 half; nothing read across the cluster
+                for (uint32_t l = threadIdx.x; l < NL; l += blockDim.x) s[l] = P::store(scale(P::load(s[l]), g1));
+            }
+            __syncthreads();
+            return;
+        }
         if (!cross(q)) {
             const uint32_t bit = 1u << q;
             for (uint32_t p = threadIdx.x; p < (NL >> 1); p += blockDim.x) {
@@ -485,7 +511,7 @@ template <class P>
 // site); P1_held is the held state's P(1), so the true one is sig^2 P1_held, and the factors that
 // renormalise the held amplitudes carry sig.
 __device__ void decide(double P1_held, double sig, const KrausParams& kp, double u1, double u2, Decision* d,
-                       double* min_margin) {
+                       double* min_margin, bool carry_ok) {
     const double P1 = sig == 1.0 ? P1_held : sig * sig * P1_held;
     // amplitude damping
     double s_ad = 1.0 - kp.gamma * P1;
@@ -520,9 +546,18 @@ __device__ void decide(double P1_held, double sig, const KrausParams& kp, double
         fp0 = s0;
         fp1 = kp.sq1ml * s0;
     }
+    d->p1 = p1;
+    if (carry_ok && !d->ad_jump && !d->pd_jump) {
+        d->carry = 1;
+        d->sig_next = fa0 * fp0 * sig;
+        d->g0 = packk<P>(1.0);
+        d->g1 = packk<P>(kp.sq1mg * kp.sq1ml);
+        return;
+    }
+    d->carry = 0;
+    d->sig_next = 1.0;
     d->g0 = packk<P>(fa0 * fp0 * sig);
     d->g1 = packk<P>(fa1 * fp1 * sig);
-    d->p1 = p1;
 }
 
 template <class P, int CL>
@@ -586,13 +621,14 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
             const TrajGate& G = gates[g];
             T.gate(G.op);
             sig *= G.f;
+            // the held state is rescaled before it could leave the FP64 range (2^300 away from
+            // its true size): scale-free rotations shrink sig, carried Kraus factors grow it
+            if (outside_2pow300(sig)) {
+                T.rescale(sig);
+                sig = 1.0;
+            }
             if (kp.mode == NOISE_DEPOL) {
-                // unitary sites: the factor is carried to the observable; the held state is
-                // rescaled before it could leave the FP64 range (2^300 above its true size)
-                if (fabs(sig) < 0x1p-300) {
-                    T.rescale(sig);
-                    sig = 1.0;
-                }
+                // unitary sites: the factor is carried to the observable
                 // decisions do not depend on the state: every thread draws the same uniforms, so
                 // the branch is uniform and needs no broadcast
                 if (!(kp.gamma > 0.0)) continue;
@@ -618,9 +654,10 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
                 if (site + 1 >= u_end) draw(site);  // AD and PD uniforms of this pair in one chunk
                 const double P1 = T.reduce(q, false, part2);
                 if (threadIdx.x == 0)
-                    decide<P>(P1, sig, kp, uni[site - u_begin], uni[site + 1 - u_begin], &dec, &min_margin);
-                sig = 1.0;  // the Kraus pass below stores the true, renormalised state
+                    decide<P>(P1, sig, kp, uni[site - u_begin], uni[site + 1 - u_begin], &dec, &min_margin,
+                              P::kPrecision == LLG_F64);
                 __syncthreads();
+                sig = dec.sig_next;  // 1: the Kraus pass below stores the true, renormalised state
                 const int code = dec.ad_jump | (dec.pd_jump << 1);
                 T.kraus_apply(q, &dec);
                 if (threadIdx.x == 0 && T.rank == 0 && jump_log)
@@ -630,7 +667,7 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
             }
         }
         double z = ob.nterms > 0 ? T.observable(ob, part2) : T.reduce(0, true, part2);
-        if (sig != 1.0) z *= sig * sig;  // a scale-free rotation with no site after it
+        if (sig != 1.0) z *= sig * sig;  // factors carried past the last site
         if (threadIdx.x == 0 && T.rank == 0) {
             z0_out[tt] = z;
             if (jumps_out) jumps_out[tt] = jumps;
