@@ -87,12 +87,14 @@ def test_non_unitary_block_and_high_qubits():
 
 
 @pytest.mark.parametrize("precision", ["df64", "fp64"])
-@pytest.mark.parametrize("n,k", [(12, 5), (14, 5), (11, 4), (13, 4), (10, 3), (12, 3)])
+@pytest.mark.parametrize("n,k", [(12, 5), (14, 5), (11, 4), (13, 4), (10, 3), (12, 3), (10, 2), (13, 2)])
 def test_tensor_core_block_edge_values(precision, n, k):
-    # 4- and 5-qubit blocks on double-float states, and 3- and 4-qubit blocks on IEEE complex128
+    # 4- and 5-qubit blocks on double-float states, and 3- to 5-qubit blocks on IEEE complex128
     # states, of k + 7 or more qubits run on the tensor cores (exact 8-bit slices against a scale
-    # per group of 2^k amplitudes: six for double-float, eight for FP64): zero groups, tiny groups,
-    # 20 orders of magnitude inside one group, a non-unitary matrix with large entries and a zero row
+    # per group of 2^k amplitudes: six for double-float, eight for FP64); an IEEE complex128 2-qubit
+    # block runs there as a 3-qubit one with the identity on another qubit: zero groups, tiny
+    # groups, 20 orders of magnitude inside one group, a non-unitary matrix with large entries and
+    # a zero row
     rng = np.random.default_rng(40 + n + k)
     psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
     qs = [0, 3, n - 5, n - 2, n - 1][5 - k:]
@@ -103,12 +105,12 @@ def test_tensor_core_block_edge_values(precision, n, k):
     psi[[free[0] | o for o in offs]] = 0.0                       # an all-zero group
     psi[[free[1] | o for o in offs]] *= 1e-25                    # a tiny group
     psi[[free[2] | o for o in offs[1:]]] *= 1e-20                # one large amplitude, the rest tiny
-    psi[free[3] | offs[5]] = 3.0 - 4.0j
+    psi[free[3] | offs[min(5, d - 1)]] = 3.0 - 4.0j
     st = llgpu.State(n, precision)
     st.load(psi)
     want = psi.copy()
     m = (rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))) * 4.0
-    m[7, :] = 0.0
+    m[min(7, d - 1), :] = 0.0
     m[:, min(9, d - 2)] *= 1e-12
     st.apply_matrix(qs, m)
     oracle.apply_matrix(want, n, qs, m)
