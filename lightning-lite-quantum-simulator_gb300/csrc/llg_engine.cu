@@ -672,25 +672,26 @@ int llg_apply_matrix(llg_state* st, int k, const int* qubits, const double* m) {
         return traced(st, LLG_PROF_GATE, 1, "block kernel (sparse)",
                       [&] { return launch_block_sparse(st->P, st->d_psi, st->n, bd, st->d_block, nz, st->stream); });
     }
-    // An IEEE complex128 2-qubit block runs as a 3-qubit one, M on its qubits and the identity on
-    // the lowest other qubit, on the tensor cores: their exact products beat the FP64 pipe's
-    // 2-qubit form (17 against 28 ms at 30 qubits)
-    double m3[2 * 8 * 8];
-    if (st->P == LLG_F64 && k == 2 && block_tc_eligible(LLG_F64, st->n, 3)) {
+    // An IEEE complex128 2-qubit block runs as a 3-qubit one, and a double-float 3-qubit block as
+    // a 4-qubit one: M on its qubits and the identity on the lowest other qubit, on the tensor
+    // cores, which beat the CUDA-core forms there (30 qubits: FP64 k = 2 28.2 -> 18.2 ms,
+    // double-float k = 3 13.2 -> 10.4 ms)
+    double mx[2 * 16 * 16];
+    if (((st->P == LLG_F64 && k == 2) || (st->P == LLG_DF64 && k == 3)) && block_tc_eligible(st->P, st->n, k + 1)) {
         int x = 0;
         while ((bd.tmask >> x) & 1) ++x;
-        std::memset(m3, 0, sizeof(m3));
-        for (int r = 0; r < 8; ++r)
-            for (int c = 0; c < 8; ++c)
-                if ((r >> 2) == (c >> 2)) {  // bit 2 of the index is qubit x
-                    m3[2 * (r * 8 + c)] = m[2 * ((r & 3) * 4 + (c & 3))];
-                    m3[2 * (r * 8 + c) + 1] = m[2 * ((r & 3) * 4 + (c & 3)) + 1];
+        const int d = 1 << k, dx = 2 * d;
+        std::memset(mx, 0, sizeof(mx));
+        for (int r = 0; r < dx; ++r)
+            for (int c = 0; c < dx; ++c)
+                if ((r >> k) == (c >> k)) {  // bit k of the index is qubit x
+                    mx[2 * (r * dx + c)] = m[2 * ((r & (d - 1)) * d + (c & (d - 1)))];
+                    mx[2 * (r * dx + c) + 1] = m[2 * ((r & (d - 1)) * d + (c & (d - 1))) + 1];
                 }
-        bd.k = 3;
-        bd.q[2] = x;
+        bd.q[k] = x;
         bd.tmask |= 1ULL << x;
-        k = 3;
-        m = m3;
+        bd.k = ++k;
+        m = mx;
     }
     if (block_tc_eligible(st->P, st->n, k)) {
         const size_t wb = block_tc_weight_bytes(st->P, k);
