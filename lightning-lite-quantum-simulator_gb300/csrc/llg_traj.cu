@@ -152,7 +152,7 @@ struct Decision {
     // product formed once in double so that a site pair costs one multiply per real instead of two
     uint64_t g0, g1;
     int ad_jump, pd_jump;
-    // IEEE complex128 without a jump: the |0> amplitudes' factor f_ad0 f_pd0 sig is carried
+    // Without a jump the |0> factor f_ad0 f_pd0 sig is carried
     // (sig_next) instead of applied, and only the |1> amplitudes are scaled, by
     // g1 = f_ad1 f_pd1 / (f_ad0 f_pd0) = sqrt(1 - gamma) sqrt(1 - lambda): one multiply per real of
     // half of the state instead of one per real of all of it
@@ -161,11 +161,13 @@ struct Decision {
     double p1;
 };
 
-// |x| < 2^-300 or |x| >= 2^300 (x not 0), from the exponent field: no FP64 instruction in the
-// per-gate path
-__device__ __forceinline__ bool outside_2pow300(double x) {
+// |x| < 2^-L or |x| >= 2^L (x not 0; L = 300 for FP64 states, 40 for the float-based formats,
+// whose floats end at 2^-126), from the exponent field: no FP64 instruction in the per-gate path
+template <class P>
+__device__ __forceinline__ bool outside_carry_range(double x) {
+    constexpr int L = P::kPrecision == LLG_F64 ? 300 : 40;
     const int e = (int)((__double_as_longlong(x) >> 52) & 0x7ff) - 1023;
-    return e < -300 || e >= 300;
+    return e < -L || e >= L;
 }
 
 // barrier for the trajectory's CTA group
@@ -511,7 +513,7 @@ template <class P>
 // site); P1_held is the held state's P(1), so the true one is sig^2 P1_held, and the factors that
 // renormalise the held amplitudes carry sig.
 __device__ void decide(double P1_held, double sig, const KrausParams& kp, double u1, double u2, Decision* d,
-                       double* min_margin, bool carry_ok) {
+                       double* min_margin) {
     const double P1 = sig == 1.0 ? P1_held : sig * sig * P1_held;
     // amplitude damping
     double s_ad = 1.0 - kp.gamma * P1;
@@ -547,7 +549,7 @@ __device__ void decide(double P1_held, double sig, const KrausParams& kp, double
         fp1 = kp.sq1ml * s0;
     }
     d->p1 = p1;
-    if (carry_ok && !d->ad_jump && !d->pd_jump) {
+    if (!d->ad_jump && !d->pd_jump) {
         d->carry = 1;
         d->sig_next = fa0 * fp0 * sig;
         d->g0 = packk<P>(1.0);
@@ -621,9 +623,10 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
             const TrajGate& G = gates[g];
             T.gate(G.op);
             sig *= G.f;
-            // the held state is rescaled before it could leave the FP64 range (2^300 away from
-            // its true size): scale-free rotations shrink sig, carried Kraus factors grow it
-            if (outside_2pow300(sig)) {
+            // the held state is rescaled before it could leave its format's range (2^300 away
+            // from its true size in FP64, 2^40 in the float-based formats): scale-free rotations
+            // shrink sig, carried Kraus factors grow it
+            if (outside_carry_range<P>(sig)) {
                 T.rescale(sig);
                 sig = 1.0;
             }
@@ -654,8 +657,7 @@ __device__ void traj_kernel_body(int n, const TrajGate* __restrict__ gates, int 
                 if (site + 1 >= u_end) draw(site);  // AD and PD uniforms of this pair in one chunk
                 const double P1 = T.reduce(q, false, part2);
                 if (threadIdx.x == 0)
-                    decide<P>(P1, sig, kp, uni[site - u_begin], uni[site + 1 - u_begin], &dec, &min_margin,
-                              P::kPrecision == LLG_F64);
+                    decide<P>(P1, sig, kp, uni[site - u_begin], uni[site + 1 - u_begin], &dec, &min_margin);
                 __syncthreads();
                 sig = dec.sig_next;  // 1: the Kraus pass below stores the true, renormalised state
                 const int code = dec.ad_jump | (dec.pd_jump << 1);

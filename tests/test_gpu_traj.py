@@ -43,13 +43,15 @@ def test_config4_circuit_jumps_bit_exact_14_qubits(precision):
     assert j.sum() > 0
 
 
+@pytest.mark.parametrize("precision", ["df64", "fp64"])
 @pytest.mark.parametrize("n", [3, 7, 10])
-def test_strong_noise_jumps_bit_exact(n):
+def test_strong_noise_jumps_bit_exact(n, precision):
     ops = workloads.noisy_layers(n, 3, seed=n)
-    check_exact(n, ops, 0.25, 0.15, seed=77, count=256, precision="df64")
+    check_exact(n, ops, 0.25, 0.15, seed=77, count=256, precision=precision)
 
 
-def test_every_gate_kind_and_cross_cta_sites():
+@pytest.mark.parametrize("precision", ["df64", "fp64"])
+def test_every_gate_kind_and_cross_cta_sites(precision):
     rng = np.random.default_rng(5)
     n = 14
     recs = []
@@ -71,7 +73,7 @@ def test_every_gate_kind_and_cross_cta_sites():
     # make sure the top qubit (the one split across the cluster) is hit as target and control
     recs += [(OP_H, 13), (OP_CNOT, 13, 2), (OP_CNOT, 4, 13), (OP_RZ, 13, 0, 0.3), (OP_CZ, 13, 0)]
     ops = make_ops(recs)
-    check_exact(n, ops, 0.3, 0.2, seed=9, count=32, precision="df64")
+    check_exact(n, ops, 0.3, 0.2, seed=9, count=32, precision=precision)
 
 
 def test_trajectory_ranges_are_reproducible():
