@@ -136,10 +136,15 @@ __device__ __forceinline__ void tile_scale(typename P::S* tile, uint32_t tsize, 
 
 __device__ __forceinline__ bool is_rot_p(int kind) { return kind == EX_RX_P || kind == EX_RY_P; }
 
-// the weight of tile_grad_apply's sum: IEEE complex128 RZ sums only the q = 1 half (-2 x)
+// RZ gradients from the q = 1 half alone (see tile_grad_apply) in the 16-byte formats; complex64
+// keeps both halves, whose rounding would not cancel to its tolerance
+template <class P>
+constexpr bool kHalfRZ = P::kPrecision != LLG_F32;
+
+// the weight of tile_grad_apply's sum: an RZ summed over the q = 1 half only counts -2 x
 template <class P>
 __device__ __forceinline__ double grad_weight(int kind) {
-    return (P::kPrecision == LLG_F64 && kind == EX_RZ_P) ? -2.0 : 1.0;
+    return (kHalfRZ<P> && kind == EX_RZ_P) ? -2.0 : 1.0;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -234,7 +239,7 @@ __device__ typename P::Acc tile_grad_apply(typename P::S* psi, typename P::S* la
         const K ms0 = P::kneg(s0);
         if (o.flags & OPF_NONLOCAL_Q0) {
             const bool one = (base >> o.q0) & 1;
-            if constexpr (P::kPrecision == LLG_F64) {
+            if constexpr (kHalfRZ<P>) {
                 if (!one) return pos;  // the q = 0 half: no contribution, no change (see below)
             }
             for (uint32_t l = threadIdx.x; l < tsize; l += blockDim.x) {
@@ -247,11 +252,11 @@ __device__ typename P::Acc tile_grad_apply(typename P::S* psi, typename P::S* la
                     lam[l] = P::store(q);
                 }
             }
-            if constexpr (P::kPrecision == LLG_F64) return pos;  // weighted -2 by the caller
+            if constexpr (kHalfRZ<P>) return pos;  // weighted -2 by the caller
             else return one ? acc_minus(P::acc_zero(), pos) : pos;
         }
         const uint32_t bit = 1u << o.q0;
-        if constexpr (P::kPrecision == LLG_F64) {
+        if constexpr (kHalfRZ<P>) {
             // <lambda|psi> = <psi_N|O|psi_N> is real at every step of the reverse sweep (both
             // vectors go through the same unitaries, O is a real diagonal), so summed over all
             // tiles Im <lambda|Z|psi> = -2 sum_{q = 1} Im(conj(l) p): the q = 0 half is not read.
