@@ -553,7 +553,7 @@ struct llg_adjoint {
     ExecOp* d_fwd_ops = nullptr;
     ExecOp* d_bwd_ops = nullptr;
     uint64_t* d_table = nullptr;
-    uint8_t* d_form = nullptr;  // IEEE complex128: the scale-free form of each RX / RY table entry
+    uint8_t* d_form = nullptr;  // the scale-free form of each RX / RY table entry (16-byte formats)
     int* d_occ_param = nullptr;
     int* d_csr_ptr = nullptr;
     int* d_csr_occ = nullptr;

@@ -509,9 +509,9 @@ template <class P>
 // The comparisons and p1 (which decides the dephasing jump) are computed exactly as the oracle
 // computes them, in IEEE double with correctly rounded division; the scale factors only rescale
 // amplitudes and use rsqrt (within 1 ulp) instead of a square root and a division.
-// sig: the factor the held state is short of its true size (scale-free rotations since the last
-// site); P1_held is the held state's P(1), so the true one is sig^2 P1_held, and the factors that
-// renormalise the held amplitudes carry sig.
+// sig: the factor the held state is short of its true size (scale-free rotations, and the |0>
+// factors of jump-free sites, carried so far); P1_held is the held state's P(1), so the true one
+// is sig^2 P1_held, and the factors that renormalise the held amplitudes carry sig.
 __device__ void decide(double P1_held, double sig, const KrausParams& kp, double u1, double u2, Decision* d,
                        double* min_margin) {
     const double P1 = sig == 1.0 ? P1_held : sig * sig * P1_held;
