@@ -893,13 +893,12 @@ bool build_gates(int n, const llg_op* ops, int nops, int precision, int mode, in
             std::memset(&g[v], 0, sizeof(TrajGate));
             g[v].op = lowered[0];
             g[v].f = 1.0;
-            if (precision == LLG_F64 && (o.kind == LLG_OP_RX || o.kind == LLG_OP_RY)) {
-                // the scale-free form (4 FP64 multiply-adds per pair instead of 8): in Kraus mode
-                // every gate is followed by its noise sites, whose renormalisation absorbs the
-                // factor; in depolarizing mode the sites are unitary Paulis and the factor is
-                // carried to the observable (IEEE complex128 Kraus trajectories 10.8k -> 12.7k per
-                // second; the barrier-bound double-float and complex64 kernels measured 2-3 %
-                // slower with it, so they keep the full forms)
+            if (precision != LLG_F32 && (o.kind == LLG_OP_RX || o.kind == LLG_OP_RY)) {
+                // the scale-free form (one multiply-add per real instead of two): the factor joins
+                // the carried one, which the next Kraus site's renormalisation or the observable
+                // takes (IEEE complex128 Kraus trajectories 10.8k -> 12.7k per second, double-float
+                // 26.1k -> 26.5k once the Kraus factors were carried too; complex64 keeps the full
+                // forms, which measured 2-3 % faster in its barrier-bound kernel)
                 const double th = (v ? inv : o).theta;
                 const double c = std::cos(0.5 * th), sn = std::sin(0.5 * th);
                 const bool tan_form = std::fabs(c) >= std::fabs(sn);
